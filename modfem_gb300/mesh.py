@@ -1,0 +1,196 @@
+"""Structured prism meshes in ModFEM's numbering, and the jk ("gradmesh") writer.
+
+ModFEM's prism mesh module reads a 2D triangulation plus a layer count
+(``mmr_import_mesh_grad``, mmd_prism/mms_prism_input_gradmesh.c:30-560) and
+numbers the 3D entities from it:
+
+* node ``istr + lay*N2`` (1-based) sits above 2D node ``istr`` at layer
+  ``lay`` (mms_prism_input_gradmesh.c:95-104);
+* element ``itri + lay*T`` (1-based) is the prism over 2D triangle ``itri`` in
+  layer ``lay`` (:180-190); its vertices, as returned by ``mmr_el_node_coor``
+  (mmd_prism/mms_prism_datstr.c:365), are the triangle's three jk nodes on the
+  bottom level followed by the same three on the top level;
+* horizontal face ``itri + lev*T`` lies at level ``lev`` (0..nlay) (:193-245);
+  vertical faces get ids ``T*(nlay+1) + (k-1)*nlay + lay + 1`` for the k-th
+  triangle edge met while scanning triangles in order and their edges
+  0,1,2, an interior edge being created by the first of its two triangles
+  (:258-330).
+
+This module generates the unit-cube mesh of n^3 hexahedra, each split into two
+prisms along the same diagonal, directly in that numbering (no file round
+trip), and also writes the jk file so the reference can read the same mesh.
+"""
+import numpy as np
+
+# element sides (reference element coordinates): 0 bottom (zeta=-1),
+# 1 top (zeta=+1), 2+i lateral face over triangle edge i (node i -> node i+1)
+SIDE_BOTTOM, SIDE_TOP = 0, 1
+
+
+class PrismMesh:
+    """Flat structure-of-arrays prism mesh (0-based indices)."""
+
+    def __init__(self, n, coords, el_nodes, bc_face_id, bc_face_el, bc_face_side, bc_face_bc,
+                 ntri, nlay):
+        self.n = n
+        self.coords = coords            # (nno, 3) float64, row = reference node id - 1
+        self.el_nodes = el_nodes        # (nel, 6) int32, 0-based, reference local order
+        self.bc_face_id = bc_face_id    # (nbc,) reference face ids (1-based), ascending
+        self.bc_face_el = bc_face_el    # (nbc,) 0-based element of each bc face
+        self.bc_face_side = bc_face_side
+        self.bc_face_bc = bc_face_bc
+        self.ntri = ntri
+        self.nlay = nlay
+
+    @property
+    def nno(self):
+        return self.coords.shape[0]
+
+    @property
+    def nel(self):
+        return self.el_nodes.shape[0]
+
+
+def _tri_grid(n):
+    """2D triangulation of the unit square: (n+1)^2 nodes, 2n^2 triangles.
+
+    Returns node xy, triangle vertex ids (1-based, counter-clockwise) and the
+    jk neighbour list (triangle id or -bc) for edges (v0,v1), (v1,v2), (v2,v0).
+    """
+    N = n + 1
+    i, j = np.meshgrid(np.arange(N), np.arange(N), indexing="xy")
+    xy = np.stack([i.reshape(-1) / n, j.reshape(-1) / n], axis=1)
+    tri = np.zeros((2 * n * n, 3), np.int64)
+    nb = np.zeros((2 * n * n, 3), np.int64)
+    ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")
+    ii = ii.reshape(-1)
+    jj = jj.reshape(-1)
+    a = ii + jj * N + 1
+    b = a + 1
+    c = a + N + 1
+    d = a + N
+    t1 = 2 * (ii + jj * n) + 1
+    t2 = t1 + 1
+    tri[t1 - 1] = np.stack([a, b, c], 1)
+    tri[t2 - 1] = np.stack([a, c, d], 1)
+    # neighbours of t1: bottom edge a-b, right edge b-c, diagonal c-a
+    nb[t1 - 1, 0] = np.where(jj > 0, 2 * (ii + (jj - 1) * n) + 2, -1)
+    nb[t1 - 1, 1] = np.where(ii < n - 1, 2 * (ii + 1 + jj * n) + 2, -1)
+    nb[t1 - 1, 2] = t2
+    # neighbours of t2: diagonal a-c, top edge c-d, left edge d-a
+    nb[t2 - 1, 0] = t1
+    nb[t2 - 1, 1] = np.where(jj < n - 1, 2 * (ii + (jj + 1) * n) + 1, -1)
+    nb[t2 - 1, 2] = np.where(ii > 0, 2 * (ii - 1 + jj * n) + 1, -1)
+    return xy, tri, nb
+
+
+def write_jk(path, n, bc=1):
+    """Writes the jk file of the n^3-hexahedra unit cube split into prisms."""
+    xy, tri, nb = _tri_grid(n)
+    nbj = np.where(nb < 0, -bc, nb)
+    with open(path, "w") as f:
+        f.write("0 0 0 0\n")
+        f.write(f"{xy.shape[0]} 0.0 1.0 {n} {bc} {bc}\n")
+        for x, y in xy:
+            f.write(f"{x:.17g} {y:.17g}\n")
+        f.write(f"{tri.shape[0]}\n")
+        for t in range(tri.shape[0]):
+            f.write("1 %d %d %d %d %d %d\n" % (tri[t, 0], tri[t, 1], tri[t, 2],
+                                                  nbj[t, 0], nbj[t, 1], nbj[t, 2]))
+
+
+def structured_prism_mesh(n, jitter=0.0, seed=0, bc=1):
+    """Unit cube, n^3 hexahedra x 2 prisms, in ModFEM's numbering.
+
+    ``jitter`` moves every node by U(-jitter*h, +jitter*h) per coordinate
+    (h = 1/n), keeping boundary nodes on their boundary planes.
+    """
+    xy, tri, nb = _tri_grid(n)
+    N2 = xy.shape[0]
+    T = tri.shape[0]
+    nlay = n
+    # z = z_bottom + lay*dz with dz = (z_top - z_bottom)/nlay, as the jk reader computes it
+    z = 0.0 + np.arange(nlay + 1) * ((1.0 - 0.0) / nlay)
+    coords = np.zeros(((nlay + 1) * N2, 3))
+    for lay in range(nlay + 1):
+        coords[lay * N2:(lay + 1) * N2, 0:2] = xy
+        coords[lay * N2:(lay + 1) * N2, 2] = z[lay]
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        h = 1.0 / n
+        d = rng.uniform(-jitter * h, jitter * h, size=coords.shape)
+        on_bnd = (np.abs(coords) < 1e-12) | (np.abs(coords - 1.0) < 1e-12)
+        d[on_bnd] = 0.0
+        coords = coords + d
+    tri0 = (tri - 1).astype(np.int64)
+    el_nodes = np.zeros((T * nlay, 6), np.int32)
+    for lay in range(nlay):
+        el_nodes[lay * T:(lay + 1) * T, 0:3] = tri0 + lay * N2
+        el_nodes[lay * T:(lay + 1) * T, 3:6] = tri0 + (lay + 1) * N2
+
+    # boundary faces (bc > 0) in ascending reference face id
+    fid, fel, fside, fbc = [], [], [], []
+    # bottom level: face ids 1..T, element = itri (layer 0), side 0
+    fid.append(np.arange(1, T + 1))
+    fel.append(np.arange(T))
+    fside.append(np.full(T, SIDE_BOTTOM))
+    fbc.append(np.full(T, bc))
+    # top level: ids nlay*T+1..(nlay+1)*T, element in the last layer, side 1
+    fid.append(nlay * T + np.arange(1, T + 1))
+    fel.append((nlay - 1) * T + np.arange(T))
+    fside.append(np.full(T, SIDE_TOP))
+    fbc.append(np.full(T, bc))
+    # vertical faces in creation order
+    nr_hor = T * (nlay + 1)
+    creator = []  # (itri0, edge) for each created vertical face column
+    is_bnd = []
+    for t in range(T):
+        for e in range(3):
+            g = nb[t, e]
+            if g < 0 or g > t + 1:
+                creator.append((t, e))
+                is_bnd.append(g < 0)
+    creator = np.array(creator, np.int64).reshape(-1, 2)
+    is_bnd = np.array(is_bnd, bool)
+    k = np.nonzero(is_bnd)[0]  # 0-based creation index of boundary columns
+    lay = np.arange(nlay)
+    ids = nr_hor + (k[:, None]) * nlay + lay[None, :] + 1
+    els = creator[k, 0][:, None] + lay[None, :] * T
+    sides = 2 + creator[k, 1][:, None] + 0 * lay[None, :]
+    fid.append(ids.reshape(-1))
+    fel.append(els.reshape(-1))
+    fside.append(sides.reshape(-1))
+    fbc.append(np.full(ids.size, bc))
+    fid = np.concatenate(fid).astype(np.int32)
+    order = np.argsort(fid, kind="stable")
+    return PrismMesh(n, coords, el_nodes, fid[order],
+                     np.concatenate(fel)[order].astype(np.int32),
+                     np.concatenate(fside)[order].astype(np.int32),
+                     np.concatenate(fbc)[order].astype(np.int32), T, nlay)
+
+
+def lognormal_k(nel, seed=0, mu=0.0, sigma=1.0):
+    """Per-element diffusion coefficient k ~ lognormal(mu, sigma) from a seed."""
+    return np.random.default_rng(seed + 7919).lognormal(mu, sigma, nel)
+
+
+def prism_min_detj(mesh):
+    """Smallest Jacobian determinant over the 6 std quadrature points."""
+    X = mesh.coords[mesh.el_nodes]  # (nel, 6, 3)
+    a0, a1, a2, b0, b1, b2 = [X[:, i, :] for i in range(6)]
+    m1 = 0.5 * ((a1 - a0) + (b1 - b0))
+    d1 = 0.5 * ((b1 - b0) - (a1 - a0))
+    m2 = 0.5 * ((a2 - a0) + (b2 - b0))
+    d2 = 0.5 * ((b2 - b0) - (a2 - a0))
+    c0 = 0.5 * (b0 - a0)
+    g = 0.577350269189626
+    pts = [(1 / 6, 1 / 6), (1 / 6, 2 / 3), (2 / 3, 1 / 6)]
+    dmin = np.inf
+    for zeta in (-g, g):
+        for (xi, eta) in pts:
+            jx = m1 + zeta * d1
+            jy = m2 + zeta * d2
+            jz = c0 + xi * d1 + eta * d2
+            det = np.einsum("ij,ij->i", jx, np.cross(jy, jz))
+            dmin = min(dmin, det.min())
+    return dmin

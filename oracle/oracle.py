@@ -1,0 +1,150 @@
+"""Test infrastructure only: ctypes access to the C restatement (liboracle.so).
+
+Used by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg,
+always as the checker or the timed CPU baseline, never as the product.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+_L = None
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+
+
+def lib():
+    global _L
+    if _L is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        vp, ci, cd = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        L.orc_std_prism_element.argtypes = [vp, vp, cd, vp, vp]
+        L.orc_std_prism_face.argtypes = [vp, ci, cd, cd, vp, vp]
+        L.orc_std_tet_element.argtypes = [vp, vp, cd, vp, vp]
+        L.orc_std_dof_order.argtypes = [ci, ci, vp, ci, vp]
+        L.orc_std_crs_structure.argtypes = [ci, ci, vp, vp, ci, vp, vp]
+        L.orc_std_crs_structure.restype = ctypes.c_long
+        L.orc_crs_table.argtypes = [ci, vp, vp, vp, vp]
+        L.orc_color_entities.argtypes = [ci, ci, vp, ci, vp]
+        L.orc_std_prism_assemble.argtypes = [ci, vp, vp, vp, vp, cd, ci, vp, vp, cd, cd, vp, vp, vp,
+                                             vp, vp, ci, vp, vp]
+        L.orc_std_prism_assemble.restype = cd
+        L.orc_crs_residual.argtypes = [ci, vp, vp, vp, ci, vp, vp, vp]
+        L.orc_gmres_jacobi.argtypes = [ci, vp, vp, vp, vp, vp, ci, ci, cd, vp, vp]
+        _L = L
+    return _L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c(a, dt):
+    return None if a is None else np.ascontiguousarray(a, dtype=dt)
+
+
+def std_prism_element(X, A, f=1.0):
+    X = _c(X, np.float64).reshape(-1)
+    A = _c(A, np.float64).reshape(-1)
+    sm = np.zeros(36)
+    rhs = np.zeros(6)
+    lib().orc_std_prism_element(_p(X), _p(A), f, _p(sm), _p(rhs))
+    return sm.reshape(6, 6).T.copy(), rhs  # (row w, column u)
+
+
+def std_prism_face(X, side, penalty=1e7, g=0.0):
+    X = _c(X, np.float64).reshape(-1)
+    sm = np.zeros(36)
+    rhs = np.zeros(6)
+    lib().orc_std_prism_face(_p(X), side, penalty, g, _p(sm), _p(rhs))
+    return sm.reshape(6, 6).T.copy(), rhs
+
+
+def std_tet_element(X, A, f=1.0):
+    X = _c(X, np.float64).reshape(-1)
+    A = _c(A, np.float64).reshape(-1)
+    sm = np.zeros(16)
+    rhs = np.zeros(4)
+    lib().orc_std_tet_element(_p(X), _p(A), f, _p(sm), _p(rhs))
+    return sm.reshape(4, 4).T.copy(), rhs
+
+
+def dof_order(el_nodes, nno):
+    el = _c(el_nodes, np.int32)
+    d = np.zeros(nno, np.int32)
+    nd = lib().orc_std_dof_order(el.shape[0], el.shape[1], _p(el), nno, _p(d))
+    return d, nd
+
+
+def crs_structure(el_nodes, dof_of_node, ndof):
+    el = _c(el_nodes, np.int32)
+    dn = _c(dof_of_node, np.int32)
+    rp = np.zeros(ndof + 1, np.int32)
+    nnz = lib().orc_std_crs_structure(el.shape[0], el.shape[1], _p(el), _p(dn), ndof, _p(rp), None)
+    ci = np.zeros(nnz, np.int32)
+    lib().orc_std_crs_structure(el.shape[0], el.shape[1], _p(el), _p(dn), ndof, _p(rp), _p(ci))
+    return rp, ci
+
+
+def crs_table(dofs, row_ptr, col_ind):
+    d = _c(dofs, np.int32)
+    n = d.size
+    t = np.zeros(n * n + n, np.int32)
+    lib().orc_crs_table(n, _p(d), _p(row_ptr), _p(col_ind), _p(t))
+    return t
+
+
+def color_entities(ent_dofs, ndof):
+    e = _c(ent_dofs, np.int32)
+    col = np.zeros(e.shape[0], np.int32)
+    nc = lib().orc_color_entities(e.shape[0], e.shape[1], _p(e), ndof, _p(col))
+    return col, nc
+
+
+def std_prism_assemble(mesh, k_el, dof_of_node, row_ptr, col_ind, f=1.0, penalty=1e7, g=0.0,
+                       D_el=None, color_ptr=None, perm=None, nthreads=1):
+    nnz = col_ind.size
+    val = np.zeros(nnz)
+    rhs = np.zeros(row_ptr.size - 1)
+    el = _c(mesh.el_nodes, np.int32)
+    xyz = _c(mesh.coords, np.float64)
+    k = _c(k_el, np.float64)
+    D = _c(D_el, np.float64)
+    fe = _c(mesh.bc_face_el, np.int32)
+    fs = _c(mesh.bc_face_side, np.int32)
+    cp = _c(color_ptr, np.int32)
+    pm = _c(perm, np.int32)
+    t = lib().orc_std_prism_assemble(el.shape[0], _p(el), _p(xyz), _p(k), _p(D), f, fe.size, _p(fe),
+                                     _p(fs), penalty, g, _p(_c(dof_of_node, np.int32)),
+                                     _p(_c(row_ptr, np.int32)), _p(_c(col_ind, np.int32)), _p(cp),
+                                     _p(pm), nthreads, _p(val), _p(rhs))
+    return val, rhs, t
+
+
+def crs_residual(row_ptr, col_ind, val, x, b=None):
+    n = row_ptr.size - 1
+    v = np.zeros(n)
+    bb = _c(b, np.float64)
+    lib().orc_crs_residual(n, _p(row_ptr), _p(col_ind), _p(_c(val, np.float64)), 0 if b is None else 1,
+                           _p(bb), _p(_c(x, np.float64)), _p(v))
+    return v
+
+
+def gmres_jacobi(row_ptr, col_ind, val, b, krylov=30, max_iter=1000, tol_rel=1e-8, x0=None):
+    n = row_ptr.size - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    res = ctypes.c_double()
+    rel = ctypes.c_double()
+    it = lib().orc_gmres_jacobi(n, _p(row_ptr), _p(col_ind), _p(_c(val, np.float64)),
+                                _p(_c(b, np.float64)), _p(x), krylov, max_iter, tol_rel,
+                                ctypes.cast(ctypes.pointer(res), ctypes.c_void_p),
+                                ctypes.cast(ctypes.pointer(rel), ctypes.c_void_p))
+    return x, it, res.value, rel.value
