@@ -1,0 +1,321 @@
+"""Benchmark: std-linear prism integrate + assemble on GB300.
+
+Workload: Poisson -div(k grad u) = 1 on the unit cube, 100^3 hexahedra split
+into 2,000,000 linear prisms (1,030,301 DOFs, 21,250,901 CRS nonzeros), node
+coordinates jittered by U(+-0.2h) (seeded), k ~ lognormal(0,1) per element
+(seeded), penalty Dirichlet faces on the whole boundary (80,000 faces).
+A step is one integrate + assemble of all elements and boundary faces into
+the CRS matrix and rhs.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  `value` is device-resident throughput
+(elements/s, CUDA events on the library's stream); `e2e` is the same metric
+through the pdr_create_assemble_stiff_mat drop-in with host buffers, the
+step's inputs (node coordinates, k) uploaded from and the CRS values and rhs
+downloaded to page-locked host memory inside the timed region.
+`--impl reference` times the CPU path (the C restatement in oracle/, all
+host cores, colour-parallel as the reference's OpenMP loop) on the same
+workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "elem/s integrate+assemble vs plain FP64 GPU @1e-10 rel; served p50/p99 latency"
+UNIT = "elem/s"
+N_HEX = 100
+JITTER, SEED = 0.2, 1
+# algorithmic FP64 work per std prism: nq*(151 + 18*ns + 2*ns) + 2*3*nq*ns^2
+# with nq = 6 quadrature points, ns = 6 shape functions
+FLOP_PER_ELEM = 6 * (151 + 18 * 6 + 2 * 6) + 2 * 3 * 6 * 36
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=N_HEX, help=argparse.SUPPRESS)
+    return p.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                backend = "gloo"
+            else:
+                torch.cuda.set_device(local)
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, ws):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(s[1]) for s in self.samples if len(s) >= 9 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) >= 9 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples if len(s) >= 9 for i in range(4)
+                          if s[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def read_profile_traffic():
+    """DRAM bytes per element-kernel launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "std_prism_elements_2M.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("dram_bytes_per_launch"):
+            try:
+                return int(line.split("=")[1].split()[0])
+            except Exception:
+                return None
+    return None
+
+
+def make_problem(n):
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(n, jitter=JITTER, seed=SEED)
+    k = lognormal_k(m.nel, seed=SEED)
+    return m, k
+
+
+def cpu_assemble(m, k, nthreads, reps=1):
+    """The C restatement's colour-parallel integrate + assemble; seconds per run."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    d, nd = O.dof_order(m.el_nodes, m.nno)
+    rp, ci = O.crs_structure(m.el_nodes, d, nd)
+    col, nc = O.color_entities(d[m.el_nodes], nd)
+    perm = np.argsort(col, kind="stable").astype(np.int32)
+    cptr = np.zeros(nc + 1, np.int32)
+    cptr[1:] = np.cumsum(np.bincount(col, minlength=nc))
+    times = []
+    for _ in range(reps):
+        _, _, t = O.std_prism_assemble(m, k, d, rp, ci, color_ptr=cptr, perm=perm, nthreads=nthreads)
+        times.append(t)
+    return times
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"])
+    m, k = make_problem(args.n)
+    nthreads = os.cpu_count() or 1
+    cpu_assemble(m, k, nthreads, reps=args.warmup)
+    times = cpu_assemble(m, k, nthreads, reps=args.steps)
+    t = sum(times) / len(times)
+    v = m.nel / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh jitter and k)",
+        "config": {"workload": f"std P1 prism integrate+assemble, {args.n}^3 hex x 2 = {m.nel} prisms, "
+                               f"lognormal(0,1) k, +-0.2h jitter, penalty Dirichlet",
+                   "parallelism": "CPU host threads"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"full {m.nel}-element assembly per step (colour-parallel OpenMP)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    import modfem_gb300 as gb
+    from modfem_gb300 import build
+    if rank == 0:
+        build.build(verbose=False)
+    barrier(ws)
+
+    m, k = make_problem(args.n)
+    c = gb.Context(local)
+    c.set_mesh(m)
+    c.set_coefficients(k=k, f=1.0, g=0.0, penalty=1e7)
+    nd, nnz, ncol = c.build_structure()
+    fp64_peak = c.measure_fp64_peak()
+
+    # ---------------- device-resident throughput ----------------
+    for _ in range(args.warmup):
+        c.assemble(gb.SCATTER_ATOMIC)
+    barrier(ws)
+    sampler = ClockSampler(local)
+    sampler.start()
+    tot_ms, el_ms, launches = 0.0, 0.0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        c.assemble(gb.SCATTER_ATOMIC)
+        a, b, nl = c.last_timing()
+        tot_ms += a
+        el_ms += b
+        launches += nl
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    ms_step = max_over_ranks(tot_ms / args.steps, ws)
+    el_ms_step = max_over_ranks(el_ms / args.steps, ws)
+    value = ws * m.nel / (ms_step * 1e-3)
+
+    # ---------------- end to end through the drop-in C ABI ----------------
+    tables = c.get_element_tables()
+    fa_tab = tables.reshape(m.nel, 42)[m.bc_face_el].reshape(-1)
+    ids = np.concatenate([np.arange(1, m.nel + 1), m.bc_face_id]).astype(np.int32)
+    types = np.concatenate([np.full(m.nel, gb.ELEMENT), np.full(m.bc_face_id.size, gb.FACE)]).astype(np.int32)
+    pos = (np.arange(ids.size) * 42).astype(np.int32)
+    table = np.concatenate([tables, fa_tab]).astype(np.int32)
+    ce = np.array([0, m.nel], np.int32)
+    cf = np.array([m.nel, ids.size], np.int32)
+    pins = {}
+    for name, arr in (("types", types), ("ids", ids), ("pos", pos), ("table", table), ("ce", ce), ("cf", cf),
+                      ("xyz", m.coords), ("k", k)):
+        pa = gb.PinnedArray(arr.shape, arr.dtype)
+        pa.array[...] = arr
+        pins[name] = pa
+    out_val = gb.PinnedArray((nnz,))
+    out_rhs = gb.PinnedArray((nd,))
+    c.set_option(gb.OPT_CACHE_TABLES, 1)
+
+    def e2e_step():
+        c.set_node_coords(pins["xyz"].array)
+        c.set_coefficients(k=pins["k"].array, f=1.0, g=0.0, penalty=1e7)
+        c.create_assemble_stiff_mat(pins["types"].array, pins["ids"].array, pins["ce"].array, pins["cf"].array,
+                                    pins["pos"].array, pins["table"].array, crs_val=out_val.array,
+                                    rhs=out_rhs.array)
+
+    for _ in range(max(args.warmup, 1)):
+        e2e_step()
+    barrier(ws)
+    et = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        e2e_step()
+        et.append(time.perf_counter() - t1)
+    e2e_s = max_over_ranks(sum(et) / len(et), ws)
+    e2e_value = ws * m.nel / e2e_s
+    h2d = m.coords.nbytes + k.nbytes
+    d2h = 8 * nnz + 8 * nd
+
+    # parity of the e2e result against the device-resident one (same kernels)
+    ref_val, ref_rhs = c.get_matrix()
+    assert np.max(np.abs(out_val.array - ref_val)) <= 1e-12 * np.max(np.abs(ref_val))
+
+    # ---------------- CPU baseline (rank 0, N=1 only) ----------------
+    cpu = None
+    if rank == 0 and ws == 1:
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"])
+        nthreads = os.cpu_count() or 1
+        times = cpu_assemble(m, k, nthreads, reps=2)
+        tc = min(times)
+        cpu = {"value": m.nel / tc, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"one full {m.nel}-element integrate+assemble (elements + faces), colour-parallel OpenMP"}
+
+    achieved = FLOP_PER_ELEM * m.nel / (el_ms_step * 1e-3) / 1e12
+    traffic = read_profile_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded mesh jitter and lognormal k)",
+        "config": {"workload": f"std P1 prism integrate+assemble, {args.n}^3 hex x 2 = {m.nel} prisms "
+                               f"({nd} dofs, nnz {nnz}, {m.bc_face_id.size} penalty faces), lognormal(0,1) k, "
+                               f"+-0.2h jitter",
+                   "scatter": "FP64 atomics", "l2": "inputs larger than L2 (tables 336 MB, values 170 MB)",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp64_peak, "traffic": traffic,
+                     "kernel": "prism_elements_kernel", "kernel_ms": el_ms_step,
+                     "flop_per_elem": FLOP_PER_ELEM,
+                     "peak_source": "FP64 FMA-chain kernel measured in this run (no FP64 figure in the peaks file)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_s * 1e3},
+        "clocks": clocks,
+        "gpu_launches": launches,
+        "wall_s_timed_region": wall,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for pa in list(pins.values()) + [out_val, out_rhs]:
+        pa.free()
+    c.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

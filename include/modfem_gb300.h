@@ -1,0 +1,175 @@
+/*
+ * modfem_gb300.h - C ABI of the GB300 (sm_103a) integrate / assemble / SpMV /
+ * GMRES path for ModFEM's convection-diffusion problem module.
+ *
+ * Plain C types only (pointers, sizes); every call returns >= 0 on success
+ * and < 0 on error, the ModFEM convention (include/pdh_intf.h: "returns: >=0 -
+ * success code, <0 - error code"); gbfem_last_error() gives the message.
+ *
+ * One context holds one problem on one GPU: its mesh geometry, coefficients,
+ * CRS structure and assembly tables, the assembled matrix and the Krylov
+ * workspace, all resident in device memory.  Host pointers passed to the calls
+ * are read or written before the call returns.  Calls on one context are not
+ * thread safe; different contexts may be used from different threads.
+ *
+ * Numbering follows ModFEM: local element matrices are column-major
+ * (Stiff_mat[u*n + w], u = trial/column, w = test/row), assembly tables give
+ * for each integration entity n*n CRS value positions (entry j + i*n is row
+ * dof j, column dof i) followed by n rhs positions
+ * (lsd_mkb/lad_crs/las_crs_intf.c:354-438).
+ */
+#ifndef MODFEM_GB300_H
+#define MODFEM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbfem_ctx_s *gbfem_ctx;
+
+/* integration entity types (include/aph_intf.h:134-135: APC_ELEMENT, APC_FACE) */
+#define GBFEM_ELEMENT 4
+#define GBFEM_FACE 3
+/* Comp_type (include/pdh_intf.h PDC_COMP_*): what to assemble */
+#define GBFEM_COMP_SM 1
+#define GBFEM_COMP_RHS 2
+#define GBFEM_COMP_BOTH 3
+/* element types */
+#define GBFEM_PRISM 6
+#define GBFEM_TETRA 4
+/* scatter modes of gbfem_assemble */
+#define GBFEM_SCATTER_ATOMIC 0 /* one launch, FP64 atomics (summation order varies) */
+#define GBFEM_SCATTER_COLOR 1  /* one launch per colour, plain adds (deterministic) */
+
+/* ---------------------------------------------------------------------- */
+/* context                                                                  */
+/* ---------------------------------------------------------------------- */
+int gbfem_version(void);
+const char *gbfem_last_error(void);
+/* Creates a context on CUDA device `device` with its own stream. */
+int gbfem_create(gbfem_ctx *ctx, int device);
+int gbfem_destroy(gbfem_ctx ctx);
+/* Bytes of device memory the context holds. */
+long long gbfem_device_bytes(gbfem_ctx ctx);
+
+/* Options (no reference counterpart).
+ * GBFEM_OPT_CACHE_TABLES = 1: gbfem_create_assemble_stiff_mat keeps the
+ * device copies of the entity lists and assembly table between calls and
+ * skips their upload while the caller passes the same pointers and sizes;
+ * the caller promises not to change their contents, as holds in ModFEM
+ * between sir_create and sir_free. */
+#define GBFEM_OPT_CACHE_TABLES 1
+int gbfem_set_option(gbfem_ctx ctx, int option, long long value);
+
+/* ---------------------------------------------------------------------- */
+/* problem data                                                             */
+/* ---------------------------------------------------------------------- */
+/* Mesh geometry, the data the reference approximation module reads through
+ * mmr_el_node_coor (mmd_prism/mms_prism_datstr.c:365) and mmr_fa_* for every
+ * element and boundary face.  el_nodes: nv vertex indices (0-based) per
+ * element in mmr_el_node_coor order (prism: bottom triangle then top,
+ * nv = 6; tetrahedron nv = 4).  Boundary faces with a Dirichlet flag
+ * (0 < bc < 10, pdr_get_bc_type in pds_conv_diff_weakform.c:1240-1252) carry
+ * the reference face id (for the entity lists of the drop-in call), the
+ * 0-based element and the element side (0 bottom, 1 top, 2..4 lateral over
+ * triangle edge 0..2). */
+int gbfem_set_mesh(gbfem_ctx ctx, int nno, const double *node_xyz, int nel, int nv,
+                   const int *el_nodes, int nfa, const int *fa_id, const int *fa_el,
+                   const int *fa_side, const int *fa_bc);
+/* Updates node coordinates only (same topology), e.g. a moved mesh. */
+int gbfem_set_node_coords(gbfem_ctx ctx, const double *node_xyz);
+
+/* PDE coefficients in place of the per-quadrature-point callback
+ * pdr_el_coeff (include/pdh_intf.h:513-612): -div(K grad u) = f with
+ * K = k_el[e]*I (k_el != NULL) or the full tensor D_el[9e..9e+8] (row-major
+ * a_ij multiplying d_i(test) d_j(trial), pds_conv_diff_weakform.c:757);
+ * Dirichlet value g imposed by the penalty face integral with factor
+ * `penalty` (1e7 in pds_conv_diff_weakform_std.c:480). */
+int gbfem_set_coefficients(gbfem_ctx ctx, const double *k_el, const double *D_el, double f,
+                           double g, double penalty);
+
+/* CRS structure as sir_create leaves it (sid_mkb/sis_mkb_intf.c:396-1690,
+ * lad_crs/las_crs_intf.c:72-300): dof index of each node (-1 if none), row
+ * pointers and ascending column indices with the diagonal included. */
+int gbfem_set_crs_structure(gbfem_ctx ctx, int ndof, const int *dof_of_node, long long nnz,
+                            const int *row_ptr, const int *col_ind);
+/* Builds the same structure in the library (first-appearance dof order over
+ * the elements, utd_util/uts_ls_intf.c:182-300; sorted neighbour columns) and
+ * the element/face assembly tables and colours used by gbfem_assemble. */
+int gbfem_build_structure(gbfem_ctx ctx, int *ndof, long long *nnz, int *nr_colors);
+/* Copies the structure out (any pointer may be NULL). */
+int gbfem_get_crs_structure(gbfem_ctx ctx, int *dof_of_node, int *row_ptr, int *col_ind);
+/* Copies out the element assembly tables gbfem_build_structure made, in the
+ * layout of lar_fill_assembly_table_int_ent_crs (las_crs_intf.c:354-438):
+ * nv*nv + nv ints per element, elements in mesh order. */
+int gbfem_get_element_tables(gbfem_ctx ctx, int *tables);
+
+/* ---------------------------------------------------------------------- */
+/* the hot path                                                             */
+/* ---------------------------------------------------------------------- */
+/* Drop-in for pdr_create_assemble_stiff_mat (include/pdh_intf.h:230-249,
+ * pdd_conv_diff/linear_solver_interface/pds_conv_diff_ls_intf.c:253;
+ * driver utr_create_assemble_stiff_mat, utd_util/uts_ls_intf.c:3368-4322):
+ * integrates every element and boundary face in the lists and adds the
+ * results into the CRS values and rhs through the given assembly tables.
+ * The lists, colours and tables are the ones sir_create built; they are
+ * copied to the device on every call.  crs_val (nnz) and rhs (ndof) are host
+ * arrays in the caller's CRS storage (itv_crs_matrices, lad_crs/lah_crs.h);
+ * when crs_val/rhs are NULL the result stays on the device for
+ * gbfem_compute_residual / gbfem_solve.  The matrix is cleared first
+ * (lsr_mkb_clear_matrix, sis_mkb_intf.c:2043).  Pdeg_coarse_p and Level_id
+ * must describe the finest (only) level. */
+int gbfem_create_assemble_stiff_mat(gbfem_ctx ctx, int Level_id, int Comp_type,
+                                    const int *Pdeg_coarse_p, int Nr_int_ent,
+                                    const int *L_int_ent_type, const int *L_int_ent_id,
+                                    int Nr_colors_elems, const int *L_color_index_elems,
+                                    int Nr_colors_faces, const int *L_color_index_faces,
+                                    const int *Asse_pos_first_dof_int_ent,
+                                    const int *Assembly_table, int Max_dofs_int_ent,
+                                    double *crs_val, double *rhs);
+
+/* Device-resident integrate + assemble with the tables gbfem_build_structure
+ * made (no host transfers): clears and fills the device CRS values and rhs. */
+int gbfem_assemble(gbfem_ctx ctx, int scatter_mode);
+/* Copies the device CRS values / rhs to host arrays (either may be NULL). */
+int gbfem_get_matrix(gbfem_ctx ctx, double *crs_val, double *rhs);
+/* Uploads CRS values / rhs (either may be NULL), e.g. a matrix assembled elsewhere. */
+int gbfem_set_matrix(gbfem_ctx ctx, const double *crs_val, const double *rhs);
+
+/* Drop-in for lar_compute_residual (lsd_mkb/las_intf.c:771,
+ * lad_crs/las_crs_intf.c:788-856): V = (Use_rhs ? B : 0) - A*X, X, B, V host
+ * arrays of Ndof entries (B NULL: the assembled rhs); Ini_zero != 0 treats X
+ * as zero. */
+int gbfem_compute_residual(gbfem_ctx ctx, int Use_rhs, int Ini_zero, int Ndof, const double *X,
+                           const double *B, double *V);
+
+/* Replaces lsr_mkb_core_gmres with the point-Jacobi preconditioner
+ * (lsd_mkb_core/lss_mkb_core.c:2317-2660, lad_crs/las_crs_intf.c:707,857):
+ * restarted GMRES(krylov), classical Gram-Schmidt, Givens rotations, stop
+ * when the preconditioned residual falls below max(tol_rel*initial, 1e-12)
+ * or after max_iter iterations.  x (host, ndof) holds the initial guess if
+ * ini_zero == 0 and receives the solution.  Returns the iteration count. */
+int gbfem_solve(gbfem_ctx ctx, int krylov, int max_iter, double tol_rel, int ini_zero, double *x,
+                double *res_out, double *res_rel_out);
+
+/* Timing of the last integrate+assemble call, from CUDA events on the
+ * context stream (no reference counterpart; the reference prints wall times
+ * under TIME_TEST, utd_util/uts_ls_intf.c:4312-4318): total_ms covers the
+ * whole call on the device timeline (uploads, clearing, kernels, downloads),
+ * element_ms only the element-integration kernel launches; launches counts
+ * the library's kernels in the call. */
+int gbfem_last_assembly_timing(gbfem_ctx ctx, double *total_ms, double *element_ms, int *launches);
+
+/* Page-locked host memory for fast transfers (no reference counterpart). */
+void *gbfem_host_alloc(long long bytes);
+int gbfem_host_free(void *ptr);
+
+/* Measures the device's FP64 FMA throughput in TFLOP/s with a register-only
+ * FMA-chain kernel (no reference counterpart; the roofline denominator of the
+ * FP64-bound integration kernels). */
+int gbfem_measure_fp64_peak(gbfem_ctx ctx, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

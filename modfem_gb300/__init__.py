@@ -1,0 +1,242 @@
+"""GB300-native integrate / assemble / SpMV / GMRES path for ModFEM.
+
+The compute lives in ``libmodfem_gb300.so`` (CUDA, sm_103a) behind the C ABI
+in ``include/modfem_gb300.h``.  This module is a thin ctypes binding used by
+the tests, the benchmark and the serving loop; there is no CPU fallback: if
+the library is missing or cannot reach a GPU, the calls raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmodfem_gb300.so")
+
+ELEMENT, FACE = 4, 3
+COMP_SM, COMP_RHS, COMP_BOTH = 1, 2, 3
+SCATTER_ATOMIC, SCATTER_COLOR = 0, 1
+OPT_CACHE_TABLES = 1
+
+# (name, restype, argtypes) of every symbol include/modfem_gb300.h declares
+_vp, _ci, _cd, _cll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+_pi, _pd, _pll, _pvp = (ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                        ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_void_p))
+SIGNATURES = [
+    ("gbfem_version", _ci, []),
+    ("gbfem_last_error", ctypes.c_char_p, []),
+    ("gbfem_create", _ci, [_pvp, _ci]),
+    ("gbfem_destroy", _ci, [_vp]),
+    ("gbfem_device_bytes", _cll, [_vp]),
+    ("gbfem_set_option", _ci, [_vp, _ci, _cll]),
+    ("gbfem_set_mesh", _ci, [_vp, _ci, _vp, _ci, _ci, _vp, _ci, _vp, _vp, _vp, _vp]),
+    ("gbfem_set_node_coords", _ci, [_vp, _vp]),
+    ("gbfem_set_coefficients", _ci, [_vp, _vp, _vp, _cd, _cd, _cd]),
+    ("gbfem_set_crs_structure", _ci, [_vp, _ci, _vp, _cll, _vp, _vp]),
+    ("gbfem_build_structure", _ci, [_vp, _pi, _pll, _pi]),
+    ("gbfem_get_crs_structure", _ci, [_vp, _vp, _vp, _vp]),
+    ("gbfem_get_element_tables", _ci, [_vp, _vp]),
+    ("gbfem_create_assemble_stiff_mat", _ci,
+     [_vp, _ci, _ci, _pi, _ci, _vp, _vp, _ci, _vp, _ci, _vp, _vp, _vp, _ci, _vp, _vp]),
+    ("gbfem_assemble", _ci, [_vp, _ci]),
+    ("gbfem_get_matrix", _ci, [_vp, _vp, _vp]),
+    ("gbfem_set_matrix", _ci, [_vp, _vp, _vp]),
+    ("gbfem_compute_residual", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
+    ("gbfem_solve", _ci, [_vp, _ci, _ci, _cd, _ci, _vp, _pd, _pd]),
+    ("gbfem_last_assembly_timing", _ci, [_vp, _pd, _pd, _pi]),
+    ("gbfem_host_alloc", _vp, [_cll]),
+    ("gbfem_host_free", _ci, [_vp]),
+    ("gbfem_measure_fp64_peak", _ci, [_vp, _pd]),
+]
+
+_LIB = None
+
+
+class GbFemError(RuntimeError):
+    pass
+
+
+def load_library(path=LIB_PATH):
+    """Loads libmodfem_gb300.so and binds every declared entry point."""
+    global _LIB
+    if _LIB is not None and path == LIB_PATH:
+        return _LIB
+    if not os.path.exists(path):
+        raise GbFemError(f"{path} is missing: build it with modfem_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path == LIB_PATH:
+        _LIB = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """One problem on one GPU (see include/modfem_gb300.h)."""
+
+    def __init__(self, device=0):
+        self.L = load_library()
+        self._h = ctypes.c_void_p()
+        self._check(self.L.gbfem_create(ctypes.byref(self._h), device))
+        self._keep = {}
+
+    def _check(self, rc):
+        if rc < 0:
+            raise GbFemError(self.L.gbfem_last_error().decode())
+        return rc
+
+    def close(self):
+        if self._h:
+            self.L.gbfem_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def device_bytes(self):
+        return self.L.gbfem_device_bytes(self._h)
+
+    def set_option(self, opt, value):
+        self._check(self.L.gbfem_set_option(self._h, opt, value))
+
+    # ---------------- problem data ----------------
+    def set_mesh(self, mesh):
+        xyz = _f64(mesh.coords)
+        el = _i32(mesh.el_nodes)
+        nv = el.shape[1]
+        fid = _i32(getattr(mesh, "bc_face_id", np.zeros(0)))
+        fel = _i32(getattr(mesh, "bc_face_el", np.zeros(0)))
+        fsd = _i32(getattr(mesh, "bc_face_side", np.zeros(0)))
+        fbc = _i32(getattr(mesh, "bc_face_bc", np.zeros(0)))
+        self._check(self.L.gbfem_set_mesh(self._h, xyz.shape[0], _p(xyz), el.shape[0], nv, _p(el), fel.size,
+                                          _p(fid), _p(fel), _p(fsd), _p(fbc)))
+        self.nno, self.nel, self.nv, self.nfa = xyz.shape[0], el.shape[0], nv, fel.size
+
+    def set_node_coords(self, xyz):
+        xyz = _f64(xyz)
+        self._keep["xyz"] = xyz
+        self._check(self.L.gbfem_set_node_coords(self._h, _p(xyz)))
+
+    def set_coefficients(self, k=None, D=None, f=1.0, g=0.0, penalty=1.0e7):
+        k = _f64(k)
+        D = _f64(D)
+        self._keep["k"], self._keep["D"] = k, D
+        self._check(self.L.gbfem_set_coefficients(self._h, _p(k), _p(D), f, g, penalty))
+
+    def set_crs_structure(self, dof_of_node, row_ptr, col_ind):
+        dn, rp, ci = _i32(dof_of_node), _i32(row_ptr), _i32(col_ind)
+        self._check(self.L.gbfem_set_crs_structure(self._h, rp.size - 1, _p(dn), ci.size, _p(rp), _p(ci)))
+        self.ndof, self.nnz = rp.size - 1, ci.size
+
+    def build_structure(self):
+        nd, nnz, nc = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_int()
+        self._check(self.L.gbfem_build_structure(self._h, ctypes.byref(nd), ctypes.byref(nnz), ctypes.byref(nc)))
+        self.ndof, self.nnz = nd.value, nnz.value
+        return nd.value, nnz.value, nc.value
+
+    def get_crs_structure(self):
+        dn = np.zeros(self.nno, np.int32)
+        rp = np.zeros(self.ndof + 1, np.int32)
+        ci = np.zeros(self.nnz, np.int32)
+        self._check(self.L.gbfem_get_crs_structure(self._h, _p(dn), _p(rp), _p(ci)))
+        return dn, rp, ci
+
+    def get_element_tables(self):
+        t = np.zeros(self.nel * (self.nv * self.nv + self.nv), np.int32)
+        self._check(self.L.gbfem_get_element_tables(self._h, _p(t)))
+        return t
+
+    # ---------------- hot path ----------------
+    def create_assemble_stiff_mat(self, int_ent_type, int_ent_id, color_elems, color_faces, asse_pos,
+                                  assembly_table, comp_type=COMP_BOTH, crs_val=None, rhs=None, level_id=0):
+        """ModFEM pdr_create_assemble_stiff_mat through the C ABI (host arrays)."""
+        t, i = _i32(int_ent_type), _i32(int_ent_id)
+        ce, cf = _i32(color_elems), _i32(color_faces)
+        ap, at = _i32(asse_pos), _i32(assembly_table)
+        self._keep["dropin"] = (t, i, ce, cf, ap, at)
+        pdeg = ctypes.c_int(-10)
+        self._check(self.L.gbfem_create_assemble_stiff_mat(
+            self._h, level_id, comp_type, ctypes.byref(pdeg), i.size, _p(t), _p(i),
+            0 if ce is None else ce.size - 1, _p(ce), 0 if cf is None else cf.size - 1, _p(cf), _p(ap), _p(at),
+            self.nv, _p(crs_val), _p(rhs)))
+
+    def assemble(self, mode=SCATTER_ATOMIC):
+        self._check(self.L.gbfem_assemble(self._h, mode))
+
+    def get_matrix(self, val=None, rhs=None):
+        val = np.zeros(self.nnz) if val is None else val
+        rhs = np.zeros(self.ndof) if rhs is None else rhs
+        self._check(self.L.gbfem_get_matrix(self._h, _p(val), _p(rhs)))
+        return val, rhs
+
+    def set_matrix(self, val=None, rhs=None):
+        self._check(self.L.gbfem_set_matrix(self._h, _p(_f64(val)), _p(_f64(rhs))))
+
+    def compute_residual(self, x, b=None, use_rhs=1, ini_zero=0):
+        x = _f64(x)
+        b = _f64(b)
+        v = np.zeros(self.ndof)
+        self._check(self.L.gbfem_compute_residual(self._h, use_rhs, ini_zero, self.ndof, _p(x), _p(b), _p(v)))
+        return v
+
+    def solve(self, krylov=30, max_iter=1000, tol_rel=1e-8, x0=None):
+        x = np.zeros(self.ndof) if x0 is None else np.array(x0, dtype=np.float64)
+        res, rel = ctypes.c_double(), ctypes.c_double()
+        it = self._check(self.L.gbfem_solve(self._h, krylov, max_iter, tol_rel, 1 if x0 is None else 0, _p(x),
+                                            ctypes.byref(res), ctypes.byref(rel)))
+        return x, it, res.value, rel.value
+
+    def last_timing(self):
+        """(total ms, element-kernel ms, kernel launches) of the last assembly call."""
+        ms, el, nl = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        self._check(self.L.gbfem_last_assembly_timing(self._h, ctypes.byref(ms), ctypes.byref(el),
+                                                      ctypes.byref(nl)))
+        return ms.value, el.value, nl.value
+
+    def measure_fp64_peak(self):
+        v = ctypes.c_double()
+        self._check(self.L.gbfem_measure_fp64_peak(self._h, ctypes.byref(v)))
+        return v.value
+
+
+class PinnedArray:
+    """numpy view of page-locked host memory from gbfem_host_alloc."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.L = load_library()
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        self.ptr = self.L.gbfem_host_alloc(max(nbytes, 8))
+        if not self.ptr:
+            raise GbFemError(self.L.gbfem_last_error().decode())
+        buf = (ctypes.c_char * max(nbytes, 8)).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            self.L.gbfem_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

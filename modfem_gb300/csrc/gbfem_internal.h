@@ -1,0 +1,144 @@
+// Internal declarations shared by the CUDA translation units of libmodfem_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/modfem_gb300.h"
+
+namespace gbfem {
+
+void set_error(const std::string &msg);
+
+#define GB_CUDA(call)                                                                        \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      ::gbfem::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                \
+      return -1;                                                                             \
+    }                                                                                        \
+  } while (0)
+
+#define GB_CHECK(cond, msg)                                                                  \
+  do {                                                                                       \
+    if (!(cond)) {                                                                           \
+      ::gbfem::set_error(msg);                                                               \
+      return -2;                                                                             \
+    }                                                                                        \
+  } while (0)
+
+// Device buffer with explicit size tracking (no torch, no allocator layers).
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  int alloc(size_t count) {
+    if (count <= n && p) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return 0;
+    if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
+      set_error("cudaMalloc failed for " + std::to_string(count * sizeof(T)) + " bytes");
+      return -1;
+    }
+    n = count;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// Host-side structure built from the mesh (DOF order, CRS, tables, colours).
+struct HostStructure {
+  int ndof = 0;
+  std::vector<int> dof_of_node;
+  std::vector<int> row_ptr;
+  std::vector<int> col_ind;
+  std::vector<int> el_table;      // 42 (prism) or 20 (tet) ints per element
+  std::vector<int> fa_table;      // per bc face: 16 value positions + 4 rhs (unused slots -1)
+  std::vector<int> el_color_ptr;  // colour c holds el_perm[el_color_ptr[c] .. el_color_ptr[c+1])
+  std::vector<int> el_perm;
+  std::vector<int> fa_color_ptr;  // same for the boundary faces
+  std::vector<int> fa_perm;
+};
+
+int build_host_structure(int nno, int nel, int nv, const int *el_nodes, int nfa, const int *fa_el,
+                         const int *fa_side, HostStructure &hs);
+void color_entities(int nent, int nv, const std::vector<int> &ent_dofs, int nd, std::vector<int> &color_ptr,
+                    std::vector<int> &perm);
+
+// kernel launchers (return the number of kernels launched, < 0 on error)
+int launch_prism_elements(cudaStream_t st, bool atomic, bool aniso, int count, const int *ent_el,
+                          int el_base, const int *ent_pos, int nel, const int *el_nodes,
+                          const double *xyz, const double *k_el, const double *D_el, double f,
+                          const int *tab, double *val, double *rhs, int do_sm, int do_rhs, int *err);
+int launch_prism_faces(cudaStream_t st, bool atomic, int count, const int *ent_fa, int fa_base,
+                       const int *fa_map, int fa_map_len, const int *ent_pos, int nfa,
+                       const int *fa_el, const int *fa_side, const int *el_nodes,
+                       const double *xyz, double penalty, double g, const int *tab, double *val,
+                       double *rhs, int do_sm, int do_rhs, int *err);
+int launch_tet_elements(cudaStream_t st, bool atomic, int count, const int *ent_el, int el_base,
+                        const int *ent_pos, int nel, const int *el_nodes, const double *xyz,
+                        const double *k_el, double f, const int *tab, double *val, double *rhs,
+                        int do_sm, int do_rhs, int *err);
+int launch_spmv(cudaStream_t st, int mode, int n, const int *row_ptr, const int *col_ind, const double *val,
+                const double *x, const double *b, const double *scale, double *v);
+int launch_jacobi_diag(cudaStream_t st, int n, const int *row_ptr, const int *col_ind, const double *val,
+                       double *dinv);
+int reduction_blocks(int n);
+int launch_multidot(cudaStream_t st, int n, int m, const double *base, long long ld, const double *w,
+                    double *partial, double *out, int sqrt_out);
+int launch_multiaxpy(cudaStream_t st, int n, int m, const double *c, double sign, const double *base,
+                     long long ld, double *y);
+int launch_scale(cudaStream_t st, int n, const double *alpha, int invert, const double *x, double *y);
+int launch_mul(cudaStream_t st, int n, const double *a, double *y);
+int measure_fp64_peak(cudaStream_t st, int device, double *tflops);
+
+}  // namespace gbfem
+
+struct gbfem_ctx_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  // mesh
+  int nno = 0, nel = 0, nv = 0, nfa = 0;
+  int max_fa_id = 0;
+  gbfem::DevBuf<double> xyz;
+  gbfem::DevBuf<int> el_nodes;
+  gbfem::DevBuf<int> fa_el, fa_side;
+  std::vector<int> h_fa_id, h_fa_el, h_fa_side, h_el_nodes;
+  std::vector<int> fa_index_of_id;  // reference face id -> bc face index (-1 none)
+  // coefficients
+  gbfem::DevBuf<double> k_el, D_el;
+  int aniso = 0;
+  double f = 1.0, g = 0.0, penalty = 1.0e7;
+  // structure
+  int ndof = 0;
+  long long nnz = 0;
+  gbfem::DevBuf<int> row_ptr, col_ind, dof_of_node;
+  gbfem::DevBuf<int> el_table, el_perm, fa_perm, fa_map;
+  std::vector<int> h_el_color_ptr, h_fa_color_ptr;
+  gbfem::HostStructure hs;
+  bool have_structure = false, have_tables = false;
+  // matrix
+  gbfem::DevBuf<double> val, rhs, dinv;
+  gbfem::DevBuf<int> err;
+  // drop-in staging (kept between calls when table caching is on)
+  gbfem::DevBuf<int> in_id, in_pos, in_table;
+  const void *cache_key[3] = {nullptr, nullptr, nullptr};
+  long long cache_len[3] = {0, 0, 0};
+  int cache_tables = 0;
+  // Krylov workspace
+  gbfem::DevBuf<double> V, w, tmp, x, b, partial, hcol;
+  // timing
+  float last_ms = 0.f, last_el_ms = 0.f;
+  int last_launches = 0;
+};

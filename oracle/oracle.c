@@ -356,6 +356,12 @@ int orc_color_entities(int nent, int nv, const int *ent_dofs, int ndof, int *col
    element loop; lar_assemble_SM_and_LV_with_table_crs,
    las_crs_intf.c:440-518).  Faces are assembled serially before the
    elements. */
+/* when set, the assemble routine adds |entries| instead of entries: the sum
+   of absolute contributions that bounds the rounding error of every assembled
+   value, used as the error scale of the parity tests */
+static int g_accumulate_abs = 0;
+void orc_set_accumulate_abs(int on) { g_accumulate_abs = on; }
+
 double orc_std_prism_assemble(int nel, const int *el_nodes, const double *coords, const double *k_el,
                               const double *D_el, double f, int nfa, const int *fa_el,
                               const int *fa_side, double penalty, double g,
@@ -375,8 +381,8 @@ double orc_std_prism_assemble(int nel, const int *el_nodes, const double *coords
     }
     orc_std_prism_face(X, fa_side[ifa], penalty, g, sm, r);
     orc_crs_table(6, dofs, row_ptr, col_ind, table);
-    for (j = 0; j < 36; j++) val[table[j]] += sm[j];
-    for (j = 0; j < 6; j++) rhs[table[36 + j]] += r[j];
+    for (j = 0; j < 36; j++) val[table[j]] += g_accumulate_abs ? fabs(sm[j]) : sm[j];
+    for (j = 0; j < 6; j++) rhs[table[36 + j]] += g_accumulate_abs ? fabs(r[j]) : r[j];
   }
   int ncol = el_color_ptr ? 1 : 0, c;
   if (el_color_ptr) { while (el_color_ptr[ncol] < nel) ncol++; }
@@ -402,8 +408,8 @@ double orc_std_prism_assemble(int nel, const int *el_nodes, const double *coords
       else { double k = k_el ? k_el[e] : 1.0; A[0] = A[4] = A[8] = k; }
       orc_std_prism_element(X, A, f, sm, r);
       orc_crs_table(6, dofs, row_ptr, col_ind, table);
-      for (j = 0; j < 36; j++) val[table[j]] += sm[j];
-      for (j = 0; j < 6; j++) rhs[table[36 + j]] += r[j];
+      for (j = 0; j < 36; j++) val[table[j]] += g_accumulate_abs ? fabs(sm[j]) : sm[j];
+      for (j = 0; j < 6; j++) rhs[table[36 + j]] += g_accumulate_abs ? fabs(r[j]) : r[j];
     }
   }
   return now_s() - t0;

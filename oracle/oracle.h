@@ -46,6 +46,9 @@ double orc_std_prism_assemble(int nel, const int *el_nodes, const double *coords
                               const int *el_color_ptr, const int *el_perm, int nthreads,
                               double *val, double *rhs);
 
+/* makes orc_std_prism_assemble add |entries| (error scale for parity checks) */
+void orc_set_accumulate_abs(int on);
+
 /* v = (use_rhs ? b : 0) - A x  (CRS) */
 void orc_crs_residual(int n, const int *row_ptr, const int *col_ind, const double *val,
                       int use_rhs, const double *b, const double *x, double *v);

@@ -37,6 +37,7 @@ def lib():
         L.orc_std_prism_assemble.argtypes = [ci, vp, vp, vp, vp, cd, ci, vp, vp, cd, cd, vp, vp, vp,
                                              vp, vp, ci, vp, vp]
         L.orc_std_prism_assemble.restype = cd
+        L.orc_set_accumulate_abs.argtypes = [ci]
         L.orc_crs_residual.argtypes = [ci, vp, vp, vp, ci, vp, vp, vp]
         L.orc_gmres_jacobi.argtypes = [ci, vp, vp, vp, vp, vp, ci, ci, cd, vp, vp]
         _L = L
@@ -127,6 +128,18 @@ def std_prism_assemble(mesh, k_el, dof_of_node, row_ptr, col_ind, f=1.0, penalty
                                      _p(_c(row_ptr, np.int32)), _p(_c(col_ind, np.int32)), _p(cp),
                                      _p(pm), nthreads, _p(val), _p(rhs))
     return val, rhs, t
+
+
+def std_prism_assemble_abs(mesh, k_el, dof_of_node, row_ptr, col_ind, **kw):
+    """Sum of |contributions| per CRS entry and rhs row: the scale against
+    which assembled values are compared (each contribution carries its own
+    relative rounding error, so a sum with cancellation cannot be matched to
+    a relative tolerance of the sum itself)."""
+    lib().orc_set_accumulate_abs(1)
+    try:
+        return std_prism_assemble(mesh, k_el, dof_of_node, row_ptr, col_ind, **kw)
+    finally:
+        lib().orc_set_accumulate_abs(0)
 
 
 def crs_residual(row_ptr, col_ind, val, x, b=None):

@@ -1,0 +1,96 @@
+"""Shared helpers for the parity tests: golden fixtures and error measures."""
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+# Parity tolerance for FP64 values: relative to the entry, with entries that
+# are cancellation-dominated (below 1e-3 of their row's largest magnitude)
+# measured against that floor instead.
+REL_TOL = 1e-12
+FLOOR = 1e-3
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+class FixtureMesh:
+    """Mesh object with the attributes the library binding and oracle use."""
+
+    def __init__(self, g):
+        self.coords = g["coords"]
+        self.el_nodes = g["el_nodes"].astype(np.int32)
+        self.bc_face_id = g["bc_face_id"].astype(np.int32)
+        self.bc_face_el = g["bc_face_el"].astype(np.int32)
+        self.bc_face_bc = g["bc_face_bc"].astype(np.int32)
+        # side from the numbering rule (checked against the generator in test_mesh)
+        from modfem_gb300.mesh import structured_prism_mesh
+        m = structured_prism_mesh(int(g["n"]), jitter=float(g["jitter"]), seed=int(g["seed"]))
+        self.bc_face_side = m.bc_face_side
+
+    @property
+    def nno(self):
+        return self.coords.shape[0]
+
+    @property
+    def nel(self):
+        return self.el_nodes.shape[0]
+
+
+def crs_rel_err(row_ptr, a, b, scale=None):
+    """Assembled-value error.
+
+    With ``scale`` (the per-entry sum of absolute element contributions,
+    oracle.std_prism_assemble_abs): max |a-b| / scale.  An assembled value is
+    a sum of element contributions, each exact to FP64 rounding relative to
+    itself; where the sum cancels, no two summation orders agree relative to
+    the sum, so the sum of magnitudes is the scale the 1e-12 applies to.  For
+    entries without cancellation (scale == |b|) this is the plain relative
+    error.  Without ``scale``: max |a-b| / max(|b|, FLOOR * max|row of b|)."""
+    if scale is not None:
+        den = np.where(scale > 0, scale, 1.0)
+        return float(np.max(np.abs(a - b) / den)) if a.size else 0.0
+    n = row_ptr.size - 1
+    rows = np.repeat(np.arange(n), np.diff(row_ptr))
+    rowmax = np.zeros(n)
+    np.maximum.at(rowmax, rows, np.abs(b))
+    den = np.maximum(np.abs(b), FLOOR * rowmax[rows])
+    den[den == 0] = 1.0
+    return float(np.max(np.abs(a - b) / den)) if a.size else 0.0
+
+
+def mat_rel_err(a, b):
+    """Element matrices: max |a-b| / max(|b|, FLOOR * max|b|) over entries."""
+    den = np.maximum(np.abs(b), FLOOR * np.abs(b).max())
+    den[den == 0] = 1.0
+    return float(np.max(np.abs(a - b) / den))
+
+
+def vec_rel_err(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def abs_scale(mesh, k, dof_of_node, row_ptr, col_ind, **kw):
+    """Per-entry sum of |element contributions| from the oracle."""
+    import oracle as O
+    sv, sr, _ = O.std_prism_assemble_abs(mesh, k, dof_of_node, row_ptr, col_ind, **kw)
+    return sv
+
+
+def energy_scale(row_ptr, col_ind, b):
+    """sqrt(|b_rr| |b_cc|) per CRS entry: the Cauchy-Schwarz bound of an entry
+    of a symmetric positive semi-definite matrix, i.e. the size of the entry in
+    the energy inner product.  Entry (r, c) of a stiffness matrix is an
+    integral of k grad(phi_r).grad(phi_c), a sum of dot products whose
+    rounding error is proportional to |grad phi_r||grad phi_c|, so this is the
+    scale a relative tolerance applies to; for diagonal entries it is the
+    entry itself."""
+    n = row_ptr.size - 1
+    rows = np.repeat(np.arange(n), np.diff(row_ptr))
+    diag = np.zeros(n)
+    isd = rows == col_ind
+    diag[rows[isd]] = np.abs(b[isd])
+    return np.sqrt(diag[rows] * diag[col_ind])

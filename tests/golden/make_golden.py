@@ -1,0 +1,106 @@
+"""Generates the golden fixtures in this directory from the reference ModFEM.
+
+Runs the reference C path compiled in-tree (``make -C oracle/ref``, which
+needs the ModFEM sources) through ``oracle/refmod.py``: the reference's own jk
+mesh reader, approximation module, weak forms, sir_create, the table-driven
+assembly driver and GMRES.  Each case runs in a fresh process because the
+reference keeps its meshes, fields and solvers in global arrays.
+
+    python tests/golden/make_golden.py            # all cases
+    python tests/golden/make_golden.py std_n4     # one case
+
+Fixtures are small .npz files; the GPU machine never needs the reference.
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+# name: (n, jitter, seed, keep element matrices, krylov, tol)
+CASES = {
+    "std_n4": (4, 0.2, 3, True, 30, 1e-8),
+    "std_n10": (10, 0.2, 5, False, 30, 1e-8),
+    "std_n3_flat": (3, 0.0, 0, True, 30, 1e-10),
+}
+
+
+def run_case(name):
+    import refmod
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh, write_jk
+
+    n, jitter, seed, keep_el, krylov, tol = CASES[name]
+    m = structured_prism_mesh(n, jitter=jitter, seed=seed)
+    k = lognormal_k(m.nel, seed=seed) if jitter > 0 else np.ones(m.nel)
+    tmp = tempfile.mkdtemp()
+    jk = os.path.join(tmp, "mesh.jk")
+    mkb = os.path.join(tmp, "mkb.dat")
+    write_jk(jk, n)
+    refmod.write_mkb(mkb, krylov=krylov, max_iter=5000, tol=tol)
+    R = refmod.RefModfem("std")
+    R.load_jk(jk)
+    ref_xyz0 = R.node_coords()
+    R.set_node_coords(m.coords)
+    R.init_field("s", 1)
+    R.set_coeffs(k=k, f=1.0, g=0.0)
+    out = dict(n=n, jitter=jitter, seed=seed, krylov=krylov, tol=tol,
+               coords=R.node_coords(), coords_unjittered=ref_xyz0, el_nodes=R.el_nodes() - 1, k=k)
+    fid, fbc, fel = R.bc_faces()
+    out.update(bc_face_id=fid, bc_face_bc=fbc, bc_face_el=fel - 1)
+    if keep_el:
+        sms, rhss = [], []
+        for e in range(R.max_el):
+            K, r, _ = R.int_ent_stiff(refmod.APC_ELEMENT, e + 1)
+            sms.append(K)
+            rhss.append(r)
+        out.update(el_sm=np.array(sms), el_rhs=np.array(rhss))
+        fsm, frhs = [], []
+        for f in fid:
+            K, r, _ = R.int_ent_stiff(refmod.APC_FACE, int(f))
+            fsm.append(K)
+            frhs.append(r)
+        out.update(fa_sm=np.array(fsm), fa_rhs=np.array(frhs))
+    R.solver_create(mkb)
+    ll = R.level_lists()
+    R.assemble()
+    rp, ci, val, rhs = R.crs()
+    dof_of_node = np.full(R.max_node, -1, np.int32)
+    dof_of_node[ll["dof_ent_id"] - 1] = ll["dof_posglob"]
+    out.update(row_ptr=rp, col_ind=ci, crs_val=val, crs_rhs=rhs, dof_of_node=dof_of_node,
+               int_ent_type=ll["int_ent_type"], int_ent_id=ll["int_ent_id"], color_elems=ll["color_elems"],
+               color_faces=ll["color_faces"], asse_pos=ll["asse_pos"], assembly_table=ll["assembly_table"])
+    # residual of a deterministic vector through lar_compute_residual
+    x = np.sin(np.arange(R.ndof) * 0.37)
+    out.update(resid_x=x, resid_v=R.residual(x, None, 1))
+    sol, nit, meas, _ = R.solve(-1, -1.0)
+    xs = np.zeros(R.ndof)
+    has = dof_of_node >= 0
+    xs[dof_of_node[has]] = sol[1:R.max_node + 1][has]
+    out.update(gmres_x=xs, gmres_iters=nit, gmres_meas=meas)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}: nel {R.max_el} ndof {R.ndof} nnz {R.nnz} colours {R.nr_colors_elems}/{R.nr_colors_faces} "
+          f"gmres {nit} it", file=sys.stderr)
+
+
+def main(argv):
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref")])
+    names = argv or list(CASES)
+    if len(names) == 1 and os.environ.get("MAKE_GOLDEN_CHILD"):
+        with open(os.devnull, "w") as dn:
+            # the reference prints progress on stdout; keep only our stderr summary
+            os.dup2(dn.fileno(), 1)
+            run_case(names[0])
+        return
+    for nm in names:
+        env = dict(os.environ, MAKE_GOLDEN_CHILD="1")
+        subprocess.check_call([sys.executable, __file__, nm], env=env)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

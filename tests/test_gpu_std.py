@@ -1,0 +1,324 @@
+"""GPU parity of the std-linear integrate / assemble / SpMV / GMRES path.
+
+All calls go through the C ABI (libmodfem_gb300.so via ctypes).  References:
+golden fixtures made by the reference ModFEM compiled in-tree
+(tests/golden/make_golden.py) and, for sizes without fixtures, the C oracle
+pinned by tests/test_oracle.py.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from _util import FixtureMesh, REL_TOL, crs_rel_err, energy_scale, load, mat_rel_err, vec_rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gb():
+    from modfem_gb300 import build
+    build.build(verbose=False)
+    import modfem_gb300
+    return modfem_gb300
+
+
+def make_ctx(gb, m, k, structure=None, f=1.0, penalty=1e7):
+    c = gb.Context(0)
+    c.set_mesh(m)
+    c.set_coefficients(k=k, f=f, g=0.0, penalty=penalty)
+    if structure is not None:
+        c.set_crs_structure(*structure)
+    return c
+
+
+# ---------------------------------------------------------------- element level
+def block_tables(nent, n):
+    """Assembly tables into a block-diagonal CRS: entity i owns values
+    [i*n*n, (i+1)*n*n) and rhs [i*n, (i+1)*n), so the assembled values are the
+    local matrices themselves."""
+    t = np.zeros((nent, n * n + n), np.int32)
+    t[:, :n * n] = np.arange(nent)[:, None] * n * n + np.arange(n * n)[None, :]
+    t[:, n * n:] = np.arange(nent)[:, None] * n + np.arange(n)[None, :]
+    return t.reshape(-1), (np.arange(nent) * (n * n + n)).astype(np.int32)
+
+
+def block_structure(nent, n):
+    rp = (np.arange(nent * n + 1) * n).astype(np.int32)
+    ci = np.tile(np.arange(n), nent * n).astype(np.int32)  # column values unused by the kernels
+    return np.zeros(1, np.int32), rp, ci
+
+
+@pytest.mark.parametrize("name", ["std_n4", "std_n3_flat"])
+def test_element_matrices_vs_reference(gb, name):
+    g = load(name)
+    m = FixtureMesh(g)
+    nel = m.nel
+    dn, rp, ci = block_structure(nel, 6)
+    c = make_ctx(gb, m, g["k"])
+    c.set_crs_structure(np.zeros(m.nno, np.int32), rp, ci)
+    tab, pos = block_tables(nel, 6)
+    types = np.full(nel, gb.ELEMENT, np.int32)
+    ids = np.arange(1, nel + 1, dtype=np.int32)
+    val = np.zeros(36 * nel)
+    rhs = np.zeros(6 * nel)
+    c.create_assemble_stiff_mat(types, ids, np.array([0, nel], np.int32), None, pos, tab, crs_val=val, rhs=rhs)
+    for e in range(nel):
+        K = val[36 * e:36 * e + 36].reshape(6, 6).T  # column-major -> (row w, column u)
+        assert mat_rel_err(K, g["el_sm"][e]) < REL_TOL, e
+        assert vec_rel_err(rhs[6 * e:6 * e + 6], g["el_rhs"][e]) < REL_TOL, e
+
+
+def test_face_matrices_vs_reference(gb):
+    g = load("std_n4")
+    m = FixtureMesh(g)
+    nfa = m.bc_face_id.size
+    c = make_ctx(gb, m, g["k"])
+    dn, rp, ci = block_structure(nfa, 6)
+    c.set_crs_structure(np.zeros(m.nno, np.int32), rp, ci)
+    tab, pos = block_tables(nfa, 6)
+    types = np.full(nfa, gb.FACE, np.int32)
+    val = np.zeros(36 * nfa)
+    rhs = np.zeros(6 * nfa)
+    c.create_assemble_stiff_mat(types, m.bc_face_id, None, np.array([0, nfa], np.int32), pos, tab, crs_val=val,
+                                rhs=rhs)
+    for i in range(nfa):
+        K = val[36 * i:36 * i + 36].reshape(6, 6).T
+        assert mat_rel_err(K, g["fa_sm"][i]) < REL_TOL, i
+
+
+# ------------------------------------------------------------- drop-in boundary
+def test_dropin_create_assemble_matches_reference(gb):
+    """pdr_create_assemble_stiff_mat drop-in fed with the reference's own
+    entity lists, colours and assembly tables (sir_create output)."""
+    g = load("std_n10")
+    m = FixtureMesh(g)
+    c = make_ctx(gb, m, g["k"], (g["dof_of_node"], g["row_ptr"], g["col_ind"]))
+    val = np.zeros(g["col_ind"].size)
+    rhs = np.zeros(g["row_ptr"].size - 1)
+    sc = energy_scale(g["row_ptr"], g["col_ind"], g["crs_val"])
+    for _ in range(2):  # the second call must clear and give the same values
+        c.create_assemble_stiff_mat(g["int_ent_type"], g["int_ent_id"], g["color_elems"], g["color_faces"],
+                                    g["asse_pos"], g["assembly_table"], crs_val=val, rhs=rhs)
+        assert crs_rel_err(g["row_ptr"], val, g["crs_val"], sc) < REL_TOL
+        assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL
+    ms, el_ms, launches = c.last_timing()
+    assert launches == 2 and ms > 0
+
+
+def test_dropin_table_cache(gb):
+    g = load("std_n10")
+    m = FixtureMesh(g)
+    c = make_ctx(gb, m, g["k"], (g["dof_of_node"], g["row_ptr"], g["col_ind"]))
+    c.set_option(gb.OPT_CACHE_TABLES, 1)
+    args = [np.ascontiguousarray(g[k], dtype=np.int32) for k in
+            ("int_ent_type", "int_ent_id", "color_elems", "color_faces", "asse_pos", "assembly_table")]
+    val = np.zeros(g["col_ind"].size)
+    rhs = np.zeros(g["row_ptr"].size - 1)
+    k2 = g["k"] * 2.0
+    c.create_assemble_stiff_mat(*args, crs_val=val, rhs=rhs)
+    c.set_coefficients(k=k2)
+    c.create_assemble_stiff_mat(*args, crs_val=val, rhs=rhs)  # cached tables, new coefficients
+    vo, ro, _ = O.std_prism_assemble(m, k2, g["dof_of_node"], g["row_ptr"], g["col_ind"])
+    sc = energy_scale(g["row_ptr"], g["col_ind"], vo)
+    assert crs_rel_err(g["row_ptr"], val, vo, sc) < REL_TOL
+
+
+def test_dropin_rejects_bad_entities_and_recovers(gb):
+    g = load("std_n4")
+    m = FixtureMesh(g)
+    d, nd = O.dof_order(m.el_nodes, m.nno)
+    rp, ci = O.crs_structure(m.el_nodes, d, nd)
+    c = make_ctx(gb, m, g["k"], (d, rp, ci))
+    nel = m.nel
+    tab = np.concatenate([O.crs_table(d[m.el_nodes[e]], rp, ci) for e in range(nel)])
+    pos = (np.arange(nel) * 42).astype(np.int32)
+    ids = np.arange(1, nel + 1, dtype=np.int32)
+    bad = ids.copy()
+    bad[5] = nel + 7  # not an element of the mesh
+    types = np.full(nel, gb.ELEMENT, np.int32)
+    with pytest.raises(gb.GbFemError, match="outside the mesh"):
+        c.create_assemble_stiff_mat(types, bad, np.array([0, nel], np.int32), None, pos, tab)
+    with pytest.raises(gb.GbFemError):
+        c.create_assemble_stiff_mat(types, ids, np.array([0, nel], np.int32), None, pos, tab, level_id=1)
+    # the context stays usable
+    val = np.zeros(ci.size)
+    rhs = np.zeros(nd)
+    c.create_assemble_stiff_mat(types, ids, np.array([0, nel], np.int32), None, pos, tab, crs_val=val, rhs=rhs)
+    vo = np.zeros(ci.size)
+    ro = np.zeros(nd)
+    for e in range(nel):
+        K, r = O.std_prism_element(m.coords[m.el_nodes[e]], np.diag([g["k"][e]] * 3))
+        t = tab[42 * e:42 * e + 42]
+        np.add.at(vo, t[:36], K.T.reshape(-1))
+        np.add.at(ro, t[36:], r)
+    assert crs_rel_err(rp, val, vo, energy_scale(rp, ci, vo)) < REL_TOL
+
+
+# -------------------------------------------------- library-built structure
+@pytest.mark.parametrize("name", ["std_n4", "std_n10"])
+def test_built_structure_and_assembly_vs_reference(gb, name):
+    g = load(name)
+    m = FixtureMesh(g)
+    c = make_ctx(gb, m, g["k"])
+    nd, nnz, ncol = c.build_structure()
+    dn, rp, ci = c.get_crs_structure()
+    assert np.array_equal(dn, g["dof_of_node"])
+    assert np.array_equal(rp, g["row_ptr"])
+    assert np.array_equal(ci, g["col_ind"])
+    sc = energy_scale(rp, ci, g["crs_val"])
+    for mode in (gb.SCATTER_ATOMIC, gb.SCATTER_COLOR):
+        c.assemble(mode)
+        val, rhs = c.get_matrix()
+        assert crs_rel_err(rp, val, g["crs_val"], sc) < REL_TOL, mode
+        assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL, mode
+
+
+def test_color_mode_is_deterministic(gb):
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(16, jitter=0.2, seed=9)
+    k = lognormal_k(m.nel, seed=9)
+    c = make_ctx(gb, m, k)
+    c.build_structure()
+    c.assemble(gb.SCATTER_COLOR)
+    v1, r1 = c.get_matrix()
+    c.assemble(gb.SCATTER_COLOR)
+    v2, r2 = c.get_matrix()
+    assert np.array_equal(v1, v2) and np.array_equal(r1, r2)
+
+
+# ------------------------------------------------------------ SpMV and GMRES
+def test_residual_vs_reference(gb):
+    g = load("std_n10")
+    m = FixtureMesh(g)
+    c = make_ctx(gb, m, g["k"], (g["dof_of_node"], g["row_ptr"], g["col_ind"]))
+    c.set_matrix(g["crs_val"], g["crs_rhs"])
+    v = c.compute_residual(g["resid_x"])
+    assert vec_rel_err(v, g["resid_v"]) < 1e-12
+    v0 = c.compute_residual(g["resid_x"], ini_zero=1)
+    assert np.array_equal(v0, g["crs_rhs"])
+    b = np.cos(np.arange(v.size))
+    v2 = c.compute_residual(g["resid_x"], b=b)
+    assert vec_rel_err(v2, O.crs_residual(g["row_ptr"], g["col_ind"], g["crs_val"], g["resid_x"], b)) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["std_n4", "std_n10", "std_n3_flat"])
+def test_gmres_vs_reference(gb, name):
+    g = load(name)
+    m = FixtureMesh(g)
+    c = make_ctx(gb, m, g["k"], (g["dof_of_node"], g["row_ptr"], g["col_ind"]))
+    c.set_matrix(g["crs_val"], g["crs_rhs"])
+    x, it, res, rel = c.solve(int(g["krylov"]), 5000, float(g["tol"]))
+    assert abs(it - int(g["gmres_iters"])) <= 1
+    assert rel < float(g["tol"])
+    # both stop at the same relative preconditioned residual; solutions agree
+    # to the accuracy that tolerance allows
+    assert vec_rel_err(x, g["gmres_x"]) < 1e3 * float(g["tol"])
+
+
+def test_gmres_tight_tolerance_vs_oracle(gb):
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(8, jitter=0.2, seed=2)
+    k = lognormal_k(m.nel, seed=2)
+    c = make_ctx(gb, m, k)
+    c.build_structure()
+    c.assemble(gb.SCATTER_ATOMIC)
+    val, rhs = c.get_matrix()
+    dn, rp, ci = c.get_crs_structure()
+    x, it, res, rel = c.solve(30, 20000, 1e-13)
+    xo, ito, _, _ = O.gmres_jacobi(rp, ci, val, rhs, 30, 20000, 1e-13)
+    assert vec_rel_err(x, xo) < 1e-9
+    # the stopping measure is the Jacobi-preconditioned residual (the 1e7
+    # penalty rows dominate the unpreconditioned one)
+    rows = np.repeat(np.arange(rp.size - 1), np.diff(rp))
+    diag = val[rows == ci]
+    r = O.crs_residual(rp, ci, val, x, rhs) / diag
+    # GMRES stops at max(1e-13 * initial, 1e-12 absolute): here the absolute floor
+    assert np.linalg.norm(r) < 1.1 * max(1e-12, 1e-13 * np.linalg.norm(rhs / diag))
+
+
+# ------------------------------------------------------------ larger sizes
+def test_stiffness_without_penalty_vs_oracle(gb):
+    """Stiffness alone (penalty 0): every entry against the oracle in the
+    energy scale sqrt(a_rr a_cc), and the diagonal entrywise."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(30, jitter=0.2, seed=6)
+    k = lognormal_k(m.nel, seed=6)
+    c = make_ctx(gb, m, k, penalty=0.0)
+    c.build_structure()
+    c.assemble(gb.SCATTER_ATOMIC)
+    val, rhs = c.get_matrix()
+    dn, rp, ci = c.get_crs_structure()
+    vo, ro, _ = O.std_prism_assemble(m, k, dn, rp, ci, penalty=0.0)
+    assert crs_rel_err(rp, val, vo, energy_scale(rp, ci, vo)) < REL_TOL
+    rows = np.repeat(np.arange(rp.size - 1), np.diff(rp))
+    d = rows == ci
+    assert np.max(np.abs(val[d] - vo[d]) / np.abs(vo[d])) < REL_TOL
+    assert vec_rel_err(rhs, ro) < REL_TOL
+
+
+def test_config1_size_vs_oracle(gb):
+    """20^3 x 2 = 16,000 prisms (the reference's CPU-runnable configuration)."""
+    from modfem_gb300.mesh import structured_prism_mesh
+    m = structured_prism_mesh(20)
+    k = np.ones(m.nel)
+    c = make_ctx(gb, m, k)
+    nd, nnz, _ = c.build_structure()
+    assert (nd, nnz) == (9261, 178181)
+    c.assemble(gb.SCATTER_ATOMIC)
+    val, rhs = c.get_matrix()
+    dn, rp, ci = c.get_crs_structure()
+    vo, ro, _ = O.std_prism_assemble(m, k, dn, rp, ci)
+    assert crs_rel_err(rp, val, vo, energy_scale(rp, ci, vo)) < REL_TOL
+    assert vec_rel_err(rhs, ro) < REL_TOL
+    x, it, res, rel = c.solve(30, 5000, 1e-8)
+    xo, ito, _, _ = O.gmres_jacobi(rp, ci, vo, ro, 30, 5000, 1e-8)
+    assert abs(it - ito) <= 1
+    assert vec_rel_err(x, xo) < 1e-5
+
+
+@pytest.mark.slow
+def test_full_size_properties():
+    """100^3 x 2 = 2,000,000 jittered prisms with lognormal k (the benchmark
+    workload): structure identical to the oracle's, colour and atomic
+    scatter agree, rhs sums to f*|cube| = 1, the matrix is symmetric, and a
+    sample of rows matches the oracle."""
+    import modfem_gb300 as gb
+    from modfem_gb300 import build
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    build.build(verbose=False)
+    m = structured_prism_mesh(100, jitter=0.2, seed=1)
+    k = lognormal_k(m.nel, seed=1)
+    c = make_ctx(gb, m, k)
+    nd, nnz, ncol = c.build_structure()
+    assert (nd, nnz) == (1030301, 21250901)
+    dn, rp, ci = c.get_crs_structure()
+    d2, _ = O.dof_order(m.el_nodes, m.nno)
+    assert np.array_equal(dn, d2)
+    rp2, ci2 = O.crs_structure(m.el_nodes, d2, nd)
+    assert np.array_equal(rp, rp2) and np.array_equal(ci, ci2)
+    c.assemble(gb.SCATTER_ATOMIC)
+    va, ra = c.get_matrix()
+    c.assemble(gb.SCATTER_COLOR)
+    vc, rc = c.get_matrix()
+    sc = energy_scale(rp, ci, va)
+    assert crs_rel_err(rp, va, vc, sc) < REL_TOL
+    assert abs(ra.sum() - 1.0) < 1e-12
+    # symmetry: A[r, c] == A[c, r]
+    rows = np.repeat(np.arange(nd), np.diff(rp))
+    key = rows.astype(np.int64) * nd + ci
+    keyt = ci.astype(np.int64) * nd + rows
+    order = np.argsort(key)
+    post = np.searchsorted(key[order], keyt)
+    assert crs_rel_err(rp, va, va[order[post]], sc) < REL_TOL
+    vo, ro, _ = O.std_prism_assemble(m, k, dn, rp, ci, nthreads=8)
+    assert crs_rel_err(rp, va, vo, energy_scale(rp, ci, vo)) < REL_TOL
+    # stiffness alone (no penalty on the diagonal to hide behind)
+    c.set_coefficients(k=k, f=1.0, g=0.0, penalty=0.0)
+    c.assemble(gb.SCATTER_ATOMIC)
+    vs, _ = c.get_matrix()
+    vso, _, _ = O.std_prism_assemble(m, k, dn, rp, ci, penalty=0.0, nthreads=8)
+    assert crs_rel_err(rp, vs, vso, energy_scale(rp, ci, vso)) < REL_TOL
+    # constants are in the kernel of the stiffness: A 1 = 0 to rounding
+    rows_sum = np.add.reduceat(vs, rp[:-1])
+    assert np.max(np.abs(rows_sum)) < 1e-12 * np.max(np.abs(vs))
+    assert vec_rel_err(ra, ro) < REL_TOL
