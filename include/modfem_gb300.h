@@ -143,6 +143,26 @@ int gbfem_set_matrix(gbfem_ctx ctx, const double *crs_val, const double *rhs);
 int gbfem_compute_residual(gbfem_ctx ctx, int Use_rhs, int Ini_zero, int Ndof, const double *X,
                            const double *B, double *V);
 
+/* No counterpart in the reference.  The same residual as
+ * gbfem_compute_residual for callers that cannot let the library allocate
+ * device memory: a host application whose own memory manager has already
+ * claimed the GPU's memory (so a cudaMalloc would fail or steal from its
+ * pool), or one calling from a latency-critical loop where the device-wide
+ * synchronisation a cudaMalloc/cudaFree may imply is not acceptable.  This call
+ * allocates nothing: the device copies of X and B and the result V are staged
+ * in one file-scope __device__ array of 3 * GBFEM_NOALLOC_MAX_NDOF doubles
+ * (6 MiB) that every GPU loading the library holds until the process exits.
+ * Ndof above GBFEM_NOALLOC_MAX_NDOF is rejected with an error.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.  All
+ * calls on a device share the one array, so calls whose work overlaps on the
+ * GPU (two contexts or threads on the same device at once) race and must be
+ * serialised by the caller.  The matrix is the context's device-resident one,
+ * set up beforehand. */
+#define GBFEM_NOALLOC_MAX_NDOF 262144
+int gbfem_compute_residual_noalloc(gbfem_ctx ctx, int Use_rhs, int Ini_zero, int Ndof, const double *X,
+                                   const double *B, double *V);
+
 /* Replaces lsr_mkb_core_gmres with the point-Jacobi preconditioner
  * (lsd_mkb_core/lss_mkb_core.c:2317-2660, lad_crs/las_crs_intf.c:707,857):
  * restarted GMRES(krylov), classical Gram-Schmidt, Givens rotations, stop

@@ -42,6 +42,7 @@ SIGNATURES = [
     ("gbfem_get_matrix", _ci, [_vp, _vp, _vp]),
     ("gbfem_set_matrix", _ci, [_vp, _vp, _vp]),
     ("gbfem_compute_residual", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
+    ("gbfem_compute_residual_noalloc", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
     ("gbfem_solve", _ci, [_vp, _ci, _ci, _cd, _ci, _vp, _pd, _pd]),
     ("gbfem_last_assembly_timing", _ci, [_vp, _pd, _pd, _pi]),
     ("gbfem_host_alloc", _vp, [_cll]),
@@ -194,6 +195,15 @@ class Context:
         b = _f64(b)
         v = np.zeros(self.ndof)
         self._check(self.L.gbfem_compute_residual(self._h, use_rhs, ini_zero, self.ndof, _p(x), _p(b), _p(v)))
+        return v
+
+    def compute_residual_noalloc(self, x, b=None, use_rhs=1, ini_zero=0):
+        """gbfem_compute_residual_noalloc: same result, no device allocation."""
+        x = _f64(x)
+        b = _f64(b)
+        v = np.zeros(self.ndof)
+        self._check(self.L.gbfem_compute_residual_noalloc(self._h, use_rhs, ini_zero, self.ndof, _p(x), _p(b),
+                                                          _p(v)))
         return v
 
     def solve(self, krylov=30, max_iter=1000, tol_rel=1e-8, x0=None):

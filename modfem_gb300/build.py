@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libmodfem_gb300.so")
 OBJDIR = os.path.join(HERE, "_build")
-SOURCES = ["api.cu", "std_kernels.cu", "krylov.cu", "structure.cpp"]
+SOURCES = ["api.cu", "std_kernels.cu", "krylov.cu", "structure.cpp", "noalloc.cu"]
 HEADERS = ["gbfem_internal.h", os.path.join("..", "..", "include", "modfem_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
