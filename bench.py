@@ -36,9 +36,14 @@ METRIC = "elem/s integrate+assemble vs plain FP64 GPU @1e-10 rel; served p50/p99
 UNIT = "elem/s"
 N_HEX = 100
 JITTER, SEED = 0.2, 1
-# algorithmic FP64 work per std prism: nq*(151 + 18*ns + 2*ns) + 2*3*nq*ns^2
-# with nq = 6 quadrature points, ns = 6 shape functions
-FLOP_PER_ELEM = 6 * (151 + 18 * 6 + 2 * 6) + 2 * 3 * 6 * 36
+# FP64 work per std prism.  Textbook count of the reference algorithm:
+# nq*(151 + 18*ns + 2*ns) + 2*3*nq*ns^2 with nq = ns = 6.  The kernel's
+# quadrature-aggregated formulation executes 289 DFMA + 213 other FP64
+# instructions per element (ncu instruction mix, profiles/std_prism_elements_2M.md),
+# i.e. 791 flop and 502 FP64-pipe issue slots.
+SURVEY_FLOP_PER_ELEM = 6 * (151 + 18 * 6 + 2 * 6) + 2 * 3 * 6 * 36
+FLOP_PER_ELEM = 2 * 289 + 213
+FP64_SLOTS_PER_ELEM = 289 + 213
 
 
 def parse():
@@ -275,6 +280,15 @@ def main():
     ref_val, ref_rhs = c.get_matrix()
     assert np.max(np.abs(out_val.array - ref_val)) <= 1e-12 * np.max(np.abs(ref_val))
 
+    # ---------------- GMRES(30) + Jacobi on the assembled matrix ----------------
+    c.assemble(gb.SCATTER_ATOMIC)
+    _, it, res, rel = c.solve(30, 300, 1e-14)
+    solve_ms, spmv_ms, nspmv, solve_kernels = c.last_solve_timing()
+    spmv_bytes = 12 * nnz + 16 * nd
+    solver = {"gmres_iterations": it, "gmres_ms_per_iteration": solve_ms / max(it, 1),
+              "spmv_ms": spmv_ms / max(nspmv, 1), "spmv_gbs": spmv_bytes * nspmv / (spmv_ms * 1e-3) / 1e9,
+              "spmv_bytes": spmv_bytes, "relative_residual_after": rel, "kernel_launches": solve_kernels}
+
     # ---------------- CPU baseline (rank 0, N=1 only) ----------------
     cpu = None
     if rank == 0 and ws == 1:
@@ -286,6 +300,7 @@ def main():
                "sample": f"one full {m.nel}-element integrate+assemble (elements + faces), colour-parallel OpenMP"}
 
     achieved = FLOP_PER_ELEM * m.nel / (el_ms_step * 1e-3) / 1e12
+    slot_frac = 2 * FP64_SLOTS_PER_ELEM * m.nel / (el_ms_step * 1e-3) / 1e12 / fp64_peak
     traffic = read_profile_traffic()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -299,12 +314,15 @@ def main():
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp64_peak, "traffic": traffic,
                      "kernel": "prism_elements_kernel", "kernel_ms": el_ms_step,
-                     "flop_per_elem": FLOP_PER_ELEM,
+                     "flop_per_elem": FLOP_PER_ELEM, "fp64_pipe_slot_frac": slot_frac,
+                     "survey_flop_per_elem": SURVEY_FLOP_PER_ELEM,
+                     "survey_equivalent_tflops": SURVEY_FLOP_PER_ELEM * m.nel / (el_ms_step * 1e-3) / 1e12,
                      "peak_source": "FP64 FMA-chain kernel measured in this run (no FP64 figure in the peaks file)"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_s * 1e3},
         "clocks": clocks,
+        "solver": solver,
         "gpu_launches": launches,
         "wall_s_timed_region": wall,
     }

@@ -180,6 +180,13 @@ int gbfem_solve(gbfem_ctx ctx, int krylov, int max_iter, double tol_rel, int ini
  * the library's kernels in the call. */
 int gbfem_last_assembly_timing(gbfem_ctx ctx, double *total_ms, double *element_ms, int *launches);
 
+/* Timing of the last gbfem_solve from CUDA events (no reference
+ * counterpart; the reference prints its iteration time under
+ * MKB_SOLVE_TIME_TEST, sid_mkb/sis_mkb_intf.c:2162-2172): the whole solve, the
+ * preconditioned SpMV launches alone and how many there were, and the
+ * library's kernel launches. */
+int gbfem_last_solve_timing(gbfem_ctx ctx, double *total_ms, double *spmv_ms, int *spmv_count, int *launches);
+
 /* Page-locked host memory for fast transfers (no reference counterpart). */
 void *gbfem_host_alloc(long long bytes);
 int gbfem_host_free(void *ptr);

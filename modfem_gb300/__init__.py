@@ -45,6 +45,7 @@ SIGNATURES = [
     ("gbfem_compute_residual_noalloc", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
     ("gbfem_solve", _ci, [_vp, _ci, _ci, _cd, _ci, _vp, _pd, _pd]),
     ("gbfem_last_assembly_timing", _ci, [_vp, _pd, _pd, _pi]),
+    ("gbfem_last_solve_timing", _ci, [_vp, _pd, _pd, _pi, _pi]),
     ("gbfem_host_alloc", _vp, [_cll]),
     ("gbfem_host_free", _ci, [_vp]),
     ("gbfem_measure_fp64_peak", _ci, [_vp, _pd]),
@@ -219,6 +220,13 @@ class Context:
         self._check(self.L.gbfem_last_assembly_timing(self._h, ctypes.byref(ms), ctypes.byref(el),
                                                       ctypes.byref(nl)))
         return ms.value, el.value, nl.value
+
+    def last_solve_timing(self):
+        """(total ms, SpMV ms, SpMV count, kernel launches) of the last solve."""
+        t, sp, n, k = ctypes.c_double(), ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.gbfem_last_solve_timing(self._h, ctypes.byref(t), ctypes.byref(sp), ctypes.byref(n),
+                                                   ctypes.byref(k)))
+        return t.value, sp.value, n.value, k.value
 
     def measure_fp64_peak(self):
         v = ctypes.c_double()

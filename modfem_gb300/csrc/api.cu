@@ -427,6 +427,15 @@ int gbfem_last_assembly_timing(gbfem_ctx c, double *total_ms, double *element_ms
   return 0;
 }
 
+int gbfem_last_solve_timing(gbfem_ctx c, double *total_ms, double *spmv_ms, int *spmv_count, int *launches) {
+  GB_CHECK(c, "null context");
+  if (total_ms) *total_ms = c->last_solve_ms;
+  if (spmv_ms) *spmv_ms = c->last_spmv_ms;
+  if (spmv_count) *spmv_count = c->last_spmv_count;
+  if (launches) *launches = c->last_solve_kernels;
+  return 0;
+}
+
 void *gbfem_host_alloc(long long bytes) {
   void *p = nullptr;
   if (bytes <= 0 || cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocPortable) != cudaSuccess) {
@@ -526,6 +535,9 @@ int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_z
   std::vector<double> H((size_t)(m + 1) * (m + 1), 0.0), cs(m + 1), sn(m + 1), s(m + 2), hh(m + 2);
   double beta0 = -1.0, resid = 0.0;
   int it = 0;
+  float spmv_ms = 0.f;
+  int spmv_n = 0, kernels = 1;
+  cudaEventRecord(c->ev0, st);
   for (;;) {
     // v0 = D^-1 (b - A x)
     GB_TRY(gbfem::launch_spmv(st, 0, n, c->row_ptr.p, c->col_ind.p, c->val.p, c->x.p, c->rhs.p, nullptr, c->tmp.p));
@@ -545,7 +557,10 @@ int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_z
       double *vj = c->V.p + (size_t)j * n, *w = c->V.p + (size_t)(j + 1) * n;
       it++;
       // w = D^-1 A v_j
+      cudaEventRecord(c->ev2, st);
       GB_TRY(gbfem::launch_spmv(st, 1, n, c->row_ptr.p, c->col_ind.p, c->val.p, vj, nullptr, c->dinv.p, w));
+      cudaEventRecord(c->ev3, st);
+      kernels += 8;
       // classical Gram-Schmidt: h = V^T w, w -= V h, h_{j+1} = |w|
       GB_TRY(gbfem::launch_multidot(st, n, j + 1, c->V.p, ld, w, c->partial.p, c->hcol.p, 0));
       GB_TRY(gbfem::launch_multiaxpy(st, n, j + 1, c->hcol.p, -1.0, c->V.p, ld, w));
@@ -553,6 +568,12 @@ int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_z
       GB_CUDA(cudaMemcpyAsync(hh.data(), c->hcol.p, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st));
       GB_TRY(gbfem::launch_scale(st, n, c->hcol.p + j + 1, 1, w, w));
       GB_CUDA(cudaStreamSynchronize(st));
+      {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev2, c->ev3);
+        spmv_ms += ms;
+        spmv_n++;
+      }
       for (int k = 0; k <= j + 1; k++) H[k + (size_t)j * (m + 1)] = hh[k];
       for (int k = 0; k < j; k++) {
         const double a = H[k + (size_t)j * (m + 1)], b = H[k + 1 + (size_t)j * (m + 1)];
@@ -587,8 +608,13 @@ int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_z
     GB_CUDA(cudaStreamSynchronize(st));
     if (resid < tol_abs || resid / beta0 < tol_rel || it >= max_iter) break;
   }
+  cudaEventRecord(c->ev1, st);
   GB_CUDA(cudaMemcpyAsync(x, c->x.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));
+  cudaEventElapsedTime(&c->last_solve_ms, c->ev0, c->ev1);
+  c->last_spmv_ms = spmv_ms;
+  c->last_spmv_count = spmv_n;
+  c->last_solve_kernels = kernels;
   if (res_out) *res_out = resid;
   if (res_rel_out) *res_rel_out = beta0 > 0 ? resid / beta0 : 0.0;
   return it;

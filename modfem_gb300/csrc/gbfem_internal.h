@@ -139,6 +139,7 @@ struct gbfem_ctx_s {
   // Krylov workspace
   gbfem::DevBuf<double> V, w, tmp, x, b, partial, hcol;
   // timing
-  float last_ms = 0.f, last_el_ms = 0.f;
+  float last_ms = 0.f, last_el_ms = 0.f, last_solve_ms = 0.f, last_spmv_ms = 0.f;
+  int last_spmv_count = 0, last_solve_kernels = 0;
   int last_launches = 0;
 };

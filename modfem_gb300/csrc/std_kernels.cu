@@ -5,22 +5,19 @@
 // the element's assembly table, so element matrices never reach HBM.  On
 // GB300 the FP64 pipe (about 1.2 TFLOP/s, 1/58 of the FP32 rate) bounds
 // these kernels, not HBM, so the arithmetic is arranged to minimise FP64
-// instructions:
+// instructions; the isotropic prism math lives in prism_std.cuh (see there).
+// The full-tensor variant below integrates per quadrature point:
 //  * the Jacobian of the linear prism splits into ζ-only columns
 //    (dx/dξ = m1 + ζ d1, dx/dη = m2 + ζ d2) and a (ξ,η)-only column
-//    (dx/dζ = c0 + ξ d1 + η d2), so the ζ-only cross product is shared by the
-//    three triangle points of each Gauss line point;
+//    (dx/dζ = c0 + ξ d1 + η d2);
 //  * gradients use the adjugate rows (no 3x3 inverse), det and the weight
-//    fold into one scale w/|det| applied once per shape function;
-//  * shape-function derivative patterns (0, ±h, ±L/2) are compile-time
-//    constants of the fixed quadrature, so each physical gradient is one
-//    FMA triple;
-//  * only the 21 upper entries of the symmetric matrix are integrated.
-// The result equals the reference's apr_num_int_el (apd_std_lin/
+//    fold into one scale w/|det| applied once per shape function.
+// Both equal the reference's apr_num_int_el (apd_std_lin/
 // aps_std_lin_intf.c:1537-2880 with apr_elem_calc_3D_prism, aps_std_util.c:
 // 520-820) up to rounding.
 
 #include "gbfem_internal.h"
+#include "prism_std.cuh"
 
 namespace gbfem {
 
@@ -88,66 +85,6 @@ __device__ __forceinline__ void scatter6(const int *__restrict__ tab, const doub
   if (do_rhs) {
 #pragma unroll
     for (int w = 0; w < 6; w++) add_val<ATOMIC>(rhs, t[36 + w], R[w]);
-  }
-}
-
-// Integrates one std prism: K (21 packed upper entries), R (6).
-// k_iso used when A == nullptr.
-__device__ __forceinline__ void prism_element(const d3 (&X)[6], double kk, double f, double (&K)[21],
-                                              double (&R)[6]) {
-  const d3 a0 = X[0], a1 = X[1], a2 = X[2], b0 = X[3], b1 = X[4], b2 = X[5];
-  const d3 ea = a1 - a0, eb = b1 - b0, fa = a2 - a0, fb = b2 - b0;
-  const d3 m1 = 0.5 * (ea + eb), d1 = 0.5 * (eb - ea);
-  const d3 m2 = 0.5 * (fa + fb), d2 = 0.5 * (fb - fa);
-  const d3 c0 = 0.5 * (b0 - a0);
-#pragma unroll
-  for (int i = 0; i < 21; i++) K[i] = 0.0;
-#pragma unroll
-  for (int i = 0; i < 6; i++) R[i] = 0.0;
-  const double wq = 0.5 * GB_TW * 1.0;
-#pragma unroll
-  for (int iz = 0; iz < 2; iz++) {
-    const double zeta = iz == 0 ? -GB_G2 : GB_G2;
-    const double hlo = (1.0 - zeta) / 2.0, hhi = (1.0 + zeta) / 2.0;
-    const d3 j1 = fma3(zeta, d1, m1), j2 = fma3(zeta, d2, m2);
-    const d3 c3 = cross(j1, j2);  // third adjugate row, ζ only
-#pragma unroll
-    for (int it = 0; it < 3; it++) {
-      const double xi = it == 2 ? GB_T2 : GB_T1;
-      const double eta = it == 1 ? GB_T2 : GB_T1;
-      const double L0 = 1.0 - xi - eta;
-      const d3 j3 = fma3(eta, d2, fma3(xi, d1, c0));
-      const d3 c1 = cross(j2, j3), c2 = cross(j3, j1);
-      const double det = dot(j1, c1);
-      const double adet = fabs(det);
-      const double inv = 1.0 / adet;
-      const double s = kk * wq * inv;      // k w / |det|
-      const double fv = f * wq * adet;     // f w |det|
-      // unscaled gradients g_{t,s} = h_s e_t + sigma_s (L_t/2) c3
-      const d3 e0 = -1.0 * (c1 + c2);
-      const double hL0 = 0.5 * L0, hL1 = 0.5 * xi, hL2 = 0.5 * eta;
-      d3 g[6];
-      g[0] = fma3(hlo, e0, -hL0 * c3);
-      g[1] = fma3(hlo, c1, -hL1 * c3);
-      g[2] = fma3(hlo, c2, -hL2 * c3);
-      g[3] = fma3(hhi, e0, hL0 * c3);
-      g[4] = fma3(hhi, c1, hL1 * c3);
-      g[5] = fma3(hhi, c2, hL2 * c3);
-      int k = 0;
-#pragma unroll
-      for (int u = 0; u < 6; u++) {
-        const d3 p = s * g[u];
-#pragma unroll
-        for (int w = u; w < 6; w++, k++) K[k] = fma(p.x, g[w].x, fma(p.y, g[w].y, fma(p.z, g[w].z, K[k])));
-      }
-      const double flo = fv * hlo, fhi = fv * hhi;
-      R[0] = fma(flo, L0, R[0]);
-      R[1] = fma(flo, xi, R[1]);
-      R[2] = fma(flo, eta, R[2]);
-      R[3] = fma(fhi, L0, R[3]);
-      R[4] = fma(fhi, xi, R[4]);
-      R[5] = fma(fhi, eta, R[5]);
-    }
   }
 }
 
@@ -238,7 +175,9 @@ __global__ void __launch_bounds__(128) prism_elements_kernel(
   double R[6];
   if (!ANISO) {
     double K[21];
-    prism_element(X, k_el ? __ldg(k_el + e) : 1.0, f, K, R);
+    const v3 Xv[6] = {{X[0].x, X[0].y, X[0].z}, {X[1].x, X[1].y, X[1].z}, {X[2].x, X[2].y, X[2].z},
+                      {X[3].x, X[3].y, X[3].z}, {X[4].x, X[4].y, X[4].z}, {X[5].x, X[5].y, X[5].z}};
+    prism_std_element(Xv, k_el ? __ldg(k_el + e) : 1.0, f, K, R);
     scatter6<ATOMIC>(tb, K, R, val, rhs, do_sm, do_rhs);
   } else {
     double K[36];

@@ -194,3 +194,54 @@ def prism_min_detj(mesh):
             det = np.einsum("ij,ij->i", jx, np.cross(jy, jz))
             dmin = min(dmin, det.min())
     return dmin
+
+
+class TetMesh:
+    """Flat tetrahedral mesh (0-based), vertices in positive orientation."""
+
+    def __init__(self, n, coords, el_nodes):
+        self.n = n
+        self.coords = coords
+        self.el_nodes = el_nodes
+        self.bc_face_id = np.zeros(0, np.int32)
+        self.bc_face_el = np.zeros(0, np.int32)
+        self.bc_face_side = np.zeros(0, np.int32)
+        self.bc_face_bc = np.zeros(0, np.int32)
+
+    @property
+    def nno(self):
+        return self.coords.shape[0]
+
+    @property
+    def nel(self):
+        return self.el_nodes.shape[0]
+
+
+# the six tetrahedra of a cube around its main diagonal (corner b = dx + 2 dy + 4 dz)
+_KUHN = np.array([[0, 1, 3, 7], [0, 1, 5, 7], [0, 2, 3, 7], [0, 2, 6, 7], [0, 4, 5, 7], [0, 4, 6, 7]])
+
+
+def structured_tet_mesh(n, jitter=0.0, seed=0):
+    """Unit cube, n^3 hexahedra x 6 tetrahedra (Kuhn split), nodes numbered
+    x fastest, then y, then z; jitter keeps boundary nodes on their planes."""
+    N = n + 1
+    i, j, k = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    coords = np.stack([i.T.reshape(-1), j.T.reshape(-1), k.T.reshape(-1)], 1) / n
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-jitter / n, jitter / n, size=coords.shape)
+        on_bnd = (np.abs(coords) < 1e-12) | (np.abs(coords - 1.0) < 1e-12)
+        d[on_bnd] = 0.0
+        coords = coords + d
+    ci, cj, ck = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    ci, cj, ck = ci.T.reshape(-1), cj.T.reshape(-1), ck.T.reshape(-1)
+    corner = np.zeros((ci.size, 8), np.int64)
+    for b in range(8):
+        dx, dy, dz = b & 1, (b >> 1) & 1, (b >> 2) & 1
+        corner[:, b] = (ci + dx) + (cj + dy) * N + (ck + dz) * N * N
+    el = corner[:, _KUHN].reshape(-1, 4)
+    X = coords[el]
+    det = np.einsum("ij,ij->i", X[:, 1] - X[:, 0], np.cross(X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]))
+    flip = det < 0
+    el[flip, 2], el[flip, 3] = el[flip, 3].copy(), el[flip, 2].copy()
+    return TetMesh(n, coords, el.astype(np.int32))

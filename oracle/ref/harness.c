@@ -717,3 +717,43 @@ int refh_solver_free(void)
   h_solver_id = -1;
   return 0;
 }
+
+#ifdef HARNESS_STD
+/* Std linear tetrahedron through the reference's own element calculations:
+   apr_set_quadr_3D (aps_std_util.c:1335) and apr_elem_calc_3D with the
+   tetra base (aps_std_util.c:869), accumulated with the 9-term diffusion and
+   source loops of apr_num_int_el (aps_std_lin_intf.c:2113-2134, 2785-2791).
+   The tet mesh module (mmd_t4_prism) needs Boost and is not linked, so the
+   element loop is driven here with given vertex coordinates. */
+extern int apr_set_quadr_3D(int Base_type, int *Pdeg_vec, int *Ngauss, double *Xg, double *Wg);
+extern double apr_elem_calc_3D(int Control, int Nreq, int *Pdeg_vec, int Base_type, double *Eta,
+                               double *Node_coor, double *Sol_dofs, double *Base_phi, double *Base_dphix,
+                               double *Base_dphiy, double *Base_dphiz, double *Xcoor, double *Sol,
+                               double *Dsolx, double *Dsoly, double *Dsolz, double *Vec_nor);
+void apr_gauss_init(void);
+
+int refh_tet_element(const double *Xin, const double *A, double f, double *sm, double *rhs)
+{
+  static int init = 0;
+  int pdeg = 1, ng, q, u, w;
+  double xg[3000], wg[1000], X[12];
+  if (!init) { apr_gauss_init(); init = 1; }
+  memcpy(X, Xin, 12 * sizeof(double));
+  apr_set_quadr_3D(APC_BASE_TETRA_STD, &pdeg, &ng, xg, wg);
+  for (u = 0; u < 16; u++) sm[u] = 0.0;
+  for (u = 0; u < 4; u++) rhs[u] = 0.0;
+  for (q = 0; q < ng; q++) {
+    double phi[APC_MAXELVD], gx[APC_MAXELVD], gy[APC_MAXELVD], gz[APC_MAXELVD], xc[3];
+    double det = apr_elem_calc_3D(2, 1, &pdeg, APC_BASE_TETRA_STD, &xg[3 * q], X, NULL, phi, gx, gy, gz, xc,
+                                  NULL, NULL, NULL, NULL, NULL);
+    double vol = det * wg[q];
+    for (u = 0; u < 4; u++)
+      for (w = 0; w < 4; w++)
+        sm[u * 4 + w] += (A[0] * gx[u] * gx[w] + A[1] * gy[u] * gx[w] + A[2] * gz[u] * gx[w] +
+                          A[3] * gx[u] * gy[w] + A[4] * gy[u] * gy[w] + A[5] * gz[u] * gy[w] +
+                          A[6] * gx[u] * gz[w] + A[7] * gy[u] * gz[w] + A[8] * gz[u] * gz[w]) * vol;
+    for (w = 0; w < 4; w++) rhs[w] += f * phi[w] * vol;
+  }
+  return ng;
+}
+#endif

@@ -63,10 +63,18 @@ def crs_rel_err(row_ptr, a, b, scale=None):
 
 
 def mat_rel_err(a, b):
-    """Element matrices: max |a-b| / max(|b|, FLOOR * max|b|) over entries."""
-    den = np.maximum(np.abs(b), FLOOR * np.abs(b).max())
-    den[den == 0] = 1.0
-    return float(np.max(np.abs(a - b) / den))
+    """Local (element or face) matrices: max |a_ij - b_ij| / sqrt(|b_ii| |b_jj|),
+    the energy-scale measure of crs_rel_err / energy_scale applied to one
+    local matrix (plain relative error on the diagonal).  Rows without a
+    diagonal (vertices off a boundary face) are compared against |b_ij|."""
+    d = np.sqrt(np.abs(np.diag(b)))
+    den = np.outer(d, d)
+    den = np.where(den > 0, den, np.abs(b))
+    err = np.abs(a - b)
+    ok = den > 0
+    if np.any(err[~ok] != 0):
+        return float("inf")
+    return float(np.max(err[ok] / den[ok])) if np.any(ok) else 0.0
 
 
 def vec_rel_err(a, b):

@@ -88,14 +88,43 @@ def run_case(name):
           f"gmres {nit} it", file=sys.stderr)
 
 
+def run_tets(name="std_tet_n2"):
+    """Std linear tetrahedra through the reference's apr_elem_calc_3D (tetra
+    base) and quadrature; no tet mesh module is linked, so the elements come
+    from the structured Kuhn split with jitter."""
+    import refmod
+    from modfem_gb300.mesh import lognormal_k, structured_tet_mesh
+    import ctypes
+    m = structured_tet_mesh(2, jitter=0.15, seed=8)
+    k = lognormal_k(m.nel, seed=8)
+    L = ctypes.CDLL(refmod.lib_path("std"))
+    L.refh_tet_element.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
+                                   ctypes.c_void_p]
+    sms, rhss = [], []
+    for e in range(m.nel):
+        X = np.ascontiguousarray(m.coords[m.el_nodes[e]]).reshape(-1)
+        A = np.ascontiguousarray(np.diag([k[e]] * 3)).reshape(-1)
+        sm = np.zeros(16)
+        r = np.zeros(4)
+        L.refh_tet_element(X.ctypes.data, A.ctypes.data, 1.0, sm.ctypes.data, r.ctypes.data)
+        sms.append(sm.reshape(4, 4).T.copy())
+        rhss.append(r)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), coords=m.coords, el_nodes=m.el_nodes, k=k,
+                        el_sm=np.array(sms), el_rhs=np.array(rhss))
+    print(f"{name}: {m.nel} tets", file=sys.stderr)
+
+
 def main(argv):
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref")])
-    names = argv or list(CASES)
+    names = argv or list(CASES) + ["std_tet_n2"]
     if len(names) == 1 and os.environ.get("MAKE_GOLDEN_CHILD"):
         with open(os.devnull, "w") as dn:
             # the reference prints progress on stdout; keep only our stderr summary
             os.dup2(dn.fileno(), 1)
-            run_case(names[0])
+            if names[0] == "std_tet_n2":
+                run_tets(names[0])
+            else:
+                run_case(names[0])
         return
     for nm in names:
         env = dict(os.environ, MAKE_GOLDEN_CHILD="1")

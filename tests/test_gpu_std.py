@@ -322,3 +322,47 @@ def test_full_size_properties():
     rows_sum = np.add.reduceat(vs, rp[:-1])
     assert np.max(np.abs(rows_sum)) < 1e-12 * np.max(np.abs(vs))
     assert vec_rel_err(ra, ro) < REL_TOL
+
+
+# ------------------------------------------------------------- tetrahedra
+def test_tet_element_matrices_vs_reference(gb):
+    g = load("std_tet_n2")
+    from modfem_gb300.mesh import TetMesh
+    m = TetMesh(2, g["coords"], g["el_nodes"])
+    nel = m.nel
+    c = make_ctx(gb, m, g["k"])
+    dn, rp, ci = block_structure(nel, 4)
+    c.set_crs_structure(np.zeros(m.nno, np.int32), rp, ci)
+    tab, pos = block_tables(nel, 4)
+    val = np.zeros(16 * nel)
+    rhs = np.zeros(4 * nel)
+    c.create_assemble_stiff_mat(np.full(nel, gb.ELEMENT, np.int32), np.arange(1, nel + 1, dtype=np.int32),
+                                np.array([0, nel], np.int32), None, pos, tab, crs_val=val, rhs=rhs)
+    for e in range(nel):
+        K = val[16 * e:16 * e + 16].reshape(4, 4).T
+        assert mat_rel_err(K, g["el_sm"][e]) < REL_TOL, e
+        assert vec_rel_err(rhs[4 * e:4 * e + 4], g["el_rhs"][e]) < REL_TOL, e
+
+
+def test_tet_mesh_structure_and_assembly_vs_oracle(gb):
+    from modfem_gb300.mesh import lognormal_k, structured_tet_mesh
+    m = structured_tet_mesh(12, jitter=0.1, seed=4)
+    k = lognormal_k(m.nel, seed=4)
+    c = make_ctx(gb, m, k)
+    nd, nnz, ncol = c.build_structure()
+    dn, rp, ci = c.get_crs_structure()
+    d2, nd2 = O.dof_order(m.el_nodes, m.nno)
+    rp2, ci2 = O.crs_structure(m.el_nodes, d2, nd2)
+    assert np.array_equal(dn, d2) and np.array_equal(rp, rp2) and np.array_equal(ci, ci2)
+    vo = np.zeros(nnz)
+    ro = np.zeros(nd)
+    for e in range(m.nel):
+        K, r = O.std_tet_element(m.coords[m.el_nodes[e]], np.diag([k[e]] * 3), 1.0)
+        t = O.crs_table(dn[m.el_nodes[e]], rp, ci)
+        np.add.at(vo, t[:16], K.T.reshape(-1))
+        np.add.at(ro, t[16:], r)
+    for mode in (gb.SCATTER_ATOMIC, gb.SCATTER_COLOR):
+        c.assemble(mode)
+        val, rhs = c.get_matrix()
+        assert crs_rel_err(rp, val, vo, energy_scale(rp, ci, vo)) < REL_TOL
+        assert vec_rel_err(rhs, ro) < REL_TOL

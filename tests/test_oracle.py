@@ -91,3 +91,11 @@ def test_gmres_matches_reference(case):
                                      int(g["krylov"]), 5000, float(g["tol"]))
     assert it == int(g["gmres_iters"])
     assert vec_rel_err(x, g["gmres_x"]) < 1e-10
+
+
+def test_tet_elements_bit_exact():
+    """Std tetrahedra: oracle equals the reference's apr_elem_calc_3D-based integral."""
+    g = load("std_tet_n2")
+    for e in range(g["el_nodes"].shape[0]):
+        K, r = O.std_tet_element(g["coords"][g["el_nodes"][e]], np.diag([g["k"][e]] * 3), 1.0)
+        assert np.array_equal(K, g["el_sm"][e]) and np.array_equal(r, g["el_rhs"][e]), e
