@@ -173,6 +173,48 @@ def cpu_assemble(m, k, nthreads, reps=1):
     return times
 
 
+def dg_fma_per_element(p):
+    """FP64 FMAs of the DG volume kernel per element: nq (9 ns + 3 ns (ns+1)/2)."""
+    ns = {1: 6, 2: 18, 3: 40, 4: 75}[p]
+    nq = {1: 6, 2: 18, 3: 48, 4: 80}[p]
+    return nq * (9 * ns + 3 * ns * (ns + 1) // 2)
+
+
+def bench_dg(gb, local, steps, fp64_peak):
+    """DG prism volume integrals: 60^3 x 2 = 432,000 p=3 prisms with the
+    anisotropic tensor R diag(1, 0.1, 0.01) R^T, and 58^3 x 2 = 390,224 prisms
+    with p drawn uniformly from 1..4 and lognormal k (prisms only)."""
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, structured_prism_mesh
+    out = {}
+    for name, n, mode in (("p3_anisotropic_432k", 60, "p3"), ("mixed_p1to4_390k", 58, "mixed")):
+        m = structured_prism_mesh(n, jitter=0.2, seed=SEED)
+        c = gb.Context(local)
+        c.set_mesh(m)
+        if mode == "p3":
+            pdeg = np.full(m.nel, 3)
+            c.set_coefficients(D=anisotropic_tensors(m.nel, seed=SEED), f=1.0)
+        else:
+            pdeg = np.random.default_rng(SEED).integers(1, 5, m.nel)
+            c.set_coefficients(k=lognormal_k(m.nel, seed=SEED), f=1.0)
+        c.dg_set_degrees(pdeg)
+        nd, nv = c.dg_build_structure()
+        for _ in range(2):
+            c.dg_assemble()
+        tot = 0.0
+        for _ in range(steps):
+            c.dg_assemble()
+            a, b, _ = c.last_timing()
+            tot += b
+        ms = tot / steps
+        fma = sum(dg_fma_per_element(p) * int(np.sum(pdeg == p)) for p in range(1, 5))
+        out[name] = {"elements": m.nel, "dofs": nd, "stored_values": nv, "ms": ms,
+                     "elem_per_s": m.nel / (ms * 1e-3),
+                     "fp64_tflops_executed": 2 * fma / (ms * 1e-3) / 1e12,
+                     "fp64_frac": 2 * fma / (ms * 1e-3) / 1e12 / fp64_peak}
+        c.close()
+    return out
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -289,6 +331,9 @@ def main():
               "spmv_ms": spmv_ms / max(nspmv, 1), "spmv_gbs": spmv_bytes * nspmv / (spmv_ms * 1e-3) / 1e9,
               "spmv_bytes": spmv_bytes, "relative_residual_after": rel, "kernel_launches": solve_kernels}
 
+    # ---------------- DG prism volume integrals ----------------
+    dg = bench_dg(gb, local, max(3, min(args.steps, 10)), fp64_peak)
+
     # ---------------- CPU baseline (rank 0, N=1 only) ----------------
     cpu = None
     if rank == 0 and ws == 1:
@@ -323,6 +368,7 @@ def main():
                 "ms_per_step": e2e_s * 1e3},
         "clocks": clocks,
         "solver": solver,
+        "dg": dg,
         "gpu_launches": launches,
         "wall_s_timed_region": wall,
     }

@@ -136,6 +136,27 @@ int gbfem_get_matrix(gbfem_ctx ctx, double *crs_val, double *rhs);
 /* Uploads CRS values / rhs (either may be NULL), e.g. a matrix assembled elsewhere. */
 int gbfem_set_matrix(gbfem_ctx ctx, const double *crs_val, const double *rhs);
 
+/* ---------------------------------------------------------------------- */
+/* DG prisms (apd_dg_prism)                                                 */
+/* ---------------------------------------------------------------------- */
+/* Per-element degree p = 1..4 of the tensor monomial DG basis (ModFEM pdeg
+ * 101 p, (p+1)^2(p+2)/2 = 6/18/40/75 functions; apr_get_el_pdeg_numshap,
+ * apd_dg_prism/aps_dg_prism_intf.c:725-775).  The mesh must be prisms;
+ * coefficients from gbfem_set_coefficients (a tensor must be symmetric). */
+int gbfem_dg_set_degrees(gbfem_ctx ctx, const int *p_el);
+/* Block-CRS structure of the DG matrix: one dof block per element in element
+ * order (the reference's DG dof entities, utd_util/uts_ls_intf.c:640-700),
+ * dense blocks ns_r x ns_c column-major.  Returns the dof count and the
+ * number of stored values. */
+int gbfem_dg_build_structure(gbfem_ctx ctx, int *ndof, long long *nval);
+/* dof_off[nel+1] first dof of each element; bptr[nel+1], bcol[nblk] block
+ * rows/columns; boff[nblk+1] value offsets.  Returns nblk. */
+int gbfem_dg_get_structure(gbfem_ctx ctx, int *dof_off, int *bptr, int *bcol, long long *boff);
+/* Integrates all elements (apr_num_int_el of apd_dg_prism,
+ * aps_dg_prism_intf.c:1239-1728) into their diagonal blocks and the rhs. */
+int gbfem_dg_assemble(gbfem_ctx ctx);
+int gbfem_dg_get_matrix(gbfem_ctx ctx, double *vals, double *rhs);
+
 /* Drop-in for lar_compute_residual (lsd_mkb/las_intf.c:771,
  * lad_crs/las_crs_intf.c:788-856): V = (Use_rhs ? B : 0) - A*X, X, B, V host
  * arrays of Ndof entries (B NULL: the assembled rhs); Ini_zero != 0 treats X

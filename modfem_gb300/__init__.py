@@ -41,6 +41,11 @@ SIGNATURES = [
     ("gbfem_assemble", _ci, [_vp, _ci]),
     ("gbfem_get_matrix", _ci, [_vp, _vp, _vp]),
     ("gbfem_set_matrix", _ci, [_vp, _vp, _vp]),
+    ("gbfem_dg_set_degrees", _ci, [_vp, _vp]),
+    ("gbfem_dg_build_structure", _ci, [_vp, _pi, _pll]),
+    ("gbfem_dg_get_structure", _ci, [_vp, _vp, _vp, _vp, _vp]),
+    ("gbfem_dg_assemble", _ci, [_vp]),
+    ("gbfem_dg_get_matrix", _ci, [_vp, _vp, _vp]),
     ("gbfem_compute_residual", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
     ("gbfem_compute_residual_noalloc", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
     ("gbfem_solve", _ci, [_vp, _ci, _ci, _cd, _ci, _vp, _pd, _pd]),
@@ -178,6 +183,36 @@ class Context:
             self._h, level_id, comp_type, ctypes.byref(pdeg), i.size, _p(t), _p(i),
             0 if ce is None else ce.size - 1, _p(ce), 0 if cf is None else cf.size - 1, _p(cf), _p(ap), _p(at),
             self.nv, _p(crs_val), _p(rhs)))
+
+    # ---------------- DG prisms ----------------
+    def dg_set_degrees(self, p_el):
+        p = _i32(p_el)
+        self._keep["dgp"] = p
+        self._check(self.L.gbfem_dg_set_degrees(self._h, _p(p)))
+
+    def dg_build_structure(self):
+        nd, nv = ctypes.c_int(), ctypes.c_longlong()
+        self._check(self.L.gbfem_dg_build_structure(self._h, ctypes.byref(nd), ctypes.byref(nv)))
+        self.dg_ndof, self.dg_nval = nd.value, nv.value
+        return nd.value, nv.value
+
+    def dg_get_structure(self):
+        nblk = self._check(self.L.gbfem_dg_get_structure(self._h, None, None, None, None))
+        off = np.zeros(self.nel + 1, np.int32)
+        bptr = np.zeros(self.nel + 1, np.int32)
+        bcol = np.zeros(nblk, np.int32)
+        boff = np.zeros(nblk + 1, np.int64)
+        self._check(self.L.gbfem_dg_get_structure(self._h, _p(off), _p(bptr), _p(bcol), _p(boff)))
+        return off, bptr, bcol, boff
+
+    def dg_assemble(self):
+        self._check(self.L.gbfem_dg_assemble(self._h))
+
+    def dg_get_matrix(self):
+        vals = np.zeros(self.dg_nval)
+        rhs = np.zeros(self.dg_ndof)
+        self._check(self.L.gbfem_dg_get_matrix(self._h, _p(vals), _p(rhs)))
+        return vals, rhs
 
     def assemble(self, mode=SCATTER_ATOMIC):
         self._check(self.L.gbfem_assemble(self._h, mode))

@@ -68,8 +68,12 @@ int gbfem_destroy(gbfem_ctx c) {
   for (auto *b : dbufs) b->release();
   DevBuf<int> *ibufs[] = {&c->el_nodes, &c->fa_el, &c->fa_side, &c->row_ptr, &c->col_ind, &c->dof_of_node,
                           &c->el_table, &c->el_perm, &c->fa_perm, &c->fa_map, &c->err, &c->in_id,
-                          &c->in_pos, &c->in_table};
+                          &c->in_pos, &c->in_table, &c->dg_roff_d};
   for (auto *b : ibufs) b->release();
+  for (int p = 0; p < 5; p++) c->dg_list[p].release();
+  c->dg_boff_diag_d.release();
+  c->dg_val.release();
+  c->dg_rhs.release();
   cudaEventDestroy(c->ev0);
   cudaEventDestroy(c->ev1);
   cudaEventDestroy(c->ev2);
@@ -416,6 +420,103 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
   cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
   cudaEventElapsedTime(&c->last_el_ms, c->ev2, c->ev3);
   c->last_launches = launches;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// DG prisms
+// ---------------------------------------------------------------------------
+int gbfem_dg_set_degrees(gbfem_ctx c, const int *p_el) {
+  GB_CHECK(c && c->nel > 0 && c->nv == GBFEM_PRISM, "DG needs a prism mesh (gbfem_set_mesh)");
+  GB_CHECK(p_el, "null degree array");
+  for (int e = 0; e < c->nel; e++) GB_CHECK(p_el[e] >= 1 && p_el[e] <= 4, "DG degree must be 1..4");
+  c->dg_p.assign(p_el, p_el + c->nel);
+  c->dg_ready = false;
+  return 0;
+}
+
+static const int kDgNs[5] = {0, 6, 18, 40, 75};
+
+int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
+  GB_CHECK(c && !c->dg_p.empty(), "DG degrees not set (gbfem_dg_set_degrees)");
+  GB_CUDA(cudaSetDevice(c->device));
+  const int nel = c->nel;
+  // dof blocks in element order (utr_get_list_ent, DG branch: one dof entity
+  // per element, uts_ls_intf.c:640-700); block rows hold the element itself
+  c->dg_roff.assign(nel + 1, 0);
+  for (int e = 0; e < nel; e++) c->dg_roff[e + 1] = c->dg_roff[e] + kDgNs[c->dg_p[e]];
+  c->dg_ndof = c->dg_roff[nel];
+  c->dg_bptr.assign(nel + 1, 0);
+  c->dg_bcol.assign(nel, 0);
+  c->dg_boff.assign(nel + 1, 0);
+  std::vector<long long> diag(nel);
+  for (int e = 0; e < nel; e++) {
+    c->dg_bptr[e + 1] = e + 1;
+    c->dg_bcol[e] = e;
+    diag[e] = c->dg_boff[e];
+    c->dg_boff[e + 1] = c->dg_boff[e] + (long long)kDgNs[c->dg_p[e]] * kDgNs[c->dg_p[e]];
+  }
+  c->dg_nval = c->dg_boff[nel];
+  for (int p = 1; p <= 4; p++) {
+    std::vector<int> lst;
+    for (int e = 0; e < nel; e++)
+      if (c->dg_p[e] == p) lst.push_back(e);
+    if (lst.empty()) {
+      c->dg_list[p].release();
+      continue;
+    }
+    GB_TRY(upload(c, c->dg_list[p], lst.data(), lst.size()));
+  }
+  GB_TRY(upload(c, c->dg_roff_d, c->dg_roff.data(), c->dg_roff.size()));
+  GB_TRY(upload(c, c->dg_boff_diag_d, diag.data(), diag.size()));
+  GB_TRY(c->dg_val.alloc((size_t)c->dg_nval));
+  GB_TRY(c->dg_rhs.alloc((size_t)c->dg_ndof));
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  c->dg_ready = true;
+  if (ndof) *ndof = c->dg_ndof;
+  if (nval) *nval = c->dg_nval;
+  return 0;
+}
+
+int gbfem_dg_get_structure(gbfem_ctx c, int *dof_off, int *bptr, int *bcol, long long *boff) {
+  GB_CHECK(c && c->dg_ready, "DG structure not built");
+  if (dof_off) memcpy(dof_off, c->dg_roff.data(), c->dg_roff.size() * sizeof(int));
+  if (bptr) memcpy(bptr, c->dg_bptr.data(), c->dg_bptr.size() * sizeof(int));
+  if (bcol) memcpy(bcol, c->dg_bcol.data(), c->dg_bcol.size() * sizeof(int));
+  if (boff) memcpy(boff, c->dg_boff.data(), c->dg_boff.size() * sizeof(long long));
+  return (int)c->dg_bcol.size();
+}
+
+int gbfem_dg_assemble(gbfem_ctx c) {
+  GB_CHECK(c && c->dg_ready, "DG structure not built (gbfem_dg_build_structure)");
+  GB_CUDA(cudaSetDevice(c->device));
+  cudaEventRecord(c->ev0, c->stream);
+  GB_CUDA(cudaMemsetAsync(c->dg_val.p, 0, c->dg_val.bytes(), c->stream));
+  GB_CUDA(cudaMemsetAsync(c->dg_rhs.p, 0, c->dg_rhs.bytes(), c->stream));
+  int launches = 0;
+  cudaEventRecord(c->ev2, c->stream);
+  for (int p = 1; p <= 4; p++) {
+    if (!c->dg_list[p].p) continue;
+    int r = gbfem::launch_dg_prism_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
+                                            c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,
+                                            c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
+    GB_TRY(r);
+    launches += r;
+  }
+  cudaEventRecord(c->ev3, c->stream);
+  cudaEventRecord(c->ev1, c->stream);
+  GB_CUDA(cudaEventSynchronize(c->ev1));
+  cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
+  cudaEventElapsedTime(&c->last_el_ms, c->ev2, c->ev3);
+  c->last_launches = launches;
+  return 0;
+}
+
+int gbfem_dg_get_matrix(gbfem_ctx c, double *vals, double *rhs) {
+  GB_CHECK(c && c->dg_ready, "DG structure not built");
+  if (vals) GB_CUDA(cudaMemcpyAsync(vals, c->dg_val.p, c->dg_val.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->dg_rhs.p, c->dg_rhs.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
 }
 

@@ -101,6 +101,9 @@ int launch_multiaxpy(cudaStream_t st, int n, int m, const double *c, double sign
 int launch_scale(cudaStream_t st, int n, const double *alpha, int invert, const double *x, double *y);
 int launch_mul(cudaStream_t st, int n, const double *a, double *y);
 int measure_fp64_peak(cudaStream_t st, int device, double *tflops);
+int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
+                             const double *xyz, const double *k_el, const double *D_el, double f,
+                             const long long *boff, const int *roff, double *val, double *rhs);
 
 }  // namespace gbfem
 
@@ -138,6 +141,15 @@ struct gbfem_ctx_s {
   int cache_tables = 0;
   // Krylov workspace
   gbfem::DevBuf<double> V, w, tmp, x, b, partial, hcol;
+  // DG prisms: per-element degree, block-CRS structure (block row = element)
+  std::vector<int> dg_p, dg_roff, dg_bptr, dg_bcol;
+  std::vector<long long> dg_boff;
+  long long dg_nval = 0;
+  int dg_ndof = 0;
+  bool dg_ready = false;
+  gbfem::DevBuf<int> dg_list[5], dg_roff_d;
+  gbfem::DevBuf<long long> dg_boff_diag_d;
+  gbfem::DevBuf<double> dg_val, dg_rhs;
   // timing
   float last_ms = 0.f, last_el_ms = 0.f, last_solve_ms = 0.f, last_spmv_ms = 0.f;
   int last_spmv_count = 0, last_solve_kernels = 0;

@@ -245,3 +245,21 @@ def structured_tet_mesh(n, jitter=0.0, seed=0):
     flip = det < 0
     el[flip, 2], el[flip, 3] = el[flip, 3].copy(), el[flip, 2].copy()
     return TetMesh(n, coords, el.astype(np.int32))
+
+
+def random_rotations(n, seed=0):
+    """n seeded random rotation matrices (QR of Gaussian matrices, det +1)."""
+    rng = np.random.default_rng(seed + 104729)
+    Q, R = np.linalg.qr(rng.standard_normal((n, 3, 3)))
+    Q = Q * np.sign(np.diagonal(R, axis1=1, axis2=2))[:, None, :]
+    det = np.linalg.det(Q)
+    Q[det < 0, :, 0] *= -1.0
+    return Q
+
+
+def anisotropic_tensors(n, seed=0, eig=(1.0, 0.1, 0.01)):
+    """D = R diag(eig) R^T per element with seeded random rotations R,
+    row-major 9 values per element."""
+    Q = random_rotations(n, seed)
+    D = np.einsum("nij,j,nkj->nik", Q, np.asarray(eig, float), Q)
+    return D.reshape(n, 9)

@@ -7,6 +7,7 @@
  * are relative to the ModFEM source tree (modfem2017/src).
  */
 #include "oracle.h"
+#include "../modfem_gb300/csrc/dg_tables.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -520,4 +521,61 @@ int orc_gmres_jacobi(int n, const int *row_ptr, const int *col_ind, const double
   *res_rel_out = beta0 > 0 ? resid / beta0 : 0.0;
   free(dinv); free(V); free(H); free(cs); free(sn); free(s); free(tmp);
   return it;
+}
+
+/* ------------------------------------------------------------------ */
+/* DG prism elements (apd_dg_prism)                                    */
+/* ------------------------------------------------------------------ */
+
+/* Tensor DG basis of degree p (pdeg = 101 p): monomials xi^a eta^b zeta^c in
+   the reference's order (apr_shape_fun_3D, apd_dg_prism/aps_dg_util.c:408-995;
+   ordering table in dg_tables.h) and their local derivatives. */
+static int dg_shape(int p, const double *e, double *phi, double *dx, double *dy, double *dz)
+{
+  int ns = GB_DG_NS[p], i;
+  double px[8], py[8], pz[8];
+  px[0] = py[0] = pz[0] = 1.0;
+  for (i = 1; i <= p; i++) { px[i] = px[i - 1] * e[0]; py[i] = py[i - 1] * e[1]; pz[i] = pz[i - 1] * e[2]; }
+  for (i = 0; i < ns; i++) {
+    int a = GB_DG_EXP[p - 1][i][0], b = GB_DG_EXP[p - 1][i][1], c = GB_DG_EXP[p - 1][i][2];
+    phi[i] = px[a] * py[b] * pz[c];
+    dx[i] = a ? a * px[a - 1] * py[b] * pz[c] : 0.0;
+    dy[i] = b ? b * px[a] * py[b - 1] * pz[c] : 0.0;
+    dz[i] = c ? c * px[a] * py[b] * pz[c - 1] : 0.0;
+  }
+  return ns;
+}
+
+int orc_dg_nshape(int p) { return (p >= 1 && p <= GB_DG_PMAX) ? GB_DG_NS[p] : -1; }
+
+/* apr_num_int_el of the DG module (apd_dg_prism/aps_dg_prism_intf.c:1239-1728)
+   for nreq = 1: the volume rule of apr_set_quadr_3D (aps_dg_util.c:1415-1480),
+   the prism geometry of apr_elem_calc_3D (aps_dg_util.c:112-400), the 9-term
+   diffusion (:1582-1606) and the source term (:1680-1715). */
+int orc_dg_prism_element(const double *X, const double *A, double f, int p, double *sm, double *rhs)
+{
+  int ns, nq, q, i;
+  if (p < 1 || p > GB_DG_PMAX) return -1;
+  ns = GB_DG_NS[p];
+  nq = GB_DG_NQ[p];
+  memset(sm, 0, (size_t)ns * ns * sizeof(double));
+  memset(rhs, 0, (size_t)ns * sizeof(double));
+  for (q = 0; q < nq; q++) {
+    const double *qp = GB_DG_QP[p - 1][q];
+    double phi[GB_DG_MAXNS], dx[GB_DG_MAXNS], dy[GB_DG_MAXNS], dz[GB_DG_MAXNS];
+    double gx[GB_DG_MAXNS], gy[GB_DG_MAXNS], gz[GB_DG_MAXNS];
+    double e[3] = {qp[0], qp[1], qp[2]};
+    double ph6[6], d6x[6], d6y[6], d6z[6], J[9], Ji[9];
+    dg_shape(p, e, phi, dx, dy, dz);
+    prism_shape(e, ph6, d6x, d6y, d6z);
+    prism_jacobian(X, d6x, d6y, d6z, J);
+    double det = fabs(mat3_inv(J, Ji));
+    for (i = 0; i < ns; i++) {
+      gx[i] = dx[i] * Ji[0] + dy[i] * Ji[3] + dz[i] * Ji[6];
+      gy[i] = dx[i] * Ji[1] + dy[i] * Ji[4] + dz[i] * Ji[7];
+      gz[i] = dx[i] * Ji[2] + dy[i] * Ji[5] + dz[i] * Ji[8];
+    }
+    accumulate_qp(ns, phi, gx, gy, gz, A, f, det * qp[3], sm, rhs);
+  }
+  return ns;
 }

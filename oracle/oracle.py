@@ -38,6 +38,7 @@ def lib():
                                              vp, vp, ci, vp, vp]
         L.orc_std_prism_assemble.restype = cd
         L.orc_set_accumulate_abs.argtypes = [ci]
+        L.orc_dg_prism_element.argtypes = [vp, vp, cd, ci, vp, vp]
         L.orc_crs_residual.argtypes = [ci, vp, vp, vp, ci, vp, vp, vp]
         L.orc_gmres_jacobi.argtypes = [ci, vp, vp, vp, vp, vp, ci, ci, cd, vp, vp]
         _L = L
@@ -76,6 +77,17 @@ def std_tet_element(X, A, f=1.0):
     rhs = np.zeros(4)
     lib().orc_std_tet_element(_p(X), _p(A), f, _p(sm), _p(rhs))
     return sm.reshape(4, 4).T.copy(), rhs
+
+
+def dg_prism_element(X, A, p, f=1.0):
+    """DG tensor prism of degree p: (ns x ns matrix (row w, column u), rhs)."""
+    X = _c(X, np.float64).reshape(-1)
+    A = _c(A, np.float64).reshape(-1)
+    ns = lib().orc_dg_nshape(p)
+    sm = np.zeros(ns * ns)
+    rhs = np.zeros(ns)
+    lib().orc_dg_prism_element(_p(X), _p(A), f, p, _p(sm), _p(rhs))
+    return sm.reshape(ns, ns).T.copy(), rhs
 
 
 def dof_order(el_nodes, nno):

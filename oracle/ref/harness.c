@@ -340,7 +340,14 @@ double pdr_ctrl_d_params(int Problem_id, int Num)
   if (Num == 12) return h_dg_penalty;
   return 0.0;
 }
-double pdr_time_d_params(int Problem_id, int Num) { (void)Problem_id; (void)Num; return 0.0; }
+/* time-integration parameters: steady problem, fully implicit (index 2 is the
+   implicitness parameter the DG face terms scale by, index 4 the time) */
+double pdr_time_d_params(int Problem_id, int Num)
+{
+  (void)Problem_id;
+  if (Num == 2) return 1.0;
+  return 0.0;
+}
 int pdr_problem_name(int Problem_id, char *Name) { (void)Problem_id; strcpy(Name, "GB300_POISSON"); return 1; }
 
 int pdr_get_bc_type(int Fa_bc)
@@ -356,9 +363,20 @@ void pdr_fa_coeff(int Face, int BC_flag, int Elem, int Mat_num, double Hsize, do
                   double *Anx, double *Any, double *Anz, double *Bn, double *Fval, double *Gval,
                   double *Qn, double *Vel_norm)
 {
-  (void)Face; (void)Elem; (void)Mat_num; (void)Hsize; (void)Time; (void)Pdeg; (void)Xcoor;
-  (void)Vec_norm; (void)U_val; (void)U_x; (void)U_y; (void)U_z;
-  Anx[0] = Any[0] = Anz[0] = 0.0;
+  /* normal diffusion An_j = sum_i a_ij n_i of the element's coefficient, as
+     pdr_fa_coeff builds it (pds_conv_diff_weakform.c:654-695); Dirichlet data */
+  double a[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  (void)Face; (void)Mat_num; (void)Hsize; (void)Time; (void)Pdeg; (void)Xcoor;
+  (void)U_val; (void)U_x; (void)U_y; (void)U_z;
+  if (h_aniso && h_D != NULL && Elem >= 0 && Elem <= h_nel_coef) {
+    memcpy(a, h_D + 9 * (size_t)Elem, 9 * sizeof(double));
+  } else {
+    double k = (h_k != NULL && Elem >= 0 && Elem <= h_nel_coef) ? h_k[Elem] : 1.0;
+    a[0] = a[4] = a[8] = k;
+  }
+  Anx[0] = a[0] * Vec_norm[0] + a[3] * Vec_norm[1] + a[6] * Vec_norm[2];
+  Any[0] = a[1] * Vec_norm[0] + a[4] * Vec_norm[1] + a[7] * Vec_norm[2];
+  Anz[0] = a[2] * Vec_norm[0] + a[5] * Vec_norm[1] + a[8] * Vec_norm[2];
   Bn[0] = 0.0; Fval[0] = 0.0; Gval[0] = 0.0; Qn[0] = 0.0; Vel_norm[0] = 0.0;
   if (pdr_get_bc_type(BC_flag) == PDC_BC_DIRI) Fval[0] = h_g;
 }
@@ -755,5 +773,44 @@ int refh_tet_element(const double *Xin, const double *A, double f, double *sm, d
     for (w = 0; w < 4; w++) rhs[w] += f * phi[w] * vol;
   }
   return ng;
+}
+#endif
+
+#ifdef HARNESS_DG
+/* DG prism approximation (apd_dg_prism) helpers: basis values, quadrature
+   rules and per-element degrees straight from the reference module. */
+extern int apr_shape_fun_3D(int Base_type, int Pdeg, double *Eta, double *Base_phi, double *Base_dphix,
+                            double *Base_dphiy, double *Base_dphiz);
+extern int apr_set_quadr_3D(int Base_type, int *Pdeg_vec, int *Ngauss, double *Xg, double *Wg);
+extern int apr_set_quadr_2D(int Fa_type, int Base_type, int *Pdeg_vec, int *Ngauss, double *Xg, double *Wg);
+void apr_gauss_init(void);
+
+int refh_dg_basis(int pdeg, const double *eta, double *phi, double *dx, double *dy, double *dz)
+{
+  double e[3] = {eta[0], eta[1], eta[2]};
+  return apr_shape_fun_3D(APC_BASE_TENSOR_DG, pdeg, e, phi, dx, dy, dz);
+}
+
+int refh_dg_quadrature(int pdeg, double *xg, double *wg)
+{
+  static int init = 0;
+  int ng = 0, p = pdeg;
+  if (!init) { apr_gauss_init(); init = 1; }
+  apr_set_quadr_3D(APC_BASE_TENSOR_DG, &p, &ng, xg, wg);
+  return ng;
+}
+
+int refh_dg_face_quadrature(int fa_type, int pdeg, double *xg, double *wg)
+{
+  static int init = 0;
+  int ng = 0, p = pdeg;
+  if (!init) { apr_gauss_init(); init = 1; }
+  apr_set_quadr_2D(fa_type, APC_BASE_TENSOR_DG, &p, &ng, xg, wg);
+  return ng;
+}
+
+int refh_set_el_pdeg(int el, int pdeg)
+{
+  return apr_set_ent_pdeg(h_field_id, APC_ELEMENT, el, pdeg);
 }
 #endif

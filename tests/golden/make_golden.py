@@ -114,15 +114,54 @@ def run_tets(name="std_tet_n2"):
     print(f"{name}: {m.nel} tets", file=sys.stderr)
 
 
+def run_dg_elements(name="dg_el_n2"):
+    """DG tensor prisms of mixed degree p in 1..4 through the reference's DG
+    module (apr_num_int_el of apd_dg_prism via the DG weak form); the
+    "aniso" case uses a full symmetric tensor R diag(1, 0.1, 0.01) R^T."""
+    import refmod
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, structured_prism_mesh, write_jk
+    n, seed = 2, 21
+    m = structured_prism_mesh(n, jitter=0.2, seed=seed)
+    k = lognormal_k(m.nel, seed=seed)
+    D = anisotropic_tensors(m.nel, seed=seed) if "aniso" in name else None
+    pdeg = np.random.default_rng(seed).integers(1, 5, m.nel)
+    tmp = tempfile.mkdtemp()
+    jk = os.path.join(tmp, "mesh.jk")
+    write_jk(jk, n)
+    R = refmod.RefModfem("dg")
+    R.load_jk(jk)
+    R.set_node_coords(m.coords)
+    R.init_field("t", 101)
+    if D is None:
+        R.set_coeffs(k=k, f=1.0, g=0.0)
+    else:
+        R.set_coeffs(D=D, f=1.0, g=0.0)
+    sms, rhss = [], []
+    for e in range(m.nel):
+        R.L.refh_set_el_pdeg(e + 1, int(101 * pdeg[e]))
+    for e in range(m.nel):
+        K, r, _ = R.int_ent_stiff(refmod.APC_ELEMENT, e + 1)
+        sms.append(K.reshape(-1))
+        rhss.append(r)
+    off = np.concatenate([[0], np.cumsum([x.size for x in sms])])
+    roff = np.concatenate([[0], np.cumsum([x.size for x in rhss])])
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), coords=m.coords, el_nodes=m.el_nodes, k=k,
+                        D=np.zeros(0) if D is None else D, pdeg=pdeg, sm=np.concatenate(sms), sm_off=off,
+                        rhs=np.concatenate(rhss), rhs_off=roff)
+    print(f"{name}: {m.nel} DG prisms, p counts {np.bincount(pdeg, minlength=5)[1:]}", file=sys.stderr)
+
+
 def main(argv):
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref")])
-    names = argv or list(CASES) + ["std_tet_n2"]
+    names = argv or list(CASES) + ["std_tet_n2", "dg_el_n2", "dg_el_aniso_n2"]
     if len(names) == 1 and os.environ.get("MAKE_GOLDEN_CHILD"):
         with open(os.devnull, "w") as dn:
             # the reference prints progress on stdout; keep only our stderr summary
             os.dup2(dn.fileno(), 1)
             if names[0] == "std_tet_n2":
                 run_tets(names[0])
+            elif names[0].startswith("dg_el_"):
+                run_dg_elements(names[0])
             else:
                 run_case(names[0])
         return

@@ -99,3 +99,18 @@ def test_tet_elements_bit_exact():
     for e in range(g["el_nodes"].shape[0]):
         K, r = O.std_tet_element(g["coords"][g["el_nodes"][e]], np.diag([g["k"][e]] * 3), 1.0)
         assert np.array_equal(K, g["el_sm"][e]) and np.array_equal(r, g["el_rhs"][e]), e
+
+
+@pytest.mark.parametrize("name", ["dg_el_n2", "dg_el_aniso_n2"])
+def test_dg_elements_vs_reference(name):
+    """DG tensor prisms (p = 1..4 mixed), isotropic and full-tensor coefficients."""
+    g = load(name)
+    for e in range(g["el_nodes"].shape[0]):
+        p = int(g["pdeg"][e])
+        A = g["D"][e] if g["D"].size else np.diag([g["k"][e]] * 3)
+        K, r = O.dg_prism_element(g["coords"][g["el_nodes"][e]], A, p)
+        ns = K.shape[0]
+        Kr = g["sm"][g["sm_off"][e]:g["sm_off"][e + 1]].reshape(ns, ns)
+        rr = g["rhs"][g["rhs_off"][e]:g["rhs_off"][e + 1]]
+        assert mat_rel_err(K, Kr) < 1e-14, (e, p)
+        assert vec_rel_err(r, rr) < 1e-14
