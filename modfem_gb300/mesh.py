@@ -263,3 +263,74 @@ def anisotropic_tensors(n, seed=0, eig=(1.0, 0.1, 0.01)):
     Q = random_rotations(n, seed)
     D = np.einsum("nij,j,nkj->nik", Q, np.asarray(eig, float), Q)
     return D.reshape(n, 9)
+
+
+class FaceTable:
+    """All faces of a structured prism mesh in the reference's numbering.
+
+    id (1-based), type (3 triangle, 4 quadrilateral), bc flag (> 0 boundary
+    condition, 0 / -1 interior), el1 / el2 (0-based, el2 = -1 on the
+    boundary), side1 / side2 (element sides), nodes (4 vertex indices, 0-based,
+    -1 padded) in the order of mmr_fa_node_coor (mmd_prism/
+    mms_prism_datstr.c:1488), which fixes the diagonal mmr_fa_area
+    (mms_prism_datstr.c:1732-1790) splits a quadrilateral along.
+    """
+
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+    @property
+    def n(self):
+        return self.id.size
+
+
+def prism_faces(mesh, bc=1):
+    """Full face table of structured_prism_mesh(n) (see mmr_import_mesh_grad,
+    mms_prism_input_gradmesh.c:193-330, for the numbering)."""
+    n = mesh.n
+    _, tri, nb = _tri_grid(n)
+    T = tri.shape[0]
+    nlay = mesh.nlay
+    N2 = (n + 1) ** 2
+    tri0 = tri - 1
+    rows = []
+    # horizontal faces, level by level
+    for lev in range(nlay + 1):
+        for t in range(T):
+            fid = t + 1 + lev * T
+            v = tri0[t] + lev * N2
+            if lev == 0:
+                rows.append((fid, 3, bc, t, -1, 0, 0, v[0], v[2], v[1], -1))
+            elif lev == nlay:
+                rows.append((fid, 3, bc, t + (nlay - 1) * T, -1, 1, 0, v[0], v[1], v[2], -1))
+            else:
+                rows.append((fid, 3, 0, t + (lev - 1) * T, t + lev * T, 1, 0, v[0], v[1], v[2], -1))
+    # vertical faces in creation order
+    nr_hor = T * (nlay + 1)
+    k = 0
+    for t in range(T):
+        for e in range(3):
+            g = nb[t, e]
+            if not (g < 0 or g > t + 1):
+                continue
+            a, b = tri0[t, e], tri0[t, (e + 1) % 3]
+            if g < 0:
+                el2s = None
+            else:
+                gi = g - 1
+                back = [j for j in range(3) if nb[gi, j] == t + 1][0]
+                el2s = (gi, 2 + back)
+            for lay in range(nlay):
+                fid = nr_hor + k * nlay + lay + 1
+                v = np.array([a, b, b + N2, a + N2]) + lay * N2
+                if el2s is None:
+                    rows.append((fid, 4, bc, t + lay * T, -1, 2 + e, 0, *v))
+                else:
+                    rows.append((fid, 4, -1, t + lay * T, el2s[0] + lay * T, 2 + e, el2s[1], *v))
+            k += 1
+    arr = np.array(rows, dtype=np.int64)
+    arr = arr[np.argsort(arr[:, 0], kind="stable")]
+    return FaceTable(id=arr[:, 0].astype(np.int32), type=arr[:, 1].astype(np.int32),
+                     bc=arr[:, 2].astype(np.int32), el1=arr[:, 3].astype(np.int32),
+                     el2=arr[:, 4].astype(np.int32), side1=arr[:, 5].astype(np.int32),
+                     side2=arr[:, 6].astype(np.int32), nodes=arr[:, 7:11].astype(np.int32))

@@ -579,3 +579,146 @@ int orc_dg_prism_element(const double *X, const double *A, double f, int p, doub
   }
   return ns;
 }
+
+/* ------------------------------------------------------------------ */
+/* DG prism faces                                                      */
+/* ------------------------------------------------------------------ */
+
+/* local coordinates of the six prism vertices */
+static const double PRISM_VLOC[6][3] = {{0, 0, -1}, {1, 0, -1}, {0, 1, -1}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}};
+
+/* |ds| and the outward normal on element side `side` at local point e
+   (apr_elem_calc_3D control 3 + side; the same side formulas as the std
+   prism, aps_std_util.c:770-805) */
+static double prism_side_ds(const double *X, int side, const double *e, double *nrm)
+{
+  double phi[6], dx[6], dy[6], dz[6], J[9], ds[3];
+  prism_shape(e, phi, dx, dy, dz);
+  prism_jacobian(X, dx, dy, dz, J);
+  if (side == 0) {
+    ds[0] = -J[3] * J[7] + J[6] * J[4]; ds[1] = -J[6] * J[1] + J[0] * J[7]; ds[2] = -J[0] * J[4] + J[3] * J[1];
+  } else if (side == 1) {
+    ds[0] = J[3] * J[7] - J[6] * J[4]; ds[1] = J[6] * J[1] - J[0] * J[7]; ds[2] = J[0] * J[4] - J[3] * J[1];
+  } else if (side == 2) {
+    ds[0] = J[3] * J[8] - J[6] * J[5]; ds[1] = J[6] * J[2] - J[0] * J[8]; ds[2] = J[0] * J[5] - J[3] * J[2];
+  } else if (side == 3) {
+    ds[0] = (J[4] - J[3]) * J[8] - (J[7] - J[6]) * J[5];
+    ds[1] = (J[7] - J[6]) * J[2] - (J[1] - J[0]) * J[8];
+    ds[2] = (J[1] - J[0]) * J[5] - (J[4] - J[3]) * J[2];
+  } else {
+    ds[0] = J[5] * J[7] - J[8] * J[4]; ds[1] = J[8] * J[1] - J[2] * J[7]; ds[2] = J[2] * J[4] - J[5] * J[1];
+  }
+  double d = sqrt(ds[0] * ds[0] + ds[1] * ds[1] + ds[2] * ds[2]);
+  nrm[0] = ds[0] / d; nrm[1] = ds[1] / d; nrm[2] = ds[2] / d;
+  return d;
+}
+
+/* basis values and global gradients of a DG element at local point e */
+static void dg_eval(const double *X, int p, const double *e, double *phi, double *gx, double *gy, double *gz)
+{
+  double dx[GB_DG_MAXNS], dy[GB_DG_MAXNS], dz[GB_DG_MAXNS], ph6[6], d6x[6], d6y[6], d6z[6], J[9], Ji[9];
+  int i, ns = dg_shape(p, e, phi, dx, dy, dz);
+  prism_shape(e, ph6, d6x, d6y, d6z);
+  prism_jacobian(X, d6x, d6y, d6z, J);
+  mat3_inv(J, Ji);
+  for (i = 0; i < ns; i++) {
+    gx[i] = dx[i] * Ji[0] + dy[i] * Ji[3] + dz[i] * Ji[6];
+    gy[i] = dx[i] * Ji[1] + dy[i] * Ji[4] + dz[i] * Ji[7];
+    gz[i] = dx[i] * Ji[2] + dy[i] * Ji[5] + dz[i] * Ji[8];
+  }
+}
+
+/* mmr_fa_area (mmd_prism/mms_prism_datstr.c:1732-1790) from the face vertices
+   in face order: triangle 0.5|a x b|, quadrilateral 0.5(|a x b| + |c x d|) */
+static double face_area(const double *V, int nfv)
+{
+  double a[3], b[3], e[3];
+  int i;
+  for (i = 0; i < 3; i++) { a[i] = V[3 + i] - V[i]; b[i] = V[6 + i] - V[3 + i]; }
+  e[0] = a[1] * b[2] - a[2] * b[1]; e[1] = a[2] * b[0] - a[0] * b[2]; e[2] = a[0] * b[1] - a[1] * b[0];
+  double s = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+  if (nfv == 3) return 0.5 * s;
+  double c[3], d[3], f[3];
+  for (i = 0; i < 3; i++) { c[i] = V[9 + i] - V[6 + i]; d[i] = V[i] - V[9 + i]; }
+  f[0] = c[1] * d[2] - c[2] * d[1]; f[1] = c[2] * d[0] - c[0] * d[2]; f[2] = c[0] * d[1] - c[1] * d[0];
+  return 0.5 * (s + sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]));
+}
+
+/* DG face integral of the conv-diff weak form for nreq = 1, steady
+   (implicitness 1), no convection (pdd_conv_diff/weak_formulation/approx_dg/
+   pds_conv_diff_weakform_dg.c:232-1140): interior faces give the four blocks
+   of the non-symmetric interior penalty form with the normal diffusion
+   An = A^T n of each side and penalty pen * min(p1, p2) / sqrt(face area);
+   Dirichlet faces give the boundary form with penalty pen * p1 and data g.
+   Face rule: the DG face quadrature of the side with more points
+   (apr_set_quadr_2D, aps_dg_util.c); a face point is placed in each element
+   by the weights of the face's vertices (barycentric on triangles, bilinear
+   on quadrilaterals), which is how both elements' maps restrict to the face.
+   loc1/loc2: local vertex index in each element of the face vertices in face
+   order.  sm: (ns1+ns2)^2 column-major, rhs: ns1+ns2.  Returns ns1+ns2. */
+int orc_dg_face(int ftype, const double *X1, const int *loc1, int p1, const double *A1, int side1,
+                const double *X2, const int *loc2, int p2, const double *A2, double pen, double g,
+                double *sm, double *rhs)
+{
+  int nfv = ftype == 4 ? 4 : 3, i, j, q;
+  int ns1 = GB_DG_NS[p1], ns2 = X2 ? GB_DG_NS[p2] : 0, n = ns1 + ns2;
+  int ti = ftype == 4 ? 1 : 0;
+  int pr = p1;
+  if (X2 && GB_DG_NQF[p2][ti] > GB_DG_NQF[p1][ti]) pr = p2;
+  int nq = GB_DG_NQF[pr][ti];
+  double V[12];
+  for (i = 0; i < nfv; i++) for (j = 0; j < 3; j++) V[3 * i + j] = X1[3 * loc1[i] + j];
+  double hf = sqrt(face_area(V, nfv));
+  double penalty = pen * (X2 ? (p1 < p2 ? p1 : p2) : p1);
+  memset(sm, 0, (size_t)n * n * sizeof(double));
+  memset(rhs, 0, (size_t)n * sizeof(double));
+  for (q = 0; q < nq; q++) {
+    const double *fq = GB_DG_FQ[pr - 1][ti][q];
+    double w[4];
+    if (nfv == 3) { w[0] = 1.0 - fq[0] - fq[1]; w[1] = fq[0]; w[2] = fq[1]; }
+    else {
+      double u = (fq[0] + 1.0) / 2.0, v = (fq[1] + 1.0) / 2.0;
+      w[0] = (1.0 - u) * (1.0 - v); w[1] = u * (1.0 - v); w[2] = u * v; w[3] = (1.0 - u) * v;
+    }
+    double e1[3] = {0, 0, 0}, e2[3] = {0, 0, 0};
+    for (i = 0; i < nfv; i++)
+      for (j = 0; j < 3; j++) {
+        e1[j] += w[i] * PRISM_VLOC[loc1[i]][j];
+        if (X2) e2[j] += w[i] * PRISM_VLOC[loc2[i]][j];
+      }
+    double nrm[3];
+    double area = prism_side_ds(X1, side1, e1, nrm) * fq[2];
+    double phi1[GB_DG_MAXNS], gx1[GB_DG_MAXNS], gy1[GB_DG_MAXNS], gz1[GB_DG_MAXNS], g1[GB_DG_MAXNS];
+    double phi2[GB_DG_MAXNS], gx2[GB_DG_MAXNS], gy2[GB_DG_MAXNS], gz2[GB_DG_MAXNS], g2[GB_DG_MAXNS];
+    dg_eval(X1, p1, e1, phi1, gx1, gy1, gz1);
+    double an1[3] = {A1[0] * nrm[0] + A1[3] * nrm[1] + A1[6] * nrm[2], A1[1] * nrm[0] + A1[4] * nrm[1] + A1[7] * nrm[2],
+                     A1[2] * nrm[0] + A1[5] * nrm[1] + A1[8] * nrm[2]};
+    for (i = 0; i < ns1; i++) g1[i] = an1[0] * gx1[i] + an1[1] * gy1[i] + an1[2] * gz1[i];
+    if (X2) {
+      dg_eval(X2, p2, e2, phi2, gx2, gy2, gz2);
+      double an2[3] = {A2[0] * nrm[0] + A2[3] * nrm[1] + A2[6] * nrm[2],
+                       A2[1] * nrm[0] + A2[4] * nrm[1] + A2[7] * nrm[2],
+                       A2[2] * nrm[0] + A2[5] * nrm[1] + A2[8] * nrm[2]};
+      for (i = 0; i < ns2; i++) g2[i] = an2[0] * gx2[i] + an2[1] * gy2[i] + an2[2] * gz2[i];
+      /* columns j (trial), rows i (test) */
+      for (j = 0; j < ns1; j++)
+        for (i = 0; i < ns1; i++)
+          sm[(size_t)j * n + i] += ((phi1[j] * g1[i] - phi1[i] * g1[j]) * 0.5 * 1.0 + penalty * phi1[j] * phi1[i] / hf) * area;
+      for (j = 0; j < ns2; j++)
+        for (i = 0; i < ns1; i++)
+          sm[(size_t)(ns1 + j) * n + i] += ((-phi2[j] * g1[i] - phi1[i] * g2[j]) * 0.5 * 1.0 - penalty * phi2[j] * phi1[i] / hf) * area;
+      for (j = 0; j < ns1; j++)
+        for (i = 0; i < ns2; i++)
+          sm[(size_t)j * n + ns1 + i] += ((phi1[j] * g2[i] + phi2[i] * g1[j]) * 0.5 * 1.0 - penalty * phi1[j] * phi2[i] / hf) * area;
+      for (j = 0; j < ns2; j++)
+        for (i = 0; i < ns2; i++)
+          sm[(size_t)(ns1 + j) * n + ns1 + i] += ((-phi2[j] * g2[i] + phi2[i] * g2[j]) * 0.5 * 1.0 + penalty * phi2[j] * phi2[i] / hf) * area;
+    } else {
+      for (j = 0; j < ns1; j++)
+        for (i = 0; i < ns1; i++)
+          sm[(size_t)j * n + i] += ((g1[i] * phi1[j] - g1[j] * phi1[i]) * 1.0 + penalty * phi1[j] * phi1[i] / hf) * area;
+      for (i = 0; i < ns1; i++) rhs[i] += (g1[i] * g + penalty * g * phi1[i] / hf) * area;
+    }
+  }
+  return n;
+}

@@ -67,6 +67,11 @@ int orc_dg_nshape(int p);
 int orc_dg_prism_element(const double *X /*18*/, const double *A /*9*/, double f, int p, double *sm,
                          double *rhs);
 
+/* DG face (interior: X2 != NULL; Dirichlet boundary: X2 == NULL); see oracle.c */
+int orc_dg_face(int ftype, const double *X1, const int *loc1, int p1, const double *A1, int side1,
+                const double *X2, const int *loc2, int p2, const double *A2, double pen, double g,
+                double *sm, double *rhs);
+
 #ifdef __cplusplus
 }
 #endif

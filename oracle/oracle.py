@@ -39,6 +39,7 @@ def lib():
         L.orc_std_prism_assemble.restype = cd
         L.orc_set_accumulate_abs.argtypes = [ci]
         L.orc_dg_prism_element.argtypes = [vp, vp, cd, ci, vp, vp]
+        L.orc_dg_face.argtypes = [ci, vp, vp, ci, vp, ci, vp, vp, ci, vp, cd, cd, vp, vp]
         L.orc_crs_residual.argtypes = [ci, vp, vp, vp, ci, vp, vp, vp]
         L.orc_gmres_jacobi.argtypes = [ci, vp, vp, vp, vp, vp, ci, ci, cd, vp, vp]
         _L = L
@@ -88,6 +89,36 @@ def dg_prism_element(X, A, p, f=1.0):
     rhs = np.zeros(ns)
     lib().orc_dg_prism_element(_p(X), _p(A), f, p, _p(sm), _p(rhs))
     return sm.reshape(ns, ns).T.copy(), rhs
+
+
+def face_local_vertices(el_nodes_e, face_nodes):
+    """Local vertex index in an element of each face vertex (face order)."""
+    return np.array([int(np.nonzero(el_nodes_e == v)[0][0]) for v in face_nodes if v >= 0], np.int32)
+
+
+def dg_face(mesh, faces, i, pdeg, A, pen=10.0, g=0.0):
+    """DG face matrix ((ns1+ns2)^2 as (row, column)) and rhs of face i of a
+    FaceTable; A: (nel, 9) coefficient tensors; pdeg per element."""
+    e1, e2 = int(faces.el1[i]), int(faces.el2[i])
+    fn = faces.nodes[i]
+    X1 = _c(mesh.coords[mesh.el_nodes[e1]], np.float64).reshape(-1)
+    l1 = face_local_vertices(mesh.el_nodes[e1], fn)
+    A1 = _c(A[e1], np.float64)
+    p1 = int(pdeg[e1])
+    n = lib().orc_dg_nshape(p1)
+    X2 = l2 = A2 = None
+    p2 = 1
+    if e2 >= 0:
+        X2 = _c(mesh.coords[mesh.el_nodes[e2]], np.float64).reshape(-1)
+        l2 = face_local_vertices(mesh.el_nodes[e2], fn)
+        A2 = _c(A[e2], np.float64)
+        p2 = int(pdeg[e2])
+        n += lib().orc_dg_nshape(p2)
+    sm = np.zeros(n * n)
+    rhs = np.zeros(n)
+    lib().orc_dg_face(int(faces.type[i]), _p(X1), _p(l1), p1, _p(A1), int(faces.side1[i]), _p(X2), _p(l2), p2,
+                      _p(A2), pen, g, _p(sm), _p(rhs))
+    return sm.reshape(n, n).T.copy(), rhs
 
 
 def dof_order(el_nodes, nno):

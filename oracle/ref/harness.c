@@ -814,3 +814,29 @@ int refh_set_el_pdeg(int el, int pdeg)
   return apr_set_ent_pdeg(h_field_id, APC_ELEMENT, el, pdeg);
 }
 #endif
+
+/* Every active face in mmr order: out[10*i ..] = id, type, bc, neig1, neig2
+   (signed, 0 = boundary), side1, side2, then up to 4 vertex ids in
+   mmr_fa_node_coor order (padded with 0); returns the count. */
+int refh_all_faces(int *out)
+{
+  int nfa = 0, cnt = 0;
+  while ((nfa = mmr_get_next_face_all(h_mesh_id, nfa)) != 0) {
+    if (mmr_fa_status(h_mesh_id, nfa) != MMC_ACTIVE) continue;
+    if (out) {
+      int neig[2] = {0, 0}, sides[2] = {0, 0}, shift = 0, gen = 0, nodes[MMC_MAXFAVNO + 1], j;
+      double ac[4], bc[2];
+      mmr_fa_neig(h_mesh_id, nfa, neig, sides, &shift, &gen, ac, bc);
+      mmr_fa_node_coor(h_mesh_id, nfa, nodes, NULL);
+      int *o = out + 10 * cnt;
+      o[0] = nfa; o[1] = mmr_fa_type(h_mesh_id, nfa); o[2] = mmr_fa_bc(h_mesh_id, nfa);
+      o[3] = neig[0]; o[4] = neig[1]; o[5] = sides[0]; o[6] = sides[1];
+      for (j = 0; j < 4; j++) o[6 + j] = 0;
+      for (j = 0; j < nodes[0] && j < 3; j++) o[7 + j] = nodes[j + 1];
+      /* the fourth vertex of a quad does not fit: store it in slot 6 after sides */
+      if (nodes[0] == 4) { o[6] = sides[1] * 1000 + nodes[4]; }
+    }
+    cnt++;
+  }
+  return cnt;
+}

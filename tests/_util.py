@@ -102,3 +102,20 @@ def energy_scale(row_ptr, col_ind, b):
     isd = rows == col_ind
     diag[rows[isd]] = np.abs(b[isd])
     return np.sqrt(diag[rows] * diag[col_ind])
+
+
+def face_rel_err(a, b):
+    """Non-symmetric local matrices (DG face blocks): max |a_ij - b_ij| /
+    sqrt(R_i C_j) with R_i, C_j the largest magnitudes of row i and column j
+    of b (the scale of the dot products entry (i, j) sums).  Functions that
+    vanish on the face make some diagonals zero, so the energy scale of
+    mat_rel_err does not apply; rows and columns that are zero in b must be
+    zero in a."""
+    R = np.abs(b).max(axis=1)
+    C = np.abs(b).max(axis=0)
+    den = np.sqrt(np.outer(R, C))
+    err = np.abs(a - b)
+    ok = den > 0
+    if np.any(err[~ok] != 0):
+        return float("inf")
+    return float(np.max(err[ok] / den[ok])) if np.any(ok) else 0.0

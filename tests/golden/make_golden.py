@@ -114,6 +114,10 @@ def run_tets(name="std_tet_n2"):
     print(f"{name}: {m.nel} tets", file=sys.stderr)
 
 
+# Dirichlet value on the DG boundary faces (enters the face load vectors)
+DG_G = 0.3
+
+
 def run_dg_elements(name="dg_el_n2"):
     """DG tensor prisms of mixed degree p in 1..4 through the reference's DG
     module (apr_num_int_el of apd_dg_prism via the DG weak form); the
@@ -133,9 +137,10 @@ def run_dg_elements(name="dg_el_n2"):
     R.set_node_coords(m.coords)
     R.init_field("t", 101)
     if D is None:
-        R.set_coeffs(k=k, f=1.0, g=0.0)
+        R.set_coeffs(k=k, f=1.0, g=DG_G)
     else:
-        R.set_coeffs(D=D, f=1.0, g=0.0)
+        R.set_coeffs(D=D, f=1.0, g=DG_G)
+    R.set_dg_penalty(10.0)
     sms, rhss = [], []
     for e in range(m.nel):
         R.L.refh_set_el_pdeg(e + 1, int(101 * pdeg[e]))
@@ -145,9 +150,20 @@ def run_dg_elements(name="dg_el_n2"):
         rhss.append(r)
     off = np.concatenate([[0], np.cumsum([x.size for x in sms])])
     roff = np.concatenate([[0], np.cumsum([x.size for x in rhss])])
+    # every face (interior and Dirichlet boundary), in mmr face order
+    from modfem_gb300.mesh import prism_faces
+    F = prism_faces(m)
+    fsm, frhs = [], []
+    for fid in F.id:
+        K, r, _ = R.int_ent_stiff(refmod.APC_FACE, int(fid), maxn=200)
+        fsm.append(K.reshape(-1))
+        frhs.append(r)
+    foff = np.concatenate([[0], np.cumsum([x.size for x in fsm])])
+    froff = np.concatenate([[0], np.cumsum([x.size for x in frhs])])
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), coords=m.coords, el_nodes=m.el_nodes, k=k,
                         D=np.zeros(0) if D is None else D, pdeg=pdeg, sm=np.concatenate(sms), sm_off=off,
-                        rhs=np.concatenate(rhss), rhs_off=roff)
+                        rhs=np.concatenate(rhss), rhs_off=roff, fa_sm=np.concatenate(fsm), fa_sm_off=foff,
+                        fa_rhs=np.concatenate(frhs), fa_rhs_off=froff, pen=10.0, g=DG_G)
     print(f"{name}: {m.nel} DG prisms, p counts {np.bincount(pdeg, minlength=5)[1:]}", file=sys.stderr)
 
 

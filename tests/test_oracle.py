@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from _util import FixtureMesh, REL_TOL, crs_rel_err, load, mat_rel_err, vec_rel_err
+from _util import FixtureMesh, REL_TOL, crs_rel_err, face_rel_err, load, mat_rel_err, vec_rel_err
 
 
 @pytest.fixture(scope="module", params=["std_n4", "std_n10", "std_n3_flat"])
@@ -114,3 +114,23 @@ def test_dg_elements_vs_reference(name):
         rr = g["rhs"][g["rhs_off"][e]:g["rhs_off"][e + 1]]
         assert mat_rel_err(K, Kr) < 1e-14, (e, p)
         assert vec_rel_err(r, rr) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["dg_el_n2", "dg_el_aniso_n2"])
+def test_dg_faces_vs_reference(name):
+    """DG faces: interior-penalty coupling of both neighbours (interior faces)
+    and the Dirichlet boundary form, every face of the mixed-p mesh."""
+    from modfem_gb300.mesh import prism_faces, structured_prism_mesh
+    g = load(name)
+    m = structured_prism_mesh(2, jitter=0.2, seed=21)
+    assert np.array_equal(m.coords, g["coords"]) and np.array_equal(m.el_nodes, g["el_nodes"])
+    F = prism_faces(m)
+    A = g["D"] if g["D"].size else np.array([np.diag([k] * 3).reshape(-1) for k in g["k"]])
+    assert F.n == g["fa_sm_off"].size - 1
+    for i in range(F.n):
+        K, r = O.dg_face(m, F, i, g["pdeg"], A, pen=float(g["pen"]), g=float(g["g"]))
+        n = K.shape[0]
+        Kr = g["fa_sm"][g["fa_sm_off"][i]:g["fa_sm_off"][i + 1]].reshape(n, n)
+        rr = g["fa_rhs"][g["fa_rhs_off"][i]:g["fa_rhs_off"][i + 1]]
+        assert face_rel_err(K, Kr) < 1e-14, (i, int(F.type[i]), int(F.el2[i]))
+        assert vec_rel_err(r, rr) < 1e-14 if np.any(rr) else not np.any(r), i
