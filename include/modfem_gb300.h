@@ -144,18 +144,56 @@ int gbfem_set_matrix(gbfem_ctx ctx, const double *crs_val, const double *rhs);
  * apd_dg_prism/aps_dg_prism_intf.c:725-775).  The mesh must be prisms;
  * coefficients from gbfem_set_coefficients (a tensor must be symmetric). */
 int gbfem_dg_set_degrees(gbfem_ctx ctx, const int *p_el);
-/* Block-CRS structure of the DG matrix: one dof block per element in element
- * order (the reference's DG dof entities, utd_util/uts_ls_intf.c:640-700),
- * dense blocks ns_r x ns_c column-major.  Returns the dof count and the
- * number of stored values. */
+/* Face table of the mesh, the data the DG weak form reads per face through
+ * mmr_fa_type (mmd_prism/mms_prism_datstr.c:969), mmr_fa_bc (:993),
+ * mmr_fa_eq_neig (:1140) and mmr_fa_node_coor (:1488): type 3 (triangle) or
+ * 4 (quadrilateral); bc flag; two neighbours per face (0-based, second -1 on
+ * the boundary, where the flag must be Dirichlet, 0 < bc < 10); the side of
+ * the first neighbour the face lies on (0 bottom, 1 top, 2..4 lateral over
+ * triangle edge 0..2; the normal points out of that element); four vertex
+ * indices per face in mmr_fa_node_coor order (fourth -1 on triangles).
+ * Without a face table only volume terms are assembled. */
+int gbfem_dg_set_faces(gbfem_ctx ctx, int nfa, const int *fa_type, const int *fa_bc, const int *fa_el,
+                       const int *fa_side, const int *fa_nodes);
+/* Interior-penalty factor, pdr_ctrl_d_params(problem, 12) in the DG weak
+ * form (pds_conv_diff_weakform_dg.c:516-531); default 10. */
+int gbfem_dg_set_penalty(gbfem_ctx ctx, double penalty);
+/* Block-CRS structure of the DG matrix (the device form of the reference's
+ * lad_block storage, lsd_mkb/lad_block/lah_block.h): one dof block per
+ * element in element order (the reference's DG dof entities,
+ * utd_util/uts_ls_intf.c:640-700); block row e holds the element and its
+ * face neighbours in ascending order; dense blocks ns_r x ns_c, column-major
+ * with leading dimension ns_r (Dia / Aux of las_block_intf.c:362-520).
+ * Returns the dof count and the number of stored values. */
 int gbfem_dg_build_structure(gbfem_ctx ctx, int *ndof, long long *nval);
 /* dof_off[nel+1] first dof of each element; bptr[nel+1], bcol[nblk] block
  * rows/columns; boff[nblk+1] value offsets.  Returns nblk. */
 int gbfem_dg_get_structure(gbfem_ctx ctx, int *dof_off, int *bptr, int *bcol, long long *boff);
 /* Integrates all elements (apr_num_int_el of apd_dg_prism,
- * aps_dg_prism_intf.c:1239-1728) into their diagonal blocks and the rhs. */
+ * aps_dg_prism_intf.c:1239-1728) and all faces of the face table
+ * (pdr_conv_diff_comp_fa_stiff_mat_app, pds_conv_diff_weakform_dg.c:
+ * 232-1140: interior penalty on interior faces, the Dirichlet form with the
+ * value g of gbfem_set_coefficients on boundary faces) into the block matrix
+ * and the rhs, each block entry written by one thread in a fixed order. */
 int gbfem_dg_assemble(gbfem_ctx ctx);
+/* Times (ms) of the last gbfem_dg_assemble: total, volume and face kernels. */
+int gbfem_dg_last_timing(gbfem_ctx ctx, double *total_ms, double *volume_ms, double *face_ms, int *launches);
 int gbfem_dg_get_matrix(gbfem_ctx ctx, double *vals, double *rhs);
+int gbfem_dg_set_matrix(gbfem_ctx ctx, const double *vals, const double *rhs);
+/* lar_compute_residual for the block storage (lar_compute_residual_block,
+ * lsd_mkb/lad_block/las_block_intf.c:2266): V = (Use_rhs ? B : 0) - A*X,
+ * host arrays of Ndof entries in dof-block order (B NULL: the assembled rhs). */
+int gbfem_dg_compute_residual(gbfem_ctx ctx, int Use_rhs, int Ini_zero, int Ndof, const double *X,
+                              const double *B, double *V);
+/* GMRES(krylov) on the DG matrix (lsr_mkb_core_gmres, lsd_mkb/lsd_mkb_core/
+ * lss_mkb_core.c:2317) with the reference's block Jacobi preconditioner for
+ * block storage (the inverse of every diagonal block,
+ * lar_fill_preconditioner_block, las_block_intf.c:1224-1330), stopping on
+ * the preconditioned residual relative to the initial one (floors 1e-12).
+ * x: host array of ndof (initial guess unless ini_zero; solution on return).
+ * Returns the iteration count. */
+int gbfem_dg_solve(gbfem_ctx ctx, int krylov, int max_iter, double tol_rel, int ini_zero, double *x,
+                   double *res, double *res_rel);
 
 /* Drop-in for lar_compute_residual (lsd_mkb/las_intf.c:771,
  * lad_crs/las_crs_intf.c:788-856): V = (Use_rhs ? B : 0) - A*X, X, B, V host

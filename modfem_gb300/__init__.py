@@ -42,10 +42,16 @@ SIGNATURES = [
     ("gbfem_get_matrix", _ci, [_vp, _vp, _vp]),
     ("gbfem_set_matrix", _ci, [_vp, _vp, _vp]),
     ("gbfem_dg_set_degrees", _ci, [_vp, _vp]),
+    ("gbfem_dg_set_faces", _ci, [_vp, _ci, _vp, _vp, _vp, _vp, _vp]),
+    ("gbfem_dg_set_penalty", _ci, [_vp, _cd]),
     ("gbfem_dg_build_structure", _ci, [_vp, _pi, _pll]),
     ("gbfem_dg_get_structure", _ci, [_vp, _vp, _vp, _vp, _vp]),
     ("gbfem_dg_assemble", _ci, [_vp]),
+    ("gbfem_dg_last_timing", _ci, [_vp, _pd, _pd, _pd, _pi]),
     ("gbfem_dg_get_matrix", _ci, [_vp, _vp, _vp]),
+    ("gbfem_dg_set_matrix", _ci, [_vp, _vp, _vp]),
+    ("gbfem_dg_compute_residual", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
+    ("gbfem_dg_solve", _ci, [_vp, _ci, _ci, _cd, _ci, _vp, _pd, _pd]),
     ("gbfem_compute_residual", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
     ("gbfem_compute_residual_noalloc", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
     ("gbfem_solve", _ci, [_vp, _ci, _ci, _cd, _ci, _vp, _pd, _pd]),
@@ -190,6 +196,19 @@ class Context:
         self._keep["dgp"] = p
         self._check(self.L.gbfem_dg_set_degrees(self._h, _p(p)))
 
+    def dg_set_faces(self, faces, penalty=None):
+        """faces: a FaceTable (modfem_gb300.mesh.prism_faces) or any object with
+        type, bc, el1, el2, side1 and nodes (n x 4) arrays."""
+        t = _i32(faces.type)
+        bc = _i32(faces.bc)
+        el = _i32(np.stack([faces.el1, faces.el2], axis=1))
+        sd = _i32(faces.side1)
+        nd = _i32(faces.nodes)
+        self._keep["dgfaces"] = (t, bc, el, sd, nd)
+        self._check(self.L.gbfem_dg_set_faces(self._h, t.size, _p(t), _p(bc), _p(el), _p(sd), _p(nd)))
+        if penalty is not None:
+            self._check(self.L.gbfem_dg_set_penalty(self._h, float(penalty)))
+
     def dg_build_structure(self):
         nd, nv = ctypes.c_int(), ctypes.c_longlong()
         self._check(self.L.gbfem_dg_build_structure(self._h, ctypes.byref(nd), ctypes.byref(nv)))
@@ -213,6 +232,31 @@ class Context:
         rhs = np.zeros(self.dg_ndof)
         self._check(self.L.gbfem_dg_get_matrix(self._h, _p(vals), _p(rhs)))
         return vals, rhs
+
+    def dg_set_matrix(self, vals=None, rhs=None):
+        self._check(self.L.gbfem_dg_set_matrix(self._h, _p(_f64(vals)), _p(_f64(rhs))))
+
+    def dg_last_timing(self):
+        """(total ms, volume-kernel ms, face-kernel ms, launches) of the last DG assembly."""
+        t, v, f, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        self._check(self.L.gbfem_dg_last_timing(self._h, ctypes.byref(t), ctypes.byref(v), ctypes.byref(f),
+                                                ctypes.byref(n)))
+        return t.value, v.value, f.value, n.value
+
+    def dg_compute_residual(self, x, b=None, use_rhs=1, ini_zero=0):
+        x = _f64(x)
+        b = _f64(b)
+        v = np.zeros(self.dg_ndof)
+        self._check(self.L.gbfem_dg_compute_residual(self._h, use_rhs, ini_zero, self.dg_ndof, _p(x), _p(b),
+                                                     _p(v)))
+        return v
+
+    def dg_solve(self, krylov=50, max_iter=1000, tol_rel=1e-8, x0=None):
+        x = np.zeros(self.dg_ndof) if x0 is None else np.array(x0, dtype=np.float64)
+        res, rel = ctypes.c_double(), ctypes.c_double()
+        it = self._check(self.L.gbfem_dg_solve(self._h, krylov, max_iter, tol_rel, 1 if x0 is None else 0, _p(x),
+                                               ctypes.byref(res), ctypes.byref(rel)))
+        return x, it, res.value, rel.value
 
     def assemble(self, mode=SCATTER_ATOMIC):
         self._check(self.L.gbfem_assemble(self._h, mode))

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <mutex>
 
 #include "gbfem_internal.h"
@@ -74,6 +75,14 @@ int gbfem_destroy(gbfem_ctx c) {
   c->dg_boff_diag_d.release();
   c->dg_val.release();
   c->dg_rhs.release();
+  c->dg_hf_ptr.release();
+  c->dg_p_d.release();
+  c->dg_hf.release();
+  c->dg_dinv.release();
+  c->dg_dinv_off_d.release();
+  c->dg_bptr_d.release();
+  c->dg_bcol_d.release();
+  c->dg_boff_d.release();
   cudaEventDestroy(c->ev0);
   cudaEventDestroy(c->ev1);
   cudaEventDestroy(c->ev2);
@@ -93,6 +102,10 @@ long long gbfem_device_bytes(gbfem_ctx c) {
                                 &c->dof_of_node, &c->el_table, &c->el_perm, &c->fa_perm, &c->fa_map,
                                 &c->err, &c->in_id, &c->in_pos, &c->in_table};
   for (auto *b : ibufs) s += b->bytes();
+  s += c->dg_val.bytes() + c->dg_rhs.bytes() + c->dg_dinv.bytes() + c->dg_hf.bytes() + c->dg_boff_d.bytes() +
+       c->dg_boff_diag_d.bytes() + c->dg_dinv_off_d.bytes() + c->dg_bptr_d.bytes() + c->dg_bcol_d.bytes() +
+       c->dg_hf_ptr.bytes() + c->dg_p_d.bytes() + c->dg_roff_d.bytes();
+  for (int p = 0; p < 5; p++) s += c->dg_list[p].bytes();
   return s;
 }
 
@@ -435,28 +448,139 @@ int gbfem_dg_set_degrees(gbfem_ctx c, const int *p_el) {
   return 0;
 }
 
+int gbfem_dg_set_faces(gbfem_ctx c, int nfa, const int *fa_type, const int *fa_bc, const int *fa_el,
+                       const int *fa_side, const int *fa_nodes) {
+  GB_CHECK(c && c->nel > 0 && c->nv == GBFEM_PRISM, "DG needs a prism mesh (gbfem_set_mesh)");
+  GB_CHECK(nfa >= 0, "negative face count");
+  GB_CHECK(nfa == 0 || (fa_type && fa_bc && fa_el && fa_side && fa_nodes), "face arrays missing");
+  const int nel = c->nel;
+  const int *en = c->h_el_nodes.data();
+  for (int f = 0; f < nfa; f++) {
+    const int t = fa_type[f], e1 = fa_el[2 * f], e2 = fa_el[2 * f + 1], sd = fa_side[f];
+    GB_CHECK(t == 3 || t == 4, "face type must be 3 (triangle) or 4 (quadrilateral)");
+    GB_CHECK(e1 >= 0 && e1 < nel, "face neighbour out of range");
+    GB_CHECK(e2 == -1 || (e2 >= 0 && e2 < nel && e2 != e1), "second face neighbour out of range");
+    GB_CHECK(sd >= 0 && sd <= 4 && (sd < 2) == (t == 3), "face side does not match the face type");
+    GB_CHECK(e2 >= 0 || (fa_bc[f] > 0 && fa_bc[f] < 10),
+             "boundary faces must carry a Dirichlet flag (0 < bc < 10)");
+    for (int i = 0; i < t; i++) {
+      const int v = fa_nodes[4 * f + i];
+      bool in1 = false, in2 = e2 < 0;
+      for (int k = 0; k < 6; k++) {
+        in1 = in1 || en[6 * (size_t)e1 + k] == v;
+        if (e2 >= 0) in2 = in2 || en[6 * (size_t)e2 + k] == v;
+      }
+      GB_CHECK(in1 && in2, "face vertex is not a vertex of its neighbours");
+    }
+  }
+  c->dg_nfa = nfa;
+  c->dg_fa_type.assign(fa_type, fa_type + nfa);
+  c->dg_fa_bc.assign(fa_bc, fa_bc + nfa);
+  c->dg_fa_el.assign(fa_el, fa_el + 2 * (size_t)nfa);
+  c->dg_fa_side.assign(fa_side, fa_side + nfa);
+  c->dg_fa_nodes.assign(fa_nodes, fa_nodes + 4 * (size_t)nfa);
+  c->dg_ready = false;
+  return 0;
+}
+
+int gbfem_dg_set_penalty(gbfem_ctx c, double pen) {
+  GB_CHECK(c, "null context");
+  GB_CHECK(pen > 0.0, "penalty must be positive");
+  c->dg_pen = pen;
+  return 0;
+}
+
 static const int kDgNs[5] = {0, 6, 18, 40, 75};
 
 int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   GB_CHECK(c && !c->dg_p.empty(), "DG degrees not set (gbfem_dg_set_degrees)");
   GB_CUDA(cudaSetDevice(c->device));
   const int nel = c->nel;
+  const int nfa = c->dg_nfa < 0 ? 0 : c->dg_nfa;
   // dof blocks in element order (utr_get_list_ent, DG branch: one dof entity
-  // per element, uts_ls_intf.c:640-700); block rows hold the element itself
+  // per element, uts_ls_intf.c:640-700)
   c->dg_roff.assign(nel + 1, 0);
   for (int e = 0; e < nel; e++) c->dg_roff[e + 1] = c->dg_roff[e] + kDgNs[c->dg_p[e]];
   c->dg_ndof = c->dg_roff[nel];
-  c->dg_bptr.assign(nel + 1, 0);
-  c->dg_bcol.assign(nel, 0);
-  c->dg_boff.assign(nel + 1, 0);
-  std::vector<long long> diag(nel);
-  for (int e = 0; e < nel; e++) {
-    c->dg_bptr[e + 1] = e + 1;
-    c->dg_bcol[e] = e;
-    diag[e] = c->dg_boff[e];
-    c->dg_boff[e + 1] = c->dg_boff[e] + (long long)kDgNs[c->dg_p[e]] * kDgNs[c->dg_p[e]];
+  // block row e: the element and its face neighbours, ascending (the sorted
+  // neighbour lists of sir_create, sis_mkb_intf.c:1100-1146)
+  std::vector<int> cnt(nel + 1, 1);
+  for (int f = 0; f < nfa; f++) {
+    const int e1 = c->dg_fa_el[2 * f], e2 = c->dg_fa_el[2 * f + 1];
+    if (e2 >= 0) {
+      cnt[e1]++;
+      cnt[e2]++;
+    }
   }
-  c->dg_nval = c->dg_boff[nel];
+  c->dg_bptr.assign(nel + 1, 0);
+  for (int e = 0; e < nel; e++) c->dg_bptr[e + 1] = c->dg_bptr[e] + cnt[e];
+  c->dg_bcol.assign(c->dg_bptr[nel], 0);
+  std::vector<int> fill(c->dg_bptr.begin(), c->dg_bptr.end() - 1);
+  for (int e = 0; e < nel; e++) c->dg_bcol[fill[e]++] = e;
+  for (int f = 0; f < nfa; f++) {
+    const int e1 = c->dg_fa_el[2 * f], e2 = c->dg_fa_el[2 * f + 1];
+    if (e2 >= 0) {
+      c->dg_bcol[fill[e1]++] = e2;
+      c->dg_bcol[fill[e2]++] = e1;
+    }
+  }
+  for (int e = 0; e < nel; e++) {
+    auto b0 = c->dg_bcol.begin() + c->dg_bptr[e], b1 = c->dg_bcol.begin() + c->dg_bptr[e + 1];
+    std::sort(b0, b1);
+    GB_CHECK(std::adjacent_find(b0, b1) == b1, "two faces join the same pair of elements");
+  }
+  const int nblk = c->dg_bptr[nel];
+  c->dg_boff.assign(nblk + 1, 0);
+  std::vector<long long> diag(nel), dinv_off(nel + 1, 0);
+  for (int e = 0; e < nel; e++) {
+    const long long ne = kDgNs[c->dg_p[e]];
+    for (int k = c->dg_bptr[e]; k < c->dg_bptr[e + 1]; k++) {
+      const int col = c->dg_bcol[k];
+      if (col == e) diag[e] = c->dg_boff[k];
+      c->dg_boff[k + 1] = c->dg_boff[k] + ne * kDgNs[c->dg_p[col]];
+    }
+    dinv_off[e + 1] = dinv_off[e] + ne * ne;
+  }
+  c->dg_nval = c->dg_boff[nblk];
+  auto block_of = [&](int row, int col) -> long long {
+    auto b0 = c->dg_bcol.begin() + c->dg_bptr[row], b1 = c->dg_bcol.begin() + c->dg_bptr[row + 1];
+    return c->dg_boff[std::lower_bound(b0, b1, col) - c->dg_bcol.begin()];
+  };
+  // face incidences per owner, faces in table order (the reference integrates
+  // faces in face order after the elements)
+  std::vector<int> hcnt(nel + 1, 0);
+  for (int f = 0; f < nfa; f++) {
+    hcnt[c->dg_fa_el[2 * f]]++;
+    if (c->dg_fa_el[2 * f + 1] >= 0) hcnt[c->dg_fa_el[2 * f + 1]]++;
+  }
+  std::vector<int> hptr(nel + 1, 0);
+  for (int e = 0; e < nel; e++) hptr[e + 1] = hptr[e] + hcnt[e];
+  std::vector<gbfem::DgHalfFace> hf(hptr[nel]);
+  std::vector<int> hfill(hptr.begin(), hptr.end() - 1);
+  const int *en = c->h_el_nodes.data();
+  for (int f = 0; f < nfa; f++) {
+    gbfem::DgHalfFace h;
+    memset(&h, 0, sizeof(h));
+    h.el1 = c->dg_fa_el[2 * f];
+    h.el2 = c->dg_fa_el[2 * f + 1];
+    h.side1 = c->dg_fa_side[f];
+    h.nfv = c->dg_fa_type[f];
+    for (int i = 0; i < h.nfv; i++) {
+      const int v = c->dg_fa_nodes[4 * f + i];
+      for (int k = 0; k < 6; k++) {
+        if (en[6 * (size_t)h.el1 + k] == v) h.loc1[i] = (unsigned char)k;
+        if (h.el2 >= 0 && en[6 * (size_t)h.el2 + k] == v) h.loc2[i] = (unsigned char)k;
+      }
+    }
+    h.owner_is_2 = 0;
+    h.blk = h.el2 >= 0 ? block_of(h.el1, h.el2) : -1;
+    hf[hfill[h.el1]++] = h;
+    if (h.el2 >= 0) {
+      h.owner_is_2 = 1;
+      h.blk = block_of(h.el2, h.el1);
+      hf[hfill[h.el2]++] = h;
+    }
+  }
   for (int p = 1; p <= 4; p++) {
     std::vector<int> lst;
     for (int e = 0; e < nel; e++)
@@ -469,6 +593,17 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   }
   GB_TRY(upload(c, c->dg_roff_d, c->dg_roff.data(), c->dg_roff.size()));
   GB_TRY(upload(c, c->dg_boff_diag_d, diag.data(), diag.size()));
+  GB_TRY(upload(c, c->dg_p_d, c->dg_p.data(), c->dg_p.size()));
+  GB_TRY(upload(c, c->dg_hf_ptr, hptr.data(), hptr.size()));
+  if (!hf.empty())
+    GB_TRY(upload(c, c->dg_hf, hf.data(), hf.size()));
+  else
+    c->dg_hf.release();
+  GB_TRY(upload(c, c->dg_bptr_d, c->dg_bptr.data(), c->dg_bptr.size()));
+  GB_TRY(upload(c, c->dg_bcol_d, c->dg_bcol.data(), c->dg_bcol.size()));
+  GB_TRY(upload(c, c->dg_boff_d, c->dg_boff.data(), c->dg_boff.size()));
+  GB_TRY(upload(c, c->dg_dinv_off_d, dinv_off.data(), dinv_off.size()));
+  c->dg_ninv = dinv_off[nel];
   GB_TRY(c->dg_val.alloc((size_t)c->dg_nval));
   GB_TRY(c->dg_rhs.alloc((size_t)c->dg_ndof));
   GB_CUDA(cudaStreamSynchronize(c->stream));
@@ -490,11 +625,10 @@ int gbfem_dg_get_structure(gbfem_ctx c, int *dof_off, int *bptr, int *bcol, long
 int gbfem_dg_assemble(gbfem_ctx c) {
   GB_CHECK(c && c->dg_ready, "DG structure not built (gbfem_dg_build_structure)");
   GB_CUDA(cudaSetDevice(c->device));
-  cudaEventRecord(c->ev0, c->stream);
-  GB_CUDA(cudaMemsetAsync(c->dg_val.p, 0, c->dg_val.bytes(), c->stream));
-  GB_CUDA(cudaMemsetAsync(c->dg_rhs.p, 0, c->dg_rhs.bytes(), c->stream));
   int launches = 0;
-  cudaEventRecord(c->ev2, c->stream);
+  // volume terms write every diagonal block and the rhs; the face kernel then
+  // adds to those and writes every off-diagonal block: nothing to clear
+  cudaEventRecord(c->ev0, c->stream);
   for (int p = 1; p <= 4; p++) {
     if (!c->dg_list[p].p) continue;
     int r = gbfem::launch_dg_prism_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
@@ -503,12 +637,33 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     GB_TRY(r);
     launches += r;
   }
-  cudaEventRecord(c->ev3, c->stream);
+  cudaEventRecord(c->ev2, c->stream);
+  if (c->dg_hf.p) {
+    for (int p = 1; p <= 4; p++) {
+      if (!c->dg_list[p].p) continue;
+      int r = gbfem::launch_dg_prism_faces(c->stream, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->dg_hf_ptr.p,
+                                           c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
+                                           c->dg_pen, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,
+                                           c->dg_rhs.p);
+      GB_TRY(r);
+      launches += r;
+    }
+  }
   cudaEventRecord(c->ev1, c->stream);
   GB_CUDA(cudaEventSynchronize(c->ev1));
   cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
-  cudaEventElapsedTime(&c->last_el_ms, c->ev2, c->ev3);
+  cudaEventElapsedTime(&c->last_el_ms, c->ev0, c->ev2);
+  cudaEventElapsedTime(&c->last_fa_ms, c->ev2, c->ev1);
   c->last_launches = launches;
+  return 0;
+}
+
+int gbfem_dg_last_timing(gbfem_ctx c, double *total_ms, double *volume_ms, double *face_ms, int *launches) {
+  GB_CHECK(c, "null context");
+  if (total_ms) *total_ms = c->last_ms;
+  if (volume_ms) *volume_ms = c->last_el_ms;
+  if (face_ms) *face_ms = c->last_fa_ms;
+  if (launches) *launches = c->last_launches;
   return 0;
 }
 
@@ -516,6 +671,44 @@ int gbfem_dg_get_matrix(gbfem_ctx c, double *vals, double *rhs) {
   GB_CHECK(c && c->dg_ready, "DG structure not built");
   if (vals) GB_CUDA(cudaMemcpyAsync(vals, c->dg_val.p, c->dg_val.bytes(), cudaMemcpyDeviceToHost, c->stream));
   if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->dg_rhs.p, c->dg_rhs.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int gbfem_dg_set_matrix(gbfem_ctx c, const double *vals, const double *rhs) {
+  GB_CHECK(c && c->dg_ready, "DG structure not built");
+  if (vals) GB_CUDA(cudaMemcpyAsync(c->dg_val.p, vals, c->dg_val.bytes(), cudaMemcpyHostToDevice, c->stream));
+  if (rhs) GB_CUDA(cudaMemcpyAsync(c->dg_rhs.p, rhs, c->dg_rhs.bytes(), cudaMemcpyHostToDevice, c->stream));
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int gbfem_dg_compute_residual(gbfem_ctx c, int Use_rhs, int Ini_zero, int Ndof, const double *X, const double *B,
+                              double *V) {
+  GB_CHECK(c && c->dg_ready, "DG structure not built");
+  GB_CHECK(Ndof == c->dg_ndof, "Ndof differs from the matrix size");
+  GB_CHECK(V != nullptr, "null output vector");
+  GB_CUDA(cudaSetDevice(c->device));
+  const size_t nb = (size_t)Ndof * sizeof(double);
+  GB_TRY(c->x.alloc(Ndof));
+  GB_TRY(c->tmp.alloc(Ndof));
+  if (Ini_zero || X == nullptr)
+    GB_CUDA(cudaMemsetAsync(c->x.p, 0, nb, c->stream));
+  else
+    GB_CUDA(cudaMemcpyAsync(c->x.p, X, nb, cudaMemcpyHostToDevice, c->stream));
+  const double *bd = nullptr;
+  if (Use_rhs) {
+    if (B) {
+      GB_TRY(c->b.alloc(Ndof));
+      GB_CUDA(cudaMemcpyAsync(c->b.p, B, nb, cudaMemcpyHostToDevice, c->stream));
+      bd = c->b.p;
+    } else {
+      bd = c->dg_rhs.p;
+    }
+  }
+  GB_TRY(gbfem::launch_dg_block_spmv(c->stream, 2, c->nel, c->dg_roff_d.p, c->dg_bptr_d.p, c->dg_bcol_d.p,
+                                     c->dg_boff_d.p, c->dg_val.p, nullptr, nullptr, c->x.p, bd, c->tmp.p));
+  GB_CUDA(cudaMemcpyAsync(V, c->tmp.p, nb, cudaMemcpyDeviceToHost, c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
 }
@@ -606,27 +799,36 @@ int gbfem_compute_residual(gbfem_ctx c, int Use_rhs, int Ini_zero, int Ndof, con
   return 0;
 }
 
-// Restarted GMRES(m) on the device-resident matrix (lss_mkb_core.c:2317-2660).
-// Vectors live on the device; the (m+1)x(m+1) Hessenberg matrix and the
-// Givens rotations live on the host (one small device-to-host copy per
-// Arnoldi step).
-int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_zero, double *x, double *res_out,
-                double *res_rel_out) {
-  GB_CHECK(c && c->have_structure, "structure not set");
-  GB_CHECK(krylov > 0 && krylov <= 256, "krylov must be in 1..256");
-  GB_CHECK(x != nullptr, "null solution vector");
-  GB_CUDA(cudaSetDevice(c->device));
-  const int n = c->ndof, m = krylov;
+}  // extern "C"
+
+// Restarted GMRES(m) on a device-resident operator (lss_mkb_core.c:2317-2660):
+// left preconditioned, classical Gram-Schmidt, Givens rotations, stopping on
+// the preconditioned residual with the reference's 1e-12 floors
+// (:2377-2378).  Vectors live on the device; the (m+1)x(m+1) Hessenberg
+// matrix and the rotations live on the host (one small device-to-host copy
+// per Arnoldi step).  op(0, in, out): out = M^-1 (b - A in);
+// op(1, in, out): out = M^-1 A in; both return the number of kernels they
+// launched.  Returns the iteration count.
+using GmresOp = std::function<int(int, const double *, double *)>;
+
+static int gmres_run(gbfem_ctx c, int n, int krylov, int max_iter, double tol_rel, int ini_zero, double *x,
+                     double *res_out, double *res_rel_out, const GmresOp &op) {
+  int kernels = 0;
+#define GB_COUNT(x)          \
+  do {                       \
+    int r_ = (x);            \
+    if (r_ < 0) return r_;   \
+    kernels += r_;           \
+  } while (0)
+  const int m = krylov;
   const long long ld = n;
   GB_TRY(c->V.alloc((size_t)n * (m + 1)));
   GB_TRY(c->x.alloc(n));
   GB_TRY(c->tmp.alloc(n));
-  GB_TRY(c->dinv.alloc(n));
   GB_TRY(c->hcol.alloc(m + 2));
   const int nb = gbfem::reduction_blocks(n);
   GB_TRY(c->partial.alloc((size_t)nb * (m + 2)));
   cudaStream_t st = c->stream;
-  GB_TRY(gbfem::launch_jacobi_diag(st, n, c->row_ptr.p, c->col_ind.p, c->val.p, c->dinv.p));
   if (ini_zero)
     GB_CUDA(cudaMemsetAsync(c->x.p, 0, (size_t)n * sizeof(double), st));
   else
@@ -637,37 +839,35 @@ int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_z
   double beta0 = -1.0, resid = 0.0;
   int it = 0;
   float spmv_ms = 0.f;
-  int spmv_n = 0, kernels = 1;
+  int spmv_n = 0;
   cudaEventRecord(c->ev0, st);
   for (;;) {
-    // v0 = D^-1 (b - A x)
-    GB_TRY(gbfem::launch_spmv(st, 0, n, c->row_ptr.p, c->col_ind.p, c->val.p, c->x.p, c->rhs.p, nullptr, c->tmp.p));
-    GB_TRY(gbfem::launch_mul(st, n, c->dinv.p, c->tmp.p));
-    GB_TRY(gbfem::launch_multidot(st, n, 1, c->tmp.p, ld, c->tmp.p, c->partial.p, c->hcol.p, 1));
+    // v0 = M^-1 (b - A x)
+    GB_COUNT(op(0, c->x.p, c->tmp.p));
+    GB_COUNT(gbfem::launch_multidot(st, n, 1, c->tmp.p, ld, c->tmp.p, c->partial.p, c->hcol.p, 1));
     double rn = 0.0;
     GB_CUDA(cudaMemcpyAsync(&rn, c->hcol.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
     if (beta0 < 0) beta0 = rn;
     resid = rn;
     if (rn < tol_abs || (beta0 > 0 && rn / beta0 < tol_rel) || it >= max_iter) break;
-    GB_TRY(gbfem::launch_scale(st, n, c->hcol.p, 1, c->tmp.p, c->V.p));
+    GB_COUNT(gbfem::launch_scale(st, n, c->hcol.p, 1, c->tmp.p, c->V.p));
     s[0] = rn;
     for (int i = 1; i <= m; i++) s[i] = 0.0;
     int done = 0;
     for (int j = 0; j < m; j++) {
       double *vj = c->V.p + (size_t)j * n, *w = c->V.p + (size_t)(j + 1) * n;
       it++;
-      // w = D^-1 A v_j
+      // w = M^-1 A v_j
       cudaEventRecord(c->ev2, st);
-      GB_TRY(gbfem::launch_spmv(st, 1, n, c->row_ptr.p, c->col_ind.p, c->val.p, vj, nullptr, c->dinv.p, w));
+      GB_COUNT(op(1, vj, w));
       cudaEventRecord(c->ev3, st);
-      kernels += 8;
       // classical Gram-Schmidt: h = V^T w, w -= V h, h_{j+1} = |w|
-      GB_TRY(gbfem::launch_multidot(st, n, j + 1, c->V.p, ld, w, c->partial.p, c->hcol.p, 0));
-      GB_TRY(gbfem::launch_multiaxpy(st, n, j + 1, c->hcol.p, -1.0, c->V.p, ld, w));
-      GB_TRY(gbfem::launch_multidot(st, n, 1, w, ld, w, c->partial.p, c->hcol.p + j + 1, 1));
+      GB_COUNT(gbfem::launch_multidot(st, n, j + 1, c->V.p, ld, w, c->partial.p, c->hcol.p, 0));
+      GB_COUNT(gbfem::launch_multiaxpy(st, n, j + 1, c->hcol.p, -1.0, c->V.p, ld, w));
+      GB_COUNT(gbfem::launch_multidot(st, n, 1, w, ld, w, c->partial.p, c->hcol.p + j + 1, 1));
       GB_CUDA(cudaMemcpyAsync(hh.data(), c->hcol.p, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st));
-      GB_TRY(gbfem::launch_scale(st, n, c->hcol.p + j + 1, 1, w, w));
+      GB_COUNT(gbfem::launch_scale(st, n, c->hcol.p + j + 1, 1, w, w));
       GB_CUDA(cudaStreamSynchronize(st));
       {
         float ms = 0.f;
@@ -705,7 +905,7 @@ int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_z
       s[k] = t / H[k + (size_t)k * (m + 1)];
     }
     GB_CUDA(cudaMemcpyAsync(c->hcol.p, s.data(), done * sizeof(double), cudaMemcpyHostToDevice, st));
-    GB_TRY(gbfem::launch_multiaxpy(st, n, done, c->hcol.p, 1.0, c->V.p, ld, c->x.p));
+    GB_COUNT(gbfem::launch_multiaxpy(st, n, done, c->hcol.p, 1.0, c->V.p, ld, c->x.p));
     GB_CUDA(cudaStreamSynchronize(st));
     if (resid < tol_abs || resid / beta0 < tol_rel || it >= max_iter) break;
   }
@@ -715,10 +915,64 @@ int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_z
   cudaEventElapsedTime(&c->last_solve_ms, c->ev0, c->ev1);
   c->last_spmv_ms = spmv_ms;
   c->last_spmv_count = spmv_n;
-  c->last_solve_kernels = kernels;
+  c->last_solve_kernels += kernels;
   if (res_out) *res_out = resid;
   if (res_rel_out) *res_rel_out = beta0 > 0 ? resid / beta0 : 0.0;
   return it;
+#undef GB_COUNT
+}
+
+extern "C" {
+
+// CRS matrix with point Jacobi (lar_fill_preconditioner_crs: 1 / a_ii,
+// las_crs_intf.c:707).
+int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_zero, double *x, double *res_out,
+                double *res_rel_out) {
+  GB_CHECK(c && c->have_structure, "structure not set");
+  GB_CHECK(krylov > 0 && krylov <= 256, "krylov must be in 1..256");
+  GB_CHECK(x != nullptr, "null solution vector");
+  GB_CUDA(cudaSetDevice(c->device));
+  const int n = c->ndof;
+  cudaStream_t st = c->stream;
+  GB_TRY(c->dinv.alloc(n));
+  GB_TRY(gbfem::launch_jacobi_diag(st, n, c->row_ptr.p, c->col_ind.p, c->val.p, c->dinv.p));
+  c->last_solve_kernels = 1;
+  GmresOp op = [&](int mode, const double *in, double *out) -> int {
+    if (mode == 0) {
+      const int r = gbfem::launch_spmv(st, 0, n, c->row_ptr.p, c->col_ind.p, c->val.p, in, c->rhs.p, nullptr, out);
+      if (r < 0) return r;
+      const int r2 = gbfem::launch_mul(st, n, c->dinv.p, out);
+      return r2 < 0 ? r2 : r + r2;
+    }
+    return gbfem::launch_spmv(st, 1, n, c->row_ptr.p, c->col_ind.p, c->val.p, in, nullptr, c->dinv.p, out);
+  };
+  return gmres_run(c, n, krylov, max_iter, tol_rel, ini_zero, x, res_out, res_rel_out, op);
+}
+
+// DG block matrix with block Jacobi (inverted diagonal blocks).
+int gbfem_dg_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_zero, double *x, double *res_out,
+                   double *res_rel_out) {
+  GB_CHECK(c && c->dg_ready, "DG structure not built");
+  GB_CHECK(krylov > 0 && krylov <= 256, "krylov must be in 1..256");
+  GB_CHECK(x != nullptr, "null solution vector");
+  GB_CUDA(cudaSetDevice(c->device));
+  const int n = c->dg_ndof;
+  cudaStream_t st = c->stream;
+  GB_TRY(c->dg_dinv.alloc((size_t)c->dg_ninv));
+  GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), st));
+  GB_TRY(gbfem::launch_dg_block_inverse(st, c->nel, c->dg_roff_d.p, c->dg_boff_diag_d.p, c->dg_val.p,
+                                        c->dg_dinv_off_d.p, c->dg_dinv.p, c->err.p));
+  int herr = 0;
+  GB_CUDA(cudaMemcpyAsync(&herr, c->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  GB_CHECK(herr == 0, "singular diagonal block in the DG block Jacobi preconditioner");
+  c->last_solve_kernels = 1;
+  GmresOp op = [&](int mode, const double *in, double *out) -> int {
+    return gbfem::launch_dg_block_spmv(st, mode, c->nel, c->dg_roff_d.p, c->dg_bptr_d.p, c->dg_bcol_d.p,
+                                       c->dg_boff_d.p, c->dg_val.p, c->dg_dinv_off_d.p, c->dg_dinv.p, in,
+                                       mode == 0 ? c->dg_rhs.p : nullptr, out);
+  };
+  return gmres_run(c, n, krylov, max_iter, tol_rel, ini_zero, x, res_out, res_rel_out, op);
 }
 
 }  // extern "C"

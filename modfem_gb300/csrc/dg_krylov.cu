@@ -1,0 +1,196 @@
+// Variable-block CRS products and block Jacobi for the DG matrix, FP64.
+//
+// Storage (the device form of lad_block, lsd_mkb/lad_block/lah_block.h): block
+// row e holds the dofs of element e (roff[e] .. roff[e+1]); its blocks
+// bptr[e] .. bptr[e+1] have column elements bcol[k] (ascending, the diagonal
+// included) and dense values at val + boff[k], column-major with the row
+// block's size as leading dimension (Dia / Aux of las_block_intf.c:362-520).
+//
+// The block Jacobi preconditioner of the reference (lar_fill_preconditioner_
+// block with Block_type 1: an LU factorisation of every diagonal block,
+// las_block_intf.c:1224-1330, applied by forward/back substitution) is kept
+// here as the explicit inverse of each diagonal block: applying it is then a
+// dense block product fused into the SpMV.
+
+#include "dg_tables.h"
+#include "gbfem_internal.h"
+
+namespace gbfem {
+
+// Gauss-Jordan inversion with partial pivoting (largest magnitude, first
+// index on ties), one CTA per diagonal block held in shared memory.
+constexpr int DGI_THREADS = 256;
+
+__global__ void __launch_bounds__(DGI_THREADS) dg_block_inverse_kernel(int nel, const int *__restrict__ roff,
+                                                                        const long long *__restrict__ boff_diag,
+                                                                        const double *__restrict__ val,
+                                                                        const long long *__restrict__ dinv_off,
+                                                                        double *__restrict__ dinv, int *err) {
+  __shared__ double a[GB_DG_MAXNS * GB_DG_MAXNS];
+  __shared__ double fcol[GB_DG_MAXNS];
+  __shared__ int piv[GB_DG_MAXNS];
+  __shared__ int s_r;
+  const int e = blockIdx.x;
+  if (e >= nel) return;
+  const int n = roff[e + 1] - roff[e];
+  if (n <= 0 || n > GB_DG_MAXNS) {
+    if (threadIdx.x == 0) atomicExch(err, 4);
+    return;
+  }
+  const double *src = val + boff_diag[e];
+  for (int t = threadIdx.x; t < n * n; t += DGI_THREADS) a[t] = src[t];
+  __syncthreads();
+  for (int k = 0; k < n; k++) {
+    if (threadIdx.x < 32) {
+      double best = -1.0;
+      int bi = n;
+      for (int i = k + (int)threadIdx.x; i < n; i += 32) {
+        const double v = fabs(a[i + n * k]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (threadIdx.x == 0) {
+        s_r = best > 0.0 ? bi : -1;
+        piv[k] = bi;
+      }
+    }
+    __syncthreads();
+    const int r = s_r;
+    if (r < 0) {  // singular diagonal block (uniform across the CTA)
+      if (threadIdx.x == 0) atomicExch(err, 3);
+      return;
+    }
+    if (r != k)
+      for (int j = threadIdx.x; j < n; j += DGI_THREADS) {
+        const double t = a[k + n * j];
+        a[k + n * j] = a[r + n * j];
+        a[r + n * j] = t;
+      }
+    __syncthreads();
+    const double pinv = 1.0 / a[k + n * k];
+    for (int i = threadIdx.x; i < n; i += DGI_THREADS) fcol[i] = a[i + n * k];
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += DGI_THREADS) a[k + n * j] = j == k ? pinv : a[k + n * j] * pinv;
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * n; t += DGI_THREADS) {
+      const int i = t % n, j = t / n;
+      if (i == k) continue;
+      a[t] = j == k ? -fcol[i] * pinv : fma(-fcol[i], a[k + n * j], a[t]);
+    }
+    __syncthreads();
+  }
+  // undo the row interchanges as column interchanges, last first
+  for (int k = n - 1; k >= 0; k--) {
+    const int r = piv[k];
+    if (r != k)
+      for (int i = threadIdx.x; i < n; i += DGI_THREADS) {
+        const double t = a[i + n * k];
+        a[i + n * k] = a[i + n * r];
+        a[i + n * r] = t;
+      }
+    __syncthreads();
+  }
+  double *dst = dinv + dinv_off[e];
+  for (int t = threadIdx.x; t < n * n; t += DGI_THREADS) dst[t] = a[t];
+}
+
+int launch_dg_block_inverse(cudaStream_t st, int nel, const int *roff, const long long *boff_diag,
+                            const double *val, const long long *dinv_off, double *dinv, int *err) {
+  if (nel <= 0) return 0;
+  dg_block_inverse_kernel<<<nel, DGI_THREADS, 0, st>>>(nel, roff, boff_diag, val, dinv_off, dinv, err);
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
+// One warp per block row: lane l accumulates rows l, l+32, l+64 (ns <= 75);
+// every block column j is a coalesced load of ns consecutive values.  With a
+// preconditioner the row block's result goes through shared memory into the
+// product with the inverted diagonal block.
+constexpr int DGS_WARPS = 8;
+
+__global__ void __launch_bounds__(DGS_WARPS * 32) dg_block_spmv_kernel(
+    int mode, int nel, const int *__restrict__ roff, const int *__restrict__ bptr, const int *__restrict__ bcol,
+    const long long *__restrict__ boff, const double *__restrict__ val, const long long *__restrict__ dinv_off,
+    const double *__restrict__ dinv, const double *__restrict__ x, const double *__restrict__ b,
+    double *__restrict__ out) {
+  __shared__ double sv[DGS_WARPS][GB_DG_MAXNS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * DGS_WARPS + warp;
+  if (e >= nel) return;  // whole warp
+  const int r0 = roff[e], ns = roff[e + 1] - r0;
+  const int i0 = lane, i1 = lane + 32, i2 = lane + 64;
+  const bool v0 = i0 < ns, v1 = i1 < ns, v2 = i2 < ns;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int k = bptr[e]; k < bptr[e + 1]; k++) {
+    const int c = bcol[k], c0 = roff[c], nc = roff[c + 1] - c0;
+    const double *blk = val + boff[k];
+    const double *xc = x + c0;
+    int j = 0;
+    for (; j + 2 <= nc; j += 2) {
+      const double x0 = xc[j], x1 = xc[j + 1];
+      const double *col0 = blk + (size_t)j * ns, *col1 = col0 + ns;
+      if (v0) a0 = fma(col1[i0], x1, fma(col0[i0], x0, a0));
+      if (v1) a1 = fma(col1[i1], x1, fma(col0[i1], x0, a1));
+      if (v2) a2 = fma(col1[i2], x1, fma(col0[i2], x0, a2));
+    }
+    if (j < nc) {
+      const double x0 = xc[j];
+      const double *col0 = blk + (size_t)j * ns;
+      if (v0) a0 = fma(col0[i0], x0, a0);
+      if (v1) a1 = fma(col0[i1], x0, a1);
+      if (v2) a2 = fma(col0[i2], x0, a2);
+    }
+  }
+  if (mode != 1) {
+    a0 = (b && v0 ? b[r0 + i0] : 0.0) - a0;
+    a1 = (b && v1 ? b[r0 + i1] : 0.0) - a1;
+    a2 = (b && v2 ? b[r0 + i2] : 0.0) - a2;
+  }
+  if (mode == 2) {
+    if (v0) out[r0 + i0] = a0;
+    if (v1) out[r0 + i1] = a1;
+    if (v2) out[r0 + i2] = a2;
+    return;
+  }
+  if (v0) sv[warp][i0] = a0;
+  if (v1) sv[warp][i1] = a1;
+  if (v2) sv[warp][i2] = a2;
+  __syncwarp();
+  const double *D = dinv + dinv_off[e];
+  double o0 = 0.0, o1 = 0.0, o2 = 0.0;
+  for (int j = 0; j < ns; j++) {
+    const double t = sv[warp][j];
+    const double *col = D + (size_t)j * ns;
+    if (v0) o0 = fma(col[i0], t, o0);
+    if (v1) o1 = fma(col[i1], t, o1);
+    if (v2) o2 = fma(col[i2], t, o2);
+  }
+  if (v0) out[r0 + i0] = o0;
+  if (v1) out[r0 + i1] = o1;
+  if (v2) out[r0 + i2] = o2;
+}
+
+int launch_dg_block_spmv(cudaStream_t st, int mode, int nel, const int *roff, const int *bptr, const int *bcol,
+                         const long long *boff, const double *val, const long long *dinv_off, const double *dinv,
+                         const double *x, const double *b, double *out) {
+  if (nel <= 0) return 0;
+  GB_CHECK(mode >= 0 && mode <= 2, "bad block SpMV mode");
+  GB_CHECK(mode == 2 || (dinv && dinv_off), "block SpMV needs the inverted diagonal blocks");
+  const int grid = (nel + DGS_WARPS - 1) / DGS_WARPS;
+  dg_block_spmv_kernel<<<grid, DGS_WARPS * 32, 0, st>>>(mode, nel, roff, bptr, bcol, boff, val, dinv_off, dinv, x,
+                                                        b, out);
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
+}  // namespace gbfem

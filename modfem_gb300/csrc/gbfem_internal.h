@@ -101,6 +101,33 @@ int launch_multiaxpy(cudaStream_t st, int n, int m, const double *c, double sign
 int launch_scale(cudaStream_t st, int n, const double *alpha, int invert, const double *x, double *y);
 int launch_mul(cudaStream_t st, int n, const double *a, double *y);
 int measure_fp64_peak(cudaStream_t st, int device, double *tflops);
+// One (element, face) incidence of the DG face assembly, built on the host:
+// the face's two neighbours (el2 = -1 on a Dirichlet boundary face), the side
+// of el1 the face lies on, its vertex count, the local vertex index in el1 /
+// el2 of each face vertex (face order), which neighbour owns this record and
+// the value offset of the owner's off-diagonal block (owner, other).
+struct DgHalfFace {
+  int el1, el2;
+  int side1, nfv;
+  long long blk;
+  unsigned char loc1[4], loc2[4];
+  int owner_is_2;
+  int pad;
+};
+
+int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
+                          const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
+                          const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
+                          const int *roff, double *val, double *rhs);
+// Variable-block CRS (one block row per DG element, dense column-major
+// blocks with the row block's size as leading dimension) and block Jacobi.
+int launch_dg_block_inverse(cudaStream_t st, int nel, const int *roff, const long long *boff_diag,
+                            const double *val, const long long *dinv_off, double *dinv, int *err);
+// mode 0: out = Minv (b - A x) (b may be NULL), 1: out = Minv A x,
+// 2: out = (b ? b : 0) - A x (Minv unused)
+int launch_dg_block_spmv(cudaStream_t st, int mode, int nel, const int *roff, const int *bptr, const int *bcol,
+                         const long long *boff, const double *val, const long long *dinv_off, const double *dinv,
+                         const double *x, const double *b, double *out);
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                              const double *xyz, const double *k_el, const double *D_el, double f,
                              const long long *boff, const int *roff, double *val, double *rhs);
@@ -144,14 +171,25 @@ struct gbfem_ctx_s {
   // DG prisms: per-element degree, block-CRS structure (block row = element)
   std::vector<int> dg_p, dg_roff, dg_bptr, dg_bcol;
   std::vector<long long> dg_boff;
-  long long dg_nval = 0;
+  long long dg_nval = 0, dg_ninv = 0;
   int dg_ndof = 0;
   bool dg_ready = false;
   gbfem::DevBuf<int> dg_list[5], dg_roff_d;
   gbfem::DevBuf<long long> dg_boff_diag_d;
   gbfem::DevBuf<double> dg_val, dg_rhs;
+  // DG faces: the caller's face table and the per-element incidences
+  std::vector<int> dg_fa_type, dg_fa_bc, dg_fa_el, dg_fa_side, dg_fa_nodes;
+  int dg_nfa = -1;  // -1: no face table (volume terms only)
+  double dg_pen = 10.0;
+  gbfem::DevBuf<int> dg_hf_ptr, dg_p_d;
+  gbfem::DevBuf<gbfem::DgHalfFace> dg_hf;
+  // DG block Jacobi: inverted diagonal blocks, block e at dg_dinv_off_d[e]
+  gbfem::DevBuf<double> dg_dinv;
+  gbfem::DevBuf<long long> dg_dinv_off_d;
+  gbfem::DevBuf<int> dg_bptr_d, dg_bcol_d;
+  gbfem::DevBuf<long long> dg_boff_d;
   // timing
-  float last_ms = 0.f, last_el_ms = 0.f, last_solve_ms = 0.f, last_spmv_ms = 0.f;
+  float last_ms = 0.f, last_el_ms = 0.f, last_fa_ms = 0.f, last_solve_ms = 0.f, last_spmv_ms = 0.f;
   int last_spmv_count = 0, last_solve_kernels = 0;
   int last_launches = 0;
 };

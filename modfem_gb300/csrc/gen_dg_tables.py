@@ -27,6 +27,13 @@ PMAX = 4
 MMC_TRIA, MMC_QUAD = 3, 4
 
 
+def table(out, ctype, name, dims, init):
+    """A host table plus its initialiser as a macro (name_INIT), so that CUDA
+    code can declare the same values as a __device__ array."""
+    out.append("#define %s_INIT \\\n  " % name + init.replace("\n", " \\\n"))
+    out.append("static const %s %s%s = %s_INIT;" % (ctype, name, dims, name))
+
+
 def main():
     import refmod
     L = ctypes.CDLL(refmod.lib_path("dg"))
@@ -72,27 +79,30 @@ def main():
     out.append("// Tensor DG prism basis (pdeg = 101 p): monomial exponents (xi, eta, zeta) in the")
     out.append("// reference's order; volume rules (xi, eta, zeta, w); face rules (s, t, w) for")
     out.append("// triangle (0) and quadrilateral (1) faces, coordinates as the reference returns them.")
+    out.append("// Each table X also exists as the initialiser macro X_INIT.")
     out.append("#pragma once")
     out.append(f"#define GB_DG_PMAX {PMAX}")
     out.append(f"#define GB_DG_MAXNS {max(ns.values())}")
     out.append(f"#define GB_DG_MAXNQ {maxq}")
     out.append(f"#define GB_DG_MAXNQF {maxf}")
-    out.append("static const int GB_DG_NS[GB_DG_PMAX + 1] = {0, " + ", ".join(str(ns[p]) for p in range(1, PMAX + 1)) + "};")
-    out.append("static const int GB_DG_NQ[GB_DG_PMAX + 1] = {0, " + ", ".join(str(len(qps[p][1])) for p in range(1, PMAX + 1)) + "};")
-    out.append("static const int GB_DG_NQF[GB_DG_PMAX + 1][2] = {{0, 0}, " + ", ".join(
-        "{%d, %d}" % (len(fq[(p, MMC_TRIA)][1]), len(fq[(p, MMC_QUAD)][1])) for p in range(1, PMAX + 1)) + "};")
+    table(out, "int", "GB_DG_NS", "[GB_DG_PMAX + 1]",
+          "{0, " + ", ".join(str(ns[p]) for p in range(1, PMAX + 1)) + "}")
+    table(out, "int", "GB_DG_NQ", "[GB_DG_PMAX + 1]",
+          "{0, " + ", ".join(str(len(qps[p][1])) for p in range(1, PMAX + 1)) + "}")
+    table(out, "int", "GB_DG_NQF", "[GB_DG_PMAX + 1][2]", "{{0, 0}, " + ", ".join(
+        "{%d, %d}" % (len(fq[(p, MMC_TRIA)][1]), len(fq[(p, MMC_QUAD)][1])) for p in range(1, PMAX + 1)) + "}")
     rows = []
     for p in range(1, PMAX + 1):
         ex = exps[p] + [(0, 0, 0)] * (max(ns.values()) - ns[p])
         rows.append("  {" + ", ".join("{%d, %d, %d}" % e for e in ex) + "}")
-    out.append("static const unsigned char GB_DG_EXP[GB_DG_PMAX][GB_DG_MAXNS][3] = {\n" + ",\n".join(rows) + "};")
+    table(out, "unsigned char", "GB_DG_EXP", "[GB_DG_PMAX][GB_DG_MAXNS][3]", "{\n" + ",\n".join(rows) + "}")
     rows = []
     for p in range(1, PMAX + 1):
         xg, wg = qps[p]
         ent = ["{%.17g, %.17g, %.17g, %.17g}" % (x[0], x[1], x[2], w) for x, w in zip(xg, wg)]
         ent += ["{0, 0, 0, 0}"] * (maxq - len(ent))
         rows.append("  {" + ",\n   ".join(ent) + "}")
-    out.append("static const double GB_DG_QP[GB_DG_PMAX][GB_DG_MAXNQ][4] = {\n" + ",\n".join(rows) + "};")
+    table(out, "double", "GB_DG_QP", "[GB_DG_PMAX][GB_DG_MAXNQ][4]", "{\n" + ",\n".join(rows) + "}")
     rows = []
     for p in range(1, PMAX + 1):
         sub = []
@@ -102,7 +112,7 @@ def main():
             ent += ["{0, 0, 0}"] * (maxf - len(ent))
             sub.append("   {" + ",\n    ".join(ent) + "}")
         rows.append("  {\n" + ",\n".join(sub) + "}")
-    out.append("static const double GB_DG_FQ[GB_DG_PMAX][2][GB_DG_MAXNQF][3] = {\n" + ",\n".join(rows) + "};")
+    table(out, "double", "GB_DG_FQ", "[GB_DG_PMAX][2][GB_DG_MAXNQF][3]", "{\n" + ",\n".join(rows) + "}")
     open(os.path.join(HERE, "dg_tables.h"), "w").write("\n".join(out) + "\n")
     print("wrote dg_tables.h", {p: (ns[p], len(qps[p][1])) for p in ns},
           {k: len(v[1]) for k, v in fq.items()}, file=sys.stderr)

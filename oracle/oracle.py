@@ -121,6 +121,62 @@ def dg_face(mesh, faces, i, pdeg, A, pen=10.0, g=0.0):
     return sm.reshape(n, n).T.copy(), rhs
 
 
+DG_NS = (0, 6, 18, 40, 75)
+
+
+def dg_block_structure(nel, faces, pdeg):
+    """Dof offsets of the DG blocks (one per element, element order:
+    utr_get_list_ent, utd_util/uts_ls_intf.c:640-700) and the column blocks
+    of each block row: the element and its face neighbours, ascending (the
+    sorted neighbour lists of sir_create, sid_mkb/sis_mkb_intf.c:1100-1146)."""
+    off = np.concatenate([[0], np.cumsum([DG_NS[int(p)] for p in pdeg])]).astype(np.int64)
+    nb = [[e] for e in range(nel)]
+    if faces is not None:
+        for e1, e2 in zip(faces.el1, faces.el2):
+            if e2 >= 0:
+                nb[int(e1)].append(int(e2))
+                nb[int(e2)].append(int(e1))
+    return off, [sorted(x) for x in nb]
+
+
+def dg_assemble(mesh, faces, pdeg, A, pen=10.0, g=0.0, f=1.0):
+    """The whole DG system: element integrals, then face integrals in face
+    order, summed block by block as lar_assemble_SM_and_LV_block does
+    (lsd_mkb/lad_block/las_block_intf.c:362-520).  A: (nel, 9) tensors.
+    Returns the scalar expansion of the block storage (every entry of every
+    block, columns ascending: row_ptr, col_ind, val), the rhs and the dof
+    offsets."""
+    nel = mesh.nel
+    off, cols = dg_block_structure(nel, faces, pdeg)
+    B = {}
+    rhs = np.zeros(int(off[-1]))
+    for e in range(nel):
+        K, r = dg_prism_element(mesh.coords[mesh.el_nodes[e]], A[e], int(pdeg[e]), f)
+        B[(e, e)] = K
+        rhs[off[e]:off[e + 1]] += r
+    if faces is not None:
+        for i in range(faces.n):
+            K, r = dg_face(mesh, faces, i, pdeg, A, pen, g)
+            e1, e2 = int(faces.el1[i]), int(faces.el2[i])
+            n1 = DG_NS[int(pdeg[e1])]
+            B[(e1, e1)] = B[(e1, e1)] + K[:n1, :n1]
+            rhs[off[e1]:off[e1 + 1]] += r[:n1]
+            if e2 >= 0:
+                B[(e1, e2)] = B.get((e1, e2), 0.0) + K[:n1, n1:]
+                B[(e2, e1)] = B.get((e2, e1), 0.0) + K[n1:, :n1]
+                B[(e2, e2)] = B[(e2, e2)] + K[n1:, n1:]
+    rp = [0]
+    ci, val = [], []
+    for e in range(nel):
+        row = np.concatenate([B[(e, c)] for c in cols[e]], axis=1)
+        cidx = np.concatenate([np.arange(off[c], off[c + 1]) for c in cols[e]])
+        for i in range(row.shape[0]):
+            ci.append(cidx)
+            val.append(row[i])
+            rp.append(rp[-1] + cidx.size)
+    return (np.array(rp, np.int64), np.concatenate(ci).astype(np.int64), np.concatenate(val), rhs, off)
+
+
 def dof_order(el_nodes, nno):
     el = _c(el_nodes, np.int32)
     d = np.zeros(nno, np.int32)

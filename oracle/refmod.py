@@ -35,7 +35,7 @@ def available(kind="std"):
 
 MKB_TEMPLATE = """FINE_LEVEL       (the only level for single-level solvers)
 1 1 {krylov}    single-level GMRES, number of levels, number of Krylov vectors
-1 1 -2  \t\ttype of preconditioner (block Jacobi), sweeps, block type (-2: CRS storage)
+1 1 {block_type}  \t\ttype of preconditioner (block Jacobi), sweeps, block type (negative: -storage type)
 {max_iter} {conv_type} {tol:.3e}   \tmax_iter, convergence type, convergence treshold
 {monitor} 1 0   \toutput level, nr_pre and post_smooth steps
 
@@ -157,6 +157,22 @@ class RefModfem:
         self.L.refh_crs_get(_p(rp), _p(ci), _p(val), _p(rhs))
         return rp, ci, val, rhs
 
+    def block_crs(self, matrix_id=0):
+        """The block-storage (lad_block) matrix of a DG solver expanded to a
+        scalar CRS over global dofs with sorted columns (harness_block.c)."""
+        L = self.L
+        L.refh_block_crs.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 5
+        nd = ctypes.c_int()
+        nnz = L.refh_block_crs(matrix_id, ctypes.addressof(nd), None, None, None, None)
+        if nnz < 0:
+            raise RuntimeError("no block matrix")
+        rp = np.zeros(nd.value + 1, np.int32)
+        ci = np.zeros(nnz, np.int32)
+        val = np.zeros(nnz)
+        rhs = np.zeros(nd.value)
+        L.refh_block_crs(matrix_id, None, _p(rp), _p(ci), _p(val), _p(rhs))
+        return rp, ci, val, rhs
+
     def residual(self, x, b=None, use_rhs=1):
         x = np.ascontiguousarray(x, dtype=np.float64)
         v = np.zeros(self.ndof)
@@ -174,9 +190,11 @@ class RefModfem:
         return sol, nit, meas.value, times
 
 
-def write_mkb(path, krylov=30, max_iter=1000, conv_type=0, tol=1e-8, monitor=0):
+def write_mkb(path, krylov=30, max_iter=1000, conv_type=0, tol=1e-8, monitor=0, block_type=-2):
     """conv_type: 0 relative to the initial residual (REL_RES_INI), 1 absolute
-    (ABS_RES), 2 relative to the rhs (lsd_mkb_core/lsh_mkb_core.h:111-113)."""
+    (ABS_RES), 2 relative to the rhs (lsd_mkb_core/lsh_mkb_core.h:111-113).
+    block_type < 0 enforces storage -block_type (lss_mkb_core.c:459-464):
+    -2 CRS (one dof per block: std), -4 generic CRS (variable blocks: DG)."""
     with open(path, "w") as f:
         f.write(MKB_TEMPLATE.format(krylov=krylov, max_iter=max_iter, conv_type=conv_type,
-                                    tol=tol, monitor=monitor))
+                                    tol=tol, monitor=monitor, block_type=block_type))

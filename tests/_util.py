@@ -119,3 +119,44 @@ def face_rel_err(a, b):
     if np.any(err[~ok] != 0):
         return float("inf")
     return float(np.max(err[ok] / den[ok])) if np.any(ok) else 0.0
+
+
+def dg_blocks_to_crs(off, bptr, bcol, boff, vals):
+    """Scalar expansion (sorted columns, every block entry) of the library's
+    variable-block storage: column-major blocks, leading dimension the row
+    block's size."""
+    rp = [0]
+    ci, out = [], []
+    for e in range(off.size - 1):
+        ns = off[e + 1] - off[e]
+        blocks, cidx = [], []
+        for k in range(bptr[e], bptr[e + 1]):
+            c = bcol[k]
+            nc = off[c + 1] - off[c]
+            blocks.append(vals[boff[k]:boff[k + 1]].reshape(nc, ns).T)
+            cidx.append(np.arange(off[c], off[c + 1]))
+        row = np.concatenate(blocks, axis=1)
+        cidx = np.concatenate(cidx)
+        for i in range(ns):
+            ci.append(cidx)
+            out.append(row[i])
+            rp.append(rp[-1] + cidx.size)
+    return np.array(rp, np.int64), np.concatenate(ci).astype(np.int64), np.concatenate(out)
+
+
+def sparse_rel_err(row_ptr, col_ind, a, b):
+    """Assembled matrices without a usable diagonal scale (DG blocks):
+    max |a_ij - b_ij| / sqrt(R_i C_j) with R_i, C_j the largest magnitudes in
+    row i and column j of b."""
+    n = row_ptr.size - 1
+    rows = np.repeat(np.arange(n), np.diff(row_ptr))
+    R = np.zeros(n)
+    C = np.zeros(n)
+    np.maximum.at(R, rows, np.abs(b))
+    np.maximum.at(C, col_ind, np.abs(b))
+    den = np.sqrt(R[rows] * C[col_ind])
+    err = np.abs(a - b)
+    ok = den > 0
+    if np.any(err[~ok] != 0):
+        return float("inf")
+    return float(np.max(err[ok] / den[ok])) if np.any(ok) else 0.0

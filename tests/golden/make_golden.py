@@ -167,9 +167,61 @@ def run_dg_elements(name="dg_el_n2"):
     print(f"{name}: {m.nel} DG prisms, p counts {np.bincount(pdeg, minlength=5)[1:]}", file=sys.stderr)
 
 
+# assembled DG systems: (n, degree mode, anisotropic)
+DG_ASM_CASES = {"dg_asm_p2": (2, 2, False), "dg_asm_mixed": (2, "mixed", False), "dg_asm_aniso": (2, "mixed", True)}
+
+
+def run_dg_assembly(name):
+    """Whole DG system from the reference: every element and face integrated
+    and assembled by the MKB solver into its block storage (lad_block), the
+    rhs, and the GMRES(50) solution with block Jacobi to 1e-10 relative."""
+    import refmod
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, structured_prism_mesh, write_jk
+    n, mode, aniso = DG_ASM_CASES[name]
+    seed = 21
+    m = structured_prism_mesh(n, jitter=0.2, seed=seed)
+    k = lognormal_k(m.nel, seed=seed)
+    D = anisotropic_tensors(m.nel, seed=seed) if aniso else None
+    pdeg = np.random.default_rng(seed).integers(1, 5, m.nel) if mode == "mixed" else np.full(m.nel, mode)
+    krylov, tol = 50, 1e-10
+    tmp = tempfile.mkdtemp()
+    jk = os.path.join(tmp, "mesh.jk")
+    mkb = os.path.join(tmp, "mkb.dat")
+    write_jk(jk, n)
+    refmod.write_mkb(mkb, krylov=krylov, max_iter=5000, tol=tol)
+    R = refmod.RefModfem("dg")
+    R.load_jk(jk)
+    R.set_node_coords(m.coords)
+    R.init_field("t", 101 * int(pdeg.max()))
+    if D is None:
+        R.set_coeffs(k=k, f=1.0, g=DG_G)
+    else:
+        R.set_coeffs(D=D, f=1.0, g=DG_G)
+    R.set_dg_penalty(10.0)
+    for e in range(m.nel):
+        R.L.refh_set_el_pdeg(e + 1, int(101 * pdeg[e]))
+    R.solver_create(mkb)
+    ll = R.level_lists()
+    R.assemble()
+    rp, ci, val, rhs = R.block_crs()
+    stride = 75
+    sol, nit, meas, _ = R.solve(-1, -1.0, stride=stride)
+    off = ll["dof_posglob"]
+    x = np.zeros(R.ndof)
+    for ent, pos in zip(ll["dof_ent_id"], off):
+        e = int(ent) - 1
+        ns = [0, 6, 18, 40, 75][int(pdeg[e])]
+        x[pos:pos + ns] = sol[(e + 1) * stride:(e + 1) * stride + ns]
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), n=n, jitter=0.2, seed=seed, coords=m.coords,
+                        el_nodes=m.el_nodes, k=k, D=np.zeros(0) if D is None else D, pdeg=pdeg, pen=10.0, g=DG_G,
+                        f=1.0, dof_ent_id=ll["dof_ent_id"], dof_posglob=off, row_ptr=rp, col_ind=ci, val=val,
+                        rhs=rhs, krylov=krylov, tol=tol, gmres_iters=nit, gmres_meas=meas, gmres_x=x)
+    print(f"{name}: {m.nel} DG prisms, ndof {R.ndof}, nnz {ci.size}, gmres {nit} it", file=sys.stderr)
+
+
 def main(argv):
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref")])
-    names = argv or list(CASES) + ["std_tet_n2", "dg_el_n2", "dg_el_aniso_n2"]
+    names = argv or list(CASES) + ["std_tet_n2", "dg_el_n2", "dg_el_aniso_n2"] + list(DG_ASM_CASES)
     if len(names) == 1 and os.environ.get("MAKE_GOLDEN_CHILD"):
         with open(os.devnull, "w") as dn:
             # the reference prints progress on stdout; keep only our stderr summary
@@ -178,6 +230,8 @@ def main(argv):
                 run_tets(names[0])
             elif names[0].startswith("dg_el_"):
                 run_dg_elements(names[0])
+            elif names[0] in DG_ASM_CASES:
+                run_dg_assembly(names[0])
             else:
                 run_case(names[0])
         return

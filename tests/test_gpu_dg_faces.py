@@ -1,0 +1,151 @@
+"""GPU parity of the whole DG system: volume and face integrals assembled
+into the variable-block storage, the block residual and block-Jacobi GMRES,
+against the reference's assembled lad_block matrices and solutions and the
+oracle."""
+import numpy as np
+import pytest
+
+import oracle as O
+from _util import REL_TOL, dg_blocks_to_crs, load, sparse_rel_err, vec_rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gb():
+    from modfem_gb300 import build
+    build.build(verbose=False)
+    import modfem_gb300
+    return modfem_gb300
+
+
+def _tensors(g):
+    return g["D"].reshape(-1, 9) if g["D"].size else None
+
+
+def _context(gb, m, F, pdeg, k=None, D=None, pen=10.0, g=0.0, f=1.0):
+    c = gb.Context(0)
+    c.set_mesh(m)
+    c.set_coefficients(k=k, D=D, f=f, g=g)
+    c.dg_set_degrees(pdeg)
+    c.dg_set_faces(F, penalty=pen)
+    c.dg_build_structure()
+    return c
+
+
+def _expand(c):
+    off, bptr, bcol, boff = c.dg_get_structure()
+    vals, rhs = c.dg_get_matrix()
+    rp, ci, v = dg_blocks_to_crs(off, bptr, bcol, boff, vals)
+    return rp, ci, v, rhs, off
+
+
+def _fixture_problem(name):
+    from modfem_gb300.mesh import prism_faces, structured_prism_mesh
+    g = load(name)
+    m = structured_prism_mesh(int(g["n"]), jitter=float(g["jitter"]), seed=int(g["seed"]))
+    assert np.array_equal(m.coords, g["coords"])
+    return g, m, prism_faces(m)
+
+
+@pytest.mark.parametrize("name", ["dg_asm_p2", "dg_asm_mixed", "dg_asm_aniso"])
+def test_dg_system_vs_reference(gb, name):
+    g, m, F = _fixture_problem(name)
+    D = _tensors(g)
+    c = _context(gb, m, F, g["pdeg"], k=None if D is not None else g["k"], D=D, pen=float(g["pen"]),
+                 g=float(g["g"]), f=float(g["f"]))
+    c.dg_assemble()
+    rp, ci, v, rhs, off = _expand(c)
+    # dof order and block pattern identical to the reference's block storage
+    assert np.array_equal(off[:-1], g["dof_posglob"])
+    assert np.array_equal(rp, g["row_ptr"]) and np.array_equal(ci, g["col_ind"])
+    assert sparse_rel_err(rp, ci, v, g["val"]) < REL_TOL
+    assert vec_rel_err(rhs, g["rhs"]) < REL_TOL
+
+
+@pytest.mark.parametrize("name", ["dg_asm_p2", "dg_asm_mixed", "dg_asm_aniso"])
+def test_dg_gmres_vs_reference(gb, name):
+    """GMRES(50) with block Jacobi to 1e-10 on the reference's problem: the
+    iteration count of lsr_mkb_core_gmres within 2, the solution within the
+    accuracy the stopping test guarantees."""
+    g, m, F = _fixture_problem(name)
+    D = _tensors(g)
+    c = _context(gb, m, F, g["pdeg"], k=None if D is not None else g["k"], D=D, pen=float(g["pen"]),
+                 g=float(g["g"]), f=float(g["f"]))
+    c.dg_assemble()
+    x, it, res, rel = c.dg_solve(krylov=int(g["krylov"]), max_iter=5000, tol_rel=float(g["tol"]))
+    assert abs(it - int(g["gmres_iters"])) <= 2, (it, int(g["gmres_iters"]))
+    assert rel < float(g["tol"])
+    assert vec_rel_err(x, g["gmres_x"]) < 1e-7
+
+
+def test_dg_residual_vs_numpy(gb):
+    g, m, F = _fixture_problem("dg_asm_mixed")
+    c = _context(gb, m, F, g["pdeg"], k=g["k"], pen=float(g["pen"]), g=float(g["g"]))
+    c.dg_assemble()
+    rp, ci, v, rhs, off = _expand(c)
+    x = np.sin(np.arange(off[-1]) * 0.37)
+    rows = np.repeat(np.arange(off[-1]), np.diff(rp))
+    ax = np.zeros(off[-1])
+    np.add.at(ax, rows, v * x[ci])
+    r = c.dg_compute_residual(x)
+    assert vec_rel_err(r, rhs - ax) < 1e-13
+    r0 = c.dg_compute_residual(x, use_rhs=0)
+    assert vec_rel_err(r0, -ax) < 1e-13
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+def test_dg_system_vs_oracle_larger(gb, aniso):
+    """n = 4 (128 prisms, 416 faces), mixed p = 1..4, against the oracle's
+    assembly of the same problem."""
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(4, jitter=0.2, seed=9)
+    F = prism_faces(m)
+    pdeg = np.random.default_rng(9).integers(1, 5, m.nel)
+    k = lognormal_k(m.nel, seed=9)
+    D = anisotropic_tensors(m.nel, seed=9).reshape(m.nel, 9) if aniso else None
+    A = D if aniso else np.array([np.diag([kk] * 3).reshape(-1) for kk in k])
+    c = _context(gb, m, F, pdeg, k=None if aniso else k, D=D, pen=7.5, g=0.4, f=1.3)
+    c.dg_assemble()
+    rp, ci, v, rhs, off = _expand(c)
+    rpo, cio, vo, rhso, offo = O.dg_assemble(m, F, pdeg, A, pen=7.5, g=0.4, f=1.3)
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+    assert sparse_rel_err(rp, ci, v, vo) < REL_TOL
+    assert vec_rel_err(rhs, rhso) < REL_TOL
+
+
+def test_dg_assembly_deterministic(gb):
+    """Every block entry is written by one thread in a fixed order: two
+    assemblies are bit-identical."""
+    from modfem_gb300.mesh import lognormal_k, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(6, jitter=0.2, seed=4)
+    F = prism_faces(m)
+    pdeg = np.random.default_rng(4).integers(1, 5, m.nel)
+    c = _context(gb, m, F, pdeg, k=lognormal_k(m.nel, seed=4), g=0.2)
+    c.dg_assemble()
+    v1, r1 = c.dg_get_matrix()
+    c.dg_assemble()
+    v2, r2 = c.dg_get_matrix()
+    assert np.array_equal(v1, v2) and np.array_equal(r1, r2)
+
+
+@pytest.mark.parametrize("n,pmax", [(12, 4), (40, 2)])
+def test_dg_constant_reproduction_full_size(gb, n, pmax):
+    """Size-independent property of the interior-penalty system: with f = 0
+    and Dirichlet value c the constant function (coefficient c on each
+    element's first monomial, 1) satisfies A x = b exactly, so the block
+    residual vanishes to rounding.  Exercises every volume and face block at
+    sizes the oracle cannot check entry by entry."""
+    from modfem_gb300.mesh import lognormal_k, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(n, jitter=0.2, seed=n)
+    F = prism_faces(m)
+    pdeg = np.random.default_rng(n).integers(1, pmax + 1, m.nel)
+    cval = 0.7
+    c = _context(gb, m, F, pdeg, k=lognormal_k(m.nel, seed=n), g=cval, f=0.0)
+    c.dg_assemble()
+    off = c.dg_get_structure()[0]
+    x = np.zeros(off[-1])
+    x[off[:-1]] = cval
+    r = c.dg_compute_residual(x)
+    vals, rhs = c.dg_get_matrix()
+    assert np.max(np.abs(r)) < 1e-11 * np.max(np.abs(rhs))

@@ -68,3 +68,70 @@ def test_prism_element_math_distorted(hostlib):
         Ko, Ro = O.std_prism_element(X, np.diag([2.5] * 3), 1.0)
         assert mat_rel_err(unpack(K21), Ko) < 1e-13
         assert np.max(np.abs(R - Ro)) <= 1e-13 * np.max(np.abs(Ro))
+
+
+DG_SRC = os.path.join(HERE, "hostcheck", "dg_face_host.cu")
+DG_HDR = os.path.join(HERE, "..", "modfem_gb300", "csrc", "dg_face.cuh")
+DG_LIB = os.path.join(HERE, "hostcheck", "libdg_face_host.so")
+
+
+@pytest.fixture(scope="module")
+def dghost():
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    if not os.path.exists(DG_LIB) or os.path.getmtime(DG_LIB) < max(os.path.getmtime(DG_SRC),
+                                                                     os.path.getmtime(DG_HDR)):
+        subprocess.check_call([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-o", DG_LIB, DG_SRC])
+    L = ctypes.CDLL(DG_LIB)
+    vp = ctypes.c_void_p
+    L.host_dg_face.argtypes = [ctypes.c_int, vp, vp, ctypes.c_int, vp, ctypes.c_int, vp, vp, ctypes.c_int, vp,
+                               ctypes.c_double, ctypes.c_double, vp, vp]
+    return L
+
+
+def _host_face(L, m, F, i, pdeg, A, pen, g):
+    e1, e2 = int(F.el1[i]), int(F.el2[i])
+    fn = F.nodes[i]
+    X1 = np.ascontiguousarray(m.coords[m.el_nodes[e1]]).reshape(-1)
+    l1 = O.face_local_vertices(m.el_nodes[e1], fn)
+    A1 = np.ascontiguousarray(A[e1], dtype=np.float64)
+    p1 = int(pdeg[e1])
+    n = O.lib().orc_dg_nshape(p1)
+    X2 = l2 = A2 = None
+    p2 = 1
+    if e2 >= 0:
+        X2 = np.ascontiguousarray(m.coords[m.el_nodes[e2]]).reshape(-1)
+        l2 = O.face_local_vertices(m.el_nodes[e2], fn)
+        A2 = np.ascontiguousarray(A[e2], dtype=np.float64)
+        p2 = int(pdeg[e2])
+        n += O.lib().orc_dg_nshape(p2)
+    sm = np.zeros(n * n)
+    rhs = np.zeros(n)
+    ptr = lambda a: None if a is None else a.ctypes.data
+    L.host_dg_face(int(F.type[i]), ptr(X1), ptr(l1), p1, ptr(A1), int(F.side1[i]), ptr(X2), ptr(l2), p2, ptr(A2),
+                   pen, g, sm.ctypes.data, rhs.ctypes.data)
+    return sm.reshape(n, n).T.copy(), rhs
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+def test_dg_face_row_form_vs_oracle(dghost, aniso):
+    """The per-owner row form of the DG face kernel against the oracle's
+    term-by-term face integral, every face of a jittered mixed-degree mesh."""
+    from _util import face_rel_err, vec_rel_err
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(3, jitter=0.25, seed=5)
+    F = prism_faces(m)
+    pdeg = np.random.default_rng(5).integers(1, 5, m.nel)
+    if aniso:
+        A = anisotropic_tensors(m.nel, seed=5).reshape(m.nel, 9)
+    else:
+        A = np.array([np.diag([k] * 3).reshape(-1) for k in lognormal_k(m.nel, seed=5)])
+    worst = 0.0
+    for i in range(F.n):
+        K, r = _host_face(dghost, m, F, i, pdeg, A, 10.0, 0.7)
+        Ko, ro = O.dg_face(m, F, i, pdeg, A, pen=10.0, g=0.7)
+        worst = max(worst, face_rel_err(K, Ko))
+        if F.el2[i] < 0:
+            assert vec_rel_err(r, ro) < 1e-13
+    assert worst < 1e-13, worst

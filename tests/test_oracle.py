@@ -134,3 +134,24 @@ def test_dg_faces_vs_reference(name):
         rr = g["fa_rhs"][g["fa_rhs_off"][i]:g["fa_rhs_off"][i + 1]]
         assert face_rel_err(K, Kr) < 1e-14, (i, int(F.type[i]), int(F.el2[i]))
         assert vec_rel_err(r, rr) < 1e-14 if np.any(rr) else not np.any(r), i
+
+
+@pytest.mark.parametrize("name", ["dg_asm_p2", "dg_asm_mixed", "dg_asm_aniso"])
+def test_dg_assembled_system_vs_reference(name):
+    """The whole DG system (elements + interior-penalty and Dirichlet faces,
+    block storage) against the reference MKB solver's lad_block matrix:
+    dof order and block pattern identical, values within 1e-12."""
+    from _util import sparse_rel_err
+    from modfem_gb300.mesh import prism_faces, structured_prism_mesh
+    g = load(name)
+    m = structured_prism_mesh(int(g["n"]), jitter=float(g["jitter"]), seed=int(g["seed"]))
+    assert np.array_equal(m.coords, g["coords"])
+    F = prism_faces(m)
+    A = g["D"].reshape(-1, 9) if g["D"].size else np.array([np.diag([k] * 3).reshape(-1) for k in g["k"]])
+    rp, ci, val, rhs, off = O.dg_assemble(m, F, g["pdeg"], A, pen=float(g["pen"]), g=float(g["g"]),
+                                          f=float(g["f"]))
+    assert np.array_equal(g["dof_ent_id"], np.arange(1, m.nel + 1))
+    assert np.array_equal(g["dof_posglob"], off[:-1])
+    assert np.array_equal(rp, g["row_ptr"]) and np.array_equal(ci, g["col_ind"])
+    assert sparse_rel_err(rp, ci, val, g["val"]) < REL_TOL
+    assert vec_rel_err(rhs, g["rhs"]) < REL_TOL
