@@ -180,37 +180,68 @@ def dg_fma_per_element(p):
     return nq * (9 * ns + 3 * ns * (ns + 1) // 2)
 
 
-def bench_dg(gb, local, steps, fp64_peak):
-    """DG prism volume integrals: 60^3 x 2 = 432,000 p=3 prisms with the
+DG_NQF = {1: (3, 4), 2: (6, 9), 3: (12, 16), 4: (16, 25)}  # face rule points (triangle, quad)
+
+
+def dg_face_fma(F, pdeg):
+    """FP64 FMAs of the face block products: every face contributes its full
+    (ns1+ns2)^2 matrix (both owners' rows) at 2 FMA per entry and point."""
+    ns = np.array([0, 6, 18, 40, 75])
+    p1 = pdeg[F.el1]
+    p2 = np.where(F.el2 >= 0, pdeg[np.maximum(F.el2, 0)], 0)
+    pr = np.maximum(p1, p2)
+    nq = np.array([DG_NQF[int(a)][int(b)] for a, b in zip(pr, (F.type == 4).astype(int))])
+    return float(np.sum(2.0 * nq * (ns[p1] + ns[p2]).astype(float) ** 2))
+
+
+def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
+    """The DG prism system: 60^3 x 2 = 432,000 p=3 prisms with the
     anisotropic tensor R diag(1, 0.1, 0.01) R^T, and 58^3 x 2 = 390,224 prisms
-    with p drawn uniformly from 1..4 and lognormal k (prisms only)."""
-    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, structured_prism_mesh
+    with p drawn uniformly from 1..4 and lognormal k.  A step integrates every
+    element (volume kernel) and every face (interior penalty + Dirichlet,
+    face kernel) into the variable-block matrix.  Then a fixed number of
+    GMRES(50) iterations with block Jacobi (the iteration count to 1e-10 grows
+    with the mesh; the per-iteration cost is the figure of merit)."""
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, prism_faces, structured_prism_mesh
     out = {}
     for name, n, mode in (("p3_anisotropic_432k", 60, "p3"), ("mixed_p1to4_390k", 58, "mixed")):
         m = structured_prism_mesh(n, jitter=0.2, seed=SEED)
+        F = prism_faces(m)
         c = gb.Context(local)
         c.set_mesh(m)
         if mode == "p3":
             pdeg = np.full(m.nel, 3)
-            c.set_coefficients(D=anisotropic_tensors(m.nel, seed=SEED), f=1.0)
+            c.set_coefficients(D=anisotropic_tensors(m.nel, seed=SEED), f=1.0, g=0.0)
         else:
             pdeg = np.random.default_rng(SEED).integers(1, 5, m.nel)
-            c.set_coefficients(k=lognormal_k(m.nel, seed=SEED), f=1.0)
+            c.set_coefficients(k=lognormal_k(m.nel, seed=SEED), f=1.0, g=0.0)
         c.dg_set_degrees(pdeg)
+        c.dg_set_faces(F, penalty=10.0)
         nd, nv = c.dg_build_structure()
         for _ in range(2):
             c.dg_assemble()
-        tot = 0.0
+        tt = np.zeros(3)
         for _ in range(steps):
             c.dg_assemble()
-            a, b, _ = c.last_timing()
-            tot += b
-        ms = tot / steps
-        fma = sum(dg_fma_per_element(p) * int(np.sum(pdeg == p)) for p in range(1, 5))
-        out[name] = {"elements": m.nel, "dofs": nd, "stored_values": nv, "ms": ms,
-                     "elem_per_s": m.nel / (ms * 1e-3),
-                     "fp64_tflops_executed": 2 * fma / (ms * 1e-3) / 1e12,
-                     "fp64_frac": 2 * fma / (ms * 1e-3) / 1e12 / fp64_peak}
+            tt += np.array(c.dg_last_timing()[:3])
+        tot, vol, fa = tt / steps
+        vfma = sum(dg_fma_per_element(p) * int(np.sum(pdeg == p)) for p in range(1, 5))
+        ffma = dg_face_fma(F, pdeg)
+        x, it, res, rel = c.dg_solve(krylov=50, max_iter=gmres_iters, tol_rel=1e-10)
+        st = c.last_solve_timing()
+        spmv_ms = st[1] / max(st[2], 1)
+        inv_bytes = 8 * sum(int(np.sum(pdeg == p)) * [0, 6, 18, 40, 75][p] ** 2 for p in range(1, 5))
+        out[name] = {
+            "elements": m.nel, "faces": int(F.n), "dofs": nd, "stored_values": nv,
+            "assemble_ms": tot, "elem_per_s": m.nel / (tot * 1e-3),
+            "volume_ms": vol, "volume_fp64_frac": 2 * vfma / (vol * 1e-3) / 1e12 / fp64_peak,
+            "face_ms": fa, "face_fp64_frac": 2 * ffma / (fa * 1e-3) / 1e12 / fp64_peak,
+            "gmres_iterations": it, "gmres_rel_residual": rel, "gmres_ms_per_iteration": st[0] / max(it, 1),
+            "spmv_ms": spmv_ms,
+            # the preconditioned block SpMV: matrix + inverted diagonal blocks, one FMA per value
+            "spmv_fp64_frac": 2 * (nv + inv_bytes / 8) / (spmv_ms * 1e-3) / 1e12 / fp64_peak,
+            "spmv_gbs": (8 * nv + inv_bytes + 24 * nd) / (spmv_ms * 1e-3) / 1e9,
+        }
         c.close()
     return out
 

@@ -30,6 +30,20 @@ static int upload(gbfem_ctx c, DevBuf<T> &d, const T *h, size_t n) {
   return 0;
 }
 
+// Block SpMV over all DG block rows, one launch per degree class.
+static int dg_spmv(gbfem_ctx c, int mode, const double *x, const double *b, double *out) {
+  int n = 0;
+  for (int p = 1; p <= 4; p++) {
+    if (!c->dg_list[p].p) continue;
+    const int r = gbfem::launch_dg_block_spmv(c->stream, mode, p, (int)c->dg_list[p].n, c->dg_list[p].p,
+                                              c->dg_roff_d.p, c->dg_row_val_d.p, c->dg_cx_off_d.p, c->dg_colx_d.p,
+                                              c->dg_val.p, c->dg_dinv_off_d.p, c->dg_dinv.p, x, b, out);
+    if (r < 0) return r;
+    n += r;
+  }
+  return n;
+}
+
 extern "C" {
 
 int gbfem_version(void) { return 1; }
@@ -83,6 +97,9 @@ int gbfem_destroy(gbfem_ctx c) {
   c->dg_bptr_d.release();
   c->dg_bcol_d.release();
   c->dg_boff_d.release();
+  c->dg_colx_d.release();
+  c->dg_row_val_d.release();
+  c->dg_cx_off_d.release();
   cudaEventDestroy(c->ev0);
   cudaEventDestroy(c->ev1);
   cudaEventDestroy(c->ev2);
@@ -104,7 +121,8 @@ long long gbfem_device_bytes(gbfem_ctx c) {
   for (auto *b : ibufs) s += b->bytes();
   s += c->dg_val.bytes() + c->dg_rhs.bytes() + c->dg_dinv.bytes() + c->dg_hf.bytes() + c->dg_boff_d.bytes() +
        c->dg_boff_diag_d.bytes() + c->dg_dinv_off_d.bytes() + c->dg_bptr_d.bytes() + c->dg_bcol_d.bytes() +
-       c->dg_hf_ptr.bytes() + c->dg_p_d.bytes() + c->dg_roff_d.bytes();
+       c->dg_hf_ptr.bytes() + c->dg_p_d.bytes() + c->dg_roff_d.bytes() + c->dg_colx_d.bytes() +
+       c->dg_row_val_d.bytes() + c->dg_cx_off_d.bytes();
   for (int p = 0; p < 5; p++) s += c->dg_list[p].bytes();
   return s;
 }
@@ -581,6 +599,24 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
       hf[hfill[h.el2]++] = h;
     }
   }
+  // per block row: value offset, and the dof index of each of its columns
+  std::vector<long long> row_val(nel), cx_off(nel + 1, 0);
+  for (int e = 0; e < nel; e++) {
+    row_val[e] = c->dg_boff[c->dg_bptr[e]];
+    long long nct = 0;
+    for (int k = c->dg_bptr[e]; k < c->dg_bptr[e + 1]; k++) nct += kDgNs[c->dg_p[c->dg_bcol[k]]];
+    cx_off[e + 1] = cx_off[e] + nct;
+  }
+  std::vector<int> colx(cx_off[nel]);
+  for (int e = 0; e < nel; e++) {
+    long long t = cx_off[e];
+    for (int k = c->dg_bptr[e]; k < c->dg_bptr[e + 1]; k++) {
+      const int col = c->dg_bcol[k];
+      for (int j = c->dg_roff[col]; j < c->dg_roff[col + 1]; j++) colx[t++] = j;
+    }
+  }
+  // elements per degree class, ordered by their row's column count so that
+  // the rows a warp multiplies together take the same number of steps
   for (int p = 1; p <= 4; p++) {
     std::vector<int> lst;
     for (int e = 0; e < nel; e++)
@@ -589,8 +625,14 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
       c->dg_list[p].release();
       continue;
     }
+    std::stable_sort(lst.begin(), lst.end(), [&](int a, int b) {
+      return cx_off[a + 1] - cx_off[a] > cx_off[b + 1] - cx_off[b];
+    });
     GB_TRY(upload(c, c->dg_list[p], lst.data(), lst.size()));
   }
+  GB_TRY(upload(c, c->dg_row_val_d, row_val.data(), row_val.size()));
+  GB_TRY(upload(c, c->dg_cx_off_d, cx_off.data(), cx_off.size()));
+  GB_TRY(upload(c, c->dg_colx_d, colx.data(), colx.size()));
   GB_TRY(upload(c, c->dg_roff_d, c->dg_roff.data(), c->dg_roff.size()));
   GB_TRY(upload(c, c->dg_boff_diag_d, diag.data(), diag.size()));
   GB_TRY(upload(c, c->dg_p_d, c->dg_p.data(), c->dg_p.size()));
@@ -706,8 +748,7 @@ int gbfem_dg_compute_residual(gbfem_ctx c, int Use_rhs, int Ini_zero, int Ndof, 
       bd = c->dg_rhs.p;
     }
   }
-  GB_TRY(gbfem::launch_dg_block_spmv(c->stream, 2, c->nel, c->dg_roff_d.p, c->dg_bptr_d.p, c->dg_bcol_d.p,
-                                     c->dg_boff_d.p, c->dg_val.p, nullptr, nullptr, c->x.p, bd, c->tmp.p));
+  GB_TRY(dg_spmv(c, 2, c->x.p, bd, c->tmp.p));
   GB_CUDA(cudaMemcpyAsync(V, c->tmp.p, nb, cudaMemcpyDeviceToHost, c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
@@ -968,9 +1009,7 @@ int gbfem_dg_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int in
   GB_CHECK(herr == 0, "singular diagonal block in the DG block Jacobi preconditioner");
   c->last_solve_kernels = 1;
   GmresOp op = [&](int mode, const double *in, double *out) -> int {
-    return gbfem::launch_dg_block_spmv(st, mode, c->nel, c->dg_roff_d.p, c->dg_bptr_d.p, c->dg_bcol_d.p,
-                                       c->dg_boff_d.p, c->dg_val.p, c->dg_dinv_off_d.p, c->dg_dinv.p, in,
-                                       mode == 0 ? c->dg_rhs.p : nullptr, out);
+    return dg_spmv(c, mode, in, mode == 0 ? c->dg_rhs.p : nullptr, out);
   };
   return gmres_run(c, n, krylov, max_iter, tol_rel, ini_zero, x, res_out, res_rel_out, op);
 }

@@ -26,27 +26,35 @@ __device__ const unsigned char d_dg_exp[GB_DG_PMAX][GB_DG_MAXNS][3] = GB_DG_EXP_
 __device__ const int d_dg_ns[GB_DG_PMAX + 1] = GB_DG_NS_INIT;
 __device__ const int d_dg_nqf[GB_DG_PMAX + 1][2] = GB_DG_NQF_INIT;
 
-constexpr int DGF_THREADS = 256;
 constexpr int DGF_NQ = GB_DG_MAXNQF;  // points of the largest face rule
-constexpr int DGF_GEO = 13;           // e1, e2, v1, v2, a per point
+constexpr int DGF_GEO = 16;           // e1, e2, v1, v2, a, then the owner-row scales
+constexpr int DGF_FAC = 30;           // monomial factors per point and side
 
+// Threads per CTA chosen so that the NS x NS diagonal block (and an off-
+// diagonal block with a neighbour of the same degree) divides evenly or
+// nearly: 36 / 64, 324 / 384 (2 x 192), 1600 / 1600 (5 x 320), 5625 / 5632
+// (22 x 256) entries per thread-slot; the block products are FP64-bound, so
+// idle lanes are lost FP64 issue.
 template <int P>
 struct DgFaceDims {
   static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
+  static constexpr int THREADS = P == 1 ? 64 : P == 2 ? 192 : P == 3 ? 320 : 256;
   static constexpr int NCOL = NS + GB_DG_MAXNS;  // own + neighbour columns
-  static constexpr int PER = (NS * NS + DGF_THREADS - 1) / DGF_THREADS;
-  static constexpr int SMEM_DOUBLES = 2 * DGF_NQ * NS + 2 * DGF_NQ * NCOL + 36 + 18 + DGF_NQ * DGF_GEO + 1;
+  static constexpr int PER = (NS * NS + THREADS - 1) / THREADS;
+  static constexpr int SMEM_DOUBLES =
+      2 * DGF_NQ * NS + 2 * DGF_NQ * NCOL + 36 + 18 + DGF_NQ * DGF_GEO + 2 * DGF_NQ * DGF_FAC + 1;
 };
 
 template <int P>
-__global__ void __launch_bounds__(DGF_THREADS) dg_prism_faces_kernel(
+__global__ void __launch_bounds__(DgFaceDims<P>::THREADS) dg_prism_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
     const double *__restrict__ k_el, const double *__restrict__ D_el, double pen, double gval,
     const long long *__restrict__ boff_diag, const int *__restrict__ roff, double *__restrict__ val,
     double *__restrict__ rhs) {
   using Dm = DgFaceDims<P>;
-  constexpr int NS = Dm::NS, NCOL = Dm::NCOL;
+  constexpr int NS = Dm::NS, NCOL = Dm::NCOL, DGF_THREADS = Dm::THREADS;
+  static_assert(DGF_THREADS >= 54 && DGF_THREADS - 1 >= DGF_NQ, "loader and penalty threads");
   extern __shared__ double smem[];
   double *sL = smem;                       // [DGF_NQ][NS]   owner rows
   double *sM = sL + DGF_NQ * NS;           // [DGF_NQ][NS]
@@ -55,7 +63,8 @@ __global__ void __launch_bounds__(DGF_THREADS) dg_prism_faces_kernel(
   double *sX = sGam + DGF_NQ * NCOL;       // [2][18] vertex coordinates of both sides
   double *sA = sX + 36;                    // [2][9] coefficient tensors
   double *sGeo = sA + 18;                  // [DGF_NQ][DGF_GEO]
-  double *sPen = sGeo + DGF_NQ * DGF_GEO;  // penalty / sqrt(face area)
+  double *sFac = sGeo + DGF_NQ * DGF_GEO;  // [DGF_NQ][2][DGF_FAC]
+  double *sPen = sFac + 2 * DGF_NQ * DGF_FAC;  // penalty / sqrt(face area)
   const int bi = blockIdx.x;
   if (bi >= count) return;
   const int e = ent_el[bi];
@@ -112,21 +121,37 @@ __global__ void __launch_bounds__(DGF_THREADS) dg_prism_faces_kernel(
     }
     __syncthreads();
     const double fac = interior ? 0.5 : 1.0;
-    const double cpen = sPen[0];
     const int nsum = ns1 + ns2;
+    // monomial factors per (point, side); the owner-row scales per point:
+    // L = alpha g + beta phi, M = gamma phi (alpha = f a, beta = s_o c a,
+    // gamma = -s_o f a)
+    for (int t = tid; t < 2 * nq; t += DGF_THREADS) {
+      const int q = t >> 1, sd = t & 1;
+      if (sd == 1 && !interior) continue;
+      const double *G = sGeo + q * DGF_GEO;
+      dg_point_factors(v3{G[3 * sd], G[3 * sd + 1], G[3 * sd + 2]}, v3{G[6 + 3 * sd], G[7 + 3 * sd], G[8 + 3 * sd]},
+                       sFac + (2 * q + sd) * DGF_FAC);
+      if (sd == 0) {
+        const double aw = G[12], so = own2 ? -1.0 : 1.0;
+        sGeo[q * DGF_GEO + 13] = fac * aw;
+        sGeo[q * DGF_GEO + 14] = so * sPen[0] * aw;
+        sGeo[q * DGF_GEO + 15] = -so * fac * aw;
+      }
+    }
+    __syncthreads();
     for (int t = tid; t < nq * nsum; t += DGF_THREADS) {
       const int q = t / nsum, j = t - q * nsum;
       const int side = j < ns1 ? 1 : 2, jj = side == 1 ? j : j - ns1, p = side == 1 ? p1 : p2;
       const unsigned char *ex = d_dg_exp[p - 1][jj];
-      const double *G = sGeo + q * DGF_GEO + (side == 1 ? 0 : 3);
-      double L, M, Phi, Gam;
-      dg_face_values(ex[0], ex[1], ex[2], side, v3{G[0], G[1], G[2]}, v3{G[6], G[7], G[8]},
-                     sGeo[q * DGF_GEO + 12], fac, cpen, L, M, Phi, Gam);
-      sPhi[q * NCOL + j] = Phi;
-      sGam[q * NCOL + j] = Gam;
+      double phi, g;
+      dg_basis_from_factors(sFac + (2 * q + side - 1) * DGF_FAC, ex[0], ex[1], ex[2], phi, g);
+      // Phi = s_t phi: the sign flip on the integer side, not the FP64 pipe
+      sPhi[q * NCOL + j] = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
+      sGam[q * NCOL + j] = g;
       if ((side == 2) == (own2 != 0)) {
-        sL[q * NS + jj] = L;
-        sM[q * NS + jj] = M;
+        const double *G = sGeo + q * DGF_GEO;
+        sL[q * NS + jj] = fma(G[13], g, G[14] * phi);
+        sM[q * NS + jj] = G[15] * phi;
       }
     }
     __syncthreads();
@@ -179,8 +204,8 @@ int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, 
     const size_t smem = sizeof(double) * DgFaceDims<PP>::SMEM_DOUBLES;                                           \
     GB_CUDA(cudaFuncSetAttribute(dg_prism_faces_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,        \
                                  (int)smem));                                                                    \
-    dg_prism_faces_kernel<PP><<<count, DGF_THREADS, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, xyz, \
-                                                                k_el, D_el, pen, g, boff_diag, roff, val, rhs);  \
+    dg_prism_faces_kernel<PP><<<count, DgFaceDims<PP>::THREADS, smem, st>>>(count, ent_el, hf_ptr, hf, el_p,   \
+        el_nodes, xyz, k_el, D_el, pen, g, boff_diag, roff, val, rhs);                                           \
   }
   switch (p) {
     case 1: GB_DGF_LAUNCH(1); break;

@@ -85,27 +85,30 @@ int dg_tables_for_device(int device, DgDeviceTables **out) {
   return 0;
 }
 
-constexpr int DG_THREADS = 256;
 constexpr int DG_QCHUNK = 8;
 
+// Threads per CTA so that the NS(NS+1)/2 upper entries fill the thread slots
+// (21 / 32, 171 / 192, 820 / 864 = 3 x 288, 2850 / 2880 = 10 x 288): the
+// accumulation is FP64-bound and idle lanes are lost FP64 issue.
 template <int P>
 struct DgDims {
   static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
   static constexpr int NQ = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 48 : 80;
+  static constexpr int THREADS = P == 1 ? 32 : P == 2 ? 192 : 288;
   static constexpr int NSYM = NS * (NS + 1) / 2;
-  static constexpr int PER_THREAD = (NSYM + DG_THREADS - 1) / DG_THREADS;
+  static constexpr int PER_THREAD = (NSYM + THREADS - 1) / THREADS;
 };
 
 // Elements of degree P: ent_el[i] (0-based), matrix block at val + boff[e],
 // rhs rows at rhs + roff[e].  A (tensor, 9 per element) or k (isotropic).
 template <int P>
-__global__ void __launch_bounds__(DG_THREADS) dg_prism_elements_kernel(
+__global__ void __launch_bounds__(DgDims<P>::THREADS) dg_prism_elements_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
     const double *__restrict__ k_el, const double *__restrict__ D_el, double f, const double *__restrict__ Dtab,
     const double *__restrict__ PHItab, const double *__restrict__ QPtab, const long long *__restrict__ boff,
     const int *__restrict__ roff, double *__restrict__ val, double *__restrict__ rhs) {
   using Dm = DgDims<P>;
-  constexpr int NS = Dm::NS, NQ = Dm::NQ;
+  constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS;
   __shared__ double sG[NQ][6];        // w/|det| C^T A C (symmetric, packed 00 01 02 11 12 22)
   __shared__ double sV[NQ];           // w |det|
   __shared__ double sT[DG_QCHUNK][3][NS];
@@ -241,7 +244,7 @@ int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, cons
   int r = dg_tables_for_device(device, &tb);
   if (r < 0) return r;
 #define GB_DG_LAUNCH(PP)                                                                                 \
-  dg_prism_elements_kernel<PP><<<count, DG_THREADS, 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, \
+  dg_prism_elements_kernel<PP><<<count, DgDims<PP>::THREADS, 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, \
                                                              tb->D[PP], tb->PHI[PP], tb->QP[PP], boff, roff, \
                                                              val, rhs)
   switch (p) {

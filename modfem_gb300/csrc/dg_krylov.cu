@@ -112,83 +112,124 @@ int launch_dg_block_inverse(cudaStream_t st, int nel, const int *roff, const lon
   return 1;
 }
 
-// One warp per block row: lane l accumulates rows l, l+32, l+64 (ns <= 75);
-// every block column j is a coalesced load of ns consecutive values.  With a
-// preconditioner the row block's result goes through shared memory into the
-// product with the inverted diagonal block.
-constexpr int DGS_WARPS = 8;
+// One 8-lane group per block row (32 block rows per CTA), launched per
+// degree class so that the row block size NS is a compile-time constant:
+// lane g accumulates rows g, g+8, ... (40 rows = 5 full slots for p = 3, 75 =
+// 10 slots of which the last is 3/8 full for p = 4).  On GB300 the SpMV is
+// bound by the FP64 pipe as much as by HBM (one FMA per 8-byte value against
+// ~0.6 T FMA/s), so lanes must not idle: a warp per row would leave 24 of 64
+// lane slots empty for NS = 40.
+//
+// The blocks of a row are consecutive and column-major with leading dimension
+// NS, so the whole block row is one NS x nct column-major matrix starting at
+// the row's first block; colx lists the dof index of each of its nct columns.
+// One flat loop over the columns (instead of blocks, then columns) keeps the
+// four groups of a warp in step when their neighbours differ in degree; the
+// rows of a class are ordered by nct for the same reason.  With a
+// preconditioner the group's rows go through shared memory into the product
+// with the inverted diagonal block.
+constexpr int DGS_LANES = 8;
+constexpr int DGS_THREADS = 256;
+constexpr int DGS_ROWS = DGS_THREADS / DGS_LANES;
 
-__global__ void __launch_bounds__(DGS_WARPS * 32) dg_block_spmv_kernel(
-    int mode, int nel, const int *__restrict__ roff, const int *__restrict__ bptr, const int *__restrict__ bcol,
-    const long long *__restrict__ boff, const double *__restrict__ val, const long long *__restrict__ dinv_off,
-    const double *__restrict__ dinv, const double *__restrict__ x, const double *__restrict__ b,
-    double *__restrict__ out) {
-  __shared__ double sv[DGS_WARPS][GB_DG_MAXNS];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int e = blockIdx.x * DGS_WARPS + warp;
-  if (e >= nel) return;  // whole warp
-  const int r0 = roff[e], ns = roff[e + 1] - r0;
-  const int i0 = lane, i1 = lane + 32, i2 = lane + 64;
-  const bool v0 = i0 < ns, v1 = i1 < ns, v2 = i2 < ns;
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  for (int k = bptr[e]; k < bptr[e + 1]; k++) {
-    const int c = bcol[k], c0 = roff[c], nc = roff[c + 1] - c0;
-    const double *blk = val + boff[k];
-    const double *xc = x + c0;
-    int j = 0;
-    for (; j + 2 <= nc; j += 2) {
-      const double x0 = xc[j], x1 = xc[j + 1];
-      const double *col0 = blk + (size_t)j * ns, *col1 = col0 + ns;
-      if (v0) a0 = fma(col1[i0], x1, fma(col0[i0], x0, a0));
-      if (v1) a1 = fma(col1[i1], x1, fma(col0[i1], x0, a1));
-      if (v2) a2 = fma(col1[i2], x1, fma(col0[i2], x0, a2));
+template <int P>
+__global__ void __launch_bounds__(DGS_THREADS) dg_block_spmv_kernel(
+    int mode, int count, const int *__restrict__ ent_el, const int *__restrict__ roff,
+    const long long *__restrict__ row_val, const long long *__restrict__ cx_off, const int *__restrict__ colx,
+    const double *__restrict__ val, const long long *__restrict__ dinv_off, const double *__restrict__ dinv,
+    const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ out) {
+  constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
+  constexpr int S = (NS + DGS_LANES - 1) / DGS_LANES;
+  __shared__ double sv[DGS_ROWS][NS];
+  const int grp = threadIdx.x / DGS_LANES, g = threadIdx.x % DGS_LANES;
+  const int idx = blockIdx.x * DGS_ROWS + grp;
+  const bool active = idx < count;
+  const int e = active ? ent_el[idx] : 0;
+  const int r0 = roff[e];
+  double acc[S];
+#pragma unroll
+  for (int s = 0; s < S; s++) acc[s] = 0.0;
+  if (active) {
+    const double *A = val + row_val[e] + g;
+    const int *cx = colx + cx_off[e];
+    const int nct = (int)(cx_off[e + 1] - cx_off[e]);
+    int t = 0;
+    for (; t + 2 <= nct; t += 2) {
+      const double x0 = x[cx[t]], x1 = x[cx[t + 1]];
+      const double *col0 = A + (size_t)t * NS, *col1 = col0 + NS;
+#pragma unroll
+      for (int s = 0; s < S; s++)
+        if (g + DGS_LANES * s < NS) acc[s] = fma(col1[DGS_LANES * s], x1, fma(col0[DGS_LANES * s], x0, acc[s]));
     }
-    if (j < nc) {
-      const double x0 = xc[j];
-      const double *col0 = blk + (size_t)j * ns;
-      if (v0) a0 = fma(col0[i0], x0, a0);
-      if (v1) a1 = fma(col0[i1], x0, a1);
-      if (v2) a2 = fma(col0[i2], x0, a2);
+    if (t < nct) {
+      const double x0 = x[cx[t]];
+      const double *col0 = A + (size_t)t * NS;
+#pragma unroll
+      for (int s = 0; s < S; s++)
+        if (g + DGS_LANES * s < NS) acc[s] = fma(col0[DGS_LANES * s], x0, acc[s]);
     }
   }
   if (mode != 1) {
-    a0 = (b && v0 ? b[r0 + i0] : 0.0) - a0;
-    a1 = (b && v1 ? b[r0 + i1] : 0.0) - a1;
-    a2 = (b && v2 ? b[r0 + i2] : 0.0) - a2;
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+      const int i = g + DGS_LANES * s;
+      acc[s] = (b && active && i < NS ? b[r0 + i] : 0.0) - acc[s];
+    }
   }
   if (mode == 2) {
-    if (v0) out[r0 + i0] = a0;
-    if (v1) out[r0 + i1] = a1;
-    if (v2) out[r0 + i2] = a2;
+    if (active) {
+#pragma unroll
+      for (int s = 0; s < S; s++) {
+        const int i = g + DGS_LANES * s;
+        if (i < NS) out[r0 + i] = acc[s];
+      }
+    }
     return;
   }
-  if (v0) sv[warp][i0] = a0;
-  if (v1) sv[warp][i1] = a1;
-  if (v2) sv[warp][i2] = a2;
-  __syncwarp();
-  const double *D = dinv + dinv_off[e];
-  double o0 = 0.0, o1 = 0.0, o2 = 0.0;
-  for (int j = 0; j < ns; j++) {
-    const double t = sv[warp][j];
-    const double *col = D + (size_t)j * ns;
-    if (v0) o0 = fma(col[i0], t, o0);
-    if (v1) o1 = fma(col[i1], t, o1);
-    if (v2) o2 = fma(col[i2], t, o2);
+#pragma unroll
+  for (int s = 0; s < S; s++) {
+    const int i = g + DGS_LANES * s;
+    if (i < NS) sv[grp][i] = acc[s];
   }
-  if (v0) out[r0 + i0] = o0;
-  if (v1) out[r0 + i1] = o1;
-  if (v2) out[r0 + i2] = o2;
+  __syncwarp();
+  if (!active) return;
+  const double *D = dinv + dinv_off[e] + g;
+  double o[S];
+#pragma unroll
+  for (int s = 0; s < S; s++) o[s] = 0.0;
+  for (int j = 0; j < NS; j++) {
+    const double t = sv[grp][j];
+    const double *col = D + (size_t)j * NS;
+#pragma unroll
+    for (int s = 0; s < S; s++)
+      if (g + DGS_LANES * s < NS) o[s] = fma(col[DGS_LANES * s], t, o[s]);
+  }
+#pragma unroll
+  for (int s = 0; s < S; s++) {
+    const int i = g + DGS_LANES * s;
+    if (i < NS) out[r0 + i] = o[s];
+  }
 }
 
-int launch_dg_block_spmv(cudaStream_t st, int mode, int nel, const int *roff, const int *bptr, const int *bcol,
-                         const long long *boff, const double *val, const long long *dinv_off, const double *dinv,
-                         const double *x, const double *b, double *out) {
-  if (nel <= 0) return 0;
+int launch_dg_block_spmv(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
+                         const long long *row_val, const long long *cx_off, const int *colx, const double *val,
+                         const long long *dinv_off, const double *dinv, const double *x, const double *b,
+                         double *out) {
+  if (count <= 0) return 0;
   GB_CHECK(mode >= 0 && mode <= 2, "bad block SpMV mode");
+  GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
   GB_CHECK(mode == 2 || (dinv && dinv_off), "block SpMV needs the inverted diagonal blocks");
-  const int grid = (nel + DGS_WARPS - 1) / DGS_WARPS;
-  dg_block_spmv_kernel<<<grid, DGS_WARPS * 32, 0, st>>>(mode, nel, roff, bptr, bcol, boff, val, dinv_off, dinv, x,
-                                                        b, out);
+  const int grid = (count + DGS_ROWS - 1) / DGS_ROWS;
+#define GB_DGS_LAUNCH(PP)                                                                                  \
+  dg_block_spmv_kernel<PP><<<grid, DGS_THREADS, 0, st>>>(mode, count, ent_el, roff, row_val, cx_off, colx, \
+                                                         val, dinv_off, dinv, x, b, out)
+  switch (p) {
+    case 1: GB_DGS_LAUNCH(1); break;
+    case 2: GB_DGS_LAUNCH(2); break;
+    case 3: GB_DGS_LAUNCH(3); break;
+    default: GB_DGS_LAUNCH(4); break;
+  }
+#undef GB_DGS_LAUNCH
   GB_CUDA(cudaGetLastError());
   return 1;
 }

@@ -124,10 +124,13 @@ int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, 
 int launch_dg_block_inverse(cudaStream_t st, int nel, const int *roff, const long long *boff_diag,
                             const double *val, const long long *dinv_off, double *dinv, int *err);
 // mode 0: out = Minv (b - A x) (b may be NULL), 1: out = Minv A x,
-// 2: out = (b ? b : 0) - A x (Minv unused)
-int launch_dg_block_spmv(cudaStream_t st, int mode, int nel, const int *roff, const int *bptr, const int *bcol,
-                         const long long *boff, const double *val, const long long *dinv_off, const double *dinv,
-                         const double *x, const double *b, double *out);
+// 2: out = (b ? b : 0) - A x (Minv unused); rows of the count elements of
+// degree p listed in ent_el.  row_val[e]: value offset of block row e (its
+// blocks are consecutive); colx[cx_off[e] ..]: dof index of each column.
+int launch_dg_block_spmv(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
+                         const long long *row_val, const long long *cx_off, const int *colx, const double *val,
+                         const long long *dinv_off, const double *dinv, const double *x, const double *b,
+                         double *out);
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                              const double *xyz, const double *k_el, const double *D_el, double f,
                              const long long *boff, const int *roff, double *val, double *rhs);
@@ -186,8 +189,8 @@ struct gbfem_ctx_s {
   // DG block Jacobi: inverted diagonal blocks, block e at dg_dinv_off_d[e]
   gbfem::DevBuf<double> dg_dinv;
   gbfem::DevBuf<long long> dg_dinv_off_d;
-  gbfem::DevBuf<int> dg_bptr_d, dg_bcol_d;
-  gbfem::DevBuf<long long> dg_boff_d;
+  gbfem::DevBuf<int> dg_bptr_d, dg_bcol_d, dg_colx_d;
+  gbfem::DevBuf<long long> dg_boff_d, dg_row_val_d, dg_cx_off_d;
   // timing
   float last_ms = 0.f, last_el_ms = 0.f, last_fa_ms = 0.f, last_solve_ms = 0.f, last_spmv_ms = 0.f;
   int last_spmv_count = 0, last_solve_kernels = 0;
