@@ -255,6 +255,64 @@ int gbfem_host_free(void *ptr);
  * FP64-bound integration kernels). */
 int gbfem_measure_fp64_peak(gbfem_ctx ctx, double *tflops);
 
+/* ---------------------------------------------------------------------- */
+/* serving (no counterpart in the reference)                                */
+/* ---------------------------------------------------------------------- */
+/* A server takes independent heat problems as they arrive and integrates,
+ * assembles and solves them on one GPU with continuous batching: requests
+ * are admitted FIFO while a slot is free and their device footprint fits in
+ * the HBM budget; worker threads upload, build, integrate and assemble each
+ * admitted request on its own stream while the engine thread advances all
+ * requests in the solve phase together, one GMRES iteration per step with
+ * batched kernels and the GMRES scalar logic on the device.  A request's
+ * result does not depend on the other requests in the mix (bit-identical
+ * alone and together).  The numerics per request are those of
+ * gbfem_assemble + gbfem_solve (std) and gbfem_dg_assemble + gbfem_dg_solve
+ * (DG): same assembly, same GMRES(krylov) with (block) Jacobi, stopping on the
+ * preconditioned residual relative to the initial one. */
+#define GBFEM_SERVE_STD 0
+#define GBFEM_SERVE_DG 1
+typedef struct gbfem_server_s *gbfem_server;
+typedef struct {
+  int kind;               /* GBFEM_SERVE_STD or GBFEM_SERVE_DG */
+  int dg_p;               /* DG degree of every element (1..4) */
+  int nno;                /* nodes, node_xyz[3 nno] */
+  const double *node_xyz;
+  int nel;                /* prisms, el_nodes[6 nel] (0-based) */
+  const int *el_nodes;
+  const double *k_el;     /* isotropic coefficient per element */
+  double f, g;            /* source, Dirichlet value */
+  int nbf;                /* std: Dirichlet boundary faces (element, side) */
+  const int *bf_el, *bf_side;
+  int nfa;                /* DG: face table as gbfem_dg_set_faces */
+  const int *fa_type, *fa_bc, *fa_el, *fa_side, *fa_nodes;
+  double dg_penalty;      /* <= 0: 10 */
+  int krylov, max_iter;   /* GMRES(krylov), krylov <= 64 */
+  double tol_rel;
+} gbfem_serve_request;
+/* hbm_budget <= 0: 85% of the free device memory; max_active: requests in
+ * preparation or solve at once (<= 64); prep_threads: host workers. */
+int gbfem_server_create(gbfem_server *srv, int device, long long hbm_budget, int max_active, int prep_threads);
+/* Finishes the requests being prepared or solved, drops the queued ones. */
+int gbfem_server_destroy(gbfem_server srv);
+/* Copies the request's inputs; returns its id (>= 0) or < 0. */
+long long gbfem_server_submit(gbfem_server srv, const gbfem_serve_request *req);
+/* 1 finished, 0 timed out (timeout_s < 0 waits without limit), < 0 failed. */
+int gbfem_server_wait(gbfem_server srv, long long id, double timeout_s);
+/* Solution (dof order of the library's structure), GMRES iterations,
+ * relative preconditioned residual and times[5] in seconds: queued,
+ * preparation, waiting for a solve slot, solve, submit-to-done latency.
+ * Returns the solution length. */
+int gbfem_server_result(gbfem_server srv, long long id, double *x, long long nx, int *iters, double *rel_res,
+                        double *times);
+/* Forgets a finished request's result. */
+int gbfem_server_release(gbfem_server srv, long long id);
+/* stats[8]: engine steps, kernel launches, peak active requests, peak
+ * bytes charged, budget, bytes charged now, queued, active. */
+int gbfem_server_stats(gbfem_server srv, long long *stats);
+/* Device bytes a request is charged at admission (host estimate). */
+long long gbfem_serve_footprint(const gbfem_serve_request *req);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,14 @@ SIGNATURES = [
     ("gbfem_host_alloc", _vp, [_cll]),
     ("gbfem_host_free", _ci, [_vp]),
     ("gbfem_measure_fp64_peak", _ci, [_vp, _pd]),
+    ("gbfem_server_create", _ci, [_pvp, _ci, _cll, _ci, _ci]),
+    ("gbfem_server_destroy", _ci, [_vp]),
+    ("gbfem_server_submit", _cll, [_vp, _vp]),
+    ("gbfem_server_wait", _ci, [_vp, _cll, _cd]),
+    ("gbfem_server_result", _ci, [_vp, _cll, _vp, _cll, _pi, _pd, _vp]),
+    ("gbfem_server_release", _ci, [_vp, _cll]),
+    ("gbfem_server_stats", _ci, [_vp, _vp]),
+    ("gbfem_serve_footprint", _cll, [_vp]),
 ]
 
 _LIB = None

@@ -12,6 +12,7 @@
 // here as the explicit inverse of each diagonal block: applying it is then a
 // dense block product fused into the SpMV.
 
+#include "dg_spmv.cuh"
 #include "dg_tables.h"
 #include "gbfem_internal.h"
 
@@ -112,103 +113,14 @@ int launch_dg_block_inverse(cudaStream_t st, int nel, const int *roff, const lon
   return 1;
 }
 
-// One 8-lane group per block row (32 block rows per CTA), launched per
-// degree class so that the row block size NS is a compile-time constant:
-// lane g accumulates rows g, g+8, ... (40 rows = 5 full slots for p = 3, 75 =
-// 10 slots of which the last is 3/8 full for p = 4).  On GB300 the SpMV is
-// bound by the FP64 pipe as much as by HBM (one FMA per 8-byte value against
-// ~0.6 T FMA/s), so lanes must not idle: a warp per row would leave 24 of 64
-// lane slots empty for NS = 40.
-//
-// The blocks of a row are consecutive and column-major with leading dimension
-// NS, so the whole block row is one NS x nct column-major matrix starting at
-// the row's first block; colx lists the dof index of each of its nct columns.
-// One flat loop over the columns (instead of blocks, then columns) keeps the
-// four groups of a warp in step when their neighbours differ in degree; the
-// rows of a class are ordered by nct for the same reason.  With a
-// preconditioner the group's rows go through shared memory into the product
-// with the inverted diagonal block.
-constexpr int DGS_LANES = 8;
-constexpr int DGS_THREADS = 256;
-constexpr int DGS_ROWS = DGS_THREADS / DGS_LANES;
-
 template <int P>
 __global__ void __launch_bounds__(DGS_THREADS) dg_block_spmv_kernel(
     int mode, int count, const int *__restrict__ ent_el, const int *__restrict__ roff,
     const long long *__restrict__ row_val, const long long *__restrict__ cx_off, const int *__restrict__ colx,
     const double *__restrict__ val, const long long *__restrict__ dinv_off, const double *__restrict__ dinv,
     const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ out) {
-  constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
-  constexpr int S = (NS + DGS_LANES - 1) / DGS_LANES;
-  __shared__ double sv[DGS_ROWS][NS];
-  const int grp = threadIdx.x / DGS_LANES, g = threadIdx.x % DGS_LANES;
-  const int idx = blockIdx.x * DGS_ROWS + grp;
-  const bool active = idx < count;
-  const int e = active ? ent_el[idx] : 0;
-  const int r0 = roff[e];
-  double acc[S];
-#pragma unroll
-  for (int s = 0; s < S; s++) acc[s] = 0.0;
-  if (active) {
-    const double *A = val + row_val[e] + g;
-    const int *cx = colx + cx_off[e];
-    const int nct = (int)(cx_off[e + 1] - cx_off[e]);
-    int t = 0;
-    for (; t + 2 <= nct; t += 2) {
-      const double x0 = x[cx[t]], x1 = x[cx[t + 1]];
-      const double *col0 = A + (size_t)t * NS, *col1 = col0 + NS;
-#pragma unroll
-      for (int s = 0; s < S; s++)
-        if (g + DGS_LANES * s < NS) acc[s] = fma(col1[DGS_LANES * s], x1, fma(col0[DGS_LANES * s], x0, acc[s]));
-    }
-    if (t < nct) {
-      const double x0 = x[cx[t]];
-      const double *col0 = A + (size_t)t * NS;
-#pragma unroll
-      for (int s = 0; s < S; s++)
-        if (g + DGS_LANES * s < NS) acc[s] = fma(col0[DGS_LANES * s], x0, acc[s]);
-    }
-  }
-  if (mode != 1) {
-#pragma unroll
-    for (int s = 0; s < S; s++) {
-      const int i = g + DGS_LANES * s;
-      acc[s] = (b && active && i < NS ? b[r0 + i] : 0.0) - acc[s];
-    }
-  }
-  if (mode == 2) {
-    if (active) {
-#pragma unroll
-      for (int s = 0; s < S; s++) {
-        const int i = g + DGS_LANES * s;
-        if (i < NS) out[r0 + i] = acc[s];
-      }
-    }
-    return;
-  }
-#pragma unroll
-  for (int s = 0; s < S; s++) {
-    const int i = g + DGS_LANES * s;
-    if (i < NS) sv[grp][i] = acc[s];
-  }
-  __syncwarp();
-  if (!active) return;
-  const double *D = dinv + dinv_off[e] + g;
-  double o[S];
-#pragma unroll
-  for (int s = 0; s < S; s++) o[s] = 0.0;
-  for (int j = 0; j < NS; j++) {
-    const double t = sv[grp][j];
-    const double *col = D + (size_t)j * NS;
-#pragma unroll
-    for (int s = 0; s < S; s++)
-      if (g + DGS_LANES * s < NS) o[s] = fma(col[DGS_LANES * s], t, o[s]);
-  }
-#pragma unroll
-  for (int s = 0; s < S; s++) {
-    const int i = g + DGS_LANES * s;
-    if (i < NS) out[r0 + i] = o[s];
-  }
+  __shared__ double sv[DGS_ROWS][DgSpmvDims<P>::NS];
+  dg_block_row_spmv<P>(mode, count, ent_el, roff, row_val, cx_off, colx, val, dinv_off, dinv, x, b, out, sv);
 }
 
 int launch_dg_block_spmv(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
