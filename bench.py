@@ -246,6 +246,78 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
     return out
 
 
+def bench_serving(gb, local, rates=(50, 200, 1000, 2000), per_rate=48):
+    """The serving workload: a Poisson stream of independent heat problems,
+    each a structured prism mesh of n^3 hexahedra x 2 with n log-uniform in
+    [10, 60], lognormal(0,1) k, f = 1, solved by GMRES(30) to 1e-8.  Half the
+    requests are std linear; the other half DG with p in {1, 2}, whose n is
+    drawn from [10, 20] (GMRES(30) with block Jacobi needs more than 3,000
+    iterations, seconds per request, beyond that).  Beside the engine: the
+    plain one-at-a-time path (gbfem Context per request: upload, structure,
+    assemble, solve) with its measured service times queued FIFO on the same
+    arrival times."""
+    from modfem_gb300.mesh import lognormal_k, prism_faces, structured_prism_mesh
+    from modfem_gb300.serve import DG, STD, Problem, Server, poisson_stream
+    rng = np.random.default_rng(SEED)
+    pool = []
+    for i in range(12):
+        kind = STD if i % 2 == 0 else DG
+        hi = 60 if kind == STD else 20
+        n = int(round(np.exp(rng.uniform(np.log(10), np.log(hi)))))
+        p = 1 if i % 4 == 1 else 2
+        m = structured_prism_mesh(n, jitter=0.2, seed=1000 + i)
+        k = lognormal_k(m.nel, seed=2000 + i)
+        F = prism_faces(m) if kind == DG else None
+        pool.append((m, k, F, Problem(m, k, kind=kind, p=p, faces=F, krylov=30, max_iter=20000, tol=1e-8)))
+    # plain one-at-a-time service times
+    service = []
+    for (m, k, F, pr) in pool:
+        t0 = time.perf_counter()
+        c = gb.Context(local)
+        c.set_mesh(m)
+        c.set_coefficients(k=k, f=1.0, g=0.0)
+        if pr.kind == DG:
+            c.dg_set_degrees(np.full(m.nel, pr.p))
+            c.dg_set_faces(F, penalty=10.0)
+            c.dg_build_structure()
+            c.dg_assemble()
+            c.dg_solve(krylov=30, max_iter=20000, tol_rel=1e-8)
+        else:
+            c.build_structure()
+            c.assemble()
+            c.solve(krylov=30, max_iter=20000, tol_rel=1e-8)
+        c.close()
+        service.append(time.perf_counter() - t0)
+    srv = Server(local, max_active=32, prep_threads=4)
+    out = {"requests_per_rate": per_rate, "pool": [{"kind": "std" if pr.kind == STD else f"dg_p{pr.p}",
+                                                     "elements": int(m.nel)} for (m, _, _, pr) in pool],
+           "rates": []}
+    try:
+        poisson_stream(srv, [pr for (_, _, _, pr) in pool], 1000.0, 12, seed=1)  # warm-up
+        for rate in rates:
+            res, span = poisson_stream(srv, [pr for (_, _, _, pr) in pool], rate, per_rate, seed=rate)
+            lat = np.array([r["latency"] for r in res])
+            big = np.array([r["latency"] for r in res if r["nel"] >= 80000 and r["kind"] == STD])
+            # the plain path on the same arrivals
+            arr = np.cumsum(np.random.default_rng(rate).exponential(1.0 / rate, per_rate))
+            fin, plain = 0.0, []
+            for i in range(per_rate):
+                fin = max(arr[i], fin) + service[i % len(pool)]
+                plain.append(fin - arr[i])
+            plain = np.array(plain)
+            out["rates"].append({
+                "rate_req_s": rate, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                "p99_ms": 1e3 * float(np.percentile(lat, 99)), "problems_per_s": per_rate / span,
+                "p99_ms_std_over_80k_elements": 1e3 * float(np.percentile(big, 99)) if big.size else None,
+                "plain_one_at_a_time": {"p50_ms": 1e3 * float(np.percentile(plain, 50)),
+                                        "p99_ms": 1e3 * float(np.percentile(plain, 99)),
+                                        "problems_per_s": per_rate / (max(fin, arr[-1]))}})
+        out["engine"] = srv.stats()
+    finally:
+        srv.close()
+    return out
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -362,8 +434,11 @@ def main():
               "spmv_ms": spmv_ms / max(nspmv, 1), "spmv_gbs": spmv_bytes * nspmv / (spmv_ms * 1e-3) / 1e9,
               "spmv_bytes": spmv_bytes, "relative_residual_after": rel, "kernel_launches": solve_kernels}
 
-    # ---------------- DG prism volume integrals ----------------
+    # ---------------- DG prism system ----------------
     dg = bench_dg(gb, local, max(3, min(args.steps, 10)), fp64_peak)
+
+    # ---------------- serving ----------------
+    serving = bench_serving(gb, local) if rank == 0 else None
 
     # ---------------- CPU baseline (rank 0, N=1 only) ----------------
     cpu = None
@@ -400,6 +475,7 @@ def main():
         "clocks": clocks,
         "solver": solver,
         "dg": dg,
+        "serving": serving,
         "gpu_launches": launches,
         "wall_s_timed_region": wall,
     }
