@@ -307,6 +307,11 @@ int gbfem_server_result(gbfem_server srv, long long id, double *x, long long nx,
                         double *times);
 /* Forgets a finished request's result. */
 int gbfem_server_release(gbfem_server srv, long long id);
+/* GBFEM_SERVE_OPT_STEPS_PER_POLL: engine steps launched between two host
+ * reads of the requests' phases (1..64, default 4): fewer host round trips
+ * against up to that many idle steps for a request that has finished. */
+#define GBFEM_SERVE_OPT_STEPS_PER_POLL 1
+int gbfem_server_set_option(gbfem_server srv, int option, long long value);
 /* stats[8]: engine steps, kernel launches, peak active requests, peak
  * bytes charged, budget, bytes charged now, queued, active. */
 int gbfem_server_stats(gbfem_server srv, long long *stats);

@@ -405,6 +405,7 @@ struct gbfem_server_s {
   int peak_active = 0;
   cudaGraphExec_t graph = nullptr;
   int graph_kernels = 0;
+  int steps_per_poll = 4;
   std::string fatal;
 };
 
@@ -745,9 +746,15 @@ void engine_loop(gbfem_server s) {
       return;
     }
     if (s->act.empty()) continue;
-    s->steps++;
-    s->launches += s->graph_kernels;
-    if (cudaGraphLaunch(s->graph, s->stream) != cudaSuccess ||
+    // several steps per host poll: a finished request's kernels are no-ops
+    // until it is retired, so the extra steps only cost their launch
+    cudaError_t ge = cudaSuccess;
+    for (int k = 0; k < s->steps_per_poll && ge == cudaSuccess; k++) {
+      ge = cudaGraphLaunch(s->graph, s->stream);
+      s->steps++;
+      s->launches += s->graph_kernels;
+    }
+    if (ge != cudaSuccess ||
         cudaMemcpyAsync(s->h_state, s->d_state.p, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaMemcpyDeviceToHost,
                         s->stream) != cudaSuccess ||
         cudaStreamSynchronize(s->stream) != cudaSuccess) {
@@ -954,6 +961,18 @@ int gbfem_server_release(gbfem_server s, long long id) {
   GB_CHECK(it->second->status == 4 || it->second->status < 0, "request not finished");
   s->reqs.erase(it);
   return 0;
+}
+
+int gbfem_server_set_option(gbfem_server s, int option, long long value) {
+  GB_CHECK(s, "null server");
+  if (option == GBFEM_SERVE_OPT_STEPS_PER_POLL) {
+    GB_CHECK(value >= 1 && value <= 64, "steps per poll must be 1..64");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->steps_per_poll = (int)value;
+    return 0;
+  }
+  gbfem::set_error("unknown server option");
+  return -2;
 }
 
 int gbfem_server_stats(gbfem_server s, long long *st) {

@@ -64,12 +64,14 @@ class Problem:
 
 
 class Server:
-    def __init__(self, device=0, hbm_budget=0, max_active=32, prep_threads=4):
+    def __init__(self, device=0, hbm_budget=0, max_active=32, prep_threads=4, steps_per_poll=None):
         self.L = load_library()
         h = ctypes.c_void_p()
         self._check(self.L.gbfem_server_create(ctypes.byref(h), device, int(hbm_budget), max_active, prep_threads))
         self._h = h
         self._lock = threading.Lock()
+        if steps_per_poll is not None:
+            self._check(self.L.gbfem_server_set_option(self._h, 1, int(steps_per_poll)))
 
     def _check(self, r):
         if r < 0:
