@@ -155,6 +155,14 @@ int gbfem_dg_set_degrees(gbfem_ctx ctx, const int *p_el);
  * Without a face table only volume terms are assembled. */
 int gbfem_dg_set_faces(gbfem_ctx ctx, int nfa, const int *fa_type, const int *fa_bc, const int *fa_el,
                        const int *fa_side, const int *fa_nodes);
+/* Volume-integral kernel (no reference counterpart; both give the reference's
+ * element matrices to FP64 accuracy): GBFEM_DG_VOLUME_FP64 (FP64 pipe) or
+ * GBFEM_DG_VOLUME_TC, the tensor cores with split BF16 products (ten 6-bit
+ * slices per operand, exact FP32 slice sums, FP64 recombination; p = 1..3,
+ * p = 4 elements keep the FP64 kernel). */
+#define GBFEM_DG_VOLUME_FP64 0
+#define GBFEM_DG_VOLUME_TC 1
+int gbfem_dg_set_volume_kernel(gbfem_ctx ctx, int mode);
 /* Interior-penalty factor, pdr_ctrl_d_params(problem, 12) in the DG weak
  * form (pds_conv_diff_weakform_dg.c:516-531); default 10. */
 int gbfem_dg_set_penalty(gbfem_ctx ctx, double penalty);

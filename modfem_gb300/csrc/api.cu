@@ -501,6 +501,13 @@ int gbfem_dg_set_faces(gbfem_ctx c, int nfa, const int *fa_type, const int *fa_b
   return 0;
 }
 
+int gbfem_dg_set_volume_kernel(gbfem_ctx c, int mode) {
+  GB_CHECK(c, "null context");
+  GB_CHECK(mode == GBFEM_DG_VOLUME_FP64 || mode == GBFEM_DG_VOLUME_TC, "unknown DG volume kernel");
+  c->dg_volume_mode = mode;
+  return 0;
+}
+
 int gbfem_dg_set_penalty(gbfem_ctx c, double pen) {
   GB_CHECK(c, "null context");
   GB_CHECK(pen > 0.0, "penalty must be positive");
@@ -670,12 +677,20 @@ int gbfem_dg_assemble(gbfem_ctx c) {
   int launches = 0;
   // volume terms write every diagonal block and the rhs; the face kernel then
   // adds to those and writes every off-diagonal block: nothing to clear
+  const bool tc = c->dg_volume_mode == GBFEM_DG_VOLUME_TC;
+  if (tc) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
   cudaEventRecord(c->ev0, c->stream);
   for (int p = 1; p <= 4; p++) {
     if (!c->dg_list[p].p) continue;
-    int r = gbfem::launch_dg_prism_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
-                                            c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,
-                                            c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
+    int r;
+    if (tc && gbfem::dg_tc_supported(p))
+      r = gbfem::launch_dg_tc_volume(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->el_nodes.p,
+                                     c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->dg_boff_diag_d.p, c->dg_roff_d.p,
+                                     c->dg_val.p, c->dg_rhs.p, c->err.p);
+    else
+      r = gbfem::launch_dg_prism_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
+                                          c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,
+                                          c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
     GB_TRY(r);
     launches += r;
   }
@@ -696,6 +711,11 @@ int gbfem_dg_assemble(gbfem_ctx c) {
   cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
   cudaEventElapsedTime(&c->last_el_ms, c->ev0, c->ev2);
   cudaEventElapsedTime(&c->last_fa_ms, c->ev2, c->ev1);
+  if (tc) {
+    int herr = 0;
+    GB_CUDA(cudaMemcpy(&herr, c->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    GB_CHECK(herr == 0, "tensor-core volume kernel: a pipeline wait expired");
+  }
   c->last_launches = launches;
   return 0;
 }

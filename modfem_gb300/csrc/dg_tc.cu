@@ -1,0 +1,530 @@
+// DG prism volume integrals on the tensor cores (tcgen05, sm_103a) with
+// FP64-equivalent results: split BF16 products.
+//
+// The element matrix of apr_num_int_el (apd_dg_prism/aps_dg_prism_intf.c:
+// 1239-1728) is a fixed linear map of per-point geometry:
+//   K_uw = sum_q sum_ab D_q[a][u] G_q[a][b] D_q[b][w]
+//        = sum_k E[(u,w)][k] g_e[k],   k = (q, ab), ab in {00,01,02,11,12,22}
+// with E (upper entries x 6 nq) constant per degree and g_e = the 6 entries
+// of G_q = (w_q / |det J|) C^T A C at every point (FP64, as the FP64 kernel
+// forms them).  For a batch of elements this is one GEMM K = E g.
+//
+// Precision (Ozaki-style splitting): E (per row) and g_e (per element) are
+// scaled by powers of two into [-1, 1) and cut into SL = 10 truncation slices
+// of 6 bits, each an integer in [-63, 63] held exactly in BF16:
+//   E = rs_r sum_i es_i 2^{-6(i+1)},  g = cs_e sum_j gs_j 2^{-6(j+1)}.
+// The products of slices are exact in the FP32 tensor accumulator: every
+// partial sum is an integer below 10 * 288 * 63^2 < 2^24.  Pairs with the same
+// i + j = d share an accumulator C_d (d = 0..9; pairs with i + j > 9 are
+// dropped), and
+//   K = rs_r cs_e sum_d C_d 2^{-6(d+2)}
+// is recombined exactly in int64 (two 49-bit partial sums) and rounded once to
+// FP64.  Measured on the oracle's elements: within 6e-15 of the FP64 element
+// matrices in the energy scale used by the parity tests.
+//
+// Kernel: one CTA per 32 elements, 256 threads.
+//  A. FP64: geometry per (element, point) -> G (registers), per-element max
+//     exponent, integer slicing of g into SL BF16 slices in shared memory
+//     (the tcgen05 canonical K-major layout), and the load vector.
+//  B. tcgen05: for each 128-row tile of E, its slices stream from global
+//     memory (pre-arranged in the canonical layout) through a 3-stage
+//     shared-memory ring by bulk-async copies (TMA engine) with mbarrier
+//     transaction counts; one thread issues tcgen05.mma (M 128, N 32, K 16,
+//     BF16 x BF16 -> FP32) into SL TMEM accumulators (SL x 32 columns).
+//  C. epilogue per tile: tcgen05.ld of the SL accumulators, int64
+//     recombination, FP64 scaling, both symmetric positions of the diagonal
+//     block written.
+// Every wait has an iteration limit; on expiry the CTA records an error,
+// drains the copies and MMAs it issued (also with a limit), frees its TMEM
+// and returns.
+
+#include <cuda_bf16.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "dg_tables.h"
+#include "gbfem_internal.h"
+
+namespace gbfem {
+
+constexpr int TC_SL = 10;       // slices per operand
+constexpr int TC_BITS = 6;      // bits per slice
+constexpr int TC_NE = 32;       // elements per CTA (MMA N)
+constexpr int TC_M = 128;       // MMA M (rows of E per tile)
+constexpr int TC_KC = 48;       // K per streamed chunk (3 MMAs of K 16)
+constexpr int TC_STAGES = 3;
+constexpr int TC_THREADS = 256;
+constexpr int TC_TMEM_COLS = 512;  // >= TC_SL * TC_NE, power of two
+constexpr long long TC_WAIT_LIMIT = 1LL << 26;
+
+template <int P>
+struct TcDims {
+  static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
+  static constexpr int NQ = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 48 : 80;
+  static constexpr int NSYM = NS * (NS + 1) / 2;
+  static constexpr int KDIM = 6 * NQ;
+  static constexpr int KPAD = (KDIM + TC_KC - 1) / TC_KC * TC_KC;
+  static constexpr int NKC = KPAD / TC_KC;
+  static constexpr int MT = (NSYM + TC_M - 1) / TC_M;
+  static constexpr int GSL_BYTES = TC_SL * TC_NE * KPAD * 2;    // G slices
+  static constexpr int CHUNK_BYTES = TC_M * TC_KC * 2;          // one E chunk
+  static constexpr int RING_BYTES = TC_STAGES * CHUNK_BYTES;
+  static constexpr int SMEM = GSL_BYTES + RING_BYTES + 256;     // + scales, barriers
+  // exactness of the FP32 accumulation: at most TC_SL slice pairs per
+  // accumulator, products of integers below 2^6
+  static_assert((long long)TC_SL * KPAD * 63 * 63 < (1LL << 24), "slice sums must stay exact in FP32");
+};
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  // tcgen05 shared-memory matrix descriptor, no swizzle (canonical K-major
+  // layout of 8-row x 16-byte core matrices)
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ bool tc_try_wait(uint32_t mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+  for (long long it = 0; it < TC_WAIT_LIMIT; it++)
+    if (tc_try_wait(mbar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tc_bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_ld8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// byte offset of (row, k) in the canonical no-swizzle K-major layout of a
+// rows x kdim operand: core matrix (row/8, k/8) at row/8 * SBO + k/8 * 128
+__host__ __device__ __forceinline__ int tc_off(int row, int k, int kdim) {
+  return (row >> 3) * (kdim / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+
+// 2^e as a double built from its bit pattern (normal range)
+__device__ __forceinline__ double tc_pow2(int e) {
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+// exponent E with |x| < 2^E for x != 0 (from the FP64 bit pattern)
+__device__ __forceinline__ int tc_exp_above(double x) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  return ex == 0 ? -1100 : ex - 1022;  // |x| < 2^(ex - 1022) for normal x
+}
+
+// ------------------------------------------------------------------ kernel
+template <int P>
+__global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
+    int count, const int *__restrict__ ent_el, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
+    const double *__restrict__ k_el, const double *__restrict__ D_el, double f, const double *__restrict__ QPtab,
+    const double *__restrict__ PHItab, const __nv_bfloat16 *__restrict__ Etc, const int *__restrict__ rowexp,
+    const int2 *__restrict__ uw, const long long *__restrict__ boff, const int *__restrict__ roff,
+    double *__restrict__ val, double *__restrict__ rhs, int *err) {
+  using Dm = TcDims<P>;
+  constexpr int NS = Dm::NS, NQ = Dm::NQ, KPAD = Dm::KPAD, NKC = Dm::NKC, MT = Dm::MT;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t *gsl = smem;                             // [TC_SL][TC_NE x KPAD] bf16, canonical layout
+  uint8_t *ring = smem + Dm::GSL_BYTES;            // [TC_STAGES][TC_M x TC_KC] bf16
+  int *sexp = (int *)(ring + Dm::RING_BYTES);      // per-element exponent
+  uint64_t *bars = (uint64_t *)(sexp + TC_NE);     // full[3], empty[3], acc
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 1);
+  int *abort_flag = (int *)(tmem_slot + 1);
+  // phase-A staging inside the ring (unused until phase B)
+  double *sxa = (double *)ring;                    // [TC_NE][27]: 18 coordinates, 9 tensor entries
+  double *svol = sxa + TC_NE * 27;                 // [TC_NE][NQ]: w |det|
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int e0 = blockIdx.x * TC_NE;
+  const int nel_here = min(TC_NE, count - e0);
+
+  // ---------------- phase A: geometry, slices of g, load vector ----------------
+  for (int t = tid; t < TC_NE * 27; t += TC_THREADS) {
+    const int el = t / 27, c = t % 27;
+    double v = 0.0;
+    if (el < nel_here) {
+      const int e = ent_el[e0 + el];
+      if (c < 18) {
+        v = xyz[3 * (size_t)el_nodes[6 * (size_t)e + c / 3] + c % 3];
+      } else {
+        const int r = c - 18;
+        v = D_el ? D_el[9 * (size_t)e + r] : ((r % 4 == 0) ? (k_el ? k_el[e] : 1.0) : 0.0);
+      }
+    }
+    sxa[t] = v;
+  }
+  if (tid < TC_NE) sexp[tid] = -1100;
+  if (tid == 0) {
+    for (int i = 0; i < 2 * TC_STAGES + 1; i++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(bars + i)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *abort_flag = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
+                 "r"(TC_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  __syncthreads();
+  constexpr int ITEMS = (TC_NE * NQ + TC_THREADS - 1) / TC_THREADS;
+  double g[ITEMS][6];
+#pragma unroll
+  for (int t = 0; t < ITEMS; t++) {
+    const int it = tid + t * TC_THREADS;
+    const int el = it / NQ, q = it % NQ;
+#pragma unroll
+    for (int c = 0; c < 6; c++) g[t][c] = 0.0;
+    if (it < TC_NE * NQ && el < nel_here) {
+      const double *X = sxa + el * 27, *A = X + 18;
+      const double xi = QPtab[4 * q], eta = QPtab[4 * q + 1], zeta = QPtab[4 * q + 2], w = QPtab[4 * q + 3];
+      const double lo = (1.0 - zeta) / 2.0, hi = (1.0 + zeta) / 2.0, l0 = 1.0 - xi - eta;
+      const double dx[6] = {-lo, lo, 0.0, -hi, hi, 0.0};
+      const double dy[6] = {-lo, 0.0, lo, -hi, 0.0, hi};
+      const double dz[6] = {-0.5 * l0, -0.5 * xi, -0.5 * eta, 0.5 * l0, 0.5 * xi, 0.5 * eta};
+      double j1[3] = {0, 0, 0}, j2[3] = {0, 0, 0}, j3[3] = {0, 0, 0};
+#pragma unroll
+      for (int i = 0; i < 6; i++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          j1[d] = fma(dx[i], X[3 * i + d], j1[d]);
+          j2[d] = fma(dy[i], X[3 * i + d], j2[d]);
+          j3[d] = fma(dz[i], X[3 * i + d], j3[d]);
+        }
+      double cb[3][3];
+      cb[0][0] = j2[1] * j3[2] - j2[2] * j3[1]; cb[0][1] = j2[2] * j3[0] - j2[0] * j3[2]; cb[0][2] = j2[0] * j3[1] - j2[1] * j3[0];
+      cb[1][0] = j3[1] * j1[2] - j3[2] * j1[1]; cb[1][1] = j3[2] * j1[0] - j3[0] * j1[2]; cb[1][2] = j3[0] * j1[1] - j3[1] * j1[0];
+      cb[2][0] = j1[1] * j2[2] - j1[2] * j2[1]; cb[2][1] = j1[2] * j2[0] - j1[0] * j2[2]; cb[2][2] = j1[0] * j2[1] - j1[1] * j2[0];
+      const double adet = fabs(fma(j1[0], cb[0][0], fma(j1[1], cb[0][1], j1[2] * cb[0][2])));
+      const double s = w / adet;
+      double Ac[3][3];
+#pragma unroll
+      for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int r = 0; r < 3; r++) Ac[b][r] = fma(A[3 * r], cb[b][0], fma(A[3 * r + 1], cb[b][1], A[3 * r + 2] * cb[b][2]));
+      // G_ab = s c_a . (A c_b), packed 00 01 02 11 12 22
+      const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+      for (int c = 0; c < 6; c++) {
+        const int a = pa[c], b = pb[c];
+        g[t][c] = s * fma(cb[a][0], Ac[b][0], fma(cb[a][1], Ac[b][1], cb[a][2] * Ac[b][2]));
+      }
+      svol[el * NQ + q] = w * adet;
+      int em = -1100;
+#pragma unroll
+      for (int c = 0; c < 6; c++)
+        if (g[t][c] != 0.0) em = max(em, tc_exp_above(g[t][c]));
+      atomicMax(sexp + el, em);
+    }
+  }
+  __syncthreads();
+  // slices: y = |g| 2^-E in [0, 1) as a 60-bit fixed-point integer, 6 bits per slice
+#pragma unroll
+  for (int t = 0; t < ITEMS; t++) {
+    const int it = tid + t * TC_THREADS;
+    if (it >= TC_NE * NQ) continue;
+    const int el = it / NQ, q = it % NQ;
+    const int E = sexp[el];
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+      const double v = g[t][c];
+      const long long bits = __double_as_longlong(v);
+      const int ex = (int)((bits >> 52) & 0x7FF);
+      // |v| = m 2^(ex - 1075) with m the 53-bit mantissa; fixed = |v| 2^(60 - E)
+      unsigned long long fixed = 0;
+      if (ex != 0) {
+        const unsigned long long m = (bits & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+        const int sh = ex - 1075 + 60 - E;  // left shift of m
+        if (sh >= 0)
+          fixed = sh < 11 ? m << sh : 0ULL;  // |v| < 2^E keeps m << sh below 2^60
+        else if (sh > -64)
+          fixed = m >> (-sh);
+      }
+      const bool neg = bits < 0;
+      const int k = 6 * q + c;
+#pragma unroll
+      for (int i = 0; i < TC_SL; i++) {
+        int chunk = (int)((fixed >> (60 - TC_BITS * (i + 1))) & 63ULL);
+        if (neg) chunk = -chunk;
+        *(__nv_bfloat16 *)(gsl + i * (TC_NE * KPAD * 2) + tc_off(el, k, KPAD)) = __int2bfloat16_rn(chunk);
+      }
+    }
+  }
+  // zero the padding of K (k >= 6 NQ) in every slice
+  if constexpr (Dm::KDIM < KPAD)
+    for (int t = tid; t < TC_SL * TC_NE * (KPAD - Dm::KDIM); t += TC_THREADS) {
+      const int i = t / (TC_NE * (KPAD - Dm::KDIM)), r = t % (TC_NE * (KPAD - Dm::KDIM));
+      const int el = r / (KPAD - Dm::KDIM), k = Dm::KDIM + r % (KPAD - Dm::KDIM);
+      *(__nv_bfloat16 *)(gsl + i * (TC_NE * KPAD * 2) + tc_off(el, k, KPAD)) = __int2bfloat16_rn(0);
+    }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  // load vector R_u = f sum_q phi_u(q) w |det|
+  for (int t = tid; t < nel_here * NS; t += TC_THREADS) {
+    const int el = t / NS, u = t % NS;
+    double r = 0.0;
+    for (int q = 0; q < NQ; q++) r = fma(PHItab[(size_t)q * NS + u], svol[el * NQ + q], r);
+    rhs[roff[ent_el[e0 + el]] + u] = f * r;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();  // the ring is free for the E chunks
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  // ---------------- phases B and C, one 128-row tile of E at a time ----------------
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_NE >> 3) << 17) |
+                         ((uint32_t)(TC_M >> 4) << 24);
+  const uint32_t full0 = tc_smem(bars), empty0 = tc_smem(bars + TC_STAGES), accb = tc_smem(bars + 2 * TC_STAGES);
+  const int T = MT * TC_SL * NKC;  // chunks, in (tile, slice i, k chunk) order
+  auto chunk_src = [&](int t) { return Etc + (size_t)t * (TC_M * TC_KC); };
+  int issued = 0, mma_done = 0;  // chunks copied / consumed (thread 0)
+  if (tid == 0)
+    for (; issued < TC_STAGES && issued < T; issued++)
+      tc_bulk_load(tc_smem(ring + issued * Dm::CHUNK_BYTES), chunk_src(issued), Dm::CHUNK_BYTES,
+                   full0 + 8 * issued);
+  for (int m = 0; m < MT; m++) {
+    if (tid == 0) {
+      for (int i = 0; i < TC_SL && !*abort_flag; i++) {
+        for (int kc = 0; kc < NKC; kc++) {
+          const int t = mma_done, s = t % TC_STAGES;
+          if (!tc_wait(full0 + 8 * s, (t / TC_STAGES) & 1)) {
+            *abort_flag = 1;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t abase = tc_smem(ring + s * Dm::CHUNK_BYTES);
+          for (int j = 0; j < TC_SL - i; j++) {
+            const int d = i + j;
+            const uint32_t bbase = tc_smem(gsl + j * (TC_NE * KPAD * 2));
+#pragma unroll
+            for (int ks = 0; ks < TC_KC / 16; ks++) {
+              const uint64_t ad = tc_desc(abase + ks * 256, 128, (TC_KC / 8) * 128);
+              const uint64_t bd = tc_desc(bbase + ((kc * TC_KC + 16 * ks) / 8) * 128, 128, (KPAD / 8) * 128);
+              tc_mma(tmem + d * TC_NE, ad, bd, idesc, (i == 0 && kc == 0 && ks == 0) ? 0u : 1u);
+            }
+          }
+          tc_commit(empty0 + 8 * s);
+          mma_done++;
+          // refill the stage of the previous chunk (its MMAs are queued ahead
+          // of this chunk's, so the tensor pipe keeps working meanwhile)
+          if (t >= 1 && issued < T) {
+            const int tp = t - 1, sp = tp % TC_STAGES;
+            if (!tc_wait(empty0 + 8 * sp, (tp / TC_STAGES) & 1)) {
+              *abort_flag = 1;
+              break;
+            }
+            tc_bulk_load(tc_smem(ring + sp * Dm::CHUNK_BYTES), chunk_src(issued), Dm::CHUNK_BYTES, full0 + 8 * sp);
+            issued++;
+          }
+        }
+      }
+      tc_commit(accb);  // also when aborting: drains every MMA issued so far
+    }
+    __syncthreads();
+    const bool waited = tc_wait(accb, m & 1);
+    if (__syncthreads_or(!waited || *abort_flag)) {
+      if (tid == 0) {
+        atomicExch(err, 5);
+        // let the copies still in flight land before the CTA leaves
+        for (int t = mma_done; t < issued; t++) tc_wait(full0 + 8 * (t % TC_STAGES), (t / TC_STAGES) & 1);
+      }
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // epilogue: warp -> TMEM lane quarter (rows) and element half (columns)
+    const int lq = warp & 3, half = warp >> 2;
+    const int r = m * TC_M + lq * 32 + (tid & 31);
+    const bool row_ok = r < Dm::NSYM;
+    const int2 pw = row_ok ? uw[r] : make_int2(0, 0);
+    const int rexp = row_ok ? rowexp[r] : 0;
+#pragma unroll
+    for (int grp = 0; grp < TC_NE / 16; grp++) {
+      const int c0 = half * (TC_NE / 2) + grp * 8;
+      float C[TC_SL][8];
+#pragma unroll
+      for (int d = 0; d < TC_SL; d++)
+        tc_ld8(tmem + ((uint32_t)(lq * 32) << 16) + d * TC_NE + c0, C[d]);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        const int el = c0 + c;
+        if (!row_ok || el >= nel_here) continue;
+        // sum_d C_d 2^(-6(d+2)) = hi 2^-36 + lo 2^-66 with hi = C_0..C_4 and
+        // lo = C_5..C_9 in base 64 (each below 2^49: exact in int64 and FP64)
+        long long hi = 0, lo = 0;
+#pragma unroll
+        for (int d = 0; d < TC_SL / 2; d++) hi = hi * 64 + (long long)__float2int_rn(C[d][c]);
+#pragma unroll
+        for (int d = TC_SL / 2; d < TC_SL; d++) lo = lo * 64 + (long long)__float2int_rn(C[d][c]);
+        const int sc = rexp + sexp[el];  // row and element scale exponents
+        const double v = fma((double)lo, tc_pow2(sc - 66), (double)hi * tc_pow2(sc - 36));
+        double *blk = val + boff[ent_el[e0 + el]];
+        blk[pw.y + NS * pw.x] = v;
+        if (pw.x != pw.y) blk[pw.x + NS * pw.y] = v;
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+  }
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
+}
+
+// ------------------------------------------------------------------ host side
+struct TcTables {
+  __nv_bfloat16 *E = nullptr;  // slices in chunk order (tile, slice, k chunk), canonical layout
+  int *rowexp = nullptr;       // row scale exponent: |E[r][k]| < 2^rowexp[r]
+  int2 *uw = nullptr;          // packed upper entry -> (u, w)
+  double *QP = nullptr, *PHI = nullptr;
+};
+static TcTables g_tc[64][GB_DG_PMAX + 1];
+static bool g_tc_ready[64][GB_DG_PMAX + 1];
+static std::mutex g_tc_mu;
+
+template <int P>
+static int tc_build_tables(int device, TcTables &T) {
+  using Dm = TcDims<P>;
+  constexpr int NS = Dm::NS, NQ = Dm::NQ, KPAD = Dm::KPAD, NKC = Dm::NKC, MT = Dm::MT;
+  // reference derivative table D[q][a][u] and values PHI[q][u] of the monomial basis
+  std::vector<double> D((size_t)NQ * 3 * NS), PHI((size_t)NQ * NS), QP((size_t)NQ * 4);
+  for (int q = 0; q < NQ; q++) {
+    const double *e = GB_DG_QP[P - 1][q];
+    for (int k = 0; k < 4; k++) QP[q * 4 + k] = e[k];
+    double px[8], py[8], pz[8];
+    px[0] = py[0] = pz[0] = 1.0;
+    for (int i = 1; i <= P; i++) {
+      px[i] = px[i - 1] * e[0];
+      py[i] = py[i - 1] * e[1];
+      pz[i] = pz[i - 1] * e[2];
+    }
+    for (int u = 0; u < NS; u++) {
+      const int a = GB_DG_EXP[P - 1][u][0], b = GB_DG_EXP[P - 1][u][1], c = GB_DG_EXP[P - 1][u][2];
+      PHI[(size_t)q * NS + u] = px[a] * py[b] * pz[c];
+      D[((size_t)q * 3 + 0) * NS + u] = a ? a * px[a - 1] * py[b] * pz[c] : 0.0;
+      D[((size_t)q * 3 + 1) * NS + u] = b ? b * px[a] * py[b - 1] * pz[c] : 0.0;
+      D[((size_t)q * 3 + 2) * NS + u] = c ? c * px[a] * py[b] * pz[c - 1] : 0.0;
+    }
+  }
+  const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+  std::vector<int2> uw(MT * TC_M, make_int2(0, 0));
+  std::vector<int> rexp(MT * TC_M, 0);
+  std::vector<__nv_bfloat16> E((size_t)MT * TC_SL * NKC * TC_M * TC_KC, __float2bfloat16(0.0f));
+  std::vector<double> row(KPAD);
+  int r = 0;
+  for (int u = 0; u < NS; u++)
+    for (int w = u; w < NS; w++, r++) {
+      uw[r] = make_int2(u, w);
+      double mx = 0.0;
+      for (int k = 0; k < KPAD; k++) {
+        double v = 0.0;
+        if (k < Dm::KDIM) {
+          const int q = k / 6, c = k % 6, a = pa[c], b = pb[c];
+          const double *Dq = D.data() + (size_t)q * 3 * NS;
+          v = a == b ? Dq[a * NS + u] * Dq[a * NS + w] : Dq[a * NS + u] * Dq[b * NS + w] + Dq[b * NS + u] * Dq[a * NS + w];
+        }
+        row[k] = v;
+        mx = std::max(mx, std::fabs(v));
+      }
+      int ex = 0;
+      if (mx > 0) {
+        std::frexp(mx, &ex);  // mx < 2^ex
+      }
+      rexp[r] = ex;
+      const int m = r / TC_M, rr = r % TC_M;
+      for (int k = 0; k < KPAD; k++) {
+        double y = std::fabs(row[k]) * std::ldexp(1.0, -ex);  // [0, 1)
+        const bool neg = row[k] < 0;
+        const int kc = k / TC_KC, kk = k % TC_KC;
+        for (int i = 0; i < TC_SL; i++) {
+          y *= 64.0;
+          const double t = std::floor(y);
+          y -= t;
+          const size_t chunk = ((size_t)m * TC_SL + i) * NKC + kc;
+          E[chunk * TC_M * TC_KC + tc_off(rr, kk, TC_KC) / 2] = __float2bfloat16((float)(neg ? -t : t));
+        }
+      }
+    }
+  GB_CUDA(cudaMalloc(&T.E, E.size() * sizeof(__nv_bfloat16)));
+  GB_CUDA(cudaMalloc(&T.rowexp, rexp.size() * sizeof(int)));
+  GB_CUDA(cudaMalloc(&T.uw, uw.size() * sizeof(int2)));
+  GB_CUDA(cudaMalloc(&T.QP, QP.size() * sizeof(double)));
+  GB_CUDA(cudaMalloc(&T.PHI, PHI.size() * sizeof(double)));
+  GB_CUDA(cudaMemcpy(T.E, E.data(), E.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(T.rowexp, rexp.data(), rexp.size() * sizeof(int), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(T.uw, uw.data(), uw.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(T.QP, QP.data(), QP.size() * sizeof(double), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(T.PHI, PHI.data(), PHI.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+bool dg_tc_supported(int p) { return p >= 1 && p <= 3; }
+
+int launch_dg_tc_volume(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
+                        const double *xyz, const double *k_el, const double *D_el, double f, const long long *boff,
+                        const int *roff, double *val, double *rhs, int *err) {
+  if (count <= 0) return 0;
+  GB_CHECK(dg_tc_supported(p), "tensor-core DG volume kernel covers p = 1..3");
+  GB_CHECK(device >= 0 && device < 64, "device index out of range");
+  {
+    std::lock_guard<std::mutex> lk(g_tc_mu);
+    if (!g_tc_ready[device][p]) {
+      int r = p == 1 ? tc_build_tables<1>(device, g_tc[device][p])
+                     : p == 2 ? tc_build_tables<2>(device, g_tc[device][p]) : tc_build_tables<3>(device, g_tc[device][p]);
+      if (r < 0) return r;
+      g_tc_ready[device][p] = true;
+    }
+  }
+  const TcTables &T = g_tc[device][p];
+  const int grid = (count + TC_NE - 1) / TC_NE;
+#define GB_TC_LAUNCH(PP)                                                                                     \
+  {                                                                                                          \
+    const int smem = TcDims<PP>::SMEM;                                                                       \
+    GB_CUDA(cudaFuncSetAttribute(dg_tc_volume_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
+    dg_tc_volume_kernel<PP><<<grid, TC_THREADS, smem, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, T.QP,  \
+                                                            T.PHI, T.E, T.rowexp, T.uw, boff, roff, val, rhs, err); \
+  }
+  switch (p) {
+    case 1: GB_TC_LAUNCH(1); break;
+    case 2: GB_TC_LAUNCH(2); break;
+    default: GB_TC_LAUNCH(3); break;
+  }
+#undef GB_TC_LAUNCH
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
+}  // namespace gbfem

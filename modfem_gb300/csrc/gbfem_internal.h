@@ -131,6 +131,11 @@ int launch_dg_block_spmv(cudaStream_t st, int mode, int p, int count, const int 
                          const long long *row_val, const long long *cx_off, const int *colx, const double *val,
                          const long long *dinv_off, const double *dinv, const double *x, const double *b,
                          double *out);
+// Tensor-core (tcgen05, split BF16) DG volume integrals, FP64-equivalent.
+bool dg_tc_supported(int p);
+int launch_dg_tc_volume(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
+                        const double *xyz, const double *k_el, const double *D_el, double f, const long long *boff,
+                        const int *roff, double *val, double *rhs, int *err);
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                              const double *xyz, const double *k_el, const double *D_el, double f,
                              const long long *boff, const int *roff, double *val, double *rhs);
@@ -184,6 +189,7 @@ struct gbfem_ctx_s {
   std::vector<int> dg_fa_type, dg_fa_bc, dg_fa_el, dg_fa_side, dg_fa_nodes;
   int dg_nfa = -1;  // -1: no face table (volume terms only)
   double dg_pen = 10.0;
+  int dg_volume_mode = 0;  // GBFEM_DG_VOLUME_FP64 / _TC
   gbfem::DevBuf<int> dg_hf_ptr, dg_p_d;
   gbfem::DevBuf<gbfem::DgHalfFace> dg_hf;
   // DG block Jacobi: inverted diagonal blocks, block e at dg_dinv_off_d[e]

@@ -149,3 +149,50 @@ def test_dg_constant_reproduction_full_size(gb, n, pmax):
     r = c.dg_compute_residual(x)
     vals, rhs = c.dg_get_matrix()
     assert np.max(np.abs(r)) < 1e-11 * np.max(np.abs(rhs))
+
+
+@pytest.mark.parametrize("name", ["dg_asm_p2", "dg_asm_aniso"])
+def test_dg_tensor_core_volume_vs_reference(gb, name):
+    """The tensor-core volume kernel (split BF16 products, FP64 recombination)
+    gives the reference's system to the same FP64 tolerance (p = 4 elements of
+    the mixed mesh stay on the FP64 kernel)."""
+    g, m, F = _fixture_problem(name)
+    D = _tensors(g)
+    c = _context(gb, m, F, g["pdeg"], k=None if D is not None else g["k"], D=D, pen=float(g["pen"]),
+                 g=float(g["g"]), f=float(g["f"]))
+    c.dg_set_volume_kernel(gb.DG_VOLUME_TC)
+    c.dg_assemble()
+    rp, ci, v, rhs, off = _expand(c)
+    assert np.array_equal(rp, g["row_ptr"]) and np.array_equal(ci, g["col_ind"])
+    assert sparse_rel_err(rp, ci, v, g["val"]) < REL_TOL
+    assert vec_rel_err(rhs, g["rhs"]) < REL_TOL
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_dg_tensor_core_volume_vs_fp64_kernel(gb, p):
+    """Element blocks of the tensor-core kernel against the FP64 kernel on a
+    jittered anisotropic mesh with more elements than one CTA batch."""
+    from modfem_gb300.mesh import anisotropic_tensors, structured_prism_mesh
+    m = structured_prism_mesh(5, jitter=0.25, seed=p + 40)
+    D = anisotropic_tensors(m.nel, seed=p + 40).reshape(m.nel, 9)
+    out = []
+    for mode in (gb.DG_VOLUME_FP64, gb.DG_VOLUME_TC):
+        c = gb.Context(0)
+        c.set_mesh(m)
+        c.set_coefficients(D=D, f=1.3)
+        c.dg_set_degrees(np.full(m.nel, p))
+        c.dg_build_structure()
+        c.dg_set_volume_kernel(mode)
+        c.dg_assemble()
+        out.append(c.dg_get_matrix())
+        off, bptr, bcol, boff = c.dg_get_structure()
+        c.close()
+    from _util import mat_rel_err
+    ns = [0, 6, 18, 40, 75][p]
+    worst = 0.0
+    for e in range(m.nel):
+        K64 = out[0][0][boff[e]:boff[e] + ns * ns].reshape(ns, ns)
+        Ktc = out[1][0][boff[e]:boff[e] + ns * ns].reshape(ns, ns)
+        worst = max(worst, mat_rel_err(Ktc, K64))
+    assert worst < 1e-13, worst
+    assert vec_rel_err(out[1][1], out[0][1]) < 1e-14
