@@ -225,6 +225,19 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
             c.dg_assemble()
             tt += np.array(c.dg_last_timing()[:3])
         tot, vol, fa = tt / steps
+        v64, r64 = c.dg_get_matrix()
+        # the same assembly with the tensor-core volume kernel (split BF16)
+        c.dg_set_volume_kernel(gb.DG_VOLUME_TC)
+        c.dg_assemble()
+        tt = np.zeros(3)
+        for _ in range(steps):
+            c.dg_assemble()
+            tt += np.array(c.dg_last_timing()[:3])
+        tot_tc, vol_tc, _ = tt / steps
+        vtc, rtc = c.dg_get_matrix()
+        tc_dev = float(np.max(np.abs(vtc - v64)) / np.max(np.abs(v64)))
+        del v64, vtc
+        c.dg_set_volume_kernel(gb.DG_VOLUME_FP64)
         vfma = sum(dg_fma_per_element(p) * int(np.sum(pdeg == p)) for p in range(1, 5))
         ffma = dg_face_fma(F, pdeg)
         x, it, res, rel = c.dg_solve(krylov=50, max_iter=gmres_iters, tol_rel=1e-10)
@@ -236,6 +249,9 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
             "assemble_ms": tot, "elem_per_s": m.nel / (tot * 1e-3),
             "volume_ms": vol, "volume_fp64_frac": 2 * vfma / (vol * 1e-3) / 1e12 / fp64_peak,
             "face_ms": fa, "face_fp64_frac": 2 * ffma / (fa * 1e-3) / 1e12 / fp64_peak,
+            "tensor_core_volume": {"volume_ms": vol_tc, "assemble_ms": tot_tc, "elem_per_s": m.nel / (tot_tc * 1e-3),
+                                   "max_abs_diff_vs_fp64_rel_to_max": tc_dev,
+                                   "note": "tcgen05 split-BF16 products (p <= 3; p = 4 stays FP64)"},
             "gmres_iterations": it, "gmres_rel_residual": rel, "gmres_ms_per_iteration": st[0] / max(it, 1),
             "spmv_ms": spmv_ms,
             # the preconditioned block SpMV: matrix + inverted diagonal blocks, one FMA per value
