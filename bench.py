@@ -53,7 +53,31 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help=argparse.SUPPRESS)
+    p.add_argument("--profile", choices=["dg", "dg_tc"], default=None,
+                   help="small DG p=3 anisotropic case (n^3 x 2 prisms, --n) for ncu captures: "
+                        "3 assemblies (FP64 or tensor-core volume kernel) and one block residual")
     return p.parse_args()
+
+
+def run_profile_case(args):
+    """One small case for an ncu capture of the DG kernels (volume, faces,
+    block SpMV); prints its CUDA-event timings."""
+    import modfem_gb300 as gb
+    from modfem_gb300.mesh import anisotropic_tensors, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(args.n, jitter=JITTER, seed=SEED)
+    c = gb.Context(0)
+    c.set_mesh(m)
+    c.set_coefficients(D=anisotropic_tensors(m.nel, seed=SEED), f=1.0, g=0.0)
+    c.dg_set_degrees(np.full(m.nel, 3))
+    c.dg_set_faces(prism_faces(m), penalty=10.0)
+    c.dg_build_structure()
+    c.dg_set_volume_kernel(gb.DG_VOLUME_TC if args.profile == "dg_tc" else gb.DG_VOLUME_FP64)
+    for _ in range(3):
+        c.dg_assemble()
+    r = c.dg_compute_residual(np.zeros(c.dg_ndof))
+    print(json.dumps({"profile_case": args.profile, "elements": m.nel, "timing_ms": c.dg_last_timing()[:3],
+                      "residual_max": float(np.abs(r).max())}))
+    c.close()
 
 
 def dist_setup():
@@ -360,6 +384,12 @@ def run_reference(args, ws, rank):
 
 def main():
     args = parse()
+    if args.profile:
+        from modfem_gb300 import build
+        build.build(verbose=False)
+        args.n = args.n if args.n != N_HEX else 24
+        run_profile_case(args)
+        return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
