@@ -202,6 +202,18 @@ int gbfem_dg_compute_residual(gbfem_ctx ctx, int Use_rhs, int Ini_zero, int Ndof
  * Returns the iteration count. */
 int gbfem_dg_solve(gbfem_ctx ctx, int krylov, int max_iter, double tol_rel, int ini_zero, double *x,
                    double *res, double *res_rel);
+/* No reference counterpart.  Mixed-precision solve of the same system:
+ * FP64 iterative refinement (true residual b - A x and correction in FP64)
+ * around GMRES(krylov) whose block SpMV and block-Jacobi product use FP32
+ * copies of the matrix and of the inverted diagonal blocks in FP32
+ * arithmetic (Arnoldi orthogonalisation stays FP64).  Each inner solve stops
+ * at inner_tol relative to its initial preconditioned residual or after 10
+ * restart cycles (10 krylov iterations); the loop
+ * stops when ||b - A x|| <= tol_rel ||b|| or max_iter inner iterations were
+ * spent.  Returns the inner iterations; *outer_steps refinement steps,
+ * *rel_res the final relative true residual. */
+int gbfem_dg_solve_ir(gbfem_ctx ctx, int krylov, int max_iter, double tol_rel, double inner_tol, double *x,
+                      int *outer_steps, double *rel_res);
 
 /* Drop-in for lar_compute_residual (lsd_mkb/las_intf.c:771,
  * lad_crs/las_crs_intf.c:788-856): V = (Use_rhs ? B : 0) - A*X, X, B, V host

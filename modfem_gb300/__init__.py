@@ -54,6 +54,7 @@ SIGNATURES = [
     ("gbfem_dg_set_matrix", _ci, [_vp, _vp, _vp]),
     ("gbfem_dg_compute_residual", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
     ("gbfem_dg_solve", _ci, [_vp, _ci, _ci, _cd, _ci, _vp, _pd, _pd]),
+    ("gbfem_dg_solve_ir", _ci, [_vp, _ci, _ci, _cd, _cd, _vp, _pi, _pd]),
     ("gbfem_compute_residual", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
     ("gbfem_compute_residual_noalloc", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
     ("gbfem_solve", _ci, [_vp, _ci, _ci, _cd, _ci, _vp, _pd, _pd]),
@@ -265,6 +266,15 @@ class Context:
         self._check(self.L.gbfem_dg_compute_residual(self._h, use_rhs, ini_zero, self.dg_ndof, _p(x), _p(b),
                                                      _p(v)))
         return v
+
+    def dg_solve_ir(self, krylov=50, max_iter=100000, tol_rel=1e-10, inner_tol=1e-4):
+        """Mixed precision: FP64 refinement around FP32-operator GMRES.
+        Returns (x, inner iterations, refinement steps, relative true residual)."""
+        x = np.zeros(self.dg_ndof)
+        k, rel = ctypes.c_int(), ctypes.c_double()
+        it = self._check(self.L.gbfem_dg_solve_ir(self._h, krylov, max_iter, tol_rel, inner_tol, _p(x),
+                                                  ctypes.byref(k), ctypes.byref(rel)))
+        return x, it, k.value, rel.value
 
     def dg_solve(self, krylov=50, max_iter=1000, tol_rel=1e-8, x0=None):
         x = np.zeros(self.dg_ndof) if x0 is None else np.array(x0, dtype=np.float64)

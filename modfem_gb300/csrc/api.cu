@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <chrono>
 #include <functional>
 #include <mutex>
 
@@ -97,6 +98,10 @@ int gbfem_destroy(gbfem_ctx c) {
   c->dg_bptr_d.release();
   c->dg_bcol_d.release();
   c->dg_boff_d.release();
+  c->dg_val32.release();
+  c->dg_dinv32.release();
+  c->ir_x.release();
+  c->ir_r.release();
   c->dg_colx_d.release();
   c->dg_row_val_d.release();
   c->dg_cx_off_d.release();
@@ -890,9 +895,10 @@ static int gmres_run(gbfem_ctx c, int n, int krylov, int max_iter, double tol_re
   const int nb = gbfem::reduction_blocks(n);
   GB_TRY(c->partial.alloc((size_t)nb * (m + 2)));
   cudaStream_t st = c->stream;
+  // x == NULL: the solution stays in c->x (zeroed when ini_zero)
   if (ini_zero)
     GB_CUDA(cudaMemsetAsync(c->x.p, 0, (size_t)n * sizeof(double), st));
-  else
+  else if (x)
     GB_CUDA(cudaMemcpyAsync(c->x.p, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
   double tol_abs = 1e-12;
   if (tol_rel < 1e-12) tol_rel = 1e-12;
@@ -971,7 +977,7 @@ static int gmres_run(gbfem_ctx c, int n, int krylov, int max_iter, double tol_re
     if (resid < tol_abs || resid / beta0 < tol_rel || it >= max_iter) break;
   }
   cudaEventRecord(c->ev1, st);
-  GB_CUDA(cudaMemcpyAsync(x, c->x.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (x) GB_CUDA(cudaMemcpyAsync(x, c->x.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));
   cudaEventElapsedTime(&c->last_solve_ms, c->ev0, c->ev1);
   c->last_spmv_ms = spmv_ms;
@@ -1032,6 +1038,96 @@ int gbfem_dg_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int in
     return dg_spmv(c, mode, in, mode == 0 ? c->dg_rhs.p : nullptr, out);
   };
   return gmres_run(c, n, krylov, max_iter, tol_rel, ini_zero, x, res_out, res_rel_out, op);
+}
+
+// DG iterative refinement: FP64 outer loop on the true residual, inner
+// GMRES on FP32 copies of the matrix and of the inverted diagonal blocks.
+static int dg_spmv32(gbfem_ctx c, int mode, const double *x, const double *b, double *out) {
+  int n = 0;
+  for (int p = 1; p <= 4; p++) {
+    if (!c->dg_list[p].p) continue;
+    const int r = gbfem::launch_dg_block_spmv32(c->stream, mode, p, (int)c->dg_list[p].n, c->dg_list[p].p,
+                                                c->dg_roff_d.p, c->dg_row_val_d.p, c->dg_cx_off_d.p,
+                                                c->dg_colx_d.p, c->dg_val32.p, c->dg_dinv_off_d.p, c->dg_dinv32.p,
+                                                x, b, out);
+    if (r < 0) return r;
+    n += r;
+  }
+  return n;
+}
+
+int gbfem_dg_solve_ir(gbfem_ctx c, int krylov, int max_iter, double tol_rel, double inner_tol, double *x,
+                      int *outer_steps, double *rel_res) {
+  GB_CHECK(c && c->dg_ready, "DG structure not built");
+  GB_CHECK(krylov > 0 && krylov <= 256, "krylov must be in 1..256");
+  GB_CHECK(x != nullptr, "null solution vector");
+  GB_CHECK(tol_rel > 0 && inner_tol > 0 && inner_tol < 1, "tolerances must be positive (inner < 1)");
+  GB_CUDA(cudaSetDevice(c->device));
+  const int n = c->dg_ndof;
+  cudaStream_t st = c->stream;
+  // preconditioner in FP64, then FP32 copies of it and of the matrix
+  GB_TRY(c->dg_dinv.alloc((size_t)c->dg_ninv));
+  GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), st));
+  GB_TRY(gbfem::launch_dg_block_inverse(st, c->nel, c->dg_roff_d.p, c->dg_boff_diag_d.p, c->dg_val.p,
+                                        c->dg_dinv_off_d.p, c->dg_dinv.p, c->err.p));
+  GB_TRY(c->dg_val32.alloc((size_t)c->dg_nval));
+  GB_TRY(c->dg_dinv32.alloc((size_t)c->dg_ninv));
+  GB_TRY(gbfem::launch_to_float(st, c->dg_nval, c->dg_val.p, c->dg_val32.p));
+  GB_TRY(gbfem::launch_to_float(st, c->dg_ninv, c->dg_dinv.p, c->dg_dinv32.p));
+  int herr = 0;
+  GB_CUDA(cudaMemcpyAsync(&herr, c->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  GB_CHECK(herr == 0, "singular diagonal block in the DG block Jacobi preconditioner");
+  GB_TRY(c->ir_x.alloc(n));
+  GB_TRY(c->ir_r.alloc(n));
+  GB_TRY(c->hcol.alloc(krylov + 2));
+  const int nb = gbfem::reduction_blocks(n);
+  GB_TRY(c->partial.alloc((size_t)nb * (krylov + 2)));
+  GB_TRY(c->b.alloc(2));
+  const double one = 1.0;
+  GB_CUDA(cudaMemcpyAsync(c->b.p, &one, sizeof(double), cudaMemcpyHostToDevice, st));
+  GB_CUDA(cudaMemsetAsync(c->ir_x.p, 0, (size_t)n * sizeof(double), st));
+  auto norm = [&](const double *v, double *out) -> int {
+    const int r = gbfem::launch_multidot(st, n, 1, v, n, v, c->partial.p, c->hcol.p, 1);
+    if (r < 0) return r;
+    if (cudaMemcpyAsync(out, c->hcol.p, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      gbfem::set_error("norm copy failed");
+      return -1;
+    }
+    return 0;
+  };
+  double bn = 0.0;
+  GB_TRY(norm(c->dg_rhs.p, &bn));
+  const double *r_dev = c->ir_r.p;
+  GmresOp op32 = [&](int mode, const double *in, double *out) -> int {
+    return dg_spmv32(c, mode, in, mode == 0 ? r_dev : nullptr, out);
+  };
+  const auto t0 = std::chrono::steady_clock::now();
+  int inner_total = 0, k = 0;
+  double rel = 1.0;
+  for (; k < 100; k++) {
+    // true residual in FP64
+    GB_TRY(dg_spmv(c, 2, c->ir_x.p, c->dg_rhs.p, c->ir_r.p));
+    double rn = 0.0;
+    GB_TRY(norm(c->ir_r.p, &rn));
+    rel = bn > 0 ? rn / bn : 0.0;
+    if (rel <= tol_rel || inner_total >= max_iter) break;
+    // correction from the FP32 operator (x0 = 0, result in c->x)
+    // each correction: at most 10 restart cycles (the FP32 operator's own
+    // rounding floor stops progress long before a tight inner tolerance)
+    const int cap = std::min(max_iter - inner_total, 10 * krylov);
+    const int it = gmres_run(c, n, krylov, cap, inner_tol, 1, nullptr, nullptr, nullptr, op32);
+    GB_TRY(it);
+    inner_total += it;
+    GB_TRY(gbfem::launch_multiaxpy(st, n, 1, c->b.p, 1.0, c->x.p, n, c->ir_x.p));
+  }
+  GB_CUDA(cudaMemcpyAsync(x, c->ir_x.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  c->last_solve_ms = (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (outer_steps) *outer_steps = k;
+  if (rel_res) *rel_res = rel;
+  return inner_total;
 }
 
 }  // extern "C"

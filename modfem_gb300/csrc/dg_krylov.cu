@@ -113,28 +113,41 @@ int launch_dg_block_inverse(cudaStream_t st, int nel, const int *roff, const lon
   return 1;
 }
 
-template <int P>
+template <int P, typename VT>
 __global__ void __launch_bounds__(DGS_THREADS) dg_block_spmv_kernel(
     int mode, int count, const int *__restrict__ ent_el, const int *__restrict__ roff,
     const long long *__restrict__ row_val, const long long *__restrict__ cx_off, const int *__restrict__ colx,
-    const double *__restrict__ val, const long long *__restrict__ dinv_off, const double *__restrict__ dinv,
+    const VT *__restrict__ val, const long long *__restrict__ dinv_off, const VT *__restrict__ dinv,
     const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ out) {
-  __shared__ double sv[DGS_ROWS][DgSpmvDims<P>::NS];
-  dg_block_row_spmv<P>(mode, count, ent_el, roff, row_val, cx_off, colx, val, dinv_off, dinv, x, b, out, sv);
+  __shared__ VT sv[DGS_ROWS][DgSpmvDims<P>::NS];
+  dg_block_row_spmv<P, VT>(mode, count, ent_el, roff, row_val, cx_off, colx, val, dinv_off, dinv, x, b, out, sv);
 }
 
-int launch_dg_block_spmv(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
-                         const long long *row_val, const long long *cx_off, const int *colx, const double *val,
-                         const long long *dinv_off, const double *dinv, const double *x, const double *b,
-                         double *out) {
+__global__ void to_float_kernel(long long n, const double *__restrict__ a, float *__restrict__ b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+int launch_to_float(cudaStream_t st, long long n, const double *a, float *b) {
+  if (n <= 0) return 0;
+  to_float_kernel<<<152 * 8, 256, 0, st>>>(n, a, b);
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
+template <typename VT>
+static int launch_dg_block_spmv_t(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
+                                  const long long *row_val, const long long *cx_off, const int *colx, const VT *val,
+                                  const long long *dinv_off, const VT *dinv, const double *x, const double *b,
+                                  double *out) {
   if (count <= 0) return 0;
   GB_CHECK(mode >= 0 && mode <= 2, "bad block SpMV mode");
   GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
   GB_CHECK(mode == 2 || (dinv && dinv_off), "block SpMV needs the inverted diagonal blocks");
   const int grid = (count + DGS_ROWS - 1) / DGS_ROWS;
-#define GB_DGS_LAUNCH(PP)                                                                                  \
-  dg_block_spmv_kernel<PP><<<grid, DGS_THREADS, 0, st>>>(mode, count, ent_el, roff, row_val, cx_off, colx, \
-                                                         val, dinv_off, dinv, x, b, out)
+#define GB_DGS_LAUNCH(PP)                                                                                      \
+  dg_block_spmv_kernel<PP, VT><<<grid, DGS_THREADS, 0, st>>>(mode, count, ent_el, roff, row_val, cx_off, colx, \
+                                                             val, dinv_off, dinv, x, b, out)
   switch (p) {
     case 1: GB_DGS_LAUNCH(1); break;
     case 2: GB_DGS_LAUNCH(2); break;
@@ -144,6 +157,22 @@ int launch_dg_block_spmv(cudaStream_t st, int mode, int p, int count, const int 
 #undef GB_DGS_LAUNCH
   GB_CUDA(cudaGetLastError());
   return 1;
+}
+
+int launch_dg_block_spmv(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
+                         const long long *row_val, const long long *cx_off, const int *colx, const double *val,
+                         const long long *dinv_off, const double *dinv, const double *x, const double *b,
+                         double *out) {
+  return launch_dg_block_spmv_t<double>(st, mode, p, count, ent_el, roff, row_val, cx_off, colx, val, dinv_off,
+                                        dinv, x, b, out);
+}
+
+int launch_dg_block_spmv32(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
+                           const long long *row_val, const long long *cx_off, const int *colx, const float *val,
+                           const long long *dinv_off, const float *dinv, const double *x, const double *b,
+                           double *out) {
+  return launch_dg_block_spmv_t<float>(st, mode, p, count, ent_el, roff, row_val, cx_off, colx, val, dinv_off,
+                                       dinv, x, b, out);
 }
 
 }  // namespace gbfem

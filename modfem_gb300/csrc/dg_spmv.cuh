@@ -24,20 +24,25 @@ constexpr int DGS_LANES = 8;
 constexpr int DGS_THREADS = 256;
 constexpr int DGS_ROWS = DGS_THREADS / DGS_LANES;
 
+__device__ __forceinline__ double dgs_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float dgs_fma(float a, float b, float c) { return fmaf(a, b, c); }
+
 template <int P>
 struct DgSpmvDims {
   static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
 };
 
 // The body of the block SpMV for the block rows of one CTA (blockDim.x ==
-// DGS_THREADS); sv: DGS_ROWS x NS doubles of shared memory.
-template <int P>
+// DGS_THREADS); sv: DGS_ROWS x NS values of shared memory.  VT is the type of
+// the stored matrix and of the arithmetic (double, or float for the inner
+// solves of iterative refinement); vectors are FP64 either way.
+template <int P, typename VT = double>
 __device__ __forceinline__ void dg_block_row_spmv(
     int mode, int count, const int *__restrict__ ent_el, const int *__restrict__ roff,
     const long long *__restrict__ row_val, const long long *__restrict__ cx_off, const int *__restrict__ colx,
-    const double *__restrict__ val, const long long *__restrict__ dinv_off, const double *__restrict__ dinv,
+    const VT *__restrict__ val, const long long *__restrict__ dinv_off, const VT *__restrict__ dinv,
     const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ out,
-    double (*sv)[DgSpmvDims<P>::NS]) {
+    VT (*sv)[DgSpmvDims<P>::NS]) {
   constexpr int NS = DgSpmvDims<P>::NS;
   constexpr int S = (NS + DGS_LANES - 1) / DGS_LANES;
   const int grp = threadIdx.x / DGS_LANES, g = threadIdx.x % DGS_LANES;
@@ -45,34 +50,34 @@ __device__ __forceinline__ void dg_block_row_spmv(
   const bool active = idx < count;
   const int e = active ? ent_el[idx] : 0;
   const int r0 = roff[e];
-  double acc[S];
+  VT acc[S];
 #pragma unroll
-  for (int s = 0; s < S; s++) acc[s] = 0.0;
+  for (int s = 0; s < S; s++) acc[s] = VT(0);
   if (active) {
-    const double *A = val + row_val[e] + g;
+    const VT *A = val + row_val[e] + g;
     const int *cx = colx + cx_off[e];
     const int nct = (int)(cx_off[e + 1] - cx_off[e]);
     int t = 0;
     for (; t + 2 <= nct; t += 2) {
-      const double x0 = x[cx[t]], x1 = x[cx[t + 1]];
-      const double *col0 = A + (size_t)t * NS, *col1 = col0 + NS;
+      const VT x0 = (VT)x[cx[t]], x1 = (VT)x[cx[t + 1]];
+      const VT *col0 = A + (size_t)t * NS, *col1 = col0 + NS;
 #pragma unroll
       for (int s = 0; s < S; s++)
-        if (g + DGS_LANES * s < NS) acc[s] = fma(col1[DGS_LANES * s], x1, fma(col0[DGS_LANES * s], x0, acc[s]));
+        if (g + DGS_LANES * s < NS) acc[s] = dgs_fma(col1[DGS_LANES * s], x1, dgs_fma(col0[DGS_LANES * s], x0, acc[s]));
     }
     if (t < nct) {
-      const double x0 = x[cx[t]];
-      const double *col0 = A + (size_t)t * NS;
+      const VT x0 = (VT)x[cx[t]];
+      const VT *col0 = A + (size_t)t * NS;
 #pragma unroll
       for (int s = 0; s < S; s++)
-        if (g + DGS_LANES * s < NS) acc[s] = fma(col0[DGS_LANES * s], x0, acc[s]);
+        if (g + DGS_LANES * s < NS) acc[s] = dgs_fma(col0[DGS_LANES * s], x0, acc[s]);
     }
   }
   if (mode != 1) {
 #pragma unroll
     for (int s = 0; s < S; s++) {
       const int i = g + DGS_LANES * s;
-      acc[s] = (b && active && i < NS ? b[r0 + i] : 0.0) - acc[s];
+      acc[s] = (b && active && i < NS ? (VT)b[r0 + i] : VT(0)) - acc[s];
     }
   }
   if (mode == 2) {
@@ -80,7 +85,7 @@ __device__ __forceinline__ void dg_block_row_spmv(
 #pragma unroll
       for (int s = 0; s < S; s++) {
         const int i = g + DGS_LANES * s;
-        if (i < NS) out[r0 + i] = acc[s];
+        if (i < NS) out[r0 + i] = (double)acc[s];
       }
     }
     return;
@@ -92,21 +97,21 @@ __device__ __forceinline__ void dg_block_row_spmv(
   }
   __syncwarp();
   if (!active) return;
-  const double *D = dinv + dinv_off[e] + g;
-  double o[S];
+  const VT *D = dinv + dinv_off[e] + g;
+  VT o[S];
 #pragma unroll
-  for (int s = 0; s < S; s++) o[s] = 0.0;
+  for (int s = 0; s < S; s++) o[s] = VT(0);
   for (int j = 0; j < NS; j++) {
-    const double t = sv[grp][j];
-    const double *col = D + (size_t)j * NS;
+    const VT t = sv[grp][j];
+    const VT *col = D + (size_t)j * NS;
 #pragma unroll
     for (int s = 0; s < S; s++)
-      if (g + DGS_LANES * s < NS) o[s] = fma(col[DGS_LANES * s], t, o[s]);
+      if (g + DGS_LANES * s < NS) o[s] = dgs_fma(col[DGS_LANES * s], t, o[s]);
   }
 #pragma unroll
   for (int s = 0; s < S; s++) {
     const int i = g + DGS_LANES * s;
-    if (i < NS) out[r0 + i] = o[s];
+    if (i < NS) out[r0 + i] = (double)o[s];
   }
 }
 

@@ -131,6 +131,13 @@ int launch_dg_block_spmv(cudaStream_t st, int mode, int p, int count, const int 
                          const long long *row_val, const long long *cx_off, const int *colx, const double *val,
                          const long long *dinv_off, const double *dinv, const double *x, const double *b,
                          double *out);
+// The same with the matrix and the arithmetic in FP32 (inner solves of
+// iterative refinement); vectors stay FP64.
+int launch_dg_block_spmv32(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
+                           const long long *row_val, const long long *cx_off, const int *colx, const float *val,
+                           const long long *dinv_off, const float *dinv, const double *x, const double *b,
+                           double *out);
+int launch_to_float(cudaStream_t st, long long n, const double *a, float *b);
 // Tensor-core (tcgen05, split BF16) DG volume integrals, FP64-equivalent.
 bool dg_tc_supported(int p);
 int launch_dg_tc_volume(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
@@ -194,6 +201,8 @@ struct gbfem_ctx_s {
   gbfem::DevBuf<gbfem::DgHalfFace> dg_hf;
   // DG block Jacobi: inverted diagonal blocks, block e at dg_dinv_off_d[e]
   gbfem::DevBuf<double> dg_dinv;
+  gbfem::DevBuf<float> dg_val32, dg_dinv32;  // FP32 copies for iterative refinement
+  gbfem::DevBuf<double> ir_x, ir_r;
   gbfem::DevBuf<long long> dg_dinv_off_d;
   gbfem::DevBuf<int> dg_bptr_d, dg_bcol_d, dg_colx_d;
   gbfem::DevBuf<long long> dg_boff_d, dg_row_val_d, dg_cx_off_d;

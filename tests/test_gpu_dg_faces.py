@@ -196,3 +196,45 @@ def test_dg_tensor_core_volume_vs_fp64_kernel(gb, p):
         worst = max(worst, mat_rel_err(Ktc, K64))
     assert worst < 1e-13, worst
     assert vec_rel_err(out[1][1], out[0][1]) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["dg_asm_mixed", "dg_asm_aniso"])
+def test_dg_iterative_refinement_vs_reference(gb, name):
+    """Mixed precision (FP64 refinement around FP32-operator GMRES) drives the
+    true relative residual to 1e-13; its solution then agrees with a dense
+    direct solve of the same system to the accuracy the conditioning allows
+    and with the reference's (which stopped at 1e-10 on the preconditioned
+    residual, so is accurate to ~1e-7) to 1e-6."""
+    g, m, F = _fixture_problem(name)
+    D = _tensors(g)
+    c = _context(gb, m, F, g["pdeg"], k=None if D is not None else g["k"], D=D, pen=float(g["pen"]),
+                 g=float(g["g"]), f=float(g["f"]))
+    c.dg_assemble()
+    x, inner, outer, rel = c.dg_solve_ir(krylov=50, max_iter=20000, tol_rel=1e-13, inner_tol=1e-6)
+    assert rel <= 1e-13 and outer >= 2
+    r = c.dg_compute_residual(x)
+    assert np.linalg.norm(r) <= 1.01e-13 * np.linalg.norm(c.dg_get_matrix()[1])
+    # dense direct solve of the same (small) system as the exact answer
+    rp, ci, v, rhs, off = _expand(c)
+    A = np.zeros((off[-1], off[-1]))
+    A[np.repeat(np.arange(off[-1]), np.diff(rp)), ci] = v
+    xd = np.linalg.solve(A, rhs)
+    # condition number ~1e5 (penalty-dominated, mixed degree): a 1e-13 true
+    # residual bounds the solution error by ~1e-8
+    assert vec_rel_err(x, xd) < 1e-7
+    assert vec_rel_err(x, g["gmres_x"]) < 1e-6
+
+
+def test_dg_iterative_refinement_vs_fp64_gmres_larger(gb):
+    from modfem_gb300.mesh import anisotropic_tensors, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(6, jitter=0.2, seed=77)
+    F = prism_faces(m)
+    pdeg = np.random.default_rng(77).integers(1, 4, m.nel)
+    c = _context(gb, m, F, pdeg, D=anisotropic_tensors(m.nel, seed=77).reshape(m.nel, 9), g=0.3)
+    c.dg_assemble()
+    x64, it64, _, _ = c.dg_solve(krylov=50, max_iter=50000, tol_rel=1e-12)
+    xir, inner, outer, rel = c.dg_solve_ir(krylov=50, max_iter=50000, tol_rel=1e-13, inner_tol=1e-6)
+    assert rel <= 1e-13
+    # both stop on residuals; their difference is bounded by the FP64 GMRES
+    # stopping accuracy (1e-12 on the preconditioned residual)
+    assert vec_rel_err(xir, x64) < 1e-7
