@@ -242,6 +242,7 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
         c.dg_set_degrees(pdeg)
         c.dg_set_faces(F, penalty=10.0)
         nd, nv = c.dg_build_structure()
+        tuned_vol, tuned_face, _ = c.dg_autotune(sample=65536)  # launch shapes per degree (results unchanged)
         for _ in range(2):
             c.dg_assemble()
         tt = np.zeros(3)
@@ -274,6 +275,7 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
         inv_bytes = 8 * sum(int(np.sum(pdeg == p)) * [0, 6, 18, 40, 75][p] ** 2 for p in range(1, 5))
         out[name] = {
             "elements": m.nel, "faces": int(F.n), "dofs": nd, "stored_values": nv,
+            "autotuned_shapes": {"volume": tuned_vol[1:].tolist(), "face": tuned_face[1:].tolist()},
             "assemble_ms": tot, "elem_per_s": m.nel / (tot * 1e-3),
             "volume_ms": vol, "volume_fp64_frac": 2 * vfma / (vol * 1e-3) / 1e12 / fp64_peak,
             "face_ms": fa, "face_fp64_frac": 2 * ffma / (fa * 1e-3) / 1e12 / fp64_peak,

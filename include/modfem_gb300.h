@@ -184,6 +184,18 @@ int gbfem_dg_get_structure(gbfem_ctx ctx, int *dof_off, int *bptr, int *bcol, lo
  * value g of gbfem_set_coefficients on boundary faces) into the block matrix
  * and the rhs, each block entry written by one thread in a fixed order. */
 int gbfem_dg_assemble(gbfem_ctx ctx);
+/* Launch-shape autotuner (no reference counterpart): per degree class,
+ * times the FP64 volume kernel's three shapes (threads per CTA, points per
+ * shared-memory chunk) and the face kernel's two (threads per CTA) on up to
+ * `sample` elements (<= 0: 16384) of the current mesh and keeps the fastest
+ * for later assemblies.  Every shape sums each matrix entry in the same
+ * order, so the choice never changes the results.  Overwrites the matrix:
+ * assemble afterwards.  vol[5], face[5] (index = degree) receive the choices
+ * and ms[20] (5 per degree: three volume, two face shapes) the timings; any
+ * may be NULL. */
+int gbfem_dg_autotune(gbfem_ctx ctx, int sample, int *vol, int *face, double *ms);
+/* Sets the shapes explicitly (vol[p] in 0..2, face[p] in 0..1, index p = 1..4). */
+int gbfem_dg_set_variants(gbfem_ctx ctx, const int *vol, const int *face);
 /* Times (ms) of the last gbfem_dg_assemble: total, volume and face kernels. */
 int gbfem_dg_last_timing(gbfem_ctx ctx, double *total_ms, double *volume_ms, double *face_ms, int *launches);
 int gbfem_dg_get_matrix(gbfem_ctx ctx, double *vals, double *rhs);

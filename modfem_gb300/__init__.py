@@ -50,6 +50,8 @@ SIGNATURES = [
     ("gbfem_dg_get_structure", _ci, [_vp, _vp, _vp, _vp, _vp]),
     ("gbfem_dg_assemble", _ci, [_vp]),
     ("gbfem_dg_last_timing", _ci, [_vp, _pd, _pd, _pd, _pi]),
+    ("gbfem_dg_autotune", _ci, [_vp, _ci, _vp, _vp, _vp]),
+    ("gbfem_dg_set_variants", _ci, [_vp, _vp, _vp]),
     ("gbfem_dg_get_matrix", _ci, [_vp, _vp, _vp]),
     ("gbfem_dg_set_matrix", _ci, [_vp, _vp, _vp]),
     ("gbfem_dg_compute_residual", _ci, [_vp, _ci, _ci, _ci, _vp, _vp, _vp]),
@@ -251,6 +253,17 @@ class Context:
 
     def dg_set_matrix(self, vals=None, rhs=None):
         self._check(self.L.gbfem_dg_set_matrix(self._h, _p(_f64(vals)), _p(_f64(rhs))))
+
+    def dg_autotune(self, sample=16384):
+        """Chooses the fastest launch shapes per degree; returns (vol[5], face[5], ms[4, 5])."""
+        vol = np.zeros(5, np.int32)
+        face = np.zeros(5, np.int32)
+        ms = np.zeros(20)
+        self._check(self.L.gbfem_dg_autotune(self._h, sample, _p(vol), _p(face), _p(ms)))
+        return vol, face, ms.reshape(4, 5)
+
+    def dg_set_variants(self, vol=None, face=None):
+        self._check(self.L.gbfem_dg_set_variants(self._h, _p(_i32(vol)), _p(_i32(face))))
 
     def dg_last_timing(self):
         """(total ms, volume-kernel ms, face-kernel ms, launches) of the last DG assembly."""

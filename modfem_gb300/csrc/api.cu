@@ -695,7 +695,8 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     else
       r = gbfem::launch_dg_prism_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
                                           c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,
-                                          c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
+                                          c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p,
+                                          c->dg_var_vol[p]);
     GB_TRY(r);
     launches += r;
   }
@@ -706,7 +707,7 @@ int gbfem_dg_assemble(gbfem_ctx c) {
       int r = gbfem::launch_dg_prism_faces(c->stream, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->dg_hf_ptr.p,
                                            c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
                                            c->dg_pen, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,
-                                           c->dg_rhs.p);
+                                           c->dg_rhs.p, c->dg_var_face[p]);
       GB_TRY(r);
       launches += r;
     }
@@ -722,6 +723,80 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     GB_CHECK(herr == 0, "tensor-core volume kernel: a pipeline wait expired");
   }
   c->last_launches = launches;
+  return 0;
+}
+
+int gbfem_dg_set_variants(gbfem_ctx c, const int *vol, const int *face) {
+  GB_CHECK(c, "null context");
+  for (int p = 1; p <= 4; p++) {
+    if (vol) GB_CHECK(vol[p] >= 0 && vol[p] < 3, "volume variant out of range");
+    if (face) GB_CHECK(face[p] >= 0 && face[p] < 2, "face variant out of range");
+  }
+  for (int p = 1; p <= 4; p++) {
+    if (vol) c->dg_var_vol[p] = vol[p];
+    if (face) c->dg_var_face[p] = face[p];
+  }
+  return 0;
+}
+
+// Times every launch-shape variant of the FP64 volume kernel and of the face
+// kernel per degree class on up to `sample` elements of the class (the
+// matrix is overwritten: assemble afterwards) and keeps the fastest.
+int gbfem_dg_autotune(gbfem_ctx c, int sample, int *vol_out, int *face_out, double *ms_out) {
+  GB_CHECK(c && c->dg_ready, "DG structure not built (gbfem_dg_build_structure)");
+  GB_CUDA(cudaSetDevice(c->device));
+  if (sample <= 0) sample = 16384;
+  cudaStream_t st = c->stream;
+  auto time_it = [&](const std::function<int()> &launch, float *best) -> int {
+    *best = 1e30f;
+    GB_TRY(launch());  // warm-up (module load, caches)
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(c->ev2, st);
+      GB_TRY(launch());
+      cudaEventRecord(c->ev3, st);
+      GB_CUDA(cudaEventSynchronize(c->ev3));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->ev2, c->ev3);
+      *best = std::min(*best, ms);
+    }
+    return 0;
+  };
+  for (int p = 1; p <= 4; p++) {
+    if (!c->dg_list[p].p) continue;
+    const int cnt = (int)std::min<size_t>(c->dg_list[p].n, (size_t)sample);
+    float bv = 1e30f, bf = 1e30f;
+    for (int v = 0; v < 3; v++) {
+      float ms;
+      GB_TRY(time_it([&] {
+        return gbfem::launch_dg_prism_elements(st, c->device, p, cnt, c->dg_list[p].p, c->el_nodes.p, c->xyz.p,
+                                               c->k_el.p, c->D_el.p, c->f, c->dg_boff_diag_d.p, c->dg_roff_d.p,
+                                               c->dg_val.p, c->dg_rhs.p, v);
+      }, &ms));
+      if (ms_out) ms_out[(p - 1) * 5 + v] = ms;
+      if (ms < bv) {
+        bv = ms;
+        c->dg_var_vol[p] = v;
+      }
+    }
+    if (c->dg_hf.p)
+      for (int v = 0; v < 2; v++) {
+        float ms;
+        GB_TRY(time_it([&] {
+          return gbfem::launch_dg_prism_faces(st, p, cnt, c->dg_list[p].p, c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p,
+                                              c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->dg_pen, c->g,
+                                              c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p, v);
+        }, &ms));
+        if (ms_out) ms_out[(p - 1) * 5 + 3 + v] = ms;
+        if (ms < bf) {
+          bf = ms;
+          c->dg_var_face[p] = v;
+        }
+      }
+  }
+  for (int p = 1; p <= 4; p++) {
+    if (vol_out) vol_out[p] = c->dg_var_vol[p];
+    if (face_out) face_out[p] = c->dg_var_face[p];
+  }
   return 0;
 }
 

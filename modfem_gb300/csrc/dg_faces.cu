@@ -30,29 +30,35 @@ constexpr int DGF_NQ = GB_DG_MAXNQF;  // points of the largest face rule
 constexpr int DGF_GEO = 16;           // e1, e2, v1, v2, a, then the owner-row scales
 constexpr int DGF_FAC = 30;           // monomial factors per point and side
 
-// Threads per CTA chosen so that the NS x NS diagonal block (and an off-
-// diagonal block with a neighbour of the same degree) divides evenly or
-// nearly: 36 / 64, 324 / 384 (2 x 192), 1600 / 1600 (5 x 320), 5625 / 5632
-// (22 x 256) entries per thread-slot; the block products are FP64-bound, so
-// idle lanes are lost FP64 issue.
-template <int P>
+// Threads per CTA per degree (variant 0 fills the thread slots of the
+// NS x NS diagonal block evenly or nearly: 36 / 64, 324 / 384 = 2 x 192,
+// 1600 / 1600 = 5 x 320, 5625 / 5632 = 22 x 256; the products are FP64-bound,
+// so idle lanes are lost FP64 issue); the autotuner times the alternatives.
+// Every variant sums each entry over the points in the same order.
+constexpr int DG_FACE_VARIANTS = 2;
+__host__ __device__ constexpr int dg_face_threads(int p, int v) {
+  return p == 1 ? (v == 0 ? 64 : 128) : p == 2 ? (v == 0 ? 192 : 128) : p == 3 ? (v == 0 ? 320 : 160)
+                                                                              : (v == 0 ? 256 : 384);
+}
+
+template <int P, int THR>
 struct DgFaceDims {
   static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
-  static constexpr int THREADS = P == 1 ? 64 : P == 2 ? 192 : P == 3 ? 320 : 256;
+  static constexpr int THREADS = THR;
   static constexpr int NCOL = NS + GB_DG_MAXNS;  // own + neighbour columns
   static constexpr int PER = (NS * NS + THREADS - 1) / THREADS;
   static constexpr int SMEM_DOUBLES =
       2 * DGF_NQ * NS + 2 * DGF_NQ * NCOL + 36 + 18 + DGF_NQ * DGF_GEO + 2 * DGF_NQ * DGF_FAC + 1;
 };
 
-template <int P>
-__global__ void __launch_bounds__(DgFaceDims<P>::THREADS) dg_prism_faces_kernel(
+template <int P, int THR>
+__global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
     const double *__restrict__ k_el, const double *__restrict__ D_el, double pen, double gval,
     const long long *__restrict__ boff_diag, const int *__restrict__ roff, double *__restrict__ val,
     double *__restrict__ rhs) {
-  using Dm = DgFaceDims<P>;
+  using Dm = DgFaceDims<P, THR>;
   constexpr int NS = Dm::NS, NCOL = Dm::NCOL, DGF_THREADS = Dm::THREADS;
   static_assert(DGF_THREADS >= 54 && DGF_THREADS - 1 >= DGF_NQ, "loader and penalty threads");
   extern __shared__ double smem[];
@@ -196,23 +202,28 @@ __global__ void __launch_bounds__(DgFaceDims<P>::THREADS) dg_prism_faces_kernel(
 int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                           const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                           const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
-                          const int *roff, double *val, double *rhs) {
+                          const int *roff, double *val, double *rhs, int variant) {
   if (count <= 0) return 0;
   GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
-#define GB_DGF_LAUNCH(PP)                                                                                        \
-  {                                                                                                              \
-    const size_t smem = sizeof(double) * DgFaceDims<PP>::SMEM_DOUBLES;                                           \
-    GB_CUDA(cudaFuncSetAttribute(dg_prism_faces_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,        \
-                                 (int)smem));                                                                    \
-    dg_prism_faces_kernel<PP><<<count, DgFaceDims<PP>::THREADS, smem, st>>>(count, ent_el, hf_ptr, hf, el_p,   \
-        el_nodes, xyz, k_el, D_el, pen, g, boff_diag, roff, val, rhs);                                           \
+  GB_CHECK(variant >= 0 && variant < DG_FACE_VARIANTS, "face kernel variant out of range");
+#define GB_DGF_LAUNCH(PP, VV)                                                                                   \
+  {                                                                                                             \
+    constexpr int T_ = dg_face_threads(PP, VV);                                                                 \
+    const size_t smem = sizeof(double) * DgFaceDims<PP, T_>::SMEM_DOUBLES;                                      \
+    GB_CUDA(cudaFuncSetAttribute(dg_prism_faces_kernel<PP, T_>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                 (int)smem));                                                                   \
+    dg_prism_faces_kernel<PP, T_><<<count, T_, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, xyz, k_el, \
+                                                           D_el, pen, g, boff_diag, roff, val, rhs);            \
   }
+#define GB_DGF_P(PP)                                     \
+  if (variant == 0) GB_DGF_LAUNCH(PP, 0) else GB_DGF_LAUNCH(PP, 1)
   switch (p) {
-    case 1: GB_DGF_LAUNCH(1); break;
-    case 2: GB_DGF_LAUNCH(2); break;
-    case 3: GB_DGF_LAUNCH(3); break;
-    default: GB_DGF_LAUNCH(4); break;
+    case 1: GB_DGF_P(1); break;
+    case 2: GB_DGF_P(2); break;
+    case 3: GB_DGF_P(3); break;
+    default: GB_DGF_P(4); break;
   }
+#undef GB_DGF_P
 #undef GB_DGF_LAUNCH
   GB_CUDA(cudaGetLastError());
   return 1;

@@ -85,30 +85,39 @@ int dg_tables_for_device(int device, DgDeviceTables **out) {
   return 0;
 }
 
-constexpr int DG_QCHUNK = 8;
+// Launch shapes (threads per CTA, quadrature points per shared-memory
+// chunk) per degree; the autotuner times them on the mesh at hand.  Thread
+// counts near a multiple of the NS(NS+1)/2 upper entries keep the FP64 lanes
+// busy (21 / 32, 171 / 192, 820 / 864 = 3 x 288, 2850 / 2880 = 10 x 288).
+// Every variant sums each entry over the points in the same order: identical
+// results.
+constexpr int DG_VOL_VARIANTS = 3;
+__host__ __device__ constexpr int dg_vol_threads(int p, int v) {
+  return p == 1 ? (v == 0 ? 32 : 64) : p == 2 ? (v == 0 ? 192 : v == 1 ? 96 : 192)
+                                       : (v == 0 ? 288 : v == 1 ? 224 : 288);
+}
+__host__ __device__ constexpr int dg_vol_qchunk(int p, int v) { return v == 2 ? 16 : 8; }
 
-// Threads per CTA so that the NS(NS+1)/2 upper entries fill the thread slots
-// (21 / 32, 171 / 192, 820 / 864 = 3 x 288, 2850 / 2880 = 10 x 288): the
-// accumulation is FP64-bound and idle lanes are lost FP64 issue.
-template <int P>
+template <int P, int THR, int QC>
 struct DgDims {
   static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
   static constexpr int NQ = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 48 : 80;
-  static constexpr int THREADS = P == 1 ? 32 : P == 2 ? 192 : 288;
+  static constexpr int THREADS = THR;
+  static constexpr int QCHUNK = QC;
   static constexpr int NSYM = NS * (NS + 1) / 2;
   static constexpr int PER_THREAD = (NSYM + THREADS - 1) / THREADS;
 };
 
 // Elements of degree P: ent_el[i] (0-based), matrix block at val + boff[e],
 // rhs rows at rhs + roff[e].  A (tensor, 9 per element) or k (isotropic).
-template <int P>
-__global__ void __launch_bounds__(DgDims<P>::THREADS) dg_prism_elements_kernel(
+template <int P, int THR, int QC>
+__global__ void __launch_bounds__(THR) dg_prism_elements_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
     const double *__restrict__ k_el, const double *__restrict__ D_el, double f, const double *__restrict__ Dtab,
     const double *__restrict__ PHItab, const double *__restrict__ QPtab, const long long *__restrict__ boff,
     const int *__restrict__ roff, double *__restrict__ val, double *__restrict__ rhs) {
-  using Dm = DgDims<P>;
-  constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS;
+  using Dm = DgDims<P, THR, QC>;
+  constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS, DG_QCHUNK = Dm::QCHUNK;
   __shared__ double sG[NQ][6];        // w/|det| C^T A C (symmetric, packed 00 01 02 11 12 22)
   __shared__ double sV[NQ];           // w |det|
   __shared__ double sT[DG_QCHUNK][3][NS];
@@ -237,22 +246,30 @@ __global__ void __launch_bounds__(DgDims<P>::THREADS) dg_prism_elements_kernel(
 
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                              const double *xyz, const double *k_el, const double *D_el, double f,
-                             const long long *boff, const int *roff, double *val, double *rhs) {
+                             const long long *boff, const int *roff, double *val, double *rhs, int variant) {
   if (count <= 0) return 0;
   GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
+  GB_CHECK(variant >= 0 && variant < DG_VOL_VARIANTS, "volume kernel variant out of range");
   DgDeviceTables *tb = nullptr;
   int r = dg_tables_for_device(device, &tb);
   if (r < 0) return r;
-#define GB_DG_LAUNCH(PP)                                                                                 \
-  dg_prism_elements_kernel<PP><<<count, DgDims<PP>::THREADS, 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, \
-                                                             tb->D[PP], tb->PHI[PP], tb->QP[PP], boff, roff, \
-                                                             val, rhs)
-  switch (p) {
-    case 1: GB_DG_LAUNCH(1); break;
-    case 2: GB_DG_LAUNCH(2); break;
-    case 3: GB_DG_LAUNCH(3); break;
-    default: GB_DG_LAUNCH(4); break;
+#define GB_DG_LAUNCH(PP, VV)                                                                               \
+  dg_prism_elements_kernel<PP, dg_vol_threads(PP, VV), dg_vol_qchunk(PP, VV)>                             \
+      <<<count, dg_vol_threads(PP, VV), 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, tb->D[PP],    \
+                                                 tb->PHI[PP], tb->QP[PP], boff, roff, val, rhs)
+#define GB_DG_P(PP)                  \
+  switch (variant) {                 \
+    case 0: GB_DG_LAUNCH(PP, 0); break; \
+    case 1: GB_DG_LAUNCH(PP, 1); break; \
+    default: GB_DG_LAUNCH(PP, 2); break; \
   }
+  switch (p) {
+    case 1: GB_DG_P(1); break;
+    case 2: GB_DG_P(2); break;
+    case 3: GB_DG_P(3); break;
+    default: GB_DG_P(4); break;
+  }
+#undef GB_DG_P
 #undef GB_DG_LAUNCH
   GB_CUDA(cudaGetLastError());
   return 1;

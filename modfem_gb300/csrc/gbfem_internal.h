@@ -118,7 +118,7 @@ struct DgHalfFace {
 int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                           const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                           const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
-                          const int *roff, double *val, double *rhs);
+                          const int *roff, double *val, double *rhs, int variant);
 // Variable-block CRS (one block row per DG element, dense column-major
 // blocks with the row block's size as leading dimension) and block Jacobi.
 int launch_dg_block_inverse(cudaStream_t st, int nel, const int *roff, const long long *boff_diag,
@@ -145,7 +145,7 @@ int launch_dg_tc_volume(cudaStream_t st, int device, int p, int count, const int
                         const int *roff, double *val, double *rhs, int *err);
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                              const double *xyz, const double *k_el, const double *D_el, double f,
-                             const long long *boff, const int *roff, double *val, double *rhs);
+                             const long long *boff, const int *roff, double *val, double *rhs, int variant);
 
 }  // namespace gbfem
 
@@ -197,6 +197,7 @@ struct gbfem_ctx_s {
   int dg_nfa = -1;  // -1: no face table (volume terms only)
   double dg_pen = 10.0;
   int dg_volume_mode = 0;  // GBFEM_DG_VOLUME_FP64 / _TC
+  int dg_var_vol[5] = {0, 0, 0, 0, 0}, dg_var_face[5] = {0, 0, 0, 0, 0};  // launch-shape variants per degree
   gbfem::DevBuf<int> dg_hf_ptr, dg_p_d;
   gbfem::DevBuf<gbfem::DgHalfFace> dg_hf;
   // DG block Jacobi: inverted diagonal blocks, block e at dg_dinv_off_d[e]

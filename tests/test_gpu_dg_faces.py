@@ -238,3 +238,28 @@ def test_dg_iterative_refinement_vs_fp64_gmres_larger(gb):
     # both stop on residuals; their difference is bounded by the FP64 GMRES
     # stopping accuracy (1e-12 on the preconditioned residual)
     assert vec_rel_err(xir, x64) < 1e-7
+
+
+def test_dg_autotune_choices_do_not_change_results(gb):
+    """Every launch shape gives the same bits; the tuner's choice is one of them."""
+    from modfem_gb300.mesh import anisotropic_tensors, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(5, jitter=0.2, seed=3)
+    F = prism_faces(m)
+    pdeg = np.random.default_rng(3).integers(1, 5, m.nel)
+    c = _context(gb, m, F, pdeg, D=anisotropic_tensors(m.nel, seed=3).reshape(m.nel, 9), g=0.2)
+    ref = None
+    for v in range(3):
+        for fv in range(2):
+            c.dg_set_variants(vol=[0, v, v, v, v], face=[0, fv, fv, fv, fv])
+            c.dg_assemble()
+            out = c.dg_get_matrix()
+            if ref is None:
+                ref = out
+            else:
+                assert np.array_equal(out[0], ref[0]) and np.array_equal(out[1], ref[1]), (v, fv)
+    vol, face, ms = c.dg_autotune(sample=1000)
+    assert all(0 <= v < 3 for v in vol[1:]) and all(0 <= f < 2 for f in face[1:])
+    assert np.all(ms[:, :3] > 0)
+    c.dg_assemble()
+    out = c.dg_get_matrix()
+    assert np.array_equal(out[0], ref[0])
