@@ -97,6 +97,11 @@ int gbfem_set_crs_structure(gbfem_ctx ctx, int ndof, const int *dof_of_node, lon
  * the elements, utd_util/uts_ls_intf.c:182-300; sorted neighbour columns) and
  * the element/face assembly tables and colours used by gbfem_assemble. */
 int gbfem_build_structure(gbfem_ctx ctx, int *ndof, long long *nnz, int *nr_colors);
+/* The same structure built on the device (first-appearance ranks by an
+ * atomicMin and a scan, incidence lists, per-row sorted unique columns,
+ * binary-searched tables): identical arrays, no host pass over the mesh.
+ * Makes no colouring, so gbfem_assemble then takes GBFEM_SCATTER_ATOMIC. */
+int gbfem_build_structure_device(gbfem_ctx ctx, int *ndof, long long *nnz);
 /* Copies the structure out (any pointer may be NULL). */
 int gbfem_get_crs_structure(gbfem_ctx ctx, int *dof_of_node, int *row_ptr, int *col_ind);
 /* Copies out the element assembly tables gbfem_build_structure made, in the

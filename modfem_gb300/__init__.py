@@ -35,6 +35,7 @@ SIGNATURES = [
     ("gbfem_set_coefficients", _ci, [_vp, _vp, _vp, _cd, _cd, _cd]),
     ("gbfem_set_crs_structure", _ci, [_vp, _ci, _vp, _cll, _vp, _vp]),
     ("gbfem_build_structure", _ci, [_vp, _pi, _pll, _pi]),
+    ("gbfem_build_structure_device", _ci, [_vp, _pi, _pll]),
     ("gbfem_get_crs_structure", _ci, [_vp, _vp, _vp, _vp]),
     ("gbfem_get_element_tables", _ci, [_vp, _vp]),
     ("gbfem_create_assemble_stiff_mat", _ci,
@@ -177,6 +178,13 @@ class Context:
         self._check(self.L.gbfem_build_structure(self._h, ctypes.byref(nd), ctypes.byref(nnz), ctypes.byref(nc)))
         self.ndof, self.nnz = nd.value, nnz.value
         return nd.value, nnz.value, nc.value
+
+    def build_structure_device(self):
+        """gbfem_build_structure_device: the same arrays built by kernels (no colouring)."""
+        nd, nnz = ctypes.c_int(), ctypes.c_longlong()
+        self._check(self.L.gbfem_build_structure_device(self._h, ctypes.byref(nd), ctypes.byref(nnz)))
+        self.ndof, self.nnz = nd.value, nnz.value
+        return nd.value, nnz.value
 
     def get_crs_structure(self):
         dn = np.zeros(self.nno, np.int32)

@@ -271,6 +271,40 @@ int gbfem_build_structure(gbfem_ctx c, int *ndof, long long *nnz, int *nr_colors
   return 0;
 }
 
+int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
+  GB_CHECK(c && c->nno > 0, "mesh not set");
+  GB_CUDA(cudaSetDevice(c->device));
+  GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+  int nd = 0;
+  long long nz = 0;
+  GB_TRY(gbfem::build_device_structure(c->stream, c->nno, c->nel, c->nv, c->el_nodes.p, c->dof_of_node, c->row_ptr,
+                                       c->col_ind, c->el_table, c->err.p, &nd, &nz));
+  c->ndof = nd;
+  c->nnz = nz;
+  // host copies for the getters; no colouring (atomic scatter only)
+  c->hs.ndof = nd;
+  c->hs.dof_of_node.resize(c->nno);
+  c->hs.row_ptr.resize((size_t)nd + 1);
+  c->hs.col_ind.resize((size_t)nz);
+  c->hs.el_table.resize(c->el_table.n);
+  GB_CUDA(cudaMemcpyAsync(c->hs.dof_of_node.data(), c->dof_of_node.p, (size_t)c->nno * sizeof(int),
+                          cudaMemcpyDeviceToHost, c->stream));
+  GB_CUDA(cudaMemcpyAsync(c->hs.row_ptr.data(), c->row_ptr.p, ((size_t)nd + 1) * sizeof(int), cudaMemcpyDeviceToHost,
+                          c->stream));
+  GB_CUDA(cudaMemcpyAsync(c->hs.col_ind.data(), c->col_ind.p, (size_t)nz * sizeof(int), cudaMemcpyDeviceToHost,
+                          c->stream));
+  GB_CUDA(cudaMemcpyAsync(c->hs.el_table.data(), c->el_table.p, c->el_table.n * sizeof(int), cudaMemcpyDeviceToHost,
+                          c->stream));
+  c->h_el_color_ptr.clear();
+  c->h_fa_color_ptr.clear();
+  GB_TRY(alloc_matrix(c));
+  c->have_structure = c->have_tables = true;
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  if (ndof) *ndof = nd;
+  if (nnz) *nnz = nz;
+  return 0;
+}
+
 int gbfem_get_crs_structure(gbfem_ctx c, int *dof_of_node, int *row_ptr, int *col_ind) {
   GB_CHECK(c && c->have_structure, "structure not set");
   if (dof_of_node && !c->hs.dof_of_node.empty())

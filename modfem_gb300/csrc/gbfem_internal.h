@@ -72,6 +72,9 @@ struct HostStructure {
 
 int build_host_structure(int nno, int nel, int nv, const int *el_nodes, int nfa, const int *fa_el,
                          const int *fa_side, HostStructure &hs);
+int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int *el_nodes, DevBuf<int> &dof_of_node,
+                           DevBuf<int> &row_ptr, DevBuf<int> &col_ind, DevBuf<int> &el_table, int *err,
+                           int *ndof_out, long long *nnz_out);
 void color_entities(int nent, int nv, const std::vector<int> &ent_dofs, int nd, std::vector<int> &color_ptr,
                     std::vector<int> &perm);
 

@@ -1,0 +1,282 @@
+// Device-side structure build for std meshes: the same DOF order, CRS and
+// assembly tables as the host build (and as the reference's sir_create),
+// made with kernels so that a new mesh (a served request) needs no host pass.
+//
+//  1. first appearance of each vertex: first[n] = min over its incidences of
+//     (element * nv + local vertex) (atomicMin); the DOF of n is the number
+//     of used vertices whose first appearance comes earlier = an exclusive
+//     scan of a 0/1 mark at every first-appearance position
+//     (utr_get_list_dof_ent, utd_util/uts_ls_intf.c:182-300);
+//  2. DOF -> element incidence lists (count, scan, fill in any order);
+//  3. CRS rows: the DOFs of the incident elements of each row, sorted and
+//     deduplicated per row (two passes: lengths, scan, columns), diagonal
+//     included (sis_mkb_intf.c:1128, lad_crs/las_crs_intf.c:72-300);
+//  4. element tables: for every (row dof j, column dof i) of an element the
+//     position found by binary search in row j, then the rhs rows
+//     (lar_fill_assembly_table_int_ent_crs, las_crs_intf.c:354-438).
+// Every output is independent of thread scheduling, so it equals the host
+// build bit for bit.  The elements-sharing-a-DOF colouring for the colour
+// scatter stays on the host (gbfem_build_structure).
+
+#include <climits>
+
+#include "gbfem_internal.h"
+
+namespace gbfem {
+
+constexpr int SG_T = 256;
+constexpr int SG_PER = 8;
+constexpr int SG_CHUNK = SG_T * SG_PER;
+constexpr int SG_MAXROW = 256;  // candidate column slots per row (6 x incident elements)
+
+__device__ __forceinline__ int sg_block_exclusive(int v, int *total) {
+  __shared__ int ws[SG_T / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int s = lane < SG_T / 32 ? ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < SG_T / 32) ws[lane] = s;
+  }
+  __syncthreads();
+  const int before = (w > 0 ? ws[w - 1] : 0) + x - v;
+  *total = ws[SG_T / 32 - 1];
+  __syncthreads();
+  return before;
+}
+
+// exclusive scan, three kernels: chunk sums, scan of the sums, chunk scans
+__global__ void sg_chunk_sums(long long n, const int *__restrict__ in, int *__restrict__ sums) {
+  long long base = (long long)blockIdx.x * SG_CHUNK;
+  int s = 0;
+  for (int t = 0; t < SG_PER; t++) {
+    const long long i = base + (long long)t * SG_T + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  int tot;
+  sg_block_exclusive(s, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void sg_scan_sums(int nb, int *sums, int *total) {
+  // one CTA: each thread scans a contiguous range sequentially
+  const int per = (nb + SG_T - 1) / SG_T, lo = threadIdx.x * per, hi = min(nb, lo + per);
+  int s = 0;
+  for (int i = lo; i < hi; i++) s += sums[i];
+  int tot;
+  int off = sg_block_exclusive(s, &tot);
+  for (int i = lo; i < hi; i++) {
+    const int v = sums[i];
+    sums[i] = off;
+    off += v;
+  }
+  if (threadIdx.x == 0) *total = tot;
+}
+
+__global__ void sg_chunk_scan(long long n, const int *__restrict__ in, const int *__restrict__ sums,
+                              int *__restrict__ out) {
+  long long base = (long long)blockIdx.x * SG_CHUNK + (long long)threadIdx.x * SG_PER;
+  int v[SG_PER], s = 0;
+#pragma unroll
+  for (int t = 0; t < SG_PER; t++) {
+    const long long i = base + t;
+    v[t] = i < n ? in[i] : 0;
+    s += v[t];
+  }
+  int tot;
+  int off = sums[blockIdx.x] + sg_block_exclusive(s, &tot);
+#pragma unroll
+  for (int t = 0; t < SG_PER; t++) {
+    const long long i = base + t;
+    if (i < n) out[i] = off;
+    off += v[t];
+  }
+}
+
+// out[i] = sum_{k < i} in[k] for i <= n (out has n + 1 entries); total in out[n]
+static int sg_scan(cudaStream_t st, long long n, const int *in, int *out, DevBuf<int> &tmp) {
+  const int nb = (int)((n + SG_CHUNK - 1) / SG_CHUNK);
+  GB_CHECK(nb <= SG_T * 4096, "scan too long");
+  if (tmp.alloc((size_t)nb + 1) < 0) return -1;
+  if (nb > 0) {
+    sg_chunk_sums<<<nb, SG_T, 0, st>>>(n, in, tmp.p);
+    sg_scan_sums<<<1, SG_T, 0, st>>>(nb, tmp.p, out + n);
+    sg_chunk_scan<<<nb, SG_T, 0, st>>>(n, in, tmp.p, out);
+  } else {
+    GB_CUDA(cudaMemsetAsync(out, 0, sizeof(int), st));
+  }
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+__global__ void sg_fill(int n, int v, int *a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = v;
+}
+
+__global__ void sg_first(long long m, int nv, const int *__restrict__ el_nodes, int *first) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x)
+    atomicMin(first + el_nodes[i], (int)i);
+}
+
+__global__ void sg_mark(int nno, const int *__restrict__ first, int *mark) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n < nno && first[n] != INT_MAX) mark[first[n]] = 1;
+}
+
+__global__ void sg_dofs(int nno, const int *__restrict__ first, const int *__restrict__ rank, int *dof_of_node) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n < nno) dof_of_node[n] = first[n] == INT_MAX ? -1 : rank[first[n]];
+}
+
+__global__ void sg_el_dofs(long long m, const int *__restrict__ el_nodes, const int *__restrict__ dof_of_node,
+                           int *el_dofs, int *inc_cnt) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+    const int d = dof_of_node[el_nodes[i]];
+    el_dofs[i] = d;
+    atomicAdd(inc_cnt + d, 1);
+  }
+}
+
+__global__ void sg_inc_fill(long long m, int nv, const int *__restrict__ el_dofs, int *cursor, int *inc) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x)
+    inc[atomicAdd(cursor + el_dofs[i], 1)] = (int)(i / nv);
+}
+
+// sorted unique columns of row r into buf (returns the count, or -1 if the
+// row has more candidates than SG_MAXROW)
+__device__ int sg_row(int r, int nv, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                      const int *__restrict__ el_dofs, int *buf) {
+  int n = 0;
+  for (int k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+    const int *ed = el_dofs + (size_t)inc[k] * nv;
+    for (int j = 0; j < nv; j++) {
+      if (n >= SG_MAXROW) return -1;
+      // insertion into the sorted prefix, skipping duplicates
+      const int v = ed[j];
+      int p = n;
+      while (p > 0 && buf[p - 1] > v) p--;
+      if (p > 0 && buf[p - 1] == v) continue;
+      for (int q = n; q > p; q--) buf[q] = buf[q - 1];
+      buf[p] = v;
+      n++;
+    }
+  }
+  return n;
+}
+
+__global__ void sg_row_len(int nd, int nv, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                           const int *__restrict__ el_dofs, int *len, int *err) {
+  int buf[SG_MAXROW];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nd) return;
+  const int n = sg_row(r, nv, inc_ptr, inc, el_dofs, buf);
+  if (n < 0) {
+    atomicExch(err, 7);
+    len[r] = 0;
+  } else {
+    len[r] = n;
+  }
+}
+
+__global__ void sg_row_fill(int nd, int nv, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                            const int *__restrict__ el_dofs, const int *__restrict__ row_ptr, int *col_ind) {
+  int buf[SG_MAXROW];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nd) return;
+  const int n = sg_row(r, nv, inc_ptr, inc, el_dofs, buf);
+  for (int i = 0; i < n && row_ptr[r] + i < row_ptr[r + 1]; i++) col_ind[row_ptr[r] + i] = buf[i];
+}
+
+__global__ void sg_tables(int nel, int nv, const int *__restrict__ el_dofs, const int *__restrict__ row_ptr,
+                          const int *__restrict__ col_ind, int *table) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  const int tl = nv * nv + nv;
+  const int *ed = el_dofs + (size_t)e * nv;
+  int *t = table + (size_t)e * tl;
+  for (int j = 0; j < nv; j++) {
+    const int r = ed[j];
+    for (int i = 0; i < nv; i++) {
+      int lo = row_ptr[r], hi = row_ptr[r + 1];  // first position with col >= ed[i]
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (col_ind[mid] < ed[i])
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      t[j + i * nv] = lo;
+    }
+    t[nv * nv + j] = r;
+  }
+}
+
+int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int *el_nodes, DevBuf<int> &dof_of_node,
+                           DevBuf<int> &row_ptr, DevBuf<int> &col_ind, DevBuf<int> &el_table, int *err,
+                           int *ndof_out, long long *nnz_out) {
+  const long long m = (long long)nel * nv;
+  DevBuf<int> first, mark, rank, el_dofs, inc_cnt, inc_ptr, inc, len, tmp;
+  auto cleanup = [&]() {
+    first.release(); mark.release(); rank.release(); el_dofs.release(); inc_cnt.release();
+    inc_ptr.release(); inc.release(); len.release(); tmp.release();
+  };
+  auto fail = [&](int r) { cleanup(); return r; };
+  const int g1 = 152 * 8;
+  if (first.alloc(nno) < 0 || mark.alloc(m + 1) < 0 || rank.alloc(m + 1) < 0 || dof_of_node.alloc(nno) < 0 ||
+      el_dofs.alloc(m) < 0)
+    return fail(-1);
+  // 1. DOF order
+  sg_fill<<<(nno + 255) / 256, 256, 0, st>>>(nno, INT_MAX, first.p);  // unused vertices keep INT_MAX
+  sg_first<<<g1, 256, 0, st>>>(m, nv, el_nodes, first.p);
+  GB_CUDA(cudaMemsetAsync(mark.p, 0, (size_t)(m + 1) * sizeof(int), st));
+  sg_mark<<<(nno + 255) / 256, 256, 0, st>>>(nno, first.p, mark.p);
+  if (sg_scan(st, m, mark.p, rank.p, tmp) < 0) return fail(-1);
+  sg_dofs<<<(nno + 255) / 256, 256, 0, st>>>(nno, first.p, rank.p, dof_of_node.p);
+  int nd = 0;
+  GB_CUDA(cudaMemcpyAsync(&nd, rank.p + m, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  // 2. incidence
+  if (inc_cnt.alloc((size_t)nd + 1) < 0 || inc_ptr.alloc((size_t)nd + 1) < 0 || inc.alloc(m) < 0) return fail(-1);
+  GB_CUDA(cudaMemsetAsync(inc_cnt.p, 0, (size_t)(nd + 1) * sizeof(int), st));
+  sg_el_dofs<<<g1, 256, 0, st>>>(m, el_nodes, dof_of_node.p, el_dofs.p, inc_cnt.p);
+  if (sg_scan(st, nd, inc_cnt.p, inc_ptr.p, tmp) < 0) return fail(-1);
+  GB_CUDA(cudaMemcpyAsync(inc_cnt.p, inc_ptr.p, (size_t)nd * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  sg_inc_fill<<<g1, 256, 0, st>>>(m, nv, el_dofs.p, inc_cnt.p, inc.p);
+  // 3. rows
+  if (len.alloc((size_t)nd + 1) < 0 || row_ptr.alloc((size_t)nd + 1) < 0) return fail(-1);
+  sg_row_len<<<(nd + 127) / 128, 128, 0, st>>>(nd, nv, inc_ptr.p, inc.p, el_dofs.p, len.p, err);
+  if (sg_scan(st, nd, len.p, row_ptr.p, tmp) < 0) return fail(-1);
+  int nnz = 0, herr = 0;
+  GB_CUDA(cudaMemcpyAsync(&nnz, row_ptr.p + nd, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  if (herr) {
+    cleanup();
+    GB_CHECK(false, "a vertex has more neighbours than the device structure build supports");
+  }
+  if (col_ind.alloc((size_t)nnz) < 0) return fail(-1);
+  sg_row_fill<<<(nd + 127) / 128, 128, 0, st>>>(nd, nv, inc_ptr.p, inc.p, el_dofs.p, row_ptr.p, col_ind.p);
+  // 4. element tables
+  if (el_table.alloc((size_t)nel * (nv * nv + nv)) < 0) return fail(-1);
+  sg_tables<<<(nel + 127) / 128, 128, 0, st>>>(nel, nv, el_dofs.p, row_ptr.p, col_ind.p, el_table.p);
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
+  cleanup();
+  *ndof_out = nd;
+  *nnz_out = nnz;
+  return 0;
+}
+
+}  // namespace gbfem

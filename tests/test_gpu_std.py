@@ -366,3 +366,39 @@ def test_tet_mesh_structure_and_assembly_vs_oracle(gb):
         val, rhs = c.get_matrix()
         assert crs_rel_err(rp, val, vo, energy_scale(rp, ci, vo)) < REL_TOL
         assert vec_rel_err(rhs, ro) < REL_TOL
+
+
+# ------------------------------------------------ structure built on the device
+@pytest.mark.parametrize("name", ["std_n4", "std_n10"])
+def test_device_structure_vs_reference(gb, name):
+    """gbfem_build_structure_device: DOF order, CRS and tables identical to
+    the reference's (and to the host build); atomic assembly on it."""
+    g = load(name)
+    m = FixtureMesh(g)
+    c = make_ctx(gb, m, g["k"])
+    c.build_structure()
+    host = (c.get_crs_structure(), c.get_element_tables())
+    nd, nnz = c.build_structure_device()
+    dn, rp, ci = c.get_crs_structure()
+    assert np.array_equal(dn, g["dof_of_node"])
+    assert np.array_equal(rp, g["row_ptr"]) and np.array_equal(ci, g["col_ind"])
+    assert np.array_equal(c.get_element_tables(), host[1])
+    c.assemble(gb.SCATTER_ATOMIC)
+    val, rhs = c.get_matrix()
+    assert crs_rel_err(rp, val, g["crs_val"], energy_scale(rp, ci, g["crs_val"])) < REL_TOL
+    assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL
+
+
+@pytest.mark.parametrize("kind", ["prism", "tet"])
+def test_device_structure_vs_host_larger(gb, kind):
+    """Jittered 2M-free sizes: 30^3 x 2 prisms / 12^3 x 6 tetrahedra, host and
+    device builds bit-identical."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh, structured_tet_mesh
+    m = structured_prism_mesh(30, jitter=0.2, seed=2) if kind == "prism" else structured_tet_mesh(12, jitter=0.2, seed=2)
+    c = make_ctx(gb, m, lognormal_k(m.nel, seed=2))
+    c.build_structure()
+    h = c.get_crs_structure() + (c.get_element_tables(),)
+    c.build_structure_device()
+    d = c.get_crs_structure() + (c.get_element_tables(),)
+    for a, b in zip(h, d):
+        assert np.array_equal(a, b)
