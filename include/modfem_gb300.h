@@ -293,6 +293,29 @@ int gbfem_host_free(void *ptr);
 int gbfem_measure_fp64_peak(gbfem_ctx ctx, double *tflops);
 
 /* ---------------------------------------------------------------------- */
+/* file formats (host only; no GPU needed)                                  */
+/* ---------------------------------------------------------------------- */
+/* Reads a jk ("gradmesh") prism mesh as mmr_import_mesh_grad does
+ * (mmd_prism/mms_prism_input_gradmesh.c:30-420), in the reference's
+ * numbering: sizes[3] = nno, nel, nfa (call with NULL arrays first);
+ * xyz[3 nno]; el_nodes[6 nel] (0-based, mmr_el_node_coor order); the face
+ * table of gbfem_dg_set_faces (type, bc, two neighbours, first neighbour's
+ * side, four vertices in mmr_fa_node_coor order) in face-id order. */
+int gbfem_read_jk(const char *path, int *sizes, double *xyz, int *el_nodes, int *fa_type, int *fa_bc, int *fa_el,
+                  int *fa_side, int *fa_nodes);
+/* field.dmp of a std scalar field as apr_write_field writes it
+ * (apd_std_lin/aps_std_lin_intf.c:539-680): x indexed by dof_of_node. */
+int gbfem_write_field_std(const char *path, int nno, const int *dof_of_node, const double *x);
+/* field.dmp of a DG field (apd_dg_prism/aps_dg_prism_intf.c:459-560):
+ * degrees p_el (1..4, written as -101 p), coefficients of element e at
+ * x[dof_off[e] .. dof_off[e+1]).  uniform != 0 writes one degree line (the
+ * first element's), as the reference does for a field created with one
+ * degree (its field_p->uniform), whatever the element degrees are later;
+ * uniform == 0 one line per element. */
+int gbfem_write_field_dg(const char *path, int nel, const int *p_el, const int *dof_off, const double *x,
+                         int uniform);
+
+/* ---------------------------------------------------------------------- */
 /* serving (no counterpart in the reference)                                */
 /* ---------------------------------------------------------------------- */
 /* A server takes independent heat problems as they arrive and integrates,

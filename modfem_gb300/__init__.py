@@ -66,6 +66,9 @@ SIGNATURES = [
     ("gbfem_host_alloc", _vp, [_cll]),
     ("gbfem_host_free", _ci, [_vp]),
     ("gbfem_measure_fp64_peak", _ci, [_vp, _pd]),
+    ("gbfem_read_jk", _ci, [ctypes.c_char_p, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("gbfem_write_field_std", _ci, [ctypes.c_char_p, _ci, _vp, _vp]),
+    ("gbfem_write_field_dg", _ci, [ctypes.c_char_p, _ci, _vp, _vp, _vp, _ci]),
     ("gbfem_server_create", _ci, [_pvp, _ci, _cll, _ci, _ci]),
     ("gbfem_server_destroy", _ci, [_vp]),
     ("gbfem_server_submit", _cll, [_vp, _vp]),

@@ -840,3 +840,22 @@ int refh_all_faces(int *out)
   }
   return cnt;
 }
+
+/* Field dump through the reference's own writer (apr_write_field): the
+ * values are first stored in the field with apr_write_ent_dofs, per vertex
+ * (std: vals[n] for vertex n+1, NaN = vertex without dofs) or per element
+ * (DG: vals + off[e] .. off[e+1]). */
+int refh_write_field(const char *path, int ent_type, int nent, const double *vals, const int *off)
+{
+  int i;
+  for (i = 0; i < nent; i++) {
+    if (ent_type == APC_VERTEX) {
+      double v = vals[i];
+      if (v != v) continue;
+      apr_write_ent_dofs(h_field_id, APC_VERTEX, i + 1, 1, 1, &v);
+    } else {
+      apr_write_ent_dofs(h_field_id, APC_ELEMENT, i + 1, off[i + 1] - off[i], 1, (double *)vals + off[i]);
+    }
+  }
+  return apr_write_field(h_field_id, 1, 1, 0.0, (char *)path);
+}

@@ -19,6 +19,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 
 APC_ELEMENT = 4
 APC_FACE = 3
+APC_VERTEX = 1
 
 
 def _p(a):

@@ -219,9 +219,47 @@ def run_dg_assembly(name):
     print(f"{name}: {m.nel} DG prisms, ndof {R.ndof}, nnz {ci.size}, gmres {nit} it", file=sys.stderr)
 
 
+def run_fields(name="fields"):
+    """field.dmp files written by the reference's apr_write_field for the
+    std_n4 solution (std module) and for the dg_asm_mixed solution (DG
+    module), with the values the fixtures hold."""
+    import ctypes
+    import refmod
+    from modfem_gb300.mesh import structured_prism_mesh, write_jk
+    tmp = tempfile.mkdtemp()
+    g = dict(np.load(os.path.join(HERE, "std_n4.npz")))
+    jk = os.path.join(tmp, "mesh4.jk")
+    write_jk(jk, int(g["n"]))
+    R = refmod.RefModfem("std")
+    R.load_jk(jk)
+    R.set_node_coords(g["coords"])
+    R.init_field("s", 1)
+    vals = np.full(g["dof_of_node"].size, np.nan)
+    has = g["dof_of_node"] >= 0
+    vals[has] = g["gmres_x"][g["dof_of_node"][has]]
+    out = os.path.join(HERE, "field_std_n4.dmp")
+    R.L.refh_write_field.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    R.L.refh_write_field(out.encode(), refmod.APC_VERTEX, vals.size, vals.ctypes.data, None)
+    gd = dict(np.load(os.path.join(HERE, "dg_asm_mixed.npz")))
+    jk = os.path.join(tmp, "mesh2.jk")
+    write_jk(jk, int(gd["n"]))
+    R = refmod.RefModfem("dg")
+    R.load_jk(jk)
+    R.set_node_coords(gd["coords"])
+    R.init_field("t", 101 * int(gd["pdeg"].max()))
+    for e, p in enumerate(gd["pdeg"]):
+        R.L.refh_set_el_pdeg(e + 1, int(101 * p))
+    off = np.concatenate([gd["dof_posglob"], [gd["gmres_x"].size]]).astype(np.int32)
+    out = os.path.join(HERE, "field_dg_mixed_n2.dmp")
+    R.L.refh_write_field.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    R.L.refh_write_field(out.encode(), refmod.APC_ELEMENT, gd["pdeg"].size, gd["gmres_x"].ctypes.data,
+                         off.ctypes.data)
+    print("fields: field_std_n4.dmp, field_dg_mixed_n2.dmp", file=sys.stderr)
+
+
 def main(argv):
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref")])
-    names = argv or list(CASES) + ["std_tet_n2", "dg_el_n2", "dg_el_aniso_n2"] + list(DG_ASM_CASES)
+    names = argv or list(CASES) + ["std_tet_n2", "dg_el_n2", "dg_el_aniso_n2"] + list(DG_ASM_CASES) + ["fields"]
     if len(names) == 1 and os.environ.get("MAKE_GOLDEN_CHILD"):
         with open(os.devnull, "w") as dn:
             # the reference prints progress on stdout; keep only our stderr summary
@@ -232,6 +270,8 @@ def main(argv):
                 run_dg_elements(names[0])
             elif names[0] in DG_ASM_CASES:
                 run_dg_assembly(names[0])
+            elif names[0] == "fields":
+                run_fields()
             else:
                 run_case(names[0])
         return
