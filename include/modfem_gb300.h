@@ -316,6 +316,33 @@ int gbfem_write_field_dg(const char *path, int nel, const int *p_el, const int *
                          int uniform);
 
 /* ---------------------------------------------------------------------- */
+/* batched DG volume integrals of mixed element types and degrees          */
+/* ---------------------------------------------------------------------- */
+/* One persistent kernel, replayed as a CUDA graph, integrates the element
+ * matrices and load vectors of any mix of DG prisms (tensor basis, as
+ * apr_num_int_el of apd_dg_prism, aps_dg_prism_intf.c:1239-1728) and affine
+ * DG tetrahedra (complete monomial basis xi^a eta^b zeta^c, a+b+c <= p, on
+ * the reference tetrahedron; no reference counterpart, apd_dg_prism is
+ * prism-only) of degrees 1..4: -div(A grad u) = f, volume terms.  The blocks
+ * are stored prisms first, then tetrahedra, each ns x ns column-major
+ * (ns = 6, 18, 40, 75 for prisms; 4, 10, 20, 35 for tetrahedra), load
+ * vectors likewise.  The prism blocks and load vectors equal, bit for bit,
+ * the diagonal blocks and rhs gbfem_dg_assemble produces without a face
+ * table. */
+typedef struct gbfem_batch_s *gbfem_batch;
+int gbfem_batch_create(gbfem_batch *batch, int device);
+int gbfem_batch_destroy(gbfem_batch batch);
+/* prism_xyz[18 np] (mmr_el_node_coor order), prism_A[9 np] row-major
+ * tensors, prism_p[np]; tet_xyz[12 nt], tet_A[9 nt], tet_p[nt]; tet_tile:
+ * tetrahedra per work tile (1..256).  nval, nrhs: output sizes. */
+int gbfem_batch_set(gbfem_batch batch, int np, const double *prism_xyz, const double *prism_A, const int *prism_p,
+                    int nt, const double *tet_xyz, const double *tet_A, const int *tet_p, double f, int tet_tile,
+                    long long *nval, long long *nrhs);
+/* Replays the graph; ms: device time of the launch.  Returns the tiles. */
+int gbfem_batch_run(gbfem_batch batch, double *ms);
+int gbfem_batch_get(gbfem_batch batch, double *vals, double *rhs);
+
+/* ---------------------------------------------------------------------- */
 /* serving (no counterpart in the reference)                                */
 /* ---------------------------------------------------------------------- */
 /* A server takes independent heat problems as they arrive and integrates,

@@ -69,6 +69,11 @@ SIGNATURES = [
     ("gbfem_read_jk", _ci, [ctypes.c_char_p, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("gbfem_write_field_std", _ci, [ctypes.c_char_p, _ci, _vp, _vp]),
     ("gbfem_write_field_dg", _ci, [ctypes.c_char_p, _ci, _vp, _vp, _vp, _ci]),
+    ("gbfem_batch_create", _ci, [_pvp, _ci]),
+    ("gbfem_batch_destroy", _ci, [_vp]),
+    ("gbfem_batch_set", _ci, [_vp, _ci, _vp, _vp, _vp, _ci, _vp, _vp, _vp, _cd, _ci, _pll, _pll]),
+    ("gbfem_batch_run", _ci, [_vp, _pd]),
+    ("gbfem_batch_get", _ci, [_vp, _vp, _vp]),
     ("gbfem_server_create", _ci, [_pvp, _ci, _cll, _ci, _ci]),
     ("gbfem_server_destroy", _ci, [_vp]),
     ("gbfem_server_submit", _cll, [_vp, _vp]),
@@ -360,6 +365,71 @@ class Context:
         v = ctypes.c_double()
         self._check(self.L.gbfem_measure_fp64_peak(self._h, ctypes.byref(v)))
         return v.value
+
+
+PRISM_NS = {1: 6, 2: 18, 3: 40, 4: 75}
+TET_NS = {1: 4, 2: 10, 3: 20, 4: 35}
+
+
+class Batch:
+    """Batched DG volume integrals of mixed prisms and tetrahedra of degrees
+    1..4 in one persistent launch (gbfem_batch_*)."""
+
+    def __init__(self, device=0):
+        self.L = load_library()
+        self._h = ctypes.c_void_p()
+        self._check(self.L.gbfem_batch_create(ctypes.byref(self._h), device))
+
+    def _check(self, rc):
+        if rc < 0:
+            raise GbFemError(self.L.gbfem_last_error().decode())
+        return rc
+
+    def set(self, prism_xyz, prism_A, prism_p, tet_xyz, tet_A, tet_p, f=1.0, tet_tile=32):
+        """prism_xyz (np, 6, 3), prism_A (np, 3, 3), prism_p (np,); tets
+        likewise with (nt, 4, 3).  Returns (nval, nrhs)."""
+        self._in = [_f64(prism_xyz), _f64(prism_A), _i32(prism_p), _f64(tet_xyz), _f64(tet_A), _i32(tet_p)]
+        self.pp, self.tp = self._in[2].ravel(), self._in[5].ravel()
+        nv, nr = ctypes.c_longlong(), ctypes.c_longlong()
+        self._check(self.L.gbfem_batch_set(self._h, self.pp.size, _p(self._in[0]), _p(self._in[1]), _p(self._in[2]),
+                                           self.tp.size, _p(self._in[3]), _p(self._in[4]), _p(self._in[5]), f,
+                                           tet_tile, ctypes.byref(nv), ctypes.byref(nr)))
+        self.nval, self.nrhs = nv.value, nr.value
+        return self.nval, self.nrhs
+
+    def run(self):
+        """Runs the batch; returns the device time in ms."""
+        ms = ctypes.c_double()
+        self._check(self.L.gbfem_batch_run(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def get(self):
+        """(vals, rhs) flat, blocks in input order: prisms, then tetrahedra."""
+        vals, rhs = np.empty(self.nval), np.empty(self.nrhs)
+        self._check(self.L.gbfem_batch_get(self._h, _p(vals), _p(rhs)))
+        return vals, rhs
+
+    def blocks(self):
+        """Lists of (ns, ns) element matrices and (ns,) load vectors."""
+        vals, rhs = self.get()
+        mats, loads, v, r = [], [], 0, 0
+        for ns in [PRISM_NS[int(p)] for p in self.pp] + [TET_NS[int(p)] for p in self.tp]:
+            mats.append(vals[v:v + ns * ns].reshape(ns, ns).T)
+            loads.append(rhs[r:r + ns])
+            v += ns * ns
+            r += ns
+        return mats, loads
+
+    def close(self):
+        if self._h:
+            self.L.gbfem_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PinnedArray:

@@ -22,16 +22,10 @@
 
 #include "gbfem_internal.h"
 #include "dg_tables.h"
+#include "dg_volume.cuh"
 #include "prism_std.cuh"
 
 namespace gbfem {
-
-// per-degree device tables: D[q][a][u] reference derivatives, PHI[q][u] values
-struct DgDeviceTables {
-  const double *D[GB_DG_PMAX + 1];
-  const double *PHI[GB_DG_PMAX + 1];
-  const double *QP[GB_DG_PMAX + 1];  // (xi, eta, zeta, w) per point
-};
 
 static DgDeviceTables g_dg_tables[64];
 static bool g_dg_tables_ready[64] = {false};
@@ -98,15 +92,6 @@ __host__ __device__ constexpr int dg_vol_threads(int p, int v) {
 }
 __host__ __device__ constexpr int dg_vol_qchunk(int p, int v) { return v == 2 ? 16 : 8; }
 
-template <int P, int THR, int QC>
-struct DgDims {
-  static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
-  static constexpr int NQ = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 48 : 80;
-  static constexpr int THREADS = THR;
-  static constexpr int QCHUNK = QC;
-  static constexpr int NSYM = NS * (NS + 1) / 2;
-  static constexpr int PER_THREAD = (NSYM + THREADS - 1) / THREADS;
-};
 
 // Elements of degree P: ent_el[i] (0-based), matrix block at val + boff[e],
 // rhs rows at rhs + roff[e].  A (tensor, 9 per element) or k (isotropic).
@@ -117,10 +102,9 @@ __global__ void __launch_bounds__(THR) dg_prism_elements_kernel(
     const double *__restrict__ PHItab, const double *__restrict__ QPtab, const long long *__restrict__ boff,
     const int *__restrict__ roff, double *__restrict__ val, double *__restrict__ rhs) {
   using Dm = DgDims<P, THR, QC>;
-  constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS, DG_QCHUNK = Dm::QCHUNK;
-  __shared__ double sG[NQ][6];        // w/|det| C^T A C (symmetric, packed 00 01 02 11 12 22)
-  __shared__ double sV[NQ];           // w |det|
-  __shared__ double sT[DG_QCHUNK][3][NS];
+  __shared__ double sG[Dm::NQ][6];  // w/|det| C^T A C (symmetric, packed 00 01 02 11 12 22)
+  __shared__ double sV[Dm::NQ];     // w |det|
+  __shared__ double sT[QC][3][Dm::NS];
   __shared__ double sX[18];
   __shared__ double sA[9];
   const int bi = blockIdx.x;
@@ -139,109 +123,7 @@ __global__ void __launch_bounds__(THR) dg_prism_elements_kernel(
     else
       sA[tid] = (tid == 0 || tid == 4 || tid == 8) ? (k_el ? k_el[e] : 1.0) : 0.0;
   }
-  __syncthreads();
-  // geometric factors at the points
-  for (int q = tid; q < NQ; q += DG_THREADS) {
-    const double xi = QPtab[4 * q], eta = QPtab[4 * q + 1], zeta = QPtab[4 * q + 2], w = QPtab[4 * q + 3];
-    const double lo = (1.0 - zeta) / 2.0, hi = (1.0 + zeta) / 2.0, l0 = 1.0 - xi - eta;
-    // d x / d(xi, eta, zeta) of the linear prism (apr_elem_calc_3D geometry)
-    const double dx[6] = {-lo, lo, 0.0, -hi, hi, 0.0};
-    const double dy[6] = {-lo, 0.0, lo, -hi, 0.0, hi};
-    const double dz[6] = {-0.5 * l0, -0.5 * xi, -0.5 * eta, 0.5 * l0, 0.5 * xi, 0.5 * eta};
-    v3 j1 = {0, 0, 0}, j2 = {0, 0, 0}, j3 = {0, 0, 0};
-#pragma unroll
-    for (int i = 0; i < 6; i++) {
-      const v3 x = {sX[3 * i], sX[3 * i + 1], sX[3 * i + 2]};
-      j1 = v3_fma(dx[i], x, j1);
-      j2 = v3_fma(dy[i], x, j2);
-      j3 = v3_fma(dz[i], x, j3);
-    }
-    const v3 c1 = v3_cross(j2, j3), c2 = v3_cross(j3, j1), c3 = v3_cross(j1, j2);
-    const double adet = fabs(v3_dot(j1, c1));
-    const double s = w / adet;
-    // A c_b for b = 1..3, then G_ab = s c_a . (A c_b)
-    const v3 cb[3] = {c1, c2, c3};
-    v3 Ac[3];
-#pragma unroll
-    for (int b = 0; b < 3; b++)
-      Ac[b] = {fma(sA[0], cb[b].x, fma(sA[1], cb[b].y, sA[2] * cb[b].z)),
-               fma(sA[3], cb[b].x, fma(sA[4], cb[b].y, sA[5] * cb[b].z)),
-               fma(sA[6], cb[b].x, fma(sA[7], cb[b].y, sA[8] * cb[b].z))};
-    // G_ab = s (A c_b) . c_a: the tensor a_ij multiplies d_i(test) d_j(trial),
-    // so with test index a and trial index b: G_ab = s c_a^T A c_b
-    sG[q][0] = s * v3_dot(cb[0], Ac[0]);
-    sG[q][1] = s * v3_dot(cb[0], Ac[1]);
-    sG[q][2] = s * v3_dot(cb[0], Ac[2]);
-    sG[q][3] = s * v3_dot(cb[1], Ac[1]);
-    sG[q][4] = s * v3_dot(cb[1], Ac[2]);
-    sG[q][5] = s * v3_dot(cb[2], Ac[2]);
-    sV[q] = w * adet;
-  }
-  __syncthreads();
-  // load vector
-  for (int u = tid; u < NS; u += DG_THREADS) {
-    double r = 0.0;
-    for (int q = 0; q < NQ; q++) r = fma(PHItab[(size_t)q * NS + u], sV[q], r);
-    rhs[roff[e] + u] = f * r;
-  }
-  // stiffness: upper entries k = tid + j * DG_THREADS
-  double acc[Dm::PER_THREAD];
-  int uu[Dm::PER_THREAD], ww[Dm::PER_THREAD];
-#pragma unroll
-  for (int j = 0; j < Dm::PER_THREAD; j++) {
-    acc[j] = 0.0;
-    int k = tid + j * DG_THREADS;
-    int u = 0;
-    if (k < Dm::NSYM) {
-      // row u holds entries (u, u..NS-1): find u with k in [off(u), off(u+1))
-      while (k >= NS - u) {
-        k -= NS - u;
-        u++;
-      }
-      uu[j] = u;
-      ww[j] = u + k;
-    } else {
-      uu[j] = 0;
-      ww[j] = -1;
-    }
-  }
-  for (int q0 = 0; q0 < NQ; q0 += DG_QCHUNK) {
-    const int qn = NQ - q0 < DG_QCHUNK ? NQ - q0 : DG_QCHUNK;
-    __syncthreads();
-    // T_q[a][w] = sum_b G_q[a][b] D_q[b][w]
-    for (int t = tid; t < qn * NS; t += DG_THREADS) {
-      const int ql = t / NS, w = t % NS, q = q0 + ql;
-      const double *Dq = Dtab + (size_t)q * 3 * NS;
-      const double d0 = Dq[w], d1 = Dq[NS + w], d2 = Dq[2 * NS + w];
-      const double *g = sG[q];
-      sT[ql][0][w] = fma(g[0], d0, fma(g[1], d1, g[2] * d2));
-      sT[ql][1][w] = fma(g[1], d0, fma(g[3], d1, g[4] * d2));
-      sT[ql][2][w] = fma(g[2], d0, fma(g[4], d1, g[5] * d2));
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < Dm::PER_THREAD; j++) {
-      if (ww[j] < 0) continue;
-      const int u = uu[j], w = ww[j];
-      double a = acc[j];
-      for (int ql = 0; ql < qn; ql++) {
-        const double *Dq = Dtab + (size_t)(q0 + ql) * 3 * NS;
-        a = fma(__ldg(Dq + u), sT[ql][0][w], a);
-        a = fma(__ldg(Dq + NS + u), sT[ql][1][w], a);
-        a = fma(__ldg(Dq + 2 * NS + u), sT[ql][2][w], a);
-      }
-      acc[j] = a;
-    }
-  }
-  // K_uw (test w, trial u) is column-major in the block: val[w + NS u]
-  double *blk = val + boff[e];
-#pragma unroll
-  for (int j = 0; j < Dm::PER_THREAD; j++) {
-    if (ww[j] < 0) continue;
-    const int u = uu[j], w = ww[j];
-    blk[w + (size_t)NS * u] = acc[j];
-    if (u != w) blk[u + (size_t)NS * w] = acc[j];
-  }
+  dg_prism_volume_body<P, THR, QC>(sX, sA, f, Dtab, PHItab, QPtab, val + boff[e], rhs + roff[e], sG, sV, sT);
 }
 
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,

@@ -56,6 +56,15 @@ struct DevBuf {
   size_t bytes() const { return n * sizeof(T); }
 };
 
+// Per-degree DG prism tables on a device (dg_kernels.cu): D[q][a][u]
+// reference derivatives, PHI[q][u] values, QP (xi, eta, zeta, w) per point.
+struct DgDeviceTables {
+  const double *D[5];
+  const double *PHI[5];
+  const double *QP[5];
+};
+int dg_tables_for_device(int device, DgDeviceTables **out);
+
 // Host-side structure built from the mesh (DOF order, CRS, tables, colours).
 struct HostStructure {
   int ndof = 0;

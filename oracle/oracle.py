@@ -260,3 +260,48 @@ def gmres_jacobi(row_ptr, col_ind, val, b, krylov=30, max_iter=1000, tol_rel=1e-
                                 ctypes.cast(ctypes.pointer(res), ctypes.c_void_p),
                                 ctypes.cast(ctypes.pointer(rel), ctypes.c_void_p))
     return x, it, res.value, rel.value
+
+
+def tet_basis_exponents(p):
+    """Complete monomial basis xi^a eta^b zeta^c, a+b+c <= p, ordered by total
+    degree d, then a descending, then b descending (the library's DG
+    tetrahedron order; no reference counterpart)."""
+    return [(a, b, d - a - b) for d in range(p + 1) for a in range(d, -1, -1) for b in range(d - a, -1, -1)]
+
+
+def _collapsed_tet_rule(n):
+    """n^3-point rule on the reference tetrahedron by the collapsed (Duffy)
+    map xi = u, eta = v (1-u), zeta = w (1-u)(1-v) of Gauss-Legendre points
+    on [0,1]^3; exact for polynomials of degree <= 2n - 3."""
+    g, w = np.polynomial.legendre.leggauss(n)
+    g, w = 0.5 * (g + 1.0), 0.5 * w
+    U, V, W = np.meshgrid(g, g, g, indexing="ij")
+    WU, WV, WW = np.meshgrid(w, w, w, indexing="ij")
+    xi = U
+    eta = V * (1.0 - U)
+    zeta = W * (1.0 - U) * (1.0 - V)
+    wt = WU * WV * WW * (1.0 - U) ** 2 * (1.0 - V)
+    return np.stack([xi.ravel(), eta.ravel(), zeta.ravel()], 1), wt.ravel()
+
+
+def dg_tet_element(X, A, p, f=1.0):
+    """DG affine tetrahedron of degree p by quadrature (independent of the
+    library's exact moment tables): K[w][u] = int a_ij d_i phi_w d_j phi_u,
+    R[w] = int f phi_w.  Returns (K (row w, column u), R)."""
+    X = np.asarray(X, np.float64).reshape(4, 3)
+    A = np.asarray(A, np.float64).reshape(3, 3)
+    J = np.stack([X[1] - X[0], X[2] - X[0], X[3] - X[0]], 1)  # dx/dxi columns
+    det = abs(np.linalg.det(J))
+    Jit = np.linalg.inv(J).T
+    E = np.array(tet_basis_exponents(p), float)
+    pts, wts = _collapsed_tet_rule(p + 3)
+    phi = np.prod(pts[:, None, :] ** E[None, :, :], axis=2)  # (q, ns)
+    dphi = np.zeros((len(pts), len(E), 3))
+    for a in range(3):
+        Ea = E.copy()
+        Ea[:, a] = np.maximum(Ea[:, a] - 1, 0)
+        dphi[:, :, a] = E[:, a] * np.prod(pts[:, None, :] ** Ea[None, :, :], axis=2)
+    grad = dphi @ Jit.T  # physical gradients (q, ns, 3)
+    K = np.einsum("q,qwi,ij,quj->wu", wts * det, grad, A, grad)
+    R = f * det * (wts @ phi)
+    return K, R
