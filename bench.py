@@ -294,6 +294,104 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
     return out
 
 
+def tet_fma_per_element(p):
+    """FP64 FMAs of the tetrahedron tile per element: 6 per upper entry."""
+    ns = (p + 1) * (p + 2) * (p + 3) // 6
+    return 6 * ns * (ns + 1) // 2
+
+
+def bench_batch(gb, local, steps, fp64_peak):
+    """Batched mixed elements: 400,000 DG prisms (the first 400k of the
+    59^3 x 2 jittered mesh) and 300,000 affine DG tetrahedra (the first 300k
+    of the 37^3 x 6 jittered Kuhn mesh), p uniform in 1..4 per element
+    (seeded), lognormal(0,1) k.  A step is one replay of the persistent
+    mixed-(type, p) volume kernel with autotuned variants per class, writing
+    every element block into one variable-block array.  Beside it: the prisms
+    through the per-degree kernels (four launches, autotuned shapes) and an
+    end-to-end step from host arrays (upload, run, download)."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh, structured_tet_mesh
+    NP, NT = 400_000, 300_000
+    m = structured_prism_mesh(59, jitter=0.2, seed=SEED)
+    t = structured_tet_mesh(37, jitter=0.2, seed=SEED)
+    rng = np.random.default_rng(SEED)
+    pp = rng.integers(1, 5, NP).astype(np.int32)
+    tp = rng.integers(1, 5, NT).astype(np.int32)
+    k = lognormal_k(NP + NT, seed=SEED)
+    A = k[:, None] * np.eye(3).reshape(1, 9)
+    pX = np.ascontiguousarray(m.coords[m.el_nodes[:NP]])
+    tX = np.ascontiguousarray(t.coords[t.el_nodes[:NT]])
+    b = gb.Batch(local)
+    nval, nrhs = b.set(pX, A[:NP], pp, tX, A[NP:], tp, f=1.0)
+    pv, tv, tune_ms = b.autotune(sample=32768)
+    for _ in range(3):
+        b.run()
+    ms = [b.run() for _ in range(steps)]
+    step_ms = float(np.mean(ms))
+    pfma = sum(dg_fma_per_element(q) * int(np.sum(pp == q)) for q in range(1, 5))
+    tfma = sum(tet_fma_per_element(q) * int(np.sum(tp == q)) for q in range(1, 5))
+    out_bytes = 8 * (nval + nrhs)
+    # the tetrahedra alone (HBM-write bound) and the prisms alone
+    bt = gb.Batch(local)
+    bt.set(np.zeros((0, 6, 3)), np.zeros((0, 9)), np.zeros(0, np.int32), tX, A[NP:], tp, f=1.0)
+    bt.set_variants(None, tv)
+    bt.run()
+    tet_ms = float(np.mean([bt.run() for _ in range(steps)]))
+    tnv, tnr = bt.nval, bt.nrhs
+    bt.close()
+    # end to end from host arrays: set (upload + tile build), run, download
+    hv, hr = gb.PinnedArray((nval,)), gb.PinnedArray((nrhs,))
+    hin = []
+    for arr in (pX, A[:NP], pp, tX, A[NP:], tp):
+        h = gb.PinnedArray(arr.shape, arr.dtype)
+        h.array[...] = arr
+        hin.append(h)
+    e2e = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        b.set(*[h.array for h in hin], f=1.0)
+        b.set_variants(pv, tv)
+        b.run()
+        b.L.gbfem_batch_get(b._h, hv.array.ctypes.data, hr.array.ctypes.data)
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = min(e2e)
+    for h in hin + [hv, hr]:
+        h.free()
+    b.close()
+    # prisms through the per-degree kernels (volume only, no faces)
+    class _M:
+        pass
+    pm = _M()
+    pm.coords, pm.el_nodes = m.coords, np.ascontiguousarray(m.el_nodes[:NP])
+    pm.bc_face_id = pm.bc_face_el = pm.bc_face_side = pm.bc_face_bc = np.zeros(0, np.int32)
+    c = gb.Context(local)
+    c.set_mesh(pm)
+    c.set_coefficients(k=k[:NP], f=1.0, g=0.0)
+    c.dg_set_degrees(pp)
+    c.dg_build_structure()
+    c.dg_autotune(sample=65536)
+    c.dg_assemble()
+    vol = []
+    for _ in range(steps):
+        c.dg_assemble()
+        vol.append(c.dg_last_timing()[1])
+    per_degree_ms = float(np.mean(vol))
+    c.close()
+    return {
+        "workload": f"{NP} DG prisms + {NT} affine DG tetrahedra, p uniform 1..4, lognormal k, one persistent launch",
+        "elements": NP + NT, "stored_values": nval, "rhs": nrhs,
+        "autotuned_variants": {"prism": pv[1:].tolist(), "tet_elements_per_tile": [8 << int(v) for v in tv[1:]]},
+        "step_ms": step_ms, "elem_per_s": (NP + NT) / (step_ms * 1e-3),
+        "fp64_frac": 2 * (pfma + tfma) / (step_ms * 1e-3) / 1e12 / fp64_peak,
+        "output_gbs": out_bytes / (step_ms * 1e-3) / 1e9,
+        "tets_alone_ms": tet_ms, "tets_alone_output_gbs": 8 * (tnv + tnr) / (tet_ms * 1e-3) / 1e9,
+        "prisms_per_degree_kernels_ms": per_degree_ms,
+        "e2e_ms": e2e_s * 1e3, "e2e_elem_per_s": (NP + NT) / e2e_s,
+        "e2e_note": "page-locked host arrays: upload of geometry and tensors, tile build, graph capture, run, "
+                    "download of "
+                    f"{out_bytes / 1e9:.2f} GB of blocks",
+    }
+
+
 def bench_serving(gb, local, rates=(50, 200, 1000, 2000), per_rate=48):
     """The serving workload: a Poisson stream of independent heat problems,
     each a structured prism mesh of n^3 hexahedra x 2 with n log-uniform in
@@ -497,6 +595,7 @@ def main():
 
     # ---------------- DG prism system ----------------
     dg = bench_dg(gb, local, max(3, min(args.steps, 10)), fp64_peak)
+    batch = bench_batch(gb, local, max(3, min(args.steps, 10)), fp64_peak)
 
     # ---------------- serving ----------------
     serving = bench_serving(gb, local) if rank == 0 else None
@@ -537,6 +636,7 @@ def main():
         "solver": solver,
         "structure": structure,
         "dg": dg,
+        "batch_mixed": batch,
         "serving": serving,
         "gpu_launches": launches,
         "wall_s_timed_region": wall,

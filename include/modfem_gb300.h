@@ -333,11 +333,28 @@ typedef struct gbfem_batch_s *gbfem_batch;
 int gbfem_batch_create(gbfem_batch *batch, int device);
 int gbfem_batch_destroy(gbfem_batch batch);
 /* prism_xyz[18 np] (mmr_el_node_coor order), prism_A[9 np] row-major
- * tensors, prism_p[np]; tet_xyz[12 nt], tet_A[9 nt], tet_p[nt]; tet_tile:
- * tetrahedra per work tile (1..256).  nval, nrhs: output sizes. */
+ * symmetric tensors, prism_p[np]; tet_xyz[12 nt], tet_A[9 nt], tet_p[nt].
+ * nval, nrhs: output sizes of the default layout. */
 int gbfem_batch_set(gbfem_batch batch, int np, const double *prism_xyz, const double *prism_A, const int *prism_p,
-                    int nt, const double *tet_xyz, const double *tet_A, const int *tet_p, double f, int tet_tile,
-                    long long *nval, long long *nrhs);
+                    int nt, const double *tet_xyz, const double *tet_A, const int *tet_p, double f, long long *nval,
+                    long long *nrhs);
+/* Scatter target: element e (prisms first, then tetrahedra) writes its block
+ * at val_off[e] of a value array of nval entries and its load vector at
+ * rhs_off[e] of an rhs of nrhs, e.g. the diagonal blocks of a block-CRS
+ * matrix (gbfem_dg_get_structure's layout); entries no element writes stay
+ * zero. */
+int gbfem_batch_set_layout(gbfem_batch batch, const long long *val_off, const int *rhs_off, long long nval,
+                           long long nrhs);
+/* Launch variant per degree (index 1..4): prisms 0..2 (threads per element,
+ * quadrature points per shared-memory chunk), tetrahedra 0..4 (8 << v
+ * elements per tile).  Either pointer may be NULL.  Every variant gives the
+ * same bits. */
+int gbfem_batch_set_variants(gbfem_batch batch, const int *prism_v, const int *tet_v);
+/* Times every variant of every (type, degree) class present on up to
+ * `sample` of its elements (<= 0: 16384), keeps the fastest.  prism_v[5],
+ * tet_v[5] receive the choices, ms[50] the timings ((type*5 + p)*5 + v,
+ * -1 where not timed); any may be NULL.  Overwrites the output: run after. */
+int gbfem_batch_autotune(gbfem_batch batch, int sample, int *prism_v, int *tet_v, double *ms);
 /* Replays the graph; ms: device time of the launch.  Returns the tiles. */
 int gbfem_batch_run(gbfem_batch batch, double *ms);
 int gbfem_batch_get(gbfem_batch batch, double *vals, double *rhs);

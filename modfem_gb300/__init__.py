@@ -71,7 +71,10 @@ SIGNATURES = [
     ("gbfem_write_field_dg", _ci, [ctypes.c_char_p, _ci, _vp, _vp, _vp, _ci]),
     ("gbfem_batch_create", _ci, [_pvp, _ci]),
     ("gbfem_batch_destroy", _ci, [_vp]),
-    ("gbfem_batch_set", _ci, [_vp, _ci, _vp, _vp, _vp, _ci, _vp, _vp, _vp, _cd, _ci, _pll, _pll]),
+    ("gbfem_batch_set", _ci, [_vp, _ci, _vp, _vp, _vp, _ci, _vp, _vp, _vp, _cd, _pll, _pll]),
+    ("gbfem_batch_set_layout", _ci, [_vp, _vp, _vp, _cll, _cll]),
+    ("gbfem_batch_set_variants", _ci, [_vp, _vp, _vp]),
+    ("gbfem_batch_autotune", _ci, [_vp, _ci, _vp, _vp, _vp]),
     ("gbfem_batch_run", _ci, [_vp, _pd]),
     ("gbfem_batch_get", _ci, [_vp, _vp, _vp]),
     ("gbfem_server_create", _ci, [_pvp, _ci, _cll, _ci, _ci]),
@@ -385,17 +388,44 @@ class Batch:
             raise GbFemError(self.L.gbfem_last_error().decode())
         return rc
 
-    def set(self, prism_xyz, prism_A, prism_p, tet_xyz, tet_A, tet_p, f=1.0, tet_tile=32):
+    def set(self, prism_xyz, prism_A, prism_p, tet_xyz, tet_A, tet_p, f=1.0):
         """prism_xyz (np, 6, 3), prism_A (np, 3, 3), prism_p (np,); tets
-        likewise with (nt, 4, 3).  Returns (nval, nrhs)."""
+        likewise with (nt, 4, 3).  Returns (nval, nrhs) of the default
+        layout (prism blocks, then tetrahedron blocks)."""
         self._in = [_f64(prism_xyz), _f64(prism_A), _i32(prism_p), _f64(tet_xyz), _f64(tet_A), _i32(tet_p)]
         self.pp, self.tp = self._in[2].ravel(), self._in[5].ravel()
         nv, nr = ctypes.c_longlong(), ctypes.c_longlong()
         self._check(self.L.gbfem_batch_set(self._h, self.pp.size, _p(self._in[0]), _p(self._in[1]), _p(self._in[2]),
                                            self.tp.size, _p(self._in[3]), _p(self._in[4]), _p(self._in[5]), f,
-                                           tet_tile, ctypes.byref(nv), ctypes.byref(nr)))
+                                           ctypes.byref(nv), ctypes.byref(nr)))
         self.nval, self.nrhs = nv.value, nr.value
+        self.layout = None
         return self.nval, self.nrhs
+
+    def set_layout(self, val_off, rhs_off, nval, nrhs):
+        """Write element e's block at val_off[e] and load vector at rhs_off[e]."""
+        vo = np.ascontiguousarray(val_off, dtype=np.int64)
+        ro = _i32(rhs_off)
+        self._check(self.L.gbfem_batch_set_layout(self._h, _p(vo), _p(ro), nval, nrhs))
+        self.nval, self.nrhs, self.layout = nval, nrhs, (vo, ro)
+
+    def set_variants(self, prism=None, tet=None):
+        """Variants per degree, dicts or length-5 sequences indexed by p."""
+        def arr(v):
+            if v is None:
+                return None
+            a = np.zeros(5, np.int32)
+            for p in range(1, 5):
+                a[p] = v[p]
+            return a
+        pv, tv = arr(prism), arr(tet)
+        self._check(self.L.gbfem_batch_set_variants(self._h, _p(pv), _p(tv)))
+
+    def autotune(self, sample=0):
+        """Returns (prism variants[5], tet variants[5], ms[2, 5, 5])."""
+        pv, tv, ms = np.zeros(5, np.int32), np.zeros(5, np.int32), np.zeros(50)
+        self._check(self.L.gbfem_batch_autotune(self._h, sample, _p(pv), _p(tv), _p(ms)))
+        return pv, tv, ms.reshape(2, 5, 5)
 
     def run(self):
         """Runs the batch; returns the device time in ms."""
@@ -413,7 +443,10 @@ class Batch:
         """Lists of (ns, ns) element matrices and (ns,) load vectors."""
         vals, rhs = self.get()
         mats, loads, v, r = [], [], 0, 0
-        for ns in [PRISM_NS[int(p)] for p in self.pp] + [TET_NS[int(p)] for p in self.tp]:
+        nss = [PRISM_NS[int(p)] for p in self.pp] + [TET_NS[int(p)] for p in self.tp]
+        for e, ns in enumerate(nss):
+            if self.layout is not None:
+                v, r = int(self.layout[0][e]), int(self.layout[1][e])
             mats.append(vals[v:v + ns * ns].reshape(ns, ns).T)
             loads.append(rhs[r:r + ns])
             v += ns * ns

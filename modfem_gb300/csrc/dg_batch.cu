@@ -15,12 +15,7 @@
 // with the reference matrices integrated exactly on the host from the
 // monomial moments int_ref xi^a eta^b zeta^c = a! b! c! / (a+b+c+3)!.
 //
-// Work: tiles of (type, degree, first element, count) sorted heaviest first;
-// persistent CTAs (one per SM, 256 threads) take tiles from an atomic
-// counter.  A prism tile is one element (the CTA integrates it as the
-// per-degree kernel does, bit-identical); a tetrahedron tile is `tet_tile`
-// elements, threads over (element, upper entry).
-
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -32,15 +27,43 @@
 namespace gbfem {
 
 constexpr int DGB_THREADS = 256;
-constexpr int DGB_QC = 8;
-
 __host__ __device__ constexpr int tet_ns(int p) { return (p + 1) * (p + 2) * (p + 3) / 6; }
 
+// Work: tiles of one (type, degree, launch variant) class, listed heaviest
+// class first; persistent CTAs (256 threads, as many as fit on the SMs) take
+// tiles from an atomic counter.  A prism tile holds 256 / THR elements, each
+// integrated by a group of THR threads exactly as the per-degree kernel does
+// (bit-identical for every variant); a tetrahedron tile holds `tile`
+// elements, threads over (element, block entry).  The variant of each class
+// (prism: threads per element, points per shared-memory chunk; tetrahedron:
+// elements per tile) is chosen by gbfem_batch_autotune.
+
+constexpr int DGB_VARIANTS = 3;    // prism variants per degree
+constexpr int DGB_TET_VARIANTS = 5;
+__host__ __device__ constexpr int dgb_prism_thr(int p, int v) {
+  return p == 1 ? (v == 0 ? 32 : v == 1 ? 64 : 128)
+       : p == 2 ? (v == 0 ? 64 : v == 1 ? 128 : 256)
+       : p == 3 ? (v == 2 ? 128 : 256)
+                : 256;
+}
+__host__ __device__ constexpr int dgb_prism_qc(int p, int v) {
+  return p == 3 ? (v == 1 ? 16 : 8) : p == 4 ? (v == 0 ? 8 : v == 1 ? 16 : 4) : 8;
+}
+__host__ __device__ constexpr int dgb_tet_tile(int v) { return 8 << v; }  // 8 .. 128
+// shared doubles of one prism group
+__host__ __device__ constexpr int dgb_prism_group_smem(int p, int v) {
+  return 32 + 7 * (p == 1 ? 6 : p == 2 ? 18 : p == 3 ? 48 : 80) +
+         dgb_prism_qc(p, v) * 3 * (p == 1 ? 6 : p == 2 ? 18 : p == 3 ? 40 : 75);
+}
+
 struct DgBatchTile {
-  int type;   // 0 prism, 1 tetrahedron
-  int p;
-  int first;  // first element of the tile within its type's arrays
+  unsigned char type;  // 0 prism, 1 tetrahedron
+  unsigned char p;
+  unsigned char variant;
+  unsigned char pad;
+  int start;  // elements order[start .. start + count)
   int count;
+  int pad2;
 };
 
 struct DgBatchTables {
@@ -49,34 +72,45 @@ struct DgBatchTables {
   const double *MOM[GB_DG_PMAX + 1];  // tets: int_ref phi_i
 };
 
-template <int P>
-__device__ void dgb_prism(const DgBatchTables &tb, int e, const double *__restrict__ X, const double *__restrict__ A,
-                          double f, const long long *__restrict__ off, const int *__restrict__ roff,
-                          double *__restrict__ val, double *__restrict__ rhs, double *smem) {
-  using Dm = DgDims<P, DGB_THREADS, DGB_QC>;
-  double *sX = smem, *sA = smem + 18;
-  double(*sG)[6] = (double(*)[6])(smem + 32);
-  double *sV = smem + 32 + 6 * Dm::NQ;
-  double(*sT)[3][Dm::NS] = (double(*)[3][Dm::NS])(smem + 32 + 7 * Dm::NQ);
-  const int tid = threadIdx.x;
-  __syncthreads();  // the previous tile is done with the scratch
-  if (tid < 18) sX[tid] = X[18 * (size_t)e + tid];
-  if (tid < 9) sA[tid] = A[9 * (size_t)e + tid];
-  dg_prism_volume_body<P, DGB_THREADS, DGB_QC>(sX, sA, f, tb.D[P], tb.PHI[P], tb.QP[P], val + off[e], rhs + roff[e],
-                                                sG, sV, sT);
+struct DgBatchArgs {
+  const DgBatchTile *tiles;
+  const int *order;
+  const double *pX, *pA, *tX, *tA;  // gathered vertices (18 / 12) and tensors (9) per element
+  const long long *poff, *toff;     // value offset of each element's block
+  const int *proff, *troff;         // rhs offset
+  double *val, *rhs;
+  double f;
+};
+
+template <int P, int THR, int QC>
+__device__ void dgb_prism(const DgBatchTables &tb, const DgBatchArgs &a, const DgBatchTile &T, double *smem) {
+  using Dm = DgDims<P, THR, QC>;
+  constexpr int GROUP = 32 + 7 * Dm::NQ + QC * 3 * Dm::NS;
+  const int g = threadIdx.x / THR, lt = threadIdx.x % THR;
+  const bool valid = g < T.count;
+  const int e = a.order[T.start + (valid ? g : T.count - 1)];
+  double *base = smem + g * GROUP;
+  double *sX = base, *sA = base + 18;
+  double(*sG)[6] = (double(*)[6])(base + 32);
+  double *sV = base + 32 + 6 * Dm::NQ;
+  double(*sT)[3][Dm::NS] = (double(*)[3][Dm::NS])(base + 32 + 7 * Dm::NQ);
+  if (lt < 18) sX[lt] = a.pX[18 * (size_t)e + lt];
+  if (lt < 9) sA[lt] = a.pA[9 * (size_t)e + lt];
+  dg_prism_volume_body<P, THR, QC>(sX, sA, a.f, tb.D[P], tb.PHI[P], tb.QP[P], a.val + a.poff[e], a.rhs + a.proff[e],
+                                   sG, sV, sT, lt, valid);
 }
 
 template <int P>
-__device__ void dgb_tets(const DgBatchTables &tb, int first, int count, const double *__restrict__ X,
-                         const double *__restrict__ A, double f, const long long *__restrict__ off,
-                         const int *__restrict__ roff, double *__restrict__ val, double *__restrict__ rhs,
-                         double *smem) {
+__device__ void dgb_tets(const DgBatchTables &tb, const DgBatchArgs &a, const DgBatchTile &T, double *smem) {
   constexpr int NS = tet_ns(P), NSYM = NS * (NS + 1) / 2;
+  static_assert(NSYM > 0, "degree");
   double *sGc = smem;  // [count][7]: 6 G entries, |det|
-  const int tid = threadIdx.x;
-  __syncthreads();
+  int *sE = (int *)(smem + 7 * 128);
+  const int tid = threadIdx.x, count = T.count;
   for (int el = tid; el < count; el += DGB_THREADS) {
-    const double *x = X + 12 * (size_t)(first + el), *a = A + 9 * (size_t)(first + el);
+    const int e = a.order[T.start + el];
+    sE[el] = e;
+    const double *x = a.tX + 12 * (size_t)e, *A = a.tA + 9 * (size_t)e;
     const v3 x0 = {x[0], x[1], x[2]};
     const v3 j1 = v3_sub(v3{x[3], x[4], x[5]}, x0), j2 = v3_sub(v3{x[6], x[7], x[8]}, x0),
              j3 = v3_sub(v3{x[9], x[10], x[11]}, x0);
@@ -85,9 +119,9 @@ __device__ void dgb_tets(const DgBatchTables &tb, int first, int count, const do
     v3 Ac[3];
 #pragma unroll
     for (int b = 0; b < 3; b++)
-      Ac[b] = {fma(a[0], cb[b].x, fma(a[1], cb[b].y, a[2] * cb[b].z)),
-               fma(a[3], cb[b].x, fma(a[4], cb[b].y, a[5] * cb[b].z)),
-               fma(a[6], cb[b].x, fma(a[7], cb[b].y, a[8] * cb[b].z))};
+      Ac[b] = {fma(A[0], cb[b].x, fma(A[1], cb[b].y, A[2] * cb[b].z)),
+               fma(A[3], cb[b].x, fma(A[4], cb[b].y, A[5] * cb[b].z)),
+               fma(A[6], cb[b].x, fma(A[7], cb[b].y, A[8] * cb[b].z))};
     const double s = 1.0 / adet;
     double *g = sGc + 7 * el;
     g[0] = s * v3_dot(cb[0], Ac[0]);
@@ -99,57 +133,60 @@ __device__ void dgb_tets(const DgBatchTables &tb, int first, int count, const do
     g[6] = adet;
   }
   __syncthreads();
-  const double *T = tb.T[P];
-  for (int t = tid; t < count * NSYM; t += DGB_THREADS) {
-    const int el = t / NSYM, k0 = t % NSYM;
-    int k = k0, u = 0;
-    while (k >= NS - u) {
-      k -= NS - u;
-      u++;
-    }
-    const int w = u + k;
+  // every entry of the tile's blocks once, column-major within a block, so
+  // consecutive threads write consecutive addresses (6 FMAs per entry from
+  // the packed upper triangle of the reference matrices)
+  const double *Tt = tb.T[P];
+  for (int t = tid; t < count * NS * NS; t += DGB_THREADS) {
+    const int el = t / (NS * NS), r = t % (NS * NS), u = r / NS, w = r % NS;
+    const int lo = u < w ? u : w, hi = u < w ? w : u;
+    const int k0 = lo * NS - lo * (lo - 1) / 2 + (hi - lo);
     const double *g = sGc + 7 * el;
     double v = 0.0;
 #pragma unroll
-    for (int c = 0; c < 6; c++) v = fma(g[c], __ldg(T + c * NSYM + k0), v);
-    double *blk = val + off[first + el];
-    blk[w + NS * u] = v;
-    if (u != w) blk[u + NS * w] = v;
+    for (int c = 0; c < 6; c++) v = fma(g[c], __ldg(Tt + c * NSYM + k0), v);
+    a.val[a.toff[sE[el]] + r] = v;
   }
   for (int t = tid; t < count * NS; t += DGB_THREADS) {
     const int el = t / NS, i = t % NS;
-    rhs[roff[first + el] + i] = f * sGc[7 * el + 6] * __ldg(tb.MOM[P] + i);
+    a.rhs[a.troff[sE[el]] + i] = a.f * sGc[7 * el + 6] * __ldg(tb.MOM[P] + i);
   }
 }
 
-__global__ void __launch_bounds__(DGB_THREADS) dg_batch_kernel(
-    int ntiles, const DgBatchTile *__restrict__ tiles, int *counter, DgBatchTables tb, double f,
-    const double *__restrict__ pX, const double *__restrict__ pA, const long long *__restrict__ poff,
-    const int *__restrict__ proff, const double *__restrict__ tX, const double *__restrict__ tA,
-    const long long *__restrict__ toff, const int *__restrict__ troff, double *__restrict__ val,
-    double *__restrict__ rhs) {
+template <int P>
+__device__ __forceinline__ void dgb_prism_variant(const DgBatchTables &tb, const DgBatchArgs &a,
+                                                  const DgBatchTile &T, double *smem) {
+  switch (T.variant) {
+    case 0: dgb_prism<P, dgb_prism_thr(P, 0), dgb_prism_qc(P, 0)>(tb, a, T, smem); break;
+    case 1: dgb_prism<P, dgb_prism_thr(P, 1), dgb_prism_qc(P, 1)>(tb, a, T, smem); break;
+    default: dgb_prism<P, dgb_prism_thr(P, 2), dgb_prism_qc(P, 2)>(tb, a, T, smem); break;
+  }
+}
+
+__global__ void __launch_bounds__(DGB_THREADS) dg_batch_kernel(int ntiles, int *counter, DgBatchTables tb,
+                                                               DgBatchArgs a) {
   extern __shared__ double smem[];
   __shared__ int s_tile;
   for (;;) {
-    __syncthreads();
+    __syncthreads();  // the previous tile is done with s_tile and the scratch
     if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1);
     __syncthreads();
     const int t = s_tile;
     if (t >= ntiles) return;
-    const DgBatchTile T = tiles[t];
+    const DgBatchTile T = a.tiles[t];
     if (T.type == 0) {
       switch (T.p) {
-        case 1: dgb_prism<1>(tb, T.first, pX, pA, f, poff, proff, val, rhs, smem); break;
-        case 2: dgb_prism<2>(tb, T.first, pX, pA, f, poff, proff, val, rhs, smem); break;
-        case 3: dgb_prism<3>(tb, T.first, pX, pA, f, poff, proff, val, rhs, smem); break;
-        default: dgb_prism<4>(tb, T.first, pX, pA, f, poff, proff, val, rhs, smem); break;
+        case 1: dgb_prism_variant<1>(tb, a, T, smem); break;
+        case 2: dgb_prism_variant<2>(tb, a, T, smem); break;
+        case 3: dgb_prism_variant<3>(tb, a, T, smem); break;
+        default: dgb_prism_variant<4>(tb, a, T, smem); break;
       }
     } else {
       switch (T.p) {
-        case 1: dgb_tets<1>(tb, T.first, T.count, tX, tA, f, toff, troff, val, rhs, smem); break;
-        case 2: dgb_tets<2>(tb, T.first, T.count, tX, tA, f, toff, troff, val, rhs, smem); break;
-        case 3: dgb_tets<3>(tb, T.first, T.count, tX, tA, f, toff, troff, val, rhs, smem); break;
-        default: dgb_tets<4>(tb, T.first, T.count, tX, tA, f, toff, troff, val, rhs, smem); break;
+        case 1: dgb_tets<1>(tb, a, T, smem); break;
+        case 2: dgb_tets<2>(tb, a, T, smem); break;
+        case 3: dgb_tets<3>(tb, a, T, smem); break;
+        default: dgb_tets<4>(tb, a, T, smem); break;
       }
     }
   }
@@ -157,9 +194,9 @@ __global__ void __launch_bounds__(DGB_THREADS) dg_batch_kernel(
 
 // ------------------------------------------------------------------ host
 // exact reference-tetrahedron matrices for degree p
-static void tet_tables(int p, std::vector<double> &T, std::vector<double> &MOM, std::vector<int> &EXP) {
+static void tet_tables(int p, std::vector<double> &T, std::vector<double> &MOM) {
   const int ns = tet_ns(p), nsym = ns * (ns + 1) / 2;
-  EXP.clear();
+  std::vector<int> EXP;
   for (int d = 0; d <= p; d++)
     for (int a = d; a >= 0; a--)
       for (int b = d - a; b >= 0; b--) {
@@ -194,7 +231,7 @@ static void tet_tables(int p, std::vector<double> &T, std::vector<double> &MOM, 
 static DgBatchTables g_bt[64];
 static bool g_bt_ready[64];
 
-int dg_batch_tables(int device, DgBatchTables *out) {
+static int dg_batch_tables(int device, DgBatchTables *out) {
   GB_CHECK(device >= 0 && device < 64, "device index out of range");
   if (!g_bt_ready[device]) {
     DgDeviceTables *pt = nullptr;
@@ -205,8 +242,7 @@ int dg_batch_tables(int device, DgBatchTables *out) {
       g_bt[device].PHI[p] = pt->PHI[p];
       g_bt[device].QP[p] = pt->QP[p];
       std::vector<double> T, MOM;
-      std::vector<int> EXP;
-      tet_tables(p, T, MOM, EXP);
+      tet_tables(p, T, MOM);
       double *dT = nullptr, *dM = nullptr;
       GB_CUDA(cudaMalloc(&dT, T.size() * sizeof(double)));
       GB_CUDA(cudaMalloc(&dM, MOM.size() * sizeof(double)));
@@ -221,6 +257,15 @@ int dg_batch_tables(int device, DgBatchTables *out) {
   return 0;
 }
 
+// dynamic shared memory covering every class and variant
+static size_t dgb_smem_bytes() {
+  int m = 7 * 128 + 128;  // tets: G and |det| per element, element ids
+  for (int p = 1; p <= 4; p++)
+    for (int v = 0; v < DGB_VARIANTS; v++)
+      m = std::max(m, (DGB_THREADS / dgb_prism_thr(p, v)) * dgb_prism_group_smem(p, v));
+  return sizeof(double) * (size_t)m;
+}
+
 }  // namespace gbfem
 
 // ------------------------------------------------------------------ C ABI
@@ -228,66 +273,109 @@ using gbfem::DevBuf;
 using gbfem::DgBatchTile;
 
 struct gbfem_batch_s {
-  int device = 0;
+  int device = 0, sms = 0, grid = 0;
+  size_t smem = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  int np = 0, nt = 0, tet_tile = 32, ntiles = 0;
+  int np = 0, nt = 0, ntiles = 0;
+  int var_prism[5] = {0, 0, 0, 0, 0}, var_tet[5] = {2, 2, 2, 2, 2};
   double f = 1.0;
   long long nval = 0, nrhs = 0;
   DevBuf<double> pX, pA, tX, tA, val, rhs;
   DevBuf<long long> poff, toff;
-  DevBuf<int> proff, troff, counter;
+  DevBuf<int> proff, troff, counter, order;
   DevBuf<DgBatchTile> tiles;
-  std::vector<int> pp, tp;
+  std::vector<int> pp, tp, order_h;
+  std::vector<int> cls_start[2][5];  // element order of each class
+  gbfem::DgBatchTables tb{};
   cudaGraphExec_t graph = nullptr;
   float last_ms = 0.f;
 };
 
-static int batch_build(gbfem_batch b) {
-  // tiles: heaviest first (prisms p4 .. p1, then tets p4 .. p1)
-  std::vector<DgBatchTile> tiles;
-  std::vector<int> order_p, order_t;
-  for (int p = 4; p >= 1; p--)
-    for (int e = 0; e < b->np; e++)
-      if (b->pp[e] == p) tiles.push_back({0, p, e, 1});
-  for (int p = 4; p >= 1; p--) {
-    int run = -1, cnt = 0;
-    for (int e = 0; e <= b->nt; e++) {
-      const bool in = e < b->nt && b->tp[e] == p;
-      // consecutive elements of one degree form tiles of up to tet_tile
-      if (in && run >= 0 && cnt < b->tet_tile && e == run + cnt) {
-        cnt++;
-        continue;
-      }
-      if (run >= 0) tiles.push_back({1, p, run, cnt});
-      run = in ? e : -1;
-      cnt = in ? 1 : 0;
+// order: elements grouped by class (prisms p = 1..4, then tets p = 1..4),
+// input order within a class; cls_start[t][p] = {begin, end}
+static void batch_order(gbfem_batch b) {
+  b->order_h.clear();
+  for (int t = 0; t < 2; t++)
+    for (int p = 1; p <= 4; p++) {
+      const std::vector<int> &deg = t == 0 ? b->pp : b->tp;
+      const int begin = (int)b->order_h.size();
+      for (int e = 0; e < (int)deg.size(); e++)
+        if (deg[e] == p) b->order_h.push_back(e);
+      b->cls_start[t][p] = {begin, (int)b->order_h.size()};
     }
-  }
-  b->ntiles = (int)tiles.size();
+}
+
+// tiles of the classes in `sel` (bit t*5+p), up to `limit` elements per class
+static void batch_tiles(gbfem_batch b, unsigned sel, int limit, std::vector<DgBatchTile> &tiles) {
+  tiles.clear();
+  for (int p = 4; p >= 1; p--)  // heaviest classes first
+    for (int t = 0; t < 2; t++) {
+      if (!(sel & (1u << (t * 5 + p)))) continue;
+      const int begin = b->cls_start[t][p][0], end = std::min(b->cls_start[t][p][1], begin + limit);
+      const int v = t == 0 ? b->var_prism[p] : b->var_tet[p];
+      const int per = t == 0 ? gbfem::DGB_THREADS / gbfem::dgb_prism_thr(p, v) : gbfem::dgb_tet_tile(v);
+      for (int s = begin; s < end; s += per) {
+        DgBatchTile T{};
+        T.type = (unsigned char)t;
+        T.p = (unsigned char)p;
+        T.variant = (unsigned char)v;
+        T.start = s;
+        T.count = std::min(per, end - s);
+        tiles.push_back(T);
+      }
+    }
+}
+
+static gbfem::DgBatchArgs batch_args(gbfem_batch b) {
+  gbfem::DgBatchArgs a;
+  a.tiles = b->tiles.p;
+  a.order = b->order.p;
+  a.pX = b->pX.p;
+  a.pA = b->pA.p;
+  a.tX = b->tX.p;
+  a.tA = b->tA.p;
+  a.poff = b->poff.p;
+  a.toff = b->toff.p;
+  a.proff = b->proff.p;
+  a.troff = b->troff.p;
+  a.val = b->val.p;
+  a.rhs = b->rhs.p;
+  a.f = b->f;
+  return a;
+}
+
+static int batch_upload_tiles(gbfem_batch b, const std::vector<DgBatchTile> &tiles) {
   if (b->tiles.alloc(std::max<size_t>(tiles.size(), 1)) < 0) return -1;
   if (!tiles.empty())
     GB_CUDA(cudaMemcpy(b->tiles.p, tiles.data(), tiles.size() * sizeof(DgBatchTile), cudaMemcpyHostToDevice));
-  // capture memset + persistent kernel as a graph
+  return 0;
+}
+
+static int batch_launch(gbfem_batch b, int ntiles) {
+  GB_CUDA(cudaMemsetAsync(b->counter.p, 0, sizeof(int), b->stream));
+  gbfem::dg_batch_kernel<<<b->grid, gbfem::DGB_THREADS, b->smem, b->stream>>>(ntiles, b->counter.p, b->tb,
+                                                                             batch_args(b));
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// full tile list with the current variants, captured with its counter reset
+static int batch_build(gbfem_batch b) {
+  std::vector<DgBatchTile> tiles;
+  batch_tiles(b, ~0u, 1 << 30, tiles);
+  b->ntiles = (int)tiles.size();
+  if (batch_upload_tiles(b, tiles) < 0) return -1;
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
-  gbfem::DgBatchTables tb;
-  if (gbfem::dg_batch_tables(b->device, &tb) < 0) return -1;
-  int sms = 0, occ = 0;
-  GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
-  const size_t smem = sizeof(double) * std::max(32 + 7 * 80 + gbfem::DGB_QC * 3 * 75, 7 * b->tet_tile);
-  GB_CUDA(cudaFuncSetAttribute(gbfem::dg_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gbfem::dg_batch_kernel, gbfem::DGB_THREADS, smem));
-  const int grid = sms * std::max(occ, 1);
   cudaGraph_t g = nullptr;
   GB_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  cudaMemsetAsync(b->counter.p, 0, sizeof(int), b->stream);
-  gbfem::dg_batch_kernel<<<grid, gbfem::DGB_THREADS, smem, b->stream>>>(
-      b->ntiles, b->tiles.p, b->counter.p, tb, b->f, b->pX.p, b->pA.p, b->poff.p, b->proff.p, b->tX.p, b->tA.p,
-      b->toff.p, b->troff.p, b->val.p, b->rhs.p);
-  GB_CUDA(cudaStreamEndCapture(b->stream, &g));
+  const int rl = batch_launch(b, b->ntiles);
+  const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+  if (rl < 0) return rl;
+  GB_CUDA(ec);
   const cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
   cudaGraphDestroy(g);
   GB_CUDA(e);
@@ -301,12 +389,22 @@ int gbfem_batch_create(gbfem_batch *out, int device) {
   GB_CUDA(cudaSetDevice(device));
   gbfem_batch b = new gbfem_batch_s();
   b->device = device;
+  b->smem = gbfem::dgb_smem_bytes();
+  int occ = 0;
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess || b->counter.alloc(1) < 0) {
+      cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess || b->counter.alloc(1) < 0 ||
+      cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaFuncSetAttribute(gbfem::dg_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gbfem::dg_batch_kernel, gbfem::DGB_THREADS, b->smem) !=
+          cudaSuccess ||
+      gbfem::dg_batch_tables(device, &b->tb) < 0) {
+    if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     gbfem::set_error("batch creation failed");
     return -1;
   }
+  b->grid = b->sms * std::max(occ, 1);
   *out = b;
   return 0;
 }
@@ -323,6 +421,7 @@ int gbfem_batch_destroy(gbfem_batch b) {
   b->proff.release();
   b->troff.release();
   b->counter.release();
+  b->order.release();
   b->tiles.release();
   cudaEventDestroy(b->e0);
   cudaEventDestroy(b->e1);
@@ -332,27 +431,30 @@ int gbfem_batch_destroy(gbfem_batch b) {
 }
 
 int gbfem_batch_set(gbfem_batch b, int np, const double *prism_xyz, const double *prism_A, const int *prism_p,
-                    int nt, const double *tet_xyz, const double *tet_A, const int *tet_p, double f, int tet_tile,
-                    long long *nval, long long *nrhs) {
+                    int nt, const double *tet_xyz, const double *tet_A, const int *tet_p, double f, long long *nval,
+                    long long *nrhs) {
   GB_CHECK(b, "null batch");
   GB_CHECK(np >= 0 && nt >= 0 && np + nt > 0, "empty batch");
   GB_CHECK(np == 0 || (prism_xyz && prism_A && prism_p), "prism arrays missing");
   GB_CHECK(nt == 0 || (tet_xyz && tet_A && tet_p), "tetrahedron arrays missing");
-  GB_CHECK(tet_tile >= 1 && tet_tile <= 256, "tet_tile must be 1..256");
+  for (int e = 0; e < np; e++) GB_CHECK(prism_p[e] >= 1 && prism_p[e] <= 4, "degree must be 1..4");
+  for (int e = 0; e < nt; e++) GB_CHECK(tet_p[e] >= 1 && tet_p[e] <= 4, "degree must be 1..4");
   GB_CUDA(cudaSetDevice(b->device));
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
   b->np = np;
   b->nt = nt;
   b->f = f;
-  b->tet_tile = tet_tile;
   b->pp.assign(prism_p, prism_p + np);
   b->tp.assign(tet_p, tet_p + nt);
-  // output: prism blocks, then tet blocks, each ns x ns column-major
+  // default layout: prism blocks, then tet blocks, each ns x ns column-major
   std::vector<long long> poff(np), toff(nt);
   std::vector<int> proff(np), troff(nt);
   long long v = 0;
   int r = 0;
   for (int e = 0; e < np; e++) {
-    GB_CHECK(prism_p[e] >= 1 && prism_p[e] <= 4, "degree must be 1..4");
     const int ns = GB_DG_NS[prism_p[e]];
     poff[e] = v;
     proff[e] = r;
@@ -360,7 +462,6 @@ int gbfem_batch_set(gbfem_batch b, int np, const double *prism_xyz, const double
     r += ns;
   }
   for (int e = 0; e < nt; e++) {
-    GB_CHECK(tet_p[e] >= 1 && tet_p[e] <= 4, "degree must be 1..4");
     const int ns = gbfem::tet_ns(tet_p[e]);
     toff[e] = v;
     troff[e] = r;
@@ -369,6 +470,7 @@ int gbfem_batch_set(gbfem_batch b, int np, const double *prism_xyz, const double
   }
   b->nval = v;
   b->nrhs = r;
+  batch_order(b);
   auto up = [&](auto &buf, const auto *h, size_t n) -> int {
     if (buf.alloc(std::max<size_t>(n, 1)) < 0) return -1;
     if (n) GB_CUDA(cudaMemcpy(buf.p, h, n * sizeof(*h), cudaMemcpyHostToDevice));
@@ -378,12 +480,102 @@ int gbfem_batch_set(gbfem_batch b, int np, const double *prism_xyz, const double
       up(b->tX, tet_xyz, 12 * (size_t)nt) < 0 || up(b->tA, tet_A, 9 * (size_t)nt) < 0 ||
       up(b->poff, poff.data(), poff.size()) < 0 || up(b->toff, toff.data(), toff.size()) < 0 ||
       up(b->proff, proff.data(), proff.size()) < 0 || up(b->troff, troff.data(), troff.size()) < 0 ||
-      b->val.alloc((size_t)v) < 0 || b->rhs.alloc((size_t)r) < 0)
+      up(b->order, b->order_h.data(), b->order_h.size()) < 0 || b->val.alloc((size_t)v) < 0 ||
+      b->rhs.alloc((size_t)r) < 0)
     return -1;
   if (batch_build(b) < 0) return -1;
   if (nval) *nval = v;
   if (nrhs) *nrhs = r;
   return 0;
+}
+
+int gbfem_batch_set_layout(gbfem_batch b, const long long *val_off, const int *rhs_off, long long nval,
+                           long long nrhs) {
+  GB_CHECK(b && b->np + b->nt > 0, "batch not set");
+  GB_CHECK(val_off && rhs_off, "null argument");
+  const int n = b->np + b->nt;
+  for (int e = 0; e < n; e++) {
+    const int p = e < b->np ? b->pp[e] : b->tp[e - b->np];
+    const long long ns = e < b->np ? GB_DG_NS[p] : gbfem::tet_ns(p);
+    GB_CHECK(val_off[e] >= 0 && val_off[e] + ns * ns <= nval, "block offset out of range");
+    GB_CHECK(rhs_off[e] >= 0 && rhs_off[e] + ns <= nrhs, "rhs offset out of range");
+  }
+  GB_CHECK(nrhs < (1ll << 31), "rhs too long");
+  GB_CUDA(cudaSetDevice(b->device));
+  if (b->poff.alloc(std::max(b->np, 1)) < 0 || b->toff.alloc(std::max(b->nt, 1)) < 0 ||
+      b->proff.alloc(std::max(b->np, 1)) < 0 || b->troff.alloc(std::max(b->nt, 1)) < 0)
+    return -1;
+  if (b->np) {
+    GB_CUDA(cudaMemcpy(b->poff.p, val_off, b->np * sizeof(long long), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(b->proff.p, rhs_off, b->np * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (b->nt) {
+    GB_CUDA(cudaMemcpy(b->toff.p, val_off + b->np, b->nt * sizeof(long long), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(b->troff.p, rhs_off + b->np, b->nt * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (b->val.alloc((size_t)nval) < 0 || b->rhs.alloc((size_t)nrhs) < 0) return -1;
+  GB_CUDA(cudaMemset(b->val.p, 0, (size_t)nval * sizeof(double)));
+  GB_CUDA(cudaMemset(b->rhs.p, 0, (size_t)nrhs * sizeof(double)));
+  b->nval = nval;
+  b->nrhs = nrhs;
+  return batch_build(b);
+}
+
+int gbfem_batch_set_variants(gbfem_batch b, const int *prism_v, const int *tet_v) {
+  GB_CHECK(b, "null batch");
+  for (int p = 1; p <= 4; p++) {
+    GB_CHECK(!prism_v || (prism_v[p] >= 0 && prism_v[p] < gbfem::DGB_VARIANTS), "prism variant out of range");
+    GB_CHECK(!tet_v || (tet_v[p] >= 0 && tet_v[p] < gbfem::DGB_TET_VARIANTS), "tetrahedron variant out of range");
+  }
+  for (int p = 1; p <= 4; p++) {
+    if (prism_v) b->var_prism[p] = prism_v[p];
+    if (tet_v) b->var_tet[p] = tet_v[p];
+  }
+  GB_CUDA(cudaSetDevice(b->device));
+  return b->np + b->nt > 0 ? batch_build(b) : 0;
+}
+
+int gbfem_batch_autotune(gbfem_batch b, int sample, int *prism_v, int *tet_v, double *ms) {
+  GB_CHECK(b && b->np + b->nt > 0, "batch not set");
+  GB_CUDA(cudaSetDevice(b->device));
+  if (sample <= 0) sample = 16384;
+  if (ms)
+    for (int i = 0; i < 2 * 5 * 5; i++) ms[i] = -1.0;
+  std::vector<DgBatchTile> tiles;
+  for (int t = 0; t < 2; t++)
+    for (int p = 1; p <= 4; p++) {
+      if (b->cls_start[t][p][1] == b->cls_start[t][p][0]) continue;
+      int *var = t == 0 ? b->var_prism : b->var_tet;
+      const int nv = t == 0 ? gbfem::DGB_VARIANTS : gbfem::DGB_TET_VARIANTS;
+      double best = 1e30;
+      int bestv = var[p];
+      for (int v = 0; v < nv; v++) {
+        var[p] = v;
+        batch_tiles(b, 1u << (t * 5 + p), sample, tiles);
+        if (batch_upload_tiles(b, tiles) < 0) return -1;
+        float tmin = 1e30f;
+        for (int rep = 0; rep < 3; rep++) {
+          cudaEventRecord(b->e0, b->stream);
+          if (batch_launch(b, (int)tiles.size()) < 0) return -1;
+          cudaEventRecord(b->e1, b->stream);
+          GB_CUDA(cudaEventSynchronize(b->e1));
+          float x = 0.f;
+          cudaEventElapsedTime(&x, b->e0, b->e1);
+          if (rep > 0) tmin = std::min(tmin, x);
+        }
+        if (ms) ms[(t * 5 + p) * 5 + v] = tmin;
+        if (tmin < best) {
+          best = tmin;
+          bestv = v;
+        }
+      }
+      var[p] = bestv;
+    }
+  for (int p = 0; p < 5; p++) {
+    if (prism_v) prism_v[p] = b->var_prism[p];
+    if (tet_v) tet_v[p] = b->var_tet[p];
+  }
+  return batch_build(b);
 }
 
 int gbfem_batch_run(gbfem_batch b, double *ms) {
@@ -400,6 +592,7 @@ int gbfem_batch_run(gbfem_batch b, double *ms) {
 
 int gbfem_batch_get(gbfem_batch b, double *vals, double *rhs) {
   GB_CHECK(b && b->graph, "batch not set");
+  GB_CUDA(cudaSetDevice(b->device));
   if (vals) GB_CUDA(cudaMemcpy(vals, b->val.p, (size_t)b->nval * sizeof(double), cudaMemcpyDeviceToHost));
   if (rhs) GB_CUDA(cudaMemcpy(rhs, b->rhs.p, (size_t)b->nrhs * sizeof(double), cudaMemcpyDeviceToHost));
   return 0;

@@ -123,7 +123,8 @@ __global__ void __launch_bounds__(THR) dg_prism_elements_kernel(
     else
       sA[tid] = (tid == 0 || tid == 4 || tid == 8) ? (k_el ? k_el[e] : 1.0) : 0.0;
   }
-  dg_prism_volume_body<P, THR, QC>(sX, sA, f, Dtab, PHItab, QPtab, val + boff[e], rhs + roff[e], sG, sV, sT);
+  dg_prism_volume_body<P, THR, QC>(sX, sA, f, Dtab, PHItab, QPtab, val + boff[e], rhs + roff[e], sG, sV, sT, tid,
+                                   true);
 }
 
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,

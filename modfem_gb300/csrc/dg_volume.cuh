@@ -5,9 +5,12 @@
 // K_uw = sum_q vol_q sum_ij a_ij d_i phi_w d_j phi_u, R_w = sum_q vol_q f phi_w.
 // With the adjugate rows c_a of the Jacobian every point contributes
 // D_q^T G_q D_q (D_q: 3 x ns reference derivatives, G_q = (w_q/|det|) C^T A C,
-// 6 entries for symmetric A).  The calling CTA (THR threads) has written the
-// vertex coordinates to sX[18] and the tensor to sA[9] (shared memory); the
-// body synchronises before reading them.
+// 6 entries for symmetric A).  A group of THR threads (tid = 0..THR-1) of the
+// calling CTA integrates one element: it has written the vertex coordinates to
+// sX[18] and the tensor to sA[9] (shared memory); the body synchronises the
+// whole CTA before reading them, so every group of the CTA runs the same body
+// (same P, THR, QC) the same number of times; a group without an element
+// passes write = false and computes on whatever sX/sA hold.
 #pragma once
 
 #include "prism_std.cuh"
@@ -31,10 +34,10 @@ __device__ __forceinline__ void dg_prism_volume_body(const double *sX, const dou
                                                      const double *__restrict__ PHItab,
                                                      const double *__restrict__ QPtab, double *blk,
                                                      double *rhs_out, double (*sG)[6], double *sV,
-                                                     double (*sT)[3][DgDims<P, THR, QC>::NS]) {
+                                                     double (*sT)[3][DgDims<P, THR, QC>::NS], int tid,
+                                                     bool write) {
   using Dm = DgDims<P, THR, QC>;
   constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS, DG_QCHUNK = Dm::QCHUNK;
-  const int tid = threadIdx.x;
   __syncthreads();
   // geometric factors at the points
   for (int q = tid; q < NQ; q += DG_THREADS) {
@@ -78,7 +81,7 @@ __device__ __forceinline__ void dg_prism_volume_body(const double *sX, const dou
   for (int u = tid; u < NS; u += DG_THREADS) {
     double r = 0.0;
     for (int q = 0; q < NQ; q++) r = fma(PHItab[(size_t)q * NS + u], sV[q], r);
-    rhs_out[u] = f * r;
+    if (write) rhs_out[u] = f * r;
   }
   // stiffness: upper entries k = tid + j * DG_THREADS
   double acc[Dm::PER_THREAD];
@@ -130,6 +133,7 @@ __device__ __forceinline__ void dg_prism_volume_body(const double *sX, const dou
     }
   }
   // K_uw (test w, trial u) is column-major in the block: blk[w + NS u]
+  if (!write) return;
 #pragma unroll
   for (int j = 0; j < Dm::PER_THREAD; j++) {
     if (ww[j] < 0) continue;

@@ -84,20 +84,64 @@ def test_prisms_bitwise_equal_per_degree_kernel(gb):
         assert mat_rel_err(mats[m.nel + e], Ko) < REL_TOL
 
 
-def test_tile_sizes_and_replays_identical(gb):
+def test_variants_and_replays_identical(gb):
     m, D, p = _prisms(2, 11)
     t, Dt, pt = _tets(3, 12)
+    b = gb.Batch(0)
+    b.set(m.coords[m.el_nodes], D, p, t.coords[t.el_nodes], Dt, pt, f=0.5)
     ref = None
-    for tile in (1, 7, 32, 256):
-        b = gb.Batch(0)
-        b.set(m.coords[m.el_nodes], D, p, t.coords[t.el_nodes], Dt, pt, f=0.5, tet_tile=tile)
-        for _ in range(2):
-            b.run()
-            v, r = b.get()
-            if ref is None:
-                ref = (v, r)
-            assert np.array_equal(v, ref[0]) and np.array_equal(r, ref[1]), tile
-        b.close()
+    for pv in range(3):
+        for tv in range(5):
+            b.set_variants([0] + [pv] * 4, [0] + [tv] * 4)
+            for _ in range(2):
+                b.run()
+                v, r = b.get()
+                if ref is None:
+                    ref = (v, r)
+                assert np.array_equal(v, ref[0]) and np.array_equal(r, ref[1]), (pv, tv)
+    pv, tv, ms = b.autotune(sample=64)
+    assert all(0 <= pv[q] < 3 and 0 <= tv[q] < 5 for q in range(1, 5))
+    assert (ms[0, 1:, :3] > 0).all() and (ms[1, 1:, :] > 0).all()
+    b.run()
+    v, r = b.get()
+    assert np.array_equal(v, ref[0]) and np.array_equal(r, ref[1])
+
+
+def test_layout_scatters_into_block_crs(gb):
+    """Diagonal blocks of the prism mesh's block-CRS structure, then a
+    second (tetrahedron) matrix appended after it."""
+    m, D, p = _prisms(2, 13)
+    c = gb.Context(0)
+    c.set_mesh(m)
+    c.set_coefficients(D=D.reshape(-1, 9), f=1.0)
+    c.dg_set_degrees(p)
+    nd, nv = c.dg_build_structure()
+    off, bptr, bcol, boff = c.dg_get_structure()
+    c.dg_assemble()
+    vals, rhs = c.dg_get_matrix()
+    t, Dt, pt = _tets(1, 14)
+    diag = [boff[bptr[e] + int(np.nonzero(bcol[bptr[e]:bptr[e + 1]] == e)[0][0])] for e in range(m.nel)]
+    tns = np.array([gb.TET_NS[int(q)] for q in pt])
+    toff = nv + np.concatenate([[0], np.cumsum(tns * tns)[:-1]])
+    troff = nd + np.concatenate([[0], np.cumsum(tns)[:-1]])
+    b = gb.Batch(0)
+    b.set(m.coords[m.el_nodes], D, p, t.coords[t.el_nodes], Dt, pt, f=1.0)
+    NV, NR = nv + int((tns * tns).sum()), nd + int(tns.sum())
+    b.set_layout(np.concatenate([diag, toff]), np.concatenate([off[:-1], troff]), NV, NR)
+    b.run()
+    v, r = b.get()
+    isdiag = np.zeros(nv, bool)
+    for e in range(m.nel):
+        ns = off[e + 1] - off[e]
+        isdiag[diag[e]:diag[e] + ns * ns] = True
+    assert np.array_equal(v[:nv][isdiag], vals[isdiag])
+    assert not v[:nv][~isdiag].any()
+    assert np.array_equal(r[:nd], rhs)
+    mats, loads = b.blocks()
+    for e in range(t.nel):
+        Ko, Ro = O.dg_tet_element(t.coords[t.el_nodes[e]], Dt[e], int(pt[e]))
+        assert mat_rel_err(mats[m.nel + e], Ko) < REL_TOL
+        assert vec_rel_err(loads[m.nel + e], Ro) < REL_TOL
 
 
 def test_errors(gb):
