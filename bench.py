@@ -53,9 +53,10 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help=argparse.SUPPRESS)
-    p.add_argument("--profile", choices=["dg", "dg_tc"], default=None,
-                   help="small DG p=3 anisotropic case (n^3 x 2 prisms, --n) for ncu captures: "
-                        "3 assemblies (FP64 or tensor-core volume kernel) and one block residual")
+    p.add_argument("--profile", choices=["dg", "dg_tc", "batch"], default=None,
+                   help="small cases for ncu captures: DG p=3 anisotropic (n^3 x 2 prisms, --n), 3 assemblies "
+                        "(FP64 or tensor-core volume kernel) and one block residual; or the mixed batch "
+                        "(40,000 prisms + 30,000 tetrahedra, p 1..4), 3 runs")
     return p.parse_args()
 
 
@@ -64,6 +65,20 @@ def run_profile_case(args):
     block SpMV); prints its CUDA-event timings."""
     import modfem_gb300 as gb
     from modfem_gb300.mesh import anisotropic_tensors, prism_faces, structured_prism_mesh
+    if args.profile == "batch":
+        from modfem_gb300.mesh import lognormal_k, structured_tet_mesh
+        NP, NT = 40_000, 30_000
+        m, t = structured_prism_mesh(28, jitter=JITTER, seed=SEED), structured_tet_mesh(18, jitter=JITTER, seed=SEED)
+        rng = np.random.default_rng(SEED)
+        pp, tp = rng.integers(1, 5, NP), rng.integers(1, 5, NT)
+        A = lognormal_k(NP + NT, seed=SEED)[:, None] * np.eye(3).reshape(1, 9)
+        b = gb.Batch(0)
+        b.set(m.coords[m.el_nodes[:NP]], A[:NP], pp, t.coords[t.el_nodes[:NT]], A[NP:], tp)
+        b.set_variants([0, 0, 0, 2, 1], [0, 4, 4, 4, 1])
+        ms = [b.run() for _ in range(3)]
+        print(json.dumps({"profile_case": "batch", "elements": NP + NT, "timing_ms": ms}))
+        b.close()
+        return
     m = structured_prism_mesh(args.n, jitter=JITTER, seed=SEED)
     c = gb.Context(0)
     c.set_mesh(m)
@@ -261,7 +276,18 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
         tot_tc, vol_tc, _ = tt / steps
         vtc, rtc = c.dg_get_matrix()
         tc_dev = float(np.max(np.abs(vtc - v64)) / np.max(np.abs(v64)))
-        del v64, vtc
+        del vtc
+        # and with the TF32 hi/lo contraction (FP32 accumulation: approximate)
+        c.dg_set_volume_kernel(gb.DG_VOLUME_TF32)
+        c.dg_assemble()
+        tt = np.zeros(3)
+        for _ in range(steps):
+            c.dg_assemble()
+            tt += np.array(c.dg_last_timing()[:3])
+        tot_tf, vol_tf, _ = tt / steps
+        vtf, _ = c.dg_get_matrix()
+        tf_dev = float(np.max(np.abs(vtf - v64)) / np.max(np.abs(v64)))
+        del v64, vtf
         c.dg_set_volume_kernel(gb.DG_VOLUME_FP64)
         vfma = sum(dg_fma_per_element(p) * int(np.sum(pdeg == p)) for p in range(1, 5))
         ffma = dg_face_fma(F, pdeg)
@@ -282,6 +308,9 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
             "tensor_core_volume": {"volume_ms": vol_tc, "assemble_ms": tot_tc, "elem_per_s": m.nel / (tot_tc * 1e-3),
                                    "max_abs_diff_vs_fp64_rel_to_max": tc_dev,
                                    "note": "tcgen05 split-BF16 products (p <= 3; p = 4 stays FP64)"},
+            "tf32_volume": {"volume_ms": vol_tf, "assemble_ms": tot_tf, "elem_per_s": m.nel / (tot_tf * 1e-3),
+                            "max_abs_diff_vs_fp64_rel_to_max": tf_dev,
+                            "note": "tcgen05 kind::tf32, hi/lo operands, FP32 accumulation (p <= 3)"},
             "gmres_iterations": it, "gmres_rel_residual": rel, "gmres_ms_per_iteration": st[0] / max(it, 1),
             "spmv_ms": spmv_ms,
             "ir_fp32_inner": {"inner_iterations": it_ir, "refinement_steps": outer_ir,

@@ -160,13 +160,17 @@ int gbfem_dg_set_degrees(gbfem_ctx ctx, const int *p_el);
  * Without a face table only volume terms are assembled. */
 int gbfem_dg_set_faces(gbfem_ctx ctx, int nfa, const int *fa_type, const int *fa_bc, const int *fa_el,
                        const int *fa_side, const int *fa_nodes);
-/* Volume-integral kernel (no reference counterpart; both give the reference's
- * element matrices to FP64 accuracy): GBFEM_DG_VOLUME_FP64 (FP64 pipe) or
- * GBFEM_DG_VOLUME_TC, the tensor cores with split BF16 products (ten 6-bit
- * slices per operand, exact FP32 slice sums, FP64 recombination; p = 1..3,
- * p = 4 elements keep the FP64 kernel). */
+/* Volume-integral kernel (no reference counterpart): GBFEM_DG_VOLUME_FP64
+ * (FP64 pipe) or GBFEM_DG_VOLUME_TC, the tensor cores with split BF16
+ * products (ten 6-bit slices per operand, exact FP32 slice sums, FP64
+ * recombination), both giving the reference's element matrices to FP64
+ * accuracy; or GBFEM_DG_VOLUME_TF32, the tensor cores with TF32 hi/lo
+ * operands and FP32 accumulation (about 1e-6 of the entry scale: an
+ * approximate matrix, for comparison).  The tensor-core kernels cover
+ * p = 1..3; p = 4 elements keep the FP64 kernel. */
 #define GBFEM_DG_VOLUME_FP64 0
 #define GBFEM_DG_VOLUME_TC 1
+#define GBFEM_DG_VOLUME_TF32 2
 int gbfem_dg_set_volume_kernel(gbfem_ctx ctx, int mode);
 /* Interior-penalty factor, pdr_ctrl_d_params(problem, 12) in the DG weak
  * form (pds_conv_diff_weakform_dg.c:516-531); default 10. */

@@ -17,7 +17,7 @@ ELEMENT, FACE = 4, 3
 COMP_SM, COMP_RHS, COMP_BOTH = 1, 2, 3
 SCATTER_ATOMIC, SCATTER_COLOR = 0, 1
 OPT_CACHE_TABLES = 1
-DG_VOLUME_FP64, DG_VOLUME_TC = 0, 1
+DG_VOLUME_FP64, DG_VOLUME_TC, DG_VOLUME_TF32 = 0, 1, 2
 
 # (name, restype, argtypes) of every symbol include/modfem_gb300.h declares
 _vp, _ci, _cd, _cll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong

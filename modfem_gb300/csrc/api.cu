@@ -542,7 +542,8 @@ int gbfem_dg_set_faces(gbfem_ctx c, int nfa, const int *fa_type, const int *fa_b
 
 int gbfem_dg_set_volume_kernel(gbfem_ctx c, int mode) {
   GB_CHECK(c, "null context");
-  GB_CHECK(mode == GBFEM_DG_VOLUME_FP64 || mode == GBFEM_DG_VOLUME_TC, "unknown DG volume kernel");
+  GB_CHECK(mode == GBFEM_DG_VOLUME_FP64 || mode == GBFEM_DG_VOLUME_TC || mode == GBFEM_DG_VOLUME_TF32,
+           "unknown DG volume kernel");
   c->dg_volume_mode = mode;
   return 0;
 }
@@ -716,7 +717,7 @@ int gbfem_dg_assemble(gbfem_ctx c) {
   int launches = 0;
   // volume terms write every diagonal block and the rhs; the face kernel then
   // adds to those and writes every off-diagonal block: nothing to clear
-  const bool tc = c->dg_volume_mode == GBFEM_DG_VOLUME_TC;
+  const bool tc = c->dg_volume_mode == GBFEM_DG_VOLUME_TC || c->dg_volume_mode == GBFEM_DG_VOLUME_TF32;
   if (tc) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
   cudaEventRecord(c->ev0, c->stream);
   for (int p = 1; p <= 4; p++) {
@@ -725,7 +726,8 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     if (tc && gbfem::dg_tc_supported(p))
       r = gbfem::launch_dg_tc_volume(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->el_nodes.p,
                                      c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->dg_boff_diag_d.p, c->dg_roff_d.p,
-                                     c->dg_val.p, c->dg_rhs.p, c->err.p);
+                                     c->dg_val.p, c->dg_rhs.p, c->err.p,
+                                     c->dg_volume_mode == GBFEM_DG_VOLUME_TF32 ? 1 : 0);
     else
       r = gbfem::launch_dg_prism_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
                                           c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,

@@ -37,6 +37,14 @@
 // Every wait has an iteration limit; on expiry the CTA records an error,
 // drains the copies and MMAs it issued (also with a limit), frees its TMEM
 // and returns.
+//
+// Second mode (TF32, FP32 accumulation): the same GEMM with each scaled
+// operand cut into a TF32 high part and a TF32 remainder (hi + lo carries
+// about 22 bits), the three products hi hi + hi lo + lo hi accumulated in one
+// FP32 TMEM accumulator per element (kind::tf32, K 8 per instruction, 64
+// elements per CTA).  Accuracy is that of FP32 accumulation (about 1e-6 of
+// the entry scale), not FP64: it stands beside the split-BF16 form as the
+// cheaper, approximate contraction.
 
 #include <cuda_bf16.h>
 
@@ -48,32 +56,44 @@
 
 namespace gbfem {
 
-constexpr int TC_SL = 10;       // slices per operand
-constexpr int TC_BITS = 6;      // bits per slice
-constexpr int TC_NE = 32;       // elements per CTA (MMA N)
 constexpr int TC_M = 128;       // MMA M (rows of E per tile)
-constexpr int TC_KC = 48;       // K per streamed chunk (3 MMAs of K 16)
-constexpr int TC_STAGES = 3;
 constexpr int TC_THREADS = 256;
-constexpr int TC_TMEM_COLS = 512;  // >= TC_SL * TC_NE, power of two
 constexpr long long TC_WAIT_LIMIT = 1LL << 26;
+constexpr int TC_BITS = 6;      // bits per slice (split-BF16 mode)
 
-template <int P>
+// MODE 0: split BF16 (exact slice products); MODE 1: TF32 hi/lo
+template <int MODE>
+struct TcMode {
+  static constexpr int ESZ = MODE == 0 ? 2 : 4;        // operand bytes
+  static constexpr int SL = MODE == 0 ? 10 : 2;        // slices per operand
+  static constexpr int NE = MODE == 0 ? 32 : 64;       // elements per CTA (MMA N)
+  static constexpr int KC = MODE == 0 ? 48 : 24;       // K per streamed chunk (96 bytes of a row)
+  static constexpr int KSTEP = MODE == 0 ? 16 : 8;     // K per instruction (32 bytes)
+  static constexpr int NACC = MODE == 0 ? SL : 1;      // TMEM accumulators
+  static constexpr int TMEM_COLS = MODE == 0 ? 512 : 64;  // >= NACC * NE, power of two
+  static constexpr uint32_t FMT = MODE == 0 ? 1u : 2u;  // operand format: BF16 / TF32
+  static constexpr int STAGES = MODE == 0 ? 3 : 4;     // E chunks in flight
+};
+
+template <int P, int MODE>
 struct TcDims {
+  using Md = TcMode<MODE>;
   static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
   static constexpr int NQ = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 48 : 80;
   static constexpr int NSYM = NS * (NS + 1) / 2;
   static constexpr int KDIM = 6 * NQ;
-  static constexpr int KPAD = (KDIM + TC_KC - 1) / TC_KC * TC_KC;
-  static constexpr int NKC = KPAD / TC_KC;
+  static constexpr int KPAD = (KDIM + Md::KC - 1) / Md::KC * Md::KC;
+  static constexpr int NKC = KPAD / Md::KC;
   static constexpr int MT = (NSYM + TC_M - 1) / TC_M;
-  static constexpr int GSL_BYTES = TC_SL * TC_NE * KPAD * 2;    // G slices
-  static constexpr int CHUNK_BYTES = TC_M * TC_KC * 2;          // one E chunk
-  static constexpr int RING_BYTES = TC_STAGES * CHUNK_BYTES;
-  static constexpr int SMEM = GSL_BYTES + RING_BYTES + 256;     // + scales, barriers
-  // exactness of the FP32 accumulation: at most TC_SL slice pairs per
-  // accumulator, products of integers below 2^6
-  static_assert((long long)TC_SL * KPAD * 63 * 63 < (1LL << 24), "slice sums must stay exact in FP32");
+  static constexpr int GSL_BYTES = Md::SL * Md::NE * KPAD * Md::ESZ;  // g slices
+  static constexpr int CHUNK_BYTES = TC_M * Md::KC * Md::ESZ;        // one E chunk
+  static constexpr int RING_BYTES = Md::STAGES * CHUNK_BYTES;
+  static constexpr int SMEM = GSL_BYTES + RING_BYTES + 512;          // + scales, barriers
+  // exactness of the FP32 accumulation in the split-BF16 mode: at most SL
+  // slice pairs per accumulator, products of integers below 2^6
+  static_assert(MODE != 0 || (long long)Md::SL * KPAD * 63 * 63 < (1LL << 24),
+                "slice sums must stay exact in FP32");
+  static_assert(SMEM <= 227 * 1024, "shared memory");
 };
 
 // ---------------------------------------------------------------- PTX helpers
@@ -109,12 +129,20 @@ __device__ __forceinline__ void tc_bulk_load(uint32_t dst, const void *src, uint
                : "memory");
 }
 
+template <int MODE>
 __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-      : "memory");
+  if constexpr (MODE == 0)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
 }
 
 __device__ __forceinline__ void tc_commit(uint32_t mbar) {
@@ -132,9 +160,25 @@ __device__ __forceinline__ void tc_ld8(uint32_t taddr, float *v) {
 }
 
 // byte offset of (row, k) in the canonical no-swizzle K-major layout of a
-// rows x kdim operand: core matrix (row/8, k/8) at row/8 * SBO + k/8 * 128
-__host__ __device__ __forceinline__ int tc_off(int row, int k, int kdim) {
-  return (row >> 3) * (kdim / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+// rows x kdim operand of esz-byte elements: core matrices of 8 rows x 16
+// bytes, core matrix (row/8, k/(16/esz)) at row/8 * SBO + k/(16/esz) * 128
+__host__ __device__ __forceinline__ int tc_off(int row, int k, int kdim, int esz) {
+  const int per = 16 / esz;
+  return (row >> 3) * (kdim / per) * 128 + (k / per) * 128 + (row & 7) * 16 + (k % per) * esz;
+}
+
+// TF32 part of a float: the 19 high bits (sign, exponent, 10 mantissa bits)
+__host__ __device__ __forceinline__ float tc_tf32(float x) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+#else
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  u &= 0xFFFFE000u;
+  float y;
+  memcpy(&y, &u, 4);
+  return y;
+#endif
 }
 
 // 2^e as a double built from its bit pattern (normal range)
@@ -150,31 +194,35 @@ __device__ __forceinline__ int tc_exp_above(double x) {
 }
 
 // ------------------------------------------------------------------ kernel
-template <int P>
+template <int P, int MODE>
 __global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
     const double *__restrict__ k_el, const double *__restrict__ D_el, double f, const double *__restrict__ QPtab,
-    const double *__restrict__ PHItab, const __nv_bfloat16 *__restrict__ Etc, const int *__restrict__ rowexp,
+    const double *__restrict__ PHItab, const uint8_t *__restrict__ Etc, const int *__restrict__ rowexp,
     const int2 *__restrict__ uw, const long long *__restrict__ boff, const int *__restrict__ roff,
     double *__restrict__ val, double *__restrict__ rhs, int *err) {
-  using Dm = TcDims<P>;
+  using Dm = TcDims<P, MODE>;
+  using Md = TcMode<MODE>;
   constexpr int NS = Dm::NS, NQ = Dm::NQ, KPAD = Dm::KPAD, NKC = Dm::NKC, MT = Dm::MT;
+  constexpr int SL = Md::SL, NE = Md::NE, KC = Md::KC, ESZ = Md::ESZ;
+  constexpr int SLICE_BYTES = NE * KPAD * ESZ;
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t *gsl = smem;                             // [TC_SL][TC_NE x KPAD] bf16, canonical layout
-  uint8_t *ring = smem + Dm::GSL_BYTES;            // [TC_STAGES][TC_M x TC_KC] bf16
+  uint8_t *gsl = smem;                             // [SL][NE x KPAD] slices, canonical layout
+  uint8_t *ring = smem + Dm::GSL_BYTES;            // [STAGES][TC_M x KC] E chunks
   int *sexp = (int *)(ring + Dm::RING_BYTES);      // per-element exponent
-  uint64_t *bars = (uint64_t *)(sexp + TC_NE);     // full[3], empty[3], acc
-  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * TC_STAGES + 1);
+  uint64_t *bars = (uint64_t *)(sexp + NE);        // full[3], empty[3], acc
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * Md::STAGES + 1);
   int *abort_flag = (int *)(tmem_slot + 1);
   // phase-A staging inside the ring (unused until phase B)
-  double *sxa = (double *)ring;                    // [TC_NE][27]: 18 coordinates, 9 tensor entries
-  double *svol = sxa + TC_NE * 27;                 // [TC_NE][NQ]: w |det|
+  double *sxa = (double *)ring;                    // [NE][27]: 18 coordinates, 9 tensor entries
+  double *svol = sxa + NE * 27;                    // [NE][NQ]: w |det|
+  static_assert(8 * (NE * 27 + NE * NQ) <= Dm::RING_BYTES, "phase-A staging fits the ring");
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int e0 = blockIdx.x * TC_NE;
-  const int nel_here = min(TC_NE, count - e0);
+  const int e0 = blockIdx.x * NE;
+  const int nel_here = min(NE, count - e0);
 
   // ---------------- phase A: geometry, slices of g, load vector ----------------
-  for (int t = tid; t < TC_NE * 27; t += TC_THREADS) {
+  for (int t = tid; t < NE * 27; t += TC_THREADS) {
     const int el = t / 27, c = t % 27;
     double v = 0.0;
     if (el < nel_here) {
@@ -188,20 +236,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
     }
     sxa[t] = v;
   }
-  if (tid < TC_NE) sexp[tid] = -1100;
+  if (tid < NE) sexp[tid] = -1100;
   if (tid == 0) {
-    for (int i = 0; i < 2 * TC_STAGES + 1; i++)
+    for (int i = 0; i < 2 * Md::STAGES + 1; i++)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(bars + i)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     *abort_flag = 0;
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
-                 "r"(TC_TMEM_COLS));
+                 "r"(Md::TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   __syncthreads();
-  constexpr int ITEMS = (TC_NE * NQ + TC_THREADS - 1) / TC_THREADS;
+  constexpr int ITEMS = (NE * NQ + TC_THREADS - 1) / TC_THREADS;
   double g[ITEMS][6];
 #pragma unroll
   for (int t = 0; t < ITEMS; t++) {
@@ -209,7 +257,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
     const int el = it / NQ, q = it % NQ;
 #pragma unroll
     for (int c = 0; c < 6; c++) g[t][c] = 0.0;
-    if (it < TC_NE * NQ && el < nel_here) {
+    if (it < NE * NQ && el < nel_here) {
       const double *X = sxa + el * 27, *A = X + 18;
       const double xi = QPtab[4 * q], eta = QPtab[4 * q + 1], zeta = QPtab[4 * q + 2], w = QPtab[4 * q + 3];
       const double lo = (1.0 - zeta) / 2.0, hi = (1.0 + zeta) / 2.0, l0 = 1.0 - xi - eta;
@@ -252,44 +300,55 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
     }
   }
   __syncthreads();
-  // slices: y = |g| 2^-E in [0, 1) as a 60-bit fixed-point integer, 6 bits per slice
 #pragma unroll
   for (int t = 0; t < ITEMS; t++) {
     const int it = tid + t * TC_THREADS;
-    if (it >= TC_NE * NQ) continue;
+    if (it >= NE * NQ) continue;
     const int el = it / NQ, q = it % NQ;
     const int E = sexp[el];
 #pragma unroll
     for (int c = 0; c < 6; c++) {
       const double v = g[t][c];
-      const long long bits = __double_as_longlong(v);
-      const int ex = (int)((bits >> 52) & 0x7FF);
-      // |v| = m 2^(ex - 1075) with m the 53-bit mantissa; fixed = |v| 2^(60 - E)
-      unsigned long long fixed = 0;
-      if (ex != 0) {
-        const unsigned long long m = (bits & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
-        const int sh = ex - 1075 + 60 - E;  // left shift of m
-        if (sh >= 0)
-          fixed = sh < 11 ? m << sh : 0ULL;  // |v| < 2^E keeps m << sh below 2^60
-        else if (sh > -64)
-          fixed = m >> (-sh);
-      }
-      const bool neg = bits < 0;
       const int k = 6 * q + c;
+      if constexpr (MODE == 0) {
+        // y = |g| 2^-E in [0, 1) as a 60-bit fixed-point integer, 6 bits per slice
+        const long long bits = __double_as_longlong(v);
+        const int ex = (int)((bits >> 52) & 0x7FF);
+        // |v| = m 2^(ex - 1075) with m the 53-bit mantissa; fixed = |v| 2^(60 - E)
+        unsigned long long fixed = 0;
+        if (ex != 0) {
+          const unsigned long long m = (bits & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+          const int sh = ex - 1075 + 60 - E;  // left shift of m
+          if (sh >= 0)
+            fixed = sh < 11 ? m << sh : 0ULL;  // |v| < 2^E keeps m << sh below 2^60
+          else if (sh > -64)
+            fixed = m >> (-sh);
+        }
+        const bool neg = bits < 0;
 #pragma unroll
-      for (int i = 0; i < TC_SL; i++) {
-        int chunk = (int)((fixed >> (60 - TC_BITS * (i + 1))) & 63ULL);
-        if (neg) chunk = -chunk;
-        *(__nv_bfloat16 *)(gsl + i * (TC_NE * KPAD * 2) + tc_off(el, k, KPAD)) = __int2bfloat16_rn(chunk);
+        for (int i = 0; i < SL; i++) {
+          int chunk = (int)((fixed >> (60 - TC_BITS * (i + 1))) & 63ULL);
+          if (neg) chunk = -chunk;
+          *(__nv_bfloat16 *)(gsl + i * SLICE_BYTES + tc_off(el, k, KPAD, ESZ)) = __int2bfloat16_rn(chunk);
+        }
+      } else {
+        // y = g 2^-E in (-1, 1): TF32 high part and TF32 remainder
+        const double y = v * tc_pow2(E < -1000 ? 0 : -E);  // E = -1100: no nonzero entry
+        const float hi = tc_tf32((float)y);
+        const float lo = tc_tf32((float)(y - (double)hi));
+        *(float *)(gsl + tc_off(el, k, KPAD, ESZ)) = hi;
+        *(float *)(gsl + SLICE_BYTES + tc_off(el, k, KPAD, ESZ)) = lo;
       }
     }
   }
-  // zero the padding of K (k >= 6 NQ) in every slice
+  // zero the padding of K (k >= 6 NQ) in every slice (byte-wise: 0 in both formats)
   if constexpr (Dm::KDIM < KPAD)
-    for (int t = tid; t < TC_SL * TC_NE * (KPAD - Dm::KDIM); t += TC_THREADS) {
-      const int i = t / (TC_NE * (KPAD - Dm::KDIM)), r = t % (TC_NE * (KPAD - Dm::KDIM));
+    for (int t = tid; t < SL * NE * (KPAD - Dm::KDIM); t += TC_THREADS) {
+      const int i = t / (NE * (KPAD - Dm::KDIM)), r = t % (NE * (KPAD - Dm::KDIM));
       const int el = r / (KPAD - Dm::KDIM), k = Dm::KDIM + r % (KPAD - Dm::KDIM);
-      *(__nv_bfloat16 *)(gsl + i * (TC_NE * KPAD * 2) + tc_off(el, k, KPAD)) = __int2bfloat16_rn(0);
+      uint8_t *dst = gsl + i * SLICE_BYTES + tc_off(el, k, KPAD, ESZ);
+#pragma unroll
+      for (int b = 0; b < ESZ; b++) dst[b] = 0;
     }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
@@ -306,35 +365,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
   const uint32_t tmem = *tmem_slot;
 
   // ---------------- phases B and C, one 128-row tile of E at a time ----------------
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_NE >> 3) << 17) |
+  const uint32_t idesc = (1u << 4) | (Md::FMT << 7) | (Md::FMT << 10) | ((uint32_t)(NE >> 3) << 17) |
                          ((uint32_t)(TC_M >> 4) << 24);
-  const uint32_t full0 = tc_smem(bars), empty0 = tc_smem(bars + TC_STAGES), accb = tc_smem(bars + 2 * TC_STAGES);
-  const int T = MT * TC_SL * NKC;  // chunks, in (tile, slice i, k chunk) order
-  auto chunk_src = [&](int t) { return Etc + (size_t)t * (TC_M * TC_KC); };
+  const uint32_t full0 = tc_smem(bars), empty0 = tc_smem(bars + Md::STAGES), accb = tc_smem(bars + 2 * Md::STAGES);
+  const int T = MT * SL * NKC;  // chunks, in (tile, slice i, k chunk) order
+  auto chunk_src = [&](int t) { return Etc + (size_t)t * Dm::CHUNK_BYTES; };
   int issued = 0, mma_done = 0;  // chunks copied / consumed (thread 0)
   if (tid == 0)
-    for (; issued < TC_STAGES && issued < T; issued++)
+    for (; issued < Md::STAGES && issued < T; issued++)
       tc_bulk_load(tc_smem(ring + issued * Dm::CHUNK_BYTES), chunk_src(issued), Dm::CHUNK_BYTES,
                    full0 + 8 * issued);
   for (int m = 0; m < MT; m++) {
     if (tid == 0) {
-      for (int i = 0; i < TC_SL && !*abort_flag; i++) {
+      for (int i = 0; i < SL && !*abort_flag; i++) {
         for (int kc = 0; kc < NKC; kc++) {
-          const int t = mma_done, s = t % TC_STAGES;
-          if (!tc_wait(full0 + 8 * s, (t / TC_STAGES) & 1)) {
+          const int t = mma_done, s = t % Md::STAGES;
+          if (!tc_wait(full0 + 8 * s, (t / Md::STAGES) & 1)) {
             *abort_flag = 1;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t abase = tc_smem(ring + s * Dm::CHUNK_BYTES);
-          for (int j = 0; j < TC_SL - i; j++) {
-            const int d = i + j;
-            const uint32_t bbase = tc_smem(gsl + j * (TC_NE * KPAD * 2));
+          for (int j = 0; j < SL - i; j++) {
+            const int d = MODE == 0 ? i + j : 0;  // accumulator
+            const uint32_t bbase = tc_smem(gsl + j * SLICE_BYTES);
 #pragma unroll
-            for (int ks = 0; ks < TC_KC / 16; ks++) {
-              const uint64_t ad = tc_desc(abase + ks * 256, 128, (TC_KC / 8) * 128);
-              const uint64_t bd = tc_desc(bbase + ((kc * TC_KC + 16 * ks) / 8) * 128, 128, (KPAD / 8) * 128);
-              tc_mma(tmem + d * TC_NE, ad, bd, idesc, (i == 0 && kc == 0 && ks == 0) ? 0u : 1u);
+            for (int ks = 0; ks < KC / Md::KSTEP; ks++) {
+              const uint64_t ad = tc_desc(abase + ks * 256, 128, (KC * ESZ / 16) * 128);
+              const uint64_t bd =
+                  tc_desc(bbase + ((kc * KC + Md::KSTEP * ks) * ESZ / 16) * 128, 128, (KPAD * ESZ / 16) * 128);
+              const bool first = i == 0 && kc == 0 && ks == 0 && (MODE == 0 || j == 0);
+              tc_mma<MODE>(tmem + d * NE, ad, bd, idesc, first ? 0u : 1u);
             }
           }
           tc_commit(empty0 + 8 * s);
@@ -342,8 +403,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
           // refill the stage of the previous chunk (its MMAs are queued ahead
           // of this chunk's, so the tensor pipe keeps working meanwhile)
           if (t >= 1 && issued < T) {
-            const int tp = t - 1, sp = tp % TC_STAGES;
-            if (!tc_wait(empty0 + 8 * sp, (tp / TC_STAGES) & 1)) {
+            const int tp = t - 1, sp = tp % Md::STAGES;
+            if (!tc_wait(empty0 + 8 * sp, (tp / Md::STAGES) & 1)) {
               *abort_flag = 1;
               break;
             }
@@ -360,7 +421,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
       if (tid == 0) {
         atomicExch(err, 5);
         // let the copies still in flight land before the CTA leaves
-        for (int t = mma_done; t < issued; t++) tc_wait(full0 + 8 * (t % TC_STAGES), (t / TC_STAGES) & 1);
+        for (int t = mma_done; t < issued; t++) tc_wait(full0 + 8 * (t % Md::STAGES), (t / Md::STAGES) & 1);
       }
       break;
     }
@@ -372,26 +433,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
     const int2 pw = row_ok ? uw[r] : make_int2(0, 0);
     const int rexp = row_ok ? rowexp[r] : 0;
 #pragma unroll
-    for (int grp = 0; grp < TC_NE / 16; grp++) {
-      const int c0 = half * (TC_NE / 2) + grp * 8;
-      float C[TC_SL][8];
+    for (int grp = 0; grp < NE / 16; grp++) {
+      const int c0 = half * (NE / 2) + grp * 8;
+      float C[Md::NACC][8];
 #pragma unroll
-      for (int d = 0; d < TC_SL; d++)
-        tc_ld8(tmem + ((uint32_t)(lq * 32) << 16) + d * TC_NE + c0, C[d]);
+      for (int d = 0; d < Md::NACC; d++)
+        tc_ld8(tmem + ((uint32_t)(lq * 32) << 16) + d * NE + c0, C[d]);
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
       for (int c = 0; c < 8; c++) {
         const int el = c0 + c;
         if (!row_ok || el >= nel_here) continue;
-        // sum_d C_d 2^(-6(d+2)) = hi 2^-36 + lo 2^-66 with hi = C_0..C_4 and
-        // lo = C_5..C_9 in base 64 (each below 2^49: exact in int64 and FP64)
-        long long hi = 0, lo = 0;
-#pragma unroll
-        for (int d = 0; d < TC_SL / 2; d++) hi = hi * 64 + (long long)__float2int_rn(C[d][c]);
-#pragma unroll
-        for (int d = TC_SL / 2; d < TC_SL; d++) lo = lo * 64 + (long long)__float2int_rn(C[d][c]);
         const int sc = rexp + sexp[el];  // row and element scale exponents
-        const double v = fma((double)lo, tc_pow2(sc - 66), (double)hi * tc_pow2(sc - 36));
+        double v;
+        if constexpr (MODE == 0) {
+          // sum_d C_d 2^(-6(d+2)) = hi 2^-36 + lo 2^-66 with hi = C_0..C_4 and
+          // lo = C_5..C_9 in base 64 (each below 2^49: exact in int64 and FP64)
+          long long hi = 0, lo = 0;
+#pragma unroll
+          for (int d = 0; d < SL / 2; d++) hi = hi * 64 + (long long)__float2int_rn(C[d][c]);
+#pragma unroll
+          for (int d = SL / 2; d < SL; d++) lo = lo * 64 + (long long)__float2int_rn(C[d][c]);
+          v = fma((double)lo, tc_pow2(sc - 66), (double)hi * tc_pow2(sc - 36));
+        } else {
+          v = (double)C[0][c] * tc_pow2(sc);
+        }
         double *blk = val + boff[ent_el[e0 + el]];
         blk[pw.y + NS * pw.x] = v;
         if (pw.x != pw.y) blk[pw.x + NS * pw.y] = v;
@@ -401,24 +467,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dg_tc_volume_kernel(
     __syncthreads();
   }
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Md::TMEM_COLS));
 }
 
 // ------------------------------------------------------------------ host side
 struct TcTables {
-  __nv_bfloat16 *E = nullptr;  // slices in chunk order (tile, slice, k chunk), canonical layout
-  int *rowexp = nullptr;       // row scale exponent: |E[r][k]| < 2^rowexp[r]
-  int2 *uw = nullptr;          // packed upper entry -> (u, w)
+  uint8_t *E = nullptr;   // slices in chunk order (tile, slice, k chunk), canonical layout
+  int *rowexp = nullptr;  // row scale exponent: |E[r][k]| < 2^rowexp[r]
+  int2 *uw = nullptr;     // packed upper entry -> (u, w)
   double *QP = nullptr, *PHI = nullptr;
 };
-static TcTables g_tc[64][GB_DG_PMAX + 1];
-static bool g_tc_ready[64][GB_DG_PMAX + 1];
+static TcTables g_tc[64][2][GB_DG_PMAX + 1];
+static bool g_tc_ready[64][2][GB_DG_PMAX + 1];
 static std::mutex g_tc_mu;
 
-template <int P>
-static int tc_build_tables(int device, TcTables &T) {
-  using Dm = TcDims<P>;
+template <int P, int MODE>
+static int tc_build_tables(TcTables &T) {
+  using Dm = TcDims<P, MODE>;
+  using Md = TcMode<MODE>;
   constexpr int NS = Dm::NS, NQ = Dm::NQ, KPAD = Dm::KPAD, NKC = Dm::NKC, MT = Dm::MT;
+  constexpr int SL = Md::SL, KC = Md::KC, ESZ = Md::ESZ;
   // reference derivative table D[q][a][u] and values PHI[q][u] of the monomial basis
   std::vector<double> D((size_t)NQ * 3 * NS), PHI((size_t)NQ * NS), QP((size_t)NQ * 4);
   for (int q = 0; q < NQ; q++) {
@@ -442,7 +511,7 @@ static int tc_build_tables(int device, TcTables &T) {
   const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
   std::vector<int2> uw(MT * TC_M, make_int2(0, 0));
   std::vector<int> rexp(MT * TC_M, 0);
-  std::vector<__nv_bfloat16> E((size_t)MT * TC_SL * NKC * TC_M * TC_KC, __float2bfloat16(0.0f));
+  std::vector<uint8_t> E((size_t)MT * SL * NKC * Dm::CHUNK_BYTES, 0);
   std::vector<double> row(KPAD);
   int r = 0;
   for (int u = 0; u < NS; u++)
@@ -466,24 +535,35 @@ static int tc_build_tables(int device, TcTables &T) {
       rexp[r] = ex;
       const int m = r / TC_M, rr = r % TC_M;
       for (int k = 0; k < KPAD; k++) {
-        double y = std::fabs(row[k]) * std::ldexp(1.0, -ex);  // [0, 1)
-        const bool neg = row[k] < 0;
-        const int kc = k / TC_KC, kk = k % TC_KC;
-        for (int i = 0; i < TC_SL; i++) {
-          y *= 64.0;
-          const double t = std::floor(y);
-          y -= t;
-          const size_t chunk = ((size_t)m * TC_SL + i) * NKC + kc;
-          E[chunk * TC_M * TC_KC + tc_off(rr, kk, TC_KC) / 2] = __float2bfloat16((float)(neg ? -t : t));
+        const int kc = k / KC, kk = k % KC;
+        auto at = [&](int i) {
+          const size_t chunk = ((size_t)m * SL + i) * NKC + kc;
+          return E.data() + chunk * Dm::CHUNK_BYTES + tc_off(rr, kk, KC, ESZ);
+        };
+        if (MODE == 0) {
+          double y = std::fabs(row[k]) * std::ldexp(1.0, -ex);  // [0, 1)
+          const bool neg = row[k] < 0;
+          for (int i = 0; i < SL; i++) {
+            y *= 64.0;
+            const double t = std::floor(y);
+            y -= t;
+            const __nv_bfloat16 h = __float2bfloat16((float)(neg ? -t : t));
+            memcpy(at(i), &h, 2);
+          }
+        } else {
+          const double y = row[k] * std::ldexp(1.0, -ex);  // (-1, 1)
+          const float hi = tc_tf32((float)y), lo = tc_tf32((float)(y - (double)hi));
+          memcpy(at(0), &hi, 4);
+          memcpy(at(1), &lo, 4);
         }
       }
     }
-  GB_CUDA(cudaMalloc(&T.E, E.size() * sizeof(__nv_bfloat16)));
+  GB_CUDA(cudaMalloc(&T.E, E.size()));
   GB_CUDA(cudaMalloc(&T.rowexp, rexp.size() * sizeof(int)));
   GB_CUDA(cudaMalloc(&T.uw, uw.size() * sizeof(int2)));
   GB_CUDA(cudaMalloc(&T.QP, QP.size() * sizeof(double)));
   GB_CUDA(cudaMalloc(&T.PHI, PHI.size() * sizeof(double)));
-  GB_CUDA(cudaMemcpy(T.E, E.data(), E.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(T.E, E.data(), E.size(), cudaMemcpyHostToDevice));
   GB_CUDA(cudaMemcpy(T.rowexp, rexp.data(), rexp.size() * sizeof(int), cudaMemcpyHostToDevice));
   GB_CUDA(cudaMemcpy(T.uw, uw.data(), uw.size() * sizeof(int2), cudaMemcpyHostToDevice));
   GB_CUDA(cudaMemcpy(T.QP, QP.data(), QP.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -493,38 +573,55 @@ static int tc_build_tables(int device, TcTables &T) {
 
 bool dg_tc_supported(int p) { return p >= 1 && p <= 3; }
 
+template <int P, int MODE>
+static int tc_launch(cudaStream_t st, const TcTables &T, int count, const int *ent_el, const int *el_nodes,
+                     const double *xyz, const double *k_el, const double *D_el, double f, const long long *boff,
+                     const int *roff, double *val, double *rhs, int *err) {
+  const int smem = TcDims<P, MODE>::SMEM;
+  const int grid = (count + TcMode<MODE>::NE - 1) / TcMode<MODE>::NE;
+  GB_CUDA(cudaFuncSetAttribute(dg_tc_volume_kernel<P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  dg_tc_volume_kernel<P, MODE><<<grid, TC_THREADS, smem, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, T.QP,
+                                                              T.PHI, T.E, T.rowexp, T.uw, boff, roff, val, rhs, err);
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
+// mode 0: split BF16 (FP64-equivalent); mode 1: TF32 hi/lo (FP32 accuracy)
 int launch_dg_tc_volume(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                         const double *xyz, const double *k_el, const double *D_el, double f, const long long *boff,
-                        const int *roff, double *val, double *rhs, int *err) {
+                        const int *roff, double *val, double *rhs, int *err, int mode) {
   if (count <= 0) return 0;
   GB_CHECK(dg_tc_supported(p), "tensor-core DG volume kernel covers p = 1..3");
   GB_CHECK(device >= 0 && device < 64, "device index out of range");
+  GB_CHECK(mode == 0 || mode == 1, "tensor-core mode must be 0 (split BF16) or 1 (TF32)");
   {
     std::lock_guard<std::mutex> lk(g_tc_mu);
-    if (!g_tc_ready[device][p]) {
-      int r = p == 1 ? tc_build_tables<1>(device, g_tc[device][p])
-                     : p == 2 ? tc_build_tables<2>(device, g_tc[device][p]) : tc_build_tables<3>(device, g_tc[device][p]);
+    if (!g_tc_ready[device][mode][p]) {
+      TcTables &T = g_tc[device][mode][p];
+      int r;
+      if (mode == 0)
+        r = p == 1 ? tc_build_tables<1, 0>(T) : p == 2 ? tc_build_tables<2, 0>(T) : tc_build_tables<3, 0>(T);
+      else
+        r = p == 1 ? tc_build_tables<1, 1>(T) : p == 2 ? tc_build_tables<2, 1>(T) : tc_build_tables<3, 1>(T);
       if (r < 0) return r;
-      g_tc_ready[device][p] = true;
+      g_tc_ready[device][mode][p] = true;
     }
   }
-  const TcTables &T = g_tc[device][p];
-  const int grid = (count + TC_NE - 1) / TC_NE;
-#define GB_TC_LAUNCH(PP)                                                                                     \
-  {                                                                                                          \
-    const int smem = TcDims<PP>::SMEM;                                                                       \
-    GB_CUDA(cudaFuncSetAttribute(dg_tc_volume_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
-    dg_tc_volume_kernel<PP><<<grid, TC_THREADS, smem, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, T.QP,  \
-                                                            T.PHI, T.E, T.rowexp, T.uw, boff, roff, val, rhs, err); \
+  const TcTables &T = g_tc[device][mode][p];
+#define GB_TC_ARGS T, count, ent_el, el_nodes, xyz, k_el, D_el, f, boff, roff, val, rhs, err
+  if (mode == 0) {
+    switch (p) {
+      case 1: return tc_launch<1, 0>(st, GB_TC_ARGS);
+      case 2: return tc_launch<2, 0>(st, GB_TC_ARGS);
+      default: return tc_launch<3, 0>(st, GB_TC_ARGS);
+    }
   }
   switch (p) {
-    case 1: GB_TC_LAUNCH(1); break;
-    case 2: GB_TC_LAUNCH(2); break;
-    default: GB_TC_LAUNCH(3); break;
+    case 1: return tc_launch<1, 1>(st, GB_TC_ARGS);
+    case 2: return tc_launch<2, 1>(st, GB_TC_ARGS);
+    default: return tc_launch<3, 1>(st, GB_TC_ARGS);
   }
-#undef GB_TC_LAUNCH
-  GB_CUDA(cudaGetLastError());
-  return 1;
+#undef GB_TC_ARGS
 }
 
 }  // namespace gbfem

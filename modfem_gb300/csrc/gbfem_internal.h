@@ -154,7 +154,7 @@ int launch_to_float(cudaStream_t st, long long n, const double *a, float *b);
 bool dg_tc_supported(int p);
 int launch_dg_tc_volume(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                         const double *xyz, const double *k_el, const double *D_el, double f, const long long *boff,
-                        const int *roff, double *val, double *rhs, int *err);
+                        const int *roff, double *val, double *rhs, int *err, int mode);
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                              const double *xyz, const double *k_el, const double *D_el, double f,
                              const long long *boff, const int *roff, double *val, double *rhs, int variant);
@@ -208,7 +208,7 @@ struct gbfem_ctx_s {
   std::vector<int> dg_fa_type, dg_fa_bc, dg_fa_el, dg_fa_side, dg_fa_nodes;
   int dg_nfa = -1;  // -1: no face table (volume terms only)
   double dg_pen = 10.0;
-  int dg_volume_mode = 0;  // GBFEM_DG_VOLUME_FP64 / _TC
+  int dg_volume_mode = 0;  // GBFEM_DG_VOLUME_FP64 / _TC / _TF32
   int dg_var_vol[5] = {0, 0, 0, 0, 0}, dg_var_face[5] = {0, 0, 0, 0, 0};  // launch-shape variants per degree
   gbfem::DevBuf<int> dg_hf_ptr, dg_p_d;
   gbfem::DevBuf<gbfem::DgHalfFace> dg_hf;

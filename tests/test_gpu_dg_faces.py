@@ -198,6 +198,39 @@ def test_dg_tensor_core_volume_vs_fp64_kernel(gb, p):
     assert vec_rel_err(out[1][1], out[0][1]) < 1e-14
 
 
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_dg_tf32_volume_vs_fp64_kernel(gb, p):
+    """TF32 hi/lo tensor-core contraction with FP32 accumulation: an
+    approximate element matrix, within 5e-5 of the FP64 kernel's in the
+    entry-scale measure (and not bit-equal: it is a different precision);
+    the load vector stays FP64."""
+    from modfem_gb300.mesh import anisotropic_tensors, structured_prism_mesh
+    m = structured_prism_mesh(5, jitter=0.25, seed=p + 50)
+    D = anisotropic_tensors(m.nel, seed=p + 50).reshape(m.nel, 9)
+    out = []
+    for mode in (gb.DG_VOLUME_FP64, gb.DG_VOLUME_TF32):
+        c = gb.Context(0)
+        c.set_mesh(m)
+        c.set_coefficients(D=D, f=1.3)
+        c.dg_set_degrees(np.full(m.nel, p))
+        c.dg_build_structure()
+        c.dg_set_volume_kernel(mode)
+        c.dg_assemble()
+        out.append(c.dg_get_matrix())
+        off, bptr, bcol, boff = c.dg_get_structure()
+        c.close()
+    from _util import mat_rel_err
+    ns = [0, 6, 18, 40, 75][p]
+    worst = 0.0
+    for e in range(m.nel):
+        K64 = out[0][0][boff[e]:boff[e] + ns * ns].reshape(ns, ns)
+        Ktf = out[1][0][boff[e]:boff[e] + ns * ns].reshape(ns, ns)
+        worst = max(worst, mat_rel_err(Ktf, K64))
+    print(f"TF32 p={p}: worst energy-scale deviation {worst:.3e}")
+    assert 0.0 < worst < 5e-5, worst  # measured 1.3e-6 / 3.5e-6 / 8.9e-6 for p = 1 / 2 / 3
+    assert vec_rel_err(out[1][1], out[0][1]) < 1e-14
+
+
 @pytest.mark.parametrize("name", ["dg_asm_mixed", "dg_asm_aniso"])
 def test_dg_iterative_refinement_vs_reference(gb, name):
     """Mixed precision (FP64 refinement around FP32-operator GMRES) drives the
