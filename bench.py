@@ -53,9 +53,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help=argparse.SUPPRESS)
-    p.add_argument("--profile", choices=["dg", "dg_tc", "batch"], default=None,
+    p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "batch"], default=None,
                    help="small cases for ncu captures: DG p=3 anisotropic (n^3 x 2 prisms, --n), 3 assemblies "
-                        "(FP64 or tensor-core volume kernel) and one block residual; or the mixed batch "
+                        "(FP64, tensor-core volume, or tensor-core volume and faces) and one block residual; or the mixed batch "
                         "(40,000 prisms + 30,000 tetrahedra, p 1..4), 3 runs")
     return p.parse_args()
 
@@ -86,7 +86,8 @@ def run_profile_case(args):
     c.dg_set_degrees(np.full(m.nel, 3))
     c.dg_set_faces(prism_faces(m), penalty=10.0)
     c.dg_build_structure()
-    c.dg_set_volume_kernel(gb.DG_VOLUME_TC if args.profile == "dg_tc" else gb.DG_VOLUME_FP64)
+    c.dg_set_volume_kernel(gb.DG_VOLUME_TC if args.profile in ("dg_tc", "dg_tcf") else gb.DG_VOLUME_FP64)
+    c.dg_set_face_kernel(gb.DG_FACE_TC if args.profile == "dg_tcf" else gb.DG_FACE_FP64)
     for _ in range(3):
         c.dg_assemble()
     r = c.dg_compute_residual(np.zeros(c.dg_ndof))

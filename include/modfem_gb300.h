@@ -172,6 +172,15 @@ int gbfem_dg_set_faces(gbfem_ctx ctx, int nfa, const int *fa_type, const int *fa
 #define GBFEM_DG_VOLUME_TC 1
 #define GBFEM_DG_VOLUME_TF32 2
 int gbfem_dg_set_volume_kernel(gbfem_ctx ctx, int mode);
+/* Face-integral kernel (no reference counterpart): GBFEM_DG_FACE_FP64 or
+ * GBFEM_DG_FACE_TC, the tensor cores with split BF16 products (seven 8-bit
+ * slices per operand, exact FP32 slice sums, recombination rounded once to
+ * FP64: the reference's face matrices to FP64 accuracy) for owners of degree
+ * <= 3 whose neighbours all have degree <= 3; other owners keep the FP64
+ * kernel. */
+#define GBFEM_DG_FACE_FP64 0
+#define GBFEM_DG_FACE_TC 1
+int gbfem_dg_set_face_kernel(gbfem_ctx ctx, int mode);
 /* Interior-penalty factor, pdr_ctrl_d_params(problem, 12) in the DG weak
  * form (pds_conv_diff_weakform_dg.c:516-531); default 10. */
 int gbfem_dg_set_penalty(gbfem_ctx ctx, double penalty);

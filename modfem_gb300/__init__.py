@@ -18,6 +18,7 @@ COMP_SM, COMP_RHS, COMP_BOTH = 1, 2, 3
 SCATTER_ATOMIC, SCATTER_COLOR = 0, 1
 OPT_CACHE_TABLES = 1
 DG_VOLUME_FP64, DG_VOLUME_TC, DG_VOLUME_TF32 = 0, 1, 2
+DG_FACE_FP64, DG_FACE_TC = 0, 1
 
 # (name, restype, argtypes) of every symbol include/modfem_gb300.h declares
 _vp, _ci, _cd, _cll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
@@ -47,6 +48,7 @@ SIGNATURES = [
     ("gbfem_dg_set_faces", _ci, [_vp, _ci, _vp, _vp, _vp, _vp, _vp]),
     ("gbfem_dg_set_penalty", _ci, [_vp, _cd]),
     ("gbfem_dg_set_volume_kernel", _ci, [_vp, _ci]),
+    ("gbfem_dg_set_face_kernel", _ci, [_vp, _ci]),
     ("gbfem_dg_build_structure", _ci, [_vp, _pi, _pll]),
     ("gbfem_dg_get_structure", _ci, [_vp, _vp, _vp, _vp, _vp]),
     ("gbfem_dg_assemble", _ci, [_vp]),
@@ -243,8 +245,13 @@ class Context:
             self._check(self.L.gbfem_dg_set_penalty(self._h, float(penalty)))
 
     def dg_set_volume_kernel(self, mode):
-        """DG_VOLUME_FP64 or DG_VOLUME_TC (tensor cores, split BF16, FP64-equivalent)."""
+        """DG_VOLUME_FP64, DG_VOLUME_TC (tensor cores, split BF16, FP64-equivalent)
+        or DG_VOLUME_TF32 (tensor cores, TF32 hi/lo, FP32 accumulation)."""
         self._check(self.L.gbfem_dg_set_volume_kernel(self._h, mode))
+
+    def dg_set_face_kernel(self, mode):
+        """DG_FACE_FP64 or DG_FACE_TC (tensor cores, split BF16, FP64-equivalent)."""
+        self._check(self.L.gbfem_dg_set_face_kernel(self._h, mode))
 
     def dg_build_structure(self):
         nd, nv = ctypes.c_int(), ctypes.c_longlong()

@@ -86,7 +86,11 @@ int gbfem_destroy(gbfem_ctx c) {
                           &c->el_table, &c->el_perm, &c->fa_perm, &c->fa_map, &c->err, &c->in_id,
                           &c->in_pos, &c->in_table, &c->dg_roff_d};
   for (auto *b : ibufs) b->release();
-  for (int p = 0; p < 5; p++) c->dg_list[p].release();
+  for (int p = 0; p < 5; p++) {
+    c->dg_list[p].release();
+    c->dg_flist_tc[p].release();
+    c->dg_flist_64[p].release();
+  }
   c->dg_boff_diag_d.release();
   c->dg_val.release();
   c->dg_rhs.release();
@@ -128,7 +132,7 @@ long long gbfem_device_bytes(gbfem_ctx c) {
        c->dg_boff_diag_d.bytes() + c->dg_dinv_off_d.bytes() + c->dg_bptr_d.bytes() + c->dg_bcol_d.bytes() +
        c->dg_hf_ptr.bytes() + c->dg_p_d.bytes() + c->dg_roff_d.bytes() + c->dg_colx_d.bytes() +
        c->dg_row_val_d.bytes() + c->dg_cx_off_d.bytes();
-  for (int p = 0; p < 5; p++) s += c->dg_list[p].bytes();
+  for (int p = 0; p < 5; p++) s += c->dg_list[p].bytes() + c->dg_flist_tc[p].bytes() + c->dg_flist_64[p].bytes();
   return s;
 }
 
@@ -548,6 +552,13 @@ int gbfem_dg_set_volume_kernel(gbfem_ctx c, int mode) {
   return 0;
 }
 
+int gbfem_dg_set_face_kernel(gbfem_ctx c, int mode) {
+  GB_CHECK(c, "null context");
+  GB_CHECK(mode == GBFEM_DG_FACE_FP64 || mode == GBFEM_DG_FACE_TC, "unknown DG face kernel");
+  c->dg_face_mode = mode;
+  return 0;
+}
+
 int gbfem_dg_set_penalty(gbfem_ctx c, double pen) {
   GB_CHECK(c, "null context");
   GB_CHECK(pen > 0.0, "penalty must be positive");
@@ -677,6 +688,24 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
     });
     GB_TRY(upload(c, c->dg_list[p], lst.data(), lst.size()));
   }
+  // face owners of degree <= 3 whose neighbours all have degree <= 3 suit
+  // the tensor-core face kernel; the others keep the FP64 one
+  for (int p = 1; p <= 4; p++) {
+    std::vector<int> tcl, fpl;
+    for (int e = 0; e < nel; e++) {
+      if (c->dg_p[e] != p) continue;
+      bool ok = p <= 3;
+      for (int h = hptr[e]; ok && h < hptr[e + 1]; h++) {
+        const int nb = hf[h].owner_is_2 ? hf[h].el1 : hf[h].el2;
+        if (nb >= 0 && c->dg_p[nb] > 3) ok = false;
+      }
+      (ok ? tcl : fpl).push_back(e);
+    }
+    c->dg_flist_tc[p].release();
+    c->dg_flist_64[p].release();
+    if (!tcl.empty()) GB_TRY(upload(c, c->dg_flist_tc[p], tcl.data(), tcl.size()));
+    if (!fpl.empty()) GB_TRY(upload(c, c->dg_flist_64[p], fpl.data(), fpl.size()));
+  }
   GB_TRY(upload(c, c->dg_row_val_d, row_val.data(), row_val.size()));
   GB_TRY(upload(c, c->dg_cx_off_d, cx_off.data(), cx_off.size()));
   GB_TRY(upload(c, c->dg_colx_d, colx.data(), colx.size()));
@@ -737,9 +766,27 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     launches += r;
   }
   cudaEventRecord(c->ev2, c->stream);
+  const bool tcf = c->dg_face_mode == GBFEM_DG_FACE_TC;
   if (c->dg_hf.p) {
+    if (tcf && !tc) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
     for (int p = 1; p <= 4; p++) {
       if (!c->dg_list[p].p) continue;
+      if (tcf) {
+        // tensor-core eligible owners, then the rest on the FP64 kernel
+        int r = gbfem::launch_dg_tc_faces(c->stream, p, (int)c->dg_flist_tc[p].n, c->dg_flist_tc[p].p,
+                                          c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p,
+                                          c->k_el.p, c->D_el.p, c->dg_pen, c->g, c->dg_boff_diag_d.p,
+                                          c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p, c->err.p);
+        GB_TRY(r);
+        launches += r;
+        r = gbfem::launch_dg_prism_faces(c->stream, p, (int)c->dg_flist_64[p].n, c->dg_flist_64[p].p, c->dg_hf_ptr.p,
+                                         c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
+                                         c->dg_pen, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,
+                                         c->dg_rhs.p, c->dg_var_face[p]);
+        GB_TRY(r);
+        launches += r;
+        continue;
+      }
       int r = gbfem::launch_dg_prism_faces(c->stream, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->dg_hf_ptr.p,
                                            c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
                                            c->dg_pen, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,
@@ -753,10 +800,13 @@ int gbfem_dg_assemble(gbfem_ctx c) {
   cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
   cudaEventElapsedTime(&c->last_el_ms, c->ev0, c->ev2);
   cudaEventElapsedTime(&c->last_fa_ms, c->ev2, c->ev1);
-  if (tc) {
+  if (tc || (tcf && c->dg_hf.p)) {
     int herr = 0;
     GB_CUDA(cudaMemcpy(&herr, c->err.p, sizeof(int), cudaMemcpyDeviceToHost));
-    GB_CHECK(herr == 0, "tensor-core volume kernel: a pipeline wait expired");
+    GB_CHECK(herr != 5, "tensor-core volume kernel: a pipeline wait expired");
+    GB_CHECK(herr != 6, "tensor-core face kernel: an MMA completion wait expired");
+    GB_CHECK(herr != 7, "tensor-core face kernel: an owner with a degree-4 neighbour reached it");
+    GB_CHECK(herr == 0, "tensor-core kernel error " + std::to_string(herr));
   }
   c->last_launches = launches;
   return 0;

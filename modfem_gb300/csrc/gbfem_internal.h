@@ -127,6 +127,11 @@ struct DgHalfFace {
   int pad;
 };
 
+bool dg_tc_faces_supported(int p);
+int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
+                       const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
+                       const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
+                       const int *roff, double *val, double *rhs, int *err);
 int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                           const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                           const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
@@ -202,6 +207,7 @@ struct gbfem_ctx_s {
   int dg_ndof = 0;
   bool dg_ready = false;
   gbfem::DevBuf<int> dg_list[5], dg_roff_d;
+  gbfem::DevBuf<int> dg_flist_tc[5], dg_flist_64[5];  // face owners: tensor-core eligible / FP64
   gbfem::DevBuf<long long> dg_boff_diag_d;
   gbfem::DevBuf<double> dg_val, dg_rhs;
   // DG faces: the caller's face table and the per-element incidences
@@ -209,6 +215,7 @@ struct gbfem_ctx_s {
   int dg_nfa = -1;  // -1: no face table (volume terms only)
   double dg_pen = 10.0;
   int dg_volume_mode = 0;  // GBFEM_DG_VOLUME_FP64 / _TC / _TF32
+  int dg_face_mode = 0;    // GBFEM_DG_FACE_FP64 / _TC
   int dg_var_vol[5] = {0, 0, 0, 0, 0}, dg_var_face[5] = {0, 0, 0, 0, 0};  // launch-shape variants per degree
   gbfem::DevBuf<int> dg_hf_ptr, dg_p_d;
   gbfem::DevBuf<gbfem::DgHalfFace> dg_hf;

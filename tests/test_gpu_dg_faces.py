@@ -168,6 +168,71 @@ def test_dg_tensor_core_volume_vs_reference(gb, name):
     assert vec_rel_err(rhs, g["rhs"]) < REL_TOL
 
 
+@pytest.mark.parametrize("name", ["dg_asm_p2", "dg_asm_mixed", "dg_asm_aniso"])
+def test_dg_tensor_core_faces_vs_reference(gb, name):
+    """The tensor-core face kernel (and volume kernel) give the reference's
+    assembled system to the FP64 tolerance; owners with a degree-4 neighbour
+    stay on the FP64 face kernel."""
+    g, m, F = _fixture_problem(name)
+    D = _tensors(g)
+    c = _context(gb, m, F, g["pdeg"], k=None if D is not None else g["k"], D=D, pen=float(g["pen"]),
+                 g=float(g["g"]), f=float(g["f"]))
+    c.dg_set_volume_kernel(gb.DG_VOLUME_TC)
+    c.dg_set_face_kernel(gb.DG_FACE_TC)
+    c.dg_assemble()
+    rp, ci, v, rhs, off = _expand(c)
+    assert np.array_equal(rp, g["row_ptr"]) and np.array_equal(ci, g["col_ind"])
+    err = sparse_rel_err(rp, ci, v, g["val"])
+    print(f"{name}: tensor-core faces vs reference {err:.2e}")
+    assert err < REL_TOL
+    assert vec_rel_err(rhs, g["rhs"]) < REL_TOL
+
+
+@pytest.mark.parametrize("n,pmax,aniso", [(6, 1, False), (6, 2, True), (7, 3, True), (8, 3, False), (8, 4, False)])
+def test_dg_tensor_core_faces_vs_fp64_kernel(gb, n, pmax, aniso):
+    """Whole block matrix with tensor-core faces against the FP64 face kernel
+    on jittered meshes larger than the fixtures (uniform and mixed degrees,
+    isotropic lognormal and anisotropic tensors)."""
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(n, jitter=0.2, seed=n + pmax)
+    F = prism_faces(m)
+    rng = np.random.default_rng(n)
+    pdeg = np.full(m.nel, pmax) if n % 2 else rng.integers(1, pmax + 1, m.nel)
+    kw = {"D": anisotropic_tensors(m.nel, seed=n).reshape(m.nel, 9)} if aniso else {"k": lognormal_k(m.nel, seed=n)}
+    out = []
+    for mode in (gb.DG_FACE_FP64, gb.DG_FACE_TC):
+        c = _context(gb, m, F, pdeg, g=0.3, f=1.0, **kw)
+        c.dg_set_face_kernel(mode)
+        c.dg_assemble()
+        out.append(_expand(c))
+        c.close()
+    (rp, ci, v64, r64, _), (rp2, ci2, vtc, rtc, _) = out
+    assert np.array_equal(rp, rp2) and np.array_equal(ci, ci2)
+    err = sparse_rel_err(rp, ci, vtc, v64)
+    print(f"n={n} pmax={pmax}: tensor-core faces vs FP64 faces {err:.2e}")
+    assert err < REL_TOL
+    assert vec_rel_err(rtc, r64) < REL_TOL
+
+
+def test_dg_tensor_core_faces_constant_reproduction(gb):
+    """With f = 0 and Dirichlet value c, the constant is an exact discrete
+    solution of the system the tensor-core kernels assemble."""
+    from modfem_gb300.mesh import lognormal_k, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(16, jitter=0.2, seed=3)
+    F = prism_faces(m)
+    pdeg = np.random.default_rng(3).integers(1, 4, m.nel)
+    c = _context(gb, m, F, pdeg, k=lognormal_k(m.nel, seed=3), g=0.7, f=0.0)
+    c.dg_set_volume_kernel(gb.DG_VOLUME_TC)
+    c.dg_set_face_kernel(gb.DG_FACE_TC)
+    c.dg_assemble()
+    off = c.dg_get_structure()[0]
+    x = np.zeros(off[-1])
+    x[off[:-1]] = 0.7
+    r = c.dg_compute_residual(x)
+    vals, rhs = c.dg_get_matrix()
+    assert np.max(np.abs(r)) < 1e-11 * np.max(np.abs(rhs))
+
+
 @pytest.mark.parametrize("p", [1, 2, 3])
 def test_dg_tensor_core_volume_vs_fp64_kernel(gb, p):
     """Element blocks of the tensor-core kernel against the FP64 kernel on a
