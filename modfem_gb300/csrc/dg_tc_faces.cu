@@ -25,8 +25,9 @@
 // <= 3 (2 nq <= 32); the others keep the FP64 face kernel.
 //
 // First the geometry and monomial factors of all the element's faces at
-// once (one thread per face, point and side: the long FP64 chains with their
-// divisions and square roots run side by side).  Then per face: FP64 basis
+// once (one thread per face and point, in two passes: first side, whose
+// Jacobian gives the normal, then the second side; the long FP64 chains with
+// their divisions and square roots run side by side).  Then per face: FP64 basis
 // values, row exponents, slicing (all threads); 56 MMAs (M 128, N = NS
 // rounded up to 16, K 16) issued by one thread into 7 accumulators; commit to
 // an mbarrier; epilogue by all warps (tcgen05.ld: warp w reads TMEM lane
@@ -45,8 +46,7 @@ static __device__ const unsigned char tf_exp[GB_DG_PMAX][GB_DG_MAXNS][3] = GB_DG
 static __device__ const int tf_ns[GB_DG_PMAX + 1] = GB_DG_NS_INIT;
 static __device__ const int tf_nqf[GB_DG_PMAX + 1][2] = GB_DG_NQF_INIT;
 
-constexpr int TF_SL = 7;          // slices per operand
-constexpr int TF_BITS = 8;        // bits per slice (integers up to 255: exact in BF16)
+constexpr int TF_SL = 7;          // slices per operand, 8 bits each (integers up to 255: exact in BF16)
 constexpr int TF_KP = 32;         // K: 2 x (up to 16 face points)
 constexpr int TF_NQ = 16;         // face points of the largest rule with max(p1, p2) <= 3
 constexpr int TF_NF = 5;          // faces of a prism
@@ -55,6 +55,7 @@ constexpr int TF_THREADS = 256;
 constexpr int TF_TMEM_COLS = 512;
 constexpr int TF_GEO = 16;
 constexpr int TF_FAC = 30;
+constexpr int TF_LD = TF_KP + 1;  // FP64 staging row stride (odd: no bank conflicts down a column)
 static_assert((long long)TF_SL * TF_KP * 255 * 255 < (1LL << 24), "slice sums must stay exact in FP32");
 static_assert(TF_NF * (2 * TF_NQ + 1) <= TF_THREADS, "one thread per (face, point, side) and per face");
 
@@ -67,8 +68,10 @@ struct TfDims {
   static constexpr int B_SLICE = NPAD * TF_KP * 2;
   static constexpr int OFF_B = TF_SL * A_SLICE;
   static constexpr int OFF_A64 = OFF_B + TF_SL * B_SLICE;
-  static constexpr int OFF_B64 = OFF_A64 + ROWS * TF_KP * 8;
-  static constexpr int OFF_MISC = OFF_B64 + NS * TF_KP * 8;
+  static constexpr int OWNQ = (NS + 3) / 4;          // own functions per TMEM lane quarter
+  static constexpr int OFF_B64 = OFF_A64 + ROWS * TF_LD * 8;
+  static constexpr int OFF_UW = OFF_B64 + NS * TF_LD * 8;
+  static constexpr int OFF_MISC = OFF_UW + TF_NQ * 2 * 16 * 2 * 8;
   // per face: sX [2][18], sA [2][9], sGeo [TF_NQ][TF_GEO], sFac [TF_NQ][2][TF_FAC], pen, spare
   static constexpr int FACE_DOUBLES = 36 + 18 + TF_NQ * TF_GEO + 2 * TF_NQ * TF_FAC + 2;
   static constexpr int OFF_HF = OFF_MISC + TF_NF * FACE_DOUBLES * 8;
@@ -77,6 +80,7 @@ struct TfDims {
   static_assert(TF_SL * NPAD <= TF_TMEM_COLS, "accumulators fit the TMEM allocation");
   static_assert(SMEM <= 227 * 1024, "shared memory");
   static_assert(OFF_HF % 16 == 0 && OFF_INT % 16 == 0, "alignment");
+  static_assert(OWNQ + 10 <= 32, "own and neighbour rows of a lane quarter");
 };
 
 // biased FP64 exponent field of x (0 for zero / subnormal)
@@ -114,15 +118,9 @@ __device__ __forceinline__ double tf_i64_scaled(long long x, int sc) {
   return __longlong_as_double((long long)bits);
 }
 
-// One side of one face point (the split of dg_face_point by side, same
-// operations): the point in that side's local coordinates and v = J^-1 A^T n;
-// also the area weight.  The normal comes from the first neighbour in both
-// cases.
-__device__ __forceinline__ void tf_face_side(int nfv, const double *fq, const double *X1, const unsigned char *loc1,
-                                             int side1, const double *A1, const double *X2,
-                                             const unsigned char *loc2, const double *A2, int sd, v3 &e, v3 &v,
-                                             double &a) {
-  double w[4];
+// Face-vertex weights of a face rule point: barycentric on triangles,
+// bilinear on quadrilaterals (as dg_face_point)
+__device__ __forceinline__ void tf_weights(int nfv, const double *fq, double *w) {
   if (nfv == 3) {
     w[0] = 1.0 - fq[0] - fq[1];
     w[1] = fq[0];
@@ -135,21 +133,32 @@ __device__ __forceinline__ void tf_face_side(int nfv, const double *fq, const do
     w[2] = u * vv;
     w[3] = (1.0 - u) * vv;
   }
-  v3 e1 = {0, 0, 0}, e2 = {0, 0, 0};
+}
+
+__device__ __forceinline__ v3 tf_local_point(int nfv, const double *w, const unsigned char *loc) {
+  v3 e = {0, 0, 0};
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     if (i >= nfv) break;
-    e1 = v3_fma(w[i], prism_vertex_local(loc1[i]), e1);
-    if (sd) e2 = v3_fma(w[i], prism_vertex_local(loc2[i]), e2);
+    e = v3_fma(w[i], prism_vertex_local(loc[i]), e);
   }
-  v3 j1, j2, j3;
-  prism_jacobian_columns(X1, e1, j1, j2, j3);
-  const v3 ds = prism_side_vector(side1, j1, j2, j3);
-  const double d = sqrt(v3_dot(ds, ds));
-  const v3 n = v3_scale(1.0 / d, ds);
-  a = d * fq[2];
-  e = sd ? e2 : e1;
-  v = sd ? dg_face_v(X2, e2, A2, n) : dg_face_v(X1, e1, A1, n);
+  return e;
+}
+
+// v = J^-1 A^T n from the Jacobian columns (the operations of dg_face_v)
+__device__ __forceinline__ v3 tf_face_v(v3 j1, v3 j2, v3 j3, const double *A, v3 n) {
+  const v3 c1 = v3_cross(j2, j3), c2 = v3_cross(j3, j1), c3 = v3_cross(j1, j2);
+  const double rdet = 1.0 / v3_dot(j1, c1);
+  const v3 an = {A[0] * n.x + A[3] * n.y + A[6] * n.z, A[1] * n.x + A[4] * n.y + A[7] * n.z,
+                 A[2] * n.x + A[5] * n.y + A[8] * n.z};
+  return {v3_dot(c1, an) * rdet, v3_dot(c2, an) * rdet, v3_dot(c3, an) * rdet};
+}
+
+// BF16 bit pattern of the integer c (|c| <= 255): through an FP32 add on the
+// FMA pipe (exact), the sign set separately
+__device__ __forceinline__ uint32_t tf_bf16_bits(uint32_t mag, bool neg) {
+  const float fv = __uint_as_float(0x4B000000u | mag) - 8388608.0f;
+  return (__float_as_uint(fv) >> 16) | (neg ? 0x8000u : 0u);
 }
 
 template <int P>
@@ -163,8 +172,9 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
   constexpr int NS = Dm::NS, NPAD = Dm::NPAD, FD = Dm::FACE_DOUBLES;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *asl = smem, *bsl = smem + Dm::OFF_B;
-  double *A64 = (double *)(smem + Dm::OFF_A64);      // [ROWS][TF_KP]
-  double *B64 = (double *)(smem + Dm::OFF_B64);      // [NS][TF_KP]
+  double *A64 = (double *)(smem + Dm::OFF_A64);      // [ROWS][TF_LD]
+  double *B64 = (double *)(smem + Dm::OFF_B64);      // [NS][TF_LD]
+  double *sUW = (double *)(smem + Dm::OFF_UW);       // [TF_NQ][2][16][2]: per (b, c) basis products
   double *sface = (double *)(smem + Dm::OFF_MISC);   // [TF_NF][FD]
   DgHalfFace *sHF = (DgHalfFace *)(smem + Dm::OFF_HF);
   int *ea = (int *)(smem + Dm::OFF_INT);             // A row exponents
@@ -216,26 +226,36 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
     }
   }
   __syncthreads();
-  // ---- geometry and monomial factors per (face, point, side); penalty per face ----
-  if (tid < nf * 2 * TF_NQ) {
-    const int f = tid / (2 * TF_NQ), q = (tid >> 1) % TF_NQ, sd = tid & 1;
+  // ---- geometry: phase 1, per (face, point), the first neighbour's side
+  // (point, Jacobian, normal, area weight, v, factors), and the penalty per
+  // face; phase 2 the second neighbour's side and the owner-row scales ----
+  if (tid < nf * TF_NQ) {
+    const int f = tid / TF_NQ, q = tid % TF_NQ;
     const DgHalfFace &F = sHF[f];
     const bool interior = F.el2 >= 0;
     const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
     const int ti = F.nfv == 4 ? 1 : 0;
     const int pr = (interior && tf_nqf[p2][ti] > tf_nqf[p1][ti]) ? p2 : p1;
-    if (pr <= 3 && q < tf_nqf[pr][ti] && (sd == 0 || interior)) {
-      double *X = sface + f * FD;
-      v3 ev, vv;
-      double aw;
-      tf_face_side(F.nfv, tf_fq[pr - 1][ti][q], X, F.loc1, F.side1, X + 36, interior ? X + 18 : nullptr, F.loc2,
-                   X + 45, sd, ev, vv, aw);
-      double *G = X + 54 + q * TF_GEO;
-      if (sd == 0) G[12] = aw;
-      dg_point_factors(ev, vv, X + 54 + TF_NQ * TF_GEO + (2 * q + sd) * TF_FAC);
+    if (pr <= 3 && q < tf_nqf[pr][ti]) {
+      double *X = sface + f * FD, *G = X + 54 + q * TF_GEO;
+      const double *fq = tf_fq[pr - 1][ti][q];
+      double w[4];
+      tf_weights(F.nfv, fq, w);
+      const v3 e1 = tf_local_point(F.nfv, w, F.loc1);
+      v3 j1, j2, j3;
+      prism_jacobian_columns(X, e1, j1, j2, j3);
+      const v3 ds = prism_side_vector(F.side1, j1, j2, j3);
+      const double d = sqrt(v3_dot(ds, ds));
+      const v3 n = v3_scale(1.0 / d, ds);
+      const v3 v1 = tf_face_v(j1, j2, j3, X + 36, n);
+      G[12] = d * fq[2];
+      G[13] = n.x;  // the normal, for phase 2 (then overwritten by the scales)
+      G[14] = n.y;
+      G[15] = n.z;
+      dg_point_factors(e1, v1, X + 54 + TF_NQ * TF_GEO + (2 * q) * TF_FAC);
     }
-  } else if (tid >= 2 * TF_NF * TF_NQ && tid < 2 * TF_NF * TF_NQ + nf) {
-    const int f = tid - 2 * TF_NF * TF_NQ;
+  } else if (tid >= TF_NF * TF_NQ && tid < TF_NF * TF_NQ + nf) {
+    const int f = tid - TF_NF * TF_NQ;
     const DgHalfFace &F = sHF[f];
     const bool interior = F.el2 >= 0;
     const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
@@ -250,24 +270,43 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
     sface[f * FD + FD - 2] = pen * pp / sqrt(dg_face_area(V, F.nfv));
   }
   __syncthreads();
-  // owner-row scales per (face, point): L = (f a) g + (s_o c a) phi, M = -(s_o f a) phi
   if (tid < nf * TF_NQ) {
     const int f = tid / TF_NQ, q = tid % TF_NQ;
     const DgHalfFace &F = sHF[f];
-    double *G = sface + f * FD + 54 + q * TF_GEO;
-    const double aw = G[12], so = F.owner_is_2 ? -1.0 : 1.0, fac = F.el2 >= 0 ? 0.5 : 1.0;
-    G[13] = fac * aw;
-    G[14] = so * sface[f * FD + FD - 2] * aw;
-    G[15] = -so * fac * aw;
+    const bool interior = F.el2 >= 0;
+    const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
+    const int ti = F.nfv == 4 ? 1 : 0;
+    const int pr = (interior && tf_nqf[p2][ti] > tf_nqf[p1][ti]) ? p2 : p1;
+    if (pr <= 3 && q < tf_nqf[pr][ti]) {
+      double *X = sface + f * FD, *G = X + 54 + q * TF_GEO;
+      if (interior) {
+        double w[4];
+        tf_weights(F.nfv, tf_fq[pr - 1][ti][q], w);
+        const v3 e2 = tf_local_point(F.nfv, w, F.loc2);
+        v3 j1, j2, j3;
+        prism_jacobian_columns(X + 18, e2, j1, j2, j3);
+        const v3 v2 = tf_face_v(j1, j2, j3, X + 45, v3{G[13], G[14], G[15]});
+        dg_point_factors(e2, v2, X + 54 + TF_NQ * TF_GEO + (2 * q + 1) * TF_FAC);
+      }
+      // owner-row scales: L = (f a) g + (s_o c a) phi, M = -(s_o f a) phi
+      const double aw = G[12], so = F.owner_is_2 ? -1.0 : 1.0, fac = interior ? 0.5 : 1.0;
+      G[13] = fac * aw;
+      G[14] = so * X[FD - 2] * aw;
+      G[15] = -so * fac * aw;
+    }
   }
   // (the per-face loop starts with a barrier)
 
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NPAD >> 3) << 17) |
                          ((uint32_t)(TF_M >> 4) << 24);
-  // the diagonal-block share: thread (row r < NS, column half) holds columns
-  // half * NPAD/2 + [0, NPAD/2)
-  const int lq = warp & 3, half = warp >> 2;
-  const int r_ep = lq * 32 + (tid & 31);
+  // Rows of A (and of D) are spread over the four TMEM lane quarters so that
+  // every warp shares the epilogue: in quarter l, lanes [0, OWNQ) hold own
+  // functions l OWNQ + lane, lanes [OWNQ, OWNQ + nbq) the neighbour's
+  // functions l nbq + lane - OWNQ.  The diagonal-block share of own function
+  // j (thread: its lane, column half) stays in that thread's registers.
+  const int lq = warp & 3, half = warp >> 2, lane = tid & 31;
+  const int r_ep = lq * 32 + lane;                                 // TMEM lane = M row
+  const int j_own = lane < Dm::OWNQ ? lq * Dm::OWNQ + lane : NS;  // NS: not an own row
   double dacc[NPAD / 2];
 #pragma unroll
   for (int c = 0; c < NPAD / 2; c++) dacc[c] = 0.0;
@@ -292,75 +331,93 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
       bad_input = true;
       break;
     }
+    const int nbq = (ns_nb + 3) / 4;
+    // M row of A row r (own functions first, then the neighbour's)
+    auto mrow = [&](int r) {
+      return r < NS ? (r / Dm::OWNQ) * 32 + r % Dm::OWNQ : ((r - NS) / nbq) * 32 + Dm::OWNQ + (r - NS) % nbq;
+    };
     __syncthreads();  // the previous face's shared arrays are free; the scales are written
-    // FP64 operands, one basis evaluation per (row, point): A rows = e's
-    // functions then the neighbour's (k = 2q: Phi, 2q + 1: Gam), B rows =
-    // e's functions (L, M); the K padding is zeroed when slicing
+    // per (point, side, b, c): U = eta^b zeta^c and W, the (eta, zeta) part of v . grad
+    for (int t = tid; t < nq * 2 * 16; t += TF_THREADS) {
+      const int q = t >> 5, sd = (t >> 4) & 1, bc = t & 15, b = bc >> 2, c = bc & 3;
+      if (sd == 1 && !interior) continue;
+      const double *T = sFac + (2 * q + sd) * TF_FAC;
+      double *uw = sUW + ((q * 2 + sd) * 16 + bc) * 2;
+      uw[0] = T[5 + b] * T[10 + c];
+      uw[1] = fma(T[5 + b], T[25 + c], T[20 + b] * T[10 + c]);
+    }
+    __syncthreads();
+    // FP64 operands, per (row, point): A rows = e's functions then the
+    // neighbour's (k = 2q: Phi, 2q + 1: Gam), B rows = e's functions (L, M);
+    // phi = xi^a U, g = v_xi a xi^(a-1) U + xi^a W (the operations of
+    // dg_basis_from_factors); the K padding is zeroed when slicing
     for (int t = tid; t < rows * nq; t += TF_THREADS) {
       const int r = t / nq, q = t - r * nq;
       const bool own = r < NS;
       const int side = own ? own_side : 3 - own_side, jj = own ? r : r - NS, p = own ? P : pnb;
       const unsigned char *ex = tf_exp[p - 1][jj];
-      double phi, g;
-      dg_basis_from_factors(sFac + (2 * q + side - 1) * TF_FAC, ex[0], ex[1], ex[2], phi, g);
+      const double *T = sFac + (2 * q + side - 1) * TF_FAC;
+      const double *uw = sUW + ((q * 2 + side - 1) * 16 + ex[1] * 4 + ex[2]) * 2;
+      const double phi = T[ex[0]] * uw[0];
+      const double g = fma(T[15 + ex[0]], uw[0], T[ex[0]] * uw[1]);
       // Phi = s_t phi: the sign flip on the integer side
-      A64[r * TF_KP + 2 * q] = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
-      A64[r * TF_KP + 2 * q + 1] = g;
+      A64[r * TF_LD + 2 * q] = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
+      A64[r * TF_LD + 2 * q + 1] = g;
       if (own) {
         const double *G = sGeo + q * TF_GEO;
-        B64[r * TF_KP + 2 * q] = fma(G[13], g, G[14] * phi);
-        B64[r * TF_KP + 2 * q + 1] = G[15] * phi;
+        B64[r * TF_LD + 2 * q] = fma(G[13], g, G[14] * phi);
+        B64[r * TF_LD + 2 * q + 1] = G[15] * phi;
       }
     }
     __syncthreads();
     if (!interior && tid < NS) {
       double s = 0.0;
-      for (int q = 0; q < nq; q++) s += B64[tid * TF_KP + 2 * q];
+      for (int q = 0; q < nq; q++) s += B64[tid * TF_LD + 2 * q];
       racc = fma(gval, s, racc);
     }
     // row exponents (integer max of the exponent fields): threads
-    // 0..rows-1 for A, 128..128+NS-1 for B
+    // 0..rows-1 for A (stored by M row), 128..128+NS-1 for B
     if (tid < rows || (tid >= 128 && tid < 128 + NS)) {
-      const double *row = tid < 128 ? A64 + tid * TF_KP : B64 + (tid - 128) * TF_KP;
+      const double *row = tid < 128 ? A64 + tid * TF_LD : B64 + (tid - 128) * TF_LD;
       int emax = 0;
       for (int k = 0; k < 2 * nq; k++) emax = max(emax, tf_biased_exp(row[k]));
       if (tid < 128)
-        ea[tid] = tf_row_exp(emax);
+        ea[mrow(tid)] = tf_row_exp(emax);
       else
         eb[tid - 128] = tf_row_exp(emax);
     }
     __syncthreads();
     // slices: one thread per (row, 8 consecutive k), one 16-byte store per
-    // slice (a core-matrix row of the canonical K-major layout); rows of A
-    // beyond `rows` and of B beyond NS are never written: their D rows and
-    // columns are discarded
+    // slice (a core-matrix row of the canonical K-major layout); M rows of A
+    // holding no function and rows of B beyond NS are never written: their D
+    // rows and columns are discarded
     for (int t = tid; t < (rows + NS) * (TF_KP / 8); t += TF_THREADS) {
       const int r = t / (TF_KP / 8), k0 = (t % (TF_KP / 8)) * 8;
       const bool isa = r < rows;
       const int rr = isa ? r : r - rows;
-      const double *src = isa ? A64 + rr * TF_KP : B64 + rr * TF_KP;
-      const int ex = isa ? ea[rr] : eb[rr];
-      unsigned long long fx[8];
+      const int drow = isa ? mrow(rr) : rr;
+      const double *src = isa ? A64 + rr * TF_LD : B64 + rr * TF_LD;
+      const int ex = isa ? ea[drow] : eb[rr];
+      uint32_t fh[8], fl[8];  // fixed-point bits 55..24 and 23..0
       bool neg[8];
 #pragma unroll
       for (int u = 0; u < 8; u++) {
         const double v = k0 + u < 2 * nq ? src[k0 + u] : 0.0;
-        fx[u] = tf_fixed(v, ex);
+        const unsigned long long fx = tf_fixed(v, ex);
+        fh[u] = (uint32_t)(fx >> 24);
+        fl[u] = (uint32_t)fx & 0xFFFFFFu;
         neg[u] = __double_as_longlong(v) < 0;
       }
-      uint8_t *dst = (isa ? asl : bsl) + tc_off(rr, k0, TF_KP, 2);
+      uint8_t *dst = (isa ? asl : bsl) + tc_off(drow, k0, TF_KP, 2);
       const int stride = isa ? Dm::A_SLICE : Dm::B_SLICE;
 #pragma unroll
       for (int i = 0; i < TF_SL; i++) {
         uint32_t w[4];
 #pragma unroll
         for (int u = 0; u < 8; u += 2) {
-          int c0 = (int)((fx[u] >> (56 - TF_BITS * (i + 1))) & 255ULL);
-          int c1 = (int)((fx[u + 1] >> (56 - TF_BITS * (i + 1))) & 255ULL);
-          if (neg[u]) c0 = -c0;
-          if (neg[u + 1]) c1 = -c1;
-          w[u / 2] = (uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(c0)) |
-                     ((uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(c1)) << 16);
+          const uint32_t c0 = i < 4 ? (fh[u] >> (24 - 8 * i)) & 255u : (fl[u] >> (16 - 8 * (i - 4))) & 255u;
+          const uint32_t c1 = i < 4 ? (fh[u + 1] >> (24 - 8 * i)) & 255u : (fl[u + 1] >> (16 - 8 * (i - 4))) & 255u;
+          w[u / 2] = tf_bf16_bits(c0, neg[u]) | (tf_bf16_bits(c1, neg[u + 1]) << 16);
         }
         *(uint4 *)(dst + i * stride) = make_uint4(w[0], w[1], w[2], w[3]);
       }
@@ -391,13 +448,15 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
       break;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    // epilogue: D[r][i] = K[i][r]
-    const bool rok = r_ep < rows;
-    const int sa = rok ? ea[r_ep] : 0;
+    // epilogue: D[m][i] = K[i][function of M row m]
+    const int j_nb = (lane >= Dm::OWNQ && lane < Dm::OWNQ + nbq) ? lq * nbq + lane - Dm::OWNQ : ns_nb;
+    const bool is_own = j_own < NS, is_nb = j_nb < ns_nb;
+    const int sa = (is_own || is_nb) ? ea[r_ep] : 0;
     double *oblk = interior ? val + F.blk : nullptr;
 #pragma unroll
     for (int grp = 0; grp < NPAD / 16; grp++) {
       const int c0 = half * (NPAD / 2) + grp * 8;
+      if (c0 >= NS) continue;  // padding columns only (uniform over the warp)
       float C[TF_SL][8];
 #pragma unroll
       for (int d = 0; d < TF_SL; d++) tc_ld8(tmem + ((uint32_t)(lq * 32) << 16) + d * NPAD + c0, C[d]);
@@ -405,7 +464,7 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
 #pragma unroll
       for (int c = 0; c < 8; c++) {
         const int i = c0 + c;
-        if (!rok || i >= NS) continue;
+        if (!(is_own || is_nb) || i >= NS) continue;
         // sum_d C_d 2^(-8(d+2)) = (hi 2^24 + lo) 2^-64 with hi = C_0..C_3 and
         // lo = C_4..C_6 in base 256 (|hi| < 2^48.01, |lo| < 2^40.01);
         // T = hi 2^14 + lo / 2^10 (< 2^63), so the sum is T 2^-54, with 9
@@ -416,10 +475,10 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
 #pragma unroll
         for (int d = 4; d < TF_SL; d++) lo = lo * 256 + (long long)__float2int_rn(C[d][c]);
         const double v = tf_i64_scaled(hi * 16384LL + (lo >> 10), sa + eb[i] - 54);
-        if (r_ep < NS)
+        if (is_own)
           dacc[grp * 8 + c] += v;
         else
-          oblk[i + (size_t)NS * (r_ep - NS)] = v;
+          oblk[i + (size_t)NS * j_nb] = v;
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -432,12 +491,12 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
     if (tid == 0) atomicExch(err, failed ? 6 : 7);
     return;
   }
-  if (r_ep < NS) {
+  if (j_own < NS) {
     double *dblk = val + boff_diag[e];
 #pragma unroll
     for (int c = 0; c < NPAD / 2; c++) {
       const int i = half * (NPAD / 2) + c;
-      if (i < NS) dblk[i + (size_t)NS * r_ep] += dacc[c];
+      if (i < NS) dblk[i + (size_t)NS * j_own] += dacc[c];
     }
   }
   if (tid < NS) rhs[roff[e] + tid] += racc;
