@@ -24,16 +24,18 @@
 // atomics).  Covers owners of degree <= 3 whose neighbours all have degree
 // <= 3 (2 nq <= 32); the others keep the FP64 face kernel.
 //
-// First the geometry and monomial factors of all the element's faces at
-// once (one thread per face and point, in two passes: first side, whose
-// Jacobian gives the normal, then the second side; the long FP64 chains with
-// their divisions and square roots run side by side).  Then per face: FP64 basis
-// values, row exponents, slicing (all threads); 56 MMAs (M 128, N = NS
-// rounded up to 16, K 16) issued by one thread into 7 accumulators; commit to
-// an mbarrier; epilogue by all warps (tcgen05.ld: warp w reads TMEM lane
-// quarter w % 4 = rows, column half w / 4).  Every wait has an iteration
-// limit: on expiry the CTA records an error, lets its MMAs drain (again with
-// a limit), frees its TMEM and returns.
+// First the geometry of all the element's faces at once (one thread per face
+// and point, in two passes: first side, whose Jacobian gives the normal, then
+// the second side; the long FP64 chains with their divisions and square roots
+// run side by side).  Then per face: monomial factors and per-(b, c) basis
+// products; one fused pass over (row, point) pairs forming the FP64 operand
+// values, each row's exponent (a shuffle max over its 16-lane segment) and
+// the BF16 slices, with no FP64 staging; 56 MMAs (M 128, N = NS rounded up to
+// 16, K 16) issued by one thread into 7 accumulators; commit to an mbarrier;
+// epilogue by the warps whose TMEM lane quarter holds rows (tcgen05.ld: warp
+// w reads lane quarter w % 4, column half w / 4).  Every wait has an
+// iteration limit: on expiry the CTA records an error, lets its MMAs drain
+// (again with a limit), frees its TMEM and returns.
 
 #include "dg_face.cuh"
 #include "gbfem_internal.h"
@@ -52,10 +54,10 @@ constexpr int TF_NQ = 16;         // face points of the largest rule with max(p1
 constexpr int TF_NF = 5;          // faces of a prism
 constexpr int TF_M = 128;         // MMA M
 constexpr int TF_THREADS = 256;
-constexpr int TF_TMEM_COLS = 512;
+constexpr int TF_TMEM_COLS = 256;  // two CTAs per SM share the 512 columns
+constexpr int TF_NCH = 32;         // MMA N per chunk of e's functions: 7 x 32 accumulator columns
 constexpr int TF_GEO = 16;
 constexpr int TF_FAC = 30;
-constexpr int TF_LD = TF_KP + 1;  // FP64 staging row stride (odd: no bank conflicts down a column)
 static_assert((long long)TF_SL * TF_KP * 255 * 255 < (1LL << 24), "slice sums must stay exact in FP32");
 static_assert(TF_NF * (2 * TF_NQ + 1) <= TF_THREADS, "one thread per (face, point, side) and per face");
 
@@ -64,23 +66,29 @@ struct TfDims {
   static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : 40;
   static constexpr int NPAD = (NS + 15) / 16 * 16;  // MMA N
   static constexpr int ROWS = NS + 40;              // own + neighbour (degree <= 3) functions
-  static constexpr int A_SLICE = TF_M * TF_KP * 2;  // bytes per A slice
+  static constexpr int ROWS8 = (ROWS + 7) / 8 * 8;
+  // A slices packed ROWS8 rows apart: the M = 128 rows an MMA reads beyond a
+  // slice's own rows belong to the next slice (or the tail) and only feed D
+  // rows that are discarded
+  static constexpr int A_STRIDE = ROWS8 * TF_KP * 2;
+  static constexpr int A_BYTES = (TF_SL - 1) * A_STRIDE + TF_M * TF_KP * 2;
   static constexpr int B_SLICE = NPAD * TF_KP * 2;
-  static constexpr int OFF_B = TF_SL * A_SLICE;
-  static constexpr int OFF_A64 = OFF_B + TF_SL * B_SLICE;
-  static constexpr int OWNQ = (NS + 3) / 4;          // own functions per TMEM lane quarter
-  static constexpr int OFF_B64 = OFF_A64 + ROWS * TF_LD * 8;
-  static constexpr int OFF_UW = OFF_B64 + NS * TF_LD * 8;
-  static constexpr int OFF_MISC = OFF_UW + TF_NQ * 2 * 16 * 2 * 8;
-  // per face: sX [2][18], sA [2][9], sGeo [TF_NQ][TF_GEO], sFac [TF_NQ][2][TF_FAC], pen, spare
-  static constexpr int FACE_DOUBLES = 36 + 18 + TF_NQ * TF_GEO + 2 * TF_NQ * TF_FAC + 2;
-  static constexpr int OFF_HF = OFF_MISC + TF_NF * FACE_DOUBLES * 8;
+  static constexpr int OFF_B = A_BYTES;
+  static constexpr int OFF_UW = OFF_B + TF_SL * B_SLICE;
+  static constexpr int OFF_FAC = OFF_UW + TF_NQ * 2 * 16 * 2 * 8;          // [TF_NQ][2][TF_FAC]
+  static constexpr int OFF_FACE = OFF_FAC + TF_NQ * 2 * TF_FAC * 8;
+  // per face: X [2][18], A [2][9], G [TF_NQ][TF_GEO], EV [TF_NQ][2][6] (point, v), pen, spare
+  static constexpr int FACE_DOUBLES = 36 + 18 + TF_NQ * TF_GEO + TF_NQ * 2 * 6 + 2;
+  static constexpr int OFF_DIAG = OFF_FACE + TF_NF * FACE_DOUBLES * 8;     // [NS][NS] diagonal-block share
+  static constexpr int OFF_RACC = OFF_DIAG + NS * NS * 8;                  // [NS] boundary rhs sums
+  static constexpr int OFF_HF = OFF_RACC + 64 * 8;
   static constexpr int OFF_INT = (OFF_HF + TF_NF * (int)sizeof(DgHalfFace) + 15) / 16 * 16;  // ea, eb, bar, slot
   static constexpr int SMEM = OFF_INT + (128 + 64) * 4 + 64;
-  static_assert(TF_SL * NPAD <= TF_TMEM_COLS, "accumulators fit the TMEM allocation");
-  static_assert(SMEM <= 227 * 1024, "shared memory");
-  static_assert(OFF_HF % 16 == 0 && OFF_INT % 16 == 0, "alignment");
-  static_assert(OWNQ + 10 <= 32, "own and neighbour rows of a lane quarter");
+  static constexpr int NCHUNK = (NPAD + TF_NCH - 1) / TF_NCH;
+  static_assert(TF_SL * (NPAD < TF_NCH ? NPAD : TF_NCH) <= TF_TMEM_COLS, "accumulators fit the TMEM allocation");
+  static_assert(SMEM <= 113 * 1024, "shared memory of two CTAs per SM");
+  static_assert(OFF_B % 1024 == 0 && OFF_HF % 16 == 0 && OFF_INT % 16 == 0, "alignment");
+  static_assert(ROWS <= TF_M && NS <= 64, "rows");
 };
 
 // biased FP64 exponent field of x (0 for zero / subnormal)
@@ -162,7 +170,7 @@ __device__ __forceinline__ uint32_t tf_bf16_bits(uint32_t mag, bool neg) {
 }
 
 template <int P>
-__global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
+__global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
     const double *__restrict__ k_el, const double *__restrict__ D_el, double pen, double gval,
@@ -172,12 +180,13 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
   constexpr int NS = Dm::NS, NPAD = Dm::NPAD, FD = Dm::FACE_DOUBLES;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *asl = smem, *bsl = smem + Dm::OFF_B;
-  double *A64 = (double *)(smem + Dm::OFF_A64);      // [ROWS][TF_LD]
-  double *B64 = (double *)(smem + Dm::OFF_B64);      // [NS][TF_LD]
   double *sUW = (double *)(smem + Dm::OFF_UW);       // [TF_NQ][2][16][2]: per (b, c) basis products
-  double *sface = (double *)(smem + Dm::OFF_MISC);   // [TF_NF][FD]
+  double *sFac = (double *)(smem + Dm::OFF_FAC);     // [TF_NQ][2][TF_FAC]: the current face's factors
+  double *sface = (double *)(smem + Dm::OFF_FACE);   // [TF_NF][FD]
+  double *sRacc = (double *)(smem + Dm::OFF_RACC);   // [NS]
+  double *sD = (double *)(smem + Dm::OFF_DIAG);      // [NS][NS]: row r (function of the trial side), column i
   DgHalfFace *sHF = (DgHalfFace *)(smem + Dm::OFF_HF);
-  int *ea = (int *)(smem + Dm::OFF_INT);             // A row exponents
+  int *ea = (int *)(smem + Dm::OFF_INT);             // A row exponents (by row = M row)
   int *eb = ea + 128;                                // B row exponents
   uint64_t *bar = (uint64_t *)(eb + 64);
   uint32_t *tmem_slot = (uint32_t *)(bar + 1);
@@ -196,6 +205,8 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (tid < nf) sHF[tid] = hf[h0 + tid];
+  if (tid < NS) sRacc[tid] = 0.0;
+  for (int t = tid; t < NS * NS; t += TF_THREADS) sD[t] = 0.0;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
                  "r"(TF_TMEM_COLS));
@@ -227,8 +238,8 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
   }
   __syncthreads();
   // ---- geometry: phase 1, per (face, point), the first neighbour's side
-  // (point, Jacobian, normal, area weight, v, factors), and the penalty per
-  // face; phase 2 the second neighbour's side and the owner-row scales ----
+  // (point, Jacobian, normal, area weight, v), and the penalty per face;
+  // phase 2 the second neighbour's side and the owner-row scales ----
   if (tid < nf * TF_NQ) {
     const int f = tid / TF_NQ, q = tid % TF_NQ;
     const DgHalfFace &F = sHF[f];
@@ -237,7 +248,7 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
     const int ti = F.nfv == 4 ? 1 : 0;
     const int pr = (interior && tf_nqf[p2][ti] > tf_nqf[p1][ti]) ? p2 : p1;
     if (pr <= 3 && q < tf_nqf[pr][ti]) {
-      double *X = sface + f * FD, *G = X + 54 + q * TF_GEO;
+      double *X = sface + f * FD, *G = X + 54 + q * TF_GEO, *EV = X + 54 + TF_NQ * TF_GEO + q * 12;
       const double *fq = tf_fq[pr - 1][ti][q];
       double w[4];
       tf_weights(F.nfv, fq, w);
@@ -252,7 +263,8 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
       G[13] = n.x;  // the normal, for phase 2 (then overwritten by the scales)
       G[14] = n.y;
       G[15] = n.z;
-      dg_point_factors(e1, v1, X + 54 + TF_NQ * TF_GEO + (2 * q) * TF_FAC);
+      EV[0] = e1.x; EV[1] = e1.y; EV[2] = e1.z;
+      EV[3] = v1.x; EV[4] = v1.y; EV[5] = v1.z;
     }
   } else if (tid >= TF_NF * TF_NQ && tid < TF_NF * TF_NQ + nf) {
     const int f = tid - TF_NF * TF_NQ;
@@ -278,7 +290,7 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
     const int ti = F.nfv == 4 ? 1 : 0;
     const int pr = (interior && tf_nqf[p2][ti] > tf_nqf[p1][ti]) ? p2 : p1;
     if (pr <= 3 && q < tf_nqf[pr][ti]) {
-      double *X = sface + f * FD, *G = X + 54 + q * TF_GEO;
+      double *X = sface + f * FD, *G = X + 54 + q * TF_GEO, *EV = X + 54 + TF_NQ * TF_GEO + q * 12;
       if (interior) {
         double w[4];
         tf_weights(F.nfv, tf_fq[pr - 1][ti][q], w);
@@ -286,7 +298,8 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
         v3 j1, j2, j3;
         prism_jacobian_columns(X + 18, e2, j1, j2, j3);
         const v3 v2 = tf_face_v(j1, j2, j3, X + 45, v3{G[13], G[14], G[15]});
-        dg_point_factors(e2, v2, X + 54 + TF_NQ * TF_GEO + (2 * q + 1) * TF_FAC);
+        EV[6] = e2.x; EV[7] = e2.y; EV[8] = e2.z;
+        EV[9] = v2.x; EV[10] = v2.y; EV[11] = v2.z;
       }
       // owner-row scales: L = (f a) g + (s_o c a) phi, M = -(s_o f a) phi
       const double aw = G[12], so = F.owner_is_2 ? -1.0 : 1.0, fac = interior ? 0.5 : 1.0;
@@ -297,26 +310,17 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
   }
   // (the per-face loop starts with a barrier)
 
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NPAD >> 3) << 17) |
-                         ((uint32_t)(TF_M >> 4) << 24);
-  // Rows of A (and of D) are spread over the four TMEM lane quarters so that
-  // every warp shares the epilogue: in quarter l, lanes [0, OWNQ) hold own
-  // functions l OWNQ + lane, lanes [OWNQ, OWNQ + nbq) the neighbour's
-  // functions l nbq + lane - OWNQ.  The diagonal-block share of own function
-  // j (thread: its lane, column half) stays in that thread's registers.
-  const int lq = warp & 3, half = warp >> 2, lane = tid & 31;
-  const int r_ep = lq * 32 + lane;                                 // TMEM lane = M row
-  const int j_own = lane < Dm::OWNQ ? lq * Dm::OWNQ + lane : NS;  // NS: not an own row
-  double dacc[NPAD / 2];
-#pragma unroll
-  for (int c = 0; c < NPAD / 2; c++) dacc[c] = 0.0;
-  double racc = 0.0;
+  // epilogue threads: warp w reads TMEM lane quarter w % 4 (rows = M rows =
+  // A rows: e's functions 0..NS-1, then the neighbour's) and column half
+  // w / 4 of the current chunk of e's functions
+  const int lq = warp & 3, half = warp >> 2;
+  const int r_ep = lq * 32 + (tid & 31);
   bool failed = false, bad_input = false;
-  int fail_parity = 0;
+  int fail_parity = 0, ncommit = 0;
 
   for (int f = 0; f < nf; f++) {
     const DgHalfFace &F = sHF[f];
-    const double *sGeo = sface + f * FD + 54, *sFac = sGeo + TF_NQ * TF_GEO;
+    const double *sGeo = sface + f * FD + 54, *sEV = sGeo + TF_NQ * TF_GEO;
     const bool interior = F.el2 >= 0;
     const int own2 = F.owner_is_2;
     const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
@@ -331,12 +335,15 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
       bad_input = true;
       break;
     }
-    const int nbq = (ns_nb + 3) / 4;
-    // M row of A row r (own functions first, then the neighbour's)
-    auto mrow = [&](int r) {
-      return r < NS ? (r / Dm::OWNQ) * 32 + r % Dm::OWNQ : ((r - NS) / nbq) * 32 + Dm::OWNQ + (r - NS) % nbq;
-    };
     __syncthreads();  // the previous face's shared arrays are free; the scales are written
+    // monomial factors of this face per (point, side)
+    for (int t = tid; t < 2 * nq; t += TF_THREADS) {
+      const int q = t >> 1, sd = t & 1;
+      if (sd == 1 && !interior) continue;
+      const double *ev = sEV + q * 12 + 6 * sd;
+      dg_point_factors(v3{ev[0], ev[1], ev[2]}, v3{ev[3], ev[4], ev[5]}, sFac + (2 * q + sd) * TF_FAC);
+    }
+    __syncthreads();
     // per (point, side, b, c): U = eta^b zeta^c and W, the (eta, zeta) part of v . grad
     for (int t = tid; t < nq * 2 * 16; t += TF_THREADS) {
       const int q = t >> 5, sd = (t >> 4) & 1, bc = t & 15, b = bc >> 2, c = bc & 3;
@@ -347,141 +354,149 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
       uw[1] = fma(T[5 + b], T[25 + c], T[20 + b] * T[10 + c]);
     }
     __syncthreads();
-    // FP64 operands, per (row, point): A rows = e's functions then the
-    // neighbour's (k = 2q: Phi, 2q + 1: Gam), B rows = e's functions (L, M);
-    // phi = xi^a U, g = v_xi a xi^(a-1) U + xi^a W (the operations of
-    // dg_basis_from_factors); the K padding is zeroed when slicing
-    for (int t = tid; t < rows * nq; t += TF_THREADS) {
-      const int r = t / nq, q = t - r * nq;
-      const bool own = r < NS;
-      const int side = own ? own_side : 3 - own_side, jj = own ? r : r - NS, p = own ? P : pnb;
-      const unsigned char *ex = tf_exp[p - 1][jj];
-      const double *T = sFac + (2 * q + side - 1) * TF_FAC;
-      const double *uw = sUW + ((q * 2 + side - 1) * 16 + ex[1] * 4 + ex[2]) * 2;
-      const double phi = T[ex[0]] * uw[0];
-      const double g = fma(T[15 + ex[0]], uw[0], T[ex[0]] * uw[1]);
-      // Phi = s_t phi: the sign flip on the integer side
-      A64[r * TF_LD + 2 * q] = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
-      A64[r * TF_LD + 2 * q + 1] = g;
-      if (own) {
-        const double *G = sGeo + q * TF_GEO;
-        B64[r * TF_LD + 2 * q] = fma(G[13], g, G[14] * phi);
-        B64[r * TF_LD + 2 * q + 1] = G[15] * phi;
-      }
-    }
-    __syncthreads();
-    if (!interior && tid < NS) {
-      double s = 0.0;
-      for (int q = 0; q < nq; q++) s += B64[tid * TF_LD + 2 * q];
-      racc = fma(gval, s, racc);
-    }
-    // row exponents (integer max of the exponent fields): threads
-    // 0..rows-1 for A (stored by M row), 128..128+NS-1 for B
-    if (tid < rows || (tid >= 128 && tid < 128 + NS)) {
-      const double *row = tid < 128 ? A64 + tid * TF_LD : B64 + (tid - 128) * TF_LD;
-      int emax = 0;
-      for (int k = 0; k < 2 * nq; k++) emax = max(emax, tf_biased_exp(row[k]));
-      if (tid < 128)
-        ea[mrow(tid)] = tf_row_exp(emax);
-      else
-        eb[tid - 128] = tf_row_exp(emax);
-    }
-    __syncthreads();
-    // slices: one thread per (row, 8 consecutive k), one 16-byte store per
-    // slice (a core-matrix row of the canonical K-major layout); M rows of A
-    // holding no function and rows of B beyond NS are never written: their D
-    // rows and columns are discarded
-    for (int t = tid; t < (rows + NS) * (TF_KP / 8); t += TF_THREADS) {
-      const int r = t / (TF_KP / 8), k0 = (t % (TF_KP / 8)) * 8;
-      const bool isa = r < rows;
-      const int rr = isa ? r : r - rows;
-      const int drow = isa ? mrow(rr) : rr;
-      const double *src = isa ? A64 + rr * TF_LD : B64 + rr * TF_LD;
-      const int ex = isa ? ea[drow] : eb[rr];
-      uint32_t fh[8], fl[8];  // fixed-point bits 55..24 and 23..0
-      bool neg[8];
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const double v = k0 + u < 2 * nq ? src[k0 + u] : 0.0;
-        const unsigned long long fx = tf_fixed(v, ex);
-        fh[u] = (uint32_t)(fx >> 24);
-        fl[u] = (uint32_t)fx & 0xFFFFFFu;
-        neg[u] = __double_as_longlong(v) < 0;
-      }
-      uint8_t *dst = (isa ? asl : bsl) + tc_off(drow, k0, TF_KP, 2);
-      const int stride = isa ? Dm::A_SLICE : Dm::B_SLICE;
-#pragma unroll
-      for (int i = 0; i < TF_SL; i++) {
-        uint32_t w[4];
-#pragma unroll
-        for (int u = 0; u < 8; u += 2) {
-          const uint32_t c0 = i < 4 ? (fh[u] >> (24 - 8 * i)) & 255u : (fl[u] >> (16 - 8 * (i - 4))) & 255u;
-          const uint32_t c1 = i < 4 ? (fh[u + 1] >> (24 - 8 * i)) & 255u : (fl[u + 1] >> (16 - 8 * (i - 4))) & 255u;
-          w[u / 2] = tf_bf16_bits(c0, neg[u]) | (tf_bf16_bits(c1, neg[u + 1]) << 16);
+    // operands in one pass, a 16-lane segment per row r and a lane per point
+    // q (k = 2q: Phi / L, 2q + 1: Gam / M; lanes q >= nq give the K
+    // padding): FP64 values (phi = xi^a U, g = v_xi a xi^(a-1) U + xi^a W,
+    // the operations of dg_basis_from_factors), the row exponent by a
+    // segment max of the exponent fields, then the seven BF16 slices of the
+    // pair as one 32-bit word each.  A rows: e's functions then the
+    // neighbour's; B rows: e's functions.
+    for (int base = 0; base < rows * 16; base += TF_THREADS) {
+      const int t = base + tid, r = t >> 4, q = t & 15;
+      const bool live = r < rows, own = r < NS;  // uniform over the segment
+      double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
+      if (live && q < nq) {
+        const int side = own ? own_side : 3 - own_side, jj = own ? r : r - NS, p = own ? P : pnb;
+        const unsigned char *ex = tf_exp[p - 1][jj];
+        const double *T = sFac + (2 * q + side - 1) * TF_FAC;
+        const double *uw = sUW + ((q * 2 + side - 1) * 16 + ex[1] * 4 + ex[2]) * 2;
+        const double phi = T[ex[0]] * uw[0];
+        const double g = fma(T[15 + ex[0]], uw[0], T[ex[0]] * uw[1]);
+        // Phi = s_t phi: the sign flip on the integer side
+        a0 = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
+        a1 = g;
+        if (own) {
+          const double *G = sGeo + q * TF_GEO;
+          b0 = fma(G[13], g, G[14] * phi);
+          b1 = G[15] * phi;
         }
-        *(uint4 *)(dst + i * stride) = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+      int xa = max(tf_biased_exp(a0), tf_biased_exp(a1)), xb = max(tf_biased_exp(b0), tf_biased_exp(b1));
+#pragma unroll
+      for (int o = 8; o >= 1; o >>= 1) {
+        xa = max(xa, __shfl_xor_sync(0xffffffffu, xa, o));
+        xb = max(xb, __shfl_xor_sync(0xffffffffu, xb, o));
+      }
+      if (!interior) {  // boundary face: the rhs of row r gets g sum_q L (uniform over the CTA)
+        double sl = b0;
+#pragma unroll
+        for (int o = 8; o >= 1; o >>= 1) sl += __shfl_xor_sync(0xffffffffu, sl, o);
+        if (live && own && q == 0) sRacc[r] = fma(gval, sl, sRacc[r]);
+      }
+      if (live) {
+        const int EA = tf_row_exp(xa), EB = tf_row_exp(xb);
+        if (q == 0) {
+          ea[r] = EA;
+          if (own) eb[r] = EB;
+        }
+        const int off = tc_off(r, 2 * q, TF_KP, 2);
+        {
+          const unsigned long long f0 = tf_fixed(a0, EA), f1 = tf_fixed(a1, EA);
+          const uint32_t h0 = (uint32_t)(f0 >> 24), l0 = (uint32_t)f0 & 0xFFFFFFu;
+          const uint32_t h1 = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
+          const bool n0 = __double_as_longlong(a0) < 0, n1 = __double_as_longlong(a1) < 0;
+#pragma unroll
+          for (int i = 0; i < TF_SL; i++) {
+            const uint32_t c0 = i < 4 ? (h0 >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
+            const uint32_t c1 = i < 4 ? (h1 >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
+            *(uint32_t *)(asl + i * Dm::A_STRIDE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
+          }
+        }
+        if (own) {
+          const unsigned long long f0 = tf_fixed(b0, EB), f1 = tf_fixed(b1, EB);
+          const uint32_t h0 = (uint32_t)(f0 >> 24), l0 = (uint32_t)f0 & 0xFFFFFFu;
+          const uint32_t h1 = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
+          const bool n0 = __double_as_longlong(b0) < 0, n1 = __double_as_longlong(b1) < 0;
+#pragma unroll
+          for (int i = 0; i < TF_SL; i++) {
+            const uint32_t c0 = i < 4 ? (h0 >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
+            const uint32_t c1 = i < 4 ? (h1 >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
+            *(uint32_t *)(bsl + i * Dm::B_SLICE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
+          }
+        }
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a0 = tc_smem(asl), b0 = tc_smem(bsl);
-      for (int i = 0; i < TF_SL; i++)
-        for (int j = 0; j < TF_SL - i; j++) {
-          const int d = i + j;
+    // per chunk of e's functions (N = TF_NCH columns at most): MMAs, commit,
+    // wait, epilogue; the accumulators are reused chunk after chunk
+    for (int ch = 0; ch < Dm::NCHUNK; ch++) {
+      const int clo = ch * TF_NCH, cn = NPAD - clo < TF_NCH ? NPAD - clo : TF_NCH;
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(cn >> 3) << 17) |
+                               ((uint32_t)(TF_M >> 4) << 24);
+        const uint32_t a0 = tc_smem(asl), b0 = tc_smem(bsl) + (clo / 8) * (TF_KP / 8) * 128;
+        for (int i = 0; i < TF_SL; i++)
+          for (int j = 0; j < TF_SL - i; j++) {
+            const int d = i + j;
 #pragma unroll
-          for (int ks = 0; ks < TF_KP / 16; ks++) {
-            const uint64_t ad = tc_desc(a0 + i * Dm::A_SLICE + ks * 256, 128, (TF_KP / 8) * 128);
-            const uint64_t bd = tc_desc(b0 + j * Dm::B_SLICE + ks * 256, 128, (TF_KP / 8) * 128);
-            tc_mma<0>(tmem + d * NPAD, ad, bd, idesc, (i == 0 && ks == 0) ? 0u : 1u);
+            for (int ks = 0; ks < TF_KP / 16; ks++) {
+              const uint64_t ad = tc_desc(a0 + i * Dm::A_STRIDE + ks * 256, 128, (TF_KP / 8) * 128);
+              const uint64_t bd = tc_desc(b0 + j * Dm::B_SLICE + ks * 256, 128, (TF_KP / 8) * 128);
+              tc_mma<0>(tmem + d * cn, ad, bd, idesc, (i == 0 && ks == 0) ? 0u : 1u);
+            }
+          }
+        tc_commit(tc_smem(bar));
+      }
+      __syncthreads();
+      const bool waited = tc_wait(tc_smem(bar), ncommit & 1);
+      if (__syncthreads_or(!waited)) {
+        failed = true;
+        fail_parity = ncommit & 1;
+        break;
+      }
+      ncommit++;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // epilogue: D[r][i] = K[i][function r] (warps whose lane quarter holds
+      // no row skip it as a whole)
+      if (lq * 32 < rows) {
+        const bool rok = r_ep < rows;
+        const int sa = rok ? ea[r_ep] : 0;
+        double *oblk = interior ? val + F.blk : nullptr;
+        for (int grp = 0; grp < cn / 16; grp++) {
+          const int cl = half * (cn / 2) + grp * 8;  // column within the chunk
+          if (clo + cl >= NS) continue;              // padding columns only (uniform over the warp)
+          float C[TF_SL][8];
+#pragma unroll
+          for (int d = 0; d < TF_SL; d++) tc_ld8(tmem + ((uint32_t)(lq * 32) << 16) + d * cn + cl, C[d]);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            const int i = clo + cl + c;
+            if (!rok || i >= NS) continue;
+            // sum_d C_d 2^(-8(d+2)) = (hi 2^24 + lo) 2^-64 with hi = C_0..C_3
+            // and lo = C_4..C_6 in base 256 (|hi| < 2^48.01, |lo| <
+            // 2^40.01); T = hi 2^14 + lo / 2^10 (< 2^63), so the sum is
+            // T 2^-54, with 9 bits beyond the 53 the double rounds to
+            long long hi = 0, lo = 0;
+#pragma unroll
+            for (int d = 0; d < 4; d++) hi = hi * 256 + (long long)__float2int_rn(C[d][c]);
+#pragma unroll
+            for (int d = 4; d < TF_SL; d++) lo = lo * 256 + (long long)__float2int_rn(C[d][c]);
+            const double v = tf_i64_scaled(hi * 16384LL + (lo >> 10), sa + eb[i] - 54);
+            if (r_ep < NS)
+              sD[r_ep * NS + i] += v;
+            else
+              oblk[i + (size_t)NS * (r_ep - NS)] = v;
           }
         }
-      tc_commit(tc_smem(bar));
-    }
-    __syncthreads();
-    const bool waited = tc_wait(tc_smem(bar), f & 1);
-    if (__syncthreads_or(!waited)) {
-      failed = true;
-      fail_parity = f & 1;
-      break;
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    // epilogue: D[m][i] = K[i][function of M row m]
-    const int j_nb = (lane >= Dm::OWNQ && lane < Dm::OWNQ + nbq) ? lq * nbq + lane - Dm::OWNQ : ns_nb;
-    const bool is_own = j_own < NS, is_nb = j_nb < ns_nb;
-    const int sa = (is_own || is_nb) ? ea[r_ep] : 0;
-    double *oblk = interior ? val + F.blk : nullptr;
-#pragma unroll
-    for (int grp = 0; grp < NPAD / 16; grp++) {
-      const int c0 = half * (NPAD / 2) + grp * 8;
-      if (c0 >= NS) continue;  // padding columns only (uniform over the warp)
-      float C[TF_SL][8];
-#pragma unroll
-      for (int d = 0; d < TF_SL; d++) tc_ld8(tmem + ((uint32_t)(lq * 32) << 16) + d * NPAD + c0, C[d]);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-      for (int c = 0; c < 8; c++) {
-        const int i = c0 + c;
-        if (!(is_own || is_nb) || i >= NS) continue;
-        // sum_d C_d 2^(-8(d+2)) = (hi 2^24 + lo) 2^-64 with hi = C_0..C_3 and
-        // lo = C_4..C_6 in base 256 (|hi| < 2^48.01, |lo| < 2^40.01);
-        // T = hi 2^14 + lo / 2^10 (< 2^63), so the sum is T 2^-54, with 9
-        // bits beyond the 53 the double rounds to
-        long long hi = 0, lo = 0;
-#pragma unroll
-        for (int d = 0; d < 4; d++) hi = hi * 256 + (long long)__float2int_rn(C[d][c]);
-#pragma unroll
-        for (int d = 4; d < TF_SL; d++) lo = lo * 256 + (long long)__float2int_rn(C[d][c]);
-        const double v = tf_i64_scaled(hi * 16384LL + (lo >> 10), sa + eb[i] - 54);
-        if (is_own)
-          dacc[grp * 8 + c] += v;
-        else
-          oblk[i + (size_t)NS * j_nb] = v;
       }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();  // TMEM read before the next chunk's MMAs overwrite it
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    if (failed) break;
   }
   if (failed) tc_wait(tc_smem(bar), fail_parity);  // let the issued MMAs drain (bounded) before freeing TMEM
   __syncthreads();
@@ -491,15 +506,12 @@ __global__ void __launch_bounds__(TF_THREADS, 1) dg_tc_faces_kernel(
     if (tid == 0) atomicExch(err, failed ? 6 : 7);
     return;
   }
-  if (j_own < NS) {
+  {
+    // the diagonal block is column-major (entry (i, r) at i + NS r): sD's layout
     double *dblk = val + boff_diag[e];
-#pragma unroll
-    for (int c = 0; c < NPAD / 2; c++) {
-      const int i = half * (NPAD / 2) + c;
-      if (i < NS) dblk[i + (size_t)NS * j_own] += dacc[c];
-    }
+    for (int t = tid; t < NS * NS; t += TF_THREADS) dblk[t] += sD[t];
   }
-  if (tid < NS) rhs[roff[e] + tid] += racc;
+  if (tid < NS) rhs[roff[e] + tid] += sRacc[tid];
 }
 
 bool dg_tc_faces_supported(int p) { return p >= 1 && p <= 3; }
