@@ -288,7 +288,20 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
         tot_tf, vol_tf, _ = tt / steps
         vtf, _ = c.dg_get_matrix()
         tf_dev = float(np.max(np.abs(vtf - v64)) / np.max(np.abs(v64)))
-        del v64, vtf
+        del vtf
+        # the whole assembly on the tensor cores: split-BF16 volume and faces
+        c.dg_set_volume_kernel(gb.DG_VOLUME_TC)
+        c.dg_set_face_kernel(gb.DG_FACE_TC)
+        c.dg_assemble()
+        tt = np.zeros(3)
+        for _ in range(steps):
+            c.dg_assemble()
+            tt += np.array(c.dg_last_timing()[:3])
+        tot_ta, vol_ta, fa_ta = tt / steps
+        vta, _ = c.dg_get_matrix()
+        ta_dev = float(np.max(np.abs(vta - v64)) / np.max(np.abs(v64)))
+        del v64, vta
+        c.dg_set_face_kernel(gb.DG_FACE_FP64)
         c.dg_set_volume_kernel(gb.DG_VOLUME_FP64)
         vfma = sum(dg_fma_per_element(p) * int(np.sum(pdeg == p)) for p in range(1, 5))
         ffma = dg_face_fma(F, pdeg)
@@ -309,6 +322,11 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
             "tensor_core_volume": {"volume_ms": vol_tc, "assemble_ms": tot_tc, "elem_per_s": m.nel / (tot_tc * 1e-3),
                                    "max_abs_diff_vs_fp64_rel_to_max": tc_dev,
                                    "note": "tcgen05 split-BF16 products (p <= 3; p = 4 stays FP64)"},
+            "tensor_core_assembly": {"volume_ms": vol_ta, "face_ms": fa_ta, "assemble_ms": tot_ta,
+                                     "elem_per_s": m.nel / (tot_ta * 1e-3), "speedup_vs_fp64": tot / tot_ta,
+                                     "max_abs_diff_vs_fp64_rel_to_max": ta_dev,
+                                     "note": "tcgen05 split-BF16 volume and faces (owners and neighbours p <= 3; "
+                                             "others stay FP64)"},
             "tf32_volume": {"volume_ms": vol_tf, "assemble_ms": tot_tf, "elem_per_s": m.nel / (tot_tf * 1e-3),
                             "max_abs_diff_vs_fp64_rel_to_max": tf_dev,
                             "note": "tcgen05 kind::tf32, hi/lo operands, FP32 accumulation (p <= 3)"},
@@ -420,6 +438,45 @@ def bench_batch(gb, local, steps, fp64_peak):
                     "download of "
                     f"{out_bytes / 1e9:.2f} GB of blocks",
     }
+
+
+def mixed_precision_solution_check(gb, local, n=10):
+    """Config-4 form at a size GMRES(50) converges on: p = 3 prisms, the
+    anisotropic tensor, assembled by the tensor-core kernels and solved by
+    FP64 iterative refinement around FP32 GMRES to 1e-10, against the plain
+    FP64 assembly solved by FP64 GMRES to 1e-13: relative solution error."""
+    from modfem_gb300.mesh import anisotropic_tensors, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(n, jitter=0.2, seed=SEED)
+    F = prism_faces(m)
+    out = {"elements": m.nel}
+    xs = []
+    for mode in ("fp64", "mixed"):
+        c = gb.Context(local)
+        c.set_mesh(m)
+        c.set_coefficients(D=anisotropic_tensors(m.nel, seed=SEED), f=1.0, g=0.0)
+        c.dg_set_degrees(np.full(m.nel, 3))
+        c.dg_set_faces(F, penalty=10.0)
+        c.dg_build_structure()
+        if mode == "mixed":
+            c.dg_set_volume_kernel(gb.DG_VOLUME_TC)
+            c.dg_set_face_kernel(gb.DG_FACE_TC)
+        c.dg_assemble()
+        if mode == "fp64":
+            x, it, _, rel = c.dg_solve(krylov=50, max_iter=200000, tol_rel=1e-13)
+            out["fp64_gmres_iterations"], out["fp64_rel_residual"] = it, rel
+        else:
+            for tol in (1e-10, 1e-12):
+                x, it, outer, rel = c.dg_solve_ir(krylov=50, max_iter=200000, tol_rel=tol, inner_tol=1e-4)
+                out[f"ir_{tol:g}"] = {"inner_iterations": it, "refinements": outer, "true_rel_residual": rel,
+                                      "solve_ms": c.last_solve_timing()[0],
+                                      "rel_solution_error_vs_fp64": float(np.linalg.norm(x - xs[0]) /
+                                                                          np.linalg.norm(xs[0]))}
+            c.close()
+            continue
+        out[mode + "_solve_ms"] = c.last_solve_timing()[0]
+        xs.append(np.array(x))
+        c.close()
+    return out
 
 
 def bench_serving(gb, local, rates=(50, 200, 1000, 2000), per_rate=48):
@@ -626,6 +683,7 @@ def main():
     # ---------------- DG prism system ----------------
     dg = bench_dg(gb, local, max(3, min(args.steps, 10)), fp64_peak)
     batch = bench_batch(gb, local, max(3, min(args.steps, 10)), fp64_peak)
+    dg["mixed_precision_solution"] = mixed_precision_solution_check(gb, local)
 
     # ---------------- serving ----------------
     serving = bench_serving(gb, local) if rank == 0 else None

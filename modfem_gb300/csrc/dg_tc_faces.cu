@@ -56,8 +56,13 @@ constexpr int TF_M = 128;         // MMA M
 constexpr int TF_THREADS = 256;
 constexpr int TF_TMEM_COLS = 256;  // two CTAs per SM share the 512 columns
 constexpr int TF_NCH = 32;         // MMA N per chunk of e's functions: 7 x 32 accumulator columns
-constexpr int TF_GEO = 16;
-constexpr int TF_FAC = 30;
+// per-point table strides in doubles, odd so that the 16 lanes of a row
+// segment (one per point) fall on different shared-memory banks
+constexpr int TF_GEO = 17;   // 13 geometry values + 3 owner-row scales, padded
+constexpr int TF_FAC = 30;   // monomial factors per point and side
+constexpr int TF_FACS = 31;  // their stride
+constexpr int TF_UWS = 33;   // 16 (b, c) x 2 basis products per point and side, padded
+static_assert(TF_FACS > TF_FAC && TF_UWS > 32 && TF_GEO > 16, "padded strides hold their tables");
 static_assert((long long)TF_SL * TF_KP * 255 * 255 < (1LL << 24), "slice sums must stay exact in FP32");
 static_assert(TF_NF * (2 * TF_NQ + 1) <= TF_THREADS, "one thread per (face, point, side) and per face");
 
@@ -75,12 +80,13 @@ struct TfDims {
   static constexpr int B_SLICE = NPAD * TF_KP * 2;
   static constexpr int OFF_B = A_BYTES;
   static constexpr int OFF_UW = OFF_B + TF_SL * B_SLICE;
-  static constexpr int OFF_FAC = OFF_UW + TF_NQ * 2 * 16 * 2 * 8;          // [TF_NQ][2][TF_FAC]
-  static constexpr int OFF_FACE = OFF_FAC + TF_NQ * 2 * TF_FAC * 8;
+  static constexpr int OFF_FAC = OFF_UW + TF_NQ * 2 * TF_UWS * 8;          // [TF_NQ][2][TF_FACS]
+  static constexpr int OFF_FACE = OFF_FAC + TF_NQ * 2 * TF_FACS * 8;
   // per face: X [2][18], A [2][9], G [TF_NQ][TF_GEO], EV [TF_NQ][2][6] (point, v), pen, spare
   static constexpr int FACE_DOUBLES = 36 + 18 + TF_NQ * TF_GEO + TF_NQ * 2 * 6 + 2;
-  static constexpr int OFF_DIAG = OFF_FACE + TF_NF * FACE_DOUBLES * 8;     // [NS][NS] diagonal-block share
-  static constexpr int OFF_RACC = OFF_DIAG + NS * NS * 8;                  // [NS] boundary rhs sums
+  static constexpr int OFF_DIAG = OFF_FACE + TF_NF * FACE_DOUBLES * 8;     // [NS][SD_LD] diagonal-block share
+  static constexpr int SD_LD = NS + 1;                                     // odd row stride
+  static constexpr int OFF_RACC = OFF_DIAG + NS * SD_LD * 8;               // [NS] boundary rhs sums
   static constexpr int OFF_HF = OFF_RACC + 64 * 8;
   static constexpr int OFF_INT = (OFF_HF + TF_NF * (int)sizeof(DgHalfFace) + 15) / 16 * 16;  // ea, eb, bar, slot
   static constexpr int SMEM = OFF_INT + (128 + 64) * 4 + 64;
@@ -180,11 +186,11 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
   constexpr int NS = Dm::NS, NPAD = Dm::NPAD, FD = Dm::FACE_DOUBLES;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *asl = smem, *bsl = smem + Dm::OFF_B;
-  double *sUW = (double *)(smem + Dm::OFF_UW);       // [TF_NQ][2][16][2]: per (b, c) basis products
-  double *sFac = (double *)(smem + Dm::OFF_FAC);     // [TF_NQ][2][TF_FAC]: the current face's factors
+  double *sUW = (double *)(smem + Dm::OFF_UW);       // [TF_NQ][2][TF_UWS]: per (b, c) basis products
+  double *sFac = (double *)(smem + Dm::OFF_FAC);     // [TF_NQ][2][TF_FACS]: the current face's factors
   double *sface = (double *)(smem + Dm::OFF_FACE);   // [TF_NF][FD]
   double *sRacc = (double *)(smem + Dm::OFF_RACC);   // [NS]
-  double *sD = (double *)(smem + Dm::OFF_DIAG);      // [NS][NS]: row r (function of the trial side), column i
+  double *sD = (double *)(smem + Dm::OFF_DIAG);      // [NS][SD_LD]: row r (trial function), column i
   DgHalfFace *sHF = (DgHalfFace *)(smem + Dm::OFF_HF);
   int *ea = (int *)(smem + Dm::OFF_INT);             // A row exponents (by row = M row)
   int *eb = ea + 128;                                // B row exponents
@@ -206,7 +212,7 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
   }
   if (tid < nf) sHF[tid] = hf[h0 + tid];
   if (tid < NS) sRacc[tid] = 0.0;
-  for (int t = tid; t < NS * NS; t += TF_THREADS) sD[t] = 0.0;
+  for (int t = tid; t < NS * Dm::SD_LD; t += TF_THREADS) sD[t] = 0.0;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
                  "r"(TF_TMEM_COLS));
@@ -341,15 +347,15 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
       const int q = t >> 1, sd = t & 1;
       if (sd == 1 && !interior) continue;
       const double *ev = sEV + q * 12 + 6 * sd;
-      dg_point_factors(v3{ev[0], ev[1], ev[2]}, v3{ev[3], ev[4], ev[5]}, sFac + (2 * q + sd) * TF_FAC);
+      dg_point_factors(v3{ev[0], ev[1], ev[2]}, v3{ev[3], ev[4], ev[5]}, sFac + (2 * q + sd) * TF_FACS);
     }
     __syncthreads();
     // per (point, side, b, c): U = eta^b zeta^c and W, the (eta, zeta) part of v . grad
     for (int t = tid; t < nq * 2 * 16; t += TF_THREADS) {
       const int q = t >> 5, sd = (t >> 4) & 1, bc = t & 15, b = bc >> 2, c = bc & 3;
       if (sd == 1 && !interior) continue;
-      const double *T = sFac + (2 * q + sd) * TF_FAC;
-      double *uw = sUW + ((q * 2 + sd) * 16 + bc) * 2;
+      const double *T = sFac + (2 * q + sd) * TF_FACS;
+      double *uw = sUW + (q * 2 + sd) * TF_UWS + bc * 2;
       uw[0] = T[5 + b] * T[10 + c];
       uw[1] = fma(T[5 + b], T[25 + c], T[20 + b] * T[10 + c]);
     }
@@ -368,8 +374,8 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
       if (live && q < nq) {
         const int side = own ? own_side : 3 - own_side, jj = own ? r : r - NS, p = own ? P : pnb;
         const unsigned char *ex = tf_exp[p - 1][jj];
-        const double *T = sFac + (2 * q + side - 1) * TF_FAC;
-        const double *uw = sUW + ((q * 2 + side - 1) * 16 + ex[1] * 4 + ex[2]) * 2;
+        const double *T = sFac + (2 * q + side - 1) * TF_FACS;
+        const double *uw = sUW + (q * 2 + side - 1) * TF_UWS + (ex[1] * 4 + ex[2]) * 2;
         const double phi = T[ex[0]] * uw[0];
         const double g = fma(T[15 + ex[0]], uw[0], T[ex[0]] * uw[1]);
         // Phi = s_t phi: the sign flip on the integer side
@@ -487,7 +493,7 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
             for (int d = 4; d < TF_SL; d++) lo = lo * 256 + (long long)__float2int_rn(C[d][c]);
             const double v = tf_i64_scaled(hi * 16384LL + (lo >> 10), sa + eb[i] - 54);
             if (r_ep < NS)
-              sD[r_ep * NS + i] += v;
+              sD[r_ep * Dm::SD_LD + i] += v;
             else
               oblk[i + (size_t)NS * (r_ep - NS)] = v;
           }
@@ -507,9 +513,9 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
     return;
   }
   {
-    // the diagonal block is column-major (entry (i, r) at i + NS r): sD's layout
+    // the diagonal block is column-major (entry (i, r) at i + NS r): sD's row r
     double *dblk = val + boff_diag[e];
-    for (int t = tid; t < NS * NS; t += TF_THREADS) dblk[t] += sD[t];
+    for (int t = tid; t < NS * NS; t += TF_THREADS) dblk[t] += sD[(t / NS) * Dm::SD_LD + t % NS];
   }
   if (tid < NS) rhs[roff[e] + tid] += sRacc[tid];
 }
