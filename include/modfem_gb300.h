@@ -100,7 +100,10 @@ int gbfem_build_structure(gbfem_ctx ctx, int *ndof, long long *nnz, int *nr_colo
 /* The same structure built on the device (first-appearance ranks by an
  * atomicMin and a scan, incidence lists, per-row sorted unique columns,
  * binary-searched tables): identical arrays, no host pass over the mesh.
- * Makes no colouring, so gbfem_assemble then takes GBFEM_SCATTER_ATOMIC. */
+ * Also colours the elements on the device (Jones-Plassmann with hashed
+ * priorities: deterministic, more colours than the host's first-fit walk)
+ * and the boundary faces on the host, so both scatter modes of
+ * gbfem_assemble work; the colour-batched one sums in a fixed order. */
 int gbfem_build_structure_device(gbfem_ctx ctx, int *ndof, long long *nnz);
 /* Copies the structure out (any pointer may be NULL). */
 int gbfem_get_crs_structure(gbfem_ctx ctx, int *dof_of_node, int *row_ptr, int *col_ind);
@@ -376,12 +379,16 @@ int gbfem_batch_get(gbfem_batch batch, double *vals, double *rhs);
 /* serving (no counterpart in the reference)                                */
 /* ---------------------------------------------------------------------- */
 /* A server takes independent heat problems as they arrive and integrates,
- * assembles and solves them on one GPU with continuous batching: requests
- * are admitted FIFO while a slot is free and their device footprint fits in
- * the HBM budget; worker threads upload, build, integrate and assemble each
- * admitted request on its own stream while the engine thread advances all
- * requests in the solve phase together, one GMRES iteration per step with
- * batched kernels and the GMRES scalar logic on the device.  A request's
+ * assembles and solves them on one GPU with continuous batching.  std and DG
+ * requests run in two lanes, each with its own FIFO queue, half of the
+ * max_active slots (more while the other lane has nobody waiting), CUDA
+ * stream and step graph, so std requests neither wait for DG requests'
+ * solves nor queue behind them; a request is admitted when its lane has a
+ * slot and its device footprint fits in the shared HBM budget.  Worker
+ * threads upload, build, integrate and assemble each admitted request on its
+ * own stream while the engine thread advances each lane's requests in the
+ * solve phase together, one GMRES iteration per step with batched kernels
+ * and the GMRES scalar logic on the device.  A request's
  * result does not depend on the other requests in the mix (bit-identical
  * alone and together).  The numerics per request are those of
  * gbfem_assemble + gbfem_solve (std) and gbfem_dg_assemble + gbfem_dg_solve

@@ -282,7 +282,8 @@ int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
   int nd = 0;
   long long nz = 0;
   GB_TRY(gbfem::build_device_structure(c->stream, c->nno, c->nel, c->nv, c->el_nodes.p, c->dof_of_node, c->row_ptr,
-                                       c->col_ind, c->el_table, c->err.p, &nd, &nz));
+                                       c->col_ind, c->el_table, c->err.p, &nd, &nz, &c->el_perm,
+                                       &c->h_el_color_ptr));
   c->ndof = nd;
   c->nnz = nz;
   // host copies for the getters; no colouring (atomic scatter only)
@@ -299,8 +300,18 @@ int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
                           c->stream));
   GB_CUDA(cudaMemcpyAsync(c->hs.el_table.data(), c->el_table.p, c->el_table.n * sizeof(int), cudaMemcpyDeviceToHost,
                           c->stream));
-  c->h_el_color_ptr.clear();
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  // boundary faces (few): first-fit colouring on the host over the dofs of
+  // their elements, as the host build does
   c->h_fa_color_ptr.clear();
+  if (c->nfa > 0) {
+    std::vector<int> fa_dofs((size_t)c->nfa * c->nv), perm;
+    for (int f = 0; f < c->nfa; f++)
+      for (int j = 0; j < c->nv; j++)
+        fa_dofs[(size_t)f * c->nv + j] = c->hs.dof_of_node[c->h_el_nodes[(size_t)c->h_fa_el[f] * c->nv + j]];
+    gbfem::color_entities(c->nfa, c->nv, fa_dofs, nd, c->h_fa_color_ptr, perm);
+    GB_TRY(upload(c, c->fa_perm, perm.data(), perm.size()));
+  }
   GB_TRY(alloc_matrix(c));
   c->have_structure = c->have_tables = true;
   GB_CUDA(cudaStreamSynchronize(c->stream));

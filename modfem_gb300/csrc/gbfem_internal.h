@@ -81,9 +81,12 @@ struct HostStructure {
 
 int build_host_structure(int nno, int nel, int nv, const int *el_nodes, int nfa, const int *fa_el,
                          const int *fa_side, HostStructure &hs);
+// el_perm / el_color_ptr (may be null): a deterministic element colouring
+// for the colour-batched scatter
 int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int *el_nodes, DevBuf<int> &dof_of_node,
                            DevBuf<int> &row_ptr, DevBuf<int> &col_ind, DevBuf<int> &el_table, int *err,
-                           int *ndof_out, long long *nnz_out);
+                           int *ndof_out, long long *nnz_out, DevBuf<int> *el_perm = nullptr,
+                           std::vector<int> *el_color_ptr = nullptr);
 void color_entities(int nent, int nv, const std::vector<int> &ent_dofs, int nd, std::vector<int> &color_ptr,
                     std::vector<int> &perm);
 

@@ -5,16 +5,22 @@
 // (gbfem_assemble / gbfem_dg_assemble, GMRES with Jacobi / block Jacobi).
 //
 // Pipeline:
-//  * admission: FIFO; a request starts when a slot is free and its estimated
-//    device footprint fits in the HBM budget (replaced by the measured
-//    footprint once it is built);
-//  * preparation (worker threads, one CUDA stream each): upload, structure,
-//    integrate + assemble, preconditioner; overlaps with the solves running;
-//  * solve (engine thread, one stream): every engine step advances every
-//    active request by one GMRES iteration with batched kernels over all of
-//    them - one CRS SpMV launch for all std requests, one launch per degree
-//    class for each DG request, and one launch each for the Gram-Schmidt dot
-//    products, updates and norms of all requests.  The scalar GMRES logic
+//  * two lanes, std and DG requests, each with its own FIFO admission queue,
+//    slot quota, CUDA stream, step graph and state readback, polled
+//    independently: a std request never waits for a DG request's FP64-bound
+//    block SpMVs, nor behind DG requests in the queue;
+//  * admission: FIFO per lane; a request starts when its lane has a free slot
+//    (half of max_active, or more while the other lane has nobody waiting)
+//    and its estimated device footprint fits in the shared HBM budget
+//    (replaced by the measured footprint once it is built);
+//  * preparation (worker threads, one CUDA stream each): upload, structure
+//    (built and coloured on the device for std requests), integrate +
+//    assemble, preconditioner; overlaps with the solves running;
+//  * solve (engine thread, one stream per lane): every step of a lane
+//    advances each of its active requests by one GMRES iteration with
+//    batched kernels over all of them - one CRS SpMV launch for all std
+//    requests, one launch per degree class for each DG request, and one
+//    launch each for the Gram-Schmidt dot products, updates and norms.  The scalar GMRES logic
 //    (Hessenberg column, Givens rotations, convergence test, restart and the
 //    small triangular solve) runs on the device per request, so a step needs
 //    no host round trip per request; the host reads the requests' phases once
@@ -26,9 +32,9 @@
 // does not depend on which other requests share the steps: a request gives
 // the same bits alone and in a mix.
 //
-// The kernel sequence of a step depends only on the set of active requests
-// (their state lives on the device), so it is captured once per change of
-// that set as a CUDA graph and replayed every step.
+// The kernel sequence of a lane's step depends only on its set of active
+// requests (their state lives on the device), so it is captured once per
+// change of that set as a CUDA graph and replayed every step.
 
 #include <algorithm>
 #include <chrono>
@@ -376,14 +382,31 @@ long long gbfem_serve_footprint_impl(int kind, int p, int nno, int nel, int nbf,
   return b;
 }
 
+// One lane of the engine: the active requests of one kind and what their
+// batched steps need.
+struct SrvLane {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;  // recorded after a poll's steps and state readback
+  bool busy = false, changed = false;
+  std::deque<ReqPtr> waitq;    // admission queue of this kind
+  int held = 0;                // admitted and not yet retired
+  std::vector<int> act;        // slots
+  DevBuf<int2> d_map_vec, d_map_crs;
+  DevBuf<int> d_act;
+  DevBuf<double> d_partial;
+  SrvState *h_state = nullptr;  // pinned readback of the last poll
+  int n_vec = 0, n_crs = 0, max_m1 = 1;
+  cudaGraphExec_t graph = nullptr;
+  int graph_kernels = 0;
+};
+
 struct gbfem_server_s {
   int device = 0;
-  cudaStream_t stream = nullptr;
   long long budget = 0, in_use = 0, peak_in_use = 0;
   int max_active = 0;
   std::mutex mu;
   std::condition_variable cv_engine, cv_prep, cv_done;
-  std::deque<ReqPtr> waitq, prepq, readyq;
+  std::deque<ReqPtr> prepq, readyq;
   std::map<long long, ReqPtr> reqs;
   long long next_id = 0;
   int n_preparing = 0, n_active = 0;
@@ -391,40 +414,42 @@ struct gbfem_server_s {
   std::vector<std::thread> workers;
   std::thread engine;
   // engine-owned
+  SrvLane lanes[2];  // 0: std requests, 1: DG requests
   ReqPtr slots[gbfem::SRV_MAXSLOTS];
   DevBuf<SrvDesc> d_desc;
   DevBuf<SrvState> d_state;
-  DevBuf<int2> d_map_vec, d_map_crs;
-  DevBuf<int> d_act;
-  DevBuf<double> d_partial;
-  SrvState *h_state = nullptr;
+  SrvState *h_init = nullptr;  // pinned: initial states of newly started requests
   SrvDesc *h_desc = nullptr;
-  int n_vec = 0, n_crs = 0, max_m1 = 1;
-  std::vector<int> act;
   long long steps = 0, launches = 0;
   int peak_active = 0;
-  cudaGraphExec_t graph = nullptr;
-  int graph_kernels = 0;
   int steps_per_poll = 4;
   std::string fatal;
 };
 
 namespace {
 
+// A lane may hold half of max_active requests, or more while the other lane
+// has nobody waiting; the HBM budget is shared.
 void try_admit(gbfem_server s) {  // caller holds s->mu
-  while (!s->waitq.empty()) {
-    ReqPtr r = s->waitq.front();
-    if (s->n_preparing + s->n_active + (int)s->readyq.size() >= s->max_active) break;
-    if (s->in_use + r->footprint > s->budget && s->in_use > 0) break;
-    s->waitq.pop_front();
-    s->in_use += r->footprint;
-    r->charged = r->footprint;
-    s->peak_in_use = std::max(s->peak_in_use, s->in_use);
-    r->status = 1;
-    r->t_admit = now_s();
-    s->n_preparing++;
-    s->prepq.push_back(r);
-    s->cv_prep.notify_one();
+  const int share = std::max(1, s->max_active / 2);
+  for (int L = 0; L < 2; L++) {
+    SrvLane &ln = s->lanes[L], &other = s->lanes[1 - L];
+    while (!ln.waitq.empty()) {
+      ReqPtr r = ln.waitq.front();
+      if (ln.held + other.held >= s->max_active) break;
+      if (ln.held >= share && !other.waitq.empty()) break;
+      if (s->in_use + r->footprint > s->budget && s->in_use > 0) break;
+      ln.waitq.pop_front();
+      ln.held++;
+      s->in_use += r->footprint;
+      r->charged = r->footprint;
+      s->peak_in_use = std::max(s->peak_in_use, s->in_use);
+      r->status = 1;
+      r->t_admit = now_s();
+      s->n_preparing++;
+      s->prepq.push_back(r);
+      s->cv_prep.notify_one();
+    }
   }
 }
 
@@ -448,7 +473,9 @@ int prepare(gbfem_server s, SrvRequest &r) {
   if (r.kind == 0) {
     int nd = 0, nc = 0;
     long long nnz = 0;
-    if ((rc = gbfem_build_structure(c, &nd, &nnz, &nc)) < 0) return rc;
+    // structure and element colouring on the device (deterministic)
+    if ((rc = gbfem_build_structure_device(c, &nd, &nnz)) < 0) return rc;
+    (void)nc;
     // colour-ordered scatter: the same summation order every time, so a
     // request's matrix (and result) does not depend on when it runs
     if ((rc = gbfem_assemble(c, GBFEM_SCATTER_COLOR)) < 0) return rc;
@@ -515,6 +542,7 @@ void prep_worker(gbfem_server s) {
       s->in_use -= r->charged;
       r->charged = 0;
       r->t_done = now_s();
+      s->lanes[r->kind].held--;
       try_admit(s);
       s->cv_done.notify_all();
       continue;
@@ -569,16 +597,17 @@ void fill_desc(SrvDesc &d, SrvRequest &r) {
   d.hcol = d.y + (m1 + 1);
 }
 
-// rebuild the block maps and descriptors after the active set changed
-int rebuild(gbfem_server s) {
+// rebuild a lane's block maps and its requests' descriptors after its
+// active set changed (the lane is idle: nothing of it is in flight)
+int rebuild(gbfem_server s, SrvLane &ln, int L) {
   std::vector<int2> mv, mc;
   int red = 0;
-  s->act.clear();
-  s->max_m1 = 1;
+  ln.act.clear();
+  ln.max_m1 = 1;
   for (int i = 0; i < gbfem::SRV_MAXSLOTS; i++) {
-    if (!s->slots[i]) continue;
+    if (!s->slots[i] || s->slots[i]->kind != L) continue;
     SrvRequest &r = *s->slots[i];
-    s->act.push_back(i);
+    ln.act.push_back(i);
     SrvDesc &d = s->h_desc[i];
     const int nb = (r.n + gbfem::SRV_CHUNK - 1) / gbfem::SRV_CHUNK;
     d.red_first = red;
@@ -587,37 +616,40 @@ int rebuild(gbfem_server s) {
     for (int b = 0; b < nb; b++) mv.push_back(make_int2(i, b * gbfem::SRV_CHUNK));
     if (r.kind == 0)
       for (int r0 = 0; r0 < r.n; r0 += gbfem::SRV_SPMV_ROWS) mc.push_back(make_int2(i, r0));
-    s->max_m1 = std::max(s->max_m1, r.krylov + 1);
+    ln.max_m1 = std::max(ln.max_m1, r.krylov + 1);
   }
-  s->n_vec = (int)mv.size();
-  s->n_crs = (int)mc.size();
-  if (s->d_map_vec.alloc(std::max<size_t>(mv.size(), 1)) < 0 || s->d_map_crs.alloc(std::max<size_t>(mc.size(), 1)) < 0 ||
-      s->d_act.alloc(std::max<size_t>(s->act.size(), 1)) < 0 ||
-      s->d_partial.alloc((size_t)std::max(red, 1) * gbfem::SRV_PART) < 0)
+  ln.n_vec = (int)mv.size();
+  ln.n_crs = (int)mc.size();
+  if (ln.d_map_vec.alloc(std::max<size_t>(mv.size(), 1)) < 0 || ln.d_map_crs.alloc(std::max<size_t>(mc.size(), 1)) < 0 ||
+      ln.d_act.alloc(std::max<size_t>(ln.act.size(), 1)) < 0 ||
+      ln.d_partial.alloc((size_t)std::max(red, 1) * gbfem::SRV_PART) < 0)
     return -1;
-  if (!mv.empty()) GB_CUDA(cudaMemcpyAsync(s->d_map_vec.p, mv.data(), mv.size() * sizeof(int2), cudaMemcpyHostToDevice, s->stream));
-  if (!mc.empty()) GB_CUDA(cudaMemcpyAsync(s->d_map_crs.p, mc.data(), mc.size() * sizeof(int2), cudaMemcpyHostToDevice, s->stream));
-  if (!s->act.empty())
-    GB_CUDA(cudaMemcpyAsync(s->d_act.p, s->act.data(), s->act.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
-  GB_CUDA(cudaMemcpyAsync(s->d_desc.p, s->h_desc, sizeof(SrvDesc) * gbfem::SRV_MAXSLOTS, cudaMemcpyHostToDevice,
-                          s->stream));
-  // the descriptors live in pinned memory that the next rebuild rewrites
-  GB_CUDA(cudaStreamSynchronize(s->stream));
+  if (!mv.empty())
+    GB_CUDA(cudaMemcpyAsync(ln.d_map_vec.p, mv.data(), mv.size() * sizeof(int2), cudaMemcpyHostToDevice, ln.stream));
+  if (!mc.empty())
+    GB_CUDA(cudaMemcpyAsync(ln.d_map_crs.p, mc.data(), mc.size() * sizeof(int2), cudaMemcpyHostToDevice, ln.stream));
+  if (!ln.act.empty())
+    GB_CUDA(cudaMemcpyAsync(ln.d_act.p, ln.act.data(), ln.act.size() * sizeof(int), cudaMemcpyHostToDevice, ln.stream));
+  // only this lane's descriptors: the other lane's kernels read theirs meanwhile
+  for (int i : ln.act)
+    GB_CUDA(cudaMemcpyAsync(s->d_desc.p + i, s->h_desc + i, sizeof(SrvDesc), cudaMemcpyHostToDevice, ln.stream));
+  // the host copies (maps, descriptors) are rewritten by the next rebuild
+  GB_CUDA(cudaStreamSynchronize(ln.stream));
   return 0;
 }
 
-int step(gbfem_server s) {
+int step(gbfem_server s, SrvLane &ln) {
   using namespace gbfem;
-  cudaStream_t st = s->stream;
-  const int nact = (int)s->act.size();
+  cudaStream_t st = ln.stream;
+  const int nact = (int)ln.act.size();
   const int lt = 128, lb = (nact + lt - 1) / lt;
   int L = 0;
-  const int2 *mv = s->d_map_vec.p, *mc = s->d_map_crs.p;
+  const int2 *mv = ln.d_map_vec.p, *mc = ln.d_map_crs.p;
   SrvDesc *dd = s->d_desc.p;
   SrvState *ss = s->d_state.p;
-  double *part = s->d_partial.p;
+  double *part = ln.d_partial.p;
   auto dg_spmv = [&](int mode) {
-    for (int i : s->act) {
+    for (int i : ln.act) {
       SrvRequest &r = *s->slots[i];
       if (r.kind != 1) continue;
       for (int p = 1; p <= 4; p++) {
@@ -642,54 +674,54 @@ int step(gbfem_server s) {
     }
   };
   // restart: x += V y, residual, its norm, new cycle or stop
-  srv_update_x<<<s->n_vec, SRV_T, 0, st>>>(mv, dd, ss);
-  if (s->n_crs) srv_crs_spmv<0><<<s->n_crs, SRV_T, 0, st>>>(mc, dd, ss);
+  srv_update_x<<<ln.n_vec, SRV_T, 0, st>>>(mv, dd, ss);
+  if (ln.n_crs) srv_crs_spmv<0><<<ln.n_crs, SRV_T, 0, st>>>(mc, dd, ss);
   dg_spmv(0);
-  srv_norm_partial<0><<<s->n_vec, SRV_T, 0, st>>>(mv, dd, ss, part);
-  srv_logic_restart<<<lb, lt, 0, st>>>(nact, s->d_act.p, dd, ss, part);
-  srv_start_cycle<<<s->n_vec, SRV_T, 0, st>>>(mv, dd, ss);
+  srv_norm_partial<0><<<ln.n_vec, SRV_T, 0, st>>>(mv, dd, ss, part);
+  srv_logic_restart<<<lb, lt, 0, st>>>(nact, ln.d_act.p, dd, ss, part);
+  srv_start_cycle<<<ln.n_vec, SRV_T, 0, st>>>(mv, dd, ss);
   // one Arnoldi step
-  if (s->n_crs) srv_crs_spmv<1><<<s->n_crs, SRV_T, 0, st>>>(mc, dd, ss);
+  if (ln.n_crs) srv_crs_spmv<1><<<ln.n_crs, SRV_T, 0, st>>>(mc, dd, ss);
   dg_spmv(1);
-  srv_dot_partial<<<dim3(s->n_vec, s->max_m1), SRV_T, 0, st>>>(mv, dd, ss, part);
-  srv_dot_sum<<<nact, 64, 0, st>>>(s->d_act.p, dd, ss, part);
-  srv_orthogonalize<<<s->n_vec, SRV_T, 0, st>>>(mv, dd, ss);
-  srv_norm_partial<1><<<s->n_vec, SRV_T, 0, st>>>(mv, dd, ss, part);
-  srv_logic_arnoldi<<<lb, lt, 0, st>>>(nact, s->d_act.p, dd, ss, part);
-  srv_normalize<<<s->n_vec, SRV_T, 0, st>>>(mv, dd, ss);
-  L += 11 + (s->n_crs ? 2 : 0);
+  srv_dot_partial<<<dim3(ln.n_vec, ln.max_m1), SRV_T, 0, st>>>(mv, dd, ss, part);
+  srv_dot_sum<<<nact, 64, 0, st>>>(ln.d_act.p, dd, ss, part);
+  srv_orthogonalize<<<ln.n_vec, SRV_T, 0, st>>>(mv, dd, ss);
+  srv_norm_partial<1><<<ln.n_vec, SRV_T, 0, st>>>(mv, dd, ss, part);
+  srv_logic_arnoldi<<<lb, lt, 0, st>>>(nact, ln.d_act.p, dd, ss, part);
+  srv_normalize<<<ln.n_vec, SRV_T, 0, st>>>(mv, dd, ss);
+  L += 11 + (ln.n_crs ? 2 : 0);
   GB_CUDA(cudaGetLastError());
   return L;
 }
 
-// capture the step for the current active set
-int capture(gbfem_server s) {
-  if (s->graph) {
-    cudaGraphExecDestroy(s->graph);
-    s->graph = nullptr;
+// capture a lane's step for its current active set
+int capture(gbfem_server s, SrvLane &ln) {
+  if (ln.graph) {
+    cudaGraphExecDestroy(ln.graph);
+    ln.graph = nullptr;
   }
-  if (s->act.empty()) return 0;
+  if (ln.act.empty()) return 0;
   cudaGraph_t g = nullptr;
-  GB_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-  const int L = step(s);
+  GB_CUDA(cudaStreamBeginCapture(ln.stream, cudaStreamCaptureModeThreadLocal));
+  const int L = step(s, ln);
   cudaGraph_t gg = nullptr;
-  const cudaError_t e = cudaStreamEndCapture(s->stream, &gg);
+  const cudaError_t e = cudaStreamEndCapture(ln.stream, &gg);
   if (L < 0) return L;
   GB_CUDA(e);
   g = gg;
-  const cudaError_t ei = cudaGraphInstantiate(&s->graph, g, 0);
+  const cudaError_t ei = cudaGraphInstantiate(&ln.graph, g, 0);
   cudaGraphDestroy(g);
   GB_CUDA(ei);
-  s->graph_kernels = L;
+  ln.graph_kernels = L;
   return 0;
 }
 
-void retire(gbfem_server s, int i) {
+void retire(gbfem_server s, SrvLane &ln, int i) {
   ReqPtr r = s->slots[i];
-  const SrvState &S = s->h_state[i];
+  const SrvState &S = ln.h_state[i];
   r->x.resize(r->n);
-  cudaMemcpyAsync(r->x.data(), r->kry.p, (size_t)r->n * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
-  cudaStreamSynchronize(s->stream);
+  cudaMemcpyAsync(r->x.data(), r->kry.p, (size_t)r->n * sizeof(double), cudaMemcpyDeviceToHost, ln.stream);
+  cudaStreamSynchronize(ln.stream);
   r->iters = S.it;
   r->rel = S.beta0 > 0 ? S.resid / S.beta0 : 0.0;
   gbfem_destroy(r->ctx);
@@ -702,17 +734,26 @@ void retire(gbfem_server s, int i) {
   r->status = 4;
   r->t_done = now_s();
   s->n_active--;
+  ln.held--;
   try_admit(s);
+  s->cv_done.notify_all();
+}
+
+void engine_fail(gbfem_server s, const std::string &msg) {
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->fatal = msg;
+  s->stop = true;
   s->cv_done.notify_all();
 }
 
 void engine_loop(gbfem_server s) {
   cudaSetDevice(s->device);
   for (;;) {
-    bool changed = false;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      if (s->act.empty() && s->readyq.empty()) {
+      const bool idle = s->lanes[0].act.empty() && s->lanes[1].act.empty() && !s->lanes[0].busy &&
+                        !s->lanes[1].busy;
+      if (idle && s->readyq.empty()) {
         s->cv_engine.wait(lk, [&] { return s->stop || !s->readyq.empty(); });
         if (s->stop && s->readyq.empty()) return;
       }
@@ -722,6 +763,7 @@ void engine_loop(gbfem_server s) {
         if (i == gbfem::SRV_MAXSLOTS) break;
         ReqPtr r = s->readyq.front();
         s->readyq.pop_front();
+        SrvLane &ln = s->lanes[r->kind];
         r->slot = i;
         r->status = 3;
         r->t_start = now_s();
@@ -732,53 +774,58 @@ void engine_loop(gbfem_server s) {
         memset(&init, 0, sizeof(init));
         init.phase = gbfem::PH_RESTART;
         init.beta0 = -1.0;
-        s->h_state[i] = init;
-        cudaMemcpyAsync(s->d_state.p + i, &s->h_state[i], sizeof(SrvState), cudaMemcpyHostToDevice, s->stream);
-        changed = true;
+        s->h_init[i] = init;
+        // behind the lane's work in flight (which does not touch slot i)
+        cudaMemcpyAsync(s->d_state.p + i, s->h_init + i, sizeof(SrvState), cudaMemcpyHostToDevice, ln.stream);
+        ln.changed = true;
       }
       s->peak_active = std::max(s->peak_active, s->n_active);
     }
-    if (changed && (rebuild(s) < 0 || capture(s) < 0)) {
-      std::lock_guard<std::mutex> lk(s->mu);
-      s->fatal = gbfem_last_error();
-      s->stop = true;
-      s->cv_done.notify_all();
-      return;
-    }
-    if (s->act.empty()) continue;
-    // several steps per host poll: a finished request's kernels are no-ops
-    // until it is retired, so the extra steps only cost their launch
-    cudaError_t ge = cudaSuccess;
-    for (int k = 0; k < s->steps_per_poll && ge == cudaSuccess; k++) {
-      ge = cudaGraphLaunch(s->graph, s->stream);
-      s->steps++;
-      s->launches += s->graph_kernels;
-    }
-    if (ge != cudaSuccess ||
-        cudaMemcpyAsync(s->h_state, s->d_state.p, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaMemcpyDeviceToHost,
-                        s->stream) != cudaSuccess ||
-        cudaStreamSynchronize(s->stream) != cudaSuccess) {
-      std::lock_guard<std::mutex> lk(s->mu);
-      s->fatal = std::string("serving step failed: ") + gbfem_last_error() + " / " +
-                 cudaGetErrorString(cudaGetLastError());
-      s->stop = true;
-      s->cv_done.notify_all();
-      return;
-    }
-    bool retired = false;
-    for (int i : std::vector<int>(s->act)) {
-      if (s->h_state[i].phase == gbfem::PH_DONE) {
-        retire(s, i);
-        retired = true;
+    bool progressed = false;
+    for (int L = 0; L < 2; L++) {
+      SrvLane &ln = s->lanes[L];
+      if (ln.busy) {
+        const cudaError_t q = cudaEventQuery(ln.done);
+        if (q == cudaErrorNotReady) continue;
+        if (q != cudaSuccess) {
+          engine_fail(s, std::string("serving step failed: ") + cudaGetErrorString(q));
+          return;
+        }
+        ln.busy = false;
+        progressed = true;
+        for (int i : std::vector<int>(ln.act))
+          if (ln.h_state[i].phase == gbfem::PH_DONE) {
+            retire(s, ln, i);
+            ln.changed = true;
+          }
       }
+      if (ln.changed) {
+        if (rebuild(s, ln, L) < 0 || capture(s, ln) < 0) {
+          engine_fail(s, gbfem_last_error());
+          return;
+        }
+        ln.changed = false;
+      }
+      if (ln.act.empty()) continue;
+      // several steps per poll: a finished request's kernels are no-ops until
+      // it is retired, so the extra steps only cost their launch
+      cudaError_t ge = cudaSuccess;
+      for (int k = 0; k < s->steps_per_poll && ge == cudaSuccess; k++) {
+        ge = cudaGraphLaunch(ln.graph, ln.stream);
+        s->steps++;
+        s->launches += ln.graph_kernels;
+      }
+      if (ge != cudaSuccess ||
+          cudaMemcpyAsync(ln.h_state, s->d_state.p, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaMemcpyDeviceToHost,
+                          ln.stream) != cudaSuccess ||
+          cudaEventRecord(ln.done, ln.stream) != cudaSuccess) {
+        engine_fail(s, std::string("serving step failed: ") + cudaGetErrorString(cudaGetLastError()));
+        return;
+      }
+      ln.busy = true;
+      progressed = true;
     }
-    if (retired && (rebuild(s) < 0 || capture(s) < 0)) {
-      std::lock_guard<std::mutex> lk(s->mu);
-      s->fatal = gbfem_last_error();
-      s->stop = true;
-      s->cv_done.notify_all();
-      return;
-    }
+    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
 }
 
@@ -805,15 +852,29 @@ int gbfem_server_create(gbfem_server *out, int device, long long hbm_budget, int
     hbm_budget = (long long)(0.85 * (double)fr);
   }
   s->budget = hbm_budget;
-  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      s->d_desc.alloc(gbfem::SRV_MAXSLOTS) < 0 || s->d_state.alloc(gbfem::SRV_MAXSLOTS) < 0 ||
-      cudaHostAlloc(&s->h_state, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) != cudaSuccess ||
-      cudaHostAlloc(&s->h_desc, sizeof(SrvDesc) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) != cudaSuccess) {
+  bool ok = s->d_desc.alloc(gbfem::SRV_MAXSLOTS) >= 0 && s->d_state.alloc(gbfem::SRV_MAXSLOTS) >= 0 &&
+            cudaHostAlloc(&s->h_init, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) == cudaSuccess &&
+            cudaHostAlloc(&s->h_desc, sizeof(SrvDesc) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) == cudaSuccess;
+  for (int L = 0; L < 2 && ok; L++) {
+    SrvLane &ln = s->lanes[L];
+    ok = cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&ln.done, cudaEventDisableTiming) == cudaSuccess &&
+         cudaHostAlloc(&ln.h_state, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) == cudaSuccess;
+    if (ok) memset(ln.h_state, 0, sizeof(SrvState) * gbfem::SRV_MAXSLOTS);
+  }
+  if (!ok) {
     gbfem::set_error("server allocation failed");
+    for (SrvLane &ln : s->lanes) {
+      if (ln.h_state) cudaFreeHost(ln.h_state);
+      if (ln.done) cudaEventDestroy(ln.done);
+      if (ln.stream) cudaStreamDestroy(ln.stream);
+    }
+    if (s->h_init) cudaFreeHost(s->h_init);
+    if (s->h_desc) cudaFreeHost(s->h_desc);
     delete s;
     return -1;
   }
-  memset(s->h_state, 0, sizeof(SrvState) * gbfem::SRV_MAXSLOTS);
+  memset(s->h_init, 0, sizeof(SrvState) * gbfem::SRV_MAXSLOTS);
   memset(s->h_desc, 0, sizeof(SrvDesc) * gbfem::SRV_MAXSLOTS);
   cudaMemset(s->d_state.p, 0, sizeof(SrvState) * gbfem::SRV_MAXSLOTS);
   for (int i = 0; i < prep_threads; i++) s->workers.emplace_back(prep_worker, s);
@@ -827,7 +888,7 @@ int gbfem_server_destroy(gbfem_server s) {
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
-    s->waitq.clear();
+    for (SrvLane &ln : s->lanes) ln.waitq.clear();
   }
   s->cv_prep.notify_all();
   s->cv_engine.notify_all();
@@ -843,16 +904,21 @@ int gbfem_server_destroy(gbfem_server s) {
     if (r->ctx) gbfem_destroy(r->ctx);
     r->kry.release();
   }
-  if (s->graph) cudaGraphExecDestroy(s->graph);
+  for (SrvLane &ln : s->lanes) {
+    if (ln.stream) cudaStreamSynchronize(ln.stream);
+    if (ln.graph) cudaGraphExecDestroy(ln.graph);
+    ln.d_map_vec.release();
+    ln.d_map_crs.release();
+    ln.d_act.release();
+    ln.d_partial.release();
+    if (ln.h_state) cudaFreeHost(ln.h_state);
+    if (ln.done) cudaEventDestroy(ln.done);
+    if (ln.stream) cudaStreamDestroy(ln.stream);
+  }
   s->d_desc.release();
   s->d_state.release();
-  s->d_map_vec.release();
-  s->d_map_crs.release();
-  s->d_act.release();
-  s->d_partial.release();
-  if (s->h_state) cudaFreeHost(s->h_state);
+  if (s->h_init) cudaFreeHost(s->h_init);
   if (s->h_desc) cudaFreeHost(s->h_desc);
-  if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return 0;
 }
@@ -902,7 +968,7 @@ long long gbfem_server_submit(gbfem_server s, const gbfem_serve_request *q) {
   r->id = s->next_id++;
   r->t_submit = now_s();
   s->reqs[r->id] = r;
-  s->waitq.push_back(r);
+  s->lanes[r->kind].waitq.push_back(r);
   try_admit(s);
   return r->id;
 }
@@ -984,7 +1050,7 @@ int gbfem_server_stats(gbfem_server s, long long *st) {
   st[3] = s->peak_in_use;
   st[4] = s->budget;
   st[5] = s->in_use;
-  st[6] = (long long)s->waitq.size();
+  st[6] = (long long)(s->lanes[0].waitq.size() + s->lanes[1].waitq.size());
   st[7] = s->n_active;
   return 0;
 }

@@ -223,9 +223,72 @@ __global__ void sg_tables(int nel, int nv, const int *__restrict__ el_dofs, cons
   }
 }
 
+// Element colouring for the deterministic colour-batched scatter: elements
+// sharing a dof must differ.  Jones-Plassmann with hashed priorities: in
+// round r an uncoloured element whose priority beats every neighbour not
+// coloured in an earlier round takes the smallest colour its earlier-coloured
+// neighbours leave free.  Two neighbours never both win a round, and every
+// decision reads only what earlier rounds fixed, so the colouring does not
+// depend on thread scheduling.  state = (round << 8) | colour, -1 uncoloured.
+__device__ __forceinline__ unsigned sg_prio(int e) {
+  unsigned h = (unsigned)e * 0x9E3779B1u;
+  h ^= h >> 16;
+  h *= 0x85EBCA6Bu;
+  h ^= h >> 13;
+  return h;
+}
+
+__global__ void sg_jp_round(int nel, int nv, int rnd, const int *__restrict__ el_dofs,
+                            const int *__restrict__ inc_ptr, const int *__restrict__ inc, int *state,
+                            int *remaining, int *err) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel || state[e] >= 0) return;
+  const unsigned pe = sg_prio(e);
+  unsigned long long used = 0;
+  bool wins = true;
+  for (int j = 0; j < nv && wins; j++) {
+    const int d = el_dofs[(size_t)e * nv + j];
+    for (int k = inc_ptr[d]; k < inc_ptr[d + 1]; k++) {
+      const int f = inc[k];
+      if (f == e) continue;
+      const int sf = ((volatile int *)state)[f];
+      if (sf >= 0 && (sf >> 8) < rnd) {
+        used |= 1ULL << (sf & 63);
+      } else {
+        const unsigned pf = sg_prio(f);
+        if (pf > pe || (pf == pe && f > e)) {
+          wins = false;
+          break;
+        }
+      }
+    }
+  }
+  if (!wins) {
+    atomicAdd(remaining, 1);
+    return;
+  }
+  const int c = __ffsll((long long)~used) - 1;
+  if (c < 0 || c >= 64) {
+    atomicExch(err, 2);
+    return;
+  }
+  state[e] = (rnd << 8) | c;
+}
+
+__global__ void sg_color_count(int nel, const int *__restrict__ state, int *cnt) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nel) atomicAdd(cnt + (state[e] & 63), 1);
+}
+
+__global__ void sg_color_fill(int nel, const int *__restrict__ state, int *cursor, int *perm) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nel) perm[atomicAdd(cursor + (state[e] & 63), 1)] = e;
+}
+
 int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int *el_nodes, DevBuf<int> &dof_of_node,
                            DevBuf<int> &row_ptr, DevBuf<int> &col_ind, DevBuf<int> &el_table, int *err,
-                           int *ndof_out, long long *nnz_out) {
+                           int *ndof_out, long long *nnz_out, DevBuf<int> *el_perm,
+                           std::vector<int> *el_color_ptr) {
   const long long m = (long long)nel * nv;
   DevBuf<int> first, mark, rank, el_dofs, inc_cnt, inc_ptr, inc, len, tmp;
   auto cleanup = [&]() {
@@ -272,6 +335,39 @@ int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int 
   if (el_table.alloc((size_t)nel * (nv * nv + nv)) < 0) return fail(-1);
   sg_tables<<<(nel + 127) / 128, 128, 0, st>>>(nel, nv, el_dofs.p, row_ptr.p, col_ind.p, el_table.p);
   GB_CUDA(cudaGetLastError());
+  // 5. colouring (optional)
+  if (el_perm && el_color_ptr) {
+    DevBuf<int> state, cnt;
+    if (state.alloc(nel) < 0 || cnt.alloc(64 + 1) < 0 || el_perm->alloc(nel) < 0) return fail(-1);
+    sg_fill<<<(nel + 255) / 256, 256, 0, st>>>(nel, -1, state.p);
+    int remaining = nel, rnd = 0;
+    while (remaining > 0) {
+      GB_CUDA(cudaMemsetAsync(cnt.p + 64, 0, sizeof(int), st));
+      sg_jp_round<<<(nel + 255) / 256, 256, 0, st>>>(nel, nv, rnd, el_dofs.p, inc_ptr.p, inc.p, state.p, cnt.p + 64,
+                                                    err);
+      GB_CUDA(cudaMemcpyAsync(&remaining, cnt.p + 64, sizeof(int), cudaMemcpyDeviceToHost, st));
+      GB_CUDA(cudaStreamSynchronize(st));
+      if (++rnd > (1 << 22)) break;  // cannot happen: every round colours the top-priority element left
+    }
+    GB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemsetAsync(cnt.p, 0, 64 * sizeof(int), st));
+    sg_color_count<<<(nel + 255) / 256, 256, 0, st>>>(nel, state.p, cnt.p);
+    std::vector<int> counts(64);
+    GB_CUDA(cudaMemcpyAsync(counts.data(), cnt.p, 64 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if (herr || remaining > 0) {
+      cleanup();
+      GB_CHECK(false, "device colouring needs more than 64 colours");
+    }
+    int ncol = 64;
+    while (ncol > 0 && counts[ncol - 1] == 0) ncol--;
+    el_color_ptr->assign(ncol + 1, 0);
+    for (int c = 0; c < ncol; c++) (*el_color_ptr)[c + 1] = (*el_color_ptr)[c] + counts[c];
+    GB_CUDA(cudaMemcpyAsync(cnt.p, el_color_ptr->data(), ncol * sizeof(int), cudaMemcpyHostToDevice, st));
+    sg_color_fill<<<(nel + 255) / 256, 256, 0, st>>>(nel, state.p, cnt.p, el_perm->p);
+    GB_CUDA(cudaGetLastError());
+    GB_CUDA(cudaStreamSynchronize(st));
+  }
   GB_CUDA(cudaStreamSynchronize(st));
   cleanup();
   *ndof_out = nd;

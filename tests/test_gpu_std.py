@@ -387,6 +387,12 @@ def test_device_structure_vs_reference(gb, name):
     val, rhs = c.get_matrix()
     assert crs_rel_err(rp, val, g["crs_val"], energy_scale(rp, ci, g["crs_val"])) < REL_TOL
     assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL
+    # the device colouring: colour-batched plain adds give the reference's
+    # matrix (a colour holding two elements with a shared dof would race)
+    c.assemble(gb.SCATTER_COLOR)
+    val, rhs = c.get_matrix()
+    assert crs_rel_err(rp, val, g["crs_val"], energy_scale(rp, ci, g["crs_val"])) < REL_TOL
+    assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL
 
 
 @pytest.mark.parametrize("kind", ["prism", "tet"])
@@ -398,7 +404,19 @@ def test_device_structure_vs_host_larger(gb, kind):
     c = make_ctx(gb, m, lognormal_k(m.nel, seed=2))
     c.build_structure()
     h = c.get_crs_structure() + (c.get_element_tables(),)
+    c.assemble(gb.SCATTER_COLOR)
+    vh, rh = c.get_matrix()
     c.build_structure_device()
     d = c.get_crs_structure() + (c.get_element_tables(),)
     for a, b in zip(h, d):
         assert np.array_equal(a, b)
+    # colour-batched assembly on the device colouring: repeatable bit for bit
+    # and equal to the host colouring's to rounding
+    c.assemble(gb.SCATTER_COLOR)
+    v1, r1 = c.get_matrix()
+    c.assemble(gb.SCATTER_COLOR)
+    v2, r2 = c.get_matrix()
+    assert np.array_equal(v1, v2) and np.array_equal(r1, r2)
+    rp, ci = d[1], d[2]
+    assert crs_rel_err(rp, v1, vh, energy_scale(rp, ci, vh)) < REL_TOL
+    assert vec_rel_err(r1, rh) < REL_TOL
