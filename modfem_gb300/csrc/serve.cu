@@ -6,9 +6,10 @@
 //
 // Pipeline:
 //  * two lanes, std and DG requests, each with its own FIFO admission queue,
-//    slot quota, CUDA stream, step graph and state readback, polled
-//    independently: a std request never waits for a DG request's FP64-bound
-//    block SpMVs, nor behind DG requests in the queue;
+//    slot quota, CUDA stream (std at the highest priority, DG at the lowest),
+//    step graph and state readback, polled independently: a std request
+//    never waits for a DG request's FP64-bound block SpMVs, nor behind DG
+//    requests in the queue;
 //  * admission: FIFO per lane; a request starts when its lane has a free slot
 //    (half of max_active, or more while the other lane has nobody waiting)
 //    and its estimated device footprint fits in the shared HBM budget
@@ -855,9 +856,15 @@ int gbfem_server_create(gbfem_server *out, int device, long long hbm_budget, int
   bool ok = s->d_desc.alloc(gbfem::SRV_MAXSLOTS) >= 0 && s->d_state.alloc(gbfem::SRV_MAXSLOTS) >= 0 &&
             cudaHostAlloc(&s->h_init, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) == cudaSuccess &&
             cudaHostAlloc(&s->h_desc, sizeof(SrvDesc) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) == cudaSuccess;
+  // the std lane's short steps get the highest stream priority, the DG lane's
+  // long FP64-bound SpMVs the lowest: when both lanes have work queued the
+  // block scheduler starts std blocks first
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
   for (int L = 0; L < 2 && ok; L++) {
     SrvLane &ln = s->lanes[L];
-    ok = cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking) == cudaSuccess &&
+    ok = cudaStreamCreateWithPriority(&ln.stream, cudaStreamNonBlocking, L == 0 ? prio_greatest : prio_least) ==
+             cudaSuccess &&
          cudaEventCreateWithFlags(&ln.done, cudaEventDisableTiming) == cudaSuccess &&
          cudaHostAlloc(&ln.h_state, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) == cudaSuccess;
     if (ok) memset(ln.h_state, 0, sizeof(SrvState) * gbfem::SRV_MAXSLOTS);
