@@ -31,12 +31,15 @@ static int upload(gbfem_ctx c, DevBuf<T> &d, const T *h, size_t n) {
   return 0;
 }
 
+// block class of the DG SpMV kernels: degree p on prisms, 4 + p on tetrahedra
+static inline int dg_class_off(gbfem_ctx c) { return c->nv == GBFEM_TETRA ? 4 : 0; }
+
 // Block SpMV over all DG block rows, one launch per degree class.
 static int dg_spmv(gbfem_ctx c, int mode, const double *x, const double *b, double *out) {
   int n = 0;
   for (int p = 1; p <= 4; p++) {
     if (!c->dg_list[p].p) continue;
-    const int r = gbfem::launch_dg_block_spmv(c->stream, mode, p, (int)c->dg_list[p].n, c->dg_list[p].p,
+    const int r = gbfem::launch_dg_block_spmv(c->stream, mode, p + dg_class_off(c), (int)c->dg_list[p].n, c->dg_list[p].p,
                                               c->dg_roff_d.p, c->dg_row_val_d.p, c->dg_cx_off_d.p, c->dg_colx_d.p,
                                               c->dg_val.p, c->dg_dinv_off_d.p, c->dg_dinv.p, x, b, out);
     if (r < 0) return r;
@@ -210,7 +213,6 @@ int gbfem_set_coefficients(gbfem_ctx c, const double *k_el, const double *D_el, 
     c->k_el.release();
   }
   if (D_el) {
-    GB_CHECK(c->nv == GBFEM_PRISM, "tensor coefficients are supported for prisms");
     GB_TRY(c->D_el.alloc((size_t)9 * c->nel));
     GB_CUDA(cudaMemcpyAsync(c->D_el.p, D_el, (size_t)9 * c->nel * sizeof(double), cudaMemcpyHostToDevice,
                             c->stream));
@@ -422,6 +424,7 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     launches += r;
   }
   cudaEventRecord(c->ev2, c->stream);
+  GB_CHECK(c->nv == GBFEM_PRISM || !c->aniso, "std tetrahedra take an isotropic k_el (tensors: prisms and DG)");
   if (c->nv == GBFEM_PRISM)
     r = gbfem::launch_prism_elements(c->stream, true, c->aniso, e1 - e0, c->in_id.p + e0, 1, c->in_pos.p + e0,
                                      c->nel, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->in_table.p,
@@ -445,6 +448,7 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
 
 int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
   GB_CHECK(c && c->have_tables, "structure not built (gbfem_build_structure)");
+  GB_CHECK(c->nv == GBFEM_PRISM || !c->aniso, "std tetrahedra take an isotropic k_el (tensors: prisms and DG)");
   GB_CHECK(scatter_mode == GBFEM_SCATTER_ATOMIC || scatter_mode == GBFEM_SCATTER_COLOR, "bad scatter mode");
   GB_CUDA(cudaSetDevice(c->device));
   const bool atomic = scatter_mode == GBFEM_SCATTER_ATOMIC;
@@ -512,7 +516,7 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
 // DG prisms
 // ---------------------------------------------------------------------------
 int gbfem_dg_set_degrees(gbfem_ctx c, const int *p_el) {
-  GB_CHECK(c && c->nel > 0 && c->nv == GBFEM_PRISM, "DG needs a prism mesh (gbfem_set_mesh)");
+  GB_CHECK(c && c->nel > 0, "DG needs a mesh (gbfem_set_mesh)");
   GB_CHECK(p_el, "null degree array");
   for (int e = 0; e < c->nel; e++) GB_CHECK(p_el[e] >= 1 && p_el[e] <= 4, "DG degree must be 1..4");
   c->dg_p.assign(p_el, p_el + c->nel);
@@ -522,8 +526,10 @@ int gbfem_dg_set_degrees(gbfem_ctx c, const int *p_el) {
 
 int gbfem_dg_set_faces(gbfem_ctx c, int nfa, const int *fa_type, const int *fa_bc, const int *fa_el,
                        const int *fa_side, const int *fa_nodes) {
-  GB_CHECK(c && c->nel > 0 && c->nv == GBFEM_PRISM, "DG needs a prism mesh (gbfem_set_mesh)");
+  GB_CHECK(c && c->nel > 0, "DG needs a mesh (gbfem_set_mesh)");
   GB_CHECK(nfa >= 0, "negative face count");
+  const bool tet = c->nv == GBFEM_TETRA;
+  const int nv = c->nv;
   GB_CHECK(nfa == 0 || (fa_type && fa_bc && fa_el && fa_side && fa_nodes), "face arrays missing");
   const int nel = c->nel;
   const int *en = c->h_el_nodes.data();
@@ -532,15 +538,18 @@ int gbfem_dg_set_faces(gbfem_ctx c, int nfa, const int *fa_type, const int *fa_b
     GB_CHECK(t == 3 || t == 4, "face type must be 3 (triangle) or 4 (quadrilateral)");
     GB_CHECK(e1 >= 0 && e1 < nel, "face neighbour out of range");
     GB_CHECK(e2 == -1 || (e2 >= 0 && e2 < nel && e2 != e1), "second face neighbour out of range");
-    GB_CHECK(sd >= 0 && sd <= 4 && (sd < 2) == (t == 3), "face side does not match the face type");
+    if (tet)
+      GB_CHECK(t == 3 && sd >= 0 && sd <= 3, "tetrahedron faces are triangles on sides 0..3");
+    else
+      GB_CHECK(sd >= 0 && sd <= 4 && (sd < 2) == (t == 3), "face side does not match the face type");
     GB_CHECK(e2 >= 0 || (fa_bc[f] > 0 && fa_bc[f] < 10),
              "boundary faces must carry a Dirichlet flag (0 < bc < 10)");
     for (int i = 0; i < t; i++) {
       const int v = fa_nodes[4 * f + i];
       bool in1 = false, in2 = e2 < 0;
-      for (int k = 0; k < 6; k++) {
-        in1 = in1 || en[6 * (size_t)e1 + k] == v;
-        if (e2 >= 0) in2 = in2 || en[6 * (size_t)e2 + k] == v;
+      for (int k = 0; k < nv; k++) {
+        in1 = in1 || en[nv * (size_t)e1 + k] == v;
+        if (e2 >= 0) in2 = in2 || en[nv * (size_t)e2 + k] == v;
       }
       GB_CHECK(in1 && in2, "face vertex is not a vertex of its neighbours");
     }
@@ -578,6 +587,10 @@ int gbfem_dg_set_penalty(gbfem_ctx c, double pen) {
 }
 
 static const int kDgNs[5] = {0, 6, 18, 40, 75};
+static const int kDgTetNs[5] = {0, 4, 10, 20, 35};
+// functions of a DG element of degree p: tensor basis on prisms, complete
+// basis on tetrahedra
+static inline int dg_ns(gbfem_ctx c, int p) { return c->nv == GBFEM_TETRA ? kDgTetNs[p] : kDgNs[p]; }
 
 int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   GB_CHECK(c && !c->dg_p.empty(), "DG degrees not set (gbfem_dg_set_degrees)");
@@ -587,7 +600,7 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   // dof blocks in element order (utr_get_list_ent, DG branch: one dof entity
   // per element, uts_ls_intf.c:640-700)
   c->dg_roff.assign(nel + 1, 0);
-  for (int e = 0; e < nel; e++) c->dg_roff[e + 1] = c->dg_roff[e] + kDgNs[c->dg_p[e]];
+  for (int e = 0; e < nel; e++) c->dg_roff[e + 1] = c->dg_roff[e] + dg_ns(c, c->dg_p[e]);
   c->dg_ndof = c->dg_roff[nel];
   // block row e: the element and its face neighbours, ascending (the sorted
   // neighbour lists of sir_create, sis_mkb_intf.c:1100-1146)
@@ -620,11 +633,11 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   c->dg_boff.assign(nblk + 1, 0);
   std::vector<long long> diag(nel), dinv_off(nel + 1, 0);
   for (int e = 0; e < nel; e++) {
-    const long long ne = kDgNs[c->dg_p[e]];
+    const long long ne = dg_ns(c, c->dg_p[e]);
     for (int k = c->dg_bptr[e]; k < c->dg_bptr[e + 1]; k++) {
       const int col = c->dg_bcol[k];
       if (col == e) diag[e] = c->dg_boff[k];
-      c->dg_boff[k + 1] = c->dg_boff[k] + ne * kDgNs[c->dg_p[col]];
+      c->dg_boff[k + 1] = c->dg_boff[k] + ne * dg_ns(c, c->dg_p[col]);
     }
     dinv_off[e + 1] = dinv_off[e] + ne * ne;
   }
@@ -654,9 +667,9 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
     h.nfv = c->dg_fa_type[f];
     for (int i = 0; i < h.nfv; i++) {
       const int v = c->dg_fa_nodes[4 * f + i];
-      for (int k = 0; k < 6; k++) {
-        if (en[6 * (size_t)h.el1 + k] == v) h.loc1[i] = (unsigned char)k;
-        if (h.el2 >= 0 && en[6 * (size_t)h.el2 + k] == v) h.loc2[i] = (unsigned char)k;
+      for (int k = 0; k < c->nv; k++) {
+        if (en[c->nv * (size_t)h.el1 + k] == v) h.loc1[i] = (unsigned char)k;
+        if (h.el2 >= 0 && en[c->nv * (size_t)h.el2 + k] == v) h.loc2[i] = (unsigned char)k;
       }
     }
     h.owner_is_2 = 0;
@@ -673,7 +686,7 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   for (int e = 0; e < nel; e++) {
     row_val[e] = c->dg_boff[c->dg_bptr[e]];
     long long nct = 0;
-    for (int k = c->dg_bptr[e]; k < c->dg_bptr[e + 1]; k++) nct += kDgNs[c->dg_p[c->dg_bcol[k]]];
+    for (int k = c->dg_bptr[e]; k < c->dg_bptr[e + 1]; k++) nct += dg_ns(c, c->dg_p[c->dg_bcol[k]]);
     cx_off[e + 1] = cx_off[e] + nct;
   }
   std::vector<int> colx(cx_off[nel]);
@@ -705,7 +718,7 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
     std::vector<int> tcl, fpl;
     for (int e = 0; e < nel; e++) {
       if (c->dg_p[e] != p) continue;
-      bool ok = p <= 3;
+      bool ok = p <= 3 && c->nv == GBFEM_PRISM;
       for (int h = hptr[e]; ok && h < hptr[e + 1]; h++) {
         const int nb = hf[h].owner_is_2 ? hf[h].el1 : hf[h].el2;
         if (nb >= 0 && c->dg_p[nb] > 3) ok = false;
@@ -763,7 +776,11 @@ int gbfem_dg_assemble(gbfem_ctx c) {
   for (int p = 1; p <= 4; p++) {
     if (!c->dg_list[p].p) continue;
     int r;
-    if (tc && gbfem::dg_tc_supported(p))
+    if (c->nv == GBFEM_TETRA)
+      r = gbfem::launch_dg_tet_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
+                                        c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->dg_boff_diag_d.p,
+                                        c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
+    else if (tc && gbfem::dg_tc_supported(p))
       r = gbfem::launch_dg_tc_volume(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->el_nodes.p,
                                      c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->dg_boff_diag_d.p, c->dg_roff_d.p,
                                      c->dg_val.p, c->dg_rhs.p, c->err.p,
@@ -782,6 +799,15 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     if (tcf && !tc) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
     for (int p = 1; p <= 4; p++) {
       if (!c->dg_list[p].p) continue;
+      if (c->nv == GBFEM_TETRA) {
+        const int r = gbfem::launch_dg_tet_faces(c->stream, p, (int)c->dg_list[p].n, c->dg_list[p].p,
+                                                 c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p,
+                                                 c->k_el.p, c->D_el.p, c->dg_pen, c->g, c->dg_boff_diag_d.p,
+                                                 c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
+        GB_TRY(r);
+        launches += r;
+        continue;
+      }
       if (tcf) {
         // tensor-core eligible owners, then the rest on the FP64 kernel
         int r = gbfem::launch_dg_tc_faces(c->stream, p, (int)c->dg_flist_tc[p].n, c->dg_flist_tc[p].p,
@@ -841,6 +867,7 @@ int gbfem_dg_set_variants(gbfem_ctx c, const int *vol, const int *face) {
 // matrix is overwritten: assemble afterwards) and keeps the fastest.
 int gbfem_dg_autotune(gbfem_ctx c, int sample, int *vol_out, int *face_out, double *ms_out) {
   GB_CHECK(c && c->dg_ready, "DG structure not built (gbfem_dg_build_structure)");
+  GB_CHECK(c->nv == GBFEM_PRISM, "the launch-shape autotuner covers the prism kernels");
   GB_CUDA(cudaSetDevice(c->device));
   if (sample <= 0) sample = 16384;
   cudaStream_t st = c->stream;
@@ -1218,7 +1245,8 @@ static int dg_spmv32(gbfem_ctx c, int mode, const double *x, const double *b, do
   int n = 0;
   for (int p = 1; p <= 4; p++) {
     if (!c->dg_list[p].p) continue;
-    const int r = gbfem::launch_dg_block_spmv32(c->stream, mode, p, (int)c->dg_list[p].n, c->dg_list[p].p,
+    const int r = gbfem::launch_dg_block_spmv32(c->stream, mode, p + dg_class_off(c), (int)c->dg_list[p].n,
+                                                c->dg_list[p].p,
                                                 c->dg_roff_d.p, c->dg_row_val_d.p, c->dg_cx_off_d.p,
                                                 c->dg_colx_d.p, c->dg_val32.p, c->dg_dinv_off_d.p, c->dg_dinv32.p,
                                                 x, b, out);

@@ -100,6 +100,30 @@ __device__ void dgb_prism(const DgBatchTables &tb, const DgBatchArgs &a, const D
                                    sG, sV, sT, lt, valid);
 }
 
+// The 6 geometric factors G = C^T A C / |det| (00 01 02 11 12 22) and |det|
+// of an affine tetrahedron from its vertices x[12] and tensor A[9]
+__device__ __forceinline__ void dg_tet_geometry(const double *x, const double *A, double *g) {
+  const v3 x0 = {x[0], x[1], x[2]};
+  const v3 j1 = v3_sub(v3{x[3], x[4], x[5]}, x0), j2 = v3_sub(v3{x[6], x[7], x[8]}, x0),
+           j3 = v3_sub(v3{x[9], x[10], x[11]}, x0);
+  const v3 cb[3] = {v3_cross(j2, j3), v3_cross(j3, j1), v3_cross(j1, j2)};
+  const double adet = fabs(v3_dot(j1, cb[0]));
+  v3 Ac[3];
+#pragma unroll
+  for (int b = 0; b < 3; b++)
+    Ac[b] = {fma(A[0], cb[b].x, fma(A[1], cb[b].y, A[2] * cb[b].z)),
+             fma(A[3], cb[b].x, fma(A[4], cb[b].y, A[5] * cb[b].z)),
+             fma(A[6], cb[b].x, fma(A[7], cb[b].y, A[8] * cb[b].z))};
+  const double s = 1.0 / adet;
+  g[0] = s * v3_dot(cb[0], Ac[0]);
+  g[1] = s * v3_dot(cb[0], Ac[1]);
+  g[2] = s * v3_dot(cb[0], Ac[2]);
+  g[3] = s * v3_dot(cb[1], Ac[1]);
+  g[4] = s * v3_dot(cb[1], Ac[2]);
+  g[5] = s * v3_dot(cb[2], Ac[2]);
+  g[6] = adet;
+}
+
 template <int P>
 __device__ void dgb_tets(const DgBatchTables &tb, const DgBatchArgs &a, const DgBatchTile &T, double *smem) {
   constexpr int NS = tet_ns(P), NSYM = NS * (NS + 1) / 2;
@@ -110,27 +134,7 @@ __device__ void dgb_tets(const DgBatchTables &tb, const DgBatchArgs &a, const Dg
   for (int el = tid; el < count; el += DGB_THREADS) {
     const int e = a.order[T.start + el];
     sE[el] = e;
-    const double *x = a.tX + 12 * (size_t)e, *A = a.tA + 9 * (size_t)e;
-    const v3 x0 = {x[0], x[1], x[2]};
-    const v3 j1 = v3_sub(v3{x[3], x[4], x[5]}, x0), j2 = v3_sub(v3{x[6], x[7], x[8]}, x0),
-             j3 = v3_sub(v3{x[9], x[10], x[11]}, x0);
-    const v3 cb[3] = {v3_cross(j2, j3), v3_cross(j3, j1), v3_cross(j1, j2)};
-    const double adet = fabs(v3_dot(j1, cb[0]));
-    v3 Ac[3];
-#pragma unroll
-    for (int b = 0; b < 3; b++)
-      Ac[b] = {fma(A[0], cb[b].x, fma(A[1], cb[b].y, A[2] * cb[b].z)),
-               fma(A[3], cb[b].x, fma(A[4], cb[b].y, A[5] * cb[b].z)),
-               fma(A[6], cb[b].x, fma(A[7], cb[b].y, A[8] * cb[b].z))};
-    const double s = 1.0 / adet;
-    double *g = sGc + 7 * el;
-    g[0] = s * v3_dot(cb[0], Ac[0]);
-    g[1] = s * v3_dot(cb[0], Ac[1]);
-    g[2] = s * v3_dot(cb[0], Ac[2]);
-    g[3] = s * v3_dot(cb[1], Ac[1]);
-    g[4] = s * v3_dot(cb[1], Ac[2]);
-    g[5] = s * v3_dot(cb[2], Ac[2]);
-    g[6] = adet;
+    dg_tet_geometry(a.tX + 12 * (size_t)e, a.tA + 9 * (size_t)e, sGc + 7 * el);
   }
   __syncthreads();
   // every entry of the tile's blocks once, column-major within a block, so
@@ -160,6 +164,51 @@ __device__ __forceinline__ void dgb_prism_variant(const DgBatchTables &tb, const
     case 0: dgb_prism<P, dgb_prism_thr(P, 0), dgb_prism_qc(P, 0)>(tb, a, T, smem); break;
     case 1: dgb_prism<P, dgb_prism_thr(P, 1), dgb_prism_qc(P, 1)>(tb, a, T, smem); break;
     default: dgb_prism<P, dgb_prism_thr(P, 2), dgb_prism_qc(P, 2)>(tb, a, T, smem); break;
+  }
+}
+
+// Tetrahedra of degree P of a DG context (one CTA per 32 elements): vertex
+// coordinates through el_nodes, tensor D_el (9 per element) or k_el I; block
+// ns x ns column-major at val + boff[e], load vector at rhs + roff[e].  The
+// same arithmetic as the batch tiles.
+template <int P>
+__global__ void __launch_bounds__(DGB_THREADS) dg_tet_elements_kernel(
+    int count, const int *__restrict__ ent_el, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
+    const double *__restrict__ k_el, const double *__restrict__ D_el, double f, const double *__restrict__ Tt,
+    const double *__restrict__ MOM, const long long *__restrict__ boff, const int *__restrict__ roff,
+    double *__restrict__ val, double *__restrict__ rhs) {
+  constexpr int NS = tet_ns(P), NSYM = NS * (NS + 1) / 2, TILE = 32;
+  __shared__ double sGc[TILE][7];
+  __shared__ int sE[TILE];
+  const int tid = threadIdx.x, first = blockIdx.x * TILE;
+  const int n = count - first < TILE ? count - first : TILE;
+  if (tid < n) {
+    const int e = ent_el[first + tid];
+    sE[tid] = e;
+    double x[12], A[9];
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const int node = el_nodes[4 * (size_t)e + v];
+#pragma unroll
+      for (int d = 0; d < 3; d++) x[3 * v + d] = xyz[3 * (size_t)node + d];
+    }
+#pragma unroll
+    for (int r = 0; r < 9; r++) A[r] = D_el ? D_el[9 * (size_t)e + r] : ((r % 4 == 0) ? (k_el ? k_el[e] : 1.0) : 0.0);
+    dg_tet_geometry(x, A, sGc[tid]);
+  }
+  __syncthreads();
+  for (int t = tid; t < n * NS * NS; t += DGB_THREADS) {
+    const int el = t / (NS * NS), r = t % (NS * NS), u = r / NS, w = r % NS;
+    const int lo = u < w ? u : w, hi = u < w ? w : u;
+    const int k0 = lo * NS - lo * (lo - 1) / 2 + (hi - lo);
+    double v = 0.0;
+#pragma unroll
+    for (int c = 0; c < 6; c++) v = fma(sGc[el][c], __ldg(Tt + c * NSYM + k0), v);
+    val[boff[sE[el]] + r] = v;
+  }
+  for (int t = tid; t < n * NS; t += DGB_THREADS) {
+    const int el = t / NS, i = t % NS;
+    rhs[roff[sE[el]] + i] = f * sGc[el][6] * __ldg(MOM + i);
   }
 }
 
@@ -255,6 +304,29 @@ static int dg_batch_tables(int device, DgBatchTables *out) {
   }
   *out = g_bt[device];
   return 0;
+}
+
+int launch_dg_tet_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
+                           const double *xyz, const double *k_el, const double *D_el, double f,
+                           const long long *boff, const int *roff, double *val, double *rhs) {
+  if (count <= 0) return 0;
+  GB_CHECK(p >= 1 && p <= 4, "DG degree must be 1..4");
+  DgBatchTables tb;
+  const int r = dg_batch_tables(device, &tb);
+  if (r < 0) return r;
+  const int grid = (count + 31) / 32;
+#define GB_TET_LAUNCH(PP)                                                                                       \
+  dg_tet_elements_kernel<PP><<<grid, DGB_THREADS, 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, tb.T[PP], \
+                                                           tb.MOM[PP], boff, roff, val, rhs)
+  switch (p) {
+    case 1: GB_TET_LAUNCH(1); break;
+    case 2: GB_TET_LAUNCH(2); break;
+    case 3: GB_TET_LAUNCH(3); break;
+    default: GB_TET_LAUNCH(4); break;
+  }
+#undef GB_TET_LAUNCH
+  GB_CUDA(cudaGetLastError());
+  return 1;
 }
 
 // dynamic shared memory covering every class and variant

@@ -142,7 +142,7 @@ static int launch_dg_block_spmv_t(cudaStream_t st, int mode, int p, int count, c
                                   double *out) {
   if (count <= 0) return 0;
   GB_CHECK(mode >= 0 && mode <= 2, "bad block SpMV mode");
-  GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
+  GB_CHECK(p >= 1 && p <= 2 * GB_DG_PMAX, "DG block class must be 1..8 (prisms 1..4, tetrahedra 5..8)");
   GB_CHECK(mode == 2 || (dinv && dinv_off), "block SpMV needs the inverted diagonal blocks");
   const int grid = (count + DGS_ROWS - 1) / DGS_ROWS;
 #define GB_DGS_LAUNCH(PP)                                                                                      \
@@ -152,7 +152,11 @@ static int launch_dg_block_spmv_t(cudaStream_t st, int mode, int p, int count, c
     case 1: GB_DGS_LAUNCH(1); break;
     case 2: GB_DGS_LAUNCH(2); break;
     case 3: GB_DGS_LAUNCH(3); break;
-    default: GB_DGS_LAUNCH(4); break;
+    case 4: GB_DGS_LAUNCH(4); break;
+    case 5: GB_DGS_LAUNCH(5); break;
+    case 6: GB_DGS_LAUNCH(6); break;
+    case 7: GB_DGS_LAUNCH(7); break;
+    default: GB_DGS_LAUNCH(8); break;
   }
 #undef GB_DGS_LAUNCH
   GB_CUDA(cudaGetLastError());

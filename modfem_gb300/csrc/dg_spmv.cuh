@@ -27,9 +27,12 @@ constexpr int DGS_ROWS = DGS_THREADS / DGS_LANES;
 __device__ __forceinline__ double dgs_fma(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float dgs_fma(float a, float b, float c) { return fmaf(a, b, c); }
 
+// P: block class, 1..4 tensor-basis prisms of degree P (6, 18, 40, 75
+// functions), 5..8 complete-basis tetrahedra of degree P - 4 (4, 10, 20, 35)
 template <int P>
 struct DgSpmvDims {
-  static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
+  static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : P == 4 ? 75
+                          : P == 5 ? 4 : P == 6 ? 10 : P == 7 ? 20 : 35;
 };
 
 // The body of the block SpMV for the block rows of one CTA (blockDim.x ==

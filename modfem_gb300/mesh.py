@@ -334,3 +334,35 @@ def prism_faces(mesh, bc=1):
                      bc=arr[:, 2].astype(np.int32), el1=arr[:, 3].astype(np.int32),
                      el2=arr[:, 4].astype(np.int32), side1=arr[:, 5].astype(np.int32),
                      side2=arr[:, 6].astype(np.int32), nodes=arr[:, 7:11].astype(np.int32))
+
+
+# local faces of a tetrahedron: side k is the face opposite local vertex k
+TET_SIDES = ((1, 2, 3), (0, 2, 3), (0, 1, 3), (0, 1, 2))
+
+
+def tet_faces(mesh, bc=1):
+    """Face table of a tetrahedral mesh in the format of prism_faces: every
+    face once, el1 the lower-numbered neighbour and side1 its local face
+    (opposite vertex side1), nodes in el1's local order of that face; type 3;
+    bc on the boundary, -1 inside.  Faces ordered by (el1, side1)."""
+    el = np.asarray(mesh.el_nodes, np.int64)
+    nel = el.shape[0]
+    own = {}
+    rows = []
+    for e in range(nel):
+        for s, loc in enumerate(TET_SIDES):
+            v = el[e, list(loc)]
+            key = tuple(sorted(v.tolist()))
+            if key in own:
+                r = own.pop(key)
+                rows[r][4] = e
+                rows[r][6] = s
+                rows[r][2] = -1
+            else:
+                own[key] = len(rows)
+                rows.append([len(rows) + 1, 3, bc, e, -1, s, 0, v[0], v[1], v[2], -1])
+    arr = np.array(rows, dtype=np.int64)
+    return FaceTable(id=arr[:, 0].astype(np.int32), type=arr[:, 1].astype(np.int32),
+                     bc=arr[:, 2].astype(np.int32), el1=arr[:, 3].astype(np.int32),
+                     el2=arr[:, 4].astype(np.int32), side1=arr[:, 5].astype(np.int32),
+                     side2=arr[:, 6].astype(np.int32), nodes=arr[:, 7:11].astype(np.int32))

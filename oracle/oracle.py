@@ -305,3 +305,81 @@ def dg_tet_element(X, A, p, f=1.0):
     K = np.einsum("q,qwi,ij,quj->wu", wts * det, grad, A, grad)
     R = f * det * (wts @ phi)
     return K, R
+
+
+def _collapsed_tri_rule(n):
+    """n^2-point rule on the reference triangle (0,0), (1,0), (0,1) by the
+    collapsed map s = u, t = v (1 - u) of Gauss-Legendre points on [0,1]^2;
+    weights sum to 1/2; exact for degree <= 2n - 2."""
+    g, w = np.polynomial.legendre.leggauss(n)
+    g, w = 0.5 * (g + 1.0), 0.5 * w
+    U, V = np.meshgrid(g, g, indexing="ij")
+    WU, WV = np.meshgrid(w, w, indexing="ij")
+    return np.stack([U.ravel(), (V * (1.0 - U)).ravel()], 1), (WU * WV * (1.0 - U)).ravel()
+
+
+def _tet_basis_at(X, p, xs):
+    """Values (q, ns) and physical gradients (q, ns, 3) of the complete
+    monomial basis of the affine tetrahedron X (4 x 3) at physical points xs."""
+    J = np.stack([X[1] - X[0], X[2] - X[0], X[3] - X[0]], 1)
+    xi = np.linalg.solve(J, (xs - X[0]).T).T  # reference coordinates
+    E = np.array(tet_basis_exponents(p), float)
+    phi = np.prod(xi[:, None, :] ** E[None, :, :], axis=2)
+    d = np.zeros((len(xi), len(E), 3))
+    for a in range(3):
+        Ea = E.copy()
+        Ea[:, a] = np.maximum(Ea[:, a] - 1, 0)
+        d[:, :, a] = E[:, a] * np.prod(xi[:, None, :] ** Ea[None, :, :], axis=2)
+    return phi, d @ np.linalg.inv(J)  # grad_x = J^-T grad_xi (row vectors: d J^-1)
+
+
+def dg_tet_assemble(mesh, faces, pdeg, A, pen=10.0, g=0.0, f=1.0):
+    """DG system of an affine tetrahedral mesh with the interior-penalty form
+    of the prism DG weak form (pds_conv_diff_weakform_dg.c:232-1140): volume
+    blocks from dg_tet_element; per face, rows i (test, side s_i) and columns
+    j (trial, side s_j): a [ s_j phi_j (f g_i + s_i c phi_i) - s_i f phi_i g_j ]
+    with g = n . (A grad phi), f = 1/2 inside and 1 on (Dirichlet) boundary
+    faces, c = pen min(p1, p2) / sqrt(area) (pen p1 / sqrt(area) on the
+    boundary), n the unit normal out of el1; boundary rhs g_D a (g_i + c phi_i).
+    Quadrature: the collapsed rule above, exact at these degrees.  Returns
+    (blocks {(row el, col el): ns_r x ns_c}, rhs list per element)."""
+    X = np.asarray(mesh.coords)[np.asarray(mesh.el_nodes)]
+    A = np.asarray(A, float).reshape(-1, 3, 3)
+    blocks, rhs = {}, []
+    for e in range(X.shape[0]):
+        K, R = dg_tet_element(X[e], A[e], int(pdeg[e]), f=f)
+        blocks[(e, e)] = K
+        rhs.append(R.copy())
+    for k in range(faces.n):
+        e1, e2 = int(faces.el1[k]), int(faces.el2[k])
+        V = np.asarray(mesh.coords)[faces.nodes[k, :3]]
+        nrm = np.cross(V[1] - V[0], V[2] - V[0])
+        area = 0.5 * np.linalg.norm(nrm)
+        n = nrm / np.linalg.norm(nrm)
+        if np.dot(n, V.mean(0) - X[e1].mean(0)) < 0:
+            n = -n
+        sides = [e1] + ([e2] if e2 >= 0 else [])
+        pmax = max(int(pdeg[s]) for s in sides)
+        st, w = _collapsed_tri_rule(pmax + 2)
+        xs = V[0] + st[:, :1] * (V[1] - V[0]) + st[:, 1:] * (V[2] - V[0])
+        aw = w * 2.0 * area
+        if e2 >= 0:
+            fac, c = 0.5, pen * min(int(pdeg[e1]), int(pdeg[e2])) / np.sqrt(area)
+        else:
+            fac, c = 1.0, pen * int(pdeg[e1]) / np.sqrt(area)
+        val = {}
+        for s, e in enumerate(sides):
+            phi, grad = _tet_basis_at(X[e], int(pdeg[e]), xs)
+            gg = np.einsum("qjk,lk,l->qj", grad, A[e], n)  # n . (A grad phi)
+            val[e] = (1.0 if s == 0 else -1.0, phi, gg)
+        for ei in sides:
+            si, phi_i, g_i = val[ei]
+            for ej in sides:
+                sj, phi_j, g_j = val[ej]
+                Kf = np.einsum("q,qi,qj->ij", aw * sj, fac * g_i + si * c * phi_i, phi_j) \
+                    - np.einsum("q,qi,qj->ij", aw * si * fac, phi_i, g_j)
+                blocks[(ei, ej)] = blocks.get((ei, ej), 0.0) + Kf
+        if e2 < 0:
+            _, phi1, g1 = val[e1]
+            rhs[e1] += g * np.einsum("q,qi->i", aw, g1 + c * phi1)
+    return blocks, rhs

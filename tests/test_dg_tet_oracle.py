@@ -88,3 +88,42 @@ def test_constant_and_linear_reproduction(p):
     lin = K @ c
     K1, _ = O.dg_tet_element(X, A, 1)
     assert np.allclose(lin[:4], K1 @ c[:4], rtol=0, atol=1e-13 * scale)
+
+
+def _tet_system(n, seed, pmax=4):
+    from modfem_gb300.mesh import anisotropic_tensors, structured_tet_mesh, tet_faces
+    t = structured_tet_mesh(n, jitter=0.2, seed=seed)
+    F = tet_faces(t)
+    p = np.random.default_rng(seed).integers(1, pmax + 1, t.nel)
+    A = anisotropic_tensors(t.nel, seed=seed + 1).reshape(-1, 3, 3)
+    return t, F, p, A
+
+
+def test_tet_face_table():
+    from modfem_gb300.mesh import TET_SIDES, structured_tet_mesh, tet_faces
+    n = 3
+    t = structured_tet_mesh(n)
+    F = tet_faces(t)
+    assert F.n == (4 * t.nel + 12 * n * n) // 2           # every face twice but the 12 n^2 boundary ones
+    assert int((F.el2 < 0).sum()) == 12 * n * n
+    for k in range(F.n):                                     # nodes: el1's face, and el2's too
+        assert sorted(F.nodes[k, :3]) == sorted(t.el_nodes[F.el1[k], list(TET_SIDES[F.side1[k]])])
+        if F.el2[k] >= 0:
+            assert set(F.nodes[k, :3]) <= set(t.el_nodes[F.el2[k]])
+
+
+def test_tet_dg_oracle_reproduces_constants():
+    """With f = 0 and Dirichlet value c the constant solves the interior-
+    penalty system exactly (consistency of the face terms)."""
+    t, F, p, A = _tet_system(2, 3)
+    B, R = O.dg_tet_assemble(t, F, p, A, pen=10.0, g=0.7, f=0.0)
+    ns = [(q + 1) * (q + 2) * (q + 3) // 6 for q in p]
+    scale = max(np.abs(r).max() for r in R)
+    for e in range(t.nel):
+        acc = -R[e].copy()
+        for (i, j), K in B.items():
+            if i == e:
+                x = np.zeros(ns[j])
+                x[0] = 0.7
+                acc += K @ x
+        assert np.abs(acc).max() < 1e-12 * scale
