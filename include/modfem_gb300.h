@@ -147,12 +147,16 @@ int gbfem_set_matrix(gbfem_ctx ctx, const double *crs_val, const double *rhs);
 /* ---------------------------------------------------------------------- */
 /* DG prisms (apd_dg_prism)                                                 */
 /* ---------------------------------------------------------------------- */
-/* Per-element degree p = 1..4 of the tensor monomial DG basis (ModFEM pdeg
- * 101 p, (p+1)^2(p+2)/2 = 6/18/40/75 functions; apr_get_el_pdeg_numshap,
- * apd_dg_prism/aps_dg_prism_intf.c:725-775).  The mesh must be prisms;
- * coefficients from gbfem_set_coefficients (a tensor must be symmetric). */
+/* Per-element degree p = 1..4 of the tensor monomial DG basis on prisms
+ * (ModFEM pdeg 101 p, (p+1)^2(p+2)/2 = 6/18/40/75 functions;
+ * apr_get_el_pdeg_numshap, apd_dg_prism/aps_dg_prism_intf.c:725-775).  On a
+ * tetrahedral mesh the complete monomial basis xi^a eta^b zeta^c,
+ * a+b+c <= p, (p+1)(p+2)(p+3)/6 = 4/10/20/35 functions (no reference
+ * counterpart: apd_dg_prism is prism-only), with the same weak form.
+ * Coefficients from gbfem_set_coefficients (a tensor must be symmetric). */
 int gbfem_dg_set_degrees(gbfem_ctx ctx, const int *p_el);
-/* Face table of the mesh, the data the DG weak form reads per face through
+/* Face table of the mesh (on tetrahedral meshes: triangles, side k = the
+ * face opposite local vertex k), the data the DG weak form reads per face through
  * mmr_fa_type (mmd_prism/mms_prism_datstr.c:969), mmr_fa_bc (:993),
  * mmr_fa_eq_neig (:1140) and mmr_fa_node_coor (:1488): type 3 (triangle) or
  * 4 (quadrilateral); bc flag; two neighbours per face (0-based, second -1 on

@@ -24,7 +24,9 @@ namespace gbfem {
 static __device__ const double tt_fq[GB_DG_PMAX][2][GB_DG_MAXNQF][3] = GB_DG_FQ_INIT;
 static __device__ const int tt_nqf[GB_DG_PMAX + 1][2] = GB_DG_NQF_INIT;
 
-constexpr int TT_THREADS = 128;
+// threads per CTA by the owner's degree: the diagonal share has NS^2 = 16,
+// 100, 400, 1225 entries
+__host__ __device__ constexpr int tt_threads(int p) { return p == 1 ? 32 : p == 2 ? 64 : p == 3 ? 128 : 256; }
 constexpr int TT_NQ = 16;   // points of the triangle rule for p = 4
 constexpr int TT_NS = 35;   // functions for p = 4
 constexpr int TT_NCOL = 2 * TT_NS;
@@ -47,7 +49,7 @@ __device__ __forceinline__ v3 tt_face_v(const double *X, const double *A, v3 n) 
   return {v3_dot(c1, an) * rdet, v3_dot(c2, an) * rdet, v3_dot(c3, an) * rdet};
 }
 
-template <int P>
+template <int P, int TT_THREADS = tt_threads(P)>
 __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
@@ -59,6 +61,7 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
   __shared__ double sPhi[TT_NQ][TT_NCOL], sGam[TT_NQ][TT_NCOL];
   __shared__ double sX[2][12], sA[2][9], sV[2][3], sAw[TT_NQ], sC[2];  // sC: |ds|, penalty factor
   __shared__ unsigned char sExp[TT_NS][3];
+  __shared__ double sFac[TT_NQ][2][30];  // monomial factors per point and side (dg_point_factors)
   const int bi = blockIdx.x;
   if (bi >= count) return;
   const int e = ent_el[bi];
@@ -87,17 +90,19 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
     const int pr = interior && p2 > p1 ? p2 : p1;
     const int nq = tt_nqf[pr][0];
     __syncthreads();  // shared arrays of the previous face are free
-    if (tid < 24) {
-      const int s = tid / 12, r = tid % 12;
-      if (s == 0 || interior) {
-        const int el = s ? F.el2 : F.el1;
-        sX[s][r] = xyz[3 * (size_t)el_nodes[4 * (size_t)el + r / 3] + r % 3];
-      }
-    } else if (tid < 42) {
-      const int t = tid - 24, s = t / 9, r = t % 9;
-      if (s == 0 || interior) {
-        const int el = s ? F.el2 : F.el1;
-        sA[s][r] = D_el ? D_el[9 * (size_t)el + r] : ((r % 4 == 0) ? (k_el ? k_el[el] : 1.0) : 0.0);
+    for (int t = tid; t < 42; t += TT_THREADS) {
+      if (t < 24) {
+        const int s = t / 12, r = t % 12;
+        if (s == 0 || interior) {
+          const int el = s ? F.el2 : F.el1;
+          sX[s][r] = xyz[3 * (size_t)el_nodes[4 * (size_t)el + r / 3] + r % 3];
+        }
+      } else {
+        const int u = t - 24, s = u / 9, r = u % 9;
+        if (s == 0 || interior) {
+          const int el = s ? F.el2 : F.el1;
+          sA[s][r] = D_el ? D_el[9 * (size_t)el + r] : ((r % 4 == 0) ? (k_el ? k_el[el] : 1.0) : 0.0);
+        }
       }
     }
     __syncthreads();
@@ -130,33 +135,28 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
       }
     }
     __syncthreads();
-    if (tid < nq) sAw[tid] = sC[0] * tt_fq[pr - 1][0][tid][2];
+    for (int q = tid; q < nq; q += TT_THREADS) sAw[q] = sC[0] * tt_fq[pr - 1][0][q][2];
+    // per (point, side): the point in that side's reference coordinates and
+    // the factor table x_k^m, m x_k^(m-1) v_k
+    for (int t = tid; t < 2 * nq; t += TT_THREADS) {
+      const int q = t >> 1, sd = t & 1;
+      if (sd == 1 && !interior) continue;
+      const double *fq = tt_fq[pr - 1][0][q];
+      const double w[3] = {1.0 - fq[0] - fq[1], fq[0], fq[1]};
+      const unsigned char *loc = sd == 0 ? F.loc1 : F.loc2;
+      v3 ev = {0, 0, 0};
+#pragma unroll
+      for (int i = 0; i < 3; i++) ev = v3_fma(w[i], tt_vertex_local(loc[i]), ev);
+      dg_point_factors(ev, v3{sV[sd][0], sV[sd][1], sV[sd][2]}, sFac[q][sd]);
+    }
     const double fac = interior ? 0.5 : 1.0;
     const int nsum = ns1 + ns2;
     __syncthreads();
     for (int t = tid; t < nq * nsum; t += TT_THREADS) {
       const int q = t / nsum, j = t - q * nsum;
       const int side = j < ns1 ? 0 : 1, jj = side == 0 ? j : j - ns1;
-      const double *fq = tt_fq[pr - 1][0][q];
-      const double w[3] = {1.0 - fq[0] - fq[1], fq[0], fq[1]};
-      const unsigned char *loc = side == 0 ? F.loc1 : F.loc2;
-      v3 ev = {0, 0, 0};
-#pragma unroll
-      for (int i = 0; i < 3; i++) ev = v3_fma(w[i], tt_vertex_local(loc[i]), ev);
-      const int a = sExp[jj][0], b = sExp[jj][1], c = sExp[jj][2];
-      double px[GB_DG_PMAX + 1], py[GB_DG_PMAX + 1], pz[GB_DG_PMAX + 1];
-      px[0] = py[0] = pz[0] = 1.0;
-#pragma unroll
-      for (int m = 1; m <= GB_DG_PMAX; m++) {
-        px[m] = px[m - 1] * ev.x;
-        py[m] = py[m - 1] * ev.y;
-        pz[m] = pz[m - 1] * ev.z;
-      }
-      const double phi = px[a] * py[b] * pz[c];
-      const double gx = a ? a * px[a - 1] * py[b] * pz[c] : 0.0;
-      const double gy = b ? b * px[a] * py[b - 1] * pz[c] : 0.0;
-      const double gz = c ? c * px[a] * py[b] * pz[c - 1] : 0.0;
-      const double g = fma(sV[side][0], gx, fma(sV[side][1], gy, sV[side][2] * gz));
+      double phi, g;
+      dg_basis_from_factors(sFac[q][side], sExp[jj][0], sExp[jj][1], sExp[jj][2], phi, g);
       sPhi[q][j] = side == 1 ? -phi : phi;
       sGam[q][j] = g;
       if (side == own2) {
@@ -211,8 +211,9 @@ int launch_dg_tet_faces(cudaStream_t st, int p, int count, const int *ent_el, co
   if (count <= 0) return 0;
   GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
 #define GB_TT_LAUNCH(PP)                                                                                        \
-  dg_tet_faces_kernel<PP><<<count, TT_THREADS, 0, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, xyz, k_el, \
-                                                        D_el, pen, g, boff_diag, roff, val, rhs)
+  dg_tet_faces_kernel<PP><<<count, tt_threads(PP), 0, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, xyz,    \
+                                                            k_el,                                             \
+                                                            D_el, pen, g, boff_diag, roff, val, rhs)
   switch (p) {
     case 1: GB_TT_LAUNCH(1); break;
     case 2: GB_TT_LAUNCH(2); break;

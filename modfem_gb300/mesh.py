@@ -347,22 +347,32 @@ def tet_faces(mesh, bc=1):
     bc on the boundary, -1 inside.  Faces ordered by (el1, side1)."""
     el = np.asarray(mesh.el_nodes, np.int64)
     nel = el.shape[0]
-    own = {}
-    rows = []
-    for e in range(nel):
-        for s, loc in enumerate(TET_SIDES):
-            v = el[e, list(loc)]
-            key = tuple(sorted(v.tolist()))
-            if key in own:
-                r = own.pop(key)
-                rows[r][4] = e
-                rows[r][6] = s
-                rows[r][2] = -1
-            else:
-                own[key] = len(rows)
-                rows.append([len(rows) + 1, 3, bc, e, -1, s, 0, v[0], v[1], v[2], -1])
-    arr = np.array(rows, dtype=np.int64)
-    return FaceTable(id=arr[:, 0].astype(np.int32), type=arr[:, 1].astype(np.int32),
-                     bc=arr[:, 2].astype(np.int32), el1=arr[:, 3].astype(np.int32),
-                     el2=arr[:, 4].astype(np.int32), side1=arr[:, 5].astype(np.int32),
-                     side2=arr[:, 6].astype(np.int32), nodes=arr[:, 7:11].astype(np.int32))
+    sides = np.array(TET_SIDES)
+    verts = el[:, sides]                        # (nel, 4, 3) in local face order
+    key = np.sort(verts, axis=2).reshape(-1, 3)
+    owner = np.repeat(np.arange(nel), 4)
+    side = np.tile(np.arange(4), nel)
+    order = np.lexsort((owner, key[:, 2], key[:, 1], key[:, 0]))
+    ks = key[order]
+    same = np.all(ks[1:] == ks[:-1], axis=1)
+    first = np.ones(len(order), bool)
+    first[1:] = ~same
+    second = np.zeros(len(order), bool)
+    second[:-1] = same                          # the next entry is this face's second neighbour
+    idx1 = order[first]
+    has2 = second[first]
+    idx2 = np.full(idx1.size, -1)
+    pos_first = np.nonzero(first)[0]
+    idx2[has2] = order[pos_first[has2] + 1]
+    e1, s1 = owner[idx1], side[idx1]
+    e2 = np.where(idx2 >= 0, owner[np.maximum(idx2, 0)], -1)
+    s2 = np.where(idx2 >= 0, side[np.maximum(idx2, 0)], 0)
+    srt = np.lexsort((s1, e1))
+    e1, s1, e2, s2 = e1[srt], s1[srt], e2[srt], s2[srt]
+    nodes = np.full((e1.size, 4), -1, np.int64)
+    nodes[:, :3] = verts[e1, s1]
+    n = e1.size
+    return FaceTable(id=np.arange(1, n + 1, dtype=np.int32), type=np.full(n, 3, np.int32),
+                     bc=np.where(e2 >= 0, -1, bc).astype(np.int32), el1=e1.astype(np.int32),
+                     el2=e2.astype(np.int32), side1=s1.astype(np.int32), side2=s2.astype(np.int32),
+                     nodes=nodes.astype(np.int32))
