@@ -82,6 +82,13 @@ int gbfem_destroy(gbfem_ctx c) {
   if (!c) return 0;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+    for (auto &ev : c->pipe_ev)
+      if (ev) cudaEventDestroy(ev);
+  }
+  c->row_last.release();
   DevBuf<double> *dbufs[] = {&c->xyz, &c->k_el, &c->D_el, &c->val, &c->rhs, &c->dinv, &c->V,
                              &c->w, &c->tmp, &c->x, &c->b, &c->partial, &c->hcol};
   for (auto *b : dbufs) b->release();
@@ -360,6 +367,65 @@ static int stage_input(gbfem_ctx c, int slot, DevBuf<int> &d, const int *h, long
   return 0;
 }
 
+// last element (position within the element range) touching each row: the
+// rows of an element's rhs positions and of its value positions (found in
+// row_ptr); entries outside the structure are left to the element kernels
+__global__ void row_last_kernel(int count, const int *__restrict__ pos, const int *__restrict__ table, int nv,
+                                int ndof, const int *__restrict__ row_ptr, int *row_last) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int *t = table + pos[i];
+  const int nnz = row_ptr[ndof];
+  for (int j = 0; j < nv; j++) {
+    const int r = t[nv * nv + j];
+    if (r >= 0 && r < ndof) atomicMax(row_last + r, i);
+  }
+  for (int j = 0; j < nv * nv; j++) {
+    const int q = t[j];
+    if (q < 0 || q >= nnz) continue;
+    int lo = 0, hi = ndof;  // row_ptr[lo] <= q < row_ptr[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (row_ptr[mid] <= q) lo = mid;
+      else hi = mid;
+    }
+    atomicMax(row_last + lo, i);
+  }
+}
+
+// Chunks of the element range and, per chunk, the number of leading rows that
+// no later element touches (dof order by first appearance makes rows finish
+// roughly in element order); built once per cached set of tables.
+static int build_pipe_plan(gbfem_ctx c, int e0, int e1) {
+  const int count = e1 - e0, nd = c->ndof;
+  GB_TRY(c->row_last.alloc((size_t)nd));
+  GB_CUDA(cudaMemsetAsync(c->row_last.p, 0xFF, (size_t)nd * sizeof(int), c->stream));
+  row_last_kernel<<<(count + 255) / 256, 256, 0, c->stream>>>(count, c->in_pos.p + e0, c->in_table.p, c->nv, nd,
+                                                              c->row_ptr.p, c->row_last.p);
+  GB_CUDA(cudaGetLastError());
+  std::vector<int> last(nd);
+  GB_CUDA(cudaMemcpyAsync(last.data(), c->row_last.p, (size_t)nd * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  for (int r = 1; r < nd; r++) last[r] = std::max(last[r], last[r - 1]);  // prefix maximum
+  const int K = std::max(1, std::min(8, count / 65536));
+  c->pipe_el.assign(K + 1, 0);
+  c->pipe_rows.assign(K, nd);
+  for (int k = 0; k <= K; k++) c->pipe_el[k] = (int)((long long)count * k / K);
+  for (int k = 0; k + 1 < K; k++)
+    c->pipe_rows[k] = (int)(std::upper_bound(last.begin(), last.end(), c->pipe_el[k + 1] - 1) - last.begin());
+  if (!c->copy_stream) {
+    GB_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (auto &ev : c->pipe_ev) GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  for (int i = 0; i < 3; i++) {
+    c->pipe_key[i] = c->cache_key[i];
+    c->pipe_len[i] = c->cache_len[i];
+  }
+  c->pipe_e0 = e0;
+  c->pipe_e1 = e1;
+  return 0;
+}
+
 int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, const int *Pdeg_coarse_p,
                                     int Nr_int_ent, const int *L_int_ent_type, const int *L_int_ent_id,
                                     int Nr_colors_elems, const int *L_color_index_elems, int Nr_colors_faces,
@@ -425,19 +491,57 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   }
   cudaEventRecord(c->ev2, c->stream);
   GB_CHECK(c->nv == GBFEM_PRISM || !c->aniso, "std tetrahedra take an isotropic k_el (tensors: prisms and DG)");
-  if (c->nv == GBFEM_PRISM)
-    r = gbfem::launch_prism_elements(c->stream, true, c->aniso, e1 - e0, c->in_id.p + e0, 1, c->in_pos.p + e0,
-                                     c->nel, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->in_table.p,
-                                     c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p);
-  else
-    r = gbfem::launch_tet_elements(c->stream, true, e1 - e0, c->in_id.p + e0, 1, c->in_pos.p + e0, c->nel,
-                                   c->el_nodes.p, c->xyz.p, c->k_el.p, c->f, c->in_table.p, c->val.p, c->rhs.p,
-                                   do_sm, do_rhs, c->err.p);
-  GB_TRY(r);
-  launches += r;
-  cudaEventRecord(c->ev3, c->stream);
-  if (crs_val) GB_CUDA(cudaMemcpyAsync(crs_val, c->val.p, c->val.bytes(), cudaMemcpyDeviceToHost, c->stream));
-  if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->rhs.p, c->rhs.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  auto elements = [&](int a, int b) -> int {
+    if (b <= a) return 0;
+    if (c->nv == GBFEM_PRISM)
+      return gbfem::launch_prism_elements(c->stream, true, c->aniso, b - a, c->in_id.p + a, 1, c->in_pos.p + a,
+                                          c->nel, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,
+                                          c->in_table.p, c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p);
+    return gbfem::launch_tet_elements(c->stream, true, b - a, c->in_id.p + a, 1, c->in_pos.p + a, c->nel,
+                                      c->el_nodes.p, c->xyz.p, c->k_el.p, c->f, c->in_table.p, c->val.p, c->rhs.p,
+                                      do_sm, do_rhs, c->err.p);
+  };
+  // with cached tables and host outputs: element chunks, each chunk's
+  // finished rows downloaded while the next chunk runs
+  bool pipe = c->cache_tables && (crs_val || rhs) && e1 > e0;
+  if (pipe) {
+    bool same = c->pipe_e0 == e0 && c->pipe_e1 == e1;
+    for (int i = 0; i < 3; i++) same = same && c->pipe_key[i] == c->cache_key[i] && c->pipe_len[i] == c->cache_len[i];
+    if (!same) GB_TRY(build_pipe_plan(c, e0, e1));
+  }
+  if (pipe) {
+    const int K = (int)c->pipe_el.size() - 1;
+    const int *rp = c->hs.row_ptr.data();
+    // all chunks first: a copy into pageable memory returns only when done
+    for (int k = 0; k < K; k++) {
+      GB_TRY(r = elements(e0 + c->pipe_el[k], e0 + c->pipe_el[k + 1]));
+      launches += r;
+      GB_CUDA(cudaEventRecord(c->pipe_ev[k], c->stream));
+    }
+    cudaEventRecord(c->ev3, c->stream);
+    int rprev = 0;
+    for (int k = 0; k < K; k++) {
+      GB_CUDA(cudaStreamWaitEvent(c->copy_stream, c->pipe_ev[k], 0));
+      const int r1 = k + 1 < K ? c->pipe_rows[k] : c->ndof;
+      if (r1 > rprev) {
+        if (crs_val)
+          GB_CUDA(cudaMemcpyAsync(crs_val + rp[rprev], c->val.p + rp[rprev], (size_t)(rp[r1] - rp[rprev]) * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->copy_stream));
+        if (rhs)
+          GB_CUDA(cudaMemcpyAsync(rhs + rprev, c->rhs.p + rprev, (size_t)(r1 - rprev) * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->copy_stream));
+        rprev = r1;
+      }
+    }
+    GB_CUDA(cudaEventRecord(c->pipe_ev[K], c->copy_stream));
+    GB_CUDA(cudaStreamWaitEvent(c->stream, c->pipe_ev[K], 0));
+  } else {
+    GB_TRY(r = elements(e0, e1));
+    launches += r;
+    cudaEventRecord(c->ev3, c->stream);
+    if (crs_val) GB_CUDA(cudaMemcpyAsync(crs_val, c->val.p, c->val.bytes(), cudaMemcpyDeviceToHost, c->stream));
+    if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->rhs.p, c->rhs.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  }
   cudaEventRecord(c->ev1, c->stream);
   GB_TRY(check_err_flag(c));
   cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);

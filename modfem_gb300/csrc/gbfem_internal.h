@@ -208,6 +208,16 @@ struct gbfem_ctx_s {
   const void *cache_key[3] = {nullptr, nullptr, nullptr};
   long long cache_len[3] = {0, 0, 0};
   int cache_tables = 0;
+  // pipelined download of the drop-in call while the tables are cached:
+  // element chunks, and per chunk the rows no later element touches, copied
+  // on copy_stream while the next chunk runs
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t pipe_ev[9] = {};
+  gbfem::DevBuf<int> row_last;
+  const void *pipe_key[3] = {nullptr, nullptr, nullptr};
+  long long pipe_len[3] = {0, 0, 0};
+  int pipe_e0 = -1, pipe_e1 = -1;
+  std::vector<int> pipe_el, pipe_rows;
   // Krylov workspace
   gbfem::DevBuf<double> V, w, tmp, x, b, partial, hcol;
   // DG prisms: per-element degree, block-CRS structure (block row = element)

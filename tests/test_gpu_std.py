@@ -123,6 +123,47 @@ def test_dropin_table_cache(gb):
     assert crs_rel_err(g["row_ptr"], val, vo, sc) < REL_TOL
 
 
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_dropin_pipelined_download(gb, shuffle):
+    """With cached tables the drop-in runs the elements in chunks and copies
+    each chunk's finished rows while the next runs: 250,000 prisms (three
+    chunks) give the values of the one-shot call, also with the elements in
+    shuffled order (rows then finish late) and with the rhs alone."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(50, jitter=0.2, seed=3)
+    k = lognormal_k(m.nel, seed=3)
+    c = make_ctx(gb, m, k)
+    nd, nnz, _ = c.build_structure()
+    tables = c.get_element_tables()
+    order = np.random.default_rng(5).permutation(m.nel) if shuffle else np.arange(m.nel)
+    fa_tab = tables.reshape(m.nel, 42)[m.bc_face_el].reshape(-1)
+    ids = np.concatenate([order + 1, m.bc_face_id]).astype(np.int32)
+    types = np.concatenate([np.full(m.nel, gb.ELEMENT), np.full(m.bc_face_id.size, gb.FACE)]).astype(np.int32)
+    table = np.concatenate([tables.reshape(m.nel, 42)[order].reshape(-1), fa_tab]).astype(np.int32)
+    pos = (np.arange(ids.size) * 42).astype(np.int32)
+    ce = np.array([0, m.nel], np.int32)
+    cf = np.array([m.nel, ids.size], np.int32)
+    args = (types, ids, ce, cf, pos, table)
+    v1, r1 = np.zeros(nnz), np.zeros(nd)
+    c.create_assemble_stiff_mat(*args, crs_val=v1, rhs=r1)  # one shot
+    c.set_option(gb.OPT_CACHE_TABLES, 1)
+    for _ in range(2):  # plan built on the first call, reused on the second
+        v2, r2 = np.full(nnz, np.nan), np.full(nd, np.nan)
+        c.create_assemble_stiff_mat(*args, crs_val=v2, rhs=r2)
+        sc = np.max(np.abs(v1))
+        assert np.max(np.abs(v2 - v1)) <= 1e-12 * sc
+        assert np.max(np.abs(r2 - r1)) <= 1e-12 * np.max(np.abs(r1))
+    _, _, launches = c.last_timing()
+    assert launches == 1 + 3
+    r3 = np.full(nd, np.nan)
+    c.create_assemble_stiff_mat(*args, crs_val=None, rhs=r3)
+    assert np.max(np.abs(r3 - r1)) <= 1e-12 * np.max(np.abs(r1))
+    dn, rp, ci = c.get_crs_structure()
+    vo, ro, _ = O.std_prism_assemble(m, k, dn, rp, ci, nthreads=8)
+    assert crs_rel_err(rp, v2, vo, energy_scale(rp, ci, vo)) < REL_TOL
+    assert vec_rel_err(r2, ro) < REL_TOL
+
+
 def test_dropin_rejects_bad_entities_and_recovers(gb):
     g = load("std_n4")
     m = FixtureMesh(g)
