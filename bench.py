@@ -53,10 +53,11 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help=argparse.SUPPRESS)
-    p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "batch"], default=None,
+    p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "batch", "std", "std_dw"], default=None,
                    help="small cases for ncu captures: DG p=3 anisotropic (n^3 x 2 prisms, --n), 3 assemblies "
                         "(FP64, tensor-core volume, or tensor-core volume and faces) and one block residual; or the mixed batch "
-                        "(40,000 prisms + 30,000 tetrahedra, p 1..4), 3 runs")
+                        "(40,000 prisms + 30,000 tetrahedra, p 1..4), 3 runs; or the std prism assembly "
+                        "(FP64 or double-word element arithmetic, n^3 x 2 prisms), 3 assemblies")
     return p.parse_args()
 
 
@@ -65,6 +66,20 @@ def run_profile_case(args):
     block SpMV); prints its CUDA-event timings."""
     import modfem_gb300 as gb
     from modfem_gb300.mesh import anisotropic_tensors, prism_faces, structured_prism_mesh
+    if args.profile in ("std", "std_dw"):
+        m, k = make_problem(args.n)
+        c = gb.Context(0)
+        c.set_mesh(m)
+        c.set_coefficients(k=k, f=1.0, g=0.0, penalty=1e7)
+        c.build_structure()
+        c.set_option(gb.OPT_STD_ARITH, gb.STD_DWORD if args.profile == "std_dw" else gb.STD_FP64)
+        ms = []
+        for _ in range(3):
+            c.assemble(gb.SCATTER_ATOMIC)
+            ms.append(c.last_timing()[:2])
+        print(json.dumps({"profile_case": args.profile, "elements": m.nel, "timing_ms": ms}))
+        c.close()
+        return
     if args.profile == "batch":
         from modfem_gb300.mesh import lognormal_k, structured_tet_mesh
         NP, NT = 40_000, 30_000
@@ -659,6 +674,37 @@ def main():
     el_ms_step = max_over_ranks(el_ms / args.steps, ws)
     value = ws * m.nel / (ms_step * 1e-3)
 
+    # ---------------- double-word element arithmetic (float pairs) ----------------
+    v64, r64 = c.get_matrix()
+    c.set_option(gb.OPT_STD_ARITH, gb.STD_DWORD)
+    for _ in range(args.warmup):
+        c.assemble(gb.SCATTER_ATOMIC)
+    dw_tot, dw_el, dw_launches = 0.0, 0.0, 0
+    for _ in range(args.steps):
+        c.assemble(gb.SCATTER_ATOMIC)
+        a, b, nl = c.last_timing()
+        dw_tot += a
+        dw_el += b
+        dw_launches += nl
+    dw_ms = max_over_ranks(dw_tot / args.steps, ws)
+    dw_el_ms = max_over_ranks(dw_el / args.steps, ws)
+    vdw, rdw = c.get_matrix()
+    c.set_option(gb.OPT_STD_ARITH, gb.STD_FP64)
+    dn_, rp_, ci_ = c.get_crs_structure()
+    rows_ = np.repeat(np.arange(nd), np.diff(rp_))
+    dg_ = np.abs(v64[rows_ == ci_])
+    diag_ = np.zeros(nd)
+    diag_[rows_[rows_ == ci_]] = dg_
+    escale = np.sqrt(diag_[rows_] * diag_[ci_])
+    double_word = {
+        "value": ws * m.nel / (dw_ms * 1e-3), "unit": UNIT, "ms_per_step": dw_ms, "element_kernel_ms": dw_el_ms,
+        "speedup_vs_plain_fp64": ms_step / dw_ms, "element_kernel_speedup": el_ms_step / dw_el_ms,
+        "max_rel_err_vs_fp64_energy_scale": float(np.max(np.abs(vdw - v64) / np.where(escale > 0, escale, 1.0))),
+        "max_abs_err_vs_fp64_over_max_entry": float(np.max(np.abs(vdw - v64)) / np.max(np.abs(v64))),
+        "rhs_max_rel_err_vs_fp64": float(np.max(np.abs(rdw - r64)) / np.max(np.abs(r64))),
+        "launches": dw_launches}
+    del rows_, escale, diag_, dg_
+
     # ---------------- end to end through the drop-in C ABI ----------------
     tables = c.get_element_tables()
     fa_tab = tables.reshape(m.nel, 42)[m.bc_face_el].reshape(-1)
@@ -754,6 +800,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_s * 1e3},
         "clocks": clocks,
+        "double_word": double_word,
         "solver": solver,
         "structure": structure,
         "dg": dg,

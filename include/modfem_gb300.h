@@ -57,8 +57,17 @@ long long gbfem_device_bytes(gbfem_ctx ctx);
  * device copies of the entity lists and assembly table between calls and
  * skips their upload while the caller passes the same pointers and sizes;
  * the caller promises not to change their contents, as holds in ModFEM
- * between sir_create and sir_free. */
+ * between sir_create and sir_free.
+ * GBFEM_OPT_STD_ARITH: arithmetic of the std prism element matrices with an
+ * isotropic coefficient (gbfem_assemble and the drop-in), GBFEM_STD_FP64
+ * (default) or GBFEM_STD_DWORD: double-word float pairs on the FP32 pipe
+ * (about 48 significant bits; entries within about 1e-14 of the FP64 ones,
+ * vertex differences and the global assembly sums stay FP64).  Tensor
+ * coefficients and tetrahedra always take FP64. */
 #define GBFEM_OPT_CACHE_TABLES 1
+#define GBFEM_OPT_STD_ARITH 2
+#define GBFEM_STD_FP64 0
+#define GBFEM_STD_DWORD 1
 int gbfem_set_option(gbfem_ctx ctx, int option, long long value);
 
 /* ---------------------------------------------------------------------- */

@@ -17,6 +17,8 @@ ELEMENT, FACE = 4, 3
 COMP_SM, COMP_RHS, COMP_BOTH = 1, 2, 3
 SCATTER_ATOMIC, SCATTER_COLOR = 0, 1
 OPT_CACHE_TABLES = 1
+OPT_STD_ARITH = 2
+STD_FP64, STD_DWORD = 0, 1
 DG_VOLUME_FP64, DG_VOLUME_TC, DG_VOLUME_TF32 = 0, 1, 2
 DG_FACE_FP64, DG_FACE_TC = 0, 1
 

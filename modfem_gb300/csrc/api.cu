@@ -156,6 +156,11 @@ int gbfem_set_option(gbfem_ctx c, int option, long long value) {
     }
     return 0;
   }
+  if (option == GBFEM_OPT_STD_ARITH) {
+    GB_CHECK(value == GBFEM_STD_FP64 || value == GBFEM_STD_DWORD, "std arithmetic must be FP64 or DWORD");
+    c->std_dword = value == GBFEM_STD_DWORD;
+    return 0;
+  }
   set_error("unknown option");
   return -2;
 }
@@ -496,7 +501,8 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     if (c->nv == GBFEM_PRISM)
       return gbfem::launch_prism_elements(c->stream, true, c->aniso, b - a, c->in_id.p + a, 1, c->in_pos.p + a,
                                           c->nel, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,
-                                          c->in_table.p, c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p);
+                                          c->in_table.p, c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p,
+                                          c->std_dword);
     return gbfem::launch_tet_elements(c->stream, true, b - a, c->in_id.p + a, 1, c->in_pos.p + a, c->nel,
                                       c->el_nodes.p, c->xyz.p, c->k_el.p, c->f, c->in_table.p, c->val.p, c->rhs.p,
                                       do_sm, do_rhs, c->err.p);
@@ -585,7 +591,7 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
     if (c->nv == GBFEM_PRISM)
       r = gbfem::launch_prism_elements(c->stream, true, c->aniso, c->nel, nullptr, 0, nullptr, c->nel,
                                        c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->el_table.p,
-                                       c->val.p, c->rhs.p, 1, 1, c->err.p);
+                                       c->val.p, c->rhs.p, 1, 1, c->err.p, c->std_dword);
     else
       r = gbfem::launch_tet_elements(c->stream, true, c->nel, nullptr, 0, nullptr, c->nel, c->el_nodes.p,
                                      c->xyz.p, c->k_el.p, c->f, c->el_table.p, c->val.p, c->rhs.p, 1, 1,
@@ -598,7 +604,7 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
       if (c->nv == GBFEM_PRISM)
         r = gbfem::launch_prism_elements(c->stream, false, c->aniso, hi - lo, c->el_perm.p + lo, 0, nullptr,
                                          c->nel, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,
-                                         c->el_table.p, c->val.p, c->rhs.p, 1, 1, c->err.p);
+                                         c->el_table.p, c->val.p, c->rhs.p, 1, 1, c->err.p, c->std_dword);
       else
         r = gbfem::launch_tet_elements(c->stream, false, hi - lo, c->el_perm.p + lo, 0, nullptr, c->nel,
                                        c->el_nodes.p, c->xyz.p, c->k_el.p, c->f, c->el_table.p, c->val.p,

@@ -94,7 +94,8 @@ void color_entities(int nent, int nv, const std::vector<int> &ent_dofs, int nd, 
 int launch_prism_elements(cudaStream_t st, bool atomic, bool aniso, int count, const int *ent_el,
                           int el_base, const int *ent_pos, int nel, const int *el_nodes,
                           const double *xyz, const double *k_el, const double *D_el, double f,
-                          const int *tab, double *val, double *rhs, int do_sm, int do_rhs, int *err);
+                          const int *tab, double *val, double *rhs, int do_sm, int do_rhs, int *err,
+                          bool dword = false);
 int launch_prism_faces(cudaStream_t st, bool atomic, int count, const int *ent_fa, int fa_base,
                        const int *fa_map, int fa_map_len, const int *ent_pos, int nfa,
                        const int *fa_el, const int *fa_side, const int *el_nodes,
@@ -208,6 +209,7 @@ struct gbfem_ctx_s {
   const void *cache_key[3] = {nullptr, nullptr, nullptr};
   long long cache_len[3] = {0, 0, 0};
   int cache_tables = 0;
+  bool std_dword = false;  // std prism elements in double-word arithmetic
   // pipelined download of the drop-in call while the tables are cached:
   // element chunks, and per chunk the rows no later element touches, copied
   // on copy_stream while the next chunk runs

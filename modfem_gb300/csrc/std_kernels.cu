@@ -17,6 +17,7 @@
 // 520-820) up to rounding.
 
 #include "gbfem_internal.h"
+#include "prism_dw.cuh"
 #include "prism_std.cuh"
 
 namespace gbfem {
@@ -154,7 +155,7 @@ __device__ __forceinline__ void prism_element_aniso(const d3 (&X)[6], const doub
 // Elements: for i in [0, count): element e = ent_el ? ent_el[i] - el_base : i,
 // table at tab + (ent_pos ? ent_pos[i] : 42*e).  Entity ids outside
 // [0, nel) set *err and are skipped.
-template <bool ATOMIC, bool ANISO>
+template <bool ATOMIC, bool ANISO, bool DWORD>
 __global__ void __launch_bounds__(128) prism_elements_kernel(
     int count, const int *__restrict__ ent_el, int el_base, const int *__restrict__ ent_pos, int nel,
     const int *__restrict__ el_nodes, const double *__restrict__ xyz, const double *__restrict__ k_el,
@@ -200,6 +201,69 @@ __global__ void __launch_bounds__(128) prism_elements_kernel(
 #pragma unroll
       for (int w = 0; w < 6; w++) add_val<ATOMIC>(rhs, t[36 + w], R[w]);
     }
+  }
+}
+
+// Isotropic std prisms in double-word arithmetic (prism_dw.cuh): each thread
+// keeps its intermediate values in kPrismDwSlots float2 slots of shared
+// memory (thread-major stride, conflict-free 8-byte accesses) and scatters
+// each entry as soon as it is formed.
+constexpr int kDwThreads = 128;
+__constant__ DwPairCodes kDwPairs = dw_pair_codes();
+template <bool ATOMIC>
+__global__ void __launch_bounds__(kDwThreads, 5) prism_elements_dw_kernel(
+    int count, const int *__restrict__ ent_el, int el_base, const int *__restrict__ ent_pos, int nel,
+    const int *__restrict__ el_nodes, const double *__restrict__ xyz, const double *__restrict__ k_el, double f,
+    const int *__restrict__ tab, double *__restrict__ val, double *__restrict__ rhs, int do_sm, int do_rhs,
+    int *__restrict__ err) {
+  extern __shared__ float2 dw_slots[];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  int e = ent_el ? __ldg(ent_el + i) - el_base : i;
+  if (e < 0 || e >= nel) {
+    atomicExch(err, 1);
+    return;
+  }
+  const int *tb = tab + (ent_pos ? (size_t)__ldg(ent_pos + i) : (size_t)42 * e);
+  // the table row (168 bytes) is read only after the element math: start
+  // bringing its lines into L2 now
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(tb));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(tb + 21));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(tb + 41));
+  const int2 *n2 = reinterpret_cast<const int2 *>(el_nodes + 6 * (size_t)e);
+  const int2 na = __ldg(n2), nb = __ldg(n2 + 1), nc = __ldg(n2 + 2);
+  const int nodes[6] = {na.x, na.y, nb.x, nb.y, nc.x, nc.y};
+  v3 X[6];
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const d3 x = load_node(xyz, nodes[j]);
+    X[j] = {x.x, x.y, x.z};
+  }
+  const DwSlots sl{dw_slots + threadIdx.x, kDwThreads};
+  prism_std_element_dw(X, k_el ? __ldg(k_el + e) : 1.0, f, sl);
+  if (do_sm) {
+    // the next entry's two table positions are loaded one iteration ahead
+    int c0 = kDwPairs.c[0];
+    int p1 = __ldg(tb + (c0 & 0xFF)), p2 = p1;
+#pragma unroll 1
+    for (int k = 0; k < 21; k++) {
+      const int c1 = kDwPairs.c[2 * k + 1];
+      const int c0n = k + 1 < 21 ? kDwPairs.c[2 * k + 2] : c0;
+      const int q1 = __ldg(tb + (c0n & 0xFF)), q2 = __ldg(tb + ((c0n >> 8) & 0xFF));
+      const double v = prism_dw_entry(sl, c0, c1);
+      add_val<ATOMIC>(val, p1, v);
+      if (!(c0 >> 24)) add_val<ATOMIC>(val, p2, v);
+      c0 = c0n;
+      p1 = q1;
+      p2 = q2;
+    }
+  }
+  if (do_rhs) {
+    const int2 *r2 = reinterpret_cast<const int2 *>(tb + 36);
+    const int2 ra = __ldg(r2), rb = __ldg(r2 + 1), rc = __ldg(r2 + 2);
+    const int rows[6] = {ra.x, ra.y, rb.x, rb.y, rc.x, rc.y};
+#pragma unroll
+    for (int j = 0; j < 6; j++) add_val<ATOMIC>(rhs, rows[j], prism_dw_load(sl, j));
   }
 }
 
@@ -374,17 +438,29 @@ static inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) 
 int launch_prism_elements(cudaStream_t st, bool atomic, bool aniso, int count, const int *ent_el,
                           int el_base, const int *ent_pos, int nel, const int *el_nodes,
                           const double *xyz, const double *k_el, const double *D_el, double f,
-                          const int *tab, double *val, double *rhs, int do_sm, int do_rhs, int *err) {
+                          const int *tab, double *val, double *rhs, int do_sm, int do_rhs, int *err,
+                          bool dword) {
   if (count <= 0) return 0;
   const int T = 128;
-#define GB_LAUNCH(A, B)                                                                        \
-  prism_elements_kernel<A, B><<<nblk(count, T), T, 0, st>>>(count, ent_el, el_base, ent_pos, nel, \
-                                                            el_nodes, xyz, k_el, D_el, f, tab,   \
-                                                            val, rhs, do_sm, do_rhs, err)
-  if (atomic && !aniso) GB_LAUNCH(true, false);
-  else if (atomic && aniso) GB_LAUNCH(true, true);
-  else if (!atomic && !aniso) GB_LAUNCH(false, false);
-  else GB_LAUNCH(false, true);
+#define GB_LAUNCH(A, B, W)                                                                        \
+  prism_elements_kernel<A, B, W><<<nblk(count, T), T, 0, st>>>(count, ent_el, el_base, ent_pos, nel, \
+                                                               el_nodes, xyz, k_el, D_el, f, tab,   \
+                                                               val, rhs, do_sm, do_rhs, err)
+  if (aniso) {
+    if (atomic) GB_LAUNCH(true, true, false);
+    else GB_LAUNCH(false, true, false);
+  } else if (dword) {
+    const size_t sm = (size_t)kPrismDwSlots * kDwThreads * sizeof(float2);
+    if (atomic)
+      prism_elements_dw_kernel<true><<<nblk(count, kDwThreads), kDwThreads, sm, st>>>(
+          count, ent_el, el_base, ent_pos, nel, el_nodes, xyz, k_el, f, tab, val, rhs, do_sm, do_rhs, err);
+    else
+      prism_elements_dw_kernel<false><<<nblk(count, kDwThreads), kDwThreads, sm, st>>>(
+          count, ent_el, el_base, ent_pos, nel, el_nodes, xyz, k_el, f, tab, val, rhs, do_sm, do_rhs, err);
+  } else {
+    if (atomic) GB_LAUNCH(true, false, false);
+    else GB_LAUNCH(false, false, false);
+  }
 #undef GB_LAUNCH
   GB_CUDA(cudaGetLastError());
   return 1;

@@ -164,6 +164,50 @@ def test_dropin_pipelined_download(gb, shuffle):
     assert vec_rel_err(r2, ro) < REL_TOL
 
 
+def test_double_word_assembly_vs_reference_and_oracle(gb):
+    """Element matrices in double-word arithmetic (float pairs on the FP32
+    pipe): the reference's own assembled matrix (golden, std_n10), and on a
+    jittered 40^3 x 2 mesh with lognormal k the oracle's stiffness without
+    penalty, both within the 1e-12 energy-scale bound; atomic, colour and
+    drop-in paths agree."""
+    g = load("std_n10")
+    m = FixtureMesh(g)
+    c = make_ctx(gb, m, g["k"], (g["dof_of_node"], g["row_ptr"], g["col_ind"]))
+    c.set_option(gb.OPT_STD_ARITH, gb.STD_DWORD)
+    val = np.zeros(g["col_ind"].size)
+    rhs = np.zeros(g["row_ptr"].size - 1)
+    c.create_assemble_stiff_mat(g["int_ent_type"], g["int_ent_id"], g["color_elems"], g["color_faces"],
+                                g["asse_pos"], g["assembly_table"], crs_val=val, rhs=rhs)
+    sc = energy_scale(g["row_ptr"], g["col_ind"], g["crs_val"])
+    assert crs_rel_err(g["row_ptr"], val, g["crs_val"], sc) < REL_TOL
+    assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL
+
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(40, jitter=0.2, seed=11)
+    k = lognormal_k(m.nel, seed=11)
+    c = make_ctx(gb, m, k, penalty=0.0)
+    c.build_structure()
+    dn, rp, ci = c.get_crs_structure()
+    c.assemble(gb.SCATTER_ATOMIC)
+    v64, r64 = c.get_matrix()
+    c.set_option(gb.OPT_STD_ARITH, gb.STD_DWORD)
+    c.assemble(gb.SCATTER_ATOMIC)
+    vdw, rdw = c.get_matrix()
+    c.assemble(gb.SCATTER_COLOR)
+    vdc, rdc = c.get_matrix()
+    vo, ro, _ = O.std_prism_assemble(m, k, dn, rp, ci, penalty=0.0, nthreads=8)
+    es = energy_scale(rp, ci, vo)
+    assert crs_rel_err(rp, vdw, vo, es) < REL_TOL
+    assert crs_rel_err(rp, vdc, vo, es) < REL_TOL
+    assert vec_rel_err(rdw, ro) < REL_TOL
+    # the double-word entries sit within 1e-13 of the FP64 kernel's
+    assert crs_rel_err(rp, vdw, v64, es) < 1e-13
+    assert vec_rel_err(rdw, r64) < 1e-13
+    # constants stay in the kernel of the stiffness
+    rows_sum = np.add.reduceat(vdw, rp[:-1])
+    assert np.max(np.abs(rows_sum)) < 1e-12 * np.max(np.abs(vdw))
+
+
 def test_dropin_rejects_bad_entities_and_recovers(gb):
     g = load("std_n4")
     m = FixtureMesh(g)

@@ -13,7 +13,7 @@ from _util import mat_rel_err
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "hostcheck", "prism_math_host.cu")
-HDR = os.path.join(HERE, "..", "modfem_gb300", "csrc", "prism_std.cuh")
+HDRS = [os.path.join(HERE, "..", "modfem_gb300", "csrc", h) for h in ("prism_std.cuh", "prism_dw.cuh", "dword.cuh")]
 LIB = os.path.join(HERE, "hostcheck", "libprism_math_host.so")
 
 
@@ -22,11 +22,13 @@ def hostlib():
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(SRC), os.path.getmtime(HDR)):
-        subprocess.check_call([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-o", LIB, SRC])
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(f) for f in [SRC] + HDRS):
+        subprocess.check_call([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-shared", "-o",
+                               LIB, SRC])
     L = ctypes.CDLL(LIB)
-    L.host_prism_std_element.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
-                                         ctypes.c_void_p]
+    for fn in (L.host_prism_std_element, L.host_prism_std_element_dw):
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+    L.host_dw_roundtrip.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     return L
 
 
@@ -54,6 +56,65 @@ def test_prism_element_math_vs_oracle(hostlib):
         worst = max(worst, mat_rel_err(unpack(K21), Ko))
         assert np.max(np.abs(R - Ro)) <= 1e-13 * np.max(np.abs(Ro))
     assert worst < 1e-13, worst
+
+
+def test_prism_element_math_double_word(hostlib):
+    """The double-word form of the same element math (float pairs): within
+    1e-13 of the oracle's FP64 matrix on jittered elements of a fine mesh
+    (h = 1/200, determinants near 1e-7) with lognormal k, and on distorted
+    elements over four decades of size."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(200, jitter=0.25, seed=7)
+    k = lognormal_k(m.nel, seed=7)
+    rng = np.random.default_rng(7)
+    worst = worst_r = 0.0
+    for e in rng.choice(m.nel, 400, replace=False):
+        X = np.ascontiguousarray(m.coords[m.el_nodes[e]]).reshape(-1)
+        K21, R = np.zeros(21), np.zeros(6)
+        hostlib.host_prism_std_element_dw(X.ctypes.data, k[e], 1.3, K21.ctypes.data, R.ctypes.data)
+        Ko, Ro = O.std_prism_element(X, np.diag([k[e]] * 3), 1.3)
+        worst = max(worst, mat_rel_err(unpack(K21), Ko))
+        worst_r = max(worst_r, np.max(np.abs(R - Ro)) / np.max(np.abs(Ro)))
+    assert worst < 1e-13 and worst_r < 1e-13, (worst, worst_r)
+    base = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [0, 1, 1]], float)
+    for _ in range(200):
+        X = (base + rng.uniform(-0.2, 0.2, base.shape)) * 10.0 ** rng.uniform(-3, 1)
+        X = np.ascontiguousarray(X).reshape(-1)
+        K21, R = np.zeros(21), np.zeros(6)
+        hostlib.host_prism_std_element_dw(X.ctypes.data, 2.5, 1.0, K21.ctypes.data, R.ctypes.data)
+        Ko, Ro = O.std_prism_element(X, np.diag([2.5] * 3), 1.0)
+        assert mat_rel_err(unpack(K21), Ko) < 1e-13
+        assert np.max(np.abs(R - Ro)) <= 1e-13 * np.max(np.abs(Ro))
+        # far from the origin the FP64 vertex differences (shared by both
+        # forms) dominate the error: compare with the FP64 form
+        X = np.ascontiguousarray(X + np.tile(rng.uniform(-5, 5, 3), 6))
+        K64, R64 = np.zeros(21), np.zeros(6)
+        hostlib.host_prism_std_element(X.ctypes.data, 2.5, 1.0, K64.ctypes.data, R64.ctypes.data)
+        hostlib.host_prism_std_element_dw(X.ctypes.data, 2.5, 1.0, K21.ctypes.data, R.ctypes.data)
+        assert mat_rel_err(unpack(K21), unpack(K64)) < 1e-13
+        assert np.max(np.abs(R - R64)) <= 1e-13 * np.max(np.abs(R64))
+
+
+def test_double_word_conversions(hostlib):
+    """double -> float pair keeps 47+ bits (the pair's sum differs from the
+    double by at most 2^-47 of it) on [2^-74, 2^127), the high word alone
+    down to 2^-126; float pair -> double is exact when the pair's bits fit
+    53; zero maps to zero."""
+    rng = np.random.default_rng(1)
+    x = np.concatenate([rng.standard_normal(2000) * 10.0 ** rng.uniform(-20, 20, 2000),
+                        [0.0, -0.0, 1.0, -1.0, 2.0 ** -80, 3e-30, -7e35, 1e-3]])
+    hl = np.zeros(2 * x.size, np.float32)
+    back = np.zeros(x.size)
+    hostlib.host_dw_roundtrip(x.ctypes.data, x.size, hl.ctypes.data, back.ctypes.data)
+    h, l = hl[0::2].astype(np.float64), hl[1::2].astype(np.float64)
+    nz = x != 0
+    fit = nz & (np.abs(x) >= 2.0 ** -74) & (np.abs(x) < 2.0 ** 127)  # pairs of normal floats
+    small = nz & ~fit & (np.abs(x) >= 2.0 ** -126)                    # high word only
+    assert np.all(np.abs((h + l - x)[fit]) <= 2.0 ** -47 * np.abs(x[fit]))
+    assert np.all(np.abs((h + l - x)[small]) <= 2.0 ** -23 * np.abs(x[small]))
+    assert np.all(back[~nz] == 0)
+    assert np.all(np.abs((back - (h + l))[fit]) <= 2.0 ** -52 * np.abs(x[fit]))
+    assert np.all(np.abs((back - x)[fit | small]) <= 2.0 ** -23 * np.abs(x[fit | small]))
 
 
 def test_prism_element_math_distorted(hostlib):
