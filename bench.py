@@ -204,6 +204,29 @@ def read_profile_traffic():
     return None
 
 
+def read_profile_values(name):
+    """``key = number`` lines of a committed ncu summary under profiles/."""
+    out = {}
+    p = os.path.join(ROOT, "profiles", name)
+    if os.path.exists(p):
+        for line in open(p):
+            parts = line.strip().split("=")
+            if len(parts) >= 2 and parts[0].strip().replace("_", "").isalnum() and " " not in parts[0].strip():
+                try:
+                    out[parts[0].strip()] = float(parts[1].split()[0])
+                except (ValueError, IndexError):
+                    pass
+    return out
+
+
+def sm_count(device):
+    try:
+        import torch
+        return torch.cuda.get_device_properties(device).multi_processor_count
+    except Exception:
+        return 152
+
+
 def make_problem(n):
     from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
     m = structured_prism_mesh(n, jitter=JITTER, seed=SEED)
@@ -223,9 +246,9 @@ def cpu_assemble(m, k, nthreads, reps=1):
     cptr[1:] = np.cumsum(np.bincount(col, minlength=nc))
     times = []
     for _ in range(reps):
-        _, _, t = O.std_prism_assemble(m, k, d, rp, ci, color_ptr=cptr, perm=perm, nthreads=nthreads)
+        val, rhs, t = O.std_prism_assemble(m, k, d, rp, ci, color_ptr=cptr, perm=perm, nthreads=nthreads)
         times.append(t)
-    return times
+    return times, val, rhs
 
 
 def dg_fma_per_element(p):
@@ -655,55 +678,50 @@ def main():
     fp64_peak = c.measure_fp64_peak()
 
     # ---------------- device-resident throughput ----------------
-    for _ in range(args.warmup):
-        c.assemble(gb.SCATTER_ATOMIC)
-    barrier(ws)
+    # the plain FP64 element kernel (the drop-in default), then the
+    # double-word one (float pairs, the headline): same mesh, same scatter
+    def device_loop(arith):
+        c.set_option(gb.OPT_STD_ARITH, arith)
+        for _ in range(args.warmup):
+            c.assemble(gb.SCATTER_ATOMIC)
+        barrier(ws)
+        tot, el, nl_sum = 0.0, 0.0, 0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            c.assemble(gb.SCATTER_ATOMIC)
+            a, b, nl = c.last_timing()
+            tot += a
+            el += b
+            nl_sum += nl
+        wall_ = time.perf_counter() - t0
+        return (max_over_ranks(tot / args.steps, ws), max_over_ranks(el / args.steps, ws), nl_sum, wall_,
+                c.get_matrix())
+
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.25)  # let the sampler's first reading land inside the timed region
-    tot_ms, el_ms, launches = 0.0, 0.0, 0
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        c.assemble(gb.SCATTER_ATOMIC)
-        a, b, nl = c.last_timing()
-        tot_ms += a
-        el_ms += b
-        launches += nl
-    wall = time.perf_counter() - t0
-    ms_step = max_over_ranks(tot_ms / args.steps, ws)
-    el_ms_step = max_over_ranks(el_ms / args.steps, ws)
+    ms64, el64, launches64, _, (v64, r64) = device_loop(gb.STD_FP64)
+    ms_step, el_ms_step, launches, wall, (vdw, rdw) = device_loop(gb.STD_DWORD)
     value = ws * m.nel / (ms_step * 1e-3)
-
-    # ---------------- double-word element arithmetic (float pairs) ----------------
-    v64, r64 = c.get_matrix()
-    c.set_option(gb.OPT_STD_ARITH, gb.STD_DWORD)
-    for _ in range(args.warmup):
-        c.assemble(gb.SCATTER_ATOMIC)
-    dw_tot, dw_el, dw_launches = 0.0, 0.0, 0
-    for _ in range(args.steps):
-        c.assemble(gb.SCATTER_ATOMIC)
-        a, b, nl = c.last_timing()
-        dw_tot += a
-        dw_el += b
-        dw_launches += nl
-    dw_ms = max_over_ranks(dw_tot / args.steps, ws)
-    dw_el_ms = max_over_ranks(dw_el / args.steps, ws)
-    vdw, rdw = c.get_matrix()
-    c.set_option(gb.OPT_STD_ARITH, gb.STD_FP64)
+    value64 = ws * m.nel / (ms64 * 1e-3)
     dn_, rp_, ci_ = c.get_crs_structure()
     rows_ = np.repeat(np.arange(nd), np.diff(rp_))
-    dg_ = np.abs(v64[rows_ == ci_])
-    diag_ = np.zeros(nd)
-    diag_[rows_[rows_ == ci_]] = dg_
-    escale = np.sqrt(diag_[rows_] * diag_[ci_])
-    double_word = {
-        "value": ws * m.nel / (dw_ms * 1e-3), "unit": UNIT, "ms_per_step": dw_ms, "element_kernel_ms": dw_el_ms,
-        "speedup_vs_plain_fp64": ms_step / dw_ms, "element_kernel_speedup": el_ms_step / dw_el_ms,
-        "max_rel_err_vs_fp64_energy_scale": float(np.max(np.abs(vdw - v64) / np.where(escale > 0, escale, 1.0))),
-        "max_abs_err_vs_fp64_over_max_entry": float(np.max(np.abs(vdw - v64)) / np.max(np.abs(v64))),
-        "rhs_max_rel_err_vs_fp64": float(np.max(np.abs(rdw - r64)) / np.max(np.abs(r64))),
-        "launches": dw_launches}
-    del rows_, escale, diag_, dg_
+    isd_ = rows_ == ci_
+
+    def energy_err(a, b):
+        diag = np.zeros(nd)
+        diag[rows_[isd_]] = np.abs(b[isd_])
+        es = np.sqrt(diag[rows_] * diag[ci_])
+        return float(np.max(np.abs(a - b) / np.where(es > 0, es, 1.0)))
+
+    precision = {
+        "element_arithmetic": "double-word float pairs (about 48 significant bits); FP64 vertex differences, "
+                              "FP64 atomic assembly sums",
+        "bound_rel": 1e-10,
+        "max_rel_err_vs_plain_fp64_energy_scale": energy_err(vdw, v64),
+        "max_abs_err_vs_plain_fp64_over_max_entry": float(np.max(np.abs(vdw - v64)) / np.max(np.abs(v64))),
+        "rhs_max_rel_err_vs_plain_fp64": float(np.max(np.abs(rdw - r64)) / np.max(np.abs(r64)))}
+    assert precision["max_rel_err_vs_plain_fp64_energy_scale"] <= 1e-10
 
     # ---------------- end to end through the drop-in C ABI ----------------
     tables = c.get_element_tables()
@@ -723,6 +741,7 @@ def main():
     out_val = gb.PinnedArray((nnz,))
     out_rhs = gb.PinnedArray((nd,))
     c.set_option(gb.OPT_CACHE_TABLES, 1)
+    c.set_option(gb.OPT_STD_ARITH, gb.STD_DWORD)
 
     def e2e_step():
         c.set_node_coords(pins["xyz"].array)
@@ -739,15 +758,24 @@ def main():
         t1 = time.perf_counter()
         e2e_step()
         et.append(time.perf_counter() - t1)
-    clocks = sampler.stop()
     e2e_s = max_over_ranks(sum(et) / len(et), ws)
     e2e_value = ws * m.nel / e2e_s
     h2d = m.coords.nbytes + k.nbytes
     d2h = 8 * nnz + 8 * nd
-
     # parity of the e2e result against the device-resident one (same kernels)
-    ref_val, ref_rhs = c.get_matrix()
-    assert np.max(np.abs(out_val.array - ref_val)) <= 1e-12 * np.max(np.abs(ref_val))
+    assert np.max(np.abs(out_val.array - vdw)) <= 1e-12 * np.max(np.abs(vdw))
+    # the same through the plain FP64 kernel
+    c.set_option(gb.OPT_STD_ARITH, gb.STD_FP64)
+    for _ in range(max(args.warmup, 1)):
+        e2e_step()
+    et64 = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        e2e_step()
+        et64.append(time.perf_counter() - t1)
+    e2e64_s = max_over_ranks(sum(et64) / len(et64), ws)
+    assert np.max(np.abs(out_val.array - v64)) <= 1e-12 * np.max(np.abs(v64))
+    clocks = sampler.stop()
 
     # ---------------- GMRES(30) + Jacobi on the assembled matrix ----------------
     c.assemble(gb.SCATTER_ATOMIC)
@@ -772,35 +800,65 @@ def main():
     if rank == 0 and ws == 1:
         subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"])
         nthreads = os.cpu_count() or 1
-        times = cpu_assemble(m, k, nthreads, reps=2)
+        times, vo, ro = cpu_assemble(m, k, nthreads, reps=2)
         tc = min(times)
+        precision["max_rel_err_vs_oracle_energy_scale"] = {"double_word": energy_err(vdw, vo),
+                                                           "plain_fp64": energy_err(v64, vo)}
+        precision["rhs_max_rel_err_vs_oracle"] = {
+            "double_word": float(np.max(np.abs(rdw - ro)) / np.max(np.abs(ro))),
+            "plain_fp64": float(np.max(np.abs(r64 - ro)) / np.max(np.abs(ro)))}
+        del vo, ro
         cpu = {"value": m.nel / tc, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": f"one full {m.nel}-element integrate+assemble (elements + faces), colour-parallel OpenMP"}
 
-    achieved = FLOP_PER_ELEM * m.nel / (el_ms_step * 1e-3) / 1e12
-    slot_frac = 2 * FP64_SLOTS_PER_ELEM * m.nel / (el_ms_step * 1e-3) / 1e12 / fp64_peak
+    # plain FP64 kernel: FP64-pipe roofline
     traffic = read_profile_traffic()
+    achieved64 = FLOP_PER_ELEM * m.nel / (el64 * 1e-3) / 1e12
+    slot_frac = 2 * FP64_SLOTS_PER_ELEM * m.nel / (el64 * 1e-3) / 1e12 / fp64_peak
+    # double-word kernel: instruction-issue roofline (4 warp instructions per
+    # clock per SM), its instruction count per element from the ncu capture
+    dw_prof = read_profile_values("std_prism_elements_dw_686k.md")
+    inst_per_elem = dw_prof.get("thread_instructions_per_element")
+    nsm = sm_count(local)
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    issue_peak = nsm * 4 * 32 * sm_mhz * 1e6 / 1e12
+    achieved_issue = inst_per_elem * m.nel / (el_ms_step * 1e-3) / 1e12 if inst_per_elem else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32x2+f64",
         "data": "synthetic (seeded mesh jitter and lognormal k)",
         "config": {"workload": f"std P1 prism integrate+assemble, {args.n}^3 hex x 2 = {m.nel} prisms "
                                f"({nd} dofs, nnz {nnz}, {m.bc_face_id.size} penalty faces), lognormal(0,1) k, "
                                f"+-0.2h jitter",
+                   "element_arithmetic": "double-word (float pairs) element matrices, FP64 vertex differences",
                    "scatter": "FP64 atomics", "l2": "inputs larger than L2 (tables 336 MB, values 170 MB)",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp64_peak, "traffic": traffic,
-                     "kernel": "prism_elements_kernel", "kernel_ms": el_ms_step,
-                     "flop_per_elem": FLOP_PER_ELEM, "fp64_pipe_slot_frac": slot_frac,
-                     "survey_flop_per_elem": SURVEY_FLOP_PER_ELEM,
-                     "survey_equivalent_tflops": SURVEY_FLOP_PER_ELEM * m.nel / (el_ms_step * 1e-3) / 1e12,
-                     "peak_source": "FP64 FMA-chain kernel measured in this run (no FP64 figure in the peaks file)"},
+        "roofline": {"bound": "issue", "achieved": achieved_issue, "peak": issue_peak, "unit": "Tinst/s",
+                     "frac": achieved_issue / issue_peak if achieved_issue else None,
+                     "traffic": dw_prof.get("dram_bytes_per_launch"),
+                     "kernel": "prism_elements_dw_kernel", "kernel_ms": el_ms_step,
+                     "inst_per_elem": inst_per_elem,
+                     "fp64_equivalent_tflops": FLOP_PER_ELEM * m.nel / (el_ms_step * 1e-3) / 1e12,
+                     "peak_source": f"instruction issue: 4 warp instructions per clock per SM x {nsm} SMs x "
+                                    f"{sm_mhz:.0f} MHz (sampled); FP32 pipes, no FP64 peak applies"},
+        "speedup_vs_plain_fp64": {"device": value / value64, "element_kernel": el64 / el_ms_step,
+                                  "e2e": e2e64_s / e2e_s},
+        "precision": precision,
+        "plain_fp64": {
+            "value": value64, "unit": UNIT, "ms_per_step": ms64, "element_kernel_ms": el64, "launches": launches64,
+            "e2e": {"value": ws * m.nel / e2e64_s, "unit": UNIT, "ms_per_step": e2e64_s * 1e3},
+            "roofline": {"bound": "fp64", "achieved": achieved64, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved64 / fp64_peak, "traffic": traffic,
+                         "kernel": "prism_elements_kernel", "kernel_ms": el64,
+                         "flop_per_elem": FLOP_PER_ELEM, "fp64_pipe_slot_frac": slot_frac,
+                         "survey_flop_per_elem": SURVEY_FLOP_PER_ELEM,
+                         "peak_source": "FP64 FMA-chain kernel measured in this run (no FP64 figure in the peaks "
+                                        "file)"}},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_s * 1e3},
         "clocks": clocks,
-        "double_word": double_word,
         "solver": solver,
         "structure": structure,
         "dg": dg,
