@@ -628,7 +628,7 @@ def run_reference(args, ws, rank):
     m, k = make_problem(args.n)
     nthreads = os.cpu_count() or 1
     cpu_assemble(m, k, nthreads, reps=args.warmup)
-    times = cpu_assemble(m, k, nthreads, reps=args.steps)
+    times, _, _ = cpu_assemble(m, k, nthreads, reps=args.steps)
     t = sum(times) / len(times)
     v = m.nel / t
     line = {
