@@ -412,10 +412,16 @@ static int build_pipe_plan(gbfem_ctx c, int e0, int e1) {
   GB_CUDA(cudaMemcpyAsync(last.data(), c->row_last.p, (size_t)nd * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
   for (int r = 1; r < nd; r++) last[r] = std::max(last[r], last[r - 1]);  // prefix maximum
-  const int K = std::max(1, std::min(8, count / 65536));
+  // chunks of whole waves of resident element threads (five 128-thread
+  // blocks per SM for both element kernels), at most eight
+  int nsm = 152;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+  const long long wave = (long long)nsm * 5 * 128;
+  const long long chunk = std::max(wave, (count / 8 + wave) / wave * wave);
+  const int K = (int)((count + chunk - 1) / chunk);
   c->pipe_el.assign(K + 1, 0);
   c->pipe_rows.assign(K, nd);
-  for (int k = 0; k <= K; k++) c->pipe_el[k] = (int)((long long)count * k / K);
+  for (int k = 0; k <= K; k++) c->pipe_el[k] = (int)std::min<long long>(count, chunk * k);
   for (int k = 0; k + 1 < K; k++)
     c->pipe_rows[k] = (int)(std::upper_bound(last.begin(), last.end(), c->pipe_el[k + 1] - 1) - last.begin());
   if (!c->copy_stream) {
