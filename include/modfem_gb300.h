@@ -193,9 +193,16 @@ int gbfem_dg_set_volume_kernel(gbfem_ctx ctx, int mode);
  * slices per operand, exact FP32 slice sums, recombination rounded once to
  * FP64: the reference's face matrices to FP64 accuracy) for owners of degree
  * <= 3 whose neighbours all have degree <= 3; other owners keep the FP64
- * kernel. */
+ * kernel; or GBFEM_DG_FACE_DWORD, the FP64 kernel's algebra with the point
+ * tables in double-word (float pair) form and every entry summed on the
+ * FP32 pipes by exact products and sums (errors of order 2^-48 of the summed
+ * magnitudes), all degrees of prism meshes; tetrahedra keep the FP64
+ * kernel; or GBFEM_DG_FACE_TC_DWORD: the tensor cores where they apply and
+ * the double-word kernel for the other owners. */
 #define GBFEM_DG_FACE_FP64 0
 #define GBFEM_DG_FACE_TC 1
+#define GBFEM_DG_FACE_DWORD 2
+#define GBFEM_DG_FACE_TC_DWORD 3
 int gbfem_dg_set_face_kernel(gbfem_ctx ctx, int mode);
 /* Interior-penalty factor, pdr_ctrl_d_params(problem, 12) in the DG weak
  * form (pds_conv_diff_weakform_dg.c:516-531); default 10. */

@@ -20,7 +20,7 @@ OPT_CACHE_TABLES = 1
 OPT_STD_ARITH = 2
 STD_FP64, STD_DWORD = 0, 1
 DG_VOLUME_FP64, DG_VOLUME_TC, DG_VOLUME_TF32 = 0, 1, 2
-DG_FACE_FP64, DG_FACE_TC = 0, 1
+DG_FACE_FP64, DG_FACE_TC, DG_FACE_DWORD, DG_FACE_TC_DWORD = 0, 1, 2, 3
 
 # (name, restype, argtypes) of every symbol include/modfem_gb300.h declares
 _vp, _ci, _cd, _cll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
@@ -252,7 +252,8 @@ class Context:
         self._check(self.L.gbfem_dg_set_volume_kernel(self._h, mode))
 
     def dg_set_face_kernel(self, mode):
-        """DG_FACE_FP64 or DG_FACE_TC (tensor cores, split BF16, FP64-equivalent)."""
+        """DG_FACE_FP64, DG_FACE_TC (tensor cores, split BF16, FP64-equivalent), DG_FACE_DWORD (double-word
+        sums on the FP32 pipes) or DG_FACE_TC_DWORD (tensor cores where they apply, double word elsewhere)."""
         self._check(self.L.gbfem_dg_set_face_kernel(self._h, mode))
 
     def dg_build_structure(self):

@@ -690,7 +690,9 @@ int gbfem_dg_set_volume_kernel(gbfem_ctx c, int mode) {
 
 int gbfem_dg_set_face_kernel(gbfem_ctx c, int mode) {
   GB_CHECK(c, "null context");
-  GB_CHECK(mode == GBFEM_DG_FACE_FP64 || mode == GBFEM_DG_FACE_TC, "unknown DG face kernel");
+  GB_CHECK(mode == GBFEM_DG_FACE_FP64 || mode == GBFEM_DG_FACE_TC || mode == GBFEM_DG_FACE_DWORD ||
+               mode == GBFEM_DG_FACE_TC_DWORD,
+           "unknown DG face kernel");
   c->dg_face_mode = mode;
   return 0;
 }
@@ -910,7 +912,7 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     launches += r;
   }
   cudaEventRecord(c->ev2, c->stream);
-  const bool tcf = c->dg_face_mode == GBFEM_DG_FACE_TC;
+  const bool tcf = c->dg_face_mode == GBFEM_DG_FACE_TC || c->dg_face_mode == GBFEM_DG_FACE_TC_DWORD;
   if (c->dg_hf.p) {
     if (tcf && !tc) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
     for (int p = 1; p <= 4; p++) {
@@ -935,7 +937,7 @@ int gbfem_dg_assemble(gbfem_ctx c) {
         r = gbfem::launch_dg_prism_faces(c->stream, p, (int)c->dg_flist_64[p].n, c->dg_flist_64[p].p, c->dg_hf_ptr.p,
                                          c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
                                          c->dg_pen, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,
-                                         c->dg_rhs.p, c->dg_var_face[p]);
+                                         c->dg_rhs.p, c->dg_var_face[p], c->dg_face_mode == GBFEM_DG_FACE_TC_DWORD);
         GB_TRY(r);
         launches += r;
         continue;
@@ -943,7 +945,7 @@ int gbfem_dg_assemble(gbfem_ctx c) {
       int r = gbfem::launch_dg_prism_faces(c->stream, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->dg_hf_ptr.p,
                                            c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
                                            c->dg_pen, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,
-                                           c->dg_rhs.p, c->dg_var_face[p]);
+                                           c->dg_rhs.p, c->dg_var_face[p], c->dg_face_mode == GBFEM_DG_FACE_DWORD);
       GB_TRY(r);
       launches += r;
     }

@@ -17,6 +17,7 @@
 // both sides (a few percent of the FP64 work; the block products dominate).
 
 #include "dg_face.cuh"
+#include "dword.cuh"
 #include "gbfem_internal.h"
 
 namespace gbfem {
@@ -47,11 +48,87 @@ struct DgFaceDims {
   static constexpr int THREADS = THR;
   static constexpr int NCOL = NS + GB_DG_MAXNS;  // own + neighbour columns
   static constexpr int PER = (NS * NS + THREADS - 1) / THREADS;
+  // degree <= 3: the coordinates, tensors, point geometry and penalty of all
+  // (up to 5) faces are prepared at once before the face loop (the long FP64
+  // chains of the face points then run side by side instead of on a few
+  // threads per face); degree 4 keeps one face at a time (shared memory)
+  static constexpr bool ALLF = P <= 3;
+  static constexpr int NFG = ALLF ? 5 : 1;
   static constexpr int SMEM_DOUBLES =
-      2 * DGF_NQ * NS + 2 * DGF_NQ * NCOL + 36 + 18 + DGF_NQ * DGF_GEO + 2 * DGF_NQ * DGF_FAC + 1;
+      2 * DGF_NQ * NS + 2 * DGF_NQ * NCOL + NFG * (36 + 18 + DGF_NQ * DGF_GEO + 1) + 2 * DGF_NQ * DGF_FAC;
 };
 
-template <int P, int THR>
+// Double-word form (DW = true): the point tables hold float pairs
+// (converted from the FP64 basis values) and each entry is a dot product of
+// length 2 nq on the FP32 pipes: per product an exact TwoProd (with the cross
+// terms of the low words), the high parts summed by TwoSum, every rounding
+// error collected in a float and folded back every four points.  The error
+// stays of order u^2 = 2^-48 of the summed magnitudes, against the FP64
+// kernel's 2 nq FP64 FMAs per entry at 1/64 of the FP32 issue rate.
+struct DwAcc {
+  float h, l, e;  // value h + l + e
+};
+__device__ __forceinline__ void dwacc_prod(DwAcc &a, float2 x, float2 y) {
+  const float p = f_mul(x.x, y.x);
+  float pe = f_fma(x.x, y.x, -p);
+  pe = f_fma(x.x, y.y, pe);
+  pe = f_fma(x.y, y.x, pe);
+  const dw s = two_sum(a.h, p);
+  a.h = s.h;
+  a.e = f_add(a.e, f_add(s.l, pe));
+}
+__device__ __forceinline__ void dwacc_fold(DwAcc &a) {
+  const dw r = fast_two_sum(a.h, f_add(a.l, a.e));
+  a.h = r.h;
+  a.l = r.l;
+  a.e = 0.0f;
+}
+__device__ __forceinline__ double dwacc_value(DwAcc a) {
+  dwacc_fold(a);
+  return dw_to_double(dw(a.h, a.l));
+}
+// Entries k = k0 + m THR (m < PER, k < kend) of an NS-row block: row
+// i = k % NS, table column j = k / NS + col_lo; sum over the points of
+// L_i Phi_j + M_i Gam_j into a[m].  The PER chains run interleaved (each
+// TwoSum waits on its predecessor in the same chain); with THR a multiple of
+// NS every entry of a thread has the same row and the L, M loads are shared.
+template <int NS, int THR, int PER>
+__device__ __forceinline__ void dwacc_face_block(DwAcc (&a)[PER], const float2 *sL, const float2 *sM,
+                                                 const float2 *sPhi, const float2 *sGam, int nq, int ncol, int k0,
+                                                 int kend, int col_lo) {
+  int ii[PER], jj[PER];
+  bool ok[PER];
+#pragma unroll
+  for (int m = 0; m < PER; m++) {
+    const int k = k0 + m * THR;
+    ok[m] = k < kend;
+    ii[m] = ok[m] ? k % NS : 0;
+    jj[m] = ok[m] ? k / NS + col_lo : 0;
+  }
+  for (int q = 0; q < nq; q++) {
+    const float2 *Lq = sL + q * NS, *Mq = sM + q * NS, *Pq = sPhi + q * ncol, *Gq = sGam + q * ncol;
+    float2 L0 = Lq[ii[0]], M0 = Mq[ii[0]];
+#pragma unroll
+    for (int m = 0; m < PER; m++) {
+      if (!ok[m]) continue;
+      const float2 L = (THR % NS == 0) ? L0 : Lq[ii[m]], M = (THR % NS == 0) ? M0 : Mq[ii[m]];
+      dwacc_prod(a[m], L, Pq[jj[m]]);
+      dwacc_prod(a[m], M, Gq[jj[m]]);
+    }
+    if ((q & 3) == 3) {
+#pragma unroll
+      for (int m = 0; m < PER; m++) dwacc_fold(a[m]);
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < PER; m++) dwacc_fold(a[m]);
+}
+__device__ __forceinline__ float2 dw_f2(double v) {
+  const dw d = dw_from_double(v);
+  return make_float2(d.h, d.l);
+}
+
+template <int P, int THR, bool DW>
 __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
@@ -66,66 +143,113 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
   double *sM = sL + DGF_NQ * NS;           // [DGF_NQ][NS]
   double *sPhi = sM + DGF_NQ * NS;         // [DGF_NQ][NCOL] columns, side 1 then side 2
   double *sGam = sPhi + DGF_NQ * NCOL;     // [DGF_NQ][NCOL]
-  double *sX = sGam + DGF_NQ * NCOL;       // [2][18] vertex coordinates of both sides
-  double *sA = sX + 36;                    // [2][9] coefficient tensors
-  double *sGeo = sA + 18;                  // [DGF_NQ][DGF_GEO]
-  double *sFac = sGeo + DGF_NQ * DGF_GEO;  // [DGF_NQ][2][DGF_FAC]
-  double *sPen = sFac + 2 * DGF_NQ * DGF_FAC;  // penalty / sqrt(face area)
+  constexpr int NFG = Dm::NFG;
+  double *sX0 = sGam + DGF_NQ * NCOL;              // [NFG][2][18] vertex coordinates of both sides
+  double *sA0 = sX0 + NFG * 36;                    // [NFG][2][9] coefficient tensors
+  double *sGeo0 = sA0 + NFG * 18;                  // [NFG][DGF_NQ][DGF_GEO]
+  double *sFac = sGeo0 + NFG * DGF_NQ * DGF_GEO;   // [DGF_NQ][2][DGF_FAC]
+  double *sPen0 = sFac + 2 * DGF_NQ * DGF_FAC;     // [NFG] penalty / sqrt(face area)
   const int bi = blockIdx.x;
   if (bi >= count) return;
   const int e = ent_el[bi];
   const int tid = threadIdx.x;
   double acc[Dm::PER];
+  DwAcc dacc[DW ? Dm::PER : 1];
 #pragma unroll
   for (int m = 0; m < Dm::PER; m++) acc[m] = 0.0;
+#pragma unroll
+  for (int m = 0; m < (DW ? Dm::PER : 1); m++) dacc[m] = DwAcc{0.0f, 0.0f, 0.0f};
   double racc = 0.0;
+  float2 *fL = reinterpret_cast<float2 *>(sL), *fM = reinterpret_cast<float2 *>(sM);
+  float2 *fPhi = reinterpret_cast<float2 *>(sPhi), *fGam = reinterpret_cast<float2 *>(sGam);
   const int h0 = hf_ptr[e], h1 = hf_ptr[e + 1];
+  // the point rule of a face: the larger of its two sides' rules
+  auto face_rule = [&](const DgHalfFace &F, int &pr, int &ti) {
+    const bool interior = F.el2 >= 0;
+    const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
+    ti = F.nfv == 4 ? 1 : 0;
+    pr = p1;
+    if (interior && d_dg_nqf[p2][ti] > d_dg_nqf[p1][ti]) pr = p2;
+  };
+  auto face_geometry = [&](const DgHalfFace &F, int q, const double *X, const double *A, double *G) {
+    int pr, ti;
+    face_rule(F, pr, ti);
+    const bool interior = F.el2 >= 0;
+    const DgFacePoint Pq = dg_face_point(F.nfv, d_dg_fq[pr - 1][ti][q], X, F.loc1, F.side1, A,
+                                         interior ? X + 18 : nullptr, F.loc2, A + 9);
+    G[0] = Pq.e1.x; G[1] = Pq.e1.y; G[2] = Pq.e1.z;
+    G[3] = Pq.e2.x; G[4] = Pq.e2.y; G[5] = Pq.e2.z;
+    G[6] = Pq.v1.x; G[7] = Pq.v1.y; G[8] = Pq.v1.z;
+    G[9] = Pq.v2.x; G[10] = Pq.v2.y; G[11] = Pq.v2.z;
+    G[12] = Pq.a;
+  };
+  auto face_penalty = [&](const DgHalfFace &F, const double *X) {
+    const bool interior = F.el2 >= 0;
+    const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
+    v3 V[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int l = i < F.nfv ? F.loc1[i] : 0;
+      V[i] = {X[3 * l], X[3 * l + 1], X[3 * l + 2]};
+    }
+    const int pp = interior ? (p1 < p2 ? p1 : p2) : p1;
+    return pen * pp / sqrt(dg_face_area(V, F.nfv));
+  };
+  auto load_face = [&](const DgHalfFace &F, int c, double *X, double *A) {  // c in [0, 54)
+    const bool interior = F.el2 >= 0;
+    if (c < 36) {
+      const int s = c / 18, r = c % 18;
+      if (s == 0 || interior) {
+        const int el = s ? F.el2 : F.el1;
+        X[c] = xyz[3 * (size_t)el_nodes[6 * (size_t)el + r / 3] + r % 3];
+      }
+    } else {
+      const int t = c - 36, s = t / 9, r = t % 9;
+      if (s == 0 || interior) {
+        const int el = s ? F.el2 : F.el1;
+        A[t] = D_el ? D_el[9 * (size_t)el + r] : ((r % 4 == 0) ? (k_el ? k_el[el] : 1.0) : 0.0);
+      }
+    }
+  };
+  const int nf = h1 - h0;
+  const bool allf = Dm::ALLF && nf <= NFG;  // uniform over the CTA
+  if (allf) {
+    for (int t = tid; t < nf * 54; t += DGF_THREADS) {
+      const int f = t / 54;
+      load_face(hf[h0 + f], t % 54, sX0 + 36 * f, sA0 + 18 * f);
+    }
+    __syncthreads();
+    for (int t = tid; t < nf * DGF_NQ; t += DGF_THREADS) {
+      const int f = t / DGF_NQ, q = t % DGF_NQ;
+      const DgHalfFace F = hf[h0 + f];
+      int pr, ti;
+      face_rule(F, pr, ti);
+      if (q < d_dg_nqf[pr][ti]) face_geometry(F, q, sX0 + 36 * f, sA0 + 18 * f, sGeo0 + (f * DGF_NQ + q) * DGF_GEO);
+    }
+    for (int f = tid; f < nf; f += DGF_THREADS) sPen0[f] = face_penalty(hf[h0 + f], sX0 + 36 * f);
+  }
   for (int h = h0; h < h1; h++) {
     const DgHalfFace F = hf[h];
     const bool interior = F.el2 >= 0;
     const int own2 = F.owner_is_2;
     const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
     const int ns1 = d_dg_ns[p1], ns2 = interior ? d_dg_ns[p2] : 0;
-    const int ti = F.nfv == 4 ? 1 : 0;
-    int pr = p1;
-    if (interior && d_dg_nqf[p2][ti] > d_dg_nqf[p1][ti]) pr = p2;
+    int pr, ti;
+    face_rule(F, pr, ti);
     const int nq = d_dg_nqf[pr][ti];
-    __syncthreads();  // shared arrays of the previous face are free
-    if (tid < 36) {
-      const int s = tid / 18, r = tid % 18;
-      if (s == 0 || interior) {
-        const int el = s ? F.el2 : F.el1;
-        const int node = el_nodes[6 * (size_t)el + r / 3];
-        sX[tid] = xyz[3 * (size_t)node + r % 3];
+    const int fo = allf ? h - h0 : 0;
+    double *sX = sX0 + 36 * fo, *sA = sA0 + 18 * fo, *sGeo = sGeo0 + fo * DGF_NQ * DGF_GEO, *sPen = sPen0 + fo;
+    __syncthreads();  // shared arrays of the previous face are free (and the prepared faces written)
+    if (!allf) {  // this face only
+      if (tid < 54) load_face(F, tid, sX, sA);
+      __syncthreads();
+      if (tid < nq) {
+        face_geometry(F, tid, sX, sA, sGeo + tid * DGF_GEO);
+      } else if (tid == DGF_THREADS - 1) {
+        sPen[0] = face_penalty(F, sX);
       }
-    } else if (tid < 54) {
-      const int t = tid - 36, s = t / 9, r = t % 9;
-      if (s == 0 || interior) {
-        const int el = s ? F.el2 : F.el1;
-        sA[t] = D_el ? D_el[9 * (size_t)el + r] : ((r % 4 == 0) ? (k_el ? k_el[el] : 1.0) : 0.0);
-      }
+      __syncthreads();
     }
-    __syncthreads();
-    if (tid < nq) {
-      const DgFacePoint Pq = dg_face_point(F.nfv, d_dg_fq[pr - 1][ti][tid], sX, F.loc1, F.side1, sA,
-                                           interior ? sX + 18 : nullptr, F.loc2, sA + 9);
-      double *G = sGeo + tid * DGF_GEO;
-      G[0] = Pq.e1.x; G[1] = Pq.e1.y; G[2] = Pq.e1.z;
-      G[3] = Pq.e2.x; G[4] = Pq.e2.y; G[5] = Pq.e2.z;
-      G[6] = Pq.v1.x; G[7] = Pq.v1.y; G[8] = Pq.v1.z;
-      G[9] = Pq.v2.x; G[10] = Pq.v2.y; G[11] = Pq.v2.z;
-      G[12] = Pq.a;
-    } else if (tid == DGF_THREADS - 1) {
-      v3 V[4];
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        const int l = i < F.nfv ? F.loc1[i] : 0;
-        V[i] = {sX[3 * l], sX[3 * l + 1], sX[3 * l + 2]};
-      }
-      const int pp = interior ? (p1 < p2 ? p1 : p2) : p1;
-      sPen[0] = pen * pp / sqrt(dg_face_area(V, F.nfv));
-    }
-    __syncthreads();
     const double fac = interior ? 0.5 : 1.0;
     const int nsum = ns1 + ns2;
     // monomial factors per (point, side); the owner-row scales per point:
@@ -152,40 +276,78 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
       double phi, g;
       dg_basis_from_factors(sFac + (2 * q + side - 1) * DGF_FAC, ex[0], ex[1], ex[2], phi, g);
       // Phi = s_t phi: the sign flip on the integer side, not the FP64 pipe
-      sPhi[q * NCOL + j] = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
-      sGam[q * NCOL + j] = g;
+      const double Phi = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
+      if (DW) {
+        fPhi[q * NCOL + j] = dw_f2(Phi);
+        fGam[q * NCOL + j] = dw_f2(g);
+      } else {
+        sPhi[q * NCOL + j] = Phi;
+        sGam[q * NCOL + j] = g;
+      }
       if ((side == 2) == (own2 != 0)) {
         const double *G = sGeo + q * DGF_GEO;
-        sL[q * NS + jj] = fma(G[13], g, G[14] * phi);
-        sM[q * NS + jj] = G[15] * phi;
+        const double L = fma(G[13], g, G[14] * phi), M = G[15] * phi;
+        if (DW) {
+          fL[q * NS + jj] = dw_f2(L);
+          fM[q * NS + jj] = dw_f2(M);
+        } else {
+          sL[q * NS + jj] = L;
+          sM[q * NS + jj] = M;
+        }
       }
     }
     __syncthreads();
     // the face's share of the diagonal block: entry k = i + NS j
     const int own_lo = own2 ? ns1 : 0;
+    if (DW) {
+      dwacc_face_block<NS, THR, (DW ? Dm::PER : 1)>(dacc, fL, fM, fPhi, fGam, nq, NCOL, tid, NS * NS, own_lo);
+    } else {
 #pragma unroll
-    for (int m = 0; m < Dm::PER; m++) {
-      const int k = tid + m * DGF_THREADS;
-      if (k < NS * NS) {
-        const int i = k % NS, j = k / NS + own_lo;
-        double a = acc[m];
-        for (int q = 0; q < nq; q++) a = fma(sL[q * NS + i], sPhi[q * NCOL + j], fma(sM[q * NS + i], sGam[q * NCOL + j], a));
-        acc[m] = a;
+      for (int m = 0; m < Dm::PER; m++) {
+        const int k = tid + m * DGF_THREADS;
+        if (k < NS * NS) {
+          const int i = k % NS, j = k / NS + own_lo;
+          double a = acc[m];
+          for (int q = 0; q < nq; q++)
+            a = fma(sL[q * NS + i], sPhi[q * NCOL + j], fma(sM[q * NS + i], sGam[q * NCOL + j], a));
+          acc[m] = a;
+        }
       }
     }
     if (interior) {
       // block (e, neighbour): NS x ns_nb, column-major, leading dimension NS
       const int nb_lo = own2 ? 0 : ns1, ns_nb = own2 ? ns1 : ns2;
       double *blk = val + F.blk;
-      for (int k = tid; k < NS * ns_nb; k += DGF_THREADS) {
-        const int i = k % NS, j = k / NS + nb_lo;
-        double a = 0.0;
-        for (int q = 0; q < nq; q++) a = fma(sL[q * NS + i], sPhi[q * NCOL + j], fma(sM[q * NS + i], sGam[q * NCOL + j], a));
-        blk[k] = a;
+      if (DW) {
+        constexpr int PB = DW ? Dm::PER : 1;
+        for (int k0 = tid; k0 < NS * ns_nb; k0 += PB * DGF_THREADS) {
+          DwAcc a[PB];
+#pragma unroll
+          for (int m = 0; m < PB; m++) a[m] = DwAcc{0.0f, 0.0f, 0.0f};
+          dwacc_face_block<NS, THR, PB>(a, fL, fM, fPhi, fGam, nq, NCOL, k0, NS * ns_nb, nb_lo);
+#pragma unroll
+          for (int m = 0; m < PB; m++)
+            if (k0 + m * DGF_THREADS < NS * ns_nb) blk[k0 + m * DGF_THREADS] = dwacc_value(a[m]);
+        }
+      } else {
+        for (int k = tid; k < NS * ns_nb; k += DGF_THREADS) {
+          const int i = k % NS, j = k / NS + nb_lo;
+          double a = 0.0;
+          for (int q = 0; q < nq; q++)
+            a = fma(sL[q * NS + i], sPhi[q * NCOL + j], fma(sM[q * NS + i], sGam[q * NCOL + j], a));
+          blk[k] = a;
+        }
       }
     } else if (tid < NS) {
       double s = 0.0;
-      for (int q = 0; q < nq; q++) s += sL[q * NS + tid];
+      for (int q = 0; q < nq; q++) {
+        if (DW) {
+          const float2 v = fL[q * NS + tid];
+          s += dw_to_double(dw(v.x, v.y));
+        } else {
+          s += sL[q * NS + tid];
+        }
+      }
       racc = fma(gval, s, racc);
     }
   }
@@ -194,7 +356,7 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
 #pragma unroll
   for (int m = 0; m < Dm::PER; m++) {
     const int k = tid + m * DGF_THREADS;
-    if (k < NS * NS) dblk[k] += acc[m];
+    if (k < NS * NS) dblk[k] += DW ? dwacc_value(dacc[DW ? m : 0]) : acc[m];
   }
   if (tid < NS) rhs[roff[e] + tid] += racc;
 }
@@ -202,21 +364,27 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
 int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                           const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                           const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
-                          const int *roff, double *val, double *rhs, int variant) {
+                          const int *roff, double *val, double *rhs, int variant, bool dword) {
   if (count <= 0) return 0;
   GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
   GB_CHECK(variant >= 0 && variant < DG_FACE_VARIANTS, "face kernel variant out of range");
-#define GB_DGF_LAUNCH(PP, VV)                                                                                   \
+#define GB_DGF_LAUNCH(PP, VV, WW)                                                                               \
   {                                                                                                             \
     constexpr int T_ = dg_face_threads(PP, VV);                                                                 \
     const size_t smem = sizeof(double) * DgFaceDims<PP, T_>::SMEM_DOUBLES;                                      \
-    GB_CUDA(cudaFuncSetAttribute(dg_prism_faces_kernel<PP, T_>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+    GB_CUDA(cudaFuncSetAttribute(dg_prism_faces_kernel<PP, T_, WW>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                  (int)smem));                                                                   \
-    dg_prism_faces_kernel<PP, T_><<<count, T_, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, xyz, k_el, \
-                                                           D_el, pen, g, boff_diag, roff, val, rhs);            \
+    dg_prism_faces_kernel<PP, T_, WW><<<count, T_, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, xyz,  \
+                                                               k_el, D_el, pen, g, boff_diag, roff, val, rhs);  \
   }
-#define GB_DGF_P(PP)                                     \
-  if (variant == 0) GB_DGF_LAUNCH(PP, 0) else GB_DGF_LAUNCH(PP, 1)
+#define GB_DGF_P(PP)                                \
+  if (dword) {                                      \
+    if (variant == 0) GB_DGF_LAUNCH(PP, 0, true)    \
+    else GB_DGF_LAUNCH(PP, 1, true)                 \
+  } else {                                          \
+    if (variant == 0) GB_DGF_LAUNCH(PP, 0, false)   \
+    else GB_DGF_LAUNCH(PP, 1, false)                \
+  }
   switch (p) {
     case 1: GB_DGF_P(1); break;
     case 2: GB_DGF_P(2); break;

@@ -233,6 +233,70 @@ def test_dg_tensor_core_faces_constant_reproduction(gb):
     assert np.max(np.abs(r)) < 1e-11 * np.max(np.abs(rhs))
 
 
+@pytest.mark.parametrize("name", ["dg_asm_p2", "dg_asm_mixed", "dg_asm_aniso"])
+def test_dg_double_word_faces_vs_reference(gb, name):
+    """Face integrals summed in double-word arithmetic give the reference's
+    assembled system to the FP64 tolerance (all degrees, p = 4 included)."""
+    g, m, F = _fixture_problem(name)
+    D = _tensors(g)
+    c = _context(gb, m, F, g["pdeg"], k=None if D is not None else g["k"], D=D, pen=float(g["pen"]),
+                 g=float(g["g"]), f=float(g["f"]))
+    c.dg_set_face_kernel(gb.DG_FACE_DWORD)
+    c.dg_assemble()
+    rp, ci, v, rhs, off = _expand(c)
+    assert np.array_equal(rp, g["row_ptr"]) and np.array_equal(ci, g["col_ind"])
+    err = sparse_rel_err(rp, ci, v, g["val"])
+    print(f"{name}: double-word faces vs reference {err:.2e}")
+    assert err < REL_TOL
+    assert vec_rel_err(rhs, g["rhs"]) < REL_TOL
+
+
+@pytest.mark.parametrize("tc", [False, True])
+@pytest.mark.parametrize("n,pmax,aniso", [(6, 1, False), (6, 2, True), (7, 3, True), (8, 4, False), (7, 4, True)])
+def test_dg_double_word_faces_vs_fp64_kernel(gb, n, pmax, aniso, tc):
+    """Whole block matrix with double-word faces (alone, or behind the tensor
+    cores for the owners they do not cover) against the FP64 face kernel
+    (uniform and mixed degrees up to 4, isotropic and anisotropic), within
+    1e-13 of the FP64 kernel's own entries."""
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(n, jitter=0.2, seed=n + pmax)
+    F = prism_faces(m)
+    rng = np.random.default_rng(n)
+    pdeg = np.full(m.nel, pmax) if n % 2 else rng.integers(1, pmax + 1, m.nel)
+    kw = {"D": anisotropic_tensors(m.nel, seed=n).reshape(m.nel, 9)} if aniso else {"k": lognormal_k(m.nel, seed=n)}
+    out = []
+    for mode in (gb.DG_FACE_FP64, gb.DG_FACE_TC_DWORD if tc else gb.DG_FACE_DWORD):
+        c = _context(gb, m, F, pdeg, g=0.3, f=1.0, **kw)
+        c.dg_set_face_kernel(mode)
+        c.dg_assemble()
+        out.append(_expand(c))
+        c.close()
+    (rp, ci, v64, r64, _), (rp2, ci2, vdw, rdw, _) = out
+    assert np.array_equal(rp, rp2) and np.array_equal(ci, ci2)
+    err = sparse_rel_err(rp, ci, vdw, v64)
+    print(f"n={n} pmax={pmax}: double-word faces vs FP64 faces {err:.2e}")
+    assert err < 1e-13
+    assert vec_rel_err(rdw, r64) < 1e-13
+
+
+def test_dg_double_word_faces_constant_reproduction(gb):
+    """With f = 0 and Dirichlet value c, the constant solves the system with
+    double-word faces (p 1..4)."""
+    from modfem_gb300.mesh import lognormal_k, prism_faces, structured_prism_mesh
+    m = structured_prism_mesh(14, jitter=0.2, seed=4)
+    F = prism_faces(m)
+    pdeg = np.random.default_rng(4).integers(1, 5, m.nel)
+    c = _context(gb, m, F, pdeg, k=lognormal_k(m.nel, seed=4), g=0.7, f=0.0)
+    c.dg_set_face_kernel(gb.DG_FACE_DWORD)
+    c.dg_assemble()
+    off = c.dg_get_structure()[0]
+    x = np.zeros(off[-1])
+    x[off[:-1]] = 0.7
+    r = c.dg_compute_residual(x)
+    vals, rhs = c.dg_get_matrix()
+    assert np.max(np.abs(r)) < 1e-11 * np.max(np.abs(rhs))
+
+
 @pytest.mark.parametrize("p", [1, 2, 3])
 def test_dg_tensor_core_volume_vs_fp64_kernel(gb, p):
     """Element blocks of the tensor-core kernel against the FP64 kernel on a
