@@ -53,9 +53,10 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help=argparse.SUPPRESS)
-    p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "dg_dwf", "batch", "std", "std_dw"], default=None,
+    p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "dg_dwf", "dg_dw", "batch", "std", "std_dw"], default=None,
                    help="small cases for ncu captures: DG p=3 anisotropic (n^3 x 2 prisms, --n), 3 assemblies "
-                        "(FP64, tensor-core volume, tensor-core volume and faces, or FP64 volume and double-word faces) and one "
+                        "(FP64, tensor-core volume, tensor-core volume and faces, FP64 volume and double-word faces, or "
+                        "double-word volume and faces) and one "
                         "block residual; or the mixed batch "
                         "(40,000 prisms + 30,000 tetrahedra, p 1..4), 3 runs; or the std prism assembly "
                         "(FP64 or double-word element arithmetic, n^3 x 2 prisms), 3 assemblies")
@@ -102,8 +103,10 @@ def run_profile_case(args):
     c.dg_set_degrees(np.full(m.nel, 3))
     c.dg_set_faces(prism_faces(m), penalty=10.0)
     c.dg_build_structure()
-    c.dg_set_volume_kernel(gb.DG_VOLUME_TC if args.profile in ("dg_tc", "dg_tcf") else gb.DG_VOLUME_FP64)
-    c.dg_set_face_kernel({"dg_tcf": gb.DG_FACE_TC, "dg_dwf": gb.DG_FACE_DWORD}.get(args.profile, gb.DG_FACE_FP64))
+    c.dg_set_volume_kernel({"dg_tc": gb.DG_VOLUME_TC, "dg_tcf": gb.DG_VOLUME_TC,
+                            "dg_dw": gb.DG_VOLUME_DWORD}.get(args.profile, gb.DG_VOLUME_FP64))
+    c.dg_set_face_kernel({"dg_tcf": gb.DG_FACE_TC, "dg_dwf": gb.DG_FACE_DWORD,
+                          "dg_dw": gb.DG_FACE_DWORD}.get(args.profile, gb.DG_FACE_FP64))
     for _ in range(3):
         c.dg_assemble()
     r = c.dg_compute_residual(np.zeros(c.dg_ndof))
@@ -340,11 +343,13 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
         vta, _ = c.dg_get_matrix()
         ta_dev = float(np.max(np.abs(vta - v64)) / np.max(np.abs(v64)))
         del vta
-        # split-BF16 volume with double-word faces: alone (all degrees), and
-        # behind the tensor-core faces for the owners those do not cover
+        # double-word sums on the FP32 pipes for volume and faces (all
+        # degrees), and the tensor cores where they apply with double words
+        # for the rest
         dwf = {}
-        for key, fmode in (("double_word_faces", gb.DG_FACE_DWORD), ("tensor_core_and_double_word_faces",
-                                                                      gb.DG_FACE_TC_DWORD)):
+        for key, vmode, fmode in (("double_word_assembly", gb.DG_VOLUME_DWORD, gb.DG_FACE_DWORD),
+                                  ("fastest_assembly", gb.DG_VOLUME_DWORD, gb.DG_FACE_TC_DWORD)):
+            c.dg_set_volume_kernel(vmode)
             c.dg_set_face_kernel(fmode)
             c.dg_assemble()
             tt = np.zeros(3)
@@ -385,9 +390,14 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
                                      "max_abs_diff_vs_fp64_rel_to_max": ta_dev,
                                      "note": "tcgen05 split-BF16 volume and faces (owners and neighbours p <= 3; "
                                              "others stay FP64)"},
-            "tensor_core_volume_double_word_faces": dict(
-                dwf, note="tcgen05 split-BF16 volume (p <= 3); faces summed in double-word arithmetic on the FP32 "
-                          "pipes (all degrees), alone or behind the tensor-core face kernel"),
+            "double_word_assembly": dict(
+                dwf["double_word_assembly"],
+                note="volume and face entries summed in double-word (float pair) arithmetic on the FP32 pipes, "
+                     "all degrees"),
+            "fastest_assembly": dict(
+                dwf["fastest_assembly"],
+                note="double-word volume (all degrees); split-BF16 tensor-core faces (owners and neighbours p <= 3), "
+                     "double-word faces for the rest"),
             "tf32_volume": {"volume_ms": vol_tf, "assemble_ms": tot_tf, "elem_per_s": m.nel / (tot_tf * 1e-3),
                             "max_abs_diff_vs_fp64_rel_to_max": tf_dev,
                             "note": "tcgen05 kind::tf32, hi/lo operands, FP32 accumulation (p <= 3)"},

@@ -183,10 +183,16 @@ int gbfem_dg_set_faces(gbfem_ctx ctx, int nfa, const int *fa_type, const int *fa
  * accuracy; or GBFEM_DG_VOLUME_TF32, the tensor cores with TF32 hi/lo
  * operands and FP32 accumulation (about 1e-6 of the entry scale: an
  * approximate matrix, for comparison).  The tensor-core kernels cover
- * p = 1..3; p = 4 elements keep the FP64 kernel. */
+ * p = 1..3; p = 4 elements keep the FP64 kernel.  GBFEM_DG_VOLUME_DWORD:
+ * the FP64 kernel's algebra with each stiffness entry summed in double-word
+ * (float pair) arithmetic on the FP32 pipes (errors of order 2^-48 of the
+ * summed magnitudes), all degrees; GBFEM_DG_VOLUME_TC_DWORD: split BF16 on
+ * the tensor cores for p = 1..3 and the double-word kernel for p = 4. */
 #define GBFEM_DG_VOLUME_FP64 0
 #define GBFEM_DG_VOLUME_TC 1
 #define GBFEM_DG_VOLUME_TF32 2
+#define GBFEM_DG_VOLUME_DWORD 3
+#define GBFEM_DG_VOLUME_TC_DWORD 4
 int gbfem_dg_set_volume_kernel(gbfem_ctx ctx, int mode);
 /* Face-integral kernel (no reference counterpart): GBFEM_DG_FACE_FP64 or
  * GBFEM_DG_FACE_TC, the tensor cores with split BF16 products (seven 8-bit

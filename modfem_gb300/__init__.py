@@ -19,7 +19,7 @@ SCATTER_ATOMIC, SCATTER_COLOR = 0, 1
 OPT_CACHE_TABLES = 1
 OPT_STD_ARITH = 2
 STD_FP64, STD_DWORD = 0, 1
-DG_VOLUME_FP64, DG_VOLUME_TC, DG_VOLUME_TF32 = 0, 1, 2
+DG_VOLUME_FP64, DG_VOLUME_TC, DG_VOLUME_TF32, DG_VOLUME_DWORD, DG_VOLUME_TC_DWORD = 0, 1, 2, 3, 4
 DG_FACE_FP64, DG_FACE_TC, DG_FACE_DWORD, DG_FACE_TC_DWORD = 0, 1, 2, 3
 
 # (name, restype, argtypes) of every symbol include/modfem_gb300.h declares

@@ -682,7 +682,8 @@ int gbfem_dg_set_faces(gbfem_ctx c, int nfa, const int *fa_type, const int *fa_b
 
 int gbfem_dg_set_volume_kernel(gbfem_ctx c, int mode) {
   GB_CHECK(c, "null context");
-  GB_CHECK(mode == GBFEM_DG_VOLUME_FP64 || mode == GBFEM_DG_VOLUME_TC || mode == GBFEM_DG_VOLUME_TF32,
+  GB_CHECK(mode == GBFEM_DG_VOLUME_FP64 || mode == GBFEM_DG_VOLUME_TC || mode == GBFEM_DG_VOLUME_TF32 ||
+               mode == GBFEM_DG_VOLUME_DWORD || mode == GBFEM_DG_VOLUME_TC_DWORD,
            "unknown DG volume kernel");
   c->dg_volume_mode = mode;
   return 0;
@@ -888,7 +889,11 @@ int gbfem_dg_assemble(gbfem_ctx c) {
   int launches = 0;
   // volume terms write every diagonal block and the rhs; the face kernel then
   // adds to those and writes every off-diagonal block: nothing to clear
-  const bool tc = c->dg_volume_mode == GBFEM_DG_VOLUME_TC || c->dg_volume_mode == GBFEM_DG_VOLUME_TF32;
+  const bool tc = c->dg_volume_mode == GBFEM_DG_VOLUME_TC || c->dg_volume_mode == GBFEM_DG_VOLUME_TF32 ||
+                  c->dg_volume_mode == GBFEM_DG_VOLUME_TC_DWORD;
+  // double-word stiffness sums: for every degree, or for those the tensor
+  // cores do not cover
+  const bool dwv = c->dg_volume_mode == GBFEM_DG_VOLUME_DWORD || c->dg_volume_mode == GBFEM_DG_VOLUME_TC_DWORD;
   if (tc) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
   cudaEventRecord(c->ev0, c->stream);
   for (int p = 1; p <= 4; p++) {
@@ -898,7 +903,7 @@ int gbfem_dg_assemble(gbfem_ctx c) {
       r = gbfem::launch_dg_tet_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
                                         c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->dg_boff_diag_d.p,
                                         c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
-    else if (tc && gbfem::dg_tc_supported(p))
+    else if (tc && gbfem::dg_tc_supported(p))  // TC_DWORD: split BF16 on the tensor cores
       r = gbfem::launch_dg_tc_volume(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->el_nodes.p,
                                      c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->dg_boff_diag_d.p, c->dg_roff_d.p,
                                      c->dg_val.p, c->dg_rhs.p, c->err.p,
@@ -907,7 +912,7 @@ int gbfem_dg_assemble(gbfem_ctx c) {
       r = gbfem::launch_dg_prism_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
                                           c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,
                                           c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p,
-                                          c->dg_var_vol[p]);
+                                          c->dg_var_vol[p], dwv);
     GB_TRY(r);
     launches += r;
   }

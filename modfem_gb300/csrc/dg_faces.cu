@@ -64,29 +64,9 @@ struct DgFaceDims {
 // terms of the low words), the high parts summed by TwoSum, every rounding
 // error collected in a float and folded back every four points.  The error
 // stays of order u^2 = 2^-48 of the summed magnitudes, against the FP64
-// kernel's 2 nq FP64 FMAs per entry at 1/64 of the FP32 issue rate.
-struct DwAcc {
-  float h, l, e;  // value h + l + e
-};
-__device__ __forceinline__ void dwacc_prod(DwAcc &a, float2 x, float2 y) {
-  const float p = f_mul(x.x, y.x);
-  float pe = f_fma(x.x, y.x, -p);
-  pe = f_fma(x.x, y.y, pe);
-  pe = f_fma(x.y, y.x, pe);
-  const dw s = two_sum(a.h, p);
-  a.h = s.h;
-  a.e = f_add(a.e, f_add(s.l, pe));
-}
-__device__ __forceinline__ void dwacc_fold(DwAcc &a) {
-  const dw r = fast_two_sum(a.h, f_add(a.l, a.e));
-  a.h = r.h;
-  a.l = r.l;
-  a.e = 0.0f;
-}
-__device__ __forceinline__ double dwacc_value(DwAcc a) {
-  dwacc_fold(a);
-  return dw_to_double(dw(a.h, a.l));
-}
+// kernel's 2 nq FP64 FMAs per entry at 1/64 of the FP32 issue rate
+// (accumulator: DwAcc, dword.cuh).
+
 // Entries k = k0 + m THR (m < PER, k < kend) of an NS-row block: row
 // i = k % NS, table column j = k / NS + col_lo; sum over the points of
 // L_i Phi_j + M_i Gam_j into a[m].  The PER chains run interleaved (each
@@ -122,10 +102,6 @@ __device__ __forceinline__ void dwacc_face_block(DwAcc (&a)[PER], const float2 *
   }
 #pragma unroll
   for (int m = 0; m < PER; m++) dwacc_fold(a[m]);
-}
-__device__ __forceinline__ float2 dw_f2(double v) {
-  const dw d = dw_from_double(v);
-  return make_float2(d.h, d.l);
 }
 
 template <int P, int THR, bool DW>

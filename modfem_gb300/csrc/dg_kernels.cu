@@ -69,9 +69,18 @@ int dg_tables_for_device(int device, DgDeviceTables **out) {
       GB_CUDA(cudaMemcpy(d, D.data(), D.size() * sizeof(double), cudaMemcpyHostToDevice));
       GB_CUDA(cudaMemcpy(ph, PHI.data(), PHI.size() * sizeof(double), cudaMemcpyHostToDevice));
       GB_CUDA(cudaMemcpy(qp, QP.data(), QP.size() * sizeof(double), cudaMemcpyHostToDevice));
+      std::vector<float2> Dw(D.size());
+      for (size_t i = 0; i < D.size(); i++) {
+        const float h = (float)D[i];
+        Dw[i] = make_float2(h, (float)(D[i] - (double)h));
+      }
+      float2 *dw = nullptr;
+      GB_CUDA(cudaMalloc(&dw, Dw.size() * sizeof(float2)));
+      GB_CUDA(cudaMemcpy(dw, Dw.data(), Dw.size() * sizeof(float2), cudaMemcpyHostToDevice));
       g_dg_tables[device].D[p] = d;
       g_dg_tables[device].PHI[p] = ph;
       g_dg_tables[device].QP[p] = qp;
+      g_dg_tables[device].Ddw[p] = dw;
     }
     g_dg_tables_ready[device] = true;
   }
@@ -127,19 +136,60 @@ __global__ void __launch_bounds__(THR) dg_prism_elements_kernel(
                                    true);
 }
 
+// The same elements with the stiffness summed in double-word arithmetic
+// (dg_prism_volume_body_dw).
+template <int P, int THR, int QC>
+__global__ void __launch_bounds__(THR) dg_prism_elements_dw_kernel(
+    int count, const int *__restrict__ ent_el, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
+    const double *__restrict__ k_el, const double *__restrict__ D_el, double f, const double *__restrict__ Dtab,
+    const float2 *__restrict__ Ddw, const double *__restrict__ PHItab, const double *__restrict__ QPtab,
+    const long long *__restrict__ boff, const int *__restrict__ roff, double *__restrict__ val,
+    double *__restrict__ rhs) {
+  using Dm = DgDims<P, THR, QC>;
+  __shared__ double sG[Dm::NQ][6];
+  __shared__ double sV[Dm::NQ];
+  __shared__ float2 sT[QC][3][Dm::NS];
+  __shared__ double sX[18];
+  __shared__ double sA[9];
+  const int bi = blockIdx.x;
+  if (bi >= count) return;
+  const int e = ent_el[bi];
+  const int tid = threadIdx.x;
+  if (tid < 6) {
+    const int n = el_nodes[6 * (size_t)e + tid];
+    sX[3 * tid] = xyz[3 * (size_t)n];
+    sX[3 * tid + 1] = xyz[3 * (size_t)n + 1];
+    sX[3 * tid + 2] = xyz[3 * (size_t)n + 2];
+  }
+  if (tid < 9) {
+    if (D_el)
+      sA[tid] = D_el[9 * (size_t)e + tid];
+    else
+      sA[tid] = (tid == 0 || tid == 4 || tid == 8) ? (k_el ? k_el[e] : 1.0) : 0.0;
+  }
+  dg_prism_volume_body_dw<P, THR, QC>(sX, sA, f, Dtab, Ddw, PHItab, QPtab, val + boff[e], rhs + roff[e], sG, sV, sT,
+                                      tid);
+}
+
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                              const double *xyz, const double *k_el, const double *D_el, double f,
-                             const long long *boff, const int *roff, double *val, double *rhs, int variant) {
+                             const long long *boff, const int *roff, double *val, double *rhs, int variant,
+                             bool dword) {
   if (count <= 0) return 0;
   GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
   GB_CHECK(variant >= 0 && variant < DG_VOL_VARIANTS, "volume kernel variant out of range");
   DgDeviceTables *tb = nullptr;
   int r = dg_tables_for_device(device, &tb);
   if (r < 0) return r;
-#define GB_DG_LAUNCH(PP, VV)                                                                               \
-  dg_prism_elements_kernel<PP, dg_vol_threads(PP, VV), dg_vol_qchunk(PP, VV)>                             \
-      <<<count, dg_vol_threads(PP, VV), 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, tb->D[PP],    \
-                                                 tb->PHI[PP], tb->QP[PP], boff, roff, val, rhs)
+#define GB_DG_LAUNCH(PP, VV)                                                                                 \
+  if (dword)                                                                                                 \
+    dg_prism_elements_dw_kernel<PP, dg_vol_threads(PP, VV), dg_vol_qchunk(PP, VV)>                           \
+        <<<count, dg_vol_threads(PP, VV), 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, tb->D[PP],    \
+                                                   tb->Ddw[PP], tb->PHI[PP], tb->QP[PP], boff, roff, val, rhs); \
+  else                                                                                                       \
+    dg_prism_elements_kernel<PP, dg_vol_threads(PP, VV), dg_vol_qchunk(PP, VV)>                              \
+        <<<count, dg_vol_threads(PP, VV), 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, tb->D[PP],    \
+                                                   tb->PHI[PP], tb->QP[PP], boff, roff, val, rhs)
 #define GB_DG_P(PP)                  \
   switch (variant) {                 \
     case 0: GB_DG_LAUNCH(PP, 0); break; \

@@ -13,6 +13,7 @@
 // passes write = false and computes on whatever sX/sA hold.
 #pragma once
 
+#include "dword.cuh"
 #include "prism_std.cuh"
 
 namespace gbfem {
@@ -27,17 +28,14 @@ struct DgDims {
   static constexpr int PER_THREAD = (NSYM + THREADS - 1) / THREADS;
 };
 
-// shared scratch: sG[NQ][6], sV[NQ], sT[QC][3][NS]
+// Geometric factors G_q, V_q at the points and the load vector (both forms)
 template <int P, int THR, int QC>
-__device__ __forceinline__ void dg_prism_volume_body(const double *sX, const double *sA, double f,
-                                                     const double *__restrict__ Dtab,
-                                                     const double *__restrict__ PHItab,
-                                                     const double *__restrict__ QPtab, double *blk,
-                                                     double *rhs_out, double (*sG)[6], double *sV,
-                                                     double (*sT)[3][DgDims<P, THR, QC>::NS], int tid,
-                                                     bool write) {
+__device__ __forceinline__ void dg_volume_points(const double *sX, const double *sA, double f,
+                                                 const double *__restrict__ PHItab,
+                                                 const double *__restrict__ QPtab, double *rhs_out,
+                                                 double (*sG)[6], double *sV, int tid, bool write) {
   using Dm = DgDims<P, THR, QC>;
-  constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS, DG_QCHUNK = Dm::QCHUNK;
+  constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS;
   __syncthreads();
   // geometric factors at the points
   for (int q = tid; q < NQ; q += DG_THREADS) {
@@ -83,6 +81,31 @@ __device__ __forceinline__ void dg_prism_volume_body(const double *sX, const dou
     for (int q = 0; q < NQ; q++) r = fma(PHItab[(size_t)q * NS + u], sV[q], r);
     if (write) rhs_out[u] = f * r;
   }
+}
+
+// upper entry k of an NS x NS block as (u, w), u <= w (row u holds (u, u..NS-1))
+template <int NS>
+__device__ __forceinline__ void dg_upper_entry(int k, int &u, int &w) {
+  u = 0;
+  while (k >= NS - u) {
+    k -= NS - u;
+    u++;
+  }
+  w = u + k;
+}
+
+// shared scratch: sG[NQ][6], sV[NQ], sT[QC][3][NS]
+template <int P, int THR, int QC>
+__device__ __forceinline__ void dg_prism_volume_body(const double *sX, const double *sA, double f,
+                                                     const double *__restrict__ Dtab,
+                                                     const double *__restrict__ PHItab,
+                                                     const double *__restrict__ QPtab, double *blk,
+                                                     double *rhs_out, double (*sG)[6], double *sV,
+                                                     double (*sT)[3][DgDims<P, THR, QC>::NS], int tid,
+                                                     bool write) {
+  using Dm = DgDims<P, THR, QC>;
+  constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS, DG_QCHUNK = Dm::QCHUNK;
+  dg_volume_points<P, THR, QC>(sX, sA, f, PHItab, QPtab, rhs_out, sG, sV, tid, write);
   // stiffness: upper entries k = tid + j * DG_THREADS
   double acc[Dm::PER_THREAD];
   int uu[Dm::PER_THREAD], ww[Dm::PER_THREAD];
@@ -140,6 +163,79 @@ __device__ __forceinline__ void dg_prism_volume_body(const double *sX, const dou
     const int u = uu[j], w = ww[j];
     blk[w + (size_t)NS * u] = acc[j];
     if (u != w) blk[u + (size_t)NS * w] = acc[j];
+  }
+}
+
+// Double-word form of the stiffness (the points and the load vector as
+// above): T_q = G_q D_q formed in FP64 and stored as double words, every
+// upper entry a sum over the points of 3 products of double words (D from
+// the double-word table) by exact products and TwoSum chains (DwAcc), the
+// entries of a thread interleaved point by point.  Entries within about
+// 2^-48 of the summed magnitudes; the FP64 pipe keeps only the geometry and
+// the T_q (9 FMAs per point and function).
+template <int P, int THR, int QC>
+__device__ __forceinline__ void dg_prism_volume_body_dw(const double *sX, const double *sA, double f,
+                                                        const double *__restrict__ Dtab,
+                                                        const float2 *__restrict__ Ddw,
+                                                        const double *__restrict__ PHItab,
+                                                        const double *__restrict__ QPtab, double *blk,
+                                                        double *rhs_out, double (*sG)[6], double *sV,
+                                                        float2 (*sT)[3][DgDims<P, THR, QC>::NS], int tid) {
+  using Dm = DgDims<P, THR, QC>;
+  constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS, DG_QCHUNK = Dm::QCHUNK;
+  constexpr int PER = Dm::PER_THREAD;
+  dg_volume_points<P, THR, QC>(sX, sA, f, PHItab, QPtab, rhs_out, sG, sV, tid, true);
+  DwAcc acc[PER];
+  int uu[PER], ww[PER];
+#pragma unroll
+  for (int j = 0; j < PER; j++) {
+    acc[j] = DwAcc{0.0f, 0.0f, 0.0f};
+    const int k = tid + j * DG_THREADS;
+    if (k < Dm::NSYM) {
+      dg_upper_entry<NS>(k, uu[j], ww[j]);
+    } else {
+      uu[j] = 0;
+      ww[j] = -1;
+    }
+  }
+  for (int q0 = 0; q0 < NQ; q0 += DG_QCHUNK) {
+    const int qn = NQ - q0 < DG_QCHUNK ? NQ - q0 : DG_QCHUNK;
+    __syncthreads();
+    for (int t = tid; t < qn * NS; t += DG_THREADS) {
+      const int ql = t / NS, w = t % NS, q = q0 + ql;
+      const double *Dq = Dtab + (size_t)q * 3 * NS;
+      const double d0 = Dq[w], d1 = Dq[NS + w], d2 = Dq[2 * NS + w];
+      const double *g = sG[q];
+      sT[ql][0][w] = dw_f2(fma(g[0], d0, fma(g[1], d1, g[2] * d2)));
+      sT[ql][1][w] = dw_f2(fma(g[1], d0, fma(g[3], d1, g[4] * d2)));
+      sT[ql][2][w] = dw_f2(fma(g[2], d0, fma(g[4], d1, g[5] * d2)));
+    }
+    __syncthreads();
+    for (int ql = 0; ql < qn; ql++) {
+      const float2 *Dq = Ddw + (size_t)(q0 + ql) * 3 * NS;
+#pragma unroll
+      for (int j = 0; j < PER; j++) {
+        if (ww[j] < 0) continue;
+        const int u = uu[j], w = ww[j];
+        dwacc_prod(acc[j], __ldg(Dq + u), sT[ql][0][w]);
+        dwacc_prod(acc[j], __ldg(Dq + NS + u), sT[ql][1][w]);
+        dwacc_prod(acc[j], __ldg(Dq + 2 * NS + u), sT[ql][2][w]);
+      }
+      if (ql & 1) {
+#pragma unroll
+        for (int j = 0; j < PER; j++) dwacc_fold(acc[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < PER; j++) dwacc_fold(acc[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < PER; j++) {
+    if (ww[j] < 0) continue;
+    const int u = uu[j], w = ww[j];
+    const double v = dwacc_value(acc[j]);
+    blk[w + (size_t)NS * u] = v;
+    if (u != w) blk[u + (size_t)NS * w] = v;
   }
 }
 

@@ -229,4 +229,39 @@ DW_HD double f_to_double_bits(float x) {
 // (h + l rounded to 53 bits)
 DW_HD double dw_to_double(dw v) { return f_to_double_bits(v.h) + f_to_double_bits(v.l); }
 
+// double -> double word as a float2 (h, l)
+DW_HD float2 dw_f2(double v) {
+  const dw d = dw_from_double(v);
+  float2 r;
+  r.x = d.h;
+  r.y = d.l;
+  return r;
+}
+
+// Accumulator of a long sum of double-word products: the high parts summed
+// by TwoSum into h, every rounding error (of the products' TwoProd and of
+// the TwoSums) collected in the float e and folded into the pair (h, l) every
+// few terms.  Error of order u^2 = 2^-48 of the summed magnitudes.
+struct DwAcc {
+  float h, l, e;  // value h + l + e
+};
+DW_HD void dwacc_prod(DwAcc &a, float2 x, float2 y) {
+  const float p = f_mul(x.x, y.x);
+  float pe = f_fma(x.x, y.x, -p);
+  pe = f_fma(x.x, y.y, pe);
+  pe = f_fma(x.y, y.x, pe);
+  const dw s = two_sum(a.h, p);
+  a.h = s.h;
+  a.e = f_add(a.e, f_add(s.l, pe));
+}
+DW_HD void dwacc_fold(DwAcc &a) {
+  const dw r = fast_two_sum(a.h, f_add(a.l, a.e));
+  a.h = r.h;
+  a.l = r.l;
+  a.e = 0.0f;
+}
+DW_HD double dwacc_value(DwAcc a) {
+  dwacc_fold(a);
+  return dw_to_double(dw(a.h, a.l));
+}
 }  // namespace gbfem

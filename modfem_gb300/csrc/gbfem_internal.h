@@ -62,6 +62,7 @@ struct DgDeviceTables {
   const double *D[5];
   const double *PHI[5];
   const double *QP[5];
+  const float2 *Ddw[5];  // D as double words (h, l) for the double-word volume kernel
 };
 int dg_tables_for_device(int device, DgDeviceTables **out);
 
@@ -173,7 +174,7 @@ int launch_dg_tc_volume(cudaStream_t st, int device, int p, int count, const int
                         const int *roff, double *val, double *rhs, int *err, int mode);
 int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                              const double *xyz, const double *k_el, const double *D_el, double f,
-                             const long long *boff, const int *roff, double *val, double *rhs, int variant);
+                             const long long *boff, const int *roff, double *val, double *rhs, int variant, bool dword = false);
 
 }  // namespace gbfem
 

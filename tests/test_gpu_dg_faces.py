@@ -297,6 +297,60 @@ def test_dg_double_word_faces_constant_reproduction(gb):
     assert np.max(np.abs(r)) < 1e-11 * np.max(np.abs(rhs))
 
 
+@pytest.mark.parametrize("name", ["dg_asm_p2", "dg_asm_mixed", "dg_asm_aniso"])
+def test_dg_double_word_assembly_vs_reference(gb, name):
+    """Volume and face entries summed in double-word arithmetic give the
+    reference's assembled system to the FP64 tolerance; likewise the tensor
+    cores with double words behind them."""
+    g, m, F = _fixture_problem(name)
+    D = _tensors(g)
+    for vmode, fmode in ((gb.DG_VOLUME_DWORD, gb.DG_FACE_DWORD), (gb.DG_VOLUME_TC_DWORD, gb.DG_FACE_TC_DWORD)):
+        c = _context(gb, m, F, g["pdeg"], k=None if D is not None else g["k"], D=D, pen=float(g["pen"]),
+                     g=float(g["g"]), f=float(g["f"]))
+        c.dg_set_volume_kernel(vmode)
+        c.dg_set_face_kernel(fmode)
+        c.dg_assemble()
+        rp, ci, v, rhs, off = _expand(c)
+        assert np.array_equal(rp, g["row_ptr"]) and np.array_equal(ci, g["col_ind"])
+        err = sparse_rel_err(rp, ci, v, g["val"])
+        print(f"{name} modes {vmode}/{fmode}: vs reference {err:.2e}")
+        assert err < REL_TOL
+        assert vec_rel_err(rhs, g["rhs"]) < REL_TOL
+        c.close()
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_dg_double_word_volume_vs_fp64_kernel(gb, p):
+    """Element blocks summed in double-word arithmetic against the FP64
+    volume kernel (jittered anisotropic mesh, every degree): within 1e-13 of
+    the FP64 blocks (energy scale of each block)."""
+    from modfem_gb300.mesh import anisotropic_tensors, structured_prism_mesh
+    m = structured_prism_mesh(7, jitter=0.2, seed=20 + p)
+    D = anisotropic_tensors(m.nel, seed=p).reshape(m.nel, 9)
+    out = []
+    for mode in (gb.DG_VOLUME_FP64, gb.DG_VOLUME_DWORD):
+        c = gb.Context(0)
+        c.set_mesh(m)
+        c.set_coefficients(D=D, f=1.0, g=0.0)
+        c.dg_set_degrees(np.full(m.nel, p))
+        c.dg_build_structure()
+        c.dg_set_volume_kernel(mode)
+        c.dg_assemble()
+        out.append(c.dg_get_matrix())
+        off, bptr, bcol, boff = c.dg_get_structure()
+        c.close()
+    from _util import mat_rel_err
+    ns = [0, 6, 18, 40, 75][p]
+    worst = 0.0
+    for e in range(m.nel):
+        K64 = out[0][0][boff[e]:boff[e] + ns * ns].reshape(ns, ns)
+        Kdw = out[1][0][boff[e]:boff[e] + ns * ns].reshape(ns, ns)
+        worst = max(worst, mat_rel_err(Kdw, K64))
+    print(f"p={p}: double-word volume vs FP64 {worst:.2e}")
+    assert worst < 1e-13, worst
+    assert np.array_equal(out[1][1], out[0][1])  # the load vector is the FP64 kernel's
+
+
 @pytest.mark.parametrize("p", [1, 2, 3])
 def test_dg_tensor_core_volume_vs_fp64_kernel(gb, p):
     """Element blocks of the tensor-core kernel against the FP64 kernel on a
