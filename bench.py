@@ -446,6 +446,16 @@ def bench_batch(gb, local, steps, fp64_peak):
         b.run()
     ms = [b.run() for _ in range(steps)]
     step_ms = float(np.mean(ms))
+    v64, _ = b.get()
+    # the same launch with the prism stiffness sums in double-word arithmetic
+    b.set_arith(True)
+    for _ in range(2):
+        b.run()
+    dw_ms = float(np.mean([b.run() for _ in range(steps)]))
+    vdw, _ = b.get()
+    dw_dev = float(np.max(np.abs(vdw - v64)) / np.max(np.abs(v64)))
+    del v64, vdw
+    b.set_arith(False)
     pfma = sum(dg_fma_per_element(q) * int(np.sum(pp == q)) for q in range(1, 5))
     tfma = sum(tet_fma_per_element(q) * int(np.sum(tp == q)) for q in range(1, 5))
     out_bytes = 8 * (nval + nrhs)
@@ -504,6 +514,9 @@ def bench_batch(gb, local, steps, fp64_peak):
         "output_gbs": out_bytes / (step_ms * 1e-3) / 1e9,
         "tets_alone_ms": tet_ms, "tets_alone_output_gbs": 8 * (tnv + tnr) / (tet_ms * 1e-3) / 1e9,
         "prisms_per_degree_kernels_ms": per_degree_ms,
+        "double_word_prisms": {"step_ms": dw_ms, "elem_per_s": (NP + NT) / (dw_ms * 1e-3),
+                               "speedup_vs_fp64": step_ms / dw_ms, "max_abs_diff_vs_fp64_rel_to_max": dw_dev,
+                               "note": "prism stiffness sums in double-word (float pair) arithmetic, tetrahedra FP64"},
         "e2e_ms": e2e_s * 1e3, "e2e_elem_per_s": (NP + NT) / e2e_s,
         "e2e_note": "page-locked host arrays: upload of geometry and tensors, tile build, graph capture, run, "
                     "download of "

@@ -392,6 +392,11 @@ int gbfem_batch_set_layout(gbfem_batch batch, const long long *val_off, const in
  * elements per tile).  Either pointer may be NULL.  Every variant gives the
  * same bits. */
 int gbfem_batch_set_variants(gbfem_batch batch, const int *prism_v, const int *tet_v);
+/* Arithmetic of the prism stiffness sums: 0 FP64 (default), 1 double word
+ * (float pairs on the FP32 pipes, exact products and TwoSum chains; entries
+ * within about 2^-48 of the summed magnitudes).  Tetrahedra (6 FMAs per
+ * entry against exact reference matrices) stay FP64. */
+int gbfem_batch_set_arith(gbfem_batch batch, int dword);
 /* Times every variant of every (type, degree) class present on up to
  * `sample` of its elements (<= 0: 16384), keeps the fastest.  prism_v[5],
  * tet_v[5] receive the choices, ms[50] the timings ((type*5 + p)*5 + v,

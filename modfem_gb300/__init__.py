@@ -78,6 +78,7 @@ SIGNATURES = [
     ("gbfem_batch_set", _ci, [_vp, _ci, _vp, _vp, _vp, _ci, _vp, _vp, _vp, _cd, _pll, _pll]),
     ("gbfem_batch_set_layout", _ci, [_vp, _vp, _vp, _cll, _cll]),
     ("gbfem_batch_set_variants", _ci, [_vp, _vp, _vp]),
+    ("gbfem_batch_set_arith", _ci, [_vp, _ci]),
     ("gbfem_batch_autotune", _ci, [_vp, _ci, _vp, _vp, _vp]),
     ("gbfem_batch_run", _ci, [_vp, _pd]),
     ("gbfem_batch_get", _ci, [_vp, _vp, _vp]),
@@ -418,6 +419,10 @@ class Batch:
         ro = _i32(rhs_off)
         self._check(self.L.gbfem_batch_set_layout(self._h, _p(vo), _p(ro), nval, nrhs))
         self.nval, self.nrhs, self.layout = nval, nrhs, (vo, ro)
+
+    def set_arith(self, dword):
+        """Prism stiffness sums in FP64 (False) or double-word arithmetic (True)."""
+        self._check(self.L.gbfem_batch_set_arith(self._h, 1 if dword else 0))
 
     def set_variants(self, prism=None, tet=None):
         """Variants per degree, dicts or length-5 sequences indexed by p."""

@@ -68,6 +68,7 @@ struct DgBatchTile {
 
 struct DgBatchTables {
   const double *D[GB_DG_PMAX + 1], *PHI[GB_DG_PMAX + 1], *QP[GB_DG_PMAX + 1];  // prisms
+  const float2 *Ddw[GB_DG_PMAX + 1];  // prisms, D as double words
   const double *T[GB_DG_PMAX + 1];    // tets: 6 x (ns(ns+1)/2) packed upper entries
   const double *MOM[GB_DG_PMAX + 1];  // tets: int_ref phi_i
 };
@@ -80,6 +81,7 @@ struct DgBatchArgs {
   const int *proff, *troff;         // rhs offset
   double *val, *rhs;
   double f;
+  int dword;  // prism stiffness sums in double-word arithmetic
 };
 
 template <int P, int THR, int QC>
@@ -96,8 +98,12 @@ __device__ void dgb_prism(const DgBatchTables &tb, const DgBatchArgs &a, const D
   double(*sT)[3][Dm::NS] = (double(*)[3][Dm::NS])(base + 32 + 7 * Dm::NQ);
   if (lt < 18) sX[lt] = a.pX[18 * (size_t)e + lt];
   if (lt < 9) sA[lt] = a.pA[9 * (size_t)e + lt];
-  dg_prism_volume_body<P, THR, QC>(sX, sA, a.f, tb.D[P], tb.PHI[P], tb.QP[P], a.val + a.poff[e], a.rhs + a.proff[e],
-                                   sG, sV, sT, lt, valid);
+  if (a.dword)  // uniform over the launch; the float2 slices fill the same scratch
+    dg_prism_volume_body_dw<P, THR, QC>(sX, sA, a.f, tb.D[P], tb.Ddw[P], tb.PHI[P], tb.QP[P], a.val + a.poff[e],
+                                        a.rhs + a.proff[e], sG, sV, (float2(*)[3][Dm::NS])sT, lt, valid);
+  else
+    dg_prism_volume_body<P, THR, QC>(sX, sA, a.f, tb.D[P], tb.PHI[P], tb.QP[P], a.val + a.poff[e],
+                                     a.rhs + a.proff[e], sG, sV, sT, lt, valid);
 }
 
 // The 6 geometric factors G = C^T A C / |det| (00 01 02 11 12 22) and |det|
@@ -290,6 +296,7 @@ static int dg_batch_tables(int device, DgBatchTables *out) {
       g_bt[device].D[p] = pt->D[p];
       g_bt[device].PHI[p] = pt->PHI[p];
       g_bt[device].QP[p] = pt->QP[p];
+      g_bt[device].Ddw[p] = pt->Ddw[p];
       std::vector<double> T, MOM;
       tet_tables(p, T, MOM);
       double *dT = nullptr, *dM = nullptr;
@@ -352,6 +359,7 @@ struct gbfem_batch_s {
   int np = 0, nt = 0, ntiles = 0;
   int var_prism[5] = {0, 0, 0, 0, 0}, var_tet[5] = {2, 2, 2, 2, 2};
   double f = 1.0;
+  int dword = 0;
   long long nval = 0, nrhs = 0;
   DevBuf<double> pX, pA, tX, tA, val, rhs;
   DevBuf<long long> poff, toff;
@@ -414,6 +422,7 @@ static gbfem::DgBatchArgs batch_args(gbfem_batch b) {
   a.val = b->val.p;
   a.rhs = b->rhs.p;
   a.f = b->f;
+  a.dword = b->dword;
   return a;
 }
 
@@ -603,6 +612,14 @@ int gbfem_batch_set_variants(gbfem_batch b, const int *prism_v, const int *tet_v
     if (prism_v) b->var_prism[p] = prism_v[p];
     if (tet_v) b->var_tet[p] = tet_v[p];
   }
+  GB_CUDA(cudaSetDevice(b->device));
+  return b->np + b->nt > 0 ? batch_build(b) : 0;
+}
+
+int gbfem_batch_set_arith(gbfem_batch b, int dword) {
+  GB_CHECK(b, "null batch");
+  GB_CHECK(dword == 0 || dword == 1, "arithmetic must be 0 (FP64) or 1 (double word)");
+  b->dword = dword;
   GB_CUDA(cudaSetDevice(b->device));
   return b->np + b->nt > 0 ? batch_build(b) : 0;
 }

@@ -100,6 +100,10 @@ __host__ __device__ constexpr int dg_vol_threads(int p, int v) {
                                        : (v == 0 ? 288 : v == 1 ? 224 : 288);
 }
 __host__ __device__ constexpr int dg_vol_qchunk(int p, int v) { return v == 2 ? 16 : 8; }
+// The double-word kernel is bound by issue and latency, not by the FP64
+// pipe: at p = 4 it takes 720 threads (four of the 2,850 entries each) so
+// that more warps share the SM; the other degrees keep the FP64 shapes.
+__host__ __device__ constexpr int dg_vol_threads_dw(int p, int v) { return p == 4 ? 720 : dg_vol_threads(p, v); }
 
 
 // Elements of degree P: ent_el[i] (0-based), matrix block at val + boff[e],
@@ -183,8 +187,8 @@ int launch_dg_prism_elements(cudaStream_t st, int device, int p, int count, cons
   if (r < 0) return r;
 #define GB_DG_LAUNCH(PP, VV)                                                                                 \
   if (dword)                                                                                                 \
-    dg_prism_elements_dw_kernel<PP, dg_vol_threads(PP, VV), dg_vol_qchunk(PP, VV)>                           \
-        <<<count, dg_vol_threads(PP, VV), 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, tb->D[PP],    \
+    dg_prism_elements_dw_kernel<PP, dg_vol_threads_dw(PP, VV), dg_vol_qchunk(PP, VV)>                        \
+        <<<count, dg_vol_threads_dw(PP, VV), 0, st>>>(count, ent_el, el_nodes, xyz, k_el, D_el, f, tb->D[PP], \
                                                    tb->Ddw[PP], tb->PHI[PP], tb->QP[PP], boff, roff, val, rhs); \
   else                                                                                                       \
     dg_prism_elements_kernel<PP, dg_vol_threads(PP, VV), dg_vol_qchunk(PP, VV)>                              \

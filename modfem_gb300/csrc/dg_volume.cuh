@@ -180,11 +180,12 @@ __device__ __forceinline__ void dg_prism_volume_body_dw(const double *sX, const 
                                                         const double *__restrict__ PHItab,
                                                         const double *__restrict__ QPtab, double *blk,
                                                         double *rhs_out, double (*sG)[6], double *sV,
-                                                        float2 (*sT)[3][DgDims<P, THR, QC>::NS], int tid) {
+                                                        float2 (*sT)[3][DgDims<P, THR, QC>::NS], int tid,
+                                                        bool write = true) {
   using Dm = DgDims<P, THR, QC>;
   constexpr int NS = Dm::NS, NQ = Dm::NQ, DG_THREADS = Dm::THREADS, DG_QCHUNK = Dm::QCHUNK;
   constexpr int PER = Dm::PER_THREAD;
-  dg_volume_points<P, THR, QC>(sX, sA, f, PHItab, QPtab, rhs_out, sG, sV, tid, true);
+  dg_volume_points<P, THR, QC>(sX, sA, f, PHItab, QPtab, rhs_out, sG, sV, tid, write);
   DwAcc acc[PER];
   int uu[PER], ww[PER];
 #pragma unroll
@@ -229,6 +230,7 @@ __device__ __forceinline__ void dg_prism_volume_body_dw(const double *sX, const 
 #pragma unroll
     for (int j = 0; j < PER; j++) dwacc_fold(acc[j]);
   }
+  if (!write) return;
 #pragma unroll
   for (int j = 0; j < PER; j++) {
     if (ww[j] < 0) continue;

@@ -84,6 +84,34 @@ def test_prisms_bitwise_equal_per_degree_kernel(gb):
         assert mat_rel_err(mats[m.nel + e], Ko) < REL_TOL
 
 
+def test_double_word_prisms_vs_fp64(gb):
+    """Prism blocks of the batch with double-word stiffness sums against the
+    FP64 batch (degrees 1..4, anisotropic tensors): within 1e-13 of each
+    block's energy scale; loads and tetrahedra unchanged (FP64 in both);
+    every prism variant within the same bound."""
+    m, D, p = _prisms(3, 17)
+    t, Dt, pt = _tets(1, 18)
+    b = gb.Batch(0)
+    b.set(m.coords[m.el_nodes], D, p, t.coords[t.el_nodes], Dt, pt, f=1.0)
+    b.run()
+    m64, l64 = b.blocks()
+    b.set_arith(True)
+    for pv in range(3):
+        b.set_variants([0] + [pv] * 4, None)
+        b.run()
+        mdw, ldw = b.blocks()
+        worst = max(mat_rel_err(mdw[e], m64[e]) for e in range(m.nel))
+        assert worst < 1e-13, (pv, worst)
+        for e in range(m.nel + t.nel):
+            assert np.array_equal(ldw[e], l64[e])
+        for e in range(m.nel, m.nel + t.nel):
+            assert np.array_equal(mdw[e], m64[e])
+    b.set_arith(False)
+    b.run()
+    mb, _ = b.blocks()
+    assert all(np.array_equal(mb[e], m64[e]) for e in range(m.nel + t.nel))
+
+
 def test_variants_and_replays_identical(gb):
     m, D, p = _prisms(2, 11)
     t, Dt, pt = _tets(3, 12)
