@@ -546,10 +546,26 @@ def bench_tet_dg(gb, local, steps):
         c.dg_assemble()
         tt += np.array(c.dg_last_timing()[:3])
     tot, vol, fa = tt / steps
+    v64, _ = c.dg_get_matrix()
+    # the faces summed in double-word arithmetic
+    c.dg_set_face_kernel(gb.DG_FACE_DWORD)
+    c.dg_assemble()
+    tt = np.zeros(3)
+    for _ in range(steps):
+        c.dg_assemble()
+        tt += np.array(c.dg_last_timing()[:3])
+    tot_dw, _, fa_dw = tt / steps
+    vdw, _ = c.dg_get_matrix()
+    dw_dev = float(np.max(np.abs(vdw - v64)) / np.max(np.abs(v64)))
+    del v64, vdw
+    c.dg_set_face_kernel(gb.DG_FACE_FP64)
+    c.dg_assemble()
     x, it, res, rel = c.dg_solve(krylov=50, max_iter=100, tol_rel=1e-10)
     st = c.last_solve_timing()
     out = {"elements": t.nel, "faces": int(F.n), "dofs": nd, "stored_values": nv,
            "assemble_ms": tot, "volume_ms": vol, "face_ms": fa, "elem_per_s": t.nel / (tot * 1e-3),
+           "double_word_faces": {"face_ms": fa_dw, "assemble_ms": tot_dw, "face_speedup_vs_fp64": fa / fa_dw,
+                                 "max_abs_diff_vs_fp64_rel_to_max": dw_dev},
            "gmres_iterations": it, "gmres_ms_per_iteration": st[0] / max(it, 1),
            "spmv_ms": st[1] / max(st[2], 1)}
     c.close()

@@ -202,9 +202,9 @@ int gbfem_dg_set_volume_kernel(gbfem_ctx ctx, int mode);
  * kernel; or GBFEM_DG_FACE_DWORD, the FP64 kernel's algebra with the point
  * tables in double-word (float pair) form and every entry summed on the
  * FP32 pipes by exact products and sums (errors of order 2^-48 of the summed
- * magnitudes), all degrees of prism meshes; tetrahedra keep the FP64
- * kernel; or GBFEM_DG_FACE_TC_DWORD: the tensor cores where they apply and
- * the double-word kernel for the other owners. */
+ * magnitudes), all degrees, prisms and tetrahedra; or
+ * GBFEM_DG_FACE_TC_DWORD: the tensor cores where they apply (prisms) and the
+ * double-word kernel for the other owners. */
 #define GBFEM_DG_FACE_FP64 0
 #define GBFEM_DG_FACE_TC 1
 #define GBFEM_DG_FACE_DWORD 2

@@ -926,7 +926,9 @@ int gbfem_dg_assemble(gbfem_ctx c) {
         const int r = gbfem::launch_dg_tet_faces(c->stream, p, (int)c->dg_list[p].n, c->dg_list[p].p,
                                                  c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p,
                                                  c->k_el.p, c->D_el.p, c->dg_pen, c->g, c->dg_boff_diag_d.p,
-                                                 c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
+                                                 c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p,
+                                                 c->dg_face_mode == GBFEM_DG_FACE_DWORD ||
+                                                     c->dg_face_mode == GBFEM_DG_FACE_TC_DWORD);
         GB_TRY(r);
         launches += r;
         continue;

@@ -17,6 +17,7 @@
 // the off-diagonal blocks and adds its share of the diagonal block once.
 
 #include "dg_face.cuh"
+#include "dword.cuh"
 #include "gbfem_internal.h"
 
 namespace gbfem {
@@ -49,7 +50,9 @@ __device__ __forceinline__ v3 tt_face_v(const double *X, const double *A, v3 n) 
   return {v3_dot(c1, an) * rdet, v3_dot(c2, an) * rdet, v3_dot(c3, an) * rdet};
 }
 
-template <int P, int TT_THREADS = tt_threads(P)>
+// DW: the point tables as double words and every entry summed by exact
+// products and TwoSum chains (DwAcc, dword.cuh), as in the prism face kernel.
+template <int P, bool DW, int TT_THREADS = tt_threads(P)>
 __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
@@ -77,9 +80,14 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
         }
   }
   double acc[PER];
+  DwAcc dacc[DW ? PER : 1];
 #pragma unroll
   for (int m = 0; m < PER; m++) acc[m] = 0.0;
+#pragma unroll
+  for (int m = 0; m < (DW ? PER : 1); m++) dacc[m] = DwAcc{0.0f, 0.0f, 0.0f};
   double racc = 0.0;
+  float2 *fL = reinterpret_cast<float2 *>(&sL[0][0]), *fM = reinterpret_cast<float2 *>(&sM[0][0]);
+  float2 *fPhi = reinterpret_cast<float2 *>(&sPhi[0][0]), *fGam = reinterpret_cast<float2 *>(&sGam[0][0]);
   const int h0 = hf_ptr[e], h1 = hf_ptr[e + 1];
   for (int h = h0; h < h1; h++) {
     const DgHalfFace F = hf[h];
@@ -157,40 +165,76 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
       const int side = j < ns1 ? 0 : 1, jj = side == 0 ? j : j - ns1;
       double phi, g;
       dg_basis_from_factors(sFac[q][side], sExp[jj][0], sExp[jj][1], sExp[jj][2], phi, g);
-      sPhi[q][j] = side == 1 ? -phi : phi;
-      sGam[q][j] = g;
+      const double Phi = side == 1 ? -phi : phi;
+      if (DW) {
+        fPhi[q * TT_NCOL + j] = dw_f2(Phi);
+        fGam[q * TT_NCOL + j] = dw_f2(g);
+      } else {
+        sPhi[q][j] = Phi;
+        sGam[q][j] = g;
+      }
       if (side == own2) {
         const double aw = sAw[q], so = own2 ? -1.0 : 1.0;
-        sL[q][jj] = aw * fma(fac, g, so * sC[1] * phi);
-        sM[q][jj] = -so * fac * aw * phi;
+        const double L = aw * fma(fac, g, so * sC[1] * phi), M = -so * fac * aw * phi;
+        if (DW) {
+          fL[q * NS + jj] = dw_f2(L);
+          fM[q * NS + jj] = dw_f2(M);
+        } else {
+          sL[q][jj] = L;
+          sM[q][jj] = M;
+        }
       }
     }
     __syncthreads();
     // the face's share of the diagonal block: entry k = i + NS j
     const int own_lo = own2 ? ns1 : 0;
+    if (DW) {
+      dwacc_face_block<NS, TT_THREADS, (DW ? PER : 1)>(dacc, fL, fM, fPhi, fGam, nq, TT_NCOL, tid, NS * NS, own_lo);
+    } else {
 #pragma unroll
-    for (int m = 0; m < PER; m++) {
-      const int k = tid + m * TT_THREADS;
-      if (k < NS * NS) {
-        const int i = k % NS, j = k / NS + own_lo;
-        double s = acc[m];
-        for (int q = 0; q < nq; q++) s = fma(sL[q][i], sPhi[q][j], fma(sM[q][i], sGam[q][j], s));
-        acc[m] = s;
+      for (int m = 0; m < PER; m++) {
+        const int k = tid + m * TT_THREADS;
+        if (k < NS * NS) {
+          const int i = k % NS, j = k / NS + own_lo;
+          double s = acc[m];
+          for (int q = 0; q < nq; q++) s = fma(sL[q][i], sPhi[q][j], fma(sM[q][i], sGam[q][j], s));
+          acc[m] = s;
+        }
       }
     }
     if (interior) {
       // block (e, neighbour): NS x ns_nb, column-major, leading dimension NS
       const int nb_lo = own2 ? 0 : ns1, ns_nb = own2 ? ns1 : ns2;
       double *blk = val + F.blk;
-      for (int k = tid; k < NS * ns_nb; k += TT_THREADS) {
-        const int i = k % NS, j = k / NS + nb_lo;
-        double s = 0.0;
-        for (int q = 0; q < nq; q++) s = fma(sL[q][i], sPhi[q][j], fma(sM[q][i], sGam[q][j], s));
-        blk[k] = s;
+      if (DW) {
+        constexpr int PB = DW ? PER : 1;
+        for (int k0 = tid; k0 < NS * ns_nb; k0 += PB * TT_THREADS) {
+          DwAcc a[PB];
+#pragma unroll
+          for (int m = 0; m < PB; m++) a[m] = DwAcc{0.0f, 0.0f, 0.0f};
+          dwacc_face_block<NS, TT_THREADS, PB>(a, fL, fM, fPhi, fGam, nq, TT_NCOL, k0, NS * ns_nb, nb_lo);
+#pragma unroll
+          for (int m = 0; m < PB; m++)
+            if (k0 + m * TT_THREADS < NS * ns_nb) blk[k0 + m * TT_THREADS] = dwacc_value(a[m]);
+        }
+      } else {
+        for (int k = tid; k < NS * ns_nb; k += TT_THREADS) {
+          const int i = k % NS, j = k / NS + nb_lo;
+          double s = 0.0;
+          for (int q = 0; q < nq; q++) s = fma(sL[q][i], sPhi[q][j], fma(sM[q][i], sGam[q][j], s));
+          blk[k] = s;
+        }
       }
     } else if (tid < NS) {
       double s = 0.0;
-      for (int q = 0; q < nq; q++) s += sL[q][tid];
+      for (int q = 0; q < nq; q++) {
+        if (DW) {
+          const float2 v = fL[q * NS + tid];
+          s += dw_to_double(dw(v.x, v.y));
+        } else {
+          s += sL[q][tid];
+        }
+      }
       racc = fma(gval, s, racc);
     }
   }
@@ -199,7 +243,7 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
 #pragma unroll
   for (int m = 0; m < PER; m++) {
     const int k = tid + m * TT_THREADS;
-    if (k < NS * NS) dblk[k] += acc[m];
+    if (k < NS * NS) dblk[k] += DW ? dwacc_value(dacc[DW ? m : 0]) : acc[m];
   }
   if (tid < NS) rhs[roff[e] + tid] += racc;
 }
@@ -207,13 +251,18 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
 int launch_dg_tet_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                         const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                         const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
-                        const int *roff, double *val, double *rhs) {
+                        const int *roff, double *val, double *rhs, bool dword) {
   if (count <= 0) return 0;
   GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
 #define GB_TT_LAUNCH(PP)                                                                                        \
-  dg_tet_faces_kernel<PP><<<count, tt_threads(PP), 0, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, xyz,    \
-                                                            k_el,                                             \
-                                                            D_el, pen, g, boff_diag, roff, val, rhs)
+  if (dword)                                                                                                    \
+    dg_tet_faces_kernel<PP, true><<<count, tt_threads(PP), 0, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes,  \
+                                                                    xyz, k_el, D_el, pen, g, boff_diag, roff,  \
+                                                                    val, rhs);                                 \
+  else                                                                                                          \
+    dg_tet_faces_kernel<PP, false><<<count, tt_threads(PP), 0, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, \
+                                                                     xyz, k_el, D_el, pen, g, boff_diag, roff, \
+                                                                     val, rhs)
   switch (p) {
     case 1: GB_TT_LAUNCH(1); break;
     case 2: GB_TT_LAUNCH(2); break;

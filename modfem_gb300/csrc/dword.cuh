@@ -264,4 +264,43 @@ DW_HD double dwacc_value(DwAcc a) {
   dwacc_fold(a);
   return dw_to_double(dw(a.h, a.l));
 }
+#if defined(__CUDACC__)
+// Entries k = k0 + m THR (m < PER, k < kend) of an NS-row block: row
+// i = k % NS, table column j = k / NS + col_lo; sum over the points of
+// L_i Phi_j + M_i Gam_j into a[m].  The PER chains run interleaved (each
+// TwoSum waits on its predecessor in the same chain); with THR a multiple of
+// NS every entry of a thread has the same row and the L, M loads are shared.
+template <int NS, int THR, int PER>
+__device__ __forceinline__ void dwacc_face_block(DwAcc (&a)[PER], const float2 *sL, const float2 *sM,
+                                                 const float2 *sPhi, const float2 *sGam, int nq, int ncol, int k0,
+                                                 int kend, int col_lo) {
+  int ii[PER], jj[PER];
+  bool ok[PER];
+#pragma unroll
+  for (int m = 0; m < PER; m++) {
+    const int k = k0 + m * THR;
+    ok[m] = k < kend;
+    ii[m] = ok[m] ? k % NS : 0;
+    jj[m] = ok[m] ? k / NS + col_lo : 0;
+  }
+  for (int q = 0; q < nq; q++) {
+    const float2 *Lq = sL + q * NS, *Mq = sM + q * NS, *Pq = sPhi + q * ncol, *Gq = sGam + q * ncol;
+    float2 L0 = Lq[ii[0]], M0 = Mq[ii[0]];
+#pragma unroll
+    for (int m = 0; m < PER; m++) {
+      if (!ok[m]) continue;
+      const float2 L = (THR % NS == 0) ? L0 : Lq[ii[m]], M = (THR % NS == 0) ? M0 : Mq[ii[m]];
+      dwacc_prod(a[m], L, Pq[jj[m]]);
+      dwacc_prod(a[m], M, Gq[jj[m]]);
+    }
+    if ((q & 3) == 3) {
+#pragma unroll
+      for (int m = 0; m < PER; m++) dwacc_fold(a[m]);
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < PER; m++) dwacc_fold(a[m]);
+}
+#endif
+
 }  // namespace gbfem

@@ -138,7 +138,7 @@ int launch_dg_tet_elements(cudaStream_t st, int device, int p, int count, const 
 int launch_dg_tet_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                         const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                         const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
-                        const int *roff, double *val, double *rhs);
+                        const int *roff, double *val, double *rhs, bool dword = false);
 bool dg_tc_faces_supported(int p);
 int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                        const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,

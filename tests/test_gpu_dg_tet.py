@@ -55,6 +55,32 @@ def test_tet_system_vs_oracle(gb):
     assert vec_rel_err(rhs, np.concatenate(R)) < REL_TOL
 
 
+def test_tet_double_word_faces(gb):
+    """Tetrahedral faces summed in double-word arithmetic: against the oracle
+    to the FP64 tolerance and within 1e-13 of the FP64 face kernel (p 1..4,
+    anisotropic tensors)."""
+    c, t, F, p, A = _system(gb, 3, 9)
+    off, bptr, bcol, boff = c.dg_get_structure()
+    v64, r64 = c.dg_get_matrix()
+    c.dg_set_face_kernel(gb.DG_FACE_DWORD)
+    c.dg_assemble()
+    vdw, rdw = c.dg_get_matrix()
+    rp, ci, a64 = dg_blocks_to_crs(off, bptr, bcol, boff, v64)
+    _, _, adw = dg_blocks_to_crs(off, bptr, bcol, boff, vdw)
+    err = sparse_rel_err(rp, ci, adw, a64)
+    print(f"tetrahedral double-word faces vs FP64 faces {err:.2e}")
+    assert err < 1e-13
+    assert vec_rel_err(rdw, r64) < 1e-13
+    B, R = O.dg_tet_assemble(t, F, p, A, pen=10.0, g=0.3, f=1.2)
+    nd = off[-1]
+    dense = np.zeros((nd, nd))
+    for (i, j), K in B.items():
+        dense[off[i]:off[i + 1], off[j]:off[j + 1]] = K
+    ref = dense[np.repeat(np.arange(nd), np.diff(rp)), ci]
+    assert sparse_rel_err(rp, ci, adw, ref) < REL_TOL
+    assert vec_rel_err(rdw, np.concatenate(R)) < REL_TOL
+
+
 @pytest.mark.parametrize("n,aniso", [(4, True), (8, False)])
 def test_tet_constant_reproduction(gb, n, aniso):
     c, t, F, p, A = _system(gb, n, 7, aniso=aniso, g=0.7, f=0.0)
