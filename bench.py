@@ -375,6 +375,14 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
         x, it, res, rel = c.dg_solve(krylov=50, max_iter=gmres_iters, tol_rel=1e-10)
         st = c.last_solve_timing()
         spmv_ms = st[1] / max(st[2], 1)
+        # the same iterations with the Arnoldi products on double-word copies
+        c.set_option(gb.OPT_DG_SPMV_ARITH, gb.STD_DWORD)
+        xdw, it_dw, _, rel_dw = c.dg_solve(krylov=50, max_iter=gmres_iters, tol_rel=1e-10)
+        st_dw = c.last_solve_timing()
+        c.set_option(gb.OPT_DG_SPMV_ARITH, gb.STD_FP64)
+        dw_solve = {"gmres_iterations": it_dw, "gmres_ms_per_iteration": st_dw[0] / max(it_dw, 1),
+                    "spmv_ms": st_dw[1] / max(st_dw[2], 1), "rel_residual": rel_dw,
+                    "solution_rel_diff_vs_fp64": float(np.max(np.abs(xdw - x)) / np.max(np.abs(x)))}
         inv_bytes = 8 * sum(int(np.sum(pdeg == p)) * [0, 6, 18, 40, 75][p] ** 2 for p in range(1, 5))
         out[name] = {
             "elements": m.nel, "faces": int(F.n), "dofs": nd, "stored_values": nv,
@@ -403,6 +411,7 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
                             "note": "tcgen05 kind::tf32, hi/lo operands, FP32 accumulation (p <= 3)"},
             "gmres_iterations": it, "gmres_rel_residual": rel, "gmres_ms_per_iteration": st[0] / max(it, 1),
             "spmv_ms": spmv_ms,
+            "gmres_double_word_operator": dw_solve,
             "ir_fp32_inner": {"inner_iterations": it_ir, "refinement_steps": outer_ir,
                               "ms_per_inner_iteration": ir_ms / max(it_ir, 1), "true_rel_residual": rel_ir},
             # the preconditioned block SpMV: matrix + inverted diagonal blocks, one FMA per value

@@ -63,9 +63,15 @@ long long gbfem_device_bytes(gbfem_ctx ctx);
  * (default) or GBFEM_STD_DWORD: double-word float pairs on the FP32 pipe
  * (about 48 significant bits; entries within about 1e-14 of the FP64 ones,
  * vertex differences and the global assembly sums stay FP64).  Tensor
- * coefficients and tetrahedra always take FP64. */
+ * coefficients and tetrahedra always take FP64.
+ * GBFEM_OPT_DG_SPMV_ARITH: arithmetic of the preconditioned block SpMV in
+ * the Arnoldi steps of gbfem_dg_solve, GBFEM_STD_FP64 (default) or
+ * GBFEM_STD_DWORD: double-word copies of the matrix and of the inverted
+ * diagonal blocks, products summed on the FP32 pipes (the FP64 form is bound
+ * by the FP64 pipe below HBM bandwidth); the restart residuals stay FP64. */
 #define GBFEM_OPT_CACHE_TABLES 1
 #define GBFEM_OPT_STD_ARITH 2
+#define GBFEM_OPT_DG_SPMV_ARITH 3
 #define GBFEM_STD_FP64 0
 #define GBFEM_STD_DWORD 1
 int gbfem_set_option(gbfem_ctx ctx, int option, long long value);

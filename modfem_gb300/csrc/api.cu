@@ -156,6 +156,11 @@ int gbfem_set_option(gbfem_ctx c, int option, long long value) {
     }
     return 0;
   }
+  if (option == GBFEM_OPT_DG_SPMV_ARITH) {
+    GB_CHECK(value == GBFEM_STD_FP64 || value == GBFEM_STD_DWORD, "DG SpMV arithmetic must be FP64 or DWORD");
+    c->dg_spmv_dword = value == GBFEM_STD_DWORD;
+    return 0;
+  }
   if (option == GBFEM_OPT_STD_ARITH) {
     GB_CHECK(value == GBFEM_STD_FP64 || value == GBFEM_STD_DWORD, "std arithmetic must be FP64 or DWORD");
     c->std_dword = value == GBFEM_STD_DWORD;
@@ -1358,7 +1363,29 @@ int gbfem_dg_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int in
   GB_CUDA(cudaStreamSynchronize(st));
   GB_CHECK(herr == 0, "singular diagonal block in the DG block Jacobi preconditioner");
   c->last_solve_kernels = 1;
+  if (c->dg_spmv_dword) {
+    // double-word copies of the matrix and of the inverted diagonal blocks
+    // for the Arnoldi products; the restart residuals stay FP64
+    GB_TRY(c->dg_valdw.alloc((size_t)c->dg_nval));
+    GB_TRY(c->dg_dinvdw.alloc((size_t)c->dg_ninv));
+    GB_TRY(gbfem::launch_to_dw(st, c->dg_nval, c->dg_val.p, c->dg_valdw.p));
+    GB_TRY(gbfem::launch_to_dw(st, c->dg_ninv, c->dg_dinv.p, c->dg_dinvdw.p));
+    c->last_solve_kernels += 2;
+  }
   GmresOp op = [&](int mode, const double *in, double *out) -> int {
+    if (mode == 1 && c->dg_spmv_dword) {
+      int nl = 0;
+      for (int p = 1; p <= 4; p++) {
+        if (!c->dg_list[p].p) continue;
+        const int r = gbfem::launch_dg_block_spmv_dw(c->stream, mode, p + dg_class_off(c), (int)c->dg_list[p].n,
+                                                     c->dg_list[p].p, c->dg_roff_d.p, c->dg_row_val_d.p,
+                                                     c->dg_cx_off_d.p, c->dg_colx_d.p, c->dg_valdw.p,
+                                                     c->dg_dinv_off_d.p, c->dg_dinvdw.p, in, nullptr, out);
+        if (r < 0) return r;
+        nl += r;
+      }
+      return nl;
+    }
     return dg_spmv(c, mode, in, mode == 0 ? c->dg_rhs.p : nullptr, out);
   };
   return gmres_run(c, n, krylov, max_iter, tol_rel, ini_zero, x, res_out, res_rel_out, op);

@@ -128,6 +128,18 @@ __global__ void to_float_kernel(long long n, const double *__restrict__ a, float
     b[i] = (float)a[i];
 }
 
+__global__ void to_dw_kernel(long long n, const double *__restrict__ a, dw *__restrict__ b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = dw_from_double(a[i]);
+}
+
+int launch_to_dw(cudaStream_t st, long long n, const double *a, void *b) {
+  if (n <= 0) return 0;
+  to_dw_kernel<<<152 * 8, 256, 0, st>>>(n, a, reinterpret_cast<dw *>(b));
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
 int launch_to_float(cudaStream_t st, long long n, const double *a, float *b) {
   if (n <= 0) return 0;
   to_float_kernel<<<152 * 8, 256, 0, st>>>(n, a, b);
@@ -177,6 +189,15 @@ int launch_dg_block_spmv32(cudaStream_t st, int mode, int p, int count, const in
                            double *out) {
   return launch_dg_block_spmv_t<float>(st, mode, p, count, ent_el, roff, row_val, cx_off, colx, val, dinv_off,
                                        dinv, x, b, out);
+}
+
+int launch_dg_block_spmv_dw(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
+                           const long long *row_val, const long long *cx_off, const int *colx, const void *val,
+                           const long long *dinv_off, const void *dinv, const double *x, const double *b,
+                           double *out) {
+  return launch_dg_block_spmv_t<dw>(st, mode, p, count, ent_el, roff, row_val, cx_off, colx,
+                                    reinterpret_cast<const dw *>(val), dinv_off, reinterpret_cast<const dw *>(dinv),
+                                    x, b, out);
 }
 
 }  // namespace gbfem

@@ -2,6 +2,8 @@
 // plain kernels and the serving engine's slot kernels).
 #pragma once
 
+#include "dword.cuh"
+
 namespace gbfem {
 
 // One 8-lane group per block row (32 block rows per CTA), launched per
@@ -19,13 +21,29 @@ namespace gbfem {
 // four groups of a warp in step when their neighbours differ in degree; the
 // rows of a class are ordered by nct for the same reason.  With a
 // preconditioner the group's rows go through shared memory into the product
-// with the inverted diagonal block.
+// with the inverted diagonal block.  The arithmetic type VT is double, float
+// (inner solves of iterative refinement) or dw (double words on the FP32
+// pipes: the FP64 pipe bounds the double form at ~5 TB/s of values, below
+// HBM; the double-word form is bound by HBM).
 constexpr int DGS_LANES = 8;
 constexpr int DGS_THREADS = 256;
 constexpr int DGS_ROWS = DGS_THREADS / DGS_LANES;
 
 __device__ __forceinline__ double dgs_fma(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float dgs_fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ dw dgs_fma(dw a, dw b, dw c) { return t_fma(a, b, c); }
+// vector entries into the arithmetic type and results back to FP64
+template <typename VT>
+__device__ __forceinline__ VT dgs_in(double v) {
+  return (VT)v;
+}
+template <>
+__device__ __forceinline__ dw dgs_in<dw>(double v) {
+  return dw_from_double(v);
+}
+__device__ __forceinline__ double dgs_out(double v) { return v; }
+__device__ __forceinline__ double dgs_out(float v) { return (double)v; }
+__device__ __forceinline__ double dgs_out(dw v) { return dw_to_double(v); }
 
 // P: block class, 1..4 tensor-basis prisms of degree P (6, 18, 40, 75
 // functions), 5..8 complete-basis tetrahedra of degree P - 4 (4, 10, 20, 35)
@@ -62,14 +80,14 @@ __device__ __forceinline__ void dg_block_row_spmv(
     const int nct = (int)(cx_off[e + 1] - cx_off[e]);
     int t = 0;
     for (; t + 2 <= nct; t += 2) {
-      const VT x0 = (VT)x[cx[t]], x1 = (VT)x[cx[t + 1]];
+      const VT x0 = dgs_in<VT>(x[cx[t]]), x1 = dgs_in<VT>(x[cx[t + 1]]);
       const VT *col0 = A + (size_t)t * NS, *col1 = col0 + NS;
 #pragma unroll
       for (int s = 0; s < S; s++)
         if (g + DGS_LANES * s < NS) acc[s] = dgs_fma(col1[DGS_LANES * s], x1, dgs_fma(col0[DGS_LANES * s], x0, acc[s]));
     }
     if (t < nct) {
-      const VT x0 = (VT)x[cx[t]];
+      const VT x0 = dgs_in<VT>(x[cx[t]]);
       const VT *col0 = A + (size_t)t * NS;
 #pragma unroll
       for (int s = 0; s < S; s++)
@@ -80,7 +98,7 @@ __device__ __forceinline__ void dg_block_row_spmv(
 #pragma unroll
     for (int s = 0; s < S; s++) {
       const int i = g + DGS_LANES * s;
-      acc[s] = (b && active && i < NS ? (VT)b[r0 + i] : VT(0)) - acc[s];
+      acc[s] = (b && active && i < NS ? dgs_in<VT>(b[r0 + i]) : VT(0)) - acc[s];
     }
   }
   if (mode == 2) {
@@ -88,7 +106,7 @@ __device__ __forceinline__ void dg_block_row_spmv(
 #pragma unroll
       for (int s = 0; s < S; s++) {
         const int i = g + DGS_LANES * s;
-        if (i < NS) out[r0 + i] = (double)acc[s];
+        if (i < NS) out[r0 + i] = dgs_out(acc[s]);
       }
     }
     return;
@@ -114,7 +132,7 @@ __device__ __forceinline__ void dg_block_row_spmv(
 #pragma unroll
   for (int s = 0; s < S; s++) {
     const int i = g + DGS_LANES * s;
-    if (i < NS) out[r0 + i] = (double)o[s];
+    if (i < NS) out[r0 + i] = dgs_out(o[s]);
   }
 }
 

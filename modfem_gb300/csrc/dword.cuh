@@ -108,7 +108,7 @@ DW_HD double d_from_bits(unsigned long long u) {
 #define DW_CX constexpr
 #endif
 
-struct dw {
+struct alignas(8) dw {
   float h, l;
   dw() = default;
   // constants: split at compile time (literal arguments fold)

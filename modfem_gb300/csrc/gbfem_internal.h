@@ -167,6 +167,13 @@ int launch_dg_block_spmv32(cudaStream_t st, int mode, int p, int count, const in
                            const long long *dinv_off, const float *dinv, const double *x, const double *b,
                            double *out);
 int launch_to_float(cudaStream_t st, long long n, const double *a, float *b);
+// double -> double word (h, l float pairs, 8 bytes each) and the block SpMV
+// on double-word copies of the matrix and of the inverted diagonal blocks
+int launch_to_dw(cudaStream_t st, long long n, const double *a, void *b);
+int launch_dg_block_spmv_dw(cudaStream_t st, int mode, int p, int count, const int *ent_el, const int *roff,
+                           const long long *row_val, const long long *cx_off, const int *colx, const void *val,
+                           const long long *dinv_off, const void *dinv, const double *x, const double *b,
+                           double *out);
 // Tensor-core (tcgen05, split BF16) DG volume integrals, FP64-equivalent.
 bool dg_tc_supported(int p);
 int launch_dg_tc_volume(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
@@ -245,6 +252,8 @@ struct gbfem_ctx_s {
   // DG block Jacobi: inverted diagonal blocks, block e at dg_dinv_off_d[e]
   gbfem::DevBuf<double> dg_dinv;
   gbfem::DevBuf<float> dg_val32, dg_dinv32;  // FP32 copies for iterative refinement
+  gbfem::DevBuf<float2> dg_valdw, dg_dinvdw;  // double-word copies for the GMRES operator
+  bool dg_spmv_dword = false;
   gbfem::DevBuf<double> ir_x, ir_r;
   gbfem::DevBuf<long long> dg_dinv_off_d;
   gbfem::DevBuf<int> dg_bptr_d, dg_bcol_d, dg_colx_d;

@@ -79,6 +79,30 @@ def test_dg_gmres_vs_reference(gb, name):
     assert vec_rel_err(x, g["gmres_x"]) < 1e-7
 
 
+@pytest.mark.parametrize("name", ["dg_asm_p2", "dg_asm_mixed", "dg_asm_aniso"])
+def test_dg_gmres_double_word_operator_vs_reference(gb, name):
+    """GMRES with the Arnoldi products on double-word copies of the matrix
+    and the block-Jacobi inverse: the reference's iteration count within 2 and
+    its solution to the same accuracy as the FP64 operator."""
+    g, m, F = _fixture_problem(name)
+    D = _tensors(g)
+    c = _context(gb, m, F, g["pdeg"], k=None if D is not None else g["k"], D=D, pen=float(g["pen"]),
+                 g=float(g["g"]), f=float(g["f"]))
+    c.dg_assemble()
+    c.set_option(gb.OPT_DG_SPMV_ARITH, gb.STD_DWORD)
+    x, it, res, rel = c.dg_solve(krylov=int(g["krylov"]), max_iter=5000, tol_rel=float(g["tol"]))
+    assert abs(it - int(g["gmres_iters"])) <= 2, (it, int(g["gmres_iters"]))
+    assert rel < float(g["tol"])
+    assert vec_rel_err(x, g["gmres_x"]) < 1e-7
+    # the FP64 operator on the same problem: iteration counts within one,
+    # solutions as close as the stopping test allows (different rounding,
+    # different iterates: about cond x tol)
+    c.set_option(gb.OPT_DG_SPMV_ARITH, gb.STD_FP64)
+    x64, it64, _, _ = c.dg_solve(krylov=int(g["krylov"]), max_iter=5000, tol_rel=float(g["tol"]))
+    assert abs(it - it64) <= 1
+    assert vec_rel_err(x, x64) < 1e-7
+
+
 def test_dg_residual_vs_numpy(gb):
     g, m, F = _fixture_problem("dg_asm_mixed")
     c = _context(gb, m, F, g["pdeg"], k=g["k"], pen=float(g["pen"]), g=float(g["g"]))
