@@ -417,11 +417,12 @@ static int build_pipe_plan(gbfem_ctx c, int e0, int e1) {
   GB_CUDA(cudaMemcpyAsync(last.data(), c->row_last.p, (size_t)nd * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
   for (int r = 1; r < nd; r++) last[r] = std::max(last[r], last[r - 1]);  // prefix maximum
-  // chunks of whole waves of resident element threads (five 128-thread
-  // blocks per SM for both element kernels), at most eight
+  // chunks of whole waves of resident element threads (128-thread blocks,
+  // five per SM for the FP64 kernel, three for the double-word one), at
+  // most eight
   int nsm = 152;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
-  const long long wave = (long long)nsm * 5 * 128;
+  const long long wave = (long long)nsm * (c->std_dword ? 3 : 5) * 128;
   const long long chunk = std::max(wave, (count / 8 + wave) / wave * wave);
   const int K = (int)((count + chunk - 1) / chunk);
   c->pipe_el.assign(K + 1, 0);
@@ -439,6 +440,7 @@ static int build_pipe_plan(gbfem_ctx c, int e0, int e1) {
   }
   c->pipe_e0 = e0;
   c->pipe_e1 = e1;
+  c->pipe_dword = c->std_dword;
   return 0;
 }
 
@@ -522,7 +524,7 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   // finished rows downloaded while the next chunk runs
   bool pipe = c->cache_tables && (crs_val || rhs) && e1 > e0;
   if (pipe) {
-    bool same = c->pipe_e0 == e0 && c->pipe_e1 == e1;
+    bool same = c->pipe_e0 == e0 && c->pipe_e1 == e1 && c->pipe_dword == c->std_dword;
     for (int i = 0; i < 3; i++) same = same && c->pipe_key[i] == c->cache_key[i] && c->pipe_len[i] == c->cache_len[i];
     if (!same) GB_TRY(build_pipe_plan(c, e0, e1));
   }

@@ -227,6 +227,7 @@ struct gbfem_ctx_s {
   const void *pipe_key[3] = {nullptr, nullptr, nullptr};
   long long pipe_len[3] = {0, 0, 0};
   int pipe_e0 = -1, pipe_e1 = -1;
+  bool pipe_dword = false;
   std::vector<int> pipe_el, pipe_rows;
   // Krylov workspace
   gbfem::DevBuf<double> V, w, tmp, x, b, partial, hcol;

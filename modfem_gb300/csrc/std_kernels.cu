@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(128) prism_elements_kernel(
 constexpr int kDwThreads = 128;
 __constant__ DwPairCodes kDwPairs = dw_pair_codes();
 template <bool ATOMIC>
-__global__ void __launch_bounds__(kDwThreads, 5) prism_elements_dw_kernel(
+__global__ void __launch_bounds__(kDwThreads, 3) prism_elements_dw_kernel(
     int count, const int *__restrict__ ent_el, int el_base, const int *__restrict__ ent_pos, int nel,
     const int *__restrict__ el_nodes, const double *__restrict__ xyz, const double *__restrict__ k_el, double f,
     const int *__restrict__ tab, double *__restrict__ val, double *__restrict__ rhs, int do_sm, int do_rhs,
