@@ -956,12 +956,19 @@ int gbfem_dg_assemble(gbfem_ctx c) {
         launches += r;
         continue;
       }
-      int r = gbfem::launch_dg_prism_faces(c->stream, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->dg_hf_ptr.p,
-                                           c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
-                                           c->dg_pen, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,
-                                           c->dg_rhs.p, c->dg_var_face[p], c->dg_face_mode == GBFEM_DG_FACE_DWORD);
-      GB_TRY(r);
-      launches += r;
+      // owners whose neighbourhood has degrees <= 3 on the compact tables
+      // (more CTAs per SM), the others on the full ones; same results
+      const bool dwf = c->dg_face_mode == GBFEM_DG_FACE_DWORD;
+      for (int low = 1; low >= 0; low--) {
+        const gbfem::DevBuf<int> &lst = low ? c->dg_flist_tc[p] : c->dg_flist_64[p];
+        if (!lst.p) continue;
+        const int r = gbfem::launch_dg_prism_faces(c->stream, p, (int)lst.n, lst.p, c->dg_hf_ptr.p, c->dg_hf.p,
+                                                   c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
+                                                   c->dg_pen, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p,
+                                                   c->dg_val.p, c->dg_rhs.p, c->dg_var_face[p], dwf, low != 0);
+        GB_TRY(r);
+        launches += r;
+      }
     }
   }
   cudaEventRecord(c->ev1, c->stream);

@@ -42,11 +42,17 @@ __host__ __device__ constexpr int dg_face_threads(int p, int v) {
                                                                               : (v == 0 ? 256 : 384);
 }
 
-template <int P, int THR>
+// LOW: the owner and all its neighbours have degree <= 3, so a face has at
+// most 16 points and a neighbour at most 40 functions: the point tables
+// shrink to 16 rows and NS + 40 columns (p = 3: 51 KB of shared memory
+// instead of 92, four CTAs per SM instead of two).  Same operations in the
+// same order: bit-identical results.
+template <int P, int THR, bool LOW = false>
 struct DgFaceDims {
   static constexpr int NS = P == 1 ? 6 : P == 2 ? 18 : P == 3 ? 40 : 75;
   static constexpr int THREADS = THR;
-  static constexpr int NCOL = NS + GB_DG_MAXNS;  // own + neighbour columns
+  static constexpr int NQ = LOW ? 16 : DGF_NQ;             // points of the largest face rule met
+  static constexpr int NCOL = NS + (LOW ? 40 : GB_DG_MAXNS);  // own + neighbour columns
   static constexpr int PER = (NS * NS + THREADS - 1) / THREADS;
   // degree <= 3: the coordinates, tensors, point geometry and penalty of all
   // (up to 5) faces are prepared at once before the face loop (the long FP64
@@ -55,7 +61,7 @@ struct DgFaceDims {
   static constexpr bool ALLF = P <= 3;
   static constexpr int NFG = ALLF ? 5 : 1;
   static constexpr int SMEM_DOUBLES =
-      2 * DGF_NQ * NS + 2 * DGF_NQ * NCOL + NFG * (36 + 18 + DGF_NQ * DGF_GEO + 1) + 2 * DGF_NQ * DGF_FAC;
+      2 * NQ * NS + 2 * NQ * NCOL + NFG * (36 + 18 + NQ * DGF_GEO + 1) + 2 * NQ * DGF_FAC;
 };
 
 // Double-word form (DW = true): the point tables hold float pairs
@@ -67,27 +73,27 @@ struct DgFaceDims {
 // kernel's 2 nq FP64 FMAs per entry at 1/64 of the FP32 issue rate
 // (accumulator: DwAcc, dword.cuh).
 
-template <int P, int THR, bool DW>
+template <int P, int THR, bool DW, bool LOW>
 __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
     const double *__restrict__ k_el, const double *__restrict__ D_el, double pen, double gval,
     const long long *__restrict__ boff_diag, const int *__restrict__ roff, double *__restrict__ val,
     double *__restrict__ rhs) {
-  using Dm = DgFaceDims<P, THR>;
-  constexpr int NS = Dm::NS, NCOL = Dm::NCOL, DGF_THREADS = Dm::THREADS;
-  static_assert(DGF_THREADS >= 54 && DGF_THREADS - 1 >= DGF_NQ, "loader and penalty threads");
+  using Dm = DgFaceDims<P, THR, LOW>;
+  constexpr int NS = Dm::NS, NCOL = Dm::NCOL, DGF_THREADS = Dm::THREADS, NQ = Dm::NQ;
+  static_assert(DGF_THREADS >= 54 && DGF_THREADS - 1 >= NQ, "loader and penalty threads");
   extern __shared__ double smem[];
-  double *sL = smem;                       // [DGF_NQ][NS]   owner rows
-  double *sM = sL + DGF_NQ * NS;           // [DGF_NQ][NS]
-  double *sPhi = sM + DGF_NQ * NS;         // [DGF_NQ][NCOL] columns, side 1 then side 2
-  double *sGam = sPhi + DGF_NQ * NCOL;     // [DGF_NQ][NCOL]
+  double *sL = smem;                       // [NQ][NS]   owner rows
+  double *sM = sL + NQ * NS;               // [NQ][NS]
+  double *sPhi = sM + NQ * NS;             // [NQ][NCOL] columns, side 1 then side 2
+  double *sGam = sPhi + NQ * NCOL;         // [NQ][NCOL]
   constexpr int NFG = Dm::NFG;
-  double *sX0 = sGam + DGF_NQ * NCOL;              // [NFG][2][18] vertex coordinates of both sides
-  double *sA0 = sX0 + NFG * 36;                    // [NFG][2][9] coefficient tensors
-  double *sGeo0 = sA0 + NFG * 18;                  // [NFG][DGF_NQ][DGF_GEO]
-  double *sFac = sGeo0 + NFG * DGF_NQ * DGF_GEO;   // [DGF_NQ][2][DGF_FAC]
-  double *sPen0 = sFac + 2 * DGF_NQ * DGF_FAC;     // [NFG] penalty / sqrt(face area)
+  double *sX0 = sGam + NQ * NCOL;              // [NFG][2][18] vertex coordinates of both sides
+  double *sA0 = sX0 + NFG * 36;                // [NFG][2][9] coefficient tensors
+  double *sGeo0 = sA0 + NFG * 18;              // [NFG][NQ][DGF_GEO]
+  double *sFac = sGeo0 + NFG * NQ * DGF_GEO;   // [NQ][2][DGF_FAC]
+  double *sPen0 = sFac + 2 * NQ * DGF_FAC;     // [NFG] penalty / sqrt(face area)
   const int bi = blockIdx.x;
   if (bi >= count) return;
   const int e = ent_el[bi];
@@ -158,12 +164,12 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
       load_face(hf[h0 + f], t % 54, sX0 + 36 * f, sA0 + 18 * f);
     }
     __syncthreads();
-    for (int t = tid; t < nf * DGF_NQ; t += DGF_THREADS) {
-      const int f = t / DGF_NQ, q = t % DGF_NQ;
+    for (int t = tid; t < nf * NQ; t += DGF_THREADS) {
+      const int f = t / NQ, q = t % NQ;
       const DgHalfFace F = hf[h0 + f];
       int pr, ti;
       face_rule(F, pr, ti);
-      if (q < d_dg_nqf[pr][ti]) face_geometry(F, q, sX0 + 36 * f, sA0 + 18 * f, sGeo0 + (f * DGF_NQ + q) * DGF_GEO);
+      if (q < d_dg_nqf[pr][ti]) face_geometry(F, q, sX0 + 36 * f, sA0 + 18 * f, sGeo0 + (f * NQ + q) * DGF_GEO);
     }
     for (int f = tid; f < nf; f += DGF_THREADS) sPen0[f] = face_penalty(hf[h0 + f], sX0 + 36 * f);
   }
@@ -177,7 +183,7 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
     face_rule(F, pr, ti);
     const int nq = d_dg_nqf[pr][ti];
     const int fo = allf ? h - h0 : 0;
-    double *sX = sX0 + 36 * fo, *sA = sA0 + 18 * fo, *sGeo = sGeo0 + fo * DGF_NQ * DGF_GEO, *sPen = sPen0 + fo;
+    double *sX = sX0 + 36 * fo, *sA = sA0 + 18 * fo, *sGeo = sGeo0 + fo * NQ * DGF_GEO, *sPen = sPen0 + fo;
     __syncthreads();  // shared arrays of the previous face are free (and the prepared faces written)
     if (!allf) {  // this face only
       if (tid < 54) load_face(F, tid, sX, sA);
@@ -303,34 +309,40 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
 int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                           const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                           const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
-                          const int *roff, double *val, double *rhs, int variant, bool dword) {
+                          const int *roff, double *val, double *rhs, int variant, bool dword, bool low) {
   if (count <= 0) return 0;
   GB_CHECK(p >= 1 && p <= GB_DG_PMAX, "DG degree must be 1..4");
   GB_CHECK(variant >= 0 && variant < DG_FACE_VARIANTS, "face kernel variant out of range");
-#define GB_DGF_LAUNCH(PP, VV, WW)                                                                               \
+#define GB_DGF_LAUNCH(PP, VV, WW, LL)                                                                          \
   {                                                                                                             \
     constexpr int T_ = dg_face_threads(PP, VV);                                                                 \
-    const size_t smem = sizeof(double) * DgFaceDims<PP, T_>::SMEM_DOUBLES;                                      \
-    GB_CUDA(cudaFuncSetAttribute(dg_prism_faces_kernel<PP, T_, WW>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                 (int)smem));                                                                   \
-    dg_prism_faces_kernel<PP, T_, WW><<<count, T_, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, xyz,  \
-                                                               k_el, D_el, pen, g, boff_diag, roff, val, rhs);  \
+    const size_t smem = sizeof(double) * DgFaceDims<PP, T_, LL>::SMEM_DOUBLES;                                  \
+    GB_CUDA(cudaFuncSetAttribute(dg_prism_faces_kernel<PP, T_, WW, LL>,                                        \
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                      \
+    dg_prism_faces_kernel<PP, T_, WW, LL><<<count, T_, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes,   \
+                                                                   xyz, k_el, D_el, pen, g, boff_diag, roff,    \
+                                                                   val, rhs);                                   \
   }
-#define GB_DGF_P(PP)                                \
-  if (dword) {                                      \
-    if (variant == 0) GB_DGF_LAUNCH(PP, 0, true)    \
-    else GB_DGF_LAUNCH(PP, 1, true)                 \
-  } else {                                          \
-    if (variant == 0) GB_DGF_LAUNCH(PP, 0, false)   \
-    else GB_DGF_LAUNCH(PP, 1, false)                \
+#define GB_DGF_W(PP, LL)                                 \
+  if (dword) {                                           \
+    if (variant == 0) GB_DGF_LAUNCH(PP, 0, true, LL)     \
+    else GB_DGF_LAUNCH(PP, 1, true, LL)                  \
+  } else {                                               \
+    if (variant == 0) GB_DGF_LAUNCH(PP, 0, false, LL)    \
+    else GB_DGF_LAUNCH(PP, 1, false, LL)                 \
   }
+#define GB_DGF_P(PP)        \
+  if (low) GB_DGF_W(PP, true) \
+  else GB_DGF_W(PP, false)
+  GB_CHECK(!low || p <= 3, "the compact face tables need degrees <= 3");
   switch (p) {
     case 1: GB_DGF_P(1); break;
     case 2: GB_DGF_P(2); break;
     case 3: GB_DGF_P(3); break;
-    default: GB_DGF_P(4); break;
+    default: GB_DGF_W(4, false); break;
   }
 #undef GB_DGF_P
+#undef GB_DGF_W
 #undef GB_DGF_LAUNCH
   GB_CUDA(cudaGetLastError());
   return 1;

@@ -147,7 +147,7 @@ int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, con
 int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                           const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                           const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
-                          const int *roff, double *val, double *rhs, int variant, bool dword = false);
+                          const int *roff, double *val, double *rhs, int variant, bool dword = false, bool low = false);
 // Variable-block CRS (one block row per DG element, dense column-major
 // blocks with the row block's size as leading dimension) and block Jacobi.
 int launch_dg_block_inverse(cudaStream_t st, int nel, const int *roff, const long long *boff_diag,
