@@ -89,6 +89,12 @@ int gbfem_destroy(gbfem_ctx c) {
       if (ev) cudaEventDestroy(ev);
   }
   c->row_last.release();
+  if (c->side_stream) {
+    cudaStreamSynchronize(c->side_stream);
+    cudaStreamDestroy(c->side_stream);
+    for (auto &ev : c->side_ev)
+      if (ev) cudaEventDestroy(ev);
+  }
   DevBuf<double> *dbufs[] = {&c->xyz, &c->k_el, &c->D_el, &c->val, &c->rhs, &c->dinv, &c->V,
                              &c->w, &c->tmp, &c->x, &c->b, &c->partial, &c->hcol};
   for (auto *b : dbufs) b->release();
@@ -377,6 +383,31 @@ static int stage_input(gbfem_ctx c, int slot, DevBuf<int> &d, const int *h, long
   return 0;
 }
 
+// The penalty faces with atomic scatter on a second stream, after the work
+// already queued on the context stream (the memsets), beside the element
+// kernel; join_side makes the context stream wait for them.  Atomic sums
+// commute, so the order against the elements does not matter.
+static int launch_faces_beside(gbfem_ctx c, int count, const int *ent_fa, const int *fa_map, int fa_map_len,
+                               const int *ent_pos, const int *tab, int do_sm, int do_rhs, int *launches) {
+  if (!c->side_stream) {
+    GB_CUDA(cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking));
+    for (auto &ev : c->side_ev) GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  GB_CUDA(cudaEventRecord(c->side_ev[0], c->stream));
+  GB_CUDA(cudaStreamWaitEvent(c->side_stream, c->side_ev[0], 0));
+  const int r = gbfem::launch_prism_faces(c->side_stream, true, count, ent_fa, 0, fa_map, fa_map_len,
+                                          ent_pos, c->nfa, c->fa_el.p, c->fa_side.p, c->el_nodes.p, c->xyz.p,
+                                          c->penalty, c->g, tab, c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p);
+  GB_TRY(r);
+  *launches += r;
+  GB_CUDA(cudaEventRecord(c->side_ev[1], c->side_stream));
+  return 0;
+}
+static int join_side(gbfem_ctx c, cudaStream_t st) {
+  GB_CUDA(cudaStreamWaitEvent(st, c->side_ev[1], 0));
+  return 0;
+}
+
 // last element (position within the element range) touching each row: the
 // rows of an element's rhs positions and of its value positions (found in
 // row_ptr); entries outside the structure are left to the element kernels
@@ -500,13 +531,10 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   if (do_sm) GB_CUDA(cudaMemsetAsync(c->val.p, 0, c->val.bytes(), c->stream));
   if (do_rhs) GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, c->rhs.bytes(), c->stream));
   int launches = 0, r;
-  if (f1 > f0) {
-    r = gbfem::launch_prism_faces(c->stream, true, f1 - f0, c->in_id.p + f0, 0, c->fa_map.p, (int)c->fa_map.n,
-                                  c->in_pos.p + f0, c->nfa, c->fa_el.p, c->fa_side.p, c->el_nodes.p, c->xyz.p,
-                                  c->penalty, c->g, c->in_table.p, c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p);
-    GB_TRY(r);
-    launches += r;
-  }
+  const bool side = f1 > f0;  // the faces run beside the element chunks
+  if (side)
+    GB_TRY(launch_faces_beside(c, f1 - f0, c->in_id.p + f0, c->fa_map.p, (int)c->fa_map.n, c->in_pos.p + f0,
+                               c->in_table.p, do_sm, do_rhs, &launches));
   cudaEventRecord(c->ev2, c->stream);
   GB_CHECK(c->nv == GBFEM_PRISM || !c->aniso, "std tetrahedra take an isotropic k_el (tensors: prisms and DG)");
   auto elements = [&](int a, int b) -> int {
@@ -538,6 +566,7 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
       GB_CUDA(cudaEventRecord(c->pipe_ev[k], c->stream));
     }
     cudaEventRecord(c->ev3, c->stream);
+    if (side) GB_TRY(join_side(c, c->copy_stream));  // face rows are final before any download
     int rprev = 0;
     for (int k = 0; k < K; k++) {
       GB_CUDA(cudaStreamWaitEvent(c->copy_stream, c->pipe_ev[k], 0));
@@ -558,6 +587,7 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     GB_TRY(r = elements(e0, e1));
     launches += r;
     cudaEventRecord(c->ev3, c->stream);
+    if (side) GB_TRY(join_side(c, c->stream));
     if (crs_val) GB_CUDA(cudaMemcpyAsync(crs_val, c->val.p, c->val.bytes(), cudaMemcpyDeviceToHost, c->stream));
     if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->rhs.p, c->rhs.bytes(), cudaMemcpyDeviceToHost, c->stream));
   }
@@ -579,14 +609,12 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
   GB_CUDA(cudaMemsetAsync(c->val.p, 0, c->val.bytes(), c->stream));
   GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, c->rhs.bytes(), c->stream));
   int launches = 0, r;
-  // boundary faces first, then elements (utd_util/uts_ls_intf.c:3629-3858, 4103-4290)
+  // boundary faces, then elements (utd_util/uts_ls_intf.c:3629-3858,
+  // 4103-4290); with atomic scatter the faces run beside the elements
+  const bool side = atomic && c->nfa > 0;
   if (c->nfa > 0) {
     if (atomic) {
-      r = gbfem::launch_prism_faces(c->stream, true, c->nfa, nullptr, 0, nullptr, 0, nullptr, c->nfa, c->fa_el.p,
-                                    c->fa_side.p, c->el_nodes.p, c->xyz.p, c->penalty, c->g, c->el_table.p,
-                                    c->val.p, c->rhs.p, 1, 1, c->err.p);
-      GB_TRY(r);
-      launches += r;
+      GB_TRY(launch_faces_beside(c, c->nfa, nullptr, nullptr, 0, nullptr, c->el_table.p, 1, 1, &launches));
     } else {
       // the colour permutation lists face indices: feed them as "ids" through an identity map
       for (size_t k = 0; k + 1 < c->h_fa_color_ptr.size(); k++) {
@@ -627,6 +655,7 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
     }
   }
   cudaEventRecord(c->ev3, c->stream);
+  if (side) GB_TRY(join_side(c, c->stream));
   cudaEventRecord(c->ev1, c->stream);
   GB_TRY(check_err_flag(c));
   cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);

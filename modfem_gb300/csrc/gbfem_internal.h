@@ -228,6 +228,9 @@ struct gbfem_ctx_s {
   long long pipe_len[3] = {0, 0, 0};
   int pipe_e0 = -1, pipe_e1 = -1;
   bool pipe_dword = false;
+  // the boundary-face kernel runs beside the element kernel (atomic scatter)
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t side_ev[2] = {};
   std::vector<int> pipe_el, pipe_rows;
   // Krylov workspace
   gbfem::DevBuf<double> V, w, tmp, x, b, partial, hcol;
