@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help=argparse.SUPPRESS)
-    p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "dg_dwf", "dg_dw", "batch", "std", "std_dw"], default=None,
+    p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "dg_dwf", "dg_dw", "dg_best", "batch", "std", "std_dw"], default=None,
                    help="small cases for ncu captures: DG p=3 anisotropic (n^3 x 2 prisms, --n), 3 assemblies "
                         "(FP64, tensor-core volume, tensor-core volume and faces, FP64 volume and double-word faces, or "
                         "double-word volume and faces) and one "
@@ -103,10 +103,10 @@ def run_profile_case(args):
     c.dg_set_degrees(np.full(m.nel, 3))
     c.dg_set_faces(prism_faces(m), penalty=10.0)
     c.dg_build_structure()
-    c.dg_set_volume_kernel({"dg_tc": gb.DG_VOLUME_TC, "dg_tcf": gb.DG_VOLUME_TC,
-                            "dg_dw": gb.DG_VOLUME_DWORD}.get(args.profile, gb.DG_VOLUME_FP64))
-    c.dg_set_face_kernel({"dg_tcf": gb.DG_FACE_TC, "dg_dwf": gb.DG_FACE_DWORD,
-                          "dg_dw": gb.DG_FACE_DWORD}.get(args.profile, gb.DG_FACE_FP64))
+    c.dg_set_volume_kernel({"dg_tc": gb.DG_VOLUME_TC, "dg_tcf": gb.DG_VOLUME_TC, "dg_dw": gb.DG_VOLUME_DWORD,
+                            "dg_best": gb.DG_VOLUME_DWORD}.get(args.profile, gb.DG_VOLUME_FP64))
+    c.dg_set_face_kernel({"dg_tcf": gb.DG_FACE_TC, "dg_dwf": gb.DG_FACE_DWORD, "dg_dw": gb.DG_FACE_DWORD,
+                          "dg_best": gb.DG_FACE_TC_DWORD}.get(args.profile, gb.DG_FACE_FP64))
     for _ in range(3):
         c.dg_assemble()
     r = c.dg_compute_residual(np.zeros(c.dg_ndof))

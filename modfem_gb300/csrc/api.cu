@@ -387,12 +387,16 @@ static int stage_input(gbfem_ctx c, int slot, DevBuf<int> &d, const int *h, long
 // already queued on the context stream (the memsets), beside the element
 // kernel; join_side makes the context stream wait for them.  Atomic sums
 // commute, so the order against the elements does not matter.
-static int launch_faces_beside(gbfem_ctx c, int count, const int *ent_fa, const int *fa_map, int fa_map_len,
-                               const int *ent_pos, const int *tab, int do_sm, int do_rhs, int *launches) {
+static int ensure_side(gbfem_ctx c) {
   if (!c->side_stream) {
     GB_CUDA(cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking));
     for (auto &ev : c->side_ev) GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   }
+  return 0;
+}
+static int launch_faces_beside(gbfem_ctx c, int count, const int *ent_fa, const int *fa_map, int fa_map_len,
+                               const int *ent_pos, const int *tab, int do_sm, int do_rhs, int *launches) {
+  GB_TRY(ensure_side(c));
   GB_CUDA(cudaEventRecord(c->side_ev[0], c->stream));
   GB_CUDA(cudaStreamWaitEvent(c->side_stream, c->side_ev[0], 0));
   const int r = gbfem::launch_prism_faces(c->side_stream, true, count, ent_fa, 0, fa_map, fa_map_len,
@@ -970,7 +974,9 @@ int gbfem_dg_assemble(gbfem_ctx c) {
         continue;
       }
       if (tcf) {
-        // tensor-core eligible owners, then the rest on the FP64 kernel
+        // tensor-core eligible owners, then the rest on the FP64 (or, in
+        // TC_DWORD mode, the double-word) kernel; running the two side by
+        // side on disjoint owners was slower (167 vs 157 ms at p = 3, 432k)
         int r = gbfem::launch_dg_tc_faces(c->stream, p, (int)c->dg_flist_tc[p].n, c->dg_flist_tc[p].p,
                                           c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p,
                                           c->k_el.p, c->D_el.p, c->dg_pen, c->g, c->dg_boff_diag_d.p,
