@@ -472,11 +472,10 @@ int prepare(gbfem_server s, SrvRequest &r) {
   rc = gbfem_set_coefficients(c, r.k.data(), nullptr, r.f, r.g, 1.0e7);
   if (rc < 0) return rc;
   if (r.kind == 0) {
-    int nd = 0, nc = 0;
+    int nd = 0;
     long long nnz = 0;
     // structure and element colouring on the device (deterministic)
     if ((rc = gbfem_build_structure_device(c, &nd, &nnz)) < 0) return rc;
-    (void)nc;
     // colour-ordered scatter: the same summation order every time, so a
     // request's matrix (and result) does not depend on when it runs
     if ((rc = gbfem_assemble(c, GBFEM_SCATTER_COLOR)) < 0) return rc;
