@@ -208,6 +208,16 @@ def read_profile_traffic():
     return None
 
 
+def hbm_peak_gbs():
+    """Measured copy bandwidth of the GB300s (MEASURED_PEAKS.json),
+    or None when the file is absent."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"])
+    except (OSError, ValueError, KeyError, TypeError):
+        return None
+
+
 def read_profile_values(name):
     """``key = number`` lines of a committed ncu summary under profiles/."""
     out = {}
@@ -418,6 +428,12 @@ def bench_dg(gb, local, steps, fp64_peak, gmres_iters=100):
             "spmv_fp64_frac": 2 * (nv + inv_bytes / 8) / (spmv_ms * 1e-3) / 1e12 / fp64_peak,
             "spmv_gbs": (8 * nv + inv_bytes + 24 * nd) / (spmv_ms * 1e-3) / 1e9,
         }
+        hbm = hbm_peak_gbs()
+        if hbm:
+            b = 8 * nv + inv_bytes + 24 * nd
+            out[name]["spmv_hbm_frac_of_measured"] = b / (max(spmv_ms, 1e-9) * 1e-3) / 1e9 / hbm
+            out[name]["gmres_double_word_operator"]["spmv_hbm_frac_of_measured"] = (
+                b / (max(dw_solve["spmv_ms"], 1e-9) * 1e-3) / 1e9 / hbm)
         c.close()
     return out
 
@@ -856,6 +872,8 @@ def main():
     solver = {"gmres_iterations": it, "gmres_ms_per_iteration": solve_ms / max(it, 1),
               "spmv_ms": spmv_ms / max(nspmv, 1), "spmv_gbs": spmv_bytes * nspmv / (spmv_ms * 1e-3) / 1e9,
               "spmv_bytes": spmv_bytes, "relative_residual_after": rel, "kernel_launches": solve_kernels}
+    if hbm_peak_gbs():
+        solver["spmv_hbm_frac_of_measured"] = solver["spmv_gbs"] / hbm_peak_gbs()
 
     # ---------------- DG prism system ----------------
     dg = bench_dg(gb, local, max(3, min(args.steps, 10)), fp64_peak)
