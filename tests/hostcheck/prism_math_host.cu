@@ -36,3 +36,36 @@ extern "C" void host_dw_roundtrip(const double *x, int n, float *hl, double *bac
     back[i] = gbfem::dw_to_double(d);
   }
 }
+
+// double-word operations on double inputs (converted to float pairs),
+// results widened back: op 0 product, 1 sum, 2 fused a b + c, 3 a b - c d,
+// 4 reciprocal of a, 5 dot3 (a, b, c) . (d, d, d)
+extern "C" void host_dw_ops(int op, int n, const double *a, const double *b, const double *c, const double *d,
+                            double *out) {
+  using namespace gbfem;
+  for (int i = 0; i < n; i++) {
+    const dw x = dw_from_double(a[i]), y = dw_from_double(b[i]), z = dw_from_double(c[i]), w = dw_from_double(d[i]);
+    dw r;
+    switch (op) {
+      case 0: r = x * y; break;
+      case 1: r = x + y; break;
+      case 2: r = t_fma(x, y, z); break;
+      case 3: r = dw_fms(x, y, z, w); break;
+      case 4: r = dw_recip(x); break;
+      default: r = dw_dot3(x, w, y, w, z, w); break;
+    }
+    out[i] = dw_to_double(r);
+  }
+}
+
+// sum_k x_k y_k through the long-sum accumulator, folded every `fold` terms
+extern "C" double host_dwacc_dot(int n, const double *x, const double *y, int fold) {
+  using namespace gbfem;
+  DwAcc a{0.0f, 0.0f, 0.0f};
+  for (int k = 0; k < n; k++) {
+    const float2 u = dw_f2(x[k]), v = dw_f2(y[k]);
+    dwacc_prod(a, u, v);
+    if (fold > 0 && k % fold == fold - 1) dwacc_fold(a);
+  }
+  return dwacc_value(a);
+}

@@ -29,6 +29,9 @@ def hostlib():
     for fn in (L.host_prism_std_element, L.host_prism_std_element_dw):
         fn.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
     L.host_dw_roundtrip.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.host_dw_ops.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
+    L.host_dwacc_dot.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    L.host_dwacc_dot.restype = ctypes.c_double
     return L
 
 
@@ -196,3 +199,64 @@ def test_dg_face_row_form_vs_oracle(dghost, aniso):
         if F.el2[i] < 0:
             assert vec_rel_err(r, ro) < 1e-13
     assert worst < 1e-13, worst
+
+
+def test_double_word_operations_error_bounds(hostlib):
+    """Each double-word operation against exact rational arithmetic on the
+    converted operands: relative error within 2^-44 of the result (products,
+    reciprocals) or of the operands' magnitude (sums, fused forms), the order
+    of the published bounds for these algorithms."""
+    from fractions import Fraction
+    rng = np.random.default_rng(5)
+    n = 400
+    a, b, c, d = (rng.standard_normal(n) * 10.0 ** rng.uniform(-6, 6, n) for _ in range(4))
+    out = np.zeros(n)
+    conv = np.zeros(2 * n, np.float32)
+    back = np.zeros(n)
+    exact_in = []
+    for v in (a, b, c, d):  # the operands as the kernels hold them (h + l)
+        hostlib.host_dw_roundtrip(np.ascontiguousarray(v).ctypes.data, n, conv.ctypes.data, back.ctypes.data)
+        exact_in.append([Fraction(float(h)) + Fraction(float(l)) for h, l in zip(conv[0::2], conv[1::2])])
+    A, B, C, D = exact_in
+    u = 2.0 ** -44
+    ptr = [np.ascontiguousarray(v).ctypes.data for v in (a, b, c, d)]
+    for op, exact, scale in (
+            (0, [x * y for x, y in zip(A, B)], None),
+            (1, [x + y for x, y in zip(A, B)], [abs(x) + abs(y) for x, y in zip(A, B)]),
+            (2, [x * y + z for x, y, z in zip(A, B, C)], [abs(x * y) + abs(z) for x, y, z in zip(A, B, C)]),
+            (3, [x * y - z * w for x, y, z, w in zip(A, B, C, D)],
+             [abs(x * y) + abs(z * w) for x, y, z, w in zip(A, B, C, D)]),
+            (4, [1 / x for x in A], None),
+            (5, [(x + y + z) * w for x, y, z, w in zip(A, B, C, D)],
+             [(abs(x) + abs(y) + abs(z)) * abs(w) for x, y, z, w in zip(A, B, C, D)])):
+        hostlib.host_dw_ops(op, n, *ptr, out.ctypes.data)
+        sc = scale if scale is not None else [abs(e) for e in exact]
+        err = max(abs(Fraction(float(o)) - e) / s for o, e, s in zip(out, exact, sc))
+        assert err < u, (op, float(err))
+
+
+def test_double_word_long_sums(hostlib):
+    """The long-sum accumulator of the DG kernels (exact products, TwoSum
+    chain, rounding errors folded every few terms) on dot products of length
+    48 with cancellation: error within 2^-46 of the summed magnitudes."""
+    from fractions import Fraction
+    rng = np.random.default_rng(9)
+    worst = 0.0
+    for _ in range(200):
+        n = 48
+        x = rng.standard_normal(n) * 10.0 ** rng.uniform(-3, 3)
+        y = rng.standard_normal(n)
+        y[-1] = -float(np.dot(x[:-1], y[:-1]) / x[-1])  # strong cancellation
+        conv = np.zeros(2 * n, np.float32)
+        back = np.zeros(n)
+        xs, ys = [], []
+        for v, acc in ((x, xs), (y, ys)):
+            hostlib.host_dw_roundtrip(np.ascontiguousarray(v).ctypes.data, n, conv.ctypes.data, back.ctypes.data)
+            acc.extend(Fraction(float(h)) + Fraction(float(l)) for h, l in zip(conv[0::2], conv[1::2]))
+        exact = sum(p * q for p, q in zip(xs, ys))
+        mag = sum(abs(p * q) for p, q in zip(xs, ys))
+        for fold in (2, 4):
+            got = hostlib.host_dwacc_dot(n, np.ascontiguousarray(x).ctypes.data, np.ascontiguousarray(y).ctypes.data,
+                                         fold)
+            worst = max(worst, float(abs(Fraction(got) - exact) / mag))
+    assert worst < 2.0 ** -46, worst
