@@ -63,9 +63,11 @@ GB_HD int packed_index(int u, int w) { return u * 6 - (u * (u - 1)) / 2 + (w - u
 // which the Binet-Cauchy identity (a x b).(c x d) = (a.c)(b.d) - (a.d)(b.c)
 // gives from the six inner products a_ij = j_i'.j_j' in two operations each;
 // det' = j3'.(j1' x j2').
-// Arithmetic-generic pieces: T is double, or a double-word type providing
-// +, -, *, unary -, t_fma, t_abs, construction from a double constant and a
-// prism_recip6 overload found by argument-dependent lookup.
+// Pieces written for an arithmetic type T with +, -, *, unary -, t_fma,
+// t_abs, construction from a double constant and a prism_recip6 overload
+// (found by argument-dependent lookup).  The element below is instantiated
+// for double; the double-word element (prism_dw.cuh) reuses the vector
+// helpers with float pairs and restructures the quadrature sums.
 GB_HD double t_fma(double a, double b, double c) { return fma(a, b, c); }
 GB_HD double t_abs(double a) { return fabs(a); }
 
