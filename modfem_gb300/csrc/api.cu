@@ -256,6 +256,16 @@ static int alloc_matrix(gbfem_ctx c) {
   return 0;
 }
 
+// A new structure voids the drop-in's cached tables and download plan
+// (they index the old row_ptr / values), whatever pointers the caller passes.
+static void forget_dropin_tables(gbfem_ctx c) {
+  for (int i = 0; i < 3; i++) {
+    c->cache_key[i] = nullptr;
+    c->cache_len[i] = 0;
+  }
+  c->pipe_e0 = c->pipe_e1 = -1;
+}
+
 int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long long nnz, const int *row_ptr,
                             const int *col_ind) {
   GB_CHECK(c && c->nno > 0, "mesh not set");
@@ -271,6 +281,7 @@ int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long 
   GB_TRY(upload(c, c->col_ind, col_ind, (size_t)nnz));
   if (dof_of_node) GB_TRY(upload(c, c->dof_of_node, dof_of_node, (size_t)c->nno));
   GB_TRY(alloc_matrix(c));
+  forget_dropin_tables(c);
   c->have_structure = true;
   c->have_tables = false;
   GB_CUDA(cudaStreamSynchronize(c->stream));
@@ -292,6 +303,7 @@ int gbfem_build_structure(gbfem_ctx c, int *ndof, long long *nnz, int *nr_colors
   c->h_el_color_ptr = c->hs.el_color_ptr;
   c->h_fa_color_ptr = c->hs.fa_color_ptr;
   GB_TRY(alloc_matrix(c));
+  forget_dropin_tables(c);
   c->have_structure = c->have_tables = true;
   GB_CUDA(cudaStreamSynchronize(c->stream));
   if (ndof) *ndof = c->ndof;
@@ -338,6 +350,7 @@ int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
     GB_TRY(upload(c, c->fa_perm, perm.data(), perm.size()));
   }
   GB_TRY(alloc_matrix(c));
+  forget_dropin_tables(c);
   c->have_structure = c->have_tables = true;
   GB_CUDA(cudaStreamSynchronize(c->stream));
   if (ndof) *ndof = nd;
