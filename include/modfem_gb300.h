@@ -57,7 +57,9 @@ long long gbfem_device_bytes(gbfem_ctx ctx);
  * device copies of the entity lists and assembly table between calls and
  * skips their upload while the caller passes the same pointers and sizes;
  * the caller promises not to change their contents, as holds in ModFEM
- * between sir_create and sir_free.
+ * between sir_create and sir_free.  A new structure (gbfem_set_crs_structure,
+ * gbfem_build_structure*) voids the cache.  With the cache on, the call also
+ * downloads each element chunk's finished rows while the next chunk runs.
  * GBFEM_OPT_STD_ARITH: arithmetic of the std prism element matrices with an
  * isotropic coefficient (gbfem_assemble and the drop-in), GBFEM_STD_FP64
  * (default) or GBFEM_STD_DWORD: double-word float pairs on the FP32 pipe
