@@ -55,11 +55,15 @@ long long gbfem_device_bytes(gbfem_ctx ctx);
 /* Options (no reference counterpart).
  * GBFEM_OPT_CACHE_TABLES = 1: gbfem_create_assemble_stiff_mat keeps the
  * device copies of the entity lists and assembly table between calls and
- * skips their upload while the caller passes the same pointers and sizes;
- * the caller promises not to change their contents, as holds in ModFEM
- * between sir_create and sir_free.  A new structure (gbfem_set_crs_structure,
- * gbfem_build_structure*) voids the cache.  With the cache on, the call also
- * downloads each element chunk's finished rows while the next chunk runs.
+ * skips their upload while the caller passes the same pointers and sizes and
+ * a sample of 257 entries of each array (first, last, equal strides) reads
+ * the same as at upload.  The caller promises not to change their contents,
+ * as holds in ModFEM between sir_create and sir_free; the sample catches most
+ * violations (new tables at a reused address), gbfem_invalidate_tables voids
+ * the cache explicitly (call it after sir_free / a new sir_create), and a new
+ * structure (gbfem_set_crs_structure, gbfem_build_structure*) or setting this
+ * option again voids it too.  With the cache on, the call also downloads each
+ * element chunk's finished rows while the next chunk runs.
  * GBFEM_OPT_STD_ARITH: arithmetic of the std prism element matrices with an
  * isotropic coefficient (gbfem_assemble and the drop-in), GBFEM_STD_FP64
  * (default) or GBFEM_STD_DWORD: double-word float pairs on the FP32 pipe
@@ -77,6 +81,13 @@ long long gbfem_device_bytes(gbfem_ctx ctx);
 #define GBFEM_STD_FP64 0
 #define GBFEM_STD_DWORD 1
 int gbfem_set_option(gbfem_ctx ctx, int option, long long value);
+/* Voids the drop-in table cache (GBFEM_OPT_CACHE_TABLES): the next
+ * gbfem_create_assemble_stiff_mat uploads its lists and table again.  No
+ * reference counterpart (ModFEM frees its tables in sir_free). */
+int gbfem_invalidate_tables(gbfem_ctx ctx);
+/* Cache bookkeeping: how often the cache was voided, and how many drop-in
+ * input arrays were copied to the device (cache misses). */
+int gbfem_table_cache_stats(gbfem_ctx ctx, long long *generation, long long *uploads);
 
 /* ---------------------------------------------------------------------- */
 /* problem data                                                             */
@@ -304,7 +315,8 @@ int gbfem_compute_residual(gbfem_ctx ctx, int Use_rhs, int Ini_zero, int Ndof, c
  * calls on a device share the one array, so calls whose work overlaps on the
  * GPU (two contexts or threads on the same device at once) race and must be
  * serialised by the caller.  The matrix is the context's device-resident one,
- * set up beforehand. */
+ * set up beforehand.  The call runs on the context's device and leaves the
+ * caller's current device as it found it. */
 #define GBFEM_NOALLOC_MAX_NDOF 262144
 int gbfem_compute_residual_noalloc(gbfem_ctx ctx, int Use_rhs, int Ini_zero, int Ndof, const double *X,
                                    const double *B, double *V);

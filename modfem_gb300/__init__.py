@@ -34,6 +34,8 @@ SIGNATURES = [
     ("gbfem_destroy", _ci, [_vp]),
     ("gbfem_device_bytes", _cll, [_vp]),
     ("gbfem_set_option", _ci, [_vp, _ci, _cll]),
+    ("gbfem_invalidate_tables", _ci, [_vp]),
+    ("gbfem_table_cache_stats", _ci, [_vp, _pll, _pll]),
     ("gbfem_set_mesh", _ci, [_vp, _ci, _vp, _ci, _ci, _vp, _ci, _vp, _vp, _vp, _vp]),
     ("gbfem_set_node_coords", _ci, [_vp, _vp]),
     ("gbfem_set_coefficients", _ci, [_vp, _vp, _vp, _cd, _cd, _cd]),
@@ -160,6 +162,16 @@ class Context:
 
     def set_option(self, opt, value):
         self._check(self.L.gbfem_set_option(self._h, opt, value))
+
+    def invalidate_tables(self):
+        """gbfem_invalidate_tables: the next drop-in call uploads its lists and table again."""
+        self._check(self.L.gbfem_invalidate_tables(self._h))
+
+    def table_cache_stats(self):
+        """(generation, uploads) of the drop-in table cache."""
+        g, u = ctypes.c_longlong(), ctypes.c_longlong()
+        self._check(self.L.gbfem_table_cache_stats(self._h, ctypes.byref(g), ctypes.byref(u)))
+        return g.value, u.value
 
     # ---------------- problem data ----------------
     def set_mesh(self, mesh):

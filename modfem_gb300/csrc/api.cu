@@ -152,14 +152,13 @@ long long gbfem_device_bytes(gbfem_ctx c) {
   return s;
 }
 
+static void forget_dropin_tables(gbfem_ctx c);
+
 int gbfem_set_option(gbfem_ctx c, int option, long long value) {
   GB_CHECK(c, "null context");
   if (option == GBFEM_OPT_CACHE_TABLES) {
     c->cache_tables = value ? 1 : 0;
-    for (int i = 0; i < 3; i++) {
-      c->cache_key[i] = nullptr;
-      c->cache_len[i] = 0;
-    }
+    forget_dropin_tables(c);
     return 0;
   }
   if (option == GBFEM_OPT_DG_SPMV_ARITH) {
@@ -262,8 +261,23 @@ static void forget_dropin_tables(gbfem_ctx c) {
   for (int i = 0; i < 3; i++) {
     c->cache_key[i] = nullptr;
     c->cache_len[i] = 0;
+    c->cache_sig[i] = 0;
   }
   c->pipe_e0 = c->pipe_e1 = -1;
+  c->table_generation++;
+}
+
+int gbfem_invalidate_tables(gbfem_ctx c) {
+  GB_CHECK(c, "null context");
+  forget_dropin_tables(c);
+  return 0;
+}
+
+int gbfem_table_cache_stats(gbfem_ctx c, long long *generation, long long *uploads) {
+  GB_CHECK(c, "null context");
+  if (generation) *generation = c->table_generation;
+  if (uploads) *uploads = c->table_uploads;
+  return 0;
 }
 
 int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long long nnz, const int *row_ptr,
@@ -387,12 +401,34 @@ static int check_err_flag(gbfem_ctx c) {
   return 0;
 }
 
-// Copies one drop-in input unless cached under the same pointer and length.
+// Fingerprint of a host int array from 257 entries spread over it (the
+// first, the last and 255 at equal strides; FNV-1a over index and value).
+static unsigned long long table_signature(const int *h, long long n) {
+  unsigned long long s = 1469598103934665603ULL ^ (unsigned long long)n;
+  if (n <= 0) return s;
+  const int kSamples = 256;
+  for (int i = 0; i <= kSamples; i++) {
+    const long long j = i == kSamples ? n - 1 : (n * i) / kSamples;
+    s = (s ^ (unsigned long long)(unsigned)j) * 1099511628211ULL;
+    s = (s ^ (unsigned long long)(unsigned)h[j]) * 1099511628211ULL;
+  }
+  return s;
+}
+
+// Copies one drop-in input unless the tables are cached and this slot holds
+// the same pointer and length with the same sampled contents; any upload
+// voids the download plan, which depends on the tables.
 static int stage_input(gbfem_ctx c, int slot, DevBuf<int> &d, const int *h, long long n) {
-  if (c->cache_tables && c->cache_key[slot] == h && c->cache_len[slot] == n && d.n >= (size_t)n) return 0;
+  const unsigned long long sig = c->cache_tables ? table_signature(h, n) : 0;
+  if (c->cache_tables && c->cache_key[slot] == h && c->cache_len[slot] == n && c->cache_sig[slot] == sig &&
+      d.n >= (size_t)n)
+    return 0;
   GB_TRY(upload(c, d, h, (size_t)n));
   c->cache_key[slot] = h;
   c->cache_len[slot] = n;
+  c->cache_sig[slot] = sig;
+  c->pipe_e0 = c->pipe_e1 = -1;
+  c->table_uploads++;
   return 0;
 }
 
@@ -545,8 +581,8 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   GB_TRY(stage_input(c, 1, c->in_pos, Asse_pos_first_dof_int_ent, Nr_int_ent));
   GB_TRY(stage_input(c, 2, c->in_table, Assembly_table, tlen));
   const int do_sm = Comp_type != GBFEM_COMP_RHS, do_rhs = Comp_type != GBFEM_COMP_SM;
-  if (do_sm) GB_CUDA(cudaMemsetAsync(c->val.p, 0, c->val.bytes(), c->stream));
-  if (do_rhs) GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, c->rhs.bytes(), c->stream));
+  if (do_sm) GB_CUDA(cudaMemsetAsync(c->val.p, 0, (size_t)c->nnz * sizeof(double), c->stream));
+  if (do_rhs) GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, (size_t)c->ndof * sizeof(double), c->stream));
   int launches = 0, r;
   const bool side = f1 > f0;  // the faces run beside the element chunks
   if (side)
@@ -605,8 +641,8 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     launches += r;
     cudaEventRecord(c->ev3, c->stream);
     if (side) GB_TRY(join_side(c, c->stream));
-    if (crs_val) GB_CUDA(cudaMemcpyAsync(crs_val, c->val.p, c->val.bytes(), cudaMemcpyDeviceToHost, c->stream));
-    if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->rhs.p, c->rhs.bytes(), cudaMemcpyDeviceToHost, c->stream));
+    if (crs_val) GB_CUDA(cudaMemcpyAsync(crs_val, c->val.p, (size_t)c->nnz * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->rhs.p, (size_t)c->ndof * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   }
   cudaEventRecord(c->ev1, c->stream);
   GB_TRY(check_err_flag(c));
@@ -623,8 +659,8 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
   GB_CUDA(cudaSetDevice(c->device));
   const bool atomic = scatter_mode == GBFEM_SCATTER_ATOMIC;
   cudaEventRecord(c->ev0, c->stream);
-  GB_CUDA(cudaMemsetAsync(c->val.p, 0, c->val.bytes(), c->stream));
-  GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, c->rhs.bytes(), c->stream));
+  GB_CUDA(cudaMemsetAsync(c->val.p, 0, (size_t)c->nnz * sizeof(double), c->stream));
+  GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, (size_t)c->ndof * sizeof(double), c->stream));
   int launches = 0, r;
   // boundary faces, then elements (utd_util/uts_ls_intf.c:3629-3858,
   // 4103-4290); with atomic scatter the faces run beside the elements
@@ -1122,16 +1158,16 @@ int gbfem_dg_last_timing(gbfem_ctx c, double *total_ms, double *volume_ms, doubl
 
 int gbfem_dg_get_matrix(gbfem_ctx c, double *vals, double *rhs) {
   GB_CHECK(c && c->dg_ready, "DG structure not built");
-  if (vals) GB_CUDA(cudaMemcpyAsync(vals, c->dg_val.p, c->dg_val.bytes(), cudaMemcpyDeviceToHost, c->stream));
-  if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->dg_rhs.p, c->dg_rhs.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  if (vals) GB_CUDA(cudaMemcpyAsync(vals, c->dg_val.p, (size_t)c->dg_nval * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->dg_rhs.p, (size_t)c->dg_ndof * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
 }
 
 int gbfem_dg_set_matrix(gbfem_ctx c, const double *vals, const double *rhs) {
   GB_CHECK(c && c->dg_ready, "DG structure not built");
-  if (vals) GB_CUDA(cudaMemcpyAsync(c->dg_val.p, vals, c->dg_val.bytes(), cudaMemcpyHostToDevice, c->stream));
-  if (rhs) GB_CUDA(cudaMemcpyAsync(c->dg_rhs.p, rhs, c->dg_rhs.bytes(), cudaMemcpyHostToDevice, c->stream));
+  if (vals) GB_CUDA(cudaMemcpyAsync(c->dg_val.p, vals, (size_t)c->dg_nval * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (rhs) GB_CUDA(cudaMemcpyAsync(c->dg_rhs.p, rhs, (size_t)c->dg_ndof * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
 }
@@ -1207,16 +1243,16 @@ int gbfem_measure_fp64_peak(gbfem_ctx c, double *tflops) {
 
 int gbfem_get_matrix(gbfem_ctx c, double *crs_val, double *rhs) {
   GB_CHECK(c && c->have_structure, "structure not set");
-  if (crs_val) GB_CUDA(cudaMemcpyAsync(crs_val, c->val.p, c->val.bytes(), cudaMemcpyDeviceToHost, c->stream));
-  if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->rhs.p, c->rhs.bytes(), cudaMemcpyDeviceToHost, c->stream));
+  if (crs_val) GB_CUDA(cudaMemcpyAsync(crs_val, c->val.p, (size_t)c->nnz * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (rhs) GB_CUDA(cudaMemcpyAsync(rhs, c->rhs.p, (size_t)c->ndof * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
 }
 
 int gbfem_set_matrix(gbfem_ctx c, const double *crs_val, const double *rhs) {
   GB_CHECK(c && c->have_structure, "structure not set");
-  if (crs_val) GB_CUDA(cudaMemcpyAsync(c->val.p, crs_val, c->val.bytes(), cudaMemcpyHostToDevice, c->stream));
-  if (rhs) GB_CUDA(cudaMemcpyAsync(c->rhs.p, rhs, c->rhs.bytes(), cudaMemcpyHostToDevice, c->stream));
+  if (crs_val) GB_CUDA(cudaMemcpyAsync(c->val.p, crs_val, (size_t)c->nnz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (rhs) GB_CUDA(cudaMemcpyAsync(c->rhs.p, rhs, (size_t)c->ndof * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
 }

@@ -216,6 +216,9 @@ struct gbfem_ctx_s {
   gbfem::DevBuf<int> in_id, in_pos, in_table;
   const void *cache_key[3] = {nullptr, nullptr, nullptr};
   long long cache_len[3] = {0, 0, 0};
+  unsigned long long cache_sig[3] = {0, 0, 0};  // sampled contents at upload
+  long long table_generation = 0;  // bumped whenever the cached tables are voided
+  long long table_uploads = 0;     // drop-in inputs copied to the device (cache misses)
   int cache_tables = 0;
   bool std_dword = false;  // std prism elements in double-word arithmetic
   // pipelined download of the drop-in call while the tables are cached:

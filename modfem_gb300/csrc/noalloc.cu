@@ -40,6 +40,18 @@ int scratch_for_device(int device, double **out) {
   return 0;
 }
 
+// Makes the context's device current for the call and puts the caller's
+// current device back on every return.
+struct DeviceGuard {
+  int saved = -1;
+  ~DeviceGuard() {
+    if (saved >= 0) cudaSetDevice(saved);
+  }
+};
+
+int residual_on_device(gbfem_ctx c, int Use_rhs, int Ini_zero, int Ndof, const double *X, const double *B,
+                       double *V);
+
 }  // namespace
 
 extern "C" int gbfem_compute_residual_noalloc(gbfem_ctx c, int Use_rhs, int Ini_zero, int Ndof, const double *X,
@@ -50,7 +62,17 @@ extern "C" int gbfem_compute_residual_noalloc(gbfem_ctx c, int Use_rhs, int Ini_
   GB_CHECK(Ndof <= GBFEM_NOALLOC_MAX_NDOF,
            "Ndof exceeds GBFEM_NOALLOC_MAX_NDOF (262144), the size of the no-alloc scratch; use "
            "gbfem_compute_residual");
+  DeviceGuard guard;
+  GB_CUDA(cudaGetDevice(&guard.saved));
+  if (guard.saved == c->device) guard.saved = -1;  // nothing to restore
   GB_CUDA(cudaSetDevice(c->device));
+  return residual_on_device(c, Use_rhs, Ini_zero, Ndof, X, B, V);
+}
+
+namespace {
+
+int residual_on_device(gbfem_ctx c, int Use_rhs, int Ini_zero, int Ndof, const double *X, const double *B,
+                       double *V) {
   double *scratch = nullptr;
   GB_TRY_NOALLOC(scratch_for_device(c->device, &scratch));
   double *xd = scratch, *bd = scratch + GBFEM_NOALLOC_MAX_NDOF, *vd = scratch + 2 * GBFEM_NOALLOC_MAX_NDOF;
@@ -75,3 +97,5 @@ extern "C" int gbfem_compute_residual_noalloc(gbfem_ctx c, int Use_rhs, int Ini_
   GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
 }
+
+}  // namespace

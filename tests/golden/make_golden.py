@@ -1,7 +1,8 @@
 """Generates the golden fixtures in this directory from the reference ModFEM.
 
-Runs the reference C path compiled in-tree (``make -C oracle/ref``, which
-needs the ModFEM sources) through ``oracle/refmod.py``: the reference's own jk
+Runs the reference C path compiled in-tree (``make -C oracle/ref REF=...``,
+which needs the ModFEM sources: $MODFEM_REF_SRC, or a checkout named
+``reference`` beside this repository) through ``oracle/refmod.py``: the reference's own jk
 mesh reader, approximation module, weak forms, sir_create, the table-driven
 assembly driver and GMRES.  Each case runs in a fresh process because the
 reference keeps its meshes, fields and solvers in global arrays.
@@ -258,7 +259,9 @@ def run_fields(name="fields"):
 
 
 def main(argv):
-    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref")])
+    ref = os.environ.get("MODFEM_REF_SRC") or os.path.normpath(
+        os.path.join(ROOT, "..", "reference", "modfem2017", "src"))
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref}"])
     names = argv or list(CASES) + ["std_tet_n2", "dg_el_n2", "dg_el_aniso_n2"] + list(DG_ASM_CASES) + ["fields"]
     if len(names) == 1 and os.environ.get("MAKE_GOLDEN_CHILD"):
         with open(os.devnull, "w") as dn:

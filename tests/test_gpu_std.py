@@ -123,6 +123,138 @@ def test_dropin_table_cache(gb):
     assert crs_rel_err(g["row_ptr"], val, vo, sc) < REL_TOL
 
 
+GUARD = 16
+
+
+def _guarded(n):
+    """A host array of n doubles followed by GUARD sentinel entries; returns
+    (the whole buffer, its first n entries as a view)."""
+    buf = np.full(n + GUARD, 7.25)
+    return buf, buf[:n]
+
+
+def _dropin_args(g, bufs=None):
+    """The reference's drop-in inputs of fixture g as int32 arrays; with
+    bufs (a dict of larger int32 arrays) written into their prefixes, so that
+    successive calls pass the same host pointers."""
+    names = ("int_ent_type", "int_ent_id", "color_elems", "color_faces", "asse_pos", "assembly_table")
+    out = []
+    for k in names:
+        a = np.ascontiguousarray(g[k], dtype=np.int32)
+        if bufs is not None:
+            bufs[k][:a.size] = a
+            a = bufs[k][:a.size]
+        out.append(a)
+    return out
+
+
+@pytest.mark.parametrize("cache", [0, 1])
+def test_smaller_structure_in_a_live_context(gb, cache):
+    """A large structure, then a smaller one in the same context: the device
+    buffers keep their larger capacity, but every copy to or from the host is
+    sized by the current structure (guard entries past the end stay as they
+    were), and the drop-in, gbfem_get_matrix and gbfem_set_matrix give the
+    small problem's values.  With the table cache on, the small problem's
+    tables sit at the same host addresses as the large one's."""
+    big, small = load("std_n10"), load("std_n4")
+    bufs = {k: np.zeros(np.asarray(big[k]).size + 64, np.int32) for k in
+            ("int_ent_type", "int_ent_id", "color_elems", "color_faces", "asse_pos", "assembly_table")}
+    c = gb.Context(0)
+    c.set_option(gb.OPT_CACHE_TABLES, cache)
+    for g in (big, small):
+        m = FixtureMesh(g)
+        c.set_mesh(m)
+        c.set_coefficients(k=g["k"], f=1.0, g=0.0, penalty=1e7)
+        c.set_crs_structure(g["dof_of_node"], g["row_ptr"], g["col_ind"])
+        nnz, nd = g["col_ind"].size, g["row_ptr"].size - 1
+        vb, val = _guarded(nnz)
+        rb, rhs = _guarded(nd)
+        c.create_assemble_stiff_mat(*_dropin_args(g, bufs), crs_val=val, rhs=rhs)
+        assert np.all(vb[nnz:] == 7.25) and np.all(rb[nd:] == 7.25)
+        sc = energy_scale(g["row_ptr"], g["col_ind"], g["crs_val"])
+        assert crs_rel_err(g["row_ptr"], val, g["crs_val"], sc) < REL_TOL
+        assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL
+        # download into exactly-sized views of guarded buffers
+        vb2, val2 = _guarded(nnz)
+        rb2, rhs2 = _guarded(nd)
+        c.get_matrix(val2, rhs2)
+        assert np.all(vb2[nnz:] == 7.25) and np.all(rb2[nd:] == 7.25)
+        assert np.array_equal(val2, val) and np.array_equal(rhs2, rhs)
+        # upload reads nnz / ndof entries only: the guard values must not arrive
+        c.set_matrix(vb2[:nnz] * 2.0, rb2[:nd] * 2.0)
+        val3, rhs3 = c.get_matrix()
+        assert np.array_equal(val3, 2.0 * val) and np.array_equal(rhs3, 2.0 * rhs)
+    c.close()
+
+
+def test_dropin_cache_sees_new_tables_at_the_same_address(gb):
+    """With cached tables, the entity order changed in place (same host
+    pointers, same lengths): the sampled contents differ, so the call
+    uploads the lists again and rebuilds its chunked download plan; setting
+    the option again or gbfem_invalidate_tables voids the cache too.  Each
+    call matches a one-shot call without the cache."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(50, jitter=0.2, seed=7)
+    k = lognormal_k(m.nel, seed=7)
+    ref = make_ctx(gb, m, k)
+    nd, nnz, _ = ref.build_structure()
+    tables = ref.get_element_tables()
+    fa_tab = tables.reshape(m.nel, 42)[m.bc_face_el].reshape(-1)
+    tab = np.concatenate([tables, fa_tab]).astype(np.int32)
+    nf = m.bc_face_id.size
+    types = np.concatenate([np.full(m.nel, gb.ELEMENT), np.full(nf, gb.FACE)]).astype(np.int32)
+    ce = np.array([0, m.nel], np.int32)
+    cf = np.array([m.nel, m.nel + nf], np.int32)
+    ids = np.zeros(m.nel + nf, np.int32)
+    pos = np.zeros(m.nel + nf, np.int32)
+
+    def fill(order):
+        ids[:m.nel] = order + 1
+        ids[m.nel:] = m.bc_face_id
+        pos[:m.nel] = order * 42
+        pos[m.nel:] = 42 * m.nel + np.arange(nf) * 42
+
+    fill(np.arange(m.nel))
+    v0, r0 = np.zeros(nnz), np.zeros(nd)
+    ref.create_assemble_stiff_mat(types, ids, ce, cf, pos, tab, crs_val=v0, rhs=r0)
+    sc = np.abs(v0) + 1e-300
+
+    c = make_ctx(gb, m, k)
+    c.build_structure()
+    c.set_option(gb.OPT_CACHE_TABLES, 1)
+    val, rhs = np.zeros(nnz), np.zeros(nd)
+
+    def run():
+        val[:] = 0
+        rhs[:] = 0
+        c.create_assemble_stiff_mat(types, ids, ce, cf, pos, tab, crs_val=val, rhs=rhs)
+        assert np.max(np.abs(val - v0) / np.maximum(sc, 1e-3 * np.max(sc))) < 1e-12
+        assert np.max(np.abs(rhs - r0)) <= 1e-12 * np.max(np.abs(r0))
+
+    run()
+    gen0, up0 = c.table_cache_stats()
+    run()  # cache hit: nothing uploaded
+    assert c.table_cache_stats() == (gen0, up0)
+    fill(np.random.default_rng(1).permutation(m.nel))  # same addresses, new order
+    run()
+    gen1, up1 = c.table_cache_stats()
+    assert up1 == up0 + 2  # ids and positions again; the assembly table is unchanged
+    fill(np.arange(m.nel)[::-1].copy())
+    c.set_option(gb.OPT_CACHE_TABLES, 1)  # voids the cache: all three arrays again
+    run()
+    gen2, up2 = c.table_cache_stats()
+    assert gen2 > gen1 and up2 == up1 + 3
+    c.invalidate_tables()
+    run()
+    assert c.table_cache_stats()[1] == up2 + 3
+    # a new structure voids the cache as well
+    c.set_crs_structure(*ref.get_crs_structure())
+    run()
+    assert c.table_cache_stats()[1] == up2 + 6
+    ref.close()
+    c.close()
+
+
 @pytest.mark.parametrize("shuffle", [False, True])
 def test_dropin_pipelined_download(gb, shuffle):
     """With cached tables the drop-in runs the elements in chunks and copies

@@ -53,6 +53,47 @@ def test_noalloc_residual_matches_allocating_entry_point_twice(gb):
     c.close()
 
 
+def _device_free_bytes():
+    """cuMemGetInfo on the calling thread's current context (the runtime's
+    primary context, made current by the library's calls)."""
+    import ctypes
+    cu = ctypes.CDLL("libcuda.so.1")
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert cu.cuMemGetInfo_v2(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
+def test_noalloc_allocates_nothing_on_a_fresh_context(gb):
+    """First residual of a fresh context through the no-alloc call: the
+    context's device buffers do not grow, and once the first call has looked
+    up the scratch array, further calls leave the device's free memory as it
+    was.  The allocating call afterwards grows the context, as a contrast."""
+    from _util import FixtureMesh
+    g = load("std_n10")
+    m = FixtureMesh(g)
+    c = gb.Context(0)
+    c.set_mesh(m)
+    c.set_coefficients(k=g["k"])
+    c.set_crs_structure(g["dof_of_node"], g["row_ptr"], g["col_ind"])
+    c.set_matrix(g["crs_val"], g["crs_rhs"])
+    n = g["row_ptr"].size - 1
+    x = np.cos(np.arange(n) * 0.3)
+    held = c.device_bytes()
+    v1 = c.compute_residual_noalloc(x)
+    assert c.device_bytes() == held
+    free1 = _device_free_bytes()
+    v2 = c.compute_residual_noalloc(x, b=np.ones(n))
+    v3 = c.compute_residual_noalloc(x)
+    assert _device_free_bytes() == free1
+    assert c.device_bytes() == held
+    assert np.array_equal(v1, v3)
+    ref = c.compute_residual(x)
+    assert vec_rel_err(v1, ref) < 1e-12
+    assert vec_rel_err(v2, c.compute_residual(x, b=np.ones(n))) < 1e-12
+    assert c.device_bytes() > held  # the allocating entry point grew its staging buffers
+    c.close()
+
+
 def test_noalloc_rejects_sizes_beyond_scratch(gb):
     from modfem_gb300.mesh import structured_prism_mesh
     m = structured_prism_mesh(64)  # 65^3 = 274,625 dofs > 262,144
