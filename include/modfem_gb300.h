@@ -74,12 +74,27 @@ long long gbfem_device_bytes(gbfem_ctx ctx);
  * the Arnoldi steps of gbfem_dg_solve, GBFEM_STD_FP64 (default) or
  * GBFEM_STD_DWORD: double-word copies of the matrix and of the inverted
  * diagonal blocks, products summed on the FP32 pipes (the FP64 form is bound
- * by the FP64 pipe below HBM bandwidth); the restart residuals stay FP64. */
+ * by the FP64 pipe below HBM bandwidth); the restart residuals stay FP64.
+ * GBFEM_OPT_DG_RESIDUAL: arithmetic of the DG true residual b - A x in
+ * gbfem_dg_compute_residual and the outer steps of gbfem_dg_solve_ir:
+ * GBFEM_RESIDUAL_FP64 (default) or GBFEM_RESIDUAL_COMPENSATED, FP64 products and sums with their rounding
+ * errors carried in a second FP64 word (as accurate as twice the working
+ * precision): refinement then reaches a solution accurate to about FP64
+ * rounding even where the FP64 residual of a penalty-scaled system stalls
+ * near 1e-11 relative.
+ * GBFEM_OPT_STD_SPMV_ARITH: arithmetic of the preconditioned SpMV in the
+ * Arnoldi steps of gbfem_solve, GBFEM_STD_FP64 (default) or GBFEM_STD_DWORD:
+ * a double-word copy of the matrix (float pairs, 8 bytes a value like FP64)
+ * with the products on the FP32 pipes; the restart residuals stay FP64. */
 #define GBFEM_OPT_CACHE_TABLES 1
 #define GBFEM_OPT_STD_ARITH 2
 #define GBFEM_OPT_DG_SPMV_ARITH 3
+#define GBFEM_OPT_DG_RESIDUAL 4
+#define GBFEM_OPT_STD_SPMV_ARITH 5
 #define GBFEM_STD_FP64 0
 #define GBFEM_STD_DWORD 1
+#define GBFEM_RESIDUAL_FP64 0
+#define GBFEM_RESIDUAL_COMPENSATED 1
 int gbfem_set_option(gbfem_ctx ctx, int option, long long value);
 /* Voids the drop-in table cache (GBFEM_OPT_CACHE_TABLES): the next
  * gbfem_create_assemble_stiff_mat uploads its lists and table again.  No
@@ -288,8 +303,12 @@ int gbfem_dg_solve(gbfem_ctx ctx, int krylov, int max_iter, double tol_rel, int 
  * at inner_tol relative to its initial preconditioned residual or after 10
  * restart cycles (10 krylov iterations); the loop
  * stops when ||b - A x|| <= tol_rel ||b|| or max_iter inner iterations were
- * spent.  Returns the inner iterations; *outer_steps refinement steps,
- * *rel_res the final relative true residual. */
+ * spent.  With GBFEM_OPT_DG_RESIDUAL = GBFEM_RESIDUAL_COMPENSATED the true
+ * residual carries twice the working precision and the loop also stops once
+ * a correction is below 4 ulp of ||x|| or no longer halves the previous one:
+ * x is then accurate to about FP64 rounding (tol_rel below the FP64 residual
+ * floor asks for exactly that).  Returns the inner iterations; *outer_steps
+ * refinement steps, *rel_res the final relative true residual. */
 int gbfem_dg_solve_ir(gbfem_ctx ctx, int krylov, int max_iter, double tol_rel, double inner_tol, double *x,
                       int *outer_steps, double *rel_res);
 

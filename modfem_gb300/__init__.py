@@ -19,7 +19,10 @@ SCATTER_ATOMIC, SCATTER_COLOR = 0, 1
 OPT_CACHE_TABLES = 1
 OPT_STD_ARITH = 2
 OPT_DG_SPMV_ARITH = 3
+OPT_DG_RESIDUAL = 4
+OPT_STD_SPMV_ARITH = 5
 STD_FP64, STD_DWORD = 0, 1
+RESIDUAL_FP64, RESIDUAL_COMPENSATED = 0, 1
 DG_VOLUME_FP64, DG_VOLUME_TC, DG_VOLUME_TF32, DG_VOLUME_DWORD, DG_VOLUME_TC_DWORD = 0, 1, 2, 3, 4
 DG_FACE_FP64, DG_FACE_TC, DG_FACE_DWORD, DG_FACE_TC_DWORD = 0, 1, 2, 3
 

@@ -18,11 +18,6 @@ void set_error(const std::string &msg) { g_err = msg; }
 using gbfem::DevBuf;
 using gbfem::set_error;
 
-#define GB_TRY(x)            \
-  do {                       \
-    int r_ = (x);            \
-    if (r_ < 0) return r_;   \
-  } while (0)
 
 template <typename T>
 static int upload(gbfem_ctx c, DevBuf<T> &d, const T *h, size_t n) {
@@ -39,6 +34,14 @@ static int dg_spmv(gbfem_ctx c, int mode, const double *x, const double *b, doub
   int n = 0;
   for (int p = 1; p <= 4; p++) {
     if (!c->dg_list[p].p) continue;
+    if (mode == 2 && c->dg_residual_dd) {
+      const int r = gbfem::launch_dg_block_residual_dd(c->stream, p + dg_class_off(c), (int)c->dg_list[p].n,
+                                                       c->dg_list[p].p, c->dg_roff_d.p, c->dg_row_val_d.p,
+                                                       c->dg_cx_off_d.p, c->dg_colx_d.p, c->dg_val.p, x, b, out);
+      if (r < 0) return r;
+      n += r;
+      continue;
+    }
     const int r = gbfem::launch_dg_block_spmv(c->stream, mode, p + dg_class_off(c), (int)c->dg_list[p].n, c->dg_list[p].p,
                                               c->dg_roff_d.p, c->dg_row_val_d.p, c->dg_cx_off_d.p, c->dg_colx_d.p,
                                               c->dg_val.p, c->dg_dinv_off_d.p, c->dg_dinv.p, x, b, out);
@@ -89,6 +92,12 @@ int gbfem_destroy(gbfem_ctx c) {
       if (ev) cudaEventDestroy(ev);
   }
   c->row_last.release();
+  if (c->gm_graph) cudaGraphExecDestroy(c->gm_graph);
+  c->sell_off.release();
+  c->sell_col.release();
+  c->sell_val.release();
+  c->sell_valdw.release();
+  c->gm_small.release();
   if (c->side_stream) {
     cudaStreamSynchronize(c->side_stream);
     cudaStreamDestroy(c->side_stream);
@@ -164,6 +173,17 @@ int gbfem_set_option(gbfem_ctx c, int option, long long value) {
   if (option == GBFEM_OPT_DG_SPMV_ARITH) {
     GB_CHECK(value == GBFEM_STD_FP64 || value == GBFEM_STD_DWORD, "DG SpMV arithmetic must be FP64 or DWORD");
     c->dg_spmv_dword = value == GBFEM_STD_DWORD;
+    return 0;
+  }
+  if (option == GBFEM_OPT_STD_SPMV_ARITH) {
+    GB_CHECK(value == GBFEM_STD_FP64 || value == GBFEM_STD_DWORD, "std SpMV arithmetic must be FP64 or DWORD");
+    c->std_spmv_dword = value == GBFEM_STD_DWORD;
+    return 0;
+  }
+  if (option == GBFEM_OPT_DG_RESIDUAL) {
+    GB_CHECK(value == GBFEM_RESIDUAL_FP64 || value == GBFEM_RESIDUAL_COMPENSATED,
+             "DG residual arithmetic must be FP64 or COMPENSATED");
+    c->dg_residual_dd = value == GBFEM_RESIDUAL_COMPENSATED;
     return 0;
   }
   if (option == GBFEM_OPT_STD_ARITH) {
@@ -297,6 +317,7 @@ int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long 
   GB_TRY(alloc_matrix(c));
   forget_dropin_tables(c);
   c->have_structure = true;
+  c->sell_ready = false;
   c->have_tables = false;
   GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
@@ -319,6 +340,7 @@ int gbfem_build_structure(gbfem_ctx c, int *ndof, long long *nnz, int *nr_colors
   GB_TRY(alloc_matrix(c));
   forget_dropin_tables(c);
   c->have_structure = c->have_tables = true;
+  c->sell_ready = false;
   GB_CUDA(cudaStreamSynchronize(c->stream));
   if (ndof) *ndof = c->ndof;
   if (nnz) *nnz = c->nnz;
@@ -366,6 +388,7 @@ int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
   GB_TRY(alloc_matrix(c));
   forget_dropin_tables(c);
   c->have_structure = c->have_tables = true;
+  c->sell_ready = false;
   GB_CUDA(cudaStreamSynchronize(c->stream));
   if (ndof) *ndof = nd;
   if (nnz) *nnz = nz;
@@ -1419,23 +1442,10 @@ int gbfem_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_z
                 double *res_rel_out) {
   GB_CHECK(c && c->have_structure, "structure not set");
   GB_CHECK(krylov > 0 && krylov <= 256, "krylov must be in 1..256");
+  GB_CHECK(max_iter >= 0, "negative iteration limit");
   GB_CHECK(x != nullptr, "null solution vector");
   GB_CUDA(cudaSetDevice(c->device));
-  const int n = c->ndof;
-  cudaStream_t st = c->stream;
-  GB_TRY(c->dinv.alloc(n));
-  GB_TRY(gbfem::launch_jacobi_diag(st, n, c->row_ptr.p, c->col_ind.p, c->val.p, c->dinv.p));
-  c->last_solve_kernels = 1;
-  GmresOp op = [&](int mode, const double *in, double *out) -> int {
-    if (mode == 0) {
-      const int r = gbfem::launch_spmv(st, 0, n, c->row_ptr.p, c->col_ind.p, c->val.p, in, c->rhs.p, nullptr, out);
-      if (r < 0) return r;
-      const int r2 = gbfem::launch_mul(st, n, c->dinv.p, out);
-      return r2 < 0 ? r2 : r + r2;
-    }
-    return gbfem::launch_spmv(st, 1, n, c->row_ptr.p, c->col_ind.p, c->val.p, in, nullptr, c->dinv.p, out);
-  };
-  return gmres_run(c, n, krylov, max_iter, tol_rel, ini_zero, x, res_out, res_rel_out, op);
+  return gbfem::gmres_device_std(c, krylov, max_iter, tol_rel, ini_zero, x, res_out, res_rel_out);
 }
 
 // DG block matrix with block Jacobi (inverted diagonal blocks).
@@ -1550,14 +1560,15 @@ int gbfem_dg_solve_ir(gbfem_ctx c, int krylov, int max_iter, double tol_rel, dou
   };
   const auto t0 = std::chrono::steady_clock::now();
   int inner_total = 0, k = 0;
-  double rel = 1.0;
+  double rel = 1.0, dprev = 0.0;
+  bool converged_x = false;
   for (; k < 100; k++) {
-    // true residual in FP64
+    // true residual in FP64 (or with compensated sums)
     GB_TRY(dg_spmv(c, 2, c->ir_x.p, c->dg_rhs.p, c->ir_r.p));
     double rn = 0.0;
     GB_TRY(norm(c->ir_r.p, &rn));
     rel = bn > 0 ? rn / bn : 0.0;
-    if (rel <= tol_rel || inner_total >= max_iter) break;
+    if (rel <= tol_rel || inner_total >= max_iter || converged_x) break;
     // correction from the FP32 operator (x0 = 0, result in c->x)
     // each correction: at most 10 restart cycles (the FP32 operator's own
     // rounding floor stops progress long before a tight inner tolerance)
@@ -1566,6 +1577,18 @@ int gbfem_dg_solve_ir(gbfem_ctx c, int krylov, int max_iter, double tol_rel, dou
     GB_TRY(it);
     inner_total += it;
     GB_TRY(gbfem::launch_multiaxpy(st, n, 1, c->b.p, 1.0, c->x.p, n, c->ir_x.p));
+    if (c->dg_residual_dd) {
+      // with an accurate residual the solution converges to FP64 rounding
+      // while the FP64-rounded residual stalls at its floor, so the steps
+      // also stop on the corrections: once one is at the rounding level of
+      // x, or stops contracting (Demmel et al., extra-precise iterative
+      // refinement, ACM TOMS 32, 2006)
+      double dn = 0.0, xn = 0.0;
+      GB_TRY(norm(c->x.p, &dn));
+      GB_TRY(norm(c->ir_x.p, &xn));
+      if (dn <= 4.0 * 2.220446049250313e-16 * xn || (k >= 1 && dn > 0.5 * dprev)) converged_x = true;
+      dprev = dn;
+    }
   }
   GB_CUDA(cudaMemcpyAsync(x, c->ir_x.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
   GB_CUDA(cudaStreamSynchronize(st));

@@ -123,6 +123,83 @@ __global__ void __launch_bounds__(DGS_THREADS) dg_block_spmv_kernel(
   dg_block_row_spmv<P, VT>(mode, count, ent_el, roff, row_val, cx_off, colx, val, dinv_off, dinv, x, b, out, sv);
 }
 
+// Residual out = b - A x with the products and sums carried in two FP64
+// words per row (error-free transformations: the exact product error from an
+// FMA, Knuth's TwoSum, the errors summed in a second word and added once at
+// the end: the compensated dot product "Dot2" of Ogita, Rump and Oishi,
+// SIAM J. Sci. Comput. 26, 2005).  The result is as accurate as if computed
+// in twice the working precision, then rounded: iterative refinement driven
+// by it reaches a forward error near FP64 rounding whatever the FP64 residual
+// floor of a badly scaled system.  Same lane layout as dg_block_row_spmv.
+template <int P>
+__global__ void __launch_bounds__(DGS_THREADS) dg_block_residual_dd_kernel(
+    int count, const int *__restrict__ ent_el, const int *__restrict__ roff, const long long *__restrict__ row_val,
+    const long long *__restrict__ cx_off, const int *__restrict__ colx, const double *__restrict__ val,
+    const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ out) {
+  constexpr int NS = DgSpmvDims<P>::NS;
+  constexpr int S = (NS + DGS_LANES - 1) / DGS_LANES;
+  const int grp = threadIdx.x / DGS_LANES, g = threadIdx.x % DGS_LANES;
+  const int idx = blockIdx.x * DGS_ROWS + grp;
+  if (idx >= count) return;
+  const int e = ent_el[idx];
+  const int r0 = roff[e];
+  double hi[S], lo[S];
+#pragma unroll
+  for (int s = 0; s < S; s++) {
+    const int i = g + DGS_LANES * s;
+    hi[s] = b && i < NS ? b[r0 + i] : 0.0;
+    lo[s] = 0.0;
+  }
+  const double *A = val + row_val[e] + g;
+  const int *cx = colx + cx_off[e];
+  const int nct = (int)(cx_off[e + 1] - cx_off[e]);
+  for (int t = 0; t < nct; t++) {
+    const double xv = -x[cx[t]];
+    const double *col = A + (size_t)t * NS;
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+      if (g + DGS_LANES * s >= NS) continue;
+      const double a = col[DGS_LANES * s];
+      const double p = a * xv;
+      const double ep = fma(a, xv, -p);  // exact: a xv = p + ep
+      const double sum = hi[s] + p;      // TwoSum(hi, p)
+      const double bb = sum - hi[s];
+      const double es = (hi[s] - (sum - bb)) + (p - bb);
+      hi[s] = sum;
+      lo[s] += ep + es;
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < S; s++) {
+    const int i = g + DGS_LANES * s;
+    if (i < NS) out[r0 + i] = hi[s] + lo[s];
+  }
+}
+
+int launch_dg_block_residual_dd(cudaStream_t st, int p, int count, const int *ent_el, const int *roff,
+                                const long long *row_val, const long long *cx_off, const int *colx,
+                                const double *val, const double *x, const double *b, double *out) {
+  if (count <= 0) return 0;
+  GB_CHECK(p >= 1 && p <= 2 * GB_DG_PMAX, "DG block class must be 1..8 (prisms 1..4, tetrahedra 5..8)");
+  const int grid = (count + DGS_ROWS - 1) / DGS_ROWS;
+#define GB_DGR_LAUNCH(PP)                                                                               \
+  dg_block_residual_dd_kernel<PP><<<grid, DGS_THREADS, 0, st>>>(count, ent_el, roff, row_val, cx_off, colx, \
+                                                                val, x, b, out)
+  switch (p) {
+    case 1: GB_DGR_LAUNCH(1); break;
+    case 2: GB_DGR_LAUNCH(2); break;
+    case 3: GB_DGR_LAUNCH(3); break;
+    case 4: GB_DGR_LAUNCH(4); break;
+    case 5: GB_DGR_LAUNCH(5); break;
+    case 6: GB_DGR_LAUNCH(6); break;
+    case 7: GB_DGR_LAUNCH(7); break;
+    default: GB_DGR_LAUNCH(8); break;
+  }
+#undef GB_DGR_LAUNCH
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
 __global__ void to_float_kernel(long long n, const double *__restrict__ a, float *__restrict__ b) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     b[i] = (float)a[i];

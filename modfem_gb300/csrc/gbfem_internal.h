@@ -30,6 +30,13 @@ void set_error(const std::string &msg);
     }                                                                                        \
   } while (0)
 
+// propagates a negative status
+#define GB_TRY(x)            \
+  do {                       \
+    int r_ = (x);            \
+    if (r_ < 0) return r_;   \
+  } while (0)
+
 // Device buffer with explicit size tracking (no torch, no allocator layers).
 template <typename T>
 struct DevBuf {
@@ -118,6 +125,10 @@ int launch_multiaxpy(cudaStream_t st, int n, int m, const double *c, double sign
 int launch_scale(cudaStream_t st, int n, const double *alpha, int invert, const double *x, double *y);
 int launch_mul(cudaStream_t st, int n, const double *a, double *y);
 int measure_fp64_peak(cudaStream_t st, int device, double *tflops);
+// restarted GMRES with point Jacobi on the context's CRS matrix, all of it on
+// the device (gmres_dev.cu); returns the iteration count
+int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_zero, double *x,
+                     double *res_out, double *res_rel_out);
 // One (element, face) incidence of the DG face assembly, built on the host:
 // the face's two neighbours (el2 = -1 on a Dirichlet boundary face), the side
 // of el1 the face lies on, its vertex count, the local vertex index in el1 /
@@ -166,6 +177,10 @@ int launch_dg_block_spmv32(cudaStream_t st, int mode, int p, int count, const in
                            const long long *row_val, const long long *cx_off, const int *colx, const float *val,
                            const long long *dinv_off, const float *dinv, const double *x, const double *b,
                            double *out);
+// out = b - A x (b may be NULL) with compensated (two-word) sums
+int launch_dg_block_residual_dd(cudaStream_t st, int p, int count, const int *ent_el, const int *roff,
+                                const long long *row_val, const long long *cx_off, const int *colx,
+                                const double *val, const double *x, const double *b, double *out);
 int launch_to_float(cudaStream_t st, long long n, const double *a, float *b);
 // double -> double word (h, l float pairs, 8 bytes each) and the block SpMV
 // on double-word copies of the matrix and of the inverted diagonal blocks
@@ -237,6 +252,18 @@ struct gbfem_ctx_s {
   std::vector<int> pipe_el, pipe_rows;
   // Krylov workspace
   gbfem::DevBuf<double> V, w, tmp, x, b, partial, hcol;
+  // device-resident std GMRES (gmres_dev.cu): sliced-ELL copy of the CRS
+  // matrix, small arrays and state, the captured restart cycle
+  gbfem::DevBuf<int> sell_off, sell_col;
+  gbfem::DevBuf<double> sell_val, gm_small;
+  gbfem::DevBuf<float2> sell_valdw;
+  bool sell_ready = false, std_spmv_dword = false;
+  int sell_n = 0;
+  long long sell_nnz = 0, sell_total = 0;
+  cudaGraphExec_t gm_graph = nullptr;
+  int gm_key_n = 0, gm_key_m = 0, gm_kernels = 0;
+  bool gm_key_dw = false;
+  unsigned char gm_key_args[256] = {};
   // DG prisms: per-element degree, block-CRS structure (block row = element)
   std::vector<int> dg_p, dg_roff, dg_bptr, dg_bcol;
   std::vector<long long> dg_boff;
@@ -261,6 +288,7 @@ struct gbfem_ctx_s {
   gbfem::DevBuf<float> dg_val32, dg_dinv32;  // FP32 copies for iterative refinement
   gbfem::DevBuf<float2> dg_valdw, dg_dinvdw;  // double-word copies for the GMRES operator
   bool dg_spmv_dword = false;
+  bool dg_residual_dd = false;  // true residuals (IR, gbfem_dg_compute_residual) with compensated sums
   gbfem::DevBuf<double> ir_x, ir_r;
   gbfem::DevBuf<long long> dg_dinv_off_d;
   gbfem::DevBuf<int> dg_bptr_d, dg_bcol_d, dg_colx_d;

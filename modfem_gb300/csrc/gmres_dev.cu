@@ -1,0 +1,592 @@
+// Device-resident restarted GMRES(m) with point Jacobi for the std CRS
+// matrix (gbfem_solve).  Same algorithm, stopping rule and iteration count as
+// lsr_mkb_core_gmres (lsd_mkb/lsd_mkb_core/lss_mkb_core.c:2317-2660): left
+// preconditioning by 1 / a_ii (lar_fill_preconditioner_crs,
+// lad_crs/las_crs_intf.c:707), classical Gram-Schmidt, Givens rotations,
+// stopping on the preconditioned residual relative to the initial one with
+// both tolerances floored at 1e-12 (lss_mkb_core.c:2377-2378).
+//
+// Nothing of an Arnoldi step goes through the host: the Hessenberg column,
+// the rotations, the convergence test and the small triangular solve run in
+// one-block "logic" kernels on the device, and every kernel of a restart
+// cycle (restart residual, m Arnoldi steps, update of x) reads a state word
+// and returns at once when the cycle has already ended.  One cycle is
+// captured as a CUDA graph (per context, matrix size and Krylov dimension)
+// and replayed; the host reads the state once per cycle.
+//
+// The SpMV runs on a sliced-ELL copy of the CRS matrix (SELL-32 in natural
+// row order: slice s = rows 32 s .. 32 s + 31, padded to the slice's longest
+// row; ModFEM's prism matrices hold 6..21 entries per row, so padding adds
+// about 1 %): a warp reads 32 consecutive values and 32 consecutive column
+// indices per step (fully coalesced 256 B and 128 B lines) instead of the
+// short scattered row segments of the CRS kernel.  The values are either FP64
+// or double words (float pairs h + l, the same 8 bytes): with double words
+// the products run on the FP32 pipes and the kernel is bound by HBM alone
+// (GB300's FP64 pipe, ~0.6 T FMA/s, is itself near the HBM rate for one FMA
+// per 12 bytes).  Row sums run in column order in one thread, as the
+// reference's loop does.  Reductions are two-stage over a fixed block
+// partition and fixed tree order: the solve is bit-reproducible.
+
+#include <cstring>
+#include <vector>
+
+#include "dword.cuh"
+#include "gbfem_internal.h"
+
+namespace gbfem {
+
+constexpr int GM_T = 256;
+constexpr int SELL_C = 32;
+
+// ---------------------------------------------------------------- SELL-32
+__global__ void sell_width_kernel(int n, int nslices, const int *__restrict__ row_ptr, int *__restrict__ width) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslices) return;
+  int w = 0;
+  for (int l = 0; l < SELL_C; l++) {
+    const int r = s * SELL_C + l;
+    if (r < n) w = max(w, row_ptr[r + 1] - row_ptr[r]);
+  }
+  width[s] = w;
+}
+
+// columns of slice s: entry j of lane l at off[s] + 32 j + l; padding points
+// at the row itself (or column 0 past the last row) with value 0
+__global__ void sell_cols_kernel(int n, int nslices, const int *__restrict__ row_ptr, const int *__restrict__ col_ind,
+                                 const int *__restrict__ off, int *__restrict__ col) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = (int)(t / SELL_C), l = (int)(t % SELL_C);
+  if (s >= nslices) return;
+  const int r = s * SELL_C + l;
+  const int w = (off[s + 1] - off[s]) / SELL_C;
+  const int lo = r < n ? row_ptr[r] : 0, len = r < n ? row_ptr[r + 1] - lo : 0;
+  for (int j = 0; j < w; j++) col[off[s] + SELL_C * j + l] = j < len ? col_ind[lo + j] : (r < n ? r : 0);
+}
+
+template <typename VT>
+__device__ __forceinline__ VT sell_value(double v);
+template <>
+__device__ __forceinline__ double sell_value<double>(double v) {
+  return v;
+}
+template <>
+__device__ __forceinline__ float2 sell_value<float2>(double v) {
+  return dw_f2(v);
+}
+
+template <typename VT>
+__global__ void sell_vals_kernel(int n, int nslices, const int *__restrict__ row_ptr, const double *__restrict__ val,
+                                 const int *__restrict__ off, VT *__restrict__ sv) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = (int)(t / SELL_C), l = (int)(t % SELL_C);
+  if (s >= nslices) return;
+  const int r = s * SELL_C + l;
+  const int w = (off[s + 1] - off[s]) / SELL_C;
+  const int lo = r < n ? row_ptr[r] : 0, len = r < n ? row_ptr[r + 1] - lo : 0;
+  for (int j = 0; j < w; j++) sv[off[s] + SELL_C * j + l] = sell_value<VT>(j < len ? val[lo + j] : 0.0);
+}
+
+// one row per thread, a warp per slice: acc = sum_j val * x[col]
+__device__ __forceinline__ double sell_row(const double *__restrict__ v, const int *__restrict__ col, int w,
+                                           const double *__restrict__ x) {
+  double acc = 0.0;
+  int j = 0;
+  for (; j + 4 <= w; j += 4) {
+    const double a0 = __ldg(v), a1 = __ldg(v + SELL_C), a2 = __ldg(v + 2 * SELL_C), a3 = __ldg(v + 3 * SELL_C);
+    const int c0 = __ldg(col), c1 = __ldg(col + SELL_C), c2 = __ldg(col + 2 * SELL_C), c3 = __ldg(col + 3 * SELL_C);
+    const double x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+    acc = fma(a0, x0, acc);
+    acc = fma(a1, x1, acc);
+    acc = fma(a2, x2, acc);
+    acc = fma(a3, x3, acc);
+    v += 4 * SELL_C;
+    col += 4 * SELL_C;
+  }
+  for (; j < w; j++) {
+    acc = fma(__ldg(v), __ldg(x + __ldg(col)), acc);
+    v += SELL_C;
+    col += SELL_C;
+  }
+  return acc;
+}
+
+__device__ __forceinline__ double sell_row(const float2 *__restrict__ v, const int *__restrict__ col, int w,
+                                           const double *__restrict__ x) {
+  dw acc(0.0f, 0.0f);
+  int j = 0;
+  for (; j + 4 <= w; j += 4) {
+    const float2 a0 = __ldg(v), a1 = __ldg(v + SELL_C), a2 = __ldg(v + 2 * SELL_C), a3 = __ldg(v + 3 * SELL_C);
+    const int c0 = __ldg(col), c1 = __ldg(col + SELL_C), c2 = __ldg(col + 2 * SELL_C), c3 = __ldg(col + 3 * SELL_C);
+    const double x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+    acc = t_fma(dw(a0.x, a0.y), dw_from_double(x0), acc);
+    acc = t_fma(dw(a1.x, a1.y), dw_from_double(x1), acc);
+    acc = t_fma(dw(a2.x, a2.y), dw_from_double(x2), acc);
+    acc = t_fma(dw(a3.x, a3.y), dw_from_double(x3), acc);
+    v += 4 * SELL_C;
+    col += 4 * SELL_C;
+  }
+  for (; j < w; j++) {
+    const float2 a = __ldg(v);
+    acc = t_fma(dw(a.x, a.y), dw_from_double(__ldg(x + __ldg(col))), acc);
+    v += SELL_C;
+    col += SELL_C;
+  }
+  return dw_to_double(acc);
+}
+
+// ---------------------------------------------------------------- state
+enum { GM_RESTART = 0, GM_ARNOLDI = 1, GM_DONE = 2 };
+
+struct GmState {
+  int phase, j, it, done_cols, final_flag, m, max_iter, pad;
+  double beta0, resid, beta, hn, tol_rel, tol_abs;
+};
+
+// device arrays of one solve
+struct GmArgs {
+  int n, nslices, nb;
+  const int *row_ptr, *col_ind, *sell_off, *sell_col;
+  const double *val, *sell_val64;
+  const float2 *sell_valdw;
+  const double *dinv, *b;
+  double *x, *V, *tmp, *H, *cs, *sn, *s, *y, *hcol, *partial;
+  GmState *st;
+};
+
+// sum of nb partials in a fixed order (one block of GM_T threads); valid in thread 0
+__device__ double gm_block_total(const double *partial, int nb) {
+  __shared__ double sh[GM_T];
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nb; b += GM_T) v += partial[b];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = GM_T / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  return sh[0];
+}
+
+__device__ __forceinline__ double gm_block_sum(double s) {
+  __shared__ double sh[GM_T / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  s = 0.0;
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < GM_T / 32 ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  }
+  return s;
+}
+
+// restart residual tmp = dinv (b - A x), FP64 (CRS rows, 4 lanes a row, or
+// the FP64 SELL copy)
+__global__ void __launch_bounds__(GM_T) gm_restart_residual(GmArgs a) {
+  const GmState &S = *a.st;
+  if (S.phase != GM_RESTART || S.final_flag) return;
+  if (a.sell_val64) {
+    const int s = blockIdx.x * (GM_T / 32) + threadIdx.x / 32, l = threadIdx.x & 31;
+    if (s >= a.nslices) return;
+    const int r = s * SELL_C + l;
+    const int o = a.sell_off[s], w = (a.sell_off[s + 1] - o) / SELL_C;
+    const double acc = sell_row(a.sell_val64 + o + l, a.sell_col + o + l, w, a.x);
+    if (r < a.n) a.tmp[r] = (a.b[r] - acc) * a.dinv[r];
+    return;
+  }
+  const int lane = threadIdx.x & 3;
+  const long long r = ((long long)blockIdx.x * GM_T + threadIdx.x) / 4;
+  const bool valid = r < a.n;
+  const int lo = valid ? a.row_ptr[r] : 0, hi = valid ? a.row_ptr[r + 1] : 0;
+  double s = 0.0;
+  for (int k = lo + lane; k < hi; k += 4) s = fma(__ldg(a.val + k), __ldg(a.x + __ldg(a.col_ind + k)), s);
+  s += __shfl_down_sync(0xffffffffu, s, 2, 4);
+  s += __shfl_down_sync(0xffffffffu, s, 1, 4);
+  if (valid && lane == 0) a.tmp[r] = (a.b[r] - s) * a.dinv[r];
+}
+
+// partial[b] = sum over block b's entries of v^2 (v = tmp, or V[j+1])
+template <int WHICH>
+__global__ void __launch_bounds__(GM_T) gm_norm_partial(GmArgs a, int j) {
+  const GmState &S = *a.st;
+  if (WHICH == 0 ? (S.phase != GM_RESTART || S.final_flag) : (S.phase != GM_ARNOLDI || S.j != j)) return;
+  const double *v = WHICH == 0 ? a.tmp : a.V + (size_t)(j + 1) * a.n;
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T)
+    s = fma(v[i], v[i], s);
+  s = gm_block_sum(s);
+  if (threadIdx.x == 0) a.partial[blockIdx.x] = s;
+}
+
+// the restart test (lss_mkb_core.c:2377-2400) and the start of a cycle
+__global__ void __launch_bounds__(GM_T) gm_logic_restart(GmArgs a) {
+  GmState &S = *a.st;
+  if (S.phase != GM_RESTART) return;
+  const double tot = gm_block_total(a.partial, a.nb);
+  if (threadIdx.x != 0) return;
+  S.done_cols = 0;
+  if (S.final_flag) {
+    S.phase = GM_DONE;
+    return;
+  }
+  const double rn = sqrt(tot);
+  if (S.beta0 < 0) S.beta0 = rn;
+  S.resid = rn;
+  if (rn < S.tol_abs || (S.beta0 > 0 && rn / S.beta0 < S.tol_rel) || S.it >= S.max_iter) {
+    S.phase = GM_DONE;
+    return;
+  }
+  a.s[0] = rn;
+  for (int i = 1; i <= S.m; i++) a.s[i] = 0.0;
+  S.beta = rn;
+  S.j = 0;
+  S.phase = GM_ARNOLDI;
+}
+
+__global__ void __launch_bounds__(GM_T) gm_start_cycle(GmArgs a) {
+  const GmState &S = *a.st;
+  if (S.phase != GM_ARNOLDI || S.j != 0) return;
+  const double inv = 1.0 / S.beta;
+  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T)
+    a.V[i] = a.tmp[i] * inv;
+}
+
+// V[j+1] = dinv A V[j]
+template <typename VT>
+__global__ void __launch_bounds__(GM_T) gm_arnoldi_spmv(GmArgs a, const VT *__restrict__ sv, int j) {
+  const GmState &S = *a.st;
+  if (S.phase != GM_ARNOLDI || S.j != j) return;
+  const int s = blockIdx.x * (GM_T / 32) + threadIdx.x / 32, l = threadIdx.x & 31;
+  if (s >= a.nslices) return;
+  const int r = s * SELL_C + l;
+  const int o = a.sell_off[s], w = (a.sell_off[s + 1] - o) / SELL_C;
+  const double acc = sell_row(sv + o + l, a.sell_col + o + l, w, a.V + (size_t)j * a.n);
+  if (r < a.n) a.V[(size_t)(j + 1) * a.n + r] = a.dinv[r] * acc;
+}
+
+// Gram-Schmidt dot products <V[k], V[j+1]>, k = blockIdx.y <= j
+__global__ void __launch_bounds__(GM_T) gm_dot_partial(GmArgs a, int j) {
+  const GmState &S = *a.st;
+  if (S.phase != GM_ARNOLDI || S.j != j) return;
+  const int k = blockIdx.y;
+  const double *v = a.V + (size_t)k * a.n, *w = a.V + (size_t)(j + 1) * a.n;
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T)
+    s = fma(__ldg(v + i), __ldg(w + i), s);
+  s = gm_block_sum(s);
+  if (threadIdx.x == 0) a.partial[(size_t)k * a.nb + blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(GM_T) gm_dot_sum(GmArgs a, int j) {
+  const GmState &S = *a.st;
+  if (S.phase != GM_ARNOLDI || S.j != j) return;
+  const double t = gm_block_total(a.partial + (size_t)blockIdx.x * a.nb, a.nb);
+  if (threadIdx.x == 0) a.hcol[blockIdx.x] = t;
+}
+
+// V[j+1] -= V[:, :j+1] hcol, and the block partials of its squared norm
+__global__ void __launch_bounds__(GM_T) gm_orthogonalize(GmArgs a, int j) {
+  const GmState &S = *a.st;
+  if (S.phase != GM_ARNOLDI || S.j != j) return;
+  double *w = a.V + (size_t)(j + 1) * a.n;
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T) {
+    double acc = 0.0;
+    for (int k = 0; k <= j; k++) acc = fma(a.hcol[k], __ldg(a.V + (size_t)k * a.n + i), acc);
+    const double wi = w[i] - acc;
+    w[i] = wi;
+    s = fma(wi, wi, s);
+  }
+  s = gm_block_sum(s);
+  if (threadIdx.x == 0) a.partial[(size_t)(j + 1) * a.nb + blockIdx.x] = s;
+}
+
+// Hessenberg column j, Givens rotations, residual estimate; at the end of a
+// cycle the triangular solve for y
+__global__ void __launch_bounds__(GM_T) gm_logic_arnoldi(GmArgs a, int j) {
+  GmState &S = *a.st;
+  if (S.phase != GM_ARNOLDI || S.j != j) return;
+  const double tot = gm_block_total(a.partial + (size_t)(j + 1) * a.nb, a.nb);
+  if (threadIdx.x != 0) return;
+  const int m = S.m, ld = m + 1;
+  const double hn = sqrt(tot);
+  double *H = a.H;
+  for (int k = 0; k <= j; k++) H[k + (size_t)j * ld] = a.hcol[k];
+  H[j + 1 + (size_t)j * ld] = hn;
+  for (int k = 0; k < j; k++) {
+    const double x0 = H[k + (size_t)j * ld], x1 = H[k + 1 + (size_t)j * ld];
+    H[k + (size_t)j * ld] = a.cs[k] * x0 + a.sn[k] * x1;
+    H[k + 1 + (size_t)j * ld] = a.cs[k] * x1 - a.sn[k] * x0;
+  }
+  {
+    const double x0 = H[j + (size_t)j * ld], x1 = H[j + 1 + (size_t)j * ld];
+    const double rr = hypot(x0, x1);
+    a.cs[j] = x0 / rr;
+    a.sn[j] = x1 / rr;
+    H[j + (size_t)j * ld] = rr;
+    H[j + 1 + (size_t)j * ld] = 0.0;
+    const double s0 = a.s[j];
+    a.s[j] = a.cs[j] * s0;
+    a.s[j + 1] = -a.sn[j] * s0;
+  }
+  S.it++;
+  S.resid = fabs(a.s[j + 1]);
+  S.hn = hn;
+  const bool conv = S.resid < S.tol_abs || S.resid / S.beta0 < S.tol_rel;
+  if (j == m - 1 || S.it >= S.max_iter || conv) {
+    const int done = j + 1;
+    for (int k = done - 1; k >= 0; k--) {
+      double v = a.s[k];
+      for (int i = k + 1; i < done; i++) v -= H[k + (size_t)i * ld] * a.y[i];
+      a.y[k] = v / H[k + (size_t)k * ld];
+    }
+    S.done_cols = done;
+    S.final_flag = (conv || S.it >= S.max_iter) ? 1 : 0;
+    S.phase = GM_RESTART;
+  } else {
+    S.j = j + 1;
+  }
+}
+
+__global__ void __launch_bounds__(GM_T) gm_normalize(GmArgs a, int j) {
+  const GmState &S = *a.st;
+  if (S.phase != GM_ARNOLDI || S.j != j + 1) return;
+  double *w = a.V + (size_t)(j + 1) * a.n;
+  const double inv = 1.0 / S.hn;
+  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T)
+    w[i] *= inv;
+}
+
+// x += V[:, :done] y at the end of a cycle
+__global__ void __launch_bounds__(GM_T) gm_update_x(GmArgs a) {
+  const GmState &S = *a.st;
+  if (S.phase != GM_RESTART || S.done_cols == 0) return;
+  const int done = S.done_cols;
+  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T) {
+    double acc = 0.0;
+    for (int k = 0; k < done; k++) acc = fma(a.y[k], __ldg(a.V + (size_t)k * a.n + i), acc);
+    a.x[i] += acc;
+  }
+}
+
+}  // namespace gbfem
+
+using gbfem::DevBuf;
+using gbfem::GmArgs;
+using gbfem::GmState;
+
+namespace {
+
+unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// SELL-32 index arrays of the context's structure (once per structure)
+int build_sell(gbfem_ctx c) {
+  const int n = c->ndof, ns = (n + gbfem::SELL_C - 1) / gbfem::SELL_C;
+  if (c->sell_ready && c->sell_n == n && c->sell_nnz == c->nnz) return 0;
+  GB_TRY(c->sell_off.alloc((size_t)ns + 1));
+  gbfem::sell_width_kernel<<<nblk(ns, 256), 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->sell_off.p);
+  GB_CUDA(cudaGetLastError());
+  std::vector<int> w(ns), off(ns + 1);
+  GB_CUDA(cudaMemcpyAsync(w.data(), c->sell_off.p, (size_t)ns * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  long long tot = 0;
+  for (int s = 0; s < ns; s++) {
+    off[s] = (int)tot;
+    tot += (long long)gbfem::SELL_C * w[s];
+  }
+  GB_CHECK(tot < 2147483647LL, "matrix too large for the sliced-ELL copy");
+  off[ns] = (int)tot;
+  GB_CUDA(cudaMemcpyAsync(c->sell_off.p, off.data(), (size_t)(ns + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                          c->stream));
+  GB_TRY(c->sell_col.alloc((size_t)std::max<long long>(tot, 1)));
+  gbfem::sell_cols_kernel<<<nblk((long long)ns * gbfem::SELL_C, 256), 256, 0, c->stream>>>(
+      n, ns, c->row_ptr.p, c->col_ind.p, c->sell_off.p, c->sell_col.p);
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(c->stream));  // off[] is a stack vector
+  c->sell_total = tot;
+  c->sell_n = n;
+  c->sell_nnz = c->nnz;
+  c->sell_ready = true;
+  return 0;
+}
+
+// the values of the current matrix into the SELL copy (every solve)
+int fill_sell_values(gbfem_ctx c) {
+  const int n = c->ndof, ns = (n + gbfem::SELL_C - 1) / gbfem::SELL_C;
+  const unsigned g = nblk((long long)ns * gbfem::SELL_C, 256);
+  if (c->std_spmv_dword) {
+    GB_TRY(c->sell_valdw.alloc((size_t)std::max<long long>(c->sell_total, 1)));
+    gbfem::sell_vals_kernel<float2><<<g, 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->val.p, c->sell_off.p,
+                                                               c->sell_valdw.p);
+  } else {
+    GB_TRY(c->sell_val.alloc((size_t)std::max<long long>(c->sell_total, 1)));
+    gbfem::sell_vals_kernel<double><<<g, 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->val.p, c->sell_off.p,
+                                                               c->sell_val.p);
+  }
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// Captures one restart cycle: restart residual and test, m Arnoldi steps,
+// update of x.  Events around the first step's SpMV time it in every replay.
+int capture_cycle(gbfem_ctx c, const GmArgs &a, int m, bool dword, int *kernels) {
+  cudaStream_t st = c->stream;
+  const int ns = a.nslices;
+  const unsigned gs = nblk(ns, gbfem::GM_T / 32);
+  const unsigned gcrs = nblk((long long)a.n * 4, gbfem::GM_T);
+  const unsigned gv = (unsigned)a.nb;
+  int k = 0;
+  cudaGraph_t graph = nullptr;
+  GB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  gbfem::gm_restart_residual<<<a.sell_val64 ? gs : gcrs, gbfem::GM_T, 0, st>>>(a);
+  gbfem::gm_norm_partial<0><<<gv, gbfem::GM_T, 0, st>>>(a, 0);
+  gbfem::gm_logic_restart<<<1, gbfem::GM_T, 0, st>>>(a);
+  gbfem::gm_start_cycle<<<gv, gbfem::GM_T, 0, st>>>(a);
+  k += 4;
+  for (int j = 0; j < m; j++) {
+    if (j == 0) cudaEventRecordWithFlags(c->ev2, st, cudaEventRecordExternal);
+    if (dword)
+      gbfem::gm_arnoldi_spmv<float2><<<gs, gbfem::GM_T, 0, st>>>(a, a.sell_valdw, j);
+    else
+      gbfem::gm_arnoldi_spmv<double><<<gs, gbfem::GM_T, 0, st>>>(a, a.sell_val64, j);
+    if (j == 0) cudaEventRecordWithFlags(c->ev3, st, cudaEventRecordExternal);
+    gbfem::gm_dot_partial<<<dim3(gv, j + 1), gbfem::GM_T, 0, st>>>(a, j);
+    gbfem::gm_dot_sum<<<j + 1, gbfem::GM_T, 0, st>>>(a, j);
+    gbfem::gm_orthogonalize<<<gv, gbfem::GM_T, 0, st>>>(a, j);
+    gbfem::gm_logic_arnoldi<<<1, gbfem::GM_T, 0, st>>>(a, j);
+    gbfem::gm_normalize<<<gv, gbfem::GM_T, 0, st>>>(a, j);
+    k += 6;
+  }
+  gbfem::gm_update_x<<<gv, gbfem::GM_T, 0, st>>>(a);
+  k += 1;
+  const cudaError_t e1 = cudaGetLastError();
+  const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+  GB_CUDA(e1);
+  GB_CUDA(e2);
+  if (c->gm_graph) cudaGraphExecDestroy(c->gm_graph);
+  c->gm_graph = nullptr;
+  const cudaError_t e3 = cudaGraphInstantiate(&c->gm_graph, graph, 0);
+  cudaGraphDestroy(graph);
+  GB_CUDA(e3);
+  *kernels = k;
+  return 0;
+}
+
+}  // namespace
+
+namespace gbfem {
+
+// gbfem_solve's body: see the file comment.
+int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int ini_zero, double *x,
+                     double *res_out, double *res_rel_out) {
+  const int n = c->ndof, m = krylov;
+  cudaStream_t st = c->stream;
+  GB_TRY(build_sell(c));
+  GB_TRY(fill_sell_values(c));
+  GB_TRY(c->dinv.alloc(n));
+  GB_TRY(launch_jacobi_diag(st, n, c->row_ptr.p, c->col_ind.p, c->val.p, c->dinv.p));
+  const int nb = reduction_blocks(n);
+  GB_TRY(c->V.alloc((size_t)n * (m + 1)));
+  GB_TRY(c->x.alloc(n));
+  GB_TRY(c->tmp.alloc(n));
+  GB_TRY(c->partial.alloc((size_t)nb * (m + 2)));
+  // H (m+1)^2, cs, sn, s (m+1 each), y (m), hcol (m+1), state
+  const size_t nsmall = (size_t)(m + 1) * (m + 1) + 3 * (size_t)(m + 1) + m + (m + 1) + 16;
+  GB_TRY(c->gm_small.alloc(nsmall));
+  double *H = c->gm_small.p, *cs = H + (size_t)(m + 1) * (m + 1), *sn = cs + (m + 1), *s = sn + (m + 1),
+         *y = s + (m + 1), *hcol = y + m;
+  GmState *state = reinterpret_cast<GmState *>(hcol + (m + 1));
+  GmArgs a;
+  memset(&a, 0, sizeof(a));  // padding too: the struct is compared bytewise below
+  a.n = n;
+  a.nslices = (n + SELL_C - 1) / SELL_C;
+  a.nb = nb;
+  a.row_ptr = c->row_ptr.p;
+  a.col_ind = c->col_ind.p;
+  a.sell_off = c->sell_off.p;
+  a.sell_col = c->sell_col.p;
+  a.val = c->val.p;
+  a.sell_val64 = c->std_spmv_dword ? nullptr : c->sell_val.p;
+  a.sell_valdw = c->std_spmv_dword ? c->sell_valdw.p : nullptr;
+  a.dinv = c->dinv.p;
+  a.b = c->rhs.p;
+  a.x = c->x.p;
+  a.V = c->V.p;
+  a.tmp = c->tmp.p;
+  a.H = H;
+  a.cs = cs;
+  a.sn = sn;
+  a.s = s;
+  a.y = y;
+  a.hcol = hcol;
+  a.partial = c->partial.p;
+  a.st = state;
+  if (ini_zero)
+    GB_CUDA(cudaMemsetAsync(c->x.p, 0, (size_t)n * sizeof(double), st));
+  else
+    GB_CUDA(cudaMemcpyAsync(c->x.p, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
+  GmState h{};
+  h.phase = GM_RESTART;
+  h.m = m;
+  h.max_iter = max_iter;
+  h.beta0 = -1.0;
+  h.tol_abs = 1e-12;
+  h.tol_rel = tol_rel < 1e-12 ? 1e-12 : tol_rel;
+  GB_CUDA(cudaMemcpyAsync(state, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  // the graph bakes in every pointer and size: capture again when one changed
+  static_assert(sizeof(GmArgs) <= sizeof(c->gm_key_args), "graph key too small");
+  const bool same = c->gm_graph && c->gm_key_n == n && c->gm_key_m == m && c->gm_key_dw == c->std_spmv_dword &&
+                    memcmp(c->gm_key_args, &a, sizeof(a)) == 0;
+  int kernels_per_cycle = c->gm_kernels;
+  if (!same) {
+    GB_TRY(capture_cycle(c, a, m, c->std_spmv_dword, &kernels_per_cycle));
+    c->gm_key_n = n;
+    c->gm_key_m = m;
+    c->gm_key_dw = c->std_spmv_dword;
+    memcpy(c->gm_key_args, &a, sizeof(a));
+    c->gm_kernels = kernels_per_cycle;
+  }
+  GmState *hs = nullptr;
+  GB_CUDA(cudaMallocHost(&hs, sizeof(GmState)));
+  float spmv_ms = 0.f;
+  int spmv_n = 0, cycles = 0, it_prev = 0;
+  cudaEventRecord(c->ev0, st);
+  int rc = 0;
+  for (;;) {
+    if (cudaGraphLaunch(c->gm_graph, st) != cudaSuccess ||
+        cudaMemcpyAsync(hs, state, sizeof(GmState), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      set_error("GMRES cycle launch failed");
+      rc = -1;
+      break;
+    }
+    cycles++;
+    if (hs->it > it_prev) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, c->ev2, c->ev3) == cudaSuccess) {
+        spmv_ms += ms;
+        spmv_n++;
+      }
+    }
+    it_prev = hs->it;
+    if (hs->phase == GM_DONE || hs->final_flag) break;
+  }
+  cudaEventRecord(c->ev1, st);
+  const GmState fin = *hs;
+  cudaFreeHost(hs);
+  GB_TRY(rc);
+  GB_CUDA(cudaMemcpyAsync(x, c->x.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  cudaEventElapsedTime(&c->last_solve_ms, c->ev0, c->ev1);
+  // one SpMV per iteration: the timed samples stand for all of them
+  c->last_spmv_ms = spmv_n ? spmv_ms / spmv_n * fin.it : 0.f;
+  c->last_spmv_count = fin.it;
+  c->last_solve_kernels = 4 + cycles * kernels_per_cycle;
+  if (res_out) *res_out = fin.resid;
+  if (res_rel_out) *res_rel_out = fin.beta0 > 0 ? fin.resid / fin.beta0 : 0.0;
+  return fin.it;
+}
+
+}  // namespace gbfem

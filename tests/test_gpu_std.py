@@ -133,19 +133,30 @@ def _guarded(n):
     return buf, buf[:n]
 
 
-def _dropin_args(g, bufs=None):
-    """The reference's drop-in inputs of fixture g as int32 arrays; with
-    bufs (a dict of larger int32 arrays) written into their prefixes, so that
-    successive calls pass the same host pointers."""
-    names = ("int_ent_type", "int_ent_id", "color_elems", "color_faces", "asse_pos", "assembly_table")
-    out = []
-    for k in names:
-        a = np.ascontiguousarray(g[k], dtype=np.int32)
-        if bufs is not None:
-            bufs[k][:a.size] = a
-            a = bufs[k][:a.size]
-        out.append(a)
-    return out
+def _own_dropin_problem(gb, n, seed):
+    """A jittered n^3 x 2 prism mesh with the library's own structure and
+    element tables laid out as the drop-in's entity lists (elements, then
+    the boundary faces with their element's table), and the oracle's
+    assembled values."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(n, jitter=0.2, seed=seed)
+    k = lognormal_k(m.nel, seed=seed)
+    c = make_ctx(gb, m, k)
+    c.build_structure()
+    tables = c.get_element_tables()
+    dn, rp, ci = c.get_crs_structure()
+    c.close()
+    nf = m.bc_face_id.size
+    lists = {"int_ent_type": np.concatenate([np.full(m.nel, gb.ELEMENT), np.full(nf, gb.FACE)]),
+             "int_ent_id": np.concatenate([np.arange(1, m.nel + 1), m.bc_face_id]),
+             "color_elems": np.array([0, m.nel]), "color_faces": np.array([m.nel, m.nel + nf]),
+             "asse_pos": np.arange(m.nel + nf) * 42,
+             "assembly_table": np.concatenate([tables, tables.reshape(m.nel, 42)[m.bc_face_el].reshape(-1)])}
+    vo, ro, _ = O.std_prism_assemble(m, k, dn, rp, ci)
+    return m, k, (dn, rp, ci), lists, vo, ro
+
+
+LIST_NAMES = ("int_ent_type", "int_ent_id", "color_elems", "color_faces", "asse_pos", "assembly_table")
 
 
 @pytest.mark.parametrize("cache", [0, 1])
@@ -155,25 +166,29 @@ def test_smaller_structure_in_a_live_context(gb, cache):
     sized by the current structure (guard entries past the end stay as they
     were), and the drop-in, gbfem_get_matrix and gbfem_set_matrix give the
     small problem's values.  With the table cache on, the small problem's
-    tables sit at the same host addresses as the large one's."""
-    big, small = load("std_n10"), load("std_n4")
-    bufs = {k: np.zeros(np.asarray(big[k]).size + 64, np.int32) for k in
-            ("int_ent_type", "int_ent_id", "color_elems", "color_faces", "asse_pos", "assembly_table")}
+    lists and tables sit at the same host addresses as the large one's."""
+    big, small = _own_dropin_problem(gb, 12, 21), _own_dropin_problem(gb, 5, 22)
+    bufs = {k: np.zeros(big[3][k].size + 64, np.int32) for k in LIST_NAMES}
     c = gb.Context(0)
     c.set_option(gb.OPT_CACHE_TABLES, cache)
-    for g in (big, small):
-        m = FixtureMesh(g)
+    for m, k, st, lists, vo, ro in (big, small):
         c.set_mesh(m)
-        c.set_coefficients(k=g["k"], f=1.0, g=0.0, penalty=1e7)
-        c.set_crs_structure(g["dof_of_node"], g["row_ptr"], g["col_ind"])
-        nnz, nd = g["col_ind"].size, g["row_ptr"].size - 1
+        c.set_coefficients(k=k, f=1.0, g=0.0, penalty=1e7)
+        c.set_crs_structure(*st)
+        rp, ci = st[1], st[2]
+        nnz, nd = ci.size, rp.size - 1
+        args = []
+        for name in LIST_NAMES:
+            a = lists[name].astype(np.int32)
+            bufs[name][:a.size] = a
+            args.append(bufs[name][:a.size])
         vb, val = _guarded(nnz)
         rb, rhs = _guarded(nd)
-        c.create_assemble_stiff_mat(*_dropin_args(g, bufs), crs_val=val, rhs=rhs)
+        c.create_assemble_stiff_mat(*args, crs_val=val, rhs=rhs)
         assert np.all(vb[nnz:] == 7.25) and np.all(rb[nd:] == 7.25)
-        sc = energy_scale(g["row_ptr"], g["col_ind"], g["crs_val"])
-        assert crs_rel_err(g["row_ptr"], val, g["crs_val"], sc) < REL_TOL
-        assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL
+        sc = energy_scale(rp, ci, vo)
+        assert crs_rel_err(rp, val, vo, sc) < REL_TOL
+        assert vec_rel_err(rhs, ro) < REL_TOL
         # download into exactly-sized views of guarded buffers
         vb2, val2 = _guarded(nnz)
         rb2, rhs2 = _guarded(nd)
@@ -539,6 +554,34 @@ def test_full_size_properties():
     rows_sum = np.add.reduceat(vs, rp[:-1])
     assert np.max(np.abs(rows_sum)) < 1e-12 * np.max(np.abs(vs))
     assert vec_rel_err(ra, ro) < REL_TOL
+    # the double-word element kernel (the benchmark's headline form) against
+    # the oracle at the same size and tolerance: stiffness alone, then with
+    # the penalty faces, through gbfem_assemble and through the drop-in with
+    # cached tables and the chunked download the benchmark times
+    c.set_option(gb.OPT_STD_ARITH, gb.STD_DWORD)
+    c.assemble(gb.SCATTER_ATOMIC)
+    vsd, _ = c.get_matrix()
+    assert crs_rel_err(rp, vsd, vso, energy_scale(rp, ci, vso)) < REL_TOL
+    assert np.max(np.abs(np.add.reduceat(vsd, rp[:-1]))) < 1e-12 * np.max(np.abs(vsd))
+    c.set_coefficients(k=k, f=1.0, g=0.0, penalty=1e7)
+    c.assemble(gb.SCATTER_ATOMIC)
+    vdw, rdw = c.get_matrix()
+    sco = energy_scale(rp, ci, vo)
+    assert crs_rel_err(rp, vdw, vo, sco) < REL_TOL
+    assert vec_rel_err(rdw, ro) < REL_TOL
+    tables = c.get_element_tables()
+    nf = m.bc_face_id.size
+    tab = np.concatenate([tables, tables.reshape(m.nel, 42)[m.bc_face_el].reshape(-1)]).astype(np.int32)
+    types = np.concatenate([np.full(m.nel, gb.ELEMENT), np.full(nf, gb.FACE)]).astype(np.int32)
+    ids = np.concatenate([np.arange(1, m.nel + 1), m.bc_face_id]).astype(np.int32)
+    pos = (np.arange(m.nel + nf) * 42).astype(np.int32)
+    c.set_option(gb.OPT_CACHE_TABLES, 1)
+    val, rhs = np.zeros(nnz), np.zeros(nd)
+    for _ in range(2):
+        c.create_assemble_stiff_mat(types, ids, np.array([0, m.nel], np.int32),
+                                    np.array([m.nel, m.nel + nf], np.int32), pos, tab, crs_val=val, rhs=rhs)
+        assert crs_rel_err(rp, val, vo, sco) < REL_TOL
+        assert vec_rel_err(rhs, ro) < REL_TOL
 
 
 # ------------------------------------------------------------- tetrahedra
