@@ -305,7 +305,8 @@ int gbfem_dg_solve(gbfem_ctx ctx, int krylov, int max_iter, double tol_rel, int 
  * stops when ||b - A x|| <= tol_rel ||b|| or max_iter inner iterations were
  * spent.  With GBFEM_OPT_DG_RESIDUAL = GBFEM_RESIDUAL_COMPENSATED the true
  * residual carries twice the working precision and the loop also stops once
- * a correction is below 4 ulp of ||x|| or no longer halves the previous one:
+ * a correction is below 4 ulp of ||x||, or is below 1e-10 ||x|| and no
+ * longer halves the previous one:
  * x is then accurate to about FP64 rounding (tol_rel below the FP64 residual
  * floor asks for exactly that).  Returns the inner iterations; *outer_steps
  * refinement steps, *rel_res the final relative true residual. */

@@ -232,7 +232,8 @@ class Context:
 
     # ---------------- hot path ----------------
     def create_assemble_stiff_mat(self, int_ent_type, int_ent_id, color_elems, color_faces, asse_pos,
-                                  assembly_table, comp_type=COMP_BOTH, crs_val=None, rhs=None, level_id=0):
+                                  assembly_table, comp_type=COMP_BOTH, crs_val=None, rhs=None, level_id=0,
+                                  max_dofs=None):
         """ModFEM pdr_create_assemble_stiff_mat through the C ABI (host arrays)."""
         t, i = _i32(int_ent_type), _i32(int_ent_id)
         ce, cf = _i32(color_elems), _i32(color_faces)
@@ -242,7 +243,7 @@ class Context:
         self._check(self.L.gbfem_create_assemble_stiff_mat(
             self._h, level_id, comp_type, ctypes.byref(pdeg), i.size, _p(t), _p(i),
             0 if ce is None else ce.size - 1, _p(ce), 0 if cf is None else cf.size - 1, _p(cf), _p(ap), _p(at),
-            self.nv, _p(crs_val), _p(rhs)))
+            self.nv if max_dofs is None else max_dofs, _p(crs_val), _p(rhs)))
 
     # ---------------- DG prisms ----------------
     def dg_set_degrees(self, p_el):

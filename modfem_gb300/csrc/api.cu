@@ -95,6 +95,7 @@ int gbfem_destroy(gbfem_ctx c) {
   if (c->gm_graph) cudaGraphExecDestroy(c->gm_graph);
   c->sell_off.release();
   c->sell_col.release();
+  c->sell_col16.release();
   c->sell_val.release();
   c->sell_valdw.release();
   c->gm_small.release();
@@ -310,7 +311,19 @@ int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long 
   c->hs.ndof = ndof;
   c->hs.row_ptr.assign(row_ptr, row_ptr + ndof + 1);
   c->hs.col_ind.assign(col_ind, col_ind + nnz);
-  if (dof_of_node) c->hs.dof_of_node.assign(dof_of_node, dof_of_node + c->nno);
+  if (dof_of_node) {
+    // a vertex of an element without a dof is a constrained (hanging) vertex
+    // (apr_get_ent_pdeg(...) == 0, apd_std_lin/aps_std_lin_intf.c:2998): its
+    // element's contributions would need the constraint rewrite of
+    // apr_get_stiff_mat_data (:2995-3170), which this library does not do
+    for (long long i = 0; i < (long long)c->nel * c->nv; i++) {
+      const int d = dof_of_node[c->h_el_nodes[i]];
+      GB_CHECK(d >= 0 && d < ndof,
+               "element " + std::to_string(i / c->nv) + " has a vertex without a dof (a constrained / hanging "
+               "vertex): the constraint rewrite of apr_get_stiff_mat_data is not supported");
+    }
+    c->hs.dof_of_node.assign(dof_of_node, dof_of_node + c->nno);
+  }
   GB_TRY(upload(c, c->row_ptr, row_ptr, (size_t)ndof + 1));
   GB_TRY(upload(c, c->col_ind, col_ind, (size_t)nnz));
   if (dof_of_node) GB_TRY(upload(c, c->dof_of_node, dof_of_node, (size_t)c->nno));
@@ -563,6 +576,10 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   GB_CHECK(Comp_type >= GBFEM_COMP_SM && Comp_type <= GBFEM_COMP_BOTH, "Comp_type must be SM, RHS or BOTH");
   GB_CHECK(Nr_int_ent >= 0 && L_int_ent_id && Asse_pos_first_dof_int_ent && Assembly_table,
            "missing entity lists or assembly table");
+  GB_CHECK(Max_dofs_int_ent <= c->nv,
+           "Max_dofs_int_ent exceeds the element vertex count: an entity's dof list holds the constraining "
+           "vertices of a constrained (hanging) vertex; the constraint rewrite of apr_get_stiff_mat_data "
+           "(apd_std_lin/aps_std_lin_intf.c:2995-3170) is not supported, refine conformingly");
   GB_CHECK(Max_dofs_int_ent == c->nv, "Max_dofs_int_ent must equal the element vertex count");
   GB_CUDA(cudaSetDevice(c->device));
   // element and face ranges in the entity lists
@@ -1581,12 +1598,15 @@ int gbfem_dg_solve_ir(gbfem_ctx c, int krylov, int max_iter, double tol_rel, dou
       // with an accurate residual the solution converges to FP64 rounding
       // while the FP64-rounded residual stalls at its floor, so the steps
       // also stop on the corrections: once one is at the rounding level of
-      // x, or stops contracting (Demmel et al., extra-precise iterative
-      // refinement, ACM TOMS 32, 2006)
+      // x, or, once the corrections are small (below 1e-10 of x: the inner
+      // solves have reached the operator's accuracy), when one stops
+      // contracting (Demmel et al., extra-precise iterative refinement,
+      // ACM TOMS 32, 2006)
       double dn = 0.0, xn = 0.0;
       GB_TRY(norm(c->x.p, &dn));
       GB_TRY(norm(c->ir_x.p, &xn));
-      if (dn <= 4.0 * 2.220446049250313e-16 * xn || (k >= 1 && dn > 0.5 * dprev)) converged_x = true;
+      if (dn <= 4.0 * 2.220446049250313e-16 * xn || (k >= 1 && dn > 0.5 * dprev && dn < 1e-10 * xn))
+        converged_x = true;
       dprev = dn;
     }
   }

@@ -257,7 +257,8 @@ struct gbfem_ctx_s {
   gbfem::DevBuf<int> sell_off, sell_col;
   gbfem::DevBuf<double> sell_val, gm_small;
   gbfem::DevBuf<float2> sell_valdw;
-  bool sell_ready = false, std_spmv_dword = false;
+  gbfem::DevBuf<short> sell_col16;  // columns relative to the row, where they fit in 16 bits
+  bool sell_ready = false, std_spmv_dword = false, sell_cols16 = false;
   int sell_n = 0;
   long long sell_nnz = 0, sell_total = 0;
   cudaGraphExec_t gm_graph = nullptr;

@@ -19,7 +19,8 @@
 // row; ModFEM's prism matrices hold 6..21 entries per row, so padding adds
 // about 1 %): a warp reads 32 consecutive values and 32 consecutive column
 // indices per step (fully coalesced 256 B and 128 B lines) instead of the
-// short scattered row segments of the CRS kernel.  The values are either FP64
+// short scattered row segments of the CRS kernel; column indices take 16
+// bits where they fit (see sell_base).  The values are either FP64
 // or double words (float pairs h + l, the same 8 bytes): with double words
 // the products run on the FP32 pipes and the kernel is bound by HBM alone
 // (GB300's FP64 pipe, ~0.6 T FMA/s, is itself near the HBM rate for one FMA
@@ -28,6 +29,7 @@
 // partition and fixed tree order: the solve is bit-reproducible.
 
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "dword.cuh"
@@ -39,29 +41,51 @@ constexpr int GM_T = 256;
 constexpr int SELL_C = 32;
 
 // ---------------------------------------------------------------- SELL-32
-__global__ void sell_width_kernel(int n, int nslices, const int *__restrict__ row_ptr, int *__restrict__ width) {
+// Column indices are stored relative to the lane's base row min(r, n - 1) in
+// 16 bits when every |column - base| of the matrix fits (ModFEM's first-
+// appearance dof order keeps a prism row's columns within about one mesh
+// layer of the row: 10 bytes a value instead of 12), as absolute 32-bit
+// indices otherwise.
+__device__ __forceinline__ int sell_base(int r, int n) { return r < n ? r : n - 1; }
+
+// width[s]: the slice's longest row; fits[s]: every column within 16 bits of its base
+__global__ void sell_width_kernel(int n, int nslices, const int *__restrict__ row_ptr, const int *__restrict__ col_ind,
+                                  int *__restrict__ width, int *__restrict__ fits) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nslices) return;
-  int w = 0;
+  int w = 0, ok = 1;
   for (int l = 0; l < SELL_C; l++) {
     const int r = s * SELL_C + l;
-    if (r < n) w = max(w, row_ptr[r + 1] - row_ptr[r]);
+    if (r >= n) continue;
+    w = max(w, row_ptr[r + 1] - row_ptr[r]);
+    for (int k = row_ptr[r]; k < row_ptr[r + 1]; k++) {
+      const int d = col_ind[k] - r;
+      ok &= d >= -32768 && d <= 32767;
+    }
   }
   width[s] = w;
+  fits[s] = ok;
 }
 
-// columns of slice s: entry j of lane l at off[s] + 32 j + l; padding points
-// at the row itself (or column 0 past the last row) with value 0
+// columns of slice s: entry j of lane l at off[s] + 32 j + l; padding entries
+// point at the lane's base row with value 0
+template <typename CT>
 __global__ void sell_cols_kernel(int n, int nslices, const int *__restrict__ row_ptr, const int *__restrict__ col_ind,
-                                 const int *__restrict__ off, int *__restrict__ col) {
+                                 const int *__restrict__ off, CT *__restrict__ col) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int s = (int)(t / SELL_C), l = (int)(t % SELL_C);
   if (s >= nslices) return;
-  const int r = s * SELL_C + l;
+  const int r = s * SELL_C + l, base = sell_base(r, n);
   const int w = (off[s + 1] - off[s]) / SELL_C;
   const int lo = r < n ? row_ptr[r] : 0, len = r < n ? row_ptr[r + 1] - lo : 0;
-  for (int j = 0; j < w; j++) col[off[s] + SELL_C * j + l] = j < len ? col_ind[lo + j] : (r < n ? r : 0);
+  for (int j = 0; j < w; j++) {
+    const int c = j < len ? col_ind[lo + j] : base;
+    col[off[s] + SELL_C * j + l] = sizeof(CT) == 2 ? (CT)(c - base) : (CT)c;
+  }
 }
+
+__device__ __forceinline__ int sell_col(const int *p, int) { return __ldg(p); }
+__device__ __forceinline__ int sell_col(const short *p, int base) { return base + (int)__ldg(p); }
 
 template <typename VT>
 __device__ __forceinline__ VT sell_value(double v);
@@ -86,52 +110,37 @@ __global__ void sell_vals_kernel(int n, int nslices, const int *__restrict__ row
   for (int j = 0; j < w; j++) sv[off[s] + SELL_C * j + l] = sell_value<VT>(j < len ? val[lo + j] : 0.0);
 }
 
-// one row per thread, a warp per slice: acc = sum_j val * x[col]
-__device__ __forceinline__ double sell_row(const double *__restrict__ v, const int *__restrict__ col, int w,
-                                           const double *__restrict__ x) {
-  double acc = 0.0;
-  int j = 0;
-  for (; j + 4 <= w; j += 4) {
-    const double a0 = __ldg(v), a1 = __ldg(v + SELL_C), a2 = __ldg(v + 2 * SELL_C), a3 = __ldg(v + 3 * SELL_C);
-    const int c0 = __ldg(col), c1 = __ldg(col + SELL_C), c2 = __ldg(col + 2 * SELL_C), c3 = __ldg(col + 3 * SELL_C);
-    const double x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-    acc = fma(a0, x0, acc);
-    acc = fma(a1, x1, acc);
-    acc = fma(a2, x2, acc);
-    acc = fma(a3, x3, acc);
-    v += 4 * SELL_C;
-    col += 4 * SELL_C;
-  }
-  for (; j < w; j++) {
-    acc = fma(__ldg(v), __ldg(x + __ldg(col)), acc);
-    v += SELL_C;
-    col += SELL_C;
-  }
-  return acc;
-}
+// one row per thread, a warp per slice: acc = sum_j val * x[col], in column
+// order; four entries' loads are issued before their products
+__device__ __forceinline__ void sell_acc(double &acc, double a, double x) { acc = fma(a, x, acc); }
+__device__ __forceinline__ void sell_acc(dw &acc, float2 a, double x) { acc = t_fma(dw(a.x, a.y), dw_from_double(x), acc); }
+__device__ __forceinline__ double sell_out(double acc) { return acc; }
+__device__ __forceinline__ double sell_out(dw acc) { return dw_to_double(acc); }
 
-__device__ __forceinline__ double sell_row(const float2 *__restrict__ v, const int *__restrict__ col, int w,
+template <typename VT, typename CT>
+__device__ __forceinline__ double sell_row(const VT *__restrict__ v, const CT *__restrict__ col, int w, int base,
                                            const double *__restrict__ x) {
-  dw acc(0.0f, 0.0f);
+  using AT = typename std::conditional<sizeof(VT) == 8 && std::is_same<VT, double>::value, double, dw>::type;
+  AT acc = AT(0.0);
   int j = 0;
   for (; j + 4 <= w; j += 4) {
-    const float2 a0 = __ldg(v), a1 = __ldg(v + SELL_C), a2 = __ldg(v + 2 * SELL_C), a3 = __ldg(v + 3 * SELL_C);
-    const int c0 = __ldg(col), c1 = __ldg(col + SELL_C), c2 = __ldg(col + 2 * SELL_C), c3 = __ldg(col + 3 * SELL_C);
+    const VT a0 = __ldg(v), a1 = __ldg(v + SELL_C), a2 = __ldg(v + 2 * SELL_C), a3 = __ldg(v + 3 * SELL_C);
+    const int c0 = sell_col(col, base), c1 = sell_col(col + SELL_C, base), c2 = sell_col(col + 2 * SELL_C, base),
+              c3 = sell_col(col + 3 * SELL_C, base);
     const double x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-    acc = t_fma(dw(a0.x, a0.y), dw_from_double(x0), acc);
-    acc = t_fma(dw(a1.x, a1.y), dw_from_double(x1), acc);
-    acc = t_fma(dw(a2.x, a2.y), dw_from_double(x2), acc);
-    acc = t_fma(dw(a3.x, a3.y), dw_from_double(x3), acc);
+    sell_acc(acc, a0, x0);
+    sell_acc(acc, a1, x1);
+    sell_acc(acc, a2, x2);
+    sell_acc(acc, a3, x3);
     v += 4 * SELL_C;
     col += 4 * SELL_C;
   }
   for (; j < w; j++) {
-    const float2 a = __ldg(v);
-    acc = t_fma(dw(a.x, a.y), dw_from_double(__ldg(x + __ldg(col))), acc);
+    sell_acc(acc, __ldg(v), __ldg(x + sell_col(col, base)));
     v += SELL_C;
     col += SELL_C;
   }
-  return dw_to_double(acc);
+  return sell_out(acc);
 }
 
 // ---------------------------------------------------------------- state
@@ -145,7 +154,8 @@ struct GmState {
 // device arrays of one solve
 struct GmArgs {
   int n, nslices, nb;
-  const int *row_ptr, *col_ind, *sell_off, *sell_col;
+  const int *row_ptr, *col_ind, *sell_off, *sell_col32;
+  const short *sell_col16;  // one of the two column arrays is set
   const double *val, *sell_val64;
   const float2 *sell_valdw;
   const double *dinv, *b;
@@ -190,9 +200,10 @@ __global__ void __launch_bounds__(GM_T) gm_restart_residual(GmArgs a) {
   if (a.sell_val64) {
     const int s = blockIdx.x * (GM_T / 32) + threadIdx.x / 32, l = threadIdx.x & 31;
     if (s >= a.nslices) return;
-    const int r = s * SELL_C + l;
+    const int r = s * SELL_C + l, base = sell_base(r, a.n);
     const int o = a.sell_off[s], w = (a.sell_off[s + 1] - o) / SELL_C;
-    const double acc = sell_row(a.sell_val64 + o + l, a.sell_col + o + l, w, a.x);
+    const double acc = a.sell_col16 ? sell_row(a.sell_val64 + o + l, a.sell_col16 + o + l, w, base, a.x)
+                                    : sell_row(a.sell_val64 + o + l, a.sell_col32 + o + l, w, base, a.x);
     if (r < a.n) a.tmp[r] = (a.b[r] - acc) * a.dinv[r];
     return;
   }
@@ -254,15 +265,16 @@ __global__ void __launch_bounds__(GM_T) gm_start_cycle(GmArgs a) {
 }
 
 // V[j+1] = dinv A V[j]
-template <typename VT>
-__global__ void __launch_bounds__(GM_T) gm_arnoldi_spmv(GmArgs a, const VT *__restrict__ sv, int j) {
+template <typename VT, typename CT>
+__global__ void __launch_bounds__(GM_T) gm_arnoldi_spmv(GmArgs a, const VT *__restrict__ sv,
+                                                        const CT *__restrict__ scol, int j) {
   const GmState &S = *a.st;
   if (S.phase != GM_ARNOLDI || S.j != j) return;
   const int s = blockIdx.x * (GM_T / 32) + threadIdx.x / 32, l = threadIdx.x & 31;
   if (s >= a.nslices) return;
   const int r = s * SELL_C + l;
   const int o = a.sell_off[s], w = (a.sell_off[s + 1] - o) / SELL_C;
-  const double acc = sell_row(sv + o + l, a.sell_col + o + l, w, a.V + (size_t)j * a.n);
+  const double acc = sell_row(sv + o + l, scol + o + l, w, sell_base(r, a.n), a.V + (size_t)j * a.n);
   if (r < a.n) a.V[(size_t)(j + 1) * a.n + r] = a.dinv[r] * acc;
 }
 
@@ -385,12 +397,16 @@ unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 int build_sell(gbfem_ctx c) {
   const int n = c->ndof, ns = (n + gbfem::SELL_C - 1) / gbfem::SELL_C;
   if (c->sell_ready && c->sell_n == n && c->sell_nnz == c->nnz) return 0;
-  GB_TRY(c->sell_off.alloc((size_t)ns + 1));
-  gbfem::sell_width_kernel<<<nblk(ns, 256), 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->sell_off.p);
+  GB_TRY(c->sell_off.alloc((size_t)2 * ns + 1));
+  gbfem::sell_width_kernel<<<nblk(ns, 256), 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->col_ind.p, c->sell_off.p,
+                                                                 c->sell_off.p + ns);
   GB_CUDA(cudaGetLastError());
-  std::vector<int> w(ns), off(ns + 1);
-  GB_CUDA(cudaMemcpyAsync(w.data(), c->sell_off.p, (size_t)ns * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  std::vector<int> w(2 * (size_t)ns), off(ns + 1);
+  GB_CUDA(cudaMemcpyAsync(w.data(), c->sell_off.p, 2 * (size_t)ns * sizeof(int), cudaMemcpyDeviceToHost,
+                          c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
+  bool fits16 = true;
+  for (int s = 0; s < ns; s++) fits16 = fits16 && w[ns + s];
   long long tot = 0;
   for (int s = 0; s < ns; s++) {
     off[s] = (int)tot;
@@ -400,10 +416,20 @@ int build_sell(gbfem_ctx c) {
   off[ns] = (int)tot;
   GB_CUDA(cudaMemcpyAsync(c->sell_off.p, off.data(), (size_t)(ns + 1) * sizeof(int), cudaMemcpyHostToDevice,
                           c->stream));
-  GB_TRY(c->sell_col.alloc((size_t)std::max<long long>(tot, 1)));
-  gbfem::sell_cols_kernel<<<nblk((long long)ns * gbfem::SELL_C, 256), 256, 0, c->stream>>>(
-      n, ns, c->row_ptr.p, c->col_ind.p, c->sell_off.p, c->sell_col.p);
+  const unsigned gc = nblk((long long)ns * gbfem::SELL_C, 256);
+  if (fits16) {
+    c->sell_col.release();
+    GB_TRY(c->sell_col16.alloc((size_t)std::max<long long>(tot, 1)));
+    gbfem::sell_cols_kernel<short><<<gc, 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->col_ind.p, c->sell_off.p,
+                                                                c->sell_col16.p);
+  } else {
+    c->sell_col16.release();
+    GB_TRY(c->sell_col.alloc((size_t)std::max<long long>(tot, 1)));
+    gbfem::sell_cols_kernel<int><<<gc, 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->col_ind.p, c->sell_off.p,
+                                                              c->sell_col.p);
+  }
   GB_CUDA(cudaGetLastError());
+  c->sell_cols16 = fits16;
   GB_CUDA(cudaStreamSynchronize(c->stream));  // off[] is a stack vector
   c->sell_total = tot;
   c->sell_n = n;
@@ -447,10 +473,17 @@ int capture_cycle(gbfem_ctx c, const GmArgs &a, int m, bool dword, int *kernels)
   k += 4;
   for (int j = 0; j < m; j++) {
     if (j == 0) cudaEventRecordWithFlags(c->ev2, st, cudaEventRecordExternal);
-    if (dword)
-      gbfem::gm_arnoldi_spmv<float2><<<gs, gbfem::GM_T, 0, st>>>(a, a.sell_valdw, j);
-    else
-      gbfem::gm_arnoldi_spmv<double><<<gs, gbfem::GM_T, 0, st>>>(a, a.sell_val64, j);
+    if (dword) {
+      if (a.sell_col16)
+        gbfem::gm_arnoldi_spmv<<<gs, gbfem::GM_T, 0, st>>>(a, a.sell_valdw, a.sell_col16, j);
+      else
+        gbfem::gm_arnoldi_spmv<<<gs, gbfem::GM_T, 0, st>>>(a, a.sell_valdw, a.sell_col32, j);
+    } else {
+      if (a.sell_col16)
+        gbfem::gm_arnoldi_spmv<<<gs, gbfem::GM_T, 0, st>>>(a, a.sell_val64, a.sell_col16, j);
+      else
+        gbfem::gm_arnoldi_spmv<<<gs, gbfem::GM_T, 0, st>>>(a, a.sell_val64, a.sell_col32, j);
+    }
     if (j == 0) cudaEventRecordWithFlags(c->ev3, st, cudaEventRecordExternal);
     gbfem::gm_dot_partial<<<dim3(gv, j + 1), gbfem::GM_T, 0, st>>>(a, j);
     gbfem::gm_dot_sum<<<j + 1, gbfem::GM_T, 0, st>>>(a, j);
@@ -506,7 +539,8 @@ int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int 
   a.row_ptr = c->row_ptr.p;
   a.col_ind = c->col_ind.p;
   a.sell_off = c->sell_off.p;
-  a.sell_col = c->sell_col.p;
+  a.sell_col32 = c->sell_cols16 ? nullptr : c->sell_col.p;
+  a.sell_col16 = c->sell_cols16 ? c->sell_col16.p : nullptr;
   a.val = c->val.p;
   a.sell_val64 = c->std_spmv_dword ? nullptr : c->sell_val.p;
   a.sell_valdw = c->std_spmv_dword ? c->sell_valdw.p : nullptr;

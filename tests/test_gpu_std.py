@@ -270,6 +270,35 @@ def test_dropin_cache_sees_new_tables_at_the_same_address(gb):
     c.close()
 
 
+def test_constrained_vertices_are_refused(gb):
+    """A once-refined ModFEM mesh has constrained (hanging) vertices: they
+    carry no dof, and the dof lists of their elements name the constraining
+    vertices instead (apr_get_stiff_mat_data, aps_std_lin_intf.c:2995-3170),
+    so sir_create reports more dofs per entity than vertices.  The library
+    does not do the constraint rewrite; both signs of it are refused with an
+    error instead of assembling a wrong matrix."""
+    g = load("std_n10")
+    m = FixtureMesh(g)
+    c = make_ctx(gb, m, g["k"])
+    dn = g["dof_of_node"].astype(np.int32).copy()
+    hanging = int(m.el_nodes[7, 4])
+    dn[hanging] = -1  # a vertex without a dof
+    with pytest.raises(gb.GbFemError, match="hanging"):
+        c.set_crs_structure(dn, g["row_ptr"], g["col_ind"])
+    # the conforming structure is accepted; a dof list longer than the
+    # element's vertex count is refused by the drop-in
+    c.set_crs_structure(g["dof_of_node"], g["row_ptr"], g["col_ind"])
+    val, rhs = np.zeros(g["col_ind"].size), np.zeros(g["row_ptr"].size - 1)
+    args = [g[k] for k in ("int_ent_type", "int_ent_id", "color_elems", "color_faces", "asse_pos",
+                           "assembly_table")]
+    with pytest.raises(gb.GbFemError, match="hanging"):
+        c.create_assemble_stiff_mat(*args, crs_val=val, rhs=rhs, max_dofs=9)
+    c.create_assemble_stiff_mat(*args, crs_val=val, rhs=rhs)
+    assert crs_rel_err(g["row_ptr"], val, g["crs_val"], energy_scale(g["row_ptr"], g["col_ind"], g["crs_val"])) \
+        < REL_TOL
+    c.close()
+
+
 @pytest.mark.parametrize("shuffle", [False, True])
 def test_dropin_pipelined_download(gb, shuffle):
     """With cached tables the drop-in runs the elements in chunks and copies
@@ -466,6 +495,51 @@ def test_gmres_tight_tolerance_vs_oracle(gb):
     r = O.crs_residual(rp, ci, val, x, rhs) / diag
     # GMRES stops at max(1e-13 * initial, 1e-12 absolute): here the absolute floor
     assert np.linalg.norm(r) < 1.1 * max(1e-12, 1e-13 * np.linalg.norm(rhs / diag))
+
+
+@pytest.mark.parametrize("spmv", ["fp64", "dword"])
+def test_gmres_sliced_ell_column_forms(gb, spmv):
+    """gbfem_solve's SpMV runs on a sliced-ELL copy with 16-bit column
+    offsets where every column lies within 32767 of its row, 32-bit indices
+    otherwise.  The same system in the first-appearance dof order (16-bit
+    form) and under a random symmetric permutation of the dofs (32-bit form:
+    columns up to 68,920 away) gives the same iterations (Jacobi-
+    preconditioned GMRES is invariant under symmetric permutations up to
+    rounding) and the same solution; both match the oracle's GMRES."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    m = structured_prism_mesh(40, jitter=0.2, seed=6)
+    k = lognormal_k(m.nel, seed=6)
+    c = make_ctx(gb, m, k)
+    nd, nnz, _ = c.build_structure()
+    c.assemble(gb.SCATTER_ATOMIC)
+    val, rhs = c.get_matrix()
+    dn, rp, ci = c.get_crs_structure()
+    rows = np.repeat(np.arange(nd), np.diff(rp))
+    assert np.max(np.abs(ci - rows)) < 32767
+    c.set_option(gb.OPT_STD_SPMV_ARITH, gb.STD_DWORD if spmv == "dword" else gb.STD_FP64)
+    x, it, _, rel = c.solve(30, 3000, 1e-10)
+    # the permuted system: new dof q = perm[old]
+    perm = np.random.default_rng(8).permutation(nd)
+    inv = np.argsort(perm)
+    cols_new = perm[ci]
+    order = np.lexsort((cols_new, perm[rows]))  # by new row, then new column
+    rp2 = np.concatenate([[0], np.cumsum(np.bincount(perm[rows], minlength=nd))]).astype(np.int32)
+    ci2 = cols_new[order].astype(np.int32)
+    assert np.max(np.abs(ci2 - np.repeat(np.arange(nd), np.diff(rp2)))) > 32767
+    c2 = gb.Context(0)
+    c2.set_mesh(m)
+    c2.set_coefficients(k=k)
+    c2.set_crs_structure(perm[dn].astype(np.int32), rp2, ci2)
+    c2.set_matrix(val[order], rhs[inv])
+    c2.set_option(gb.OPT_STD_SPMV_ARITH, gb.STD_DWORD if spmv == "dword" else gb.STD_FP64)
+    x2, it2, _, rel2 = c2.solve(30, 3000, 1e-10)
+    assert abs(it - it2) <= 1 and rel < 1e-10 and rel2 < 1e-10
+    assert vec_rel_err(x2[perm], x) < 1e-8
+    xo, ito, _, _ = O.gmres_jacobi(rp, ci, val, rhs, 30, 3000, 1e-10)
+    assert abs(it - ito) <= 1
+    assert vec_rel_err(x, xo) < 1e-8
+    c.close()
+    c2.close()
 
 
 # ------------------------------------------------------------ larger sizes
