@@ -135,6 +135,11 @@ int gbfem_destroy(gbfem_ctx c) {
   c->dg_colx_d.release();
   c->dg_row_val_d.release();
   c->dg_cx_off_d.release();
+  c->dg_fcfg.release();
+  c->dg_ftab_off.release();
+  c->dg_ftab.release();
+  c->dg_tcface.release();
+  c->dg_fgeo.release();
   cudaEventDestroy(c->ev0);
   cudaEventDestroy(c->ev1);
   cudaEventDestroy(c->ev2);
@@ -906,6 +911,19 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   std::vector<gbfem::DgHalfFace> hf(hptr[nel]);
   std::vector<int> hfill(hptr.begin(), hptr.end() - 1);
   const int *en = c->h_el_nodes.data();
+  // face-point configurations (vertex count, local vertex order) of the
+  // tensor-core face kernel's basis tables
+  std::vector<unsigned char> cfgs;
+  auto cfg_of = [&](int nfv, const unsigned char *loc) -> int {
+    const int ncfg = (int)cfgs.size() / 5;
+    for (int k = 0; k < ncfg; k++)
+      if (cfgs[5 * k] == nfv && memcmp(&cfgs[5 * k + 1], loc, nfv) == 0) return k;
+    if (ncfg >= gbfem::DG_TF_MAXCFG) return 255;
+    cfgs.push_back((unsigned char)nfv);
+    for (int i = 0; i < 4; i++) cfgs.push_back(i < nfv ? loc[i] : 0);
+    return ncfg;
+  };
+  std::vector<int> face_rep(nfa, -1);  // the first neighbour's record of each face
   for (int f = 0; f < nfa; f++) {
     gbfem::DgHalfFace h;
     memset(&h, 0, sizeof(h));
@@ -913,6 +931,7 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
     h.el2 = c->dg_fa_el[2 * f + 1];
     h.side1 = c->dg_fa_side[f];
     h.nfv = c->dg_fa_type[f];
+    h.face = f;
     for (int i = 0; i < h.nfv; i++) {
       const int v = c->dg_fa_nodes[4 * f + i];
       for (int k = 0; k < c->nv; k++) {
@@ -920,14 +939,39 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
         if (h.el2 >= 0 && en[c->nv * (size_t)h.el2 + k] == v) h.loc2[i] = (unsigned char)k;
       }
     }
+    if (c->nv == GBFEM_PRISM) {
+      h.cfg1 = (unsigned char)cfg_of(h.nfv, h.loc1);
+      h.cfg2 = h.el2 >= 0 ? (unsigned char)cfg_of(h.nfv, h.loc2) : 0;
+    }
     h.owner_is_2 = 0;
     h.blk = h.el2 >= 0 ? block_of(h.el1, h.el2) : -1;
+    face_rep[f] = hfill[h.el1];
     hf[hfill[h.el1]++] = h;
     if (h.el2 >= 0) {
       h.owner_is_2 = 1;
       h.blk = block_of(h.el2, h.el1);
       hf[hfill[h.el2]++] = h;
     }
+  }
+  // tables and face list for the tensor-core face kernel (prisms, at most
+  // DG_TF_MAXCFG configurations; otherwise that kernel is not used)
+  c->dg_ftab_ok = false;
+  c->dg_tcface.release();
+  if (c->nv == GBFEM_PRISM && (int)cfgs.size() / 5 < gbfem::DG_TF_MAXCFG && nfa > 0) {
+    const int ncfg = (int)cfgs.size() / 5;
+    std::vector<long long> toff((size_t)ncfg * 9);
+    const long long tsize = gbfem::dg_face_table_size(ncfg, cfgs.data(), toff.data());
+    std::vector<int> tcf;  // faces whose sides both have degree <= 3
+    for (int f = 0; f < nfa; f++) {
+      const int e1 = c->dg_fa_el[2 * f], e2 = c->dg_fa_el[2 * f + 1];
+      if (c->dg_p[e1] <= 3 && (e2 < 0 || c->dg_p[e2] <= 3)) tcf.push_back(face_rep[f]);
+    }
+    GB_TRY(upload(c, c->dg_fcfg, cfgs.data(), cfgs.size()));
+    GB_TRY(upload(c, c->dg_ftab_off, toff.data(), toff.size()));
+    GB_TRY(c->dg_ftab.alloc((size_t)tsize));
+    GB_TRY(gbfem::launch_dg_face_tables(c->stream, ncfg, c->dg_fcfg.p, c->dg_ftab_off.p, c->dg_ftab.p));
+    if (!tcf.empty()) GB_TRY(upload(c, c->dg_tcface, tcf.data(), tcf.size()));
+    c->dg_ftab_ok = true;
   }
   // per block row: value offset, and the dof index of each of its columns
   std::vector<long long> row_val(nel), cx_off(nel + 1, 0);
@@ -1047,6 +1091,7 @@ int gbfem_dg_assemble(gbfem_ctx c) {
   }
   cudaEventRecord(c->ev2, c->stream);
   const bool tcf = c->dg_face_mode == GBFEM_DG_FACE_TC || c->dg_face_mode == GBFEM_DG_FACE_TC_DWORD;
+  bool geo_done = false;
   if (c->dg_hf.p) {
     if (tcf && !tc) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
     for (int p = 1; p <= 4; p++) {
@@ -1062,14 +1107,25 @@ int gbfem_dg_assemble(gbfem_ctx c) {
         launches += r;
         continue;
       }
-      if (tcf) {
+      if (tcf && c->dg_ftab_ok) {
         // tensor-core eligible owners, then the rest on the FP64 (or, in
         // TC_DWORD mode, the double-word) kernel; running the two side by
         // side on disjoint owners was slower (167 vs 157 ms at p = 3, 432k)
+        if (!geo_done) {
+          // per-point geometry of every face between degree <= 3 elements,
+          // once per face (both owners read it)
+          GB_TRY(c->dg_fgeo.alloc((size_t)c->dg_nfa * 16 * 8));
+          const int r = gbfem::launch_dg_face_geometry(c->stream, (int)c->dg_tcface.n, c->dg_tcface.p, c->dg_hf.p,
+                                                       c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
+                                                       c->dg_pen, c->dg_fgeo.p);
+          GB_TRY(r);
+          launches += r;
+          geo_done = true;
+        }
         int r = gbfem::launch_dg_tc_faces(c->stream, p, (int)c->dg_flist_tc[p].n, c->dg_flist_tc[p].p,
-                                          c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p,
-                                          c->k_el.p, c->D_el.p, c->dg_pen, c->g, c->dg_boff_diag_d.p,
-                                          c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p, c->err.p);
+                                          c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->dg_fgeo.p, c->dg_ftab.p,
+                                          c->dg_ftab_off.p, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p,
+                                          c->dg_val.p, c->dg_rhs.p, c->err.p);
         GB_TRY(r);
         launches += r;
         r = gbfem::launch_dg_prism_faces(c->stream, p, (int)c->dg_flist_64[p].n, c->dg_flist_64[p].p, c->dg_hf_ptr.p,

@@ -24,18 +24,27 @@
 // atomics).  Covers owners of degree <= 3 whose neighbours all have degree
 // <= 3 (2 nq <= 32); the others keep the FP64 face kernel.
 //
-// First the geometry of all the element's faces at once (one thread per face
-// and point, in two passes: first side, whose Jacobian gives the normal, then
-// the second side; the long FP64 chains with their divisions and square roots
-// run side by side).  Then per face: monomial factors and per-(b, c) basis
-// products; one fused pass over (row, point) pairs forming the FP64 operand
-// values, each row's exponent (a shuffle max over its 16-lane segment) and
-// the BF16 slices, with no FP64 staging; 56 MMAs (M 128, N = NS rounded up to
-// 16, K 16) issued by one thread into 7 accumulators; commit to an mbarrier;
-// epilogue by the warps whose TMEM lane quarter holds rows (tcgen05.ld: warp
-// w reads lane quarter w % 4, column half w / 4).  Every wait has an
-// iteration limit: on expiry the CTA records an error, lets its MMAs drain
-// (again with a limit), frees its TMEM and returns.
+// Two things the face matrices need do not depend on the owner, and are
+// built outside this kernel so that no CTA repeats them:
+//  * the per-point geometry of every face (area weight, penalty, and for both
+//    sides v = J^-1 A^T n), once per face by dg_face_geometry_kernel, where
+//    an owner-computes kernel would form it once per owner;
+//  * the reference basis and its three local derivatives at the face points,
+//    which depend only on the face's rule, the basis degree and how the face's
+//    vertices sit in the element (its "configuration": vertex count and local
+//    vertex order, at most 6 per triangle side and 8 per quadrilateral side),
+//    so they are tables (dg_face_table_kernel, built once per structure,
+//    about 2 MB, L2-resident), where the kernel otherwise evaluated monomial
+//    factors per face, point and side.
+// Per face the CTA then reads its points' geometry, and one fused pass over
+// (row, point) pairs forms the FP64 operand values (phi from the table,
+// g = v . grad phi: three FMAs), each row's exponent (a shuffle max over its
+// 16-lane segment) and the BF16 slices, with no FP64 staging; 56 MMAs (M 128,
+// N = NS rounded up to 16, K 16) issued by one thread into 7 accumulators;
+// commit to an mbarrier; epilogue by the warps whose TMEM lane quarter holds
+// rows (tcgen05.ld: warp w reads lane quarter w % 4, column half w / 4).
+// Every wait has an iteration limit: on expiry the CTA records an error, lets
+// its MMAs drain (again with a limit), frees its TMEM and returns.
 
 #include "dg_face.cuh"
 #include "gbfem_internal.h"
@@ -56,15 +65,8 @@ constexpr int TF_M = 128;         // MMA M
 constexpr int TF_THREADS = 256;
 constexpr int TF_TMEM_COLS = 256;  // two CTAs per SM share the 512 columns
 constexpr int TF_NCH = 32;         // MMA N per chunk of e's functions: 7 x 32 accumulator columns
-// per-point table strides in doubles, odd so that the 16 lanes of a row
-// segment (one per point) fall on different shared-memory banks
-constexpr int TF_GEO = 17;   // 13 geometry values + 3 owner-row scales, padded
-constexpr int TF_FAC = 30;   // monomial factors per point and side
-constexpr int TF_FACS = 31;  // their stride
-constexpr int TF_UWS = 33;   // 16 (b, c) x 2 basis products per point and side, padded
-static_assert(TF_FACS > TF_FAC && TF_UWS > 32 && TF_GEO > 16, "padded strides hold their tables");
+constexpr int TF_GEO = 8;    // per face point: f a, c a, v1 (3), v2 (3)
 static_assert((long long)TF_SL * TF_KP * 255 * 255 < (1LL << 24), "slice sums must stay exact in FP32");
-static_assert(TF_NF * (2 * TF_NQ + 1) <= TF_THREADS, "one thread per (face, point, side) and per face");
 
 template <int P>
 struct TfDims {
@@ -79,11 +81,8 @@ struct TfDims {
   static constexpr int A_BYTES = (TF_SL - 1) * A_STRIDE + TF_M * TF_KP * 2;
   static constexpr int B_SLICE = NPAD * TF_KP * 2;
   static constexpr int OFF_B = A_BYTES;
-  static constexpr int OFF_UW = OFF_B + TF_SL * B_SLICE;
-  static constexpr int OFF_FAC = OFF_UW + TF_NQ * 2 * TF_UWS * 8;          // [TF_NQ][2][TF_FACS]
-  static constexpr int OFF_FACE = OFF_FAC + TF_NQ * 2 * TF_FACS * 8;
-  // per face: X [2][18], A [2][9], G [TF_NQ][TF_GEO], EV [TF_NQ][2][6] (point, v), pen, spare
-  static constexpr int FACE_DOUBLES = 36 + 18 + TF_NQ * TF_GEO + TF_NQ * 2 * 6 + 2;
+  static constexpr int OFF_FACE = OFF_B + TF_SL * B_SLICE;                 // [TF_NF][TF_NQ][TF_GEO]
+  static constexpr int FACE_DOUBLES = TF_NQ * TF_GEO;
   static constexpr int OFF_DIAG = OFF_FACE + TF_NF * FACE_DOUBLES * 8;     // [NS][SD_LD] diagonal-block share
   static constexpr int SD_LD = NS + 1;                                     // odd row stride
   static constexpr int OFF_RACC = OFF_DIAG + NS * SD_LD * 8;               // [NS] boundary rhs sums
@@ -175,20 +174,107 @@ __device__ __forceinline__ uint32_t tf_bf16_bits(uint32_t mag, bool neg) {
   return (__float_as_uint(fv) >> 16) | (neg ? 0x8000u : 0u);
 }
 
+// The reference basis at the face points of every configuration: one block
+// per (configuration, rule degree pr, basis degree pb), a thread per (point,
+// function): value and the xi / eta / zeta derivatives, from the monomial
+// factors of dg_point_factors (so the values are those of the FP64 kernel).
+__global__ void dg_face_table_kernel(const unsigned char *__restrict__ cfg, const long long *__restrict__ tab_off,
+                                     double *__restrict__ tab) {
+  const int c = blockIdx.x / 9, pr = (blockIdx.x / 3) % 3 + 1, pb = blockIdx.x % 3 + 1;
+  const int nfv = cfg[5 * c], ti = nfv == 4 ? 1 : 0;
+  const int nq = tf_nqf[pr][ti], ns = tf_ns[pb];
+  double *out = tab + tab_off[blockIdx.x];
+  for (int t = threadIdx.x; t < nq * ns; t += blockDim.x) {
+    const int q = t / ns, j = t % ns;
+    double w[4];
+    tf_weights(nfv, tf_fq[pr - 1][ti][q], w);
+    const v3 e = tf_local_point(nfv, w, cfg + 5 * c + 1);
+    double T[30];
+    dg_point_factors(e, v3{1.0, 1.0, 1.0}, T);
+    const unsigned char *ex = tf_exp[pb - 1][j];
+    const int a = ex[0], b = ex[1], cc = ex[2];
+    const double u = T[5 + b] * T[10 + cc];
+    double *o = out + 4 * (size_t)t;
+    o[0] = T[a] * u;
+    o[1] = T[15 + a] * u;
+    o[2] = T[a] * (T[20 + b] * T[10 + cc]);
+    o[3] = T[a] * (T[5 + b] * T[25 + cc]);
+  }
+}
+
+// Per-point geometry of a face, from its first neighbour's half-face record:
+// the point in each side's local coordinates, the first side's Jacobian
+// (normal, area weight), both sides' v = J^-1 A^T n; the penalty
+// pen min(p1, p2) / sqrt(area) (p1 on the boundary) with mmr_fa_area's split
+// of a quadrilateral.  One thread per (face, point); the same operations as
+// the FP64 face kernel's dg_face_point.
+__global__ void __launch_bounds__(128) dg_face_geometry_kernel(
+    int count, const int *__restrict__ faces_hf, const DgHalfFace *__restrict__ hf, const int *__restrict__ el_p,
+    const int *__restrict__ el_nodes, const double *__restrict__ xyz, const double *__restrict__ k_el,
+    const double *__restrict__ D_el, double pen, double *__restrict__ geo) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(t / TF_NQ), q = (int)(t % TF_NQ);
+  if (i >= count) return;
+  const DgHalfFace F = hf[faces_hf[i]];
+  const bool interior = F.el2 >= 0;
+  const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
+  const int ti = F.nfv == 4 ? 1 : 0;
+  const int pr = (interior && tf_nqf[p2][ti] > tf_nqf[p1][ti]) ? p2 : p1;
+  double *G = geo + ((size_t)F.face * TF_NQ + q) * TF_GEO;
+  if (pr > 3 || q >= tf_nqf[pr][ti]) return;
+  double X1[18], X2[18], A1[9], A2[9];
+  for (int r = 0; r < 18; r++) X1[r] = xyz[3 * (size_t)el_nodes[6 * (size_t)F.el1 + r / 3] + r % 3];
+  for (int r = 0; r < 9; r++)
+    A1[r] = D_el ? D_el[9 * (size_t)F.el1 + r] : ((r % 4 == 0) ? (k_el ? k_el[F.el1] : 1.0) : 0.0);
+  const double *fq = tf_fq[pr - 1][ti][q];
+  double w[4];
+  tf_weights(F.nfv, fq, w);
+  const v3 e1 = tf_local_point(F.nfv, w, F.loc1);
+  v3 j1, j2, j3;
+  prism_jacobian_columns(X1, e1, j1, j2, j3);
+  const v3 ds = prism_side_vector(F.side1, j1, j2, j3);
+  const double d = sqrt(v3_dot(ds, ds));
+  const v3 n = v3_scale(1.0 / d, ds);
+  const v3 v1 = tf_face_v(j1, j2, j3, A1, n);
+  v3 v2 = {0.0, 0.0, 0.0};
+  if (interior) {
+    for (int r = 0; r < 18; r++) X2[r] = xyz[3 * (size_t)el_nodes[6 * (size_t)F.el2 + r / 3] + r % 3];
+    for (int r = 0; r < 9; r++)
+      A2[r] = D_el ? D_el[9 * (size_t)F.el2 + r] : ((r % 4 == 0) ? (k_el ? k_el[F.el2] : 1.0) : 0.0);
+    const v3 e2 = tf_local_point(F.nfv, w, F.loc2);
+    prism_jacobian_columns(X2, e2, j1, j2, j3);
+    v2 = tf_face_v(j1, j2, j3, A2, n);
+  }
+  v3 V[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int l = k < F.nfv ? F.loc1[k] : 0;
+    V[k] = {X1[3 * l], X1[3 * l + 1], X1[3 * l + 2]};
+  }
+  const int pp = interior ? (p1 < p2 ? p1 : p2) : p1;
+  const double cpen = pen * pp / sqrt(dg_face_area(V, F.nfv));
+  const double aw = d * fq[2];
+  G[0] = (interior ? 0.5 : 1.0) * aw;
+  G[1] = cpen * aw;
+  G[2] = v1.x;
+  G[3] = v1.y;
+  G[4] = v1.z;
+  G[5] = v2.x;
+  G[6] = v2.y;
+  G[7] = v2.z;
+}
+
 template <int P>
 __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
-    const int *__restrict__ el_p, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
-    const double *__restrict__ k_el, const double *__restrict__ D_el, double pen, double gval,
-    const long long *__restrict__ boff_diag, const int *__restrict__ roff, double *__restrict__ val,
-    double *__restrict__ rhs, int *err) {
+    const int *__restrict__ el_p, const double *__restrict__ geo, const double *__restrict__ ftab,
+    const long long *__restrict__ ftab_off, double gval, const long long *__restrict__ boff_diag,
+    const int *__restrict__ roff, double *__restrict__ val, double *__restrict__ rhs, int *err) {
   using Dm = TfDims<P>;
   constexpr int NS = Dm::NS, NPAD = Dm::NPAD, FD = Dm::FACE_DOUBLES;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *asl = smem, *bsl = smem + Dm::OFF_B;
-  double *sUW = (double *)(smem + Dm::OFF_UW);       // [TF_NQ][2][TF_UWS]: per (b, c) basis products
-  double *sFac = (double *)(smem + Dm::OFF_FAC);     // [TF_NQ][2][TF_FACS]: the current face's factors
-  double *sface = (double *)(smem + Dm::OFF_FACE);   // [TF_NF][FD]
+  double *sface = (double *)(smem + Dm::OFF_FACE);   // [TF_NF][TF_NQ][TF_GEO]
   double *sRacc = (double *)(smem + Dm::OFF_RACC);   // [NS]
   double *sD = (double *)(smem + Dm::OFF_DIAG);      // [NS][SD_LD]: row r (trial function), column i
   DgHalfFace *sHF = (DgHalfFace *)(smem + Dm::OFF_HF);
@@ -223,96 +309,11 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  // ---- all faces at once: coordinates and tensors of both sides ----
-  for (int t = tid; t < nf * 54; t += TF_THREADS) {
-    const int f = t / 54, c = t % 54;
-    const DgHalfFace &F = sHF[f];
-    double *X = sface + f * FD;
-    if (c < 36) {
-      const int s = c / 18, r = c % 18;
-      if (s == 0 || F.el2 >= 0) {
-        const int el = s ? F.el2 : F.el1;
-        X[c] = xyz[3 * (size_t)el_nodes[6 * (size_t)el + r / 3] + r % 3];
-      }
-    } else {
-      const int tt = c - 36, s = tt / 9, r = tt % 9;
-      if (s == 0 || F.el2 >= 0) {
-        const int el = s ? F.el2 : F.el1;
-        X[c] = D_el ? D_el[9 * (size_t)el + r] : ((r % 4 == 0) ? (k_el ? k_el[el] : 1.0) : 0.0);
-      }
-    }
-  }
-  __syncthreads();
-  // ---- geometry: phase 1, per (face, point), the first neighbour's side
-  // (point, Jacobian, normal, area weight, v), and the penalty per face;
-  // phase 2 the second neighbour's side and the owner-row scales ----
-  if (tid < nf * TF_NQ) {
-    const int f = tid / TF_NQ, q = tid % TF_NQ;
-    const DgHalfFace &F = sHF[f];
-    const bool interior = F.el2 >= 0;
-    const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
-    const int ti = F.nfv == 4 ? 1 : 0;
-    const int pr = (interior && tf_nqf[p2][ti] > tf_nqf[p1][ti]) ? p2 : p1;
-    if (pr <= 3 && q < tf_nqf[pr][ti]) {
-      double *X = sface + f * FD, *G = X + 54 + q * TF_GEO, *EV = X + 54 + TF_NQ * TF_GEO + q * 12;
-      const double *fq = tf_fq[pr - 1][ti][q];
-      double w[4];
-      tf_weights(F.nfv, fq, w);
-      const v3 e1 = tf_local_point(F.nfv, w, F.loc1);
-      v3 j1, j2, j3;
-      prism_jacobian_columns(X, e1, j1, j2, j3);
-      const v3 ds = prism_side_vector(F.side1, j1, j2, j3);
-      const double d = sqrt(v3_dot(ds, ds));
-      const v3 n = v3_scale(1.0 / d, ds);
-      const v3 v1 = tf_face_v(j1, j2, j3, X + 36, n);
-      G[12] = d * fq[2];
-      G[13] = n.x;  // the normal, for phase 2 (then overwritten by the scales)
-      G[14] = n.y;
-      G[15] = n.z;
-      EV[0] = e1.x; EV[1] = e1.y; EV[2] = e1.z;
-      EV[3] = v1.x; EV[4] = v1.y; EV[5] = v1.z;
-    }
-  } else if (tid >= TF_NF * TF_NQ && tid < TF_NF * TF_NQ + nf) {
-    const int f = tid - TF_NF * TF_NQ;
-    const DgHalfFace &F = sHF[f];
-    const bool interior = F.el2 >= 0;
-    const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
-    const double *X = sface + f * FD;
-    v3 V[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-      const int l = i < F.nfv ? F.loc1[i] : 0;
-      V[i] = {X[3 * l], X[3 * l + 1], X[3 * l + 2]};
-    }
-    const int pp = interior ? (p1 < p2 ? p1 : p2) : p1;
-    sface[f * FD + FD - 2] = pen * pp / sqrt(dg_face_area(V, F.nfv));
-  }
-  __syncthreads();
-  if (tid < nf * TF_NQ) {
-    const int f = tid / TF_NQ, q = tid % TF_NQ;
-    const DgHalfFace &F = sHF[f];
-    const bool interior = F.el2 >= 0;
-    const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
-    const int ti = F.nfv == 4 ? 1 : 0;
-    const int pr = (interior && tf_nqf[p2][ti] > tf_nqf[p1][ti]) ? p2 : p1;
-    if (pr <= 3 && q < tf_nqf[pr][ti]) {
-      double *X = sface + f * FD, *G = X + 54 + q * TF_GEO, *EV = X + 54 + TF_NQ * TF_GEO + q * 12;
-      if (interior) {
-        double w[4];
-        tf_weights(F.nfv, tf_fq[pr - 1][ti][q], w);
-        const v3 e2 = tf_local_point(F.nfv, w, F.loc2);
-        v3 j1, j2, j3;
-        prism_jacobian_columns(X + 18, e2, j1, j2, j3);
-        const v3 v2 = tf_face_v(j1, j2, j3, X + 45, v3{G[13], G[14], G[15]});
-        EV[6] = e2.x; EV[7] = e2.y; EV[8] = e2.z;
-        EV[9] = v2.x; EV[10] = v2.y; EV[11] = v2.z;
-      }
-      // owner-row scales: L = (f a) g + (s_o c a) phi, M = -(s_o f a) phi
-      const double aw = G[12], so = F.owner_is_2 ? -1.0 : 1.0, fac = interior ? 0.5 : 1.0;
-      G[13] = fac * aw;
-      G[14] = so * X[FD - 2] * aw;
-      G[15] = -so * fac * aw;
-    }
+  // ---- the per-point geometry of all the element's faces ----
+  for (int t = tid; t < nf * FD / 2; t += TF_THREADS) {
+    const int f = t / (FD / 2), r = t % (FD / 2);
+    reinterpret_cast<double2 *>(sface + f * FD)[r] =
+        reinterpret_cast<const double2 *>(geo + (size_t)sHF[f].face * FD)[r];
   }
   // (the per-face loop starts with a barrier)
 
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
 
   for (int f = 0; f < nf; f++) {
     const DgHalfFace &F = sHF[f];
-    const double *sGeo = sface + f * FD + 54, *sEV = sGeo + TF_NQ * TF_GEO;
+    const double *sGeo = sface + f * FD;
     const bool interior = F.el2 >= 0;
     const int own2 = F.owner_is_2;
     const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
@@ -337,54 +338,43 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
     const int ns_nb = interior ? tf_ns[pnb] : 0;
     const int rows = NS + ns_nb;
     const int own_side = own2 ? 2 : 1;
+    const int cfg_own = own2 ? F.cfg2 : F.cfg1, cfg_nb = own2 ? F.cfg1 : F.cfg2;
     if (pr > 3 || rows > Dm::ROWS || nq > TF_NQ) {  // a degree-4 neighbour: not this kernel's (uniform)
       bad_input = true;
       break;
     }
-    __syncthreads();  // the previous face's shared arrays are free; the scales are written
-    // monomial factors of this face per (point, side)
-    for (int t = tid; t < 2 * nq; t += TF_THREADS) {
-      const int q = t >> 1, sd = t & 1;
-      if (sd == 1 && !interior) continue;
-      const double *ev = sEV + q * 12 + 6 * sd;
-      dg_point_factors(v3{ev[0], ev[1], ev[2]}, v3{ev[3], ev[4], ev[5]}, sFac + (2 * q + sd) * TF_FACS);
-    }
-    __syncthreads();
-    // per (point, side, b, c): U = eta^b zeta^c and W, the (eta, zeta) part of v . grad
-    for (int t = tid; t < nq * 2 * 16; t += TF_THREADS) {
-      const int q = t >> 5, sd = (t >> 4) & 1, bc = t & 15, b = bc >> 2, c = bc & 3;
-      if (sd == 1 && !interior) continue;
-      const double *T = sFac + (2 * q + sd) * TF_FACS;
-      double *uw = sUW + (q * 2 + sd) * TF_UWS + bc * 2;
-      uw[0] = T[5 + b] * T[10 + c];
-      uw[1] = fma(T[5 + b], T[25 + c], T[20 + b] * T[10 + c]);
-    }
-    __syncthreads();
+    // basis tables of this face: own side, other side ([point][function][4])
+    const double *tab_own = ftab + ftab_off[(cfg_own * 3 + pr - 1) * 3 + P - 1];
+    const double *tab_nb = interior ? ftab + ftab_off[(cfg_nb * 3 + pr - 1) * 3 + pnb - 1] : tab_own;
+    // owner-row sign s_o: L = f a g + s_o c a phi, M = -s_o f a phi
+    const long long so_bit = own2 ? (long long)1 << 63 : 0;
+    __syncthreads();  // the previous face's operand slices are consumed; the geometry is in place
     // operands in one pass, a 16-lane segment per row r and a lane per point
     // q (k = 2q: Phi / L, 2q + 1: Gam / M; lanes q >= nq give the K
-    // padding): FP64 values (phi = xi^a U, g = v_xi a xi^(a-1) U + xi^a W,
-    // the operations of dg_basis_from_factors), the row exponent by a
-    // segment max of the exponent fields, then the seven BF16 slices of the
-    // pair as one 32-bit word each.  A rows: e's functions then the
-    // neighbour's; B rows: e's functions.
+    // padding): FP64 values (phi from the table, g = v . grad phi), the row
+    // exponent by a segment max of the exponent fields, then the seven BF16
+    // slices of the pair as one 32-bit word each.  A rows: e's functions
+    // then the neighbour's; B rows: e's functions.
     for (int base = 0; base < rows * 16; base += TF_THREADS) {
       const int t = base + tid, r = t >> 4, q = t & 15;
       const bool live = r < rows, own = r < NS;  // uniform over the segment
       double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
       if (live && q < nq) {
-        const int side = own ? own_side : 3 - own_side, jj = own ? r : r - NS, p = own ? P : pnb;
-        const unsigned char *ex = tf_exp[p - 1][jj];
-        const double *T = sFac + (2 * q + side - 1) * TF_FACS;
-        const double *uw = sUW + (q * 2 + side - 1) * TF_UWS + (ex[1] * 4 + ex[2]) * 2;
-        const double phi = T[ex[0]] * uw[0];
-        const double g = fma(T[15 + ex[0]], uw[0], T[ex[0]] * uw[1]);
+        const int side = own ? own_side : 3 - own_side, jj = own ? r : r - NS;
+        const double *tb = (own ? tab_own : tab_nb) + ((size_t)q * (own ? NS : ns_nb) + jj) * 4;
+        const double2 t01 = __ldg(reinterpret_cast<const double2 *>(tb));
+        const double2 t23 = __ldg(reinterpret_cast<const double2 *>(tb) + 1);
+        const double *G = sGeo + q * TF_GEO;
+        const double *v = G + (side == 1 ? 2 : 5);
+        const double phi = t01.x;
+        const double g = fma(v[0], t01.y, fma(v[1], t23.x, v[2] * t23.y));
         // Phi = s_t phi: the sign flip on the integer side
         a0 = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
         a1 = g;
         if (own) {
-          const double *G = sGeo + q * TF_GEO;
-          b0 = fma(G[13], g, G[14] * phi);
-          b1 = G[15] * phi;
+          const double sphi = __longlong_as_double(__double_as_longlong(phi) ^ so_bit);  // s_o phi
+          b0 = fma(G[0], g, G[1] * sphi);
+          b1 = -(G[0] * sphi);
         }
       }
       int xa = max(tf_biased_exp(a0), tf_biased_exp(a1)), xb = max(tf_biased_exp(b0), tf_biased_exp(b1));
@@ -523,17 +513,18 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
 bool dg_tc_faces_supported(int p) { return p >= 1 && p <= 3; }
 
 int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
-                       const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
-                       const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
-                       const int *roff, double *val, double *rhs, int *err) {
+                       const DgHalfFace *hf, const int *el_p, const double *geo, const double *ftab,
+                       const long long *ftab_off, double g, const long long *boff_diag, const int *roff,
+                       double *val, double *rhs, int *err) {
   if (count <= 0) return 0;
   GB_CHECK(dg_tc_faces_supported(p), "tensor-core DG face kernel covers p = 1..3");
+  GB_CHECK(geo && ftab && ftab_off, "tensor-core DG faces need the face geometry and basis tables");
 #define GB_TF_LAUNCH(PP)                                                                                      \
   {                                                                                                           \
     const int smem = TfDims<PP>::SMEM;                                                                        \
     GB_CUDA(cudaFuncSetAttribute(dg_tc_faces_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
-    dg_tc_faces_kernel<PP><<<count, TF_THREADS, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, el_nodes, xyz,   \
-                                                            k_el, D_el, pen, g, boff_diag, roff, val, rhs, err); \
+    dg_tc_faces_kernel<PP><<<count, TF_THREADS, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, geo, ftab,       \
+                                                            ftab_off, g, boff_diag, roff, val, rhs, err);     \
   }
   switch (p) {
     case 1: GB_TF_LAUNCH(1); break;
@@ -541,6 +532,38 @@ int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, con
     default: GB_TF_LAUNCH(3); break;
   }
 #undef GB_TF_LAUNCH
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
+long long dg_face_table_size(int ncfg, const unsigned char *cfg, long long *tab_off) {
+  long long off = 0;
+  for (int c = 0; c < ncfg; c++) {
+    const int ti = cfg[5 * c] == 4 ? 1 : 0;
+    for (int pr = 1; pr <= 3; pr++)
+      for (int pb = 1; pb <= 3; pb++) {
+        tab_off[(c * 3 + pr - 1) * 3 + pb - 1] = off;
+        off += 4LL * GB_DG_NQF[pr][ti] * GB_DG_NS[pb];
+      }
+  }
+  return off;
+}
+
+int launch_dg_face_tables(cudaStream_t st, int ncfg, const unsigned char *cfg, const long long *tab_off,
+                          double *tab) {
+  if (ncfg <= 0) return 0;
+  dg_face_table_kernel<<<ncfg * 9, 256, 0, st>>>(cfg, tab_off, tab);
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
+int launch_dg_face_geometry(cudaStream_t st, int count, const int *faces_hf, const DgHalfFace *hf,
+                            const int *el_p, const int *el_nodes, const double *xyz, const double *k_el,
+                            const double *D_el, double pen, double *geo) {
+  if (count <= 0) return 0;
+  const long long threads = (long long)count * TF_NQ;
+  dg_face_geometry_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(count, faces_hf, hf, el_p, el_nodes,
+                                                                            xyz, k_el, D_el, pen, geo);
   GB_CUDA(cudaGetLastError());
   return 1;
 }

@@ -132,16 +132,20 @@ int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int 
 // One (element, face) incidence of the DG face assembly, built on the host:
 // the face's two neighbours (el2 = -1 on a Dirichlet boundary face), the side
 // of el1 the face lies on, its vertex count, the local vertex index in el1 /
-// el2 of each face vertex (face order), which neighbour owns this record and
-// the value offset of the owner's off-diagonal block (owner, other).
+// el2 of each face vertex (face order), which neighbour owns this record, the
+// value offset of the owner's off-diagonal block (owner, other), the
+// face-point configurations of both sides (index of the (vertex count, local
+// vertex order) pair in the basis tables of the tensor-core face kernel) and
+// the face's index in the caller's face table.
 struct DgHalfFace {
   int el1, el2;
   int side1, nfv;
   long long blk;
   unsigned char loc1[4], loc2[4];
-  int owner_is_2;
-  int pad;
+  unsigned char owner_is_2, cfg1, cfg2, spare;
+  int face;
 };
+static_assert(sizeof(DgHalfFace) == 40, "half-face record layout");
 
 int launch_dg_tet_elements(cudaStream_t st, int device, int p, int count, const int *ent_el, const int *el_nodes,
                            const double *xyz, const double *k_el, const double *D_el, double f,
@@ -151,10 +155,25 @@ int launch_dg_tet_faces(cudaStream_t st, int p, int count, const int *ent_el, co
                         const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
                         const int *roff, double *val, double *rhs, bool dword = false);
 bool dg_tc_faces_supported(int p);
+// Face-point configurations of the tensor-core face kernel: cfg[5 c ..]
+// = (vertex count, local vertex of each face vertex); tables of the reference
+// basis (value and xi / eta / zeta derivatives, [point][function][4]) at the
+// face points of every configuration c, rule degree pr and basis degree pb
+// (1..3) from tab_off[(3 c + pr - 1) 3 + pb - 1]
+constexpr int DG_TF_MAXCFG = 64;
+long long dg_face_table_size(int ncfg, const unsigned char *cfg, long long *tab_off);
+int launch_dg_face_tables(cudaStream_t st, int ncfg, const unsigned char *cfg, const long long *tab_off,
+                          double *tab);
+// Per-point geometry of the faces in `faces` (one half-face record each):
+// geo[(face * 16 + q) * 8 ..] = (f a, c a, v1, v2) with f = 0.5 interior / 1
+// boundary, a = |ds| w_q, c = pen p / sqrt(area), v_s = J_s^-1 A_s^T n
+int launch_dg_face_geometry(cudaStream_t st, int count, const int *faces_hf, const DgHalfFace *hf,
+                            const int *el_p, const int *el_nodes, const double *xyz, const double *k_el,
+                            const double *D_el, double pen, double *geo);
 int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
-                       const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
-                       const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
-                       const int *roff, double *val, double *rhs, int *err);
+                       const DgHalfFace *hf, const int *el_p, const double *geo, const double *ftab,
+                       const long long *ftab_off, double g, const long long *boff_diag, const int *roff,
+                       double *val, double *rhs, int *err);
 int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                           const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                           const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
@@ -284,6 +303,14 @@ struct gbfem_ctx_s {
   int dg_var_vol[5] = {0, 0, 0, 0, 0}, dg_var_face[5] = {0, 0, 0, 0, 0};  // launch-shape variants per degree
   gbfem::DevBuf<int> dg_hf_ptr, dg_p_d;
   gbfem::DevBuf<gbfem::DgHalfFace> dg_hf;
+  // tensor-core faces: face-point configurations, basis tables at the face
+  // points, faces between degree <= 3 elements (a record of each) and their
+  // per-point geometry
+  gbfem::DevBuf<unsigned char> dg_fcfg;
+  gbfem::DevBuf<long long> dg_ftab_off;
+  gbfem::DevBuf<double> dg_ftab, dg_fgeo;
+  gbfem::DevBuf<int> dg_tcface;
+  bool dg_ftab_ok = false;
   // DG block Jacobi: inverted diagonal blocks, block e at dg_dinv_off_d[e]
   gbfem::DevBuf<double> dg_dinv;
   gbfem::DevBuf<float> dg_val32, dg_dinv32;  // FP32 copies for iterative refinement
