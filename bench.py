@@ -57,13 +57,15 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help=argparse.SUPPRESS)
-    p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "dg_dwf", "dg_dw", "dg_best", "batch", "std", "std_dw"], default=None,
+    p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "dg_dwf", "dg_dw", "dg_best", "batch", "std", "std_dw",
+                                         "std_solve"], default=None,
                    help="small cases for ncu captures: DG p=3 anisotropic (n^3 x 2 prisms, --n), 3 assemblies "
                         "(FP64, tensor-core volume, tensor-core volume and faces, FP64 volume and double-word faces, or "
                         "double-word volume and faces) and one "
                         "block residual; or the mixed batch "
                         "(40,000 prisms + 30,000 tetrahedra, p 1..4), 3 runs; or the std prism assembly "
-                        "(FP64 or double-word element arithmetic, n^3 x 2 prisms), 3 assemblies")
+                        "(FP64 or double-word element arithmetic, n^3 x 2 prisms), 3 assemblies; or "
+                        "the std GMRES(30) (one restart cycle, device-resident, SELL SpMV)")
     return p.parse_args()
 
 
@@ -84,6 +86,20 @@ def run_profile_case(args):
             c.assemble(gb.SCATTER_ATOMIC)
             ms.append(c.last_timing()[:2])
         print(json.dumps({"profile_case": args.profile, "elements": m.nel, "timing_ms": ms}))
+        c.close()
+        return
+    if args.profile == "std_solve":
+        m, k = make_problem(args.n)
+        c = gb.Context(0)
+        c.set_mesh(m)
+        c.set_coefficients(k=k, f=1.0, g=0.0, penalty=1e7)
+        nd, nnz, _ = c.build_structure()
+        c.assemble(gb.SCATTER_ATOMIC)
+        _, it, _, _ = c.solve(30, 30, 1e-14)
+        t = c.last_solve_timing()
+        print(json.dumps({"profile_case": args.profile, "dofs": nd, "nnz": nnz, "iterations": it,
+                          "solve_ms": t[0], "spmv_ms": t[1] / max(t[2], 1),
+                          "spmv_gbs": (12 * nnz + 16 * nd) / (t[1] / max(t[2], 1) * 1e-3) / 1e9}))
         c.close()
         return
     if args.profile == "batch":

@@ -84,8 +84,12 @@ __global__ void sell_cols_kernel(int n, int nslices, const int *__restrict__ row
   }
 }
 
-__device__ __forceinline__ int sell_col(const int *p, int) { return __ldg(p); }
-__device__ __forceinline__ int sell_col(const short *p, int base) { return base + (int)__ldg(p); }
+// the values and columns stream through once per product: loaded with the
+// evict-first hint (ld.global.cs) so that L2 keeps the gathered vector
+__device__ __forceinline__ int sell_col(const int *p, int) { return __ldcs(p); }
+__device__ __forceinline__ int sell_col(const short *p, int base) { return base + (int)__ldcs(p); }
+__device__ __forceinline__ double sell_ld(const double *p) { return __ldcs(p); }
+__device__ __forceinline__ float2 sell_ld(const float2 *p) { return __ldcs(p); }
 
 template <typename VT>
 __device__ __forceinline__ VT sell_value(double v);
@@ -111,7 +115,7 @@ __global__ void sell_vals_kernel(int n, int nslices, const int *__restrict__ row
 }
 
 // one row per thread, a warp per slice: acc = sum_j val * x[col], in column
-// order; four entries' loads are issued before their products
+// order; eight entries' loads are issued before their products
 __device__ __forceinline__ void sell_acc(double &acc, double a, double x) { acc = fma(a, x, acc); }
 __device__ __forceinline__ void sell_acc(dw &acc, float2 a, double x) { acc = t_fma(dw(a.x, a.y), dw_from_double(x), acc); }
 __device__ __forceinline__ double sell_out(double acc) { return acc; }
@@ -121,22 +125,23 @@ template <typename VT, typename CT>
 __device__ __forceinline__ double sell_row(const VT *__restrict__ v, const CT *__restrict__ col, int w, int base,
                                            const double *__restrict__ x) {
   using AT = typename std::conditional<sizeof(VT) == 8 && std::is_same<VT, double>::value, double, dw>::type;
+  constexpr int U = 8;  // entries whose loads are in flight together
   AT acc = AT(0.0);
   int j = 0;
-  for (; j + 4 <= w; j += 4) {
-    const VT a0 = __ldg(v), a1 = __ldg(v + SELL_C), a2 = __ldg(v + 2 * SELL_C), a3 = __ldg(v + 3 * SELL_C);
-    const int c0 = sell_col(col, base), c1 = sell_col(col + SELL_C, base), c2 = sell_col(col + 2 * SELL_C, base),
-              c3 = sell_col(col + 3 * SELL_C, base);
-    const double x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-    sell_acc(acc, a0, x0);
-    sell_acc(acc, a1, x1);
-    sell_acc(acc, a2, x2);
-    sell_acc(acc, a3, x3);
-    v += 4 * SELL_C;
-    col += 4 * SELL_C;
+  for (; j + U <= w; j += U) {
+    VT a[U];
+    double xv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) a[u] = sell_ld(v + u * SELL_C);
+#pragma unroll
+    for (int u = 0; u < U; u++) xv[u] = __ldg(x + sell_col(col + u * SELL_C, base));
+#pragma unroll
+    for (int u = 0; u < U; u++) sell_acc(acc, a[u], xv[u]);
+    v += U * SELL_C;
+    col += U * SELL_C;
   }
   for (; j < w; j++) {
-    sell_acc(acc, __ldg(v), __ldg(x + sell_col(col, base)));
+    sell_acc(acc, sell_ld(v), __ldg(x + sell_col(col, base)));
     v += SELL_C;
     col += SELL_C;
   }
