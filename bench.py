@@ -692,21 +692,26 @@ def mixed_precision_solution_check(gb, local, sizes=(10, 16)):
 def bench_serving(gb, local, rates=(50, 200, 1000, 2000), per_rate=48):
     """The serving workload: a Poisson stream of independent heat problems,
     each a structured prism mesh of n^3 hexahedra x 2 with n log-uniform in
-    [10, 60], lognormal(0,1) k, f = 1, solved by GMRES(30) to 1e-8.  Half the
-    requests are std linear; the other half DG with p in {1, 2}, whose n is
-    drawn from [10, 20] (GMRES(30) with block Jacobi needs more than 3,000
-    iterations, seconds per request, beyond that).  Beside the engine: the
+    [10, 60] (a stratified sample of 8 sizes), lognormal(0,1) k, f = 1,
+    solved by GMRES(30) to 1e-8.  Half the requests are std linear; the
+    other half DG with p in {1, 2}, whose n is drawn from [10, 20] (GMRES(30)
+    with block Jacobi needs more than 3,000 iterations, seconds per request,
+    beyond that).  Beside the engine: the
     plain one-at-a-time path (gbfem Context per request: upload, structure,
     assemble, solve) with its measured service times queued FIFO on the same
     arrival times."""
     from modfem_gb300.mesh import lognormal_k, prism_faces, structured_prism_mesh
     from modfem_gb300.serve import DG, STD, Problem, Server, poisson_stream
+    # 16 problems, alternating std and DG; n stratified over the log-uniform
+    # distribution (the i-th of 8 at quantile (i + 1/2) / 8, in a seeded
+    # order), so the pool holds its share of >= 100k-element std requests
     rng = np.random.default_rng(SEED)
+    qs = rng.permutation(8)
     pool = []
-    for i in range(12):
+    for i in range(16):
         kind = STD if i % 2 == 0 else DG
         hi = 60 if kind == STD else 20
-        n = int(round(np.exp(rng.uniform(np.log(10), np.log(hi)))))
+        n = int(round(10.0 * (hi / 10.0) ** ((qs[i // 2] + 0.5) / 8)))
         p = 1 if i % 4 == 1 else 2
         m = structured_prism_mesh(n, jitter=0.2, seed=1000 + i)
         k = lognormal_k(m.nel, seed=2000 + i)
@@ -741,6 +746,11 @@ def bench_serving(gb, local, rates=(50, 200, 1000, 2000), per_rate=48):
             res, span = poisson_stream(srv, [pr for (_, _, _, pr) in pool], rate, per_rate, seed=rate)
             lat = np.array([r["latency"] for r in res])
             big = np.array([r["latency"] for r in res if r["nel"] >= 80000 and r["kind"] == STD])
+            b100 = [r for r in res if r["nel"] >= 100000 and r["kind"] == STD]
+            l100 = np.array([r["latency"] for r in b100])
+            # where the large std requests' time goes: admission queue,
+            # preparation, wait for the engine, GMRES (means over them)
+            parts = (np.mean([r["times"][:4] for r in b100], axis=0) * 1e3).tolist() if b100 else None
             # the plain path on the same arrivals
             arr = np.cumsum(np.random.default_rng(rate).exponential(1.0 / rate, per_rate))
             fin, plain = 0.0, []
@@ -752,6 +762,10 @@ def bench_serving(gb, local, rates=(50, 200, 1000, 2000), per_rate=48):
                 "rate_req_s": rate, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                 "p99_ms": 1e3 * float(np.percentile(lat, 99)), "problems_per_s": per_rate / span,
                 "p99_ms_std_over_80k_elements": 1e3 * float(np.percentile(big, 99)) if big.size else None,
+                "p99_ms_std_100k": 1e3 * float(np.percentile(l100, 99)) if l100.size else None,
+                "p50_ms_std_100k": 1e3 * float(np.percentile(l100, 50)) if l100.size else None,
+                "std_100k_requests": int(l100.size),
+                "std_100k_mean_ms_queue_prep_wait_solve": parts,
                 "plain_one_at_a_time": {"p50_ms": 1e3 * float(np.percentile(plain, 50)),
                                         "p99_ms": 1e3 * float(np.percentile(plain, 99)),
                                         "problems_per_s": per_rate / (max(fin, arr[-1]))}})
@@ -840,11 +854,20 @@ def compact_line(full):
     out["batch_mixed"] = {"step_ms": _r(b["step_ms"]), "elem_per_s": _r(b["elem_per_s"]),
                           "fp64_frac": _r(b["fp64_frac"], 3),
                           "double_word_step_ms": _r(b["double_word_prisms"]["step_ms"])}
-    if "with_faces" in b:
-        out["batch_mixed"]["with_faces"] = b["with_faces"]
+    # BASELINE config 3 as a whole step: the mixed-degree prism DG system and
+    # the tetrahedral DG system (volume and faces each, measured above in this
+    # run; the two element types form separate systems, no prism-tetrahedron
+    # faces)
+    mx, tet = dg.get("mixed_p1to4_390k"), b.get("tet_dg_system")
+    if mx and tet:
+        out["batch_mixed"]["config3_whole_step_ms"] = {
+            "fp64": _r(mx["assemble_ms"] + tet["assemble_ms"]),
+            "double_word": _r(mx["double_word_assembly"]["assemble_ms"] + tet["double_word_faces"]["assemble_ms"]),
+            "elements": mx["elements"] + tet["elements"]}
     sv = full.get("serving")
     if sv:
         out["serving"] = {"p50_ms": {str(r["rate_req_s"]): _r(r["p50_ms"]) for r in sv["rates"]},
+                          "p50_ms_std_100k": {str(r["rate_req_s"]): _r(r.get("p50_ms_std_100k")) for r in sv["rates"]},
                           "p99_ms": {str(r["rate_req_s"]): _r(r["p99_ms"]) for r in sv["rates"]},
                           "p99_ms_std_100k": {str(r["rate_req_s"]): _r(r.get("p99_ms_std_100k")) for r in sv["rates"]},
                           "problems_per_s": {str(r["rate_req_s"]): _r(r["problems_per_s"]) for r in sv["rates"]},

@@ -98,6 +98,7 @@ int gbfem_destroy(gbfem_ctx c) {
   c->sell_col16.release();
   c->sell_val.release();
   c->sell_valdw.release();
+  c->gm_xdw.release();
   c->gm_small.release();
   if (c->side_stream) {
     cudaStreamSynchronize(c->side_stream);

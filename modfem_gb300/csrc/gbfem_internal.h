@@ -275,7 +275,7 @@ struct gbfem_ctx_s {
   // matrix, small arrays and state, the captured restart cycle
   gbfem::DevBuf<int> sell_off, sell_col;
   gbfem::DevBuf<double> sell_val, gm_small;
-  gbfem::DevBuf<float2> sell_valdw;
+  gbfem::DevBuf<float2> sell_valdw, gm_xdw;
   gbfem::DevBuf<short> sell_col16;  // columns relative to the row, where they fit in 16 bits
   bool sell_ready = false, std_spmv_dword = false, sell_cols16 = false;
   int sell_n = 0;

@@ -121,6 +121,40 @@ __device__ __forceinline__ void sell_acc(dw &acc, float2 a, double x) { acc = t_
 __device__ __forceinline__ double sell_out(double acc) { return acc; }
 __device__ __forceinline__ double sell_out(dw acc) { return dw_to_double(acc); }
 
+// double-word form: values and the vector both as float pairs (the vector's
+// pair copy is written where the Arnoldi vector is formed), products summed
+// exactly (TwoProd) with their errors collected (DwAcc), two accumulators
+// (even and odd entries) so that the TwoSum chains overlap
+template <typename CT>
+__device__ __forceinline__ double sell_row_dw(const float2 *__restrict__ v, const CT *__restrict__ col, int w,
+                                              int base, const float2 *__restrict__ x) {
+  constexpr int U = 8;
+  DwAcc acc0 = {0.0f, 0.0f, 0.0f}, acc1 = {0.0f, 0.0f, 0.0f};
+  int j = 0;
+  for (; j + U <= w; j += U) {
+    float2 a[U], xv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) a[u] = sell_ld(v + u * SELL_C);
+#pragma unroll
+    for (int u = 0; u < U; u++) xv[u] = __ldg(x + sell_col(col + u * SELL_C, base));
+#pragma unroll
+    for (int u = 0; u < U; u += 2) {
+      dwacc_prod(acc0, a[u], xv[u]);
+      dwacc_prod(acc1, a[u + 1], xv[u + 1]);
+    }
+    v += U * SELL_C;
+    col += U * SELL_C;
+  }
+  for (; j < w; j++) {
+    dwacc_prod(acc0, sell_ld(v), __ldg(x + sell_col(col, base)));
+    v += SELL_C;
+    col += SELL_C;
+  }
+  dwacc_fold(acc0);
+  dwacc_fold(acc1);
+  return dw_to_double(dw(acc0.h, acc0.l) + dw(acc1.h, acc1.l));
+}
+
 template <typename VT, typename CT>
 __device__ __forceinline__ double sell_row(const VT *__restrict__ v, const CT *__restrict__ col, int w, int base,
                                            const double *__restrict__ x) {
@@ -165,6 +199,7 @@ struct GmArgs {
   const float2 *sell_valdw;
   const double *dinv, *b;
   double *x, *V, *tmp, *H, *cs, *sn, *s, *y, *hcol, *partial;
+  float2 *xdw;  // double-word copy of the current Arnoldi vector (double-word SpMV only)
   GmState *st;
 };
 
@@ -265,8 +300,11 @@ __global__ void __launch_bounds__(GM_T) gm_start_cycle(GmArgs a) {
   const GmState &S = *a.st;
   if (S.phase != GM_ARNOLDI || S.j != 0) return;
   const double inv = 1.0 / S.beta;
-  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T)
-    a.V[i] = a.tmp[i] * inv;
+  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T) {
+    const double v = a.tmp[i] * inv;
+    a.V[i] = v;
+    if (a.xdw) a.xdw[i] = dw_f2(v);
+  }
 }
 
 // V[j+1] = dinv A V[j]
@@ -279,7 +317,11 @@ __global__ void __launch_bounds__(GM_T) gm_arnoldi_spmv(GmArgs a, const VT *__re
   if (s >= a.nslices) return;
   const int r = s * SELL_C + l;
   const int o = a.sell_off[s], w = (a.sell_off[s + 1] - o) / SELL_C;
-  const double acc = sell_row(sv + o + l, scol + o + l, w, sell_base(r, a.n), a.V + (size_t)j * a.n);
+  double acc;
+  if constexpr (std::is_same<VT, float2>::value)
+    acc = sell_row_dw(sv + o + l, scol + o + l, w, sell_base(r, a.n), a.xdw);
+  else
+    acc = sell_row(sv + o + l, scol + o + l, w, sell_base(r, a.n), a.V + (size_t)j * a.n);
   if (r < a.n) a.V[(size_t)(j + 1) * a.n + r] = a.dinv[r] * acc;
 }
 
@@ -372,8 +414,11 @@ __global__ void __launch_bounds__(GM_T) gm_normalize(GmArgs a, int j) {
   if (S.phase != GM_ARNOLDI || S.j != j + 1) return;
   double *w = a.V + (size_t)(j + 1) * a.n;
   const double inv = 1.0 / S.hn;
-  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T)
-    w[i] *= inv;
+  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T) {
+    const double v = w[i] * inv;
+    w[i] = v;
+    if (a.xdw) a.xdw[i] = dw_f2(v);
+  }
 }
 
 // x += V[:, :done] y at the end of a cycle
@@ -561,6 +606,10 @@ int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int 
   a.y = y;
   a.hcol = hcol;
   a.partial = c->partial.p;
+  if (c->std_spmv_dword) {
+    GB_TRY(c->gm_xdw.alloc(n));
+    a.xdw = c->gm_xdw.p;
+  }
   a.st = state;
   if (ini_zero)
     GB_CUDA(cudaMemsetAsync(c->x.p, 0, (size_t)n * sizeof(double), st));
