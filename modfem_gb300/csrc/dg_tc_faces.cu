@@ -18,8 +18,8 @@
 // accumulation is exact, and
 //   D = 2^(ea_j + eb_i) sum_d C_d 2^(-8(d+2))
 // is recombined in int64 and rounded once to FP64 on the integer pipe.
-// The owner's diagonal-block share of each face is added (face by face, one
-// thread per entry) to the block the volume kernel wrote; the off-diagonal block
+// The owner's diagonal-block share is summed over its faces in FP64 registers
+// and added once to the block the volume kernel wrote; the off-diagonal block
 // (e, neighbour) is written whole, as in the FP64 kernel (deterministic, no
 // atomics).  Covers owners of degree <= 3 whose neighbours all have degree
 // <= 3 (2 nq <= 32); the others keep the FP64 face kernel.
@@ -63,9 +63,8 @@ constexpr int TF_NQ = 16;         // face points of the largest rule with max(p1
 constexpr int TF_NF = 5;          // faces of a prism
 constexpr int TF_M = 128;         // MMA M
 constexpr int TF_THREADS = 256;
-constexpr int TF_TMEM_COLS = 128;  // three CTAs per SM share the 512 columns
-constexpr int TF_NCH = 16;         // MMA N per chunk of e's functions: 7 x 16 accumulator columns
-constexpr int TF_CTAS = 3;         // CTAs per SM (TMEM, shared memory and registers are sized for it)
+constexpr int TF_TMEM_COLS = 256;  // two CTAs per SM share the 512 columns
+constexpr int TF_NCH = 32;         // MMA N per chunk of e's functions: 7 x 32 accumulator columns
 constexpr int TF_GEO = 8;    // per face point: f a, c a, v1 (3), v2 (3)
 static_assert((long long)TF_SL * TF_KP * 255 * 255 < (1LL << 24), "slice sums must stay exact in FP32");
 
@@ -84,14 +83,15 @@ struct TfDims {
   static constexpr int OFF_B = A_BYTES;
   static constexpr int OFF_FACE = OFF_B + TF_SL * B_SLICE;                 // [TF_NF][TF_NQ][TF_GEO]
   static constexpr int FACE_DOUBLES = TF_NQ * TF_GEO;
-  static constexpr int OFF_RACC = OFF_FACE + TF_NF * FACE_DOUBLES * 8;     // [NS] boundary rhs sums
+  static constexpr int OFF_DIAG = OFF_FACE + TF_NF * FACE_DOUBLES * 8;     // [NS][SD_LD] diagonal-block share
+  static constexpr int SD_LD = NS + 1;                                     // odd row stride
+  static constexpr int OFF_RACC = OFF_DIAG + NS * SD_LD * 8;               // [NS] boundary rhs sums
   static constexpr int OFF_HF = OFF_RACC + 64 * 8;
   static constexpr int OFF_INT = (OFF_HF + TF_NF * (int)sizeof(DgHalfFace) + 15) / 16 * 16;  // ea, eb, bar, slot
   static constexpr int SMEM = OFF_INT + (128 + 64) * 4 + 64;
   static constexpr int NCHUNK = (NPAD + TF_NCH - 1) / TF_NCH;
   static_assert(TF_SL * (NPAD < TF_NCH ? NPAD : TF_NCH) <= TF_TMEM_COLS, "accumulators fit the TMEM allocation");
-  static_assert(TF_CTAS * (SMEM + 1024) <= 228 * 1024, "shared memory of TF_CTAS CTAs per SM");
-  static_assert(TF_CTAS * TF_TMEM_COLS <= 512, "TMEM of TF_CTAS CTAs per SM");
+  static_assert(SMEM <= 113 * 1024, "shared memory of two CTAs per SM");
   static_assert(OFF_B % 1024 == 0 && OFF_HF % 16 == 0 && OFF_INT % 16 == 0, "alignment");
   static_assert(ROWS <= TF_M && NS <= 64, "rows");
 };
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(128) dg_face_geometry_kernel(
 }
 
 template <int P>
-__global__ void __launch_bounds__(TF_THREADS, TF_CTAS) dg_tc_faces_kernel(
+__global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const double *__restrict__ geo, const double *__restrict__ ftab,
     const long long *__restrict__ ftab_off, double gval, const long long *__restrict__ boff_diag,
@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(TF_THREADS, TF_CTAS) dg_tc_faces_kernel(
   uint8_t *asl = smem, *bsl = smem + Dm::OFF_B;
   double *sface = (double *)(smem + Dm::OFF_FACE);   // [TF_NF][TF_NQ][TF_GEO]
   double *sRacc = (double *)(smem + Dm::OFF_RACC);   // [NS]
+  double *sD = (double *)(smem + Dm::OFF_DIAG);      // [NS][SD_LD]: row r (trial function), column i
   DgHalfFace *sHF = (DgHalfFace *)(smem + Dm::OFF_HF);
   int *ea = (int *)(smem + Dm::OFF_INT);             // A row exponents (by row = M row)
   int *eb = ea + 128;                                // B row exponents
@@ -297,9 +298,7 @@ __global__ void __launch_bounds__(TF_THREADS, TF_CTAS) dg_tc_faces_kernel(
   }
   if (tid < nf) sHF[tid] = hf[h0 + tid];
   if (tid < NS) sRacc[tid] = 0.0;
-  // the diagonal block (column-major: entry (i, r) at i + NS r), written by
-  // the volume kernel; this CTA adds each face's share in face order
-  double *dblk = val + boff_diag[e];
+  for (int t = tid; t < NS * Dm::SD_LD; t += TF_THREADS) sD[t] = 0.0;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
                  "r"(TF_TMEM_COLS));
@@ -484,7 +483,7 @@ __global__ void __launch_bounds__(TF_THREADS, TF_CTAS) dg_tc_faces_kernel(
             for (int d = 4; d < TF_SL; d++) lo = lo * 256 + (long long)__float2int_rn(C[d][c]);
             const double v = tf_i64_scaled(hi * 16384LL + (lo >> 10), sa + eb[i] - 54);
             if (r_ep < NS)
-              dblk[i + (size_t)NS * r_ep] += v;
+              sD[r_ep * Dm::SD_LD + i] += v;
             else
               oblk[i + (size_t)NS * (r_ep - NS)] = v;
           }
@@ -502,6 +501,11 @@ __global__ void __launch_bounds__(TF_THREADS, TF_CTAS) dg_tc_faces_kernel(
   if (failed || bad_input) {
     if (tid == 0) atomicExch(err, failed ? 6 : 7);
     return;
+  }
+  {
+    // the diagonal block is column-major (entry (i, r) at i + NS r): sD's row r
+    double *dblk = val + boff_diag[e];
+    for (int t = tid; t < NS * NS; t += TF_THREADS) dblk[t] += sD[(t / NS) * Dm::SD_LD + t % NS];
   }
   if (tid < NS) rhs[roff[e] + tid] += sRacc[tid];
 }
