@@ -141,6 +141,7 @@ int gbfem_destroy(gbfem_ctx c) {
   c->dg_ftab.release();
   c->dg_tcface.release();
   c->dg_fgeo.release();
+  c->dg_fshare.release();
   cudaEventDestroy(c->ev0);
   cudaEventDestroy(c->ev1);
   cudaEventDestroy(c->ev2);
@@ -1069,7 +1070,47 @@ int gbfem_dg_assemble(gbfem_ctx c) {
   // cores do not cover
   const bool dwv = c->dg_volume_mode == GBFEM_DG_VOLUME_DWORD || c->dg_volume_mode == GBFEM_DG_VOLUME_TC_DWORD;
   if (tc) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+  const bool tcf = c->dg_face_mode == GBFEM_DG_FACE_TC || c->dg_face_mode == GBFEM_DG_FACE_TC_DWORD;
+  // Tensor-core faces beside a volume kernel on the CUDA cores (FP64 or
+  // double word): the face kernel runs on the side stream from the start,
+  // its diagonal-block and rhs shares go to scratch and are added once both
+  // are done (the result is the same as in sequence: volume block + share).
+  // The face kernel is latency bound at two CTAs per SM (its TMEM), which
+  // leaves room for a volume CTA beside them.
+  const bool overlap = tcf && !tc && c->dg_ftab_ok && c->dg_hf.p && c->nv == GBFEM_PRISM;
+  long long share_off[5] = {0, 0, 0, 0, 0};
+  if (overlap) {
+    GB_TRY(ensure_side(c));
+    GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+    long long tot = 0;
+    for (int p = 1; p <= 3; p++) {
+      share_off[p] = tot;
+      const long long ns = dg_ns(c, p);
+      tot += (long long)c->dg_flist_tc[p].n * (ns * ns + ns);
+    }
+    GB_TRY(c->dg_fshare.alloc((size_t)std::max(tot, 1LL)));
+    GB_TRY(c->dg_fgeo.alloc((size_t)c->dg_nfa * 16 * 8));
+  }
   cudaEventRecord(c->ev0, c->stream);
+  if (overlap) {
+    GB_CUDA(cudaEventRecord(c->side_ev[0], c->stream));
+    GB_CUDA(cudaStreamWaitEvent(c->side_stream, c->side_ev[0], 0));
+    int r = gbfem::launch_dg_face_geometry(c->side_stream, (int)c->dg_tcface.n, c->dg_tcface.p, c->dg_hf.p,
+                                           c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->dg_pen,
+                                           c->dg_fgeo.p);
+    GB_TRY(r);
+    launches += r;
+    for (int p = 1; p <= 3; p++) {
+      if (!c->dg_flist_tc[p].p) continue;
+      r = gbfem::launch_dg_tc_faces(c->side_stream, p, (int)c->dg_flist_tc[p].n, c->dg_flist_tc[p].p,
+                                    c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->dg_fgeo.p, c->dg_ftab.p,
+                                    c->dg_ftab_off.p, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,
+                                    c->dg_rhs.p, c->err.p, c->dg_fshare.p + share_off[p]);
+      GB_TRY(r);
+      launches += r;
+    }
+    GB_CUDA(cudaEventRecord(c->side_ev[1], c->side_stream));
+  }
   for (int p = 1; p <= 4; p++) {
     if (!c->dg_list[p].p) continue;
     int r;
@@ -1091,10 +1132,20 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     launches += r;
   }
   cudaEventRecord(c->ev2, c->stream);
-  const bool tcf = c->dg_face_mode == GBFEM_DG_FACE_TC || c->dg_face_mode == GBFEM_DG_FACE_TC_DWORD;
   bool geo_done = false;
+  if (overlap) {
+    // the shares of the tensor-core owners, then the other owners below
+    GB_CUDA(cudaStreamWaitEvent(c->stream, c->side_ev[1], 0));
+    for (int p = 1; p <= 3; p++) {
+      const int r = gbfem::launch_dg_face_share_add(c->stream, p, (int)c->dg_flist_tc[p].n, c->dg_flist_tc[p].p,
+                                                    c->dg_fshare.p + share_off[p], c->dg_boff_diag_d.p,
+                                                    c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
+      GB_TRY(r);
+      launches += r;
+    }
+  }
   if (c->dg_hf.p) {
-    if (tcf && !tc) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+    if (tcf && !tc && !overlap) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
     for (int p = 1; p <= 4; p++) {
       if (!c->dg_list[p].p) continue;
       if (c->nv == GBFEM_TETRA) {
@@ -1109,10 +1160,11 @@ int gbfem_dg_assemble(gbfem_ctx c) {
         continue;
       }
       if (tcf && c->dg_ftab_ok) {
-        // tensor-core eligible owners, then the rest on the FP64 (or, in
-        // TC_DWORD mode, the double-word) kernel; running the two side by
-        // side on disjoint owners was slower (167 vs 157 ms at p = 3, 432k)
-        if (!geo_done) {
+        // tensor-core eligible owners (done above when overlapped), then the
+        // rest on the FP64 (or, in TC_DWORD mode, the double-word) kernel;
+        // running those two side by side on disjoint owners was slower (167
+        // vs 157 ms at p = 3, 432k)
+        if (!overlap && !geo_done) {
           // per-point geometry of every face between degree <= 3 elements,
           // once per face (both owners read it)
           GB_TRY(c->dg_fgeo.alloc((size_t)c->dg_nfa * 16 * 8));
@@ -1123,12 +1175,15 @@ int gbfem_dg_assemble(gbfem_ctx c) {
           launches += r;
           geo_done = true;
         }
-        int r = gbfem::launch_dg_tc_faces(c->stream, p, (int)c->dg_flist_tc[p].n, c->dg_flist_tc[p].p,
-                                          c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->dg_fgeo.p, c->dg_ftab.p,
-                                          c->dg_ftab_off.p, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p,
-                                          c->dg_val.p, c->dg_rhs.p, c->err.p);
-        GB_TRY(r);
-        launches += r;
+        int r = 0;
+        if (!overlap) {
+          r = gbfem::launch_dg_tc_faces(c->stream, p, (int)c->dg_flist_tc[p].n, c->dg_flist_tc[p].p,
+                                        c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->dg_fgeo.p, c->dg_ftab.p,
+                                        c->dg_ftab_off.p, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p,
+                                        c->dg_val.p, c->dg_rhs.p, c->err.p, nullptr);
+          GB_TRY(r);
+          launches += r;
+        }
         r = gbfem::launch_dg_prism_faces(c->stream, p, (int)c->dg_flist_64[p].n, c->dg_flist_64[p].p, c->dg_hf_ptr.p,
                                          c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p,
                                          c->dg_pen, c->g, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,

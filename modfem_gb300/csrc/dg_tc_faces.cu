@@ -66,6 +66,7 @@ constexpr int TF_THREADS = 256;
 constexpr int TF_TMEM_COLS = 256;  // two CTAs per SM share the 512 columns
 constexpr int TF_NCH = 32;         // MMA N per chunk of e's functions: 7 x 32 accumulator columns
 constexpr int TF_GEO = 8;    // per face point: f a, c a, v1 (3), v2 (3)
+constexpr int TF_GEOS = 9;   // their stride in shared memory: odd, so the 16 points of a row segment hit distinct banks
 static_assert((long long)TF_SL * TF_KP * 255 * 255 < (1LL << 24), "slice sums must stay exact in FP32");
 
 template <int P>
@@ -81,8 +82,8 @@ struct TfDims {
   static constexpr int A_BYTES = (TF_SL - 1) * A_STRIDE + TF_M * TF_KP * 2;
   static constexpr int B_SLICE = NPAD * TF_KP * 2;
   static constexpr int OFF_B = A_BYTES;
-  static constexpr int OFF_FACE = OFF_B + TF_SL * B_SLICE;                 // [TF_NF][TF_NQ][TF_GEO]
-  static constexpr int FACE_DOUBLES = TF_NQ * TF_GEO;
+  static constexpr int OFF_FACE = OFF_B + TF_SL * B_SLICE;                 // [TF_NF][TF_NQ][TF_GEOS]
+  static constexpr int FACE_DOUBLES = TF_NQ * TF_GEOS;
   static constexpr int OFF_DIAG = OFF_FACE + TF_NF * FACE_DOUBLES * 8;     // [NS][SD_LD] diagonal-block share
   static constexpr int SD_LD = NS + 1;                                     // odd row stride
   static constexpr int OFF_RACC = OFF_DIAG + NS * SD_LD * 8;               // [NS] boundary rhs sums
@@ -269,12 +270,13 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const double *__restrict__ geo, const double *__restrict__ ftab,
     const long long *__restrict__ ftab_off, double gval, const long long *__restrict__ boff_diag,
-    const int *__restrict__ roff, double *__restrict__ val, double *__restrict__ rhs, int *err) {
+    const int *__restrict__ roff, double *__restrict__ val, double *__restrict__ rhs, int *err,
+    double *__restrict__ share) {
   using Dm = TfDims<P>;
   constexpr int NS = Dm::NS, NPAD = Dm::NPAD, FD = Dm::FACE_DOUBLES;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *asl = smem, *bsl = smem + Dm::OFF_B;
-  double *sface = (double *)(smem + Dm::OFF_FACE);   // [TF_NF][TF_NQ][TF_GEO]
+  double *sface = (double *)(smem + Dm::OFF_FACE);   // [TF_NF][TF_NQ][TF_GEOS]
   double *sRacc = (double *)(smem + Dm::OFF_RACC);   // [NS]
   double *sD = (double *)(smem + Dm::OFF_DIAG);      // [NS][SD_LD]: row r (trial function), column i
   DgHalfFace *sHF = (DgHalfFace *)(smem + Dm::OFF_HF);
@@ -310,10 +312,9 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
   const uint32_t tmem = *tmem_slot;
 
   // ---- the per-point geometry of all the element's faces ----
-  for (int t = tid; t < nf * FD / 2; t += TF_THREADS) {
-    const int f = t / (FD / 2), r = t % (FD / 2);
-    reinterpret_cast<double2 *>(sface + f * FD)[r] =
-        reinterpret_cast<const double2 *>(geo + (size_t)sHF[f].face * FD)[r];
+  for (int t = tid; t < nf * TF_NQ * TF_GEO; t += TF_THREADS) {
+    const int f = t / (TF_NQ * TF_GEO), r = t % (TF_NQ * TF_GEO);
+    sface[f * FD + (r / TF_GEO) * TF_GEOS + r % TF_GEO] = geo[(size_t)sHF[f].face * TF_NQ * TF_GEO + r];
   }
   // (the per-face loop starts with a barrier)
 
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
         const double *tb = (own ? tab_own : tab_nb) + ((size_t)q * (own ? NS : ns_nb) + jj) * 4;
         const double2 t01 = __ldg(reinterpret_cast<const double2 *>(tb));
         const double2 t23 = __ldg(reinterpret_cast<const double2 *>(tb) + 1);
-        const double *G = sGeo + q * TF_GEO;
+        const double *G = sGeo + q * TF_GEOS;
         const double *v = G + (side == 1 ? 2 : 5);
         const double phi = t01.x;
         const double g = fma(v[0], t01.y, fma(v[1], t23.x, v[2] * t23.y));
@@ -502,6 +503,14 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
     if (tid == 0) atomicExch(err, failed ? 6 : 7);
     return;
   }
+  if (share) {
+    // the diagonal-block and rhs shares to this owner's scratch slot: the
+    // volume kernel may still be writing the block (it runs alongside)
+    double *sd = share + (size_t)bi * (NS * NS + NS);
+    for (int t = tid; t < NS * NS; t += TF_THREADS) sd[t] = sD[(t / NS) * Dm::SD_LD + t % NS];
+    if (tid < NS) sd[NS * NS + tid] = sRacc[tid];
+    return;
+  }
   {
     // the diagonal block is column-major (entry (i, r) at i + NS r): sD's row r
     double *dblk = val + boff_diag[e];
@@ -512,10 +521,40 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
 
 bool dg_tc_faces_supported(int p) { return p >= 1 && p <= 3; }
 
+// The owners' diagonal-block and rhs shares from scratch (one slot of
+// NS^2 + NS values per owner, in list order) added to the blocks and rows the
+// volume kernel wrote: one block per owner.
+template <int NS>
+__global__ void __launch_bounds__(256) dg_face_share_add_kernel(int count, const int *__restrict__ ent_el,
+                                                                const double *__restrict__ share,
+                                                                const long long *__restrict__ boff_diag,
+                                                                const int *__restrict__ roff, double *__restrict__ val,
+                                                                double *__restrict__ rhs) {
+  const int bi = blockIdx.x;
+  if (bi >= count) return;
+  const int e = ent_el[bi];
+  const double *sd = share + (size_t)bi * (NS * NS + NS);
+  double *dblk = val + boff_diag[e];
+  for (int t = threadIdx.x; t < NS * NS; t += blockDim.x) dblk[t] += sd[t];
+  if (threadIdx.x < NS) rhs[roff[e] + threadIdx.x] += sd[NS * NS + threadIdx.x];
+}
+
+int launch_dg_face_share_add(cudaStream_t st, int p, int count, const int *ent_el, const double *share,
+                             const long long *boff_diag, const int *roff, double *val, double *rhs) {
+  if (count <= 0) return 0;
+  switch (p) {
+    case 1: dg_face_share_add_kernel<6><<<count, 256, 0, st>>>(count, ent_el, share, boff_diag, roff, val, rhs); break;
+    case 2: dg_face_share_add_kernel<18><<<count, 256, 0, st>>>(count, ent_el, share, boff_diag, roff, val, rhs); break;
+    default: dg_face_share_add_kernel<40><<<count, 256, 0, st>>>(count, ent_el, share, boff_diag, roff, val, rhs); break;
+  }
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
 int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                        const DgHalfFace *hf, const int *el_p, const double *geo, const double *ftab,
                        const long long *ftab_off, double g, const long long *boff_diag, const int *roff,
-                       double *val, double *rhs, int *err) {
+                       double *val, double *rhs, int *err, double *share) {
   if (count <= 0) return 0;
   GB_CHECK(dg_tc_faces_supported(p), "tensor-core DG face kernel covers p = 1..3");
   GB_CHECK(geo && ftab && ftab_off, "tensor-core DG faces need the face geometry and basis tables");
@@ -524,7 +563,7 @@ int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, con
     const int smem = TfDims<PP>::SMEM;                                                                        \
     GB_CUDA(cudaFuncSetAttribute(dg_tc_faces_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
     dg_tc_faces_kernel<PP><<<count, TF_THREADS, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, geo, ftab,       \
-                                                            ftab_off, g, boff_diag, roff, val, rhs, err);     \
+                                                            ftab_off, g, boff_diag, roff, val, rhs, err, share); \
   }
   switch (p) {
     case 1: GB_TF_LAUNCH(1); break;

@@ -170,10 +170,16 @@ int launch_dg_face_tables(cudaStream_t st, int ncfg, const unsigned char *cfg, c
 int launch_dg_face_geometry(cudaStream_t st, int count, const int *faces_hf, const DgHalfFace *hf,
                             const int *el_p, const int *el_nodes, const double *xyz, const double *k_el,
                             const double *D_el, double pen, double *geo);
+// share == NULL: each owner's diagonal-block and rhs shares are added to its
+// block and rows; else they are stored in the owner's slot of share (NS^2 +
+// NS values, list order) for launch_dg_face_share_add, so that the kernel may
+// run beside the volume kernel that writes those blocks
 int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                        const DgHalfFace *hf, const int *el_p, const double *geo, const double *ftab,
                        const long long *ftab_off, double g, const long long *boff_diag, const int *roff,
-                       double *val, double *rhs, int *err);
+                       double *val, double *rhs, int *err, double *share);
+int launch_dg_face_share_add(cudaStream_t st, int p, int count, const int *ent_el, const double *share,
+                             const long long *boff_diag, const int *roff, double *val, double *rhs);
 int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, const int *hf_ptr,
                           const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                           const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
@@ -308,7 +314,7 @@ struct gbfem_ctx_s {
   // per-point geometry
   gbfem::DevBuf<unsigned char> dg_fcfg;
   gbfem::DevBuf<long long> dg_ftab_off;
-  gbfem::DevBuf<double> dg_ftab, dg_fgeo;
+  gbfem::DevBuf<double> dg_ftab, dg_fgeo, dg_fshare;
   gbfem::DevBuf<int> dg_tcface;
   bool dg_ftab_ok = false;
   // DG block Jacobi: inverted diagonal blocks, block e at dg_dinv_off_d[e]
