@@ -66,7 +66,6 @@ constexpr int TF_THREADS = 256;
 constexpr int TF_TMEM_COLS = 256;  // two CTAs per SM share the 512 columns
 constexpr int TF_NCH = 32;         // MMA N per chunk of e's functions: 7 x 32 accumulator columns
 constexpr int TF_GEO = 8;    // per face point: f a, c a, v1 (3), v2 (3)
-constexpr int TF_SPAD = 32;  // padding between operand slices (bytes)
 constexpr int TF_GEOS = 9;   // their stride in shared memory: odd, so the 16 points of a row segment hit distinct banks
 static_assert((long long)TF_SL * TF_KP * 255 * 255 < (1LL << 24), "slice sums must stay exact in FP32");
 
@@ -79,14 +78,9 @@ struct TfDims {
   // A slices packed ROWS8 rows apart: the M = 128 rows an MMA reads beyond a
   // slice's own rows belong to the next slice (or the tail) and only feed D
   // rows that are discarded
-  // Slices TF_SPAD bytes apart beyond their data: slice i starts 8 i banks
-  // further, and the operand pass stores slice (q / 4 + k) mod 7 of the
-  // (row, point) pair in its k-th store, so that the 32 words of a store
-  // (two rows, 16 points: 8 core-matrix rows x 4 words, repeated over the 4
-  // K blocks 128 bytes apart) fall on 32 different banks
-  static constexpr int A_STRIDE = ROWS8 * TF_KP * 2 + TF_SPAD;
-  static constexpr int A_BYTES = ((TF_SL - 1) * A_STRIDE + TF_M * TF_KP * 2 + 1023) / 1024 * 1024;
-  static constexpr int B_SLICE = NPAD * TF_KP * 2 + TF_SPAD;
+  static constexpr int A_STRIDE = ROWS8 * TF_KP * 2;
+  static constexpr int A_BYTES = (TF_SL - 1) * A_STRIDE + TF_M * TF_KP * 2;
+  static constexpr int B_SLICE = NPAD * TF_KP * 2;
   static constexpr int OFF_B = A_BYTES;
   static constexpr int OFF_FACE = OFF_B + TF_SL * B_SLICE;                 // [TF_NF][TF_NQ][TF_GEOS]
   static constexpr int FACE_DOUBLES = TF_NQ * TF_GEOS;
@@ -409,8 +403,7 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
           const uint32_t h1 = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
           const bool n0 = __double_as_longlong(a0) < 0, n1 = __double_as_longlong(a1) < 0;
 #pragma unroll
-          for (int k = 0; k < TF_SL; k++) {
-            const int i = (q >> 2) + k < TF_SL ? (q >> 2) + k : (q >> 2) + k - TF_SL;  // rotated slice order
+          for (int i = 0; i < TF_SL; i++) {
             const uint32_t c0 = i < 4 ? (h0 >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
             const uint32_t c1 = i < 4 ? (h1 >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
             *(uint32_t *)(asl + i * Dm::A_STRIDE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
@@ -422,8 +415,7 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
           const uint32_t h1 = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
           const bool n0 = __double_as_longlong(b0) < 0, n1 = __double_as_longlong(b1) < 0;
 #pragma unroll
-          for (int k = 0; k < TF_SL; k++) {
-            const int i = (q >> 2) + k < TF_SL ? (q >> 2) + k : (q >> 2) + k - TF_SL;
+          for (int i = 0; i < TF_SL; i++) {
             const uint32_t c0 = i < 4 ? (h0 >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
             const uint32_t c1 = i < 4 ? (h1 >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
             *(uint32_t *)(bsl + i * Dm::B_SLICE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
