@@ -502,10 +502,21 @@ int gbfem_server_result(gbfem_server srv, long long id, double *x, long long nx,
                         double *times);
 /* Forgets a finished request's result. */
 int gbfem_server_release(gbfem_server srv, long long id);
+/* Cancels a request: a queued or prepared one leaves at once, one being
+ * prepared or solved at the end of its preparation or at the engine's next
+ * poll; its device memory returns to the budget and gbfem_server_wait then
+ * reports it failed ("cancelled").  Returns 0, or 1 when the request had
+ * already finished, failed or been cancelled. */
+int gbfem_server_cancel(gbfem_server srv, long long id);
 /* GBFEM_SERVE_OPT_STEPS_PER_POLL: engine steps launched between two host
  * reads of the requests' phases (1..64, default 4): fewer host round trips
- * against up to that many idle steps for a request that has finished. */
+ * against up to that many idle steps for a request that has finished.
+ * GBFEM_SERVE_OPT_FAIL_PREPARATIONS: the next `value` request preparations
+ * fail as a device allocation would ("injected allocation failure"), before
+ * any device work; for testing how callers and the admission accounting
+ * handle failed requests (the failure is made on the host). */
 #define GBFEM_SERVE_OPT_STEPS_PER_POLL 1
+#define GBFEM_SERVE_OPT_FAIL_PREPARATIONS 2
 int gbfem_server_set_option(gbfem_server srv, int option, long long value);
 /* stats[8]: engine steps, kernel launches, peak active requests, peak
  * bytes charged, budget, bytes charged now, queued, active. */

@@ -94,6 +94,7 @@ SIGNATURES = [
     ("gbfem_server_wait", _ci, [_vp, _cll, _cd]),
     ("gbfem_server_result", _ci, [_vp, _cll, _vp, _cll, _pi, _pd, _vp]),
     ("gbfem_server_release", _ci, [_vp, _cll]),
+    ("gbfem_server_cancel", _ci, [_vp, _cll]),
     ("gbfem_server_set_option", _ci, [_vp, _ci, _cll]),
     ("gbfem_server_stats", _ci, [_vp, _vp]),
     ("gbfem_serve_footprint", _cll, [_vp]),

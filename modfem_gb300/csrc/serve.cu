@@ -354,7 +354,8 @@ struct SrvRequest {
   std::vector<int> el, bf_el, bf_side, fa_type, fa_bc, fa_el, fa_side, fa_nodes;
   long long footprint = 0, charged = 0;
   double t_submit = 0, t_admit = 0, t_ready = 0, t_start = 0, t_done = 0;
-  int status = 0;  // 0 queued, 1 preparing, 2 ready, 3 solving, 4 done, -1 failed
+  int status = 0;  // 0 queued, 1 preparing, 2 ready, 3 solving, 4 done, -1 failed, -2 cancelled
+  bool cancel = false;  // cancellation asked while preparing or solving
   std::string err;
   gbfem_ctx ctx = nullptr;
   DevBuf<double> kry;
@@ -424,6 +425,7 @@ struct gbfem_server_s {
   long long steps = 0, launches = 0;
   int peak_active = 0;
   int steps_per_poll = 4;
+  int inject_prep_failures = 0;  // GBFEM_SERVE_OPT_FAIL_PREPARATIONS
   std::string fatal;
 };
 
@@ -455,6 +457,16 @@ void try_admit(gbfem_server s) {  // caller holds s->mu
 }
 
 int prepare(gbfem_server s, SrvRequest &r) {
+  {
+    // host-side fault injection: this preparation fails as a device
+    // allocation would, before any device work
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->inject_prep_failures > 0) {
+      s->inject_prep_failures--;
+      gbfem::set_error("injected allocation failure (GBFEM_SERVE_OPT_FAIL_PREPARATIONS)");
+      return -1;
+    }
+  }
   gbfem_ctx c = nullptr;
   int rc = gbfem_create(&c, s->device);
   if (rc < 0) return rc;
@@ -533,9 +545,9 @@ void prep_worker(gbfem_server s) {
     std::unique_lock<std::mutex> lk(s->mu);
     s->n_preparing--;
     r->t_ready = now_s();
-    if (rc < 0) {
-      r->status = -1;
-      r->err = gbfem_last_error();
+    if (rc < 0 || r->cancel) {
+      r->status = rc < 0 ? -1 : -2;
+      r->err = rc < 0 ? gbfem_last_error() : "cancelled";
       if (r->ctx) gbfem_destroy(r->ctx);
       r->ctx = nullptr;
       r->kry.release();
@@ -716,14 +728,18 @@ int capture(gbfem_server s, SrvLane &ln) {
   return 0;
 }
 
-void retire(gbfem_server s, SrvLane &ln, int i) {
+// A finished (or cancelled) request leaves its slot; the lane is idle here
+// (its last poll completed), so nothing of it is in flight.
+void retire(gbfem_server s, SrvLane &ln, int i, bool cancelled = false) {
   ReqPtr r = s->slots[i];
   const SrvState &S = ln.h_state[i];
-  r->x.resize(r->n);
-  cudaMemcpyAsync(r->x.data(), r->kry.p, (size_t)r->n * sizeof(double), cudaMemcpyDeviceToHost, ln.stream);
-  cudaStreamSynchronize(ln.stream);
-  r->iters = S.it;
-  r->rel = S.beta0 > 0 ? S.resid / S.beta0 : 0.0;
+  if (!cancelled) {
+    r->x.resize(r->n);
+    cudaMemcpyAsync(r->x.data(), r->kry.p, (size_t)r->n * sizeof(double), cudaMemcpyDeviceToHost, ln.stream);
+    cudaStreamSynchronize(ln.stream);
+    r->iters = S.it;
+    r->rel = S.beta0 > 0 ? S.resid / S.beta0 : 0.0;
+  }
   gbfem_destroy(r->ctx);
   r->ctx = nullptr;
   r->kry.release();
@@ -731,7 +747,8 @@ void retire(gbfem_server s, SrvLane &ln, int i) {
   std::lock_guard<std::mutex> lk(s->mu);
   s->in_use -= r->charged;
   r->charged = 0;
-  r->status = 4;
+  r->status = cancelled ? -2 : 4;
+  if (cancelled) r->err = "cancelled";
   r->t_done = now_s();
   s->n_active--;
   ln.held--;
@@ -793,11 +810,17 @@ void engine_loop(gbfem_server s) {
         }
         ln.busy = false;
         progressed = true;
-        for (int i : std::vector<int>(ln.act))
-          if (ln.h_state[i].phase == gbfem::PH_DONE) {
-            retire(s, ln, i);
+        for (int i : std::vector<int>(ln.act)) {
+          bool cancelled;
+          {
+            std::lock_guard<std::mutex> lk(s->mu);
+            cancelled = s->slots[i]->cancel;
+          }
+          if (ln.h_state[i].phase == gbfem::PH_DONE || cancelled) {
+            retire(s, ln, i, cancelled);
             ln.changed = true;
           }
+        }
       }
       if (ln.changed) {
         if (rebuild(s, ln, L) < 0 || capture(s, ln) < 0) {
@@ -1025,6 +1048,36 @@ int gbfem_server_result(gbfem_server s, long long id, double *x, long long nx, i
   return (int)r.x.size();
 }
 
+int gbfem_server_cancel(gbfem_server s, long long id) {
+  GB_CHECK(s, "null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  GB_CHECK(it != s->reqs.end(), "unknown request id");
+  ReqPtr r = it->second;
+  if (r->status == 4 || r->status < 0) return 1;  // finished, failed or cancelled already
+  if (r->status == 0) {  // queued: leaves the queue now
+    auto &q = s->lanes[r->kind].waitq;
+    q.erase(std::remove(q.begin(), q.end(), r), q.end());
+  } else if (r->status == 2) {  // prepared, waiting for an engine slot: freed now
+    s->readyq.erase(std::remove(s->readyq.begin(), s->readyq.end(), r), s->readyq.end());
+    if (r->ctx) gbfem_destroy(r->ctx);
+    r->ctx = nullptr;
+    r->kry.release();
+    s->in_use -= r->charged;
+    r->charged = 0;
+    s->lanes[r->kind].held--;
+    try_admit(s);
+  } else {  // preparing or solving: its worker or the engine retires it
+    r->cancel = true;
+    return 0;
+  }
+  r->status = -2;
+  r->err = "cancelled";
+  r->t_done = now_s();
+  s->cv_done.notify_all();
+  return 0;
+}
+
 int gbfem_server_release(gbfem_server s, long long id) {
   GB_CHECK(s, "null server");
   std::lock_guard<std::mutex> lk(s->mu);
@@ -1041,6 +1094,12 @@ int gbfem_server_set_option(gbfem_server s, int option, long long value) {
     GB_CHECK(value >= 1 && value <= 64, "steps per poll must be 1..64");
     std::lock_guard<std::mutex> lk(s->mu);
     s->steps_per_poll = (int)value;
+    return 0;
+  }
+  if (option == GBFEM_SERVE_OPT_FAIL_PREPARATIONS) {
+    GB_CHECK(value >= 0 && value <= 1000000, "injected failure count out of range");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->inject_prep_failures = (int)value;
     return 0;
   }
   gbfem::set_error("unknown server option");

@@ -97,6 +97,15 @@ class Server:
     def release(self, rid):
         self._check(self.L.gbfem_server_release(self._h, rid))
 
+    def cancel(self, rid):
+        """gbfem_server_cancel: 0 cancelled, 1 already finished or failed."""
+        return self._check(self.L.gbfem_server_cancel(self._h, rid))
+
+    def inject_preparation_failures(self, count):
+        """The next `count` preparations fail as a device allocation would
+        (GBFEM_SERVE_OPT_FAIL_PREPARATIONS; host-side fault injection)."""
+        self._check(self.L.gbfem_server_set_option(self._h, 2, int(count)))
+
     def stats(self):
         st = np.zeros(8, np.int64)
         self._check(self.L.gbfem_server_stats(self._h, st.ctypes.data))

@@ -105,3 +105,102 @@ def test_admission_respects_budget(gb):
         srv.close()
     assert len(res) == len(probs)
     assert st["peak_bytes"] <= st["budget"]
+
+
+# ----------------------------------------------------------- failure handling
+# Failures are made on the host (an injected allocation failure, a malformed
+# request, a cancellation); no GPU fault is provoked.
+
+def test_injected_preparation_failure_is_contained(gb):
+    """The next preparation fails as if its device allocation had failed: that
+    request reports the failure, the others are served as usual, and the
+    admission accounting returns to zero."""
+    from modfem_gb300.serve import Server, dof_count
+    probs = [pr for (_, _, _, pr) in _problems()[:4]]
+    srv = Server(0, max_active=1, prep_threads=1)  # one at a time: the failure hits the first request
+    try:
+        srv.inject_preparation_failures(1)
+        ids = [srv.submit(pr) for pr in probs]
+        with pytest.raises(gb.GbFemError, match="injected allocation failure"):
+            srv.wait(ids[0], 120.0)
+        for rid, pr in zip(ids[1:], probs[1:]):
+            assert srv.wait(rid, 120.0) == 1
+            x, it, rel, _ = srv.result(rid, dof_count(pr))
+            assert rel < 1e-8 and np.all(np.isfinite(x))
+        for rid in ids:
+            srv.release(rid)
+        st = srv.stats()
+        assert st["bytes"] == 0 and st["active"] == 0 and st["queued"] == 0
+    finally:
+        srv.close()
+
+
+def test_malformed_request_fails_alone(gb):
+    """A request whose element names a node that does not exist is refused
+    by its preparation (gbfem_set_mesh's range check) with a message; a
+    request without elements is refused at submission; the server keeps
+    serving."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    from modfem_gb300.serve import STD, Problem, Server, dof_count
+    m = structured_prism_mesh(4, jitter=0.1, seed=3)
+    k = lognormal_k(m.nel, seed=3)
+    bad = Problem(m, k, kind=STD)
+    bad.el[5, 2] = m.nno + 7  # out of range, in the array the request points to
+    good = _problems()[0][3]
+    srv = Server(0, max_active=4, prep_threads=2)
+    try:
+        rb = srv.submit(bad)
+        rg = srv.submit(good)
+        with pytest.raises(gb.GbFemError, match="out of range"):
+            srv.wait(rb, 120.0)
+        assert srv.wait(rg, 120.0) == 1
+        assert srv.result(rg, dof_count(good))[2] < 1e-8
+        empty = Problem(m, k, kind=STD)
+        empty.req.nel = 0
+        with pytest.raises(gb.GbFemError, match="empty request"):
+            srv.submit(empty)
+        srv.release(rb)
+        srv.release(rg)
+        assert srv.stats()["bytes"] == 0
+    finally:
+        srv.close()
+
+
+def test_cancel_queued_and_running_requests(gb):
+    """Cancelling a queued request removes it before it is prepared; a
+    request already admitted is retired at the end of its preparation or at
+    the engine's next poll.  Cancelled requests report "cancelled", their
+    memory returns to the budget, and the requests not cancelled give the
+    same solutions as when served alone."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    from modfem_gb300.serve import STD, Problem, Server, dof_count
+    big = []
+    for n in (30, 31, 32):  # long enough solves that a cancellation finds them running
+        m = structured_prism_mesh(n, jitter=0.2, seed=n)
+        big.append(Problem(m, lognormal_k(m.nel, seed=n), kind=STD, krylov=30, max_iter=20000, tol=1e-10))
+    small = _problems()[0][3]
+    srv = Server(0, max_active=2, prep_threads=1)
+    try:
+        ref_id = srv.submit(small)
+        assert srv.wait(ref_id, 120.0) == 1
+        x_ref = srv.result(ref_id, dof_count(small))[0]
+        srv.release(ref_id)
+        ids = [srv.submit(pr) for pr in big] + [srv.submit(small)]
+        # the third big request is still queued (two slots): cancelled at once
+        assert srv.cancel(ids[2]) == 0
+        with pytest.raises(gb.GbFemError, match="cancelled"):
+            srv.wait(ids[2], 120.0)
+        # the first one is being prepared or solved
+        assert srv.cancel(ids[0]) == 0
+        with pytest.raises(gb.GbFemError, match="cancelled"):
+            srv.wait(ids[0], 120.0)
+        assert srv.wait(ids[1], 300.0) == 1
+        assert srv.wait(ids[3], 300.0) == 1
+        assert np.array_equal(srv.result(ids[3], dof_count(small))[0], x_ref)
+        assert srv.cancel(ids[3]) == 1  # finished: nothing to cancel
+        for rid in ids:
+            srv.release(rid)
+        st = srv.stats()
+        assert st["bytes"] == 0 and st["active"] == 0
+    finally:
+        srv.close()
