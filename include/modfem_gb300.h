@@ -517,6 +517,13 @@ int gbfem_server_cancel(gbfem_server srv, long long id);
  * handle failed requests (the failure is made on the host). */
 #define GBFEM_SERVE_OPT_STEPS_PER_POLL 1
 #define GBFEM_SERVE_OPT_FAIL_PREPARATIONS 2
+/* GBFEM_SERVE_OPT_SOLO_DOFS: std requests with at least this many dofs
+ * (default 40,000; 0: none) are not batched into the engine's steps: their
+ * preparation worker solves them alone with gbfem_solve's device-resident
+ * GMRES (sliced-ELL SpMV, restart cycles as a CUDA graph) on the request's
+ * own stream, beside the batched lanes.  Same stopping rule; the result does
+ * not depend on the other requests either way. */
+#define GBFEM_SERVE_OPT_SOLO_DOFS 3
 int gbfem_server_set_option(gbfem_server srv, int option, long long value);
 /* stats[8]: engine steps, kernel launches, peak active requests, peak
  * bytes charged, budget, bytes charged now, queued, active. */

@@ -24,8 +24,9 @@
 // or double words (float pairs h + l, the same 8 bytes): with double words
 // the products run on the FP32 pipes and the kernel is bound by HBM alone
 // (GB300's FP64 pipe, ~0.6 T FMA/s, is itself near the HBM rate for one FMA
-// per 12 bytes).  Row sums run in column order in one thread, as the
-// reference's loop does.  Reductions are two-stage over a fixed block
+// per 12 bytes).  The copy holds the rows of D^-1 A (the point-Jacobi
+// scaling folded in once per solve), so the product reads no preconditioner.
+// Row sums run in column order in one thread, as the reference's loop does.  Reductions are two-stage over a fixed block
 // partition and fixed tree order: the solve is bit-reproducible.
 
 #include <cstring>
@@ -102,16 +103,19 @@ __device__ __forceinline__ float2 sell_value<float2>(double v) {
   return dw_f2(v);
 }
 
+// the rows of the Jacobi-preconditioned matrix D^-1 A (dinv[r] a_rj): the
+// preconditioner is folded into the copy, so the product reads no dinv
 template <typename VT>
 __global__ void sell_vals_kernel(int n, int nslices, const int *__restrict__ row_ptr, const double *__restrict__ val,
-                                 const int *__restrict__ off, VT *__restrict__ sv) {
+                                 const double *__restrict__ dinv, const int *__restrict__ off, VT *__restrict__ sv) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int s = (int)(t / SELL_C), l = (int)(t % SELL_C);
   if (s >= nslices) return;
   const int r = s * SELL_C + l;
   const int w = (off[s + 1] - off[s]) / SELL_C;
   const int lo = r < n ? row_ptr[r] : 0, len = r < n ? row_ptr[r + 1] - lo : 0;
-  for (int j = 0; j < w; j++) sv[off[s] + SELL_C * j + l] = sell_value<VT>(j < len ? val[lo + j] : 0.0);
+  const double d = r < n ? dinv[r] : 0.0;
+  for (int j = 0; j < w; j++) sv[off[s] + SELL_C * j + l] = sell_value<VT>(j < len ? d * val[lo + j] : 0.0);
 }
 
 // one row per thread, a warp per slice: acc = sum_j val * x[col], in column
@@ -244,7 +248,7 @@ __global__ void __launch_bounds__(GM_T) gm_restart_residual(GmArgs a) {
     const int o = a.sell_off[s], w = (a.sell_off[s + 1] - o) / SELL_C;
     const double acc = a.sell_col16 ? sell_row(a.sell_val64 + o + l, a.sell_col16 + o + l, w, base, a.x)
                                     : sell_row(a.sell_val64 + o + l, a.sell_col32 + o + l, w, base, a.x);
-    if (r < a.n) a.tmp[r] = (a.b[r] - acc) * a.dinv[r];
+    if (r < a.n) a.tmp[r] = a.dinv[r] * a.b[r] - acc;  // the copy holds D^-1 A
     return;
   }
   const int lane = threadIdx.x & 3;
@@ -322,7 +326,7 @@ __global__ void __launch_bounds__(GM_T) gm_arnoldi_spmv(GmArgs a, const VT *__re
     acc = sell_row_dw(sv + o + l, scol + o + l, w, sell_base(r, a.n), a.xdw);
   else
     acc = sell_row(sv + o + l, scol + o + l, w, sell_base(r, a.n), a.V + (size_t)j * a.n);
-  if (r < a.n) a.V[(size_t)(j + 1) * a.n + r] = a.dinv[r] * acc;
+  if (r < a.n) a.V[(size_t)(j + 1) * a.n + r] = acc;  // the copy holds D^-1 A
 }
 
 // Gram-Schmidt dot products <V[k], V[j+1]>, k = blockIdx.y <= j
@@ -494,12 +498,12 @@ int fill_sell_values(gbfem_ctx c) {
   const unsigned g = nblk((long long)ns * gbfem::SELL_C, 256);
   if (c->std_spmv_dword) {
     GB_TRY(c->sell_valdw.alloc((size_t)std::max<long long>(c->sell_total, 1)));
-    gbfem::sell_vals_kernel<float2><<<g, 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->val.p, c->sell_off.p,
-                                                               c->sell_valdw.p);
+    gbfem::sell_vals_kernel<float2><<<g, 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->val.p, c->dinv.p,
+                                                               c->sell_off.p, c->sell_valdw.p);
   } else {
     GB_TRY(c->sell_val.alloc((size_t)std::max<long long>(c->sell_total, 1)));
-    gbfem::sell_vals_kernel<double><<<g, 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->val.p, c->sell_off.p,
-                                                               c->sell_val.p);
+    gbfem::sell_vals_kernel<double><<<g, 256, 0, c->stream>>>(n, ns, c->row_ptr.p, c->val.p, c->dinv.p,
+                                                               c->sell_off.p, c->sell_val.p);
   }
   GB_CUDA(cudaGetLastError());
   return 0;
@@ -567,9 +571,9 @@ int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int 
   const int n = c->ndof, m = krylov;
   cudaStream_t st = c->stream;
   GB_TRY(build_sell(c));
-  GB_TRY(fill_sell_values(c));
   GB_TRY(c->dinv.alloc(n));
   GB_TRY(launch_jacobi_diag(st, n, c->row_ptr.p, c->col_ind.p, c->val.p, c->dinv.p));
+  GB_TRY(fill_sell_values(c));
   const int nb = reduction_blocks(n);
   GB_TRY(c->V.alloc((size_t)n * (m + 1)));
   GB_TRY(c->x.alloc(n));

@@ -356,6 +356,7 @@ struct SrvRequest {
   double t_submit = 0, t_admit = 0, t_ready = 0, t_start = 0, t_done = 0;
   int status = 0;  // 0 queued, 1 preparing, 2 ready, 3 solving, 4 done, -1 failed, -2 cancelled
   bool cancel = false;  // cancellation asked while preparing or solving
+  bool solo = false;    // large std request: solved alone by its preparation worker
   std::string err;
   gbfem_ctx ctx = nullptr;
   DevBuf<double> kry;
@@ -426,6 +427,7 @@ struct gbfem_server_s {
   int peak_active = 0;
   int steps_per_poll = 4;
   int inject_prep_failures = 0;  // GBFEM_SERVE_OPT_FAIL_PREPARATIONS
+  int solo_dofs = 40000;         // GBFEM_SERVE_OPT_SOLO_DOFS
   std::string fatal;
 };
 
@@ -492,6 +494,18 @@ int prepare(gbfem_server s, SrvRequest &r) {
     // request's matrix (and result) does not depend on when it runs
     if ((rc = gbfem_assemble(c, GBFEM_SCATTER_COLOR)) < 0) return rc;
     r.n = nd;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      r.solo = s->solo_dofs > 0 && nd >= s->solo_dofs;
+    }
+    if (r.solo) {
+      // solved by the preparation worker with the device-resident GMRES
+      if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        gbfem::set_error("preparation failed on the device");
+        return -1;
+      }
+      return 0;
+    }
     if ((rc = c->dinv.alloc(nd)) < 0) return rc;
     if ((rc = gbfem::launch_jacobi_diag(c->stream, nd, c->row_ptr.p, c->col_ind.p, c->val.p, c->dinv.p)) < 0)
       return rc;
@@ -554,6 +568,35 @@ void prep_worker(gbfem_server s) {
       s->in_use -= r->charged;
       r->charged = 0;
       r->t_done = now_s();
+      s->lanes[r->kind].held--;
+      try_admit(s);
+      s->cv_done.notify_all();
+      continue;
+    }
+    if (r->solo) {
+      // a large std request: its own stream and restart-cycle graph
+      // (gbfem_solve's device GMRES), beside the engine's batched lanes;
+      // the estimate (which includes the Krylov space) stays charged
+      s->n_active++;
+      r->status = 3;
+      r->t_start = now_s();
+      lk.unlock();
+      r->x.assign(r->n, 0.0);
+      double res = 0.0, rel = 0.0;
+      const int it = gbfem::gmres_device_std(r->ctx, r->krylov, r->max_iter, r->tol, 1, r->x.data(), &res, &rel);
+      const std::string err = it < 0 ? std::string(gbfem_last_error()) : std::string();
+      gbfem_destroy(r->ctx);
+      lk.lock();
+      r->ctx = nullptr;
+      r->iters = it < 0 ? 0 : it;
+      r->rel = rel;
+      s->in_use -= r->charged;
+      r->charged = 0;
+      r->status = it < 0 ? -1 : (r->cancel ? -2 : 4);
+      if (it < 0) r->err = err;
+      if (r->cancel && it >= 0) r->err = "cancelled";
+      r->t_done = now_s();
+      s->n_active--;
       s->lanes[r->kind].held--;
       try_admit(s);
       s->cv_done.notify_all();
@@ -1094,6 +1137,12 @@ int gbfem_server_set_option(gbfem_server s, int option, long long value) {
     GB_CHECK(value >= 1 && value <= 64, "steps per poll must be 1..64");
     std::lock_guard<std::mutex> lk(s->mu);
     s->steps_per_poll = (int)value;
+    return 0;
+  }
+  if (option == GBFEM_SERVE_OPT_SOLO_DOFS) {
+    GB_CHECK(value >= 0 && value <= 2000000000LL, "solo threshold out of range");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->solo_dofs = (int)value;
     return 0;
   }
   if (option == GBFEM_SERVE_OPT_FAIL_PREPARATIONS) {

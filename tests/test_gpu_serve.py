@@ -204,3 +204,43 @@ def test_cancel_queued_and_running_requests(gb):
         assert st["bytes"] == 0 and st["active"] == 0
     finally:
         srv.close()
+
+
+def test_large_std_request_solved_alone_on_its_stream(gb):
+    """A std request with at least GBFEM_SERVE_OPT_SOLO_DOFS dofs (default
+    40,000) is solved by its preparation worker with the device-resident
+    GMRES on its own stream: the same bits alone and beside a mix of small
+    requests, and the plain one-problem path's solution within the solver
+    tolerance."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    from modfem_gb300.serve import STD, Problem, Server, dof_count
+    m = structured_prism_mesh(36, jitter=0.2, seed=36)
+    k = lognormal_k(m.nel, seed=36)
+    big = Problem(m, k, kind=STD, krylov=30, max_iter=20000, tol=1e-8)
+    assert dof_count(big) >= 40000
+    small = [pr for (_, _, _, pr) in _problems()]
+    srv = Server(0, max_active=16, prep_threads=4)
+    try:
+        rid = srv.submit(big)
+        assert srv.wait(rid, 300.0) == 1
+        xa, ia, ra, _ = srv.result(rid, dof_count(big))
+        srv.release(rid)
+        ids = [srv.submit(pr) for pr in small[:3]] + [srv.submit(big)] + [srv.submit(pr) for pr in small[3:]]
+        for i in ids:
+            assert srv.wait(i, 300.0) == 1
+        xm, im, rm, _ = srv.result(ids[3], dof_count(big))
+        for i in ids:
+            srv.release(i)
+    finally:
+        srv.close()
+    assert ia == im and np.array_equal(xa, xm)
+    assert ra < 1e-8
+    c = gb.Context(0)
+    c.set_mesh(m)
+    c.set_coefficients(k=k, f=1.0, g=0.0)
+    c.build_structure_device()
+    c.assemble(gb.SCATTER_COLOR)
+    x, it, _, rel = c.solve(30, 20000, 1e-8)
+    c.close()
+    assert abs(it - ia) <= 1
+    assert np.max(np.abs(x - xa)) <= 1e-6 * np.max(np.abs(x))
