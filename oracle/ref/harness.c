@@ -473,6 +473,9 @@ int pdr_assemble_local_stiff_mat_with_table(int Problem_id, int Level_id, int Co
   return 1;
 }
 
+#ifndef HARNESS_GB300_SHIM
+/* the reference's CPU driver; the GB300 shim build takes
+   modfem_gb300/modfem_side/pds_gb300_ls_intf.c's function instead */
 int pdr_create_assemble_stiff_mat(int Problem_id, int Level_id, int Comp_type, int *Pdeg_coarse_p,
                                   int Nr_int_ent, int *L_int_ent_type, int *L_int_ent_id,
                                   int Nr_colors_elems, int *L_color_index_elems, int Nr_colors_faces,
@@ -487,6 +490,7 @@ int pdr_create_assemble_stiff_mat(int Problem_id, int Level_id, int Comp_type, i
   h_last_assembly_s = wall() - t;
   return 1;
 }
+#endif
 
 int pdr_get_list_ent(int Problem_id, int *Nr_int_ent, int **List_int_ent_type, int **List_int_ent_id,
                      int *Nr_dof_ent, int **List_dof_ent_type, int **List_dof_ent_id,
