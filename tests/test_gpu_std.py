@@ -105,6 +105,42 @@ def test_dropin_create_assemble_matches_reference(gb):
     assert launches == 2 and ms > 0
 
 
+@pytest.mark.parametrize("cache", [0, 1])
+def test_dropin_comp_types_and_empty_lists(gb, cache):
+    """Comp_type SM only and RHS only clear and fill just their part (the
+    other keeps what the caller's array held, as MKB's matrix does between
+    the calls); an empty entity list clears the matrix and rhs; entity ids
+    outside the mesh are refused."""
+    g = load("std_n10")
+    m = FixtureMesh(g)
+    c = make_ctx(gb, m, g["k"], (g["dof_of_node"], g["row_ptr"], g["col_ind"]))
+    c.set_option(gb.OPT_CACHE_TABLES, cache)
+    args = [np.ascontiguousarray(g[k], dtype=np.int32) for k in
+            ("int_ent_type", "int_ent_id", "color_elems", "color_faces", "asse_pos", "assembly_table")]
+    nnz, nd = g["col_ind"].size, g["row_ptr"].size - 1
+    sc = energy_scale(g["row_ptr"], g["col_ind"], g["crs_val"])
+    val, rhs = np.full(nnz, 3.5), np.full(nd, 3.5)
+    c.create_assemble_stiff_mat(*args, comp_type=gb.COMP_SM, crs_val=val, rhs=None)
+    assert crs_rel_err(g["row_ptr"], val, g["crs_val"], sc) < REL_TOL
+    assert np.all(rhs == 3.5)
+    c.create_assemble_stiff_mat(*args, comp_type=gb.COMP_RHS, crs_val=None, rhs=rhs)
+    assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL
+    # both again through the device copy
+    v2, r2 = c.get_matrix()
+    assert crs_rel_err(g["row_ptr"], v2, g["crs_val"], sc) < REL_TOL and vec_rel_err(r2, g["crs_rhs"]) < REL_TOL
+    # no entities: a cleared matrix
+    e = np.zeros(0, np.int32)
+    val0, rhs0 = np.full(nnz, 1.0), np.full(nd, 1.0)
+    c.create_assemble_stiff_mat(e, e, np.array([0, 0], np.int32), None, e, args[5], crs_val=val0, rhs=rhs0)
+    assert not np.any(val0) and not np.any(rhs0)
+    # an element id beyond the mesh
+    bad = args[1].copy()
+    bad[3] = m.nel + 5
+    with pytest.raises(gb.GbFemError, match="outside the mesh"):
+        c.create_assemble_stiff_mat(args[0], bad, *args[2:], crs_val=val, rhs=rhs)
+    c.close()
+
+
 def test_dropin_table_cache(gb):
     g = load("std_n10")
     m = FixtureMesh(g)
