@@ -736,7 +736,7 @@ def bench_serving(gb, local, rates=(50, 200, 1000, 2000), per_rate=48):
             c.solve(krylov=30, max_iter=20000, tol_rel=1e-8)
         c.close()
         service.append(time.perf_counter() - t0)
-    srv = Server(local, max_active=32, prep_threads=4)
+    srv = Server(local, max_active=32, prep_threads=8)
     out = {"requests_per_rate": per_rate, "pool": [{"kind": "std" if pr.kind == STD else f"dg_p{pr.p}",
                                                      "elements": int(m.nel)} for (m, _, _, pr) in pool],
            "rates": []}

@@ -14,9 +14,12 @@
 //    (half of max_active, or more while the other lane has nobody waiting)
 //    and its estimated device footprint fits in the shared HBM budget
 //    (replaced by the measured footprint once it is built);
-//  * preparation (worker threads, one CUDA stream each): upload, structure
-//    (built and coloured on the device for std requests), integrate +
-//    assemble, preconditioner; overlaps with the solves running;
+//  * preparation (worker threads, one CUDA stream each; std requests taken
+//    before DG ones): upload, structure (built and coloured on the device for
+//    std requests), integrate + assemble, preconditioner; overlaps with the
+//    solves running.  Std requests of GBFEM_SERVE_OPT_SOLO_DOFS dofs or more
+//    are then solved by their worker, alone on their stream, with the
+//    device-resident GMRES of gbfem_solve;
 //  * solve (engine thread, one stream per lane): every step of a lane
 //    advances each of its active requests by one GMRES iteration with
 //    batched kernels over all of them - one CRS SpMV launch for all std
@@ -552,8 +555,12 @@ void prep_worker(gbfem_server s) {
       std::unique_lock<std::mutex> lk(s->mu);
       s->cv_prep.wait(lk, [&] { return s->stop || !s->prepq.empty(); });
       if (s->prepq.empty()) return;
-      r = s->prepq.front();
-      s->prepq.pop_front();
+      // std requests first (their preparation is short and their solve
+      // is latency bound), in admission order; then DG in admission order
+      auto it = std::find_if(s->prepq.begin(), s->prepq.end(), [](const ReqPtr &q) { return q->kind == 0; });
+      if (it == s->prepq.end()) it = s->prepq.begin();
+      r = *it;
+      s->prepq.erase(it);
     }
     const int rc = prepare(s, *r);
     std::unique_lock<std::mutex> lk(s->mu);
