@@ -457,9 +457,10 @@ int gbfem_batch_get(gbfem_batch batch, double *vals, double *rhs);
  * solves nor queue behind them; a request is admitted when its lane has a
  * slot and its device footprint fits in the shared HBM budget.  Worker
  * threads upload, build, integrate and assemble each admitted request on its
- * own stream while the engine thread advances each lane's requests in the
- * solve phase together, one GMRES iteration per step with batched kernels
- * and the GMRES scalar logic on the device.  A request's
+ * own stream (std requests before DG ones) while the engine thread advances
+ * each lane's requests in the solve phase together, one GMRES iteration per
+ * step with batched kernels and the GMRES scalar logic on the device; large
+ * std requests are solved by their worker instead (GBFEM_SERVE_OPT_SOLO_DOFS).  A request's
  * result does not depend on the other requests in the mix (bit-identical
  * alone and together).  The numerics per request are those of
  * gbfem_assemble + gbfem_solve (std) and gbfem_dg_assemble + gbfem_dg_solve
