@@ -376,3 +376,94 @@ def tet_faces(mesh, bc=1):
                      bc=np.where(e2 >= 0, -1, bc).astype(np.int32), el1=e1.astype(np.int32),
                      el2=e2.astype(np.int32), side1=s1.astype(np.int32), side2=s2.astype(np.int32),
                      nodes=nodes.astype(np.int32))
+
+
+# local faces of a prism in the orientation of prism_faces (side 0 bottom
+# seen from below, 1 top, 2 + e the lateral face over triangle edge e)
+PRISM_SIDES = ((0, 2, 1), (3, 4, 5), (0, 1, 4, 3), (1, 2, 5, 4), (2, 0, 3, 5))
+
+
+class MixedMesh:
+    """Prisms and tetrahedra in one mesh (0-based): el_nodes (nel, 6) with a
+    tetrahedron's 4 vertices first and -1 after them, el_nv (nel,) 6 or 4."""
+
+    def __init__(self, n, coords, el_nodes, el_nv, n_prism_layers):
+        self.n = n
+        self.coords = coords
+        self.el_nodes = el_nodes
+        self.el_nv = el_nv
+        self.n_prism_layers = n_prism_layers
+        self.bc_face_id = np.zeros(0, np.int32)
+        self.bc_face_el = np.zeros(0, np.int32)
+        self.bc_face_side = np.zeros(0, np.int32)
+        self.bc_face_bc = np.zeros(0, np.int32)
+
+    @property
+    def nno(self):
+        return self.coords.shape[0]
+
+    @property
+    def nel(self):
+        return self.el_nodes.shape[0]
+
+
+def structured_mixed_mesh(n, prism_layers, jitter=0.0, seed=0):
+    """Unit cube of n^3 hexahedra: the lower `prism_layers` layers split into
+    two prisms each (structured_prism_mesh), the layers above into six
+    tetrahedra each (structured_tet_mesh's Kuhn split).  Both splits cut the
+    horizontal squares along the same diagonal, so the prisms' top triangles
+    are the tetrahedra's bottom faces.  One node grid (x fastest, then y,
+    then z), prisms first, then tetrahedra; jitter keeps boundary nodes on
+    their planes."""
+    assert 0 < prism_layers < n
+    pm = structured_prism_mesh(n, jitter=jitter, seed=seed)
+    tm = structured_tet_mesh(n, jitter=0.0)
+    T = 2 * n * n
+    prisms = pm.el_nodes[:prism_layers * T]
+    per_layer = 6 * n * n
+    tets = tm.el_nodes[prism_layers * per_layer:]
+    # the tetrahedra's orientation check on the jittered coordinates
+    X = pm.coords[tets]
+    det = np.einsum("ij,ij->i", X[:, 1] - X[:, 0], np.cross(X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]))
+    tets = tets.copy()
+    flip = det < 0
+    tets[flip, 2], tets[flip, 3] = tets[flip, 3].copy(), tets[flip, 2].copy()
+    el = np.full((prisms.shape[0] + tets.shape[0], 6), -1, np.int32)
+    el[:prisms.shape[0]] = prisms
+    el[prisms.shape[0]:, :4] = tets
+    nv = np.concatenate([np.full(prisms.shape[0], 6), np.full(tets.shape[0], 4)]).astype(np.int32)
+    return MixedMesh(n, pm.coords, el, nv, prism_layers)
+
+
+def mixed_faces(mesh, bc=1):
+    """Face table of a MixedMesh in the format of prism_faces: every face
+    once, el1 the lower-numbered neighbour and side1 its local face (prisms:
+    PRISM_SIDES, tetrahedra: TET_SIDES), nodes in el1's local order of that
+    face; type 3 or 4; bc on the boundary, -1 inside.  Ordered by (el1,
+    side1)."""
+    rows = []
+    for e in range(mesh.nel):
+        sides = PRISM_SIDES if mesh.el_nv[e] == 6 else TET_SIDES
+        for s, loc in enumerate(sides):
+            verts = [int(mesh.el_nodes[e, i]) for i in loc]
+            rows.append((tuple(sorted(verts)), e, s, verts))
+    rows.sort(key=lambda r: (r[0], r[1]))
+    out = []
+    i = 0
+    while i < len(rows):
+        key, e1, s1, verts = rows[i]
+        if i + 1 < len(rows) and rows[i + 1][0] == key:
+            e2, s2 = rows[i + 1][1], rows[i + 1][2]
+            i += 2
+        else:
+            e2, s2 = -1, 0
+            i += 1
+        out.append((e1, s1, e2, s2, len(verts), verts + [-1] * (4 - len(verts))))
+    out.sort(key=lambda r: (r[0], r[1]))
+    nf = len(out)
+    e1 = np.array([r[0] for r in out], np.int32)
+    e2 = np.array([r[2] for r in out], np.int32)
+    return FaceTable(id=np.arange(1, nf + 1, dtype=np.int32), type=np.array([r[4] for r in out], np.int32),
+                     bc=np.where(e2 >= 0, -1, bc).astype(np.int32), el1=e1, el2=e2,
+                     side1=np.array([r[1] for r in out], np.int32), side2=np.array([r[3] for r in out], np.int32),
+                     nodes=np.array([r[5] for r in out], np.int32))

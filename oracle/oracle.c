@@ -548,6 +548,34 @@ static int dg_shape(int p, const double *e, double *phi, double *dx, double *dy,
 
 int orc_dg_nshape(int p) { return (p >= 1 && p <= GB_DG_PMAX) ? GB_DG_NS[p] : -1; }
 
+/* the DG face rule of degree p (apr_set_quadr_2D of the DG module, ti 0
+   triangle, 1 quadrilateral): (s, t, w) per point; returns the point count */
+int orc_dg_face_rule(int p, int ti, double *out)
+{
+  int q, nq;
+  if (p < 1 || p > GB_DG_PMAX || ti < 0 || ti > 1) return -1;
+  nq = GB_DG_NQF[p][ti];
+  for (q = 0; q < nq; q++) {
+    out[3 * q] = GB_DG_FQ[p - 1][ti][q][0];
+    out[3 * q + 1] = GB_DG_FQ[p - 1][ti][q][1];
+    out[3 * q + 2] = GB_DG_FQ[p - 1][ti][q][2];
+  }
+  return nq;
+}
+
+/* the tensor basis exponents (a, b, c) of degree p in the reference's order */
+int orc_dg_exponents(int p, int *out)
+{
+  int i;
+  if (p < 1 || p > GB_DG_PMAX) return -1;
+  for (i = 0; i < GB_DG_NS[p]; i++) {
+    out[3 * i] = GB_DG_EXP[p - 1][i][0];
+    out[3 * i + 1] = GB_DG_EXP[p - 1][i][1];
+    out[3 * i + 2] = GB_DG_EXP[p - 1][i][2];
+  }
+  return GB_DG_NS[p];
+}
+
 /* apr_num_int_el of the DG module (apd_dg_prism/aps_dg_prism_intf.c:1239-1728)
    for nreq = 1: the volume rule of apr_set_quadr_3D (aps_dg_util.c:1415-1480),
    the prism geometry of apr_elem_calc_3D (aps_dg_util.c:112-400), the 9-term

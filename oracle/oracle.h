@@ -64,6 +64,8 @@ int orc_gmres_jacobi(int n, const int *row_ptr, const int *col_ind, const double
 /* DG prisms, tensor basis of degree p = 1..4 (pdeg 101 p): ns x ns column-major
    matrix and ns load vector; returns ns (< 0 for an unsupported p) */
 int orc_dg_nshape(int p);
+int orc_dg_face_rule(int p, int ti, double *out);
+int orc_dg_exponents(int p, int *out);
 int orc_dg_prism_element(const double *X /*18*/, const double *A /*9*/, double f, int p, double *sm,
                          double *rhs);
 

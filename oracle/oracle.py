@@ -353,33 +353,207 @@ def dg_tet_assemble(mesh, faces, pdeg, A, pen=10.0, g=0.0, f=1.0):
     for k in range(faces.n):
         e1, e2 = int(faces.el1[k]), int(faces.el2[k])
         V = np.asarray(mesh.coords)[faces.nodes[k, :3]]
-        nrm = np.cross(V[1] - V[0], V[2] - V[0])
-        area = 0.5 * np.linalg.norm(nrm)
-        n = nrm / np.linalg.norm(nrm)
-        if np.dot(n, V.mean(0) - X[e1].mean(0)) < 0:
-            n = -n
-        sides = [e1] + ([e2] if e2 >= 0 else [])
-        pmax = max(int(pdeg[s]) for s in sides)
-        st, w = _collapsed_tri_rule(pmax + 2)
-        xs = V[0] + st[:, :1] * (V[1] - V[0]) + st[:, 1:] * (V[2] - V[0])
-        aw = w * 2.0 * area
-        if e2 >= 0:
-            fac, c = 0.5, pen * min(int(pdeg[e1]), int(pdeg[e2])) / np.sqrt(area)
-        else:
-            fac, c = 1.0, pen * int(pdeg[e1]) / np.sqrt(area)
-        val = {}
-        for s, e in enumerate(sides):
-            phi, grad = _tet_basis_at(X[e], int(pdeg[e]), xs)
-            gg = np.einsum("qjk,lk,l->qj", grad, A[e], n)  # n . (A grad phi)
-            val[e] = (1.0 if s == 0 else -1.0, phi, gg)
-        for ei in sides:
-            si, phi_i, g_i = val[ei]
-            for ej in sides:
-                sj, phi_j, g_j = val[ej]
-                Kf = np.einsum("q,qi,qj->ij", aw * sj, fac * g_i + si * c * phi_i, phi_j) \
-                    - np.einsum("q,qi,qj->ij", aw * si * fac, phi_i, g_j)
-                blocks[(ei, ej)] = blocks.get((ei, ej), 0.0) + Kf
-        if e2 < 0:
-            _, phi1, g1 = val[e1]
-            rhs[e1] += g * np.einsum("q,qi->i", aw, g1 + c * phi1)
+        fb, r1 = _tet_face(X, A, pdeg, V, e1, e2, pen, g)
+        for key, v in fb.items():
+            blocks[key] = blocks.get(key, 0.0) + v
+        if r1 is not None:
+            rhs[e1] += r1
     return blocks, rhs
+
+
+def _tet_face(X, A, pdeg, V, e1, e2, pen, g):
+    """One face of dg_tet_assemble: blocks {(row el, col el)} and, on the
+    boundary, el1's rhs (else None).  X[e]: vertices, A[e]: 3 x 3 tensor."""
+    nrm = np.cross(V[1] - V[0], V[2] - V[0])
+    area = 0.5 * np.linalg.norm(nrm)
+    n = nrm / np.linalg.norm(nrm)
+    if np.dot(n, V.mean(0) - X[e1].mean(0)) < 0:
+        n = -n
+    sides = [e1] + ([e2] if e2 >= 0 else [])
+    pmax = max(int(pdeg[s]) for s in sides)
+    st, w = _collapsed_tri_rule(pmax + 2)
+    xs = V[0] + st[:, :1] * (V[1] - V[0]) + st[:, 1:] * (V[2] - V[0])
+    aw = w * 2.0 * area
+    if e2 >= 0:
+        fac, c = 0.5, pen * min(int(pdeg[e1]), int(pdeg[e2])) / np.sqrt(area)
+    else:
+        fac, c = 1.0, pen * int(pdeg[e1]) / np.sqrt(area)
+    val = {}
+    for s, e in enumerate(sides):
+        phi, grad = _tet_basis_at(X[e], int(pdeg[e]), xs)
+        gg = np.einsum("qjk,lk,l->qj", grad, A[e], n)  # n . (A grad phi)
+        val[e] = (1.0 if s == 0 else -1.0, phi, gg)
+    blocks = {}
+    for ei in sides:
+        si, phi_i, g_i = val[ei]
+        for ej in sides:
+            sj, phi_j, g_j = val[ej]
+            blocks[(ei, ej)] = np.einsum("q,qi,qj->ij", aw * sj, fac * g_i + si * c * phi_i, phi_j) \
+                - np.einsum("q,qi,qj->ij", aw * si * fac, phi_i, g_j)
+    r1 = None
+    if e2 < 0:
+        _, phi1, g1 = val[e1]
+        r1 = g * np.einsum("q,qi->i", aw, g1 + c * phi1)
+    return blocks, r1
+
+
+# ----------------------------------------------------------------------------
+# DG systems on meshes of prisms and tetrahedra together.  No reference
+# counterpart (the reference's DG module is prism-only): the volume blocks are
+# the pinned prism element (dg_prism_element) and the independent tetrahedron
+# element (dg_tet_element); prism-prism faces the pinned dg_face,
+# tetrahedron-tetrahedron faces the form of dg_tet_assemble, and the faces
+# between a prism and a tetrahedron the same form with each side's own basis.
+# ----------------------------------------------------------------------------
+PRISM_VLOC = np.array([(0, 0, -1), (1, 0, -1), (0, 1, -1), (0, 0, 1), (1, 0, 1), (0, 1, 1)], float)
+TET_VLOC = np.array([(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)], float)
+DG_TET_NS = (0, 4, 10, 20, 35)
+
+
+def dg_face_rule(p, ti):
+    """The DG module's face rule of degree p (ti 0 triangle, 1 quadrilateral):
+    points (s, t) and weights."""
+    out = np.zeros(3 * 64)
+    nq = lib().orc_dg_face_rule(p, ti, _p(out))
+    r = out[:3 * nq].reshape(nq, 3)
+    return r[:, :2].copy(), r[:, 2].copy()
+
+
+def dg_exponents(p):
+    """Exponents (a, b, c) of the tensor prism basis of degree p, reference order."""
+    out = np.zeros(3 * 128, np.int32)
+    ns = lib().orc_dg_exponents(p, _p(out))
+    return out[:3 * ns].reshape(ns, 3).copy()
+
+
+def _monomials(E, e):
+    """Values (q, ns) and local gradients (q, ns, 3) of xi^a eta^b zeta^c."""
+    E = np.asarray(E, float)
+    phi = np.prod(e[:, None, :] ** E[None, :, :], axis=2)
+    d = np.zeros((e.shape[0], E.shape[0], 3))
+    for a in range(3):
+        Ea = E.copy()
+        Ea[:, a] = np.maximum(Ea[:, a] - 1, 0)
+        d[:, :, a] = E[:, a] * np.prod(e[:, None, :] ** Ea[None, :, :], axis=2)
+    return phi, d
+
+
+def _prism_jacobians(X, e):
+    """dx/dxi columns of the linear prism at local points e (q, 3): (q, 3, 3)."""
+    xi, eta, z = e[:, 0], e[:, 1], e[:, 2]
+    lo, hi, l0 = (1 - z) / 2, (1 + z) / 2, 1 - xi - eta
+    dN = np.zeros((e.shape[0], 6, 3))
+    dN[:, :, 0] = np.stack([-lo, lo, 0 * z, -hi, hi, 0 * z], 1)
+    dN[:, :, 1] = np.stack([-lo, 0 * z, lo, -hi, 0 * z, hi], 1)
+    dN[:, :, 2] = 0.5 * np.stack([-l0, -xi, -eta, l0, xi, eta], 1)
+    return np.einsum("ia,qib->qab", X, dN)
+
+
+def _basis_at_local(X, nv, p, e):
+    """Values (q, ns) and physical gradients (q, ns, 3) of an element's DG
+    basis at local points e: the prism tensor basis (reference order) or the
+    tetrahedron's complete basis (tet_basis_exponents)."""
+    if nv == 6:
+        phi, d = _monomials(dg_exponents(p), e)
+        J = _prism_jacobians(X, e)
+    else:
+        phi, d = _monomials(tet_basis_exponents(p), e)
+        J0 = np.stack([X[1] - X[0], X[2] - X[0], X[3] - X[0]], 1)
+        J = np.broadcast_to(J0, (e.shape[0], 3, 3))
+    return phi, np.einsum("qja,qab->qjb", d, np.linalg.inv(J))
+
+
+def dg_mixed_face(coords, el_nodes, el_nv, faces, k, pdeg, A, pen=10.0):
+    """Blocks {(row el, col el)} of interior triangle face k between any two
+    elements: the interior-penalty form of dg_tet_assemble, at the DG
+    module's triangle rule of degree max(p1, p2); each side's local point from
+    the face-vertex weights (barycentric), n the unit normal out of el1,
+    weights 2 area w_q, penalty pen min(p1, p2) / sqrt(area)."""
+    e1, e2 = int(faces.el1[k]), int(faces.el2[k])
+    assert e2 >= 0 and faces.type[k] == 3
+    nodes = faces.nodes[k, :3]
+    V = coords[nodes]
+    nrm = np.cross(V[1] - V[0], V[2] - V[0])
+    area = 0.5 * np.linalg.norm(nrm)
+    n = nrm / np.linalg.norm(nrm)
+    X1 = coords[el_nodes[e1, :el_nv[e1]]]
+    if np.dot(n, V.mean(0) - X1.mean(0)) < 0:
+        n = -n
+    p1, p2 = int(pdeg[e1]), int(pdeg[e2])
+    st, w = dg_face_rule(max(p1, p2), 0)
+    bary = np.stack([1 - st[:, 0] - st[:, 1], st[:, 0], st[:, 1]], 1)
+    aw = w * 2.0 * area
+    fac, c = 0.5, pen * min(p1, p2) / np.sqrt(area)
+    val = {}
+    for s, e in enumerate((e1, e2)):
+        nv = int(el_nv[e])
+        X = coords[el_nodes[e, :nv]]
+        loc = [int(np.nonzero(el_nodes[e, :nv] == v)[0][0]) for v in nodes]
+        vloc = PRISM_VLOC if nv == 6 else TET_VLOC
+        el = bary @ vloc[loc]
+        phi, grad = _basis_at_local(X, nv, int(pdeg[e]), el)
+        gg = grad @ (A[e].reshape(3, 3).T @ n)
+        val[e] = (1.0 if s == 0 else -1.0, phi, gg)
+    blocks = {}
+    for ei in (e1, e2):
+        si, phi_i, g_i = val[ei]
+        for ej in (e1, e2):
+            sj, phi_j, g_j = val[ej]
+            blocks[(ei, ej)] = np.einsum("q,qi,qj->ij", aw * sj, fac * g_i + si * c * phi_i, phi_j) \
+                - np.einsum("q,qi,qj->ij", aw * si * fac, phi_i, g_j)
+    return blocks
+
+
+def dg_mixed_assemble(mesh, faces, pdeg, A, pen=10.0, g=0.0, f=1.0):
+    """The DG system of a MixedMesh (prisms and tetrahedra): blocks {(row el,
+    col el)} and the rhs list per element."""
+    coords = np.asarray(mesh.coords, float)
+    el, nv = np.asarray(mesh.el_nodes), np.asarray(mesh.el_nv)
+    A = np.asarray(A, float).reshape(-1, 9)
+    blocks, rhs = {}, []
+    for e in range(mesh.nel):
+        X = coords[el[e, :nv[e]]]
+        K, R = (dg_prism_element(X, A[e], int(pdeg[e]), f) if nv[e] == 6 else
+                dg_tet_element(X, A[e], int(pdeg[e]), f))
+        blocks[(e, e)] = K
+        rhs.append(R.copy())
+
+    class _PM:  # the prism-only view dg_face reads
+        pass
+    pm = _PM()
+    pm.coords, pm.el_nodes = coords, el
+    for k in range(faces.n):
+        e1, e2 = int(faces.el1[k]), int(faces.el2[k])
+        if e2 >= 0 and nv[e1] != nv[e2]:
+            fb = dg_mixed_face(coords, el, nv, faces, k, pdeg, A, pen)
+            for key, v in fb.items():
+                blocks[key] = blocks.get(key, 0.0) + v
+            continue
+        if nv[e1] == 6:
+            K, r = dg_face(pm, faces, k, pdeg, A, pen, g)
+            n1 = DG_NS[int(pdeg[e1])]
+            blocks[(e1, e1)] = blocks[(e1, e1)] + K[:n1, :n1]
+            rhs[e1] += r[:n1]
+            if e2 >= 0:
+                blocks[(e1, e2)] = blocks.get((e1, e2), 0.0) + K[:n1, n1:]
+                blocks[(e2, e1)] = blocks.get((e2, e1), 0.0) + K[n1:, :n1]
+                blocks[(e2, e2)] = blocks[(e2, e2)] + K[n1:, n1:]
+            continue
+
+        Xt = {e1: coords[el[e1, :4]]}
+        At = {e1: A[e1].reshape(3, 3)}
+        if e2 >= 0:
+            Xt[e2], At[e2] = coords[el[e2, :4]], A[e2].reshape(3, 3)
+        fb, r1 = _tet_face(Xt, At, pdeg, coords[faces.nodes[k, :3]], e1, e2, pen, g)
+        for key, v in fb.items():
+            blocks[key] = blocks.get(key, 0.0) + v
+        if r1 is not None:
+            rhs[e1] += r1
+    return blocks, rhs
+
+
+def _prism_shape(e):
+    """Linear prism shape functions (q, 6) at local points e (q, 3)."""
+    xi, eta, z = e[:, 0], e[:, 1], e[:, 2]
+    lo, hi, l0 = (1 - z) / 2, (1 + z) / 2, 1 - xi - eta
+    return np.stack([l0 * lo, xi * lo, eta * lo, l0 * hi, xi * hi, eta * hi], 1)
