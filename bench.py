@@ -634,6 +634,66 @@ def bench_tet_dg(gb, local, steps):
     return out
 
 
+def bench_mixed_dg_system(gb, local, steps, n=63, layers=50):
+    """Config 3 as one DG system on one connected mesh: 63^3 hexahedra, the
+    lower 50 layers split into 2 prisms each (396,900 jittered prisms), the
+    upper 13 into 6 tetrahedra each (309,582 affine tetrahedra), the two
+    regions joined by 7,938 prism-tetrahedron triangles; p uniform in 1..4
+    (seeded), lognormal(0,1) k, interior-penalty faces into the
+    variable-block storage.  Assembly (volume and all faces) in plain FP64
+    and in the fastest form (double-word volume sums, split-BF16 tensor-core
+    faces between prisms), then a fixed 100 GMRES(50) iterations with block
+    Jacobi."""
+    from modfem_gb300.mesh import lognormal_k, mixed_faces, structured_mixed_mesh
+    m = structured_mixed_mesh(n, layers, jitter=0.2, seed=SEED)
+    F = mixed_faces(m)
+    p = np.random.default_rng(SEED).integers(1, 5, m.nel)
+    c = gb.Context(local)
+    c.set_mesh_mixed(m)
+    c.set_coefficients(k=lognormal_k(m.nel, seed=SEED), f=1.0, g=0.0)
+    c.dg_set_degrees(p)
+    c.dg_set_faces(F, penalty=10.0)
+    nd, nv = c.dg_build_structure()
+    out = {"prisms": int((m.el_nv == 6).sum()), "tetrahedra": int((m.el_nv == 4).sum()), "faces": int(F.n),
+           "prism_tetrahedron_faces": int(((F.el2 >= 0) & (m.el_nv[F.el1] != m.el_nv[np.maximum(F.el2, 0)])).sum()),
+           "dofs": nd, "stored_values": nv}
+    v64 = None
+    for key, vol, face in (("fp64", gb.DG_VOLUME_FP64, gb.DG_FACE_FP64),
+                           ("fastest", gb.DG_VOLUME_DWORD, gb.DG_FACE_TC_DWORD)):
+        c.dg_set_volume_kernel(vol)
+        c.dg_set_face_kernel(face)
+        for _ in range(2):
+            c.dg_assemble()
+        tt = np.zeros(3)
+        launches = 0
+        for _ in range(steps):
+            c.dg_assemble()
+            t = c.dg_last_timing()
+            tt += np.array(t[:3])
+            launches = t[3]
+        tot, vol_ms, fa = tt / steps
+        r = {"assemble_ms": tot, "volume_ms": vol_ms, "face_ms": fa, "elem_per_s": m.nel / (tot * 1e-3),
+             "launches": launches}
+        vals, _ = c.dg_get_matrix()
+        if v64 is None:
+            v64 = vals
+        else:
+            r["max_abs_diff_vs_fp64_rel_to_max"] = float(np.max(np.abs(vals - v64)) / np.max(np.abs(v64)))
+            r["speedup_vs_fp64"] = out["fp64"]["assemble_ms"] / tot
+        del vals
+        out[key] = r
+    del v64
+    c.dg_set_volume_kernel(gb.DG_VOLUME_FP64)
+    c.dg_set_face_kernel(gb.DG_FACE_FP64)
+    c.dg_assemble()
+    x, it, res, rel = c.dg_solve(krylov=50, max_iter=100, tol_rel=1e-10)
+    st = c.last_solve_timing()
+    out.update({"elements": m.nel, "gmres_iterations": it, "gmres_ms_per_iteration": st[0] / max(it, 1),
+                "spmv_ms": st[1] / max(st[2], 1)})
+    c.close()
+    return out
+
+
 def mixed_precision_solution_check(gb, local, sizes=(10, 16)):
     """Config-4 form at sizes GMRES(50) converges on in a bench run: p = 3
     prisms, the anisotropic tensor, Dirichlet value 0.3.  Every assembly
@@ -864,6 +924,14 @@ def compact_line(full):
             "fp64": _r(mx["assemble_ms"] + tet["assemble_ms"]),
             "double_word": _r(mx["double_word_assembly"]["assemble_ms"] + tet["double_word_faces"]["assemble_ms"]),
             "elements": mx["elements"] + tet["elements"]}
+    # config 3 as one system on one connected prism + tetrahedron mesh
+    ms = b.get("mixed_dg_system")
+    if ms:
+        out["batch_mixed"]["config3_one_system"] = {
+            "elements": ms["elements"], "prism_tetrahedron_faces": ms["prism_tetrahedron_faces"],
+            "fp64_assemble_ms": _r(ms["fp64"]["assemble_ms"]), "fastest_assemble_ms": _r(ms["fastest"]["assemble_ms"]),
+            "fastest_max_dev_rel_to_max": _r(ms["fastest"]["max_abs_diff_vs_fp64_rel_to_max"], 2),
+            "gmres_ms_per_iteration": _r(ms["gmres_ms_per_iteration"])}
     sv = full.get("serving")
     if sv:
         out["serving"] = {"p50_ms": {str(r["rate_req_s"]): _r(r["p50_ms"]) for r in sv["rates"]},
@@ -1053,6 +1121,7 @@ def main():
     batch = bench_batch(gb, local, max(3, min(args.steps, 10)), fp64_peak)
     dg["mixed_precision_solution"] = mixed_precision_solution_check(gb, local)
     batch["tet_dg_system"] = bench_tet_dg(gb, local, max(3, min(args.steps, 10)))
+    batch["mixed_dg_system"] = bench_mixed_dg_system(gb, local, max(3, min(args.steps, 10)))
 
     # ---------------- serving ----------------
     serving = bench_serving(gb, local) if rank == 0 else None

@@ -119,6 +119,17 @@ int gbfem_table_cache_stats(gbfem_ctx ctx, long long *generation, long long *upl
 int gbfem_set_mesh(gbfem_ctx ctx, int nno, const double *node_xyz, int nel, int nv,
                    const int *el_nodes, int nfa, const int *fa_id, const int *fa_el,
                    const int *fa_side, const int *fa_bc);
+/* A mesh of prisms and tetrahedra together, for the DG path (gbfem_dg_*):
+ * el_nv[e] = 6 (prism) or 4 (tetrahedron), the vertex count
+ * mmr_el_node_coor returns in nodes[0] (mmd_prism/mms_prism_datstr.c:365);
+ * el_nodes: 6 slots per element, the element's vertices first in
+ * mmr_el_node_coor order (a tetrahedron's slots 4 and 5 are ignored).  The
+ * DG face table (gbfem_dg_set_faces) then joins any two elements; a face
+ * between a prism and a tetrahedron is a triangle (the prism's bottom or
+ * top).  The std path refuses such a mesh.  No reference counterpart for the
+ * DG system on it: the reference's DG module is prism-only. */
+int gbfem_set_mesh_mixed(gbfem_ctx ctx, int nno, const double *node_xyz, int nel, const int *el_nv,
+                         const int *el_nodes);
 /* Updates node coordinates only (same topology), e.g. a moved mesh. */
 int gbfem_set_node_coords(gbfem_ctx ctx, const double *node_xyz);
 
@@ -192,14 +203,15 @@ int gbfem_set_matrix(gbfem_ctx ctx, const double *crs_val, const double *rhs);
 /* ---------------------------------------------------------------------- */
 /* Per-element degree p = 1..4 of the tensor monomial DG basis on prisms
  * (ModFEM pdeg 101 p, (p+1)^2(p+2)/2 = 6/18/40/75 functions;
- * apr_get_el_pdeg_numshap, apd_dg_prism/aps_dg_prism_intf.c:725-775).  On a
- * tetrahedral mesh the complete monomial basis xi^a eta^b zeta^c,
+ * apr_get_el_pdeg_numshap, apd_dg_prism/aps_dg_prism_intf.c:725-775).  On
+ * tetrahedra (of a tetrahedral or a mixed mesh) the complete monomial basis xi^a eta^b zeta^c,
  * a+b+c <= p, (p+1)(p+2)(p+3)/6 = 4/10/20/35 functions (no reference
  * counterpart: apd_dg_prism is prism-only), with the same weak form.
  * Coefficients from gbfem_set_coefficients (a tensor must be symmetric). */
 int gbfem_dg_set_degrees(gbfem_ctx ctx, const int *p_el);
-/* Face table of the mesh (on tetrahedral meshes: triangles, side k = the
- * face opposite local vertex k), the data the DG weak form reads per face through
+/* Face table of the mesh (tetrahedra: triangles, side k = the face
+ * opposite local vertex k; on a mesh of prisms and tetrahedra each face's
+ * side is that of its first neighbour's type), the data the DG weak form reads per face through
  * mmr_fa_type (mmd_prism/mms_prism_datstr.c:969), mmr_fa_bc (:993),
  * mmr_fa_eq_neig (:1140) and mmr_fa_node_coor (:1488): type 3 (triangle) or
  * 4 (quadrilateral); bc flag; two neighbours per face (0-based, second -1 on

@@ -40,6 +40,7 @@ SIGNATURES = [
     ("gbfem_invalidate_tables", _ci, [_vp]),
     ("gbfem_table_cache_stats", _ci, [_vp, _pll, _pll]),
     ("gbfem_set_mesh", _ci, [_vp, _ci, _vp, _ci, _ci, _vp, _ci, _vp, _vp, _vp, _vp]),
+    ("gbfem_set_mesh_mixed", _ci, [_vp, _ci, _vp, _ci, _vp, _vp]),
     ("gbfem_set_node_coords", _ci, [_vp, _vp]),
     ("gbfem_set_coefficients", _ci, [_vp, _vp, _vp, _cd, _cd, _cd]),
     ("gbfem_set_crs_structure", _ci, [_vp, _ci, _vp, _cll, _vp, _vp]),
@@ -189,6 +190,16 @@ class Context:
         self._check(self.L.gbfem_set_mesh(self._h, xyz.shape[0], _p(xyz), el.shape[0], nv, _p(el), fel.size,
                                           _p(fid), _p(fel), _p(fsd), _p(fbc)))
         self.nno, self.nel, self.nv, self.nfa = xyz.shape[0], el.shape[0], nv, fel.size
+
+    def set_mesh_mixed(self, mesh):
+        """gbfem_set_mesh_mixed: a mesh of prisms and tetrahedra together (DG
+        only); mesh.el_nodes has 6 slots per element, mesh.el_nv the vertex
+        count (modfem_gb300.mesh.structured_mixed_mesh)."""
+        xyz = _f64(mesh.coords)
+        el = _i32(mesh.el_nodes)
+        nv = _i32(mesh.el_nv)
+        self._check(self.L.gbfem_set_mesh_mixed(self._h, xyz.shape[0], _p(xyz), el.shape[0], _p(nv), _p(el)))
+        self.nno, self.nel, self.nv, self.nfa = xyz.shape[0], el.shape[0], 6, 0
 
     def set_node_coords(self, xyz):
         xyz = _f64(xyz)

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libmodfem_gb300.so")
 OBJDIR = os.path.join(HERE, "_build")
 SOURCES = ["api.cu", "std_kernels.cu", "krylov.cu", "structure.cpp", "noalloc.cu", "dg_kernels.cu", "dg_faces.cu",
-           "dg_krylov.cu", "serve.cu", "dg_tc.cu", "structure_gpu.cu", "io.cpp", "dg_batch.cu", "dg_tc_faces.cu", "dg_tet_faces.cu", "gmres_dev.cu"]
+           "dg_krylov.cu", "serve.cu", "dg_tc.cu", "structure_gpu.cu", "io.cpp", "dg_batch.cu", "dg_tc_faces.cu", "dg_tet_faces.cu", "gmres_dev.cu", "dg_mixed_faces.cu"]
 HEADERS = ["gbfem_internal.h", "prism_std.cuh", "prism_dw.cuh", "dword.cuh", "dg_face.cuh", "dg_spmv.cuh", "dg_volume.cuh", "tc_ptx.cuh", "dg_tables.h", os.path.join("..", "..", "include", "modfem_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

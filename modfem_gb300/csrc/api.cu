@@ -26,23 +26,35 @@ static int upload(gbfem_ctx c, DevBuf<T> &d, const T *h, size_t n) {
   return 0;
 }
 
-// block class of the DG SpMV kernels: degree p on prisms, 4 + p on tetrahedra
-static inline int dg_class_off(gbfem_ctx c) { return c->nv == GBFEM_TETRA ? 4 : 0; }
+static const int kDgNs[5] = {0, 6, 18, 40, 75};
+static const int kDgTetNs[5] = {0, 4, 10, 20, 35};
+static inline bool el_is_tet(gbfem_ctx c, int e) { return c->mixed ? c->h_el_tet[e] != 0 : c->nv == GBFEM_TETRA; }
+static inline int el_nverts(gbfem_ctx c, int e) { return el_is_tet(c, e) ? 4 : 6; }
+// functions of DG element e: tensor basis on prisms, complete basis on
+// tetrahedra
+static inline int dg_ns_el(gbfem_ctx c, int e) {
+  return el_is_tet(c, e) ? kDgTetNs[c->dg_p[e]] : kDgNs[c->dg_p[e]];
+}
+// element class of the DG kernels: 1..4 prisms of degree p, 5..8 tetrahedra
+static inline int dg_cls(gbfem_ctx c, int e) { return c->dg_p[e] + (el_is_tet(c, e) ? 4 : 0); }
+// the tetrahedron kernels' vertex array (4 per element)
+static inline const int *tet_nodes(gbfem_ctx c) { return c->mixed ? c->el_nodes4.p : c->el_nodes.p; }
 
-// Block SpMV over all DG block rows, one launch per degree class.
+// Block SpMV over all DG block rows, one launch per element class (1..4:
+// prisms of degree 1..4, 5..8: tetrahedra of degree 1..4).
 static int dg_spmv(gbfem_ctx c, int mode, const double *x, const double *b, double *out) {
   int n = 0;
-  for (int p = 1; p <= 4; p++) {
-    if (!c->dg_list[p].p) continue;
+  for (int cls = 1; cls <= 8; cls++) {
+    if (!c->dg_list[cls].p) continue;
     if (mode == 2 && c->dg_residual_dd) {
-      const int r = gbfem::launch_dg_block_residual_dd(c->stream, p + dg_class_off(c), (int)c->dg_list[p].n,
-                                                       c->dg_list[p].p, c->dg_roff_d.p, c->dg_row_val_d.p,
-                                                       c->dg_cx_off_d.p, c->dg_colx_d.p, c->dg_val.p, x, b, out);
+      const int r = gbfem::launch_dg_block_residual_dd(c->stream, cls, (int)c->dg_list[cls].n, c->dg_list[cls].p,
+                                                       c->dg_roff_d.p, c->dg_row_val_d.p, c->dg_cx_off_d.p,
+                                                       c->dg_colx_d.p, c->dg_val.p, x, b, out);
       if (r < 0) return r;
       n += r;
       continue;
     }
-    const int r = gbfem::launch_dg_block_spmv(c->stream, mode, p + dg_class_off(c), (int)c->dg_list[p].n, c->dg_list[p].p,
+    const int r = gbfem::launch_dg_block_spmv(c->stream, mode, cls, (int)c->dg_list[cls].n, c->dg_list[cls].p,
                                               c->dg_roff_d.p, c->dg_row_val_d.p, c->dg_cx_off_d.p, c->dg_colx_d.p,
                                               c->dg_val.p, c->dg_dinv_off_d.p, c->dg_dinv.p, x, b, out);
     if (r < 0) return r;
@@ -113,11 +125,17 @@ int gbfem_destroy(gbfem_ctx c) {
                           &c->el_table, &c->el_perm, &c->fa_perm, &c->fa_map, &c->err, &c->in_id,
                           &c->in_pos, &c->in_table, &c->dg_roff_d};
   for (auto *b : ibufs) b->release();
+  for (int cls = 0; cls < 9; cls++) {
+    c->dg_list[cls].release();
+    c->dg_mlist[cls].release();
+  }
   for (int p = 0; p < 5; p++) {
-    c->dg_list[p].release();
     c->dg_flist_tc[p].release();
     c->dg_flist_64[p].release();
   }
+  c->dg_mhf_ptr.release();
+  c->dg_mhf.release();
+  c->el_nodes4.release();
   c->dg_boff_diag_d.release();
   c->dg_val.release();
   c->dg_rhs.release();
@@ -165,7 +183,9 @@ long long gbfem_device_bytes(gbfem_ctx c) {
        c->dg_boff_diag_d.bytes() + c->dg_dinv_off_d.bytes() + c->dg_bptr_d.bytes() + c->dg_bcol_d.bytes() +
        c->dg_hf_ptr.bytes() + c->dg_p_d.bytes() + c->dg_roff_d.bytes() + c->dg_colx_d.bytes() +
        c->dg_row_val_d.bytes() + c->dg_cx_off_d.bytes();
-  for (int p = 0; p < 5; p++) s += c->dg_list[p].bytes() + c->dg_flist_tc[p].bytes() + c->dg_flist_64[p].bytes();
+  for (int cls = 0; cls < 9; cls++) s += c->dg_list[cls].bytes() + c->dg_mlist[cls].bytes();
+  for (int p = 0; p < 5; p++) s += c->dg_flist_tc[p].bytes() + c->dg_flist_64[p].bytes();
+  s += c->dg_mhf_ptr.bytes() + c->dg_mhf.bytes() + c->el_nodes4.bytes();
   return s;
 }
 
@@ -223,6 +243,9 @@ int gbfem_set_mesh(gbfem_ctx c, int nno, const double *node_xyz, int nel, int nv
   c->nel = nel;
   c->nv = nv;
   c->nfa = nfa;
+  c->mixed = false;
+  c->h_el_tet.clear();
+  c->el_nodes4.release();
   c->h_el_nodes.assign(el_nodes, el_nodes + (size_t)nel * nv);
   c->h_fa_el.assign(fa_el, fa_el + nfa);
   c->h_fa_side.assign(fa_side, fa_side + nfa);
@@ -241,6 +264,51 @@ int gbfem_set_mesh(gbfem_ctx c, int nno, const double *node_xyz, int nel, int nv
   GB_TRY(upload(c, c->fa_side, fa_side, (size_t)nfa));
   GB_TRY(upload(c, c->fa_map, c->fa_index_of_id.data(), c->fa_index_of_id.size()));
   c->have_structure = c->have_tables = false;
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int gbfem_set_mesh_mixed(gbfem_ctx c, int nno, const double *node_xyz, int nel, const int *el_nv,
+                         const int *el_nodes) {
+  GB_CHECK(c, "null context");
+  GB_CHECK(nno > 0 && nel > 0 && node_xyz && el_nodes && el_nv, "empty mesh");
+  GB_CUDA(cudaSetDevice(c->device));
+  std::vector<int> en((size_t)nel * 6), en4((size_t)nel * 4);
+  std::vector<unsigned char> tet(nel);
+  for (int e = 0; e < nel; e++) {
+    GB_CHECK(el_nv[e] == GBFEM_PRISM || el_nv[e] == GBFEM_TETRA,
+             "element " + std::to_string(e) + ": vertex count must be 6 (prism) or 4 (tetrahedron)");
+    tet[e] = el_nv[e] == GBFEM_TETRA;
+    for (int k = 0; k < el_nv[e]; k++)
+      GB_CHECK(el_nodes[6 * (size_t)e + k] >= 0 && el_nodes[6 * (size_t)e + k] < nno,
+               "element vertex index out of range");
+    // unused slots of a tetrahedron repeat its first vertex: every slot is
+    // a valid node
+    for (int k = 0; k < 6; k++) en[6 * (size_t)e + k] = el_nodes[6 * (size_t)e + (k < el_nv[e] ? k : 0)];
+    for (int k = 0; k < 4; k++) en4[4 * (size_t)e + k] = el_nodes[6 * (size_t)e + k];
+  }
+  c->nno = nno;
+  c->nel = nel;
+  c->nv = GBFEM_PRISM;  // element slots
+  c->nfa = 0;
+  c->mixed = true;
+  c->h_el_tet.swap(tet);
+  c->h_el_nodes.swap(en);
+  c->h_fa_el.clear();
+  c->h_fa_side.clear();
+  c->h_fa_id.clear();
+  c->max_fa_id = 0;
+  c->fa_index_of_id.assign(1, -1);
+  GB_TRY(upload(c, c->xyz, node_xyz, (size_t)nno * 3));
+  GB_TRY(upload(c, c->el_nodes, c->h_el_nodes.data(), c->h_el_nodes.size()));
+  GB_TRY(upload(c, c->el_nodes4, en4.data(), en4.size()));
+  GB_TRY(upload(c, c->fa_map, c->fa_index_of_id.data(), c->fa_index_of_id.size()));
+  c->fa_el.release();
+  c->fa_side.release();
+  c->have_structure = c->have_tables = false;
+  c->dg_p.clear();
+  c->dg_nfa = -1;
+  c->dg_ready = false;
   GB_CUDA(cudaStreamSynchronize(c->stream));
   return 0;
 }
@@ -311,6 +379,7 @@ int gbfem_table_cache_stats(gbfem_ctx c, long long *generation, long long *uploa
 int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long long nnz, const int *row_ptr,
                             const int *col_ind) {
   GB_CHECK(c && c->nno > 0, "mesh not set");
+  GB_CHECK(!c->mixed, "meshes of prisms and tetrahedra together are for the DG path (gbfem_dg_*)");
   GB_CHECK(ndof > 0 && nnz > 0 && nnz < 2147483647LL && row_ptr && col_ind, "bad CRS structure");
   GB_CHECK(row_ptr[0] == 0 && row_ptr[ndof] == nnz, "row_ptr inconsistent with nnz");
   c->ndof = ndof;
@@ -345,6 +414,7 @@ int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long 
 
 int gbfem_build_structure(gbfem_ctx c, int *ndof, long long *nnz, int *nr_colors) {
   GB_CHECK(c && c->nno > 0, "mesh not set");
+  GB_CHECK(!c->mixed, "meshes of prisms and tetrahedra together are for the DG path (gbfem_dg_*)");
   GB_TRY(gbfem::build_host_structure(c->nno, c->nel, c->nv, c->h_el_nodes.data(), c->nfa, c->h_fa_el.data(),
                                      c->h_fa_side.data(), c->hs));
   c->ndof = c->hs.ndof;
@@ -370,6 +440,7 @@ int gbfem_build_structure(gbfem_ctx c, int *ndof, long long *nnz, int *nr_colors
 
 int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
   GB_CHECK(c && c->nno > 0, "mesh not set");
+  GB_CHECK(!c->mixed, "meshes of prisms and tetrahedra together are for the DG path (gbfem_dg_*)");
   GB_CUDA(cudaSetDevice(c->device));
   GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
   int nd = 0;
@@ -780,29 +851,28 @@ int gbfem_dg_set_faces(gbfem_ctx c, int nfa, const int *fa_type, const int *fa_b
                        const int *fa_side, const int *fa_nodes) {
   GB_CHECK(c && c->nel > 0, "DG needs a mesh (gbfem_set_mesh)");
   GB_CHECK(nfa >= 0, "negative face count");
-  const bool tet = c->nv == GBFEM_TETRA;
-  const int nv = c->nv;
   GB_CHECK(nfa == 0 || (fa_type && fa_bc && fa_el && fa_side && fa_nodes), "face arrays missing");
-  const int nel = c->nel;
+  const int nel = c->nel, stride = c->nv;
   const int *en = c->h_el_nodes.data();
   for (int f = 0; f < nfa; f++) {
     const int t = fa_type[f], e1 = fa_el[2 * f], e2 = fa_el[2 * f + 1], sd = fa_side[f];
     GB_CHECK(t == 3 || t == 4, "face type must be 3 (triangle) or 4 (quadrilateral)");
     GB_CHECK(e1 >= 0 && e1 < nel, "face neighbour out of range");
     GB_CHECK(e2 == -1 || (e2 >= 0 && e2 < nel && e2 != e1), "second face neighbour out of range");
-    if (tet)
+    if (el_is_tet(c, e1))
       GB_CHECK(t == 3 && sd >= 0 && sd <= 3, "tetrahedron faces are triangles on sides 0..3");
     else
       GB_CHECK(sd >= 0 && sd <= 4 && (sd < 2) == (t == 3), "face side does not match the face type");
+    GB_CHECK(e2 < 0 || el_is_tet(c, e1) == el_is_tet(c, e2) || t == 3,
+             "a face between a prism and a tetrahedron must be a triangle");
     GB_CHECK(e2 >= 0 || (fa_bc[f] > 0 && fa_bc[f] < 10),
              "boundary faces must carry a Dirichlet flag (0 < bc < 10)");
+    const int nv1 = el_nverts(c, e1), nv2 = e2 >= 0 ? el_nverts(c, e2) : 0;
     for (int i = 0; i < t; i++) {
       const int v = fa_nodes[4 * f + i];
       bool in1 = false, in2 = e2 < 0;
-      for (int k = 0; k < nv; k++) {
-        in1 = in1 || en[nv * (size_t)e1 + k] == v;
-        if (e2 >= 0) in2 = in2 || en[nv * (size_t)e2 + k] == v;
-      }
+      for (int k = 0; k < nv1; k++) in1 = in1 || en[stride * (size_t)e1 + k] == v;
+      for (int k = 0; k < nv2; k++) in2 = in2 || en[stride * (size_t)e2 + k] == v;
       GB_CHECK(in1 && in2, "face vertex is not a vertex of its neighbours");
     }
   }
@@ -841,12 +911,6 @@ int gbfem_dg_set_penalty(gbfem_ctx c, double pen) {
   return 0;
 }
 
-static const int kDgNs[5] = {0, 6, 18, 40, 75};
-static const int kDgTetNs[5] = {0, 4, 10, 20, 35};
-// functions of a DG element of degree p: tensor basis on prisms, complete
-// basis on tetrahedra
-static inline int dg_ns(gbfem_ctx c, int p) { return c->nv == GBFEM_TETRA ? kDgTetNs[p] : kDgNs[p]; }
-
 int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   GB_CHECK(c && !c->dg_p.empty(), "DG degrees not set (gbfem_dg_set_degrees)");
   GB_CUDA(cudaSetDevice(c->device));
@@ -855,7 +919,7 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   // dof blocks in element order (utr_get_list_ent, DG branch: one dof entity
   // per element, uts_ls_intf.c:640-700)
   c->dg_roff.assign(nel + 1, 0);
-  for (int e = 0; e < nel; e++) c->dg_roff[e + 1] = c->dg_roff[e] + dg_ns(c, c->dg_p[e]);
+  for (int e = 0; e < nel; e++) c->dg_roff[e + 1] = c->dg_roff[e] + dg_ns_el(c, e);
   c->dg_ndof = c->dg_roff[nel];
   // block row e: the element and its face neighbours, ascending (the sorted
   // neighbour lists of sir_create, sis_mkb_intf.c:1100-1146)
@@ -888,11 +952,11 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   c->dg_boff.assign(nblk + 1, 0);
   std::vector<long long> diag(nel), dinv_off(nel + 1, 0);
   for (int e = 0; e < nel; e++) {
-    const long long ne = dg_ns(c, c->dg_p[e]);
+    const long long ne = dg_ns_el(c, e);
     for (int k = c->dg_bptr[e]; k < c->dg_bptr[e + 1]; k++) {
       const int col = c->dg_bcol[k];
       if (col == e) diag[e] = c->dg_boff[k];
-      c->dg_boff[k + 1] = c->dg_boff[k] + ne * dg_ns(c, c->dg_p[col]);
+      c->dg_boff[k + 1] = c->dg_boff[k] + ne * dg_ns_el(c, col);
     }
     dinv_off[e + 1] = dinv_off[e] + ne * ne;
   }
@@ -902,19 +966,29 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
     return c->dg_boff[std::lower_bound(b0, b1, col) - c->dg_bcol.begin()];
   };
   // face incidences per owner, faces in table order (the reference integrates
-  // faces in face order after the elements)
-  std::vector<int> hcnt(nel + 1, 0);
+  // faces in face order after the elements); faces between a prism and a
+  // tetrahedron go to a second table of their own
+  auto is_mixed_face = [&](int f) {
+    const int e1 = c->dg_fa_el[2 * f], e2 = c->dg_fa_el[2 * f + 1];
+    return e2 >= 0 && el_is_tet(c, e1) != el_is_tet(c, e2);
+  };
+  std::vector<int> hcnt(nel + 1, 0), mcnt(nel + 1, 0);
   for (int f = 0; f < nfa; f++) {
-    hcnt[c->dg_fa_el[2 * f]]++;
-    if (c->dg_fa_el[2 * f + 1] >= 0) hcnt[c->dg_fa_el[2 * f + 1]]++;
+    std::vector<int> &cn = is_mixed_face(f) ? mcnt : hcnt;
+    cn[c->dg_fa_el[2 * f]]++;
+    if (c->dg_fa_el[2 * f + 1] >= 0) cn[c->dg_fa_el[2 * f + 1]]++;
   }
-  std::vector<int> hptr(nel + 1, 0);
-  for (int e = 0; e < nel; e++) hptr[e + 1] = hptr[e] + hcnt[e];
-  std::vector<gbfem::DgHalfFace> hf(hptr[nel]);
-  std::vector<int> hfill(hptr.begin(), hptr.end() - 1);
+  std::vector<int> hptr(nel + 1, 0), mptr(nel + 1, 0);
+  for (int e = 0; e < nel; e++) {
+    hptr[e + 1] = hptr[e] + hcnt[e];
+    mptr[e + 1] = mptr[e] + mcnt[e];
+  }
+  std::vector<gbfem::DgHalfFace> hf(hptr[nel]), mhf(mptr[nel]);
+  std::vector<int> hfill(hptr.begin(), hptr.end() - 1), mfill(mptr.begin(), mptr.end() - 1);
   const int *en = c->h_el_nodes.data();
+  const int stride = c->nv;  // element slots in h_el_nodes (6 on mixed meshes)
   // face-point configurations (vertex count, local vertex order) of the
-  // tensor-core face kernel's basis tables
+  // tensor-core face kernel's basis tables (faces between prisms)
   std::vector<unsigned char> cfgs;
   auto cfg_of = [&](int nfv, const unsigned char *loc) -> int {
     const int ncfg = (int)cfgs.size() / 5;
@@ -925,7 +999,7 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
     for (int i = 0; i < 4; i++) cfgs.push_back(i < nfv ? loc[i] : 0);
     return ncfg;
   };
-  std::vector<int> face_rep(nfa, -1);  // the first neighbour's record of each face
+  std::vector<int> face_rep(nfa, -1);  // the first neighbour's record of each face between prisms
   for (int f = 0; f < nfa; f++) {
     gbfem::DgHalfFace h;
     memset(&h, 0, sizeof(h));
@@ -934,20 +1008,29 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
     h.side1 = c->dg_fa_side[f];
     h.nfv = c->dg_fa_type[f];
     h.face = f;
+    const int nv1 = el_nverts(c, h.el1), nv2 = h.el2 >= 0 ? el_nverts(c, h.el2) : 0;
     for (int i = 0; i < h.nfv; i++) {
       const int v = c->dg_fa_nodes[4 * f + i];
-      for (int k = 0; k < c->nv; k++) {
-        if (en[c->nv * (size_t)h.el1 + k] == v) h.loc1[i] = (unsigned char)k;
-        if (h.el2 >= 0 && en[c->nv * (size_t)h.el2 + k] == v) h.loc2[i] = (unsigned char)k;
-      }
+      for (int k = 0; k < nv1; k++)
+        if (en[stride * (size_t)h.el1 + k] == v) h.loc1[i] = (unsigned char)k;
+      for (int k = 0; k < nv2; k++)
+        if (en[stride * (size_t)h.el2 + k] == v) h.loc2[i] = (unsigned char)k;
     }
-    if (c->nv == GBFEM_PRISM) {
+    const bool mixedf = is_mixed_face(f);
+    if (!mixedf && !el_is_tet(c, h.el1)) {
       h.cfg1 = (unsigned char)cfg_of(h.nfv, h.loc1);
       h.cfg2 = h.el2 >= 0 ? (unsigned char)cfg_of(h.nfv, h.loc2) : 0;
     }
     h.owner_is_2 = 0;
     h.blk = h.el2 >= 0 ? block_of(h.el1, h.el2) : -1;
-    face_rep[f] = hfill[h.el1];
+    if (mixedf) {
+      mhf[mfill[h.el1]++] = h;
+      h.owner_is_2 = 1;
+      h.blk = block_of(h.el2, h.el1);
+      mhf[mfill[h.el2]++] = h;
+      continue;
+    }
+    if (!el_is_tet(c, h.el1)) face_rep[f] = hfill[h.el1];
     hf[hfill[h.el1]++] = h;
     if (h.el2 >= 0) {
       h.owner_is_2 = 1;
@@ -955,18 +1038,19 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
       hf[hfill[h.el2]++] = h;
     }
   }
-  // tables and face list for the tensor-core face kernel (prisms, at most
-  // DG_TF_MAXCFG configurations; otherwise that kernel is not used)
+  // tables and face list for the tensor-core face kernel (faces between
+  // prisms, at most DG_TF_MAXCFG configurations; otherwise that kernel is
+  // not used)
   c->dg_ftab_ok = false;
   c->dg_tcface.release();
-  if (c->nv == GBFEM_PRISM && (int)cfgs.size() / 5 < gbfem::DG_TF_MAXCFG && nfa > 0) {
+  if (!cfgs.empty() && (int)cfgs.size() / 5 < gbfem::DG_TF_MAXCFG) {
     const int ncfg = (int)cfgs.size() / 5;
     std::vector<long long> toff((size_t)ncfg * 9);
     const long long tsize = gbfem::dg_face_table_size(ncfg, cfgs.data(), toff.data());
     std::vector<int> tcf;  // faces whose sides both have degree <= 3
     for (int f = 0; f < nfa; f++) {
       const int e1 = c->dg_fa_el[2 * f], e2 = c->dg_fa_el[2 * f + 1];
-      if (c->dg_p[e1] <= 3 && (e2 < 0 || c->dg_p[e2] <= 3)) tcf.push_back(face_rep[f]);
+      if (face_rep[f] >= 0 && c->dg_p[e1] <= 3 && (e2 < 0 || c->dg_p[e2] <= 3)) tcf.push_back(face_rep[f]);
     }
     GB_TRY(upload(c, c->dg_fcfg, cfgs.data(), cfgs.size()));
     GB_TRY(upload(c, c->dg_ftab_off, toff.data(), toff.size()));
@@ -980,7 +1064,7 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
   for (int e = 0; e < nel; e++) {
     row_val[e] = c->dg_boff[c->dg_bptr[e]];
     long long nct = 0;
-    for (int k = c->dg_bptr[e]; k < c->dg_bptr[e + 1]; k++) nct += dg_ns(c, c->dg_p[c->dg_bcol[k]]);
+    for (int k = c->dg_bptr[e]; k < c->dg_bptr[e + 1]; k++) nct += dg_ns_el(c, c->dg_bcol[k]);
     cx_off[e + 1] = cx_off[e] + nct;
   }
   std::vector<int> colx(cx_off[nel]);
@@ -991,28 +1075,34 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
       for (int j = c->dg_roff[col]; j < c->dg_roff[col + 1]; j++) colx[t++] = j;
     }
   }
-  // elements per degree class, ordered by their row's column count so that
-  // the rows a warp multiplies together take the same number of steps
-  for (int p = 1; p <= 4; p++) {
-    std::vector<int> lst;
+  // elements per class (1..4 prisms, 5..8 tetrahedra of degree 1..4),
+  // ordered by their row's column count so that the rows a warp multiplies
+  // together take the same number of steps; the owners of faces between a
+  // prism and a tetrahedron per class
+  for (int cls = 1; cls <= 8; cls++) {
+    std::vector<int> lst, mlst;
     for (int e = 0; e < nel; e++)
-      if (c->dg_p[e] == p) lst.push_back(e);
-    if (lst.empty()) {
-      c->dg_list[p].release();
-      continue;
-    }
+      if (dg_cls(c, e) == cls) {
+        lst.push_back(e);
+        if (mcnt[e]) mlst.push_back(e);
+      }
+    c->dg_list[cls].release();
+    c->dg_mlist[cls].release();
+    if (lst.empty()) continue;
     std::stable_sort(lst.begin(), lst.end(), [&](int a, int b) {
       return cx_off[a + 1] - cx_off[a] > cx_off[b + 1] - cx_off[b];
     });
-    GB_TRY(upload(c, c->dg_list[p], lst.data(), lst.size()));
+    GB_TRY(upload(c, c->dg_list[cls], lst.data(), lst.size()));
+    if (!mlst.empty()) GB_TRY(upload(c, c->dg_mlist[cls], mlst.data(), mlst.size()));
   }
-  // face owners of degree <= 3 whose neighbours all have degree <= 3 suit
-  // the tensor-core face kernel; the others keep the FP64 one
+  // prism face owners of degree <= 3 whose neighbours across faces between
+  // prisms all have degree <= 3 suit the tensor-core face kernel; the others
+  // keep the FP64 one
   for (int p = 1; p <= 4; p++) {
     std::vector<int> tcl, fpl;
     for (int e = 0; e < nel; e++) {
-      if (c->dg_p[e] != p) continue;
-      bool ok = p <= 3 && c->nv == GBFEM_PRISM;
+      if (c->dg_p[e] != p || el_is_tet(c, e)) continue;
+      bool ok = p <= 3;
       for (int h = hptr[e]; ok && h < hptr[e + 1]; h++) {
         const int nb = hf[h].owner_is_2 ? hf[h].el1 : hf[h].el2;
         if (nb >= 0 && c->dg_p[nb] > 3) ok = false;
@@ -1035,6 +1125,13 @@ int gbfem_dg_build_structure(gbfem_ctx c, int *ndof, long long *nval) {
     GB_TRY(upload(c, c->dg_hf, hf.data(), hf.size()));
   else
     c->dg_hf.release();
+  if (!mhf.empty()) {
+    GB_TRY(upload(c, c->dg_mhf_ptr, mptr.data(), mptr.size()));
+    GB_TRY(upload(c, c->dg_mhf, mhf.data(), mhf.size()));
+  } else {
+    c->dg_mhf_ptr.release();
+    c->dg_mhf.release();
+  }
   GB_TRY(upload(c, c->dg_bptr_d, c->dg_bptr.data(), c->dg_bptr.size()));
   GB_TRY(upload(c, c->dg_bcol_d, c->dg_bcol.data(), c->dg_bcol.size()));
   GB_TRY(upload(c, c->dg_boff_d, c->dg_boff.data(), c->dg_boff.size()));
@@ -1085,7 +1182,7 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     long long tot = 0;
     for (int p = 1; p <= 3; p++) {
       share_off[p] = tot;
-      const long long ns = dg_ns(c, p);
+      const long long ns = kDgNs[p];
       tot += (long long)c->dg_flist_tc[p].n * (ns * ns + ns);
     }
     GB_TRY(c->dg_fshare.alloc((size_t)std::max(tot, 1LL)));
@@ -1111,14 +1208,19 @@ int gbfem_dg_assemble(gbfem_ctx c) {
     }
     GB_CUDA(cudaEventRecord(c->side_ev[1], c->side_stream));
   }
+  for (int cls = 5; cls <= 8; cls++) {
+    if (!c->dg_list[cls].p) continue;
+    const int r = gbfem::launch_dg_tet_elements(c->stream, c->device, cls - 4, (int)c->dg_list[cls].n,
+                                                c->dg_list[cls].p, tet_nodes(c), c->xyz.p, c->k_el.p, c->D_el.p,
+                                                c->f, c->dg_boff_diag_d.p, c->dg_roff_d.p, c->dg_val.p,
+                                                c->dg_rhs.p);
+    GB_TRY(r);
+    launches += r;
+  }
   for (int p = 1; p <= 4; p++) {
     if (!c->dg_list[p].p) continue;
     int r;
-    if (c->nv == GBFEM_TETRA)
-      r = gbfem::launch_dg_tet_elements(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p,
-                                        c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->dg_boff_diag_d.p,
-                                        c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p);
-    else if (tc && gbfem::dg_tc_supported(p))  // TC_DWORD: split BF16 on the tensor cores
+    if (tc && gbfem::dg_tc_supported(p))  // TC_DWORD: split BF16 on the tensor cores
       r = gbfem::launch_dg_tc_volume(c->stream, c->device, p, (int)c->dg_list[p].n, c->dg_list[p].p, c->el_nodes.p,
                                      c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->dg_boff_diag_d.p, c->dg_roff_d.p,
                                      c->dg_val.p, c->dg_rhs.p, c->err.p,
@@ -1144,21 +1246,24 @@ int gbfem_dg_assemble(gbfem_ctx c) {
       launches += r;
     }
   }
+  const bool mixed_faces = c->dg_mhf.p != nullptr;
+  if (mixed_faces && !tc && !(tcf && c->dg_hf.p) && !overlap)
+    GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
   if (c->dg_hf.p) {
     if (tcf && !tc && !overlap) GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+    for (int cls = 5; cls <= 8; cls++) {
+      if (!c->dg_list[cls].p) continue;
+      const int r = gbfem::launch_dg_tet_faces(c->stream, cls - 4, (int)c->dg_list[cls].n, c->dg_list[cls].p,
+                                               c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, tet_nodes(c), c->xyz.p,
+                                               c->k_el.p, c->D_el.p, c->dg_pen, c->g, c->dg_boff_diag_d.p,
+                                               c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p,
+                                               c->dg_face_mode == GBFEM_DG_FACE_DWORD ||
+                                                   c->dg_face_mode == GBFEM_DG_FACE_TC_DWORD);
+      GB_TRY(r);
+      launches += r;
+    }
     for (int p = 1; p <= 4; p++) {
       if (!c->dg_list[p].p) continue;
-      if (c->nv == GBFEM_TETRA) {
-        const int r = gbfem::launch_dg_tet_faces(c->stream, p, (int)c->dg_list[p].n, c->dg_list[p].p,
-                                                 c->dg_hf_ptr.p, c->dg_hf.p, c->dg_p_d.p, c->el_nodes.p, c->xyz.p,
-                                                 c->k_el.p, c->D_el.p, c->dg_pen, c->g, c->dg_boff_diag_d.p,
-                                                 c->dg_roff_d.p, c->dg_val.p, c->dg_rhs.p,
-                                                 c->dg_face_mode == GBFEM_DG_FACE_DWORD ||
-                                                     c->dg_face_mode == GBFEM_DG_FACE_TC_DWORD);
-        GB_TRY(r);
-        launches += r;
-        continue;
-      }
       if (tcf && c->dg_ftab_ok) {
         // tensor-core eligible owners (done above when overlapped), then the
         // rest on the FP64 (or, in TC_DWORD mode, the double-word) kernel;
@@ -1207,18 +1312,30 @@ int gbfem_dg_assemble(gbfem_ctx c) {
       }
     }
   }
+  // faces between a prism and a tetrahedron, after every other face kernel
+  // (their owners add to the diagonal blocks directly); FP64 in every mode
+  for (int cls = 1; mixed_faces && cls <= 8; cls++) {
+    if (!c->dg_mlist[cls].p) continue;
+    const int r = gbfem::launch_dg_mixed_faces(c->stream, cls, (int)c->dg_mlist[cls].n, c->dg_mlist[cls].p,
+                                               c->dg_mhf_ptr.p, c->dg_mhf.p, c->dg_p_d.p, c->el_nodes.p,
+                                               tet_nodes(c), c->xyz.p, c->k_el.p, c->D_el.p, c->dg_pen,
+                                               c->dg_boff_diag_d.p, c->dg_val.p, c->err.p);
+    GB_TRY(r);
+    launches += r;
+  }
   cudaEventRecord(c->ev1, c->stream);
   GB_CUDA(cudaEventSynchronize(c->ev1));
   cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
   cudaEventElapsedTime(&c->last_el_ms, c->ev0, c->ev2);
   cudaEventElapsedTime(&c->last_fa_ms, c->ev2, c->ev1);
-  if (tc || (tcf && c->dg_hf.p)) {
+  if (tc || (tcf && c->dg_hf.p) || mixed_faces) {
     int herr = 0;
     GB_CUDA(cudaMemcpy(&herr, c->err.p, sizeof(int), cudaMemcpyDeviceToHost));
     GB_CHECK(herr != 5, "tensor-core volume kernel: a pipeline wait expired");
     GB_CHECK(herr != 6, "tensor-core face kernel: an MMA completion wait expired");
     GB_CHECK(herr != 7, "tensor-core face kernel: an owner with a degree-4 neighbour reached it");
-    GB_CHECK(herr == 0, "tensor-core kernel error " + std::to_string(herr));
+    GB_CHECK(herr != 8, "prism-tetrahedron face kernel: a face record does not match its owner class");
+    GB_CHECK(herr == 0, "DG assembly kernel error " + std::to_string(herr));
   }
   c->last_launches = launches;
   return 0;
@@ -1607,10 +1724,10 @@ int gbfem_dg_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int in
   GmresOp op = [&](int mode, const double *in, double *out) -> int {
     if (mode == 1 && c->dg_spmv_dword) {
       int nl = 0;
-      for (int p = 1; p <= 4; p++) {
-        if (!c->dg_list[p].p) continue;
-        const int r = gbfem::launch_dg_block_spmv_dw(c->stream, mode, p + dg_class_off(c), (int)c->dg_list[p].n,
-                                                     c->dg_list[p].p, c->dg_roff_d.p, c->dg_row_val_d.p,
+      for (int cls = 1; cls <= 8; cls++) {
+        if (!c->dg_list[cls].p) continue;
+        const int r = gbfem::launch_dg_block_spmv_dw(c->stream, mode, cls, (int)c->dg_list[cls].n,
+                                                     c->dg_list[cls].p, c->dg_roff_d.p, c->dg_row_val_d.p,
                                                      c->dg_cx_off_d.p, c->dg_colx_d.p, c->dg_valdw.p,
                                                      c->dg_dinv_off_d.p, c->dg_dinvdw.p, in, nullptr, out);
         if (r < 0) return r;
@@ -1627,10 +1744,9 @@ int gbfem_dg_solve(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int in
 // GMRES on FP32 copies of the matrix and of the inverted diagonal blocks.
 static int dg_spmv32(gbfem_ctx c, int mode, const double *x, const double *b, double *out) {
   int n = 0;
-  for (int p = 1; p <= 4; p++) {
-    if (!c->dg_list[p].p) continue;
-    const int r = gbfem::launch_dg_block_spmv32(c->stream, mode, p + dg_class_off(c), (int)c->dg_list[p].n,
-                                                c->dg_list[p].p,
+  for (int cls = 1; cls <= 8; cls++) {
+    if (!c->dg_list[cls].p) continue;
+    const int r = gbfem::launch_dg_block_spmv32(c->stream, mode, cls, (int)c->dg_list[cls].n, c->dg_list[cls].p,
                                                 c->dg_roff_d.p, c->dg_row_val_d.p, c->dg_cx_off_d.p,
                                                 c->dg_colx_d.p, c->dg_val32.p, c->dg_dinv_off_d.p, c->dg_dinv32.p,
                                                 x, b, out);

@@ -138,6 +138,22 @@ GB_HD DgFacePoint dg_face_point(int nfv, const double *fq, const double *X1, con
   return P;
 }
 
+// local coordinates of the tetrahedron vertices (0,0,0), (1,0,0), (0,1,0), (0,0,1)
+GB_HD v3 tet_vertex_local(int k) { return {k == 1 ? 1.0 : 0.0, k == 2 ? 1.0 : 0.0, k == 3 ? 1.0 : 0.0}; }
+
+// v = J^-1 A^T n for the affine tetrahedron X[12] (J constant: columns
+// X1-X0, X2-X0, X3-X0)
+GB_HD v3 tet_face_v(const double *X, const double *A, v3 n) {
+  const v3 x0 = {X[0], X[1], X[2]};
+  const v3 j1 = v3_sub(v3{X[3], X[4], X[5]}, x0), j2 = v3_sub(v3{X[6], X[7], X[8]}, x0),
+           j3 = v3_sub(v3{X[9], X[10], X[11]}, x0);
+  const v3 c1 = v3_cross(j2, j3), c2 = v3_cross(j3, j1), c3 = v3_cross(j1, j2);
+  const double rdet = 1.0 / v3_dot(j1, c1);
+  const v3 an = {A[0] * n.x + A[3] * n.y + A[6] * n.z, A[1] * n.x + A[4] * n.y + A[7] * n.z,
+                 A[2] * n.x + A[5] * n.y + A[8] * n.z};
+  return {v3_dot(c1, an) * rdet, v3_dot(c2, an) * rdet, v3_dot(c3, an) * rdet};
+}
+
 // Per point and side, the monomial factors of the basis: powers
 // T[k][m] = x_k^m and the gradient factors T[3 + k][m] = m x_k^(m-1) v_k
 // (m = 0..4, k = xi, eta, zeta), so that for xi^a eta^b zeta^c

@@ -34,22 +34,6 @@ constexpr int TT_NCOL = 2 * TT_NS;
 
 __host__ __device__ constexpr int tt_ns(int p) { return (p + 1) * (p + 2) * (p + 3) / 6; }
 
-__device__ __forceinline__ v3 tt_vertex_local(int k) {
-  return {k == 1 ? 1.0 : 0.0, k == 2 ? 1.0 : 0.0, k == 3 ? 1.0 : 0.0};
-}
-
-// v = J^-1 A^T n for the tetrahedron X[12] (J constant: columns X1-X0, X2-X0, X3-X0)
-__device__ __forceinline__ v3 tt_face_v(const double *X, const double *A, v3 n) {
-  const v3 x0 = {X[0], X[1], X[2]};
-  const v3 j1 = v3_sub(v3{X[3], X[4], X[5]}, x0), j2 = v3_sub(v3{X[6], X[7], X[8]}, x0),
-           j3 = v3_sub(v3{X[9], X[10], X[11]}, x0);
-  const v3 c1 = v3_cross(j2, j3), c2 = v3_cross(j3, j1), c3 = v3_cross(j1, j2);
-  const double rdet = 1.0 / v3_dot(j1, c1);
-  const v3 an = {A[0] * n.x + A[3] * n.y + A[6] * n.z, A[1] * n.x + A[4] * n.y + A[7] * n.z,
-                 A[2] * n.x + A[5] * n.y + A[8] * n.z};
-  return {v3_dot(c1, an) * rdet, v3_dot(c2, an) * rdet, v3_dot(c3, an) * rdet};
-}
-
 // DW: the point tables as double words and every entry summed by exact
 // products and TwoSum chains (DwAcc, dword.cuh), as in the prism face kernel.
 template <int P, bool DW, int TT_THREADS = tt_threads(P)>
@@ -128,7 +112,7 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
       const v3 vo = {X1[3 * F.side1], X1[3 * F.side1 + 1], X1[3 * F.side1 + 2]};
       if (v3_dot(n, v3_sub(vo, va)) > 0.0) n = v3_scale(-1.0, n);
       if (tid == 0) {
-        const v3 v1 = tt_face_v(sX[0], sA[0], n);
+        const v3 v1 = tet_face_v(sX[0], sA[0], n);
         sV[0][0] = v1.x;
         sV[0][1] = v1.y;
         sV[0][2] = v1.z;
@@ -136,7 +120,7 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
         const int pp = interior ? (p1 < p2 ? p1 : p2) : p1;
         sC[1] = pen * pp / sqrt(0.5 * d);
       } else if (interior) {
-        const v3 v2 = tt_face_v(sX[1], sA[1], n);
+        const v3 v2 = tet_face_v(sX[1], sA[1], n);
         sV[1][0] = v2.x;
         sV[1][1] = v2.y;
         sV[1][2] = v2.z;
@@ -154,7 +138,7 @@ __global__ void __launch_bounds__(TT_THREADS) dg_tet_faces_kernel(
       const unsigned char *loc = sd == 0 ? F.loc1 : F.loc2;
       v3 ev = {0, 0, 0};
 #pragma unroll
-      for (int i = 0; i < 3; i++) ev = v3_fma(w[i], tt_vertex_local(loc[i]), ev);
+      for (int i = 0; i < 3; i++) ev = v3_fma(w[i], tet_vertex_local(loc[i]), ev);
       dg_point_factors(ev, v3{sV[sd][0], sV[sd][1], sV[sd][2]}, sFac[q][sd]);
     }
     const double fac = interior ? 0.5 : 1.0;

@@ -154,6 +154,15 @@ int launch_dg_tet_faces(cudaStream_t st, int p, int count, const int *ent_el, co
                         const DgHalfFace *hf, const int *el_p, const int *el_nodes, const double *xyz,
                         const double *k_el, const double *D_el, double pen, double g, const long long *boff_diag,
                         const int *roff, double *val, double *rhs, bool dword = false);
+// Faces between a prism and a tetrahedron (dg_mixed_faces.cu): owners of
+// class cls (1..4 prisms of degree cls, 5..8 tetrahedra of degree cls - 4),
+// their mixed half-faces mhf[mhf_ptr[e] .. mhf_ptr[e + 1]); prism vertices
+// from el_nodes6 (6 per element), tetrahedron vertices from el_nodes4 (4 per
+// element).  Runs after the same-type face kernels on the same stream.
+int launch_dg_mixed_faces(cudaStream_t st, int cls, int count, const int *ent_el, const int *mhf_ptr,
+                          const DgHalfFace *mhf, const int *el_p, const int *el_nodes6, const int *el_nodes4,
+                          const double *xyz, const double *k_el, const double *D_el, double pen,
+                          const long long *boff_diag, double *val, int *err);
 bool dg_tc_faces_supported(int p);
 // Face-point configurations of the tensor-core face kernel: cfg[5 c ..]
 // = (vertex count, local vertex of each face vertex); tables of the reference
@@ -230,10 +239,16 @@ struct gbfem_ctx_s {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   // mesh
-  int nno = 0, nel = 0, nv = 0, nfa = 0;
+  int nno = 0, nel = 0, nv = 0, nfa = 0;  // nv: vertices per element (6 per element slot on mixed meshes)
   int max_fa_id = 0;
   gbfem::DevBuf<double> xyz;
   gbfem::DevBuf<int> el_nodes;
+  // meshes of prisms and tetrahedra together (gbfem_set_mesh_mixed, DG
+  // only): el_nodes holds 6 slots per element, el_nodes4 the first 4 of each
+  // (the tetrahedron kernels' layout); h_el_tet marks the tetrahedra
+  bool mixed = false;
+  std::vector<unsigned char> h_el_tet;
+  gbfem::DevBuf<int> el_nodes4;
   gbfem::DevBuf<int> fa_el, fa_side;
   std::vector<int> h_fa_id, h_fa_el, h_fa_side, h_el_nodes;
   std::vector<int> fa_index_of_id;  // reference face id -> bc face index (-1 none)
@@ -296,8 +311,14 @@ struct gbfem_ctx_s {
   long long dg_nval = 0, dg_ninv = 0;
   int dg_ndof = 0;
   bool dg_ready = false;
-  gbfem::DevBuf<int> dg_list[5], dg_roff_d;
-  gbfem::DevBuf<int> dg_flist_tc[5], dg_flist_64[5];  // face owners: tensor-core eligible / FP64
+  // elements per class: 1..4 prisms of degree 1..4, 5..8 tetrahedra of
+  // degree 1..4
+  gbfem::DevBuf<int> dg_list[9], dg_roff_d;
+  gbfem::DevBuf<int> dg_flist_tc[5], dg_flist_64[5];  // prism face owners: tensor-core eligible / FP64
+  // faces between a prism and a tetrahedron: half-face records per owner
+  // and the owners per class that have any
+  gbfem::DevBuf<int> dg_mhf_ptr, dg_mlist[9];
+  gbfem::DevBuf<gbfem::DgHalfFace> dg_mhf;
   gbfem::DevBuf<long long> dg_boff_diag_d;
   gbfem::DevBuf<double> dg_val, dg_rhs;
   // DG faces: the caller's face table and the per-element incidences

@@ -440,30 +440,36 @@ def mixed_faces(mesh, bc=1):
     once, el1 the lower-numbered neighbour and side1 its local face (prisms:
     PRISM_SIDES, tetrahedra: TET_SIDES), nodes in el1's local order of that
     face; type 3 or 4; bc on the boundary, -1 inside.  Ordered by (el1,
-    side1)."""
-    rows = []
-    for e in range(mesh.nel):
-        sides = PRISM_SIDES if mesh.el_nv[e] == 6 else TET_SIDES
+    side1).  Faces are matched by their sorted vertex sets (numpy sorts, no
+    per-face loop)."""
+    el, nv = np.asarray(mesh.el_nodes), np.asarray(mesh.el_nv)
+    parts_e, parts_s, parts_v = [], [], []
+    for typ, sides in ((6, PRISM_SIDES), (4, TET_SIDES)):
+        es = np.nonzero(nv == typ)[0]
         for s, loc in enumerate(sides):
-            verts = [int(mesh.el_nodes[e, i]) for i in loc]
-            rows.append((tuple(sorted(verts)), e, s, verts))
-    rows.sort(key=lambda r: (r[0], r[1]))
-    out = []
-    i = 0
-    while i < len(rows):
-        key, e1, s1, verts = rows[i]
-        if i + 1 < len(rows) and rows[i + 1][0] == key:
-            e2, s2 = rows[i + 1][1], rows[i + 1][2]
-            i += 2
-        else:
-            e2, s2 = -1, 0
-            i += 1
-        out.append((e1, s1, e2, s2, len(verts), verts + [-1] * (4 - len(verts))))
-    out.sort(key=lambda r: (r[0], r[1]))
-    nf = len(out)
-    e1 = np.array([r[0] for r in out], np.int32)
-    e2 = np.array([r[2] for r in out], np.int32)
-    return FaceTable(id=np.arange(1, nf + 1, dtype=np.int32), type=np.array([r[4] for r in out], np.int32),
-                     bc=np.where(e2 >= 0, -1, bc).astype(np.int32), el1=e1, el2=e2,
-                     side1=np.array([r[1] for r in out], np.int32), side2=np.array([r[3] for r in out], np.int32),
-                     nodes=np.array([r[5] for r in out], np.int32))
+            v = np.full((es.size, 4), -1, np.int64)
+            v[:, :len(loc)] = el[es][:, list(loc)]
+            parts_e.append(es)
+            parts_s.append(np.full(es.size, s, np.int64))
+            parts_v.append(v)
+    E, S, V = np.concatenate(parts_e), np.concatenate(parts_s), np.concatenate(parts_v)
+    K = np.sort(np.where(V >= 0, V, np.iinfo(np.int64).max), axis=1)
+    order = np.lexsort((E, K[:, 3], K[:, 2], K[:, 1], K[:, 0]))
+    Ks = K[order]
+    first = np.nonzero(np.all(Ks[1:] == Ks[:-1], axis=1))[0]  # a face met twice: rows i, i + 1
+    paired = np.zeros(order.size, bool)
+    paired[first] = True
+    paired[first + 1] = True
+    single = np.nonzero(~paired)[0]
+    i1 = np.concatenate([order[first], order[single]])
+    i2 = np.concatenate([order[first + 1], np.full(single.size, -1)])
+    e1, s1 = E[i1], S[i1]
+    e2 = np.where(i2 >= 0, E[np.maximum(i2, 0)], -1)
+    s2 = np.where(i2 >= 0, S[np.maximum(i2, 0)], 0)
+    srt = np.lexsort((s1, e1))
+    e1, s1, e2, s2, nodes = e1[srt], s1[srt], e2[srt], s2[srt], V[i1][srt]
+    nf = e1.size
+    return FaceTable(id=np.arange(1, nf + 1, dtype=np.int32), type=(nodes >= 0).sum(1).astype(np.int32),
+                     bc=np.where(e2 >= 0, -1, bc).astype(np.int32), el1=e1.astype(np.int32),
+                     el2=e2.astype(np.int32), side1=s1.astype(np.int32), side2=s2.astype(np.int32),
+                     nodes=nodes.astype(np.int32))

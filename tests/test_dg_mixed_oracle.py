@@ -122,3 +122,42 @@ def test_mixed_system_consistent_for_linear_functions():
         for i in range(F.n))]
     assert len(mixed_rows) > 0
     assert np.max(np.abs(r[rows])) < 1e-11 * np.max(np.abs(K))
+
+
+def _faces_by_loop(mesh):
+    """The face table by a plain loop over element sides (the definition
+    mixed_faces vectorises)."""
+    from modfem_gb300.mesh import PRISM_SIDES, TET_SIDES
+    rows = []
+    for e in range(mesh.nel):
+        sides = PRISM_SIDES if mesh.el_nv[e] == 6 else TET_SIDES
+        for s, loc in enumerate(sides):
+            verts = [int(mesh.el_nodes[e, i]) for i in loc]
+            rows.append((tuple(sorted(verts)), e, s, verts))
+    rows.sort(key=lambda r: (r[0], r[1]))
+    out, i = [], 0
+    while i < len(rows):
+        key, e1, s1, verts = rows[i]
+        if i + 1 < len(rows) and rows[i + 1][0] == key:
+            e2, s2 = rows[i + 1][1], rows[i + 1][2]
+            i += 2
+        else:
+            e2, s2 = -1, 0
+            i += 1
+        out.append((e1, s1, e2, s2, len(verts), verts + [-1] * (4 - len(verts))))
+    out.sort(key=lambda r: (r[0], r[1]))
+    return out
+
+
+@pytest.mark.parametrize("n,layers", [(2, 1), (4, 3)])
+def test_mixed_faces_matches_loop_definition(n, layers):
+    m = structured_mixed_mesh(n, layers, jitter=0.1, seed=1)
+    F = mixed_faces(m)
+    ref = _faces_by_loop(m)
+    assert F.n == len(ref)
+    for k, (e1, s1, e2, s2, t, v) in enumerate(ref):
+        assert (F.el1[k], F.side1[k], F.el2[k], F.side2[k], F.type[k]) == (e1, s1, e2, s2, t)
+        assert list(F.nodes[k]) == v
+        assert F.bc[k] == (-1 if e2 >= 0 else 1)
+    # interface triangles between the two element types exist
+    assert np.any((F.el2 >= 0) & (m.el_nv[F.el1] != m.el_nv[np.maximum(F.el2, 0)]))
