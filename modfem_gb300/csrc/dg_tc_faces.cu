@@ -168,6 +168,12 @@ __device__ __forceinline__ v3 tf_face_v(v3 j1, v3 j2, v3 j3, const double *A, v3
   return {v3_dot(c1, an) * rdet, v3_dot(c2, an) * rdet, v3_dot(c3, an) * rdet};
 }
 
+// An FP32 accumulator value that is an exact integer of magnitude below
+// 2^22, as an int32: adding 1.5 * 2^23 puts the integer in the low mantissa
+// bits (the ulp there is 1, so the add is exact); FP32 add and integer
+// subtract instead of a conversion instruction
+__device__ __forceinline__ int tf_exact_int(float c) { return __float_as_int(c + 12582912.0f) - 0x4B400000; }
+
 // BF16 bit pattern of the integer c (|c| <= 255): through an FP32 add on the
 // FMA pipe (exact), the sign set separately
 __device__ __forceinline__ uint32_t tf_bf16_bits(uint32_t mag, bool neg) {
@@ -349,6 +355,23 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
     const double *tab_nb = interior ? ftab + ftab_off[(cfg_nb * 3 + pr - 1) * 3 + pnb - 1] : tab_own;
     // owner-row sign s_o: L = f a g + s_o c a phi, M = -s_o f a phi
     const long long so_bit = own2 ? (long long)1 << 63 : 0;
+    // table values of a (row, point) pair, loaded one round ahead of their
+    // use so that the L2 latency of round k + 1 overlaps the work of round k
+    // (the first round's loads overlap the barrier below)
+    auto tab_load = [&](int t, double2 &x01, double2 &x23) {
+      const int r = t >> 4, q = t & 15;
+      if (r < rows && q < nq) {
+        const bool own = r < NS;
+        const double *tb = (own ? tab_own : tab_nb) + ((size_t)q * (own ? NS : ns_nb) + (own ? r : r - NS)) * 4;
+        x01 = __ldg(reinterpret_cast<const double2 *>(tb));
+        x23 = __ldg(reinterpret_cast<const double2 *>(tb) + 1);
+      } else {
+        x01 = make_double2(0.0, 0.0);
+        x23 = x01;
+      }
+    };
+    double2 n01, n23;
+    tab_load(tid, n01, n23);
     __syncthreads();  // the previous face's operand slices are consumed; the geometry is in place
     // operands in one pass, a 16-lane segment per row r and a lane per point
     // q (k = 2q: Phi / L, 2q + 1: Gam / M; lanes q >= nq give the K
@@ -359,12 +382,11 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
     for (int base = 0; base < rows * 16; base += TF_THREADS) {
       const int t = base + tid, r = t >> 4, q = t & 15;
       const bool live = r < rows, own = r < NS;  // uniform over the segment
+      const double2 t01 = n01, t23 = n23;
+      if (base + TF_THREADS < rows * 16) tab_load(t + TF_THREADS, n01, n23);
       double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
       if (live && q < nq) {
-        const int side = own ? own_side : 3 - own_side, jj = own ? r : r - NS;
-        const double *tb = (own ? tab_own : tab_nb) + ((size_t)q * (own ? NS : ns_nb) + jj) * 4;
-        const double2 t01 = __ldg(reinterpret_cast<const double2 *>(tb));
-        const double2 t23 = __ldg(reinterpret_cast<const double2 *>(tb) + 1);
+        const int side = own ? own_side : 3 - own_side;
         const double *G = sGeo + q * TF_GEOS;
         const double *v = G + (side == 1 ? 2 : 5);
         const double phi = t01.x;
@@ -434,17 +456,20 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(cn >> 3) << 17) |
                                ((uint32_t)(TF_M >> 4) << 24);
-        const uint32_t a0 = tc_smem(asl), b0 = tc_smem(bsl) + (clo / 8) * (TF_KP / 8) * 128;
-        for (int i = 0; i < TF_SL; i++)
-          for (int j = 0; j < TF_SL - i; j++) {
-            const int d = i + j;
+        // the descriptors of one chunk differ only in their start-address
+        // field (address / 16, 14 bits: every shared address fits without a
+        // carry), so each MMA's are constant offsets from two base
+        // descriptors and the 56 issues unroll into straight-line code
+        const uint64_t ad0 = tc_desc(tc_smem(asl), 128, (TF_KP / 8) * 128);
+        const uint64_t bd0 = tc_desc(tc_smem(bsl) + (clo / 8) * (TF_KP / 8) * 128, 128, (TF_KP / 8) * 128);
 #pragma unroll
-            for (int ks = 0; ks < TF_KP / 16; ks++) {
-              const uint64_t ad = tc_desc(a0 + i * Dm::A_STRIDE + ks * 256, 128, (TF_KP / 8) * 128);
-              const uint64_t bd = tc_desc(b0 + j * Dm::B_SLICE + ks * 256, 128, (TF_KP / 8) * 128);
-              tc_mma<0>(tmem + d * cn, ad, bd, idesc, (i == 0 && ks == 0) ? 0u : 1u);
-            }
-          }
+        for (int i = 0; i < TF_SL; i++)
+#pragma unroll
+          for (int j = 0; j < TF_SL - i; j++)
+#pragma unroll
+            for (int ks = 0; ks < TF_KP / 16; ks++)
+              tc_mma<0>(tmem + (i + j) * cn, ad0 + (uint64_t)((i * Dm::A_STRIDE + ks * 256) >> 4),
+                        bd0 + (uint64_t)((j * Dm::B_SLICE + ks * 256) >> 4), idesc, (i == 0 && ks == 0) ? 0u : 1u);
         tc_commit(tc_smem(bar));
       }
       __syncthreads();
@@ -477,11 +502,12 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
             // and lo = C_4..C_6 in base 256 (|hi| < 2^48.01, |lo| <
             // 2^40.01); T = hi 2^14 + lo / 2^10 (< 2^63), so the sum is
             // T 2^-54, with 9 bits beyond the 53 the double rounds to
-            long long hi = 0, lo = 0;
-#pragma unroll
-            for (int d = 0; d < 4; d++) hi = hi * 256 + (long long)__float2int_rn(C[d][c]);
-#pragma unroll
-            for (int d = 4; d < TF_SL; d++) lo = lo * 256 + (long long)__float2int_rn(C[d][c]);
+            // |C_d| <= 32 * 255^2 < 2^21: pairs of them combine in int32
+            static_assert(TF_SL == 7 && TF_KP == 32, "seven accumulators of K = 32 products");
+            const int u01 = tf_exact_int(C[0][c]) * 256 + tf_exact_int(C[1][c]);
+            const int u23 = tf_exact_int(C[2][c]) * 256 + tf_exact_int(C[3][c]);
+            const int u45 = tf_exact_int(C[4][c]) * 256 + tf_exact_int(C[5][c]);
+            const long long hi = (long long)u01 * 65536 + u23, lo = (long long)u45 * 256 + tf_exact_int(C[6][c]);
             const double v = tf_i64_scaled(hi * 16384LL + (lo >> 10), sa + eb[i] - 54);
             if (r_ep < NS)
               sD[r_ep * Dm::SD_LD + i] += v;
