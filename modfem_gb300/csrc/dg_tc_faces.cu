@@ -1,5 +1,6 @@
 // DG prism face integrals on the tensor cores (tcgen05, sm_103a) with
-// FP64-equivalent results: split BF16 products, one CTA per owner element.
+// FP64-equivalent results: split BF16 products in a persistent, warp-
+// specialised kernel (one CTA per SM).
 //
 // Reference: pdr_conv_diff_comp_fa_stiff_mat_app of the DG weak form
 // (pds_conv_diff_weakform_dg.c:232-1140); the face algebra and the owner-row
@@ -18,7 +19,7 @@
 // accumulation is exact, and
 //   D = 2^(ea_j + eb_i) sum_d C_d 2^(-8(d+2))
 // is recombined in int64 and rounded once to FP64 on the integer pipe.
-// The owner's diagonal-block share is summed over its faces in FP64 registers
+// The owner's diagonal-block share is summed over its faces in shared memory
 // and added once to the block the volume kernel wrote; the off-diagonal block
 // (e, neighbour) is written whole, as in the FP64 kernel (deterministic, no
 // atomics).  Covers owners of degree <= 3 whose neighbours all have degree
@@ -36,13 +37,16 @@
 //    so they are tables (dg_face_table_kernel, built once per structure,
 //    about 2 MB, L2-resident), where the kernel otherwise evaluated monomial
 //    factors per face, point and side.
-// Per face the CTA then reads its points' geometry, and one fused pass over
-// (row, point) pairs forms the FP64 operand values (phi from the table,
-// g = v . grad phi: three FMAs), each row's exponent (a shuffle max over its
-// 16-lane segment) and the BF16 slices, with no FP64 staging; 56 MMAs (M 128,
-// N = NS rounded up to 16, K 16) issued by one thread into 7 accumulators;
-// commit to an mbarrier; epilogue by the warps whose TMEM lane quarter holds
-// rows (tcgen05.ld: warp w reads lane quarter w % 4, column half w / 4).
+// Per face one fused pass over (row, point) pairs forms the FP64 operand
+// values (phi from the table, g = v . grad phi: three FMAs), each row's
+// exponent (a shuffle max over its 16-lane segment) and the BF16 slices, with
+// no FP64 staging; 56 MMAs (M 128, N = NS rounded up to 16, K 16) issued by
+// one thread into 7 accumulators; an epilogue by the warps whose TMEM lane
+// quarter holds rows (tcgen05.ld: warp w reads lane quarter w % 4).  Measured
+// on GB300, a tcgen05.mma of these small shapes costs a fixed issue time (the
+// same for N = 16 and 32, and for M = 64 and 128), so the kernel keeps the
+// MMA count low (one N chunk per face, which needs the whole TMEM) and
+// overlaps the three phases of consecutive faces by warp role (below).
 // Every wait has an iteration limit: on expiry the CTA records an error, lets
 // its MMAs drain (again with a limit), frees its TMEM and returns.
 
@@ -62,9 +66,6 @@ constexpr int TF_KP = 32;         // K: 2 x (up to 16 face points)
 constexpr int TF_NQ = 16;         // face points of the largest rule with max(p1, p2) <= 3
 constexpr int TF_NF = 5;          // faces of a prism
 constexpr int TF_M = 128;         // MMA M
-constexpr int TF_THREADS = 256;
-constexpr int TF_TMEM_COLS = 256;  // two CTAs per SM share the 512 columns
-constexpr int TF_NCH = 32;         // MMA N per chunk of e's functions: 7 x 32 accumulator columns
 constexpr int TF_GEO = 8;    // per face point: f a, c a, v1 (3), v2 (3)
 constexpr int TF_GEOS = 9;   // their stride in shared memory: odd, so the 16 points of a row segment hit distinct banks
 static_assert((long long)TF_SL * TF_KP * 255 * 255 < (1LL << 24), "slice sums must stay exact in FP32");
@@ -81,19 +82,7 @@ struct TfDims {
   static constexpr int A_STRIDE = ROWS8 * TF_KP * 2;
   static constexpr int A_BYTES = (TF_SL - 1) * A_STRIDE + TF_M * TF_KP * 2;
   static constexpr int B_SLICE = NPAD * TF_KP * 2;
-  static constexpr int OFF_B = A_BYTES;
-  static constexpr int OFF_FACE = OFF_B + TF_SL * B_SLICE;                 // [TF_NF][TF_NQ][TF_GEOS]
   static constexpr int FACE_DOUBLES = TF_NQ * TF_GEOS;
-  static constexpr int OFF_DIAG = OFF_FACE + TF_NF * FACE_DOUBLES * 8;     // [NS][SD_LD] diagonal-block share
-  static constexpr int SD_LD = NS + 1;                                     // odd row stride
-  static constexpr int OFF_RACC = OFF_DIAG + NS * SD_LD * 8;               // [NS] boundary rhs sums
-  static constexpr int OFF_HF = OFF_RACC + 64 * 8;
-  static constexpr int OFF_INT = (OFF_HF + TF_NF * (int)sizeof(DgHalfFace) + 15) / 16 * 16;  // ea, eb, bar, slot
-  static constexpr int SMEM = OFF_INT + (128 + 64) * 4 + 64;
-  static constexpr int NCHUNK = (NPAD + TF_NCH - 1) / TF_NCH;
-  static_assert(TF_SL * (NPAD < TF_NCH ? NPAD : TF_NCH) <= TF_TMEM_COLS, "accumulators fit the TMEM allocation");
-  static_assert(SMEM <= 113 * 1024, "shared memory of two CTAs per SM");
-  static_assert(OFF_B % 1024 == 0 && OFF_HF % 16 == 0 && OFF_INT % 16 == 0, "alignment");
   static_assert(ROWS <= TF_M && NS <= 64, "rows");
 };
 
@@ -271,45 +260,118 @@ __global__ void __launch_bounds__(128) dg_face_geometry_kernel(
   G[7] = v2.z;
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined form: one persistent CTA per SM with 512 threads and all 512
+// TMEM columns, the phases of consecutive faces overlapped by warp role:
+//   warps 0-7 (producers): per face, the operand pass into one of two
+//       shared-memory buffers, up to two faces ahead of the epilogue and
+//       across owner boundaries; each owner's boundary rhs share;
+//   warp 8, one thread: the face's MMAs in one N chunk (N = NPAD <= 48, the
+//       seven accumulators 7 NPAD <= 336 columns: 56 MMAs a face at p = 3
+//       instead of 112 in two chunks), commit;
+//   warps 8-15 (epilogue): accumulators to FP64, the owner rows into the
+//       diagonal-block share, the neighbour rows to the off-diagonal block;
+//       each owner's diagonal-block share when its last face is done.
+// Hand-offs are mbarriers: full[b] (operands of buffer b written), mma[b]
+// (its MMAs complete), free[b] (the epilogue is done with buffer b).  One
+// elected thread per group waits (bounded, and it gives up early once any
+// role has given up) and the group then meets at its named barrier and reads
+// the outcome, so every decision is uniform over the group.  The
+// arithmetic is that of dg_tc_faces_kernel: bit-identical results.
+constexpr int TP_THREADS = 512;
+
+struct TpMeta {
+  long long blk;  // block (owner, neighbour); -1 on the boundary
+  int rows, pad0, pad1, pad2;
+};
+
 template <int P>
-__global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
+struct TpDims {
+  using D = TfDims<P>;
+  static constexpr int B_BYTES = TF_SL * D::B_SLICE;
+  static constexpr int BUF = D::A_BYTES + B_BYTES;  // one operand buffer
+  static constexpr int OFF_FACE = 2 * BUF;           // [TF_NF][TF_NQ][TF_GEOS]
+  static constexpr int SD_LD = D::NS + 1;
+  static constexpr int OFF_DIAG = OFF_FACE + TF_NF * D::FACE_DOUBLES * 8;  // [NS][SD_LD]
+  static constexpr int OFF_RACC = OFF_DIAG + D::NS * SD_LD * 8;            // [64]
+  static constexpr int OFF_HF = OFF_RACC + 64 * 8;                          // [TF_NF]
+  static constexpr int OFF_META = (OFF_HF + TF_NF * (int)sizeof(DgHalfFace) + 15) / 16 * 16;  // [2]
+  static constexpr int OFF_EXP = OFF_META + 2 * (int)sizeof(TpMeta);       // [2][128 + 64]
+  static constexpr int OFF_BAR = OFF_EXP + 2 * 192 * 4;                     // full[2], mma[2], free[2]
+  static constexpr int SMEM_USED = OFF_BAR + 6 * 8 + 32;
+  // requested at least 116 KB so that no two CTAs share an SM (each
+  // allocates all 512 TMEM columns)
+  static constexpr int SMEM = SMEM_USED > 116 * 1024 ? SMEM_USED : 116 * 1024;
+  static_assert(BUF % 1024 == 0 && D::A_BYTES % 1024 == 0, "operand buffers 1024-aligned");
+  static_assert(TF_SL * D::NPAD <= 512, "one chunk of accumulators fits the TMEM");
+  static_assert(SMEM <= 227 * 1024, "shared memory of one CTA");
+  static_assert(OFF_BAR % 8 == 0, "mbarrier alignment");
+};
+
+// named barrier of one role group (256 threads); the non-aligned form, as
+// a group's elected thread may arrive on its own
+__device__ __forceinline__ void tp_bar(int id) {
+  asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(256) : "memory");
+}
+
+__device__ __forceinline__ void tp_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc_smem(bar)) : "memory");
+}
+
+// Bounded wait of one thread; gives up early once another role has given up.
+__device__ __forceinline__ bool tp_wait1(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
+  for (long long it = 0; it < TC_WAIT_LIMIT; it++) {
+    if (tc_try_wait(tc_smem(bar), parity)) return true;
+    if ((it & 255) == 255 && *abort_flag) return false;
+  }
+  *abort_flag = 1;
+  return false;
+}
+
+// Group wait (256 threads, named barrier id): the elected thread waits, the
+// group reads the outcome after the barrier (slot alternates between
+// consecutive waits, so a slot is rewritten only after another barrier).
+__device__ __forceinline__ bool tp_group_wait(uint64_t *bar, uint32_t parity, bool elected, int id,
+                                              volatile int *abort_flag, volatile int *slot) {
+  if (elected) *slot = tp_wait1(bar, parity, abort_flag) ? 1 : 0;
+  tp_bar(id);
+  return *slot != 0;
+}
+
+template <int P>
+__global__ void __launch_bounds__(TP_THREADS, 1) dg_tc_faces_pipe_kernel(
     int count, const int *__restrict__ ent_el, const int *__restrict__ hf_ptr, const DgHalfFace *__restrict__ hf,
     const int *__restrict__ el_p, const double *__restrict__ geo, const double *__restrict__ ftab,
     const long long *__restrict__ ftab_off, double gval, const long long *__restrict__ boff_diag,
     const int *__restrict__ roff, double *__restrict__ val, double *__restrict__ rhs, int *err,
     double *__restrict__ share) {
   using Dm = TfDims<P>;
-  constexpr int NS = Dm::NS, NPAD = Dm::NPAD, FD = Dm::FACE_DOUBLES;
+  using Tp = TpDims<P>;
+  constexpr int NS = Dm::NS, NPAD = Dm::NPAD, FD = Dm::FACE_DOUBLES, SD_LD = Tp::SD_LD;
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t *asl = smem, *bsl = smem + Dm::OFF_B;
-  double *sface = (double *)(smem + Dm::OFF_FACE);   // [TF_NF][TF_NQ][TF_GEOS]
-  double *sRacc = (double *)(smem + Dm::OFF_RACC);   // [NS]
-  double *sD = (double *)(smem + Dm::OFF_DIAG);      // [NS][SD_LD]: row r (trial function), column i
-  DgHalfFace *sHF = (DgHalfFace *)(smem + Dm::OFF_HF);
-  int *ea = (int *)(smem + Dm::OFF_INT);             // A row exponents (by row = M row)
-  int *eb = ea + 128;                                // B row exponents
-  uint64_t *bar = (uint64_t *)(eb + 64);
-  uint32_t *tmem_slot = (uint32_t *)(bar + 1);
-  const int bi = blockIdx.x;
-  if (bi >= count) return;
-  const int e = ent_el[bi];
-  const int h0 = hf_ptr[e], nf = hf_ptr[e + 1] - h0;
-  if (nf <= 0) return;
+  double *sface = (double *)(smem + Tp::OFF_FACE);
+  double *sD = (double *)(smem + Tp::OFF_DIAG);   // row r (trial function), column i
+  double *sRacc = (double *)(smem + Tp::OFF_RACC);
+  DgHalfFace *sHF = (DgHalfFace *)(smem + Tp::OFF_HF);
+  TpMeta *meta = (TpMeta *)(smem + Tp::OFF_META);
+  int *sexp = (int *)(smem + Tp::OFF_EXP);        // buffer b: ea at 192 b, eb at 192 b + 128
+  uint64_t *bar_full = (uint64_t *)(smem + Tp::OFF_BAR), *bar_mma = bar_full + 2, *bar_free = bar_full + 4;
+  uint32_t *tmem_slot = (uint32_t *)(bar_full + 6);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  volatile int *slots = (volatile int *)(tmem_slot + 2);  // [2] producers, [2] epilogue
+  int *s_issued = (int *)(tmem_slot + 6);                 // faces whose MMAs were issued
   const int tid = threadIdx.x, warp = tid >> 5;
-  if (nf > TF_NF) {  // not a prism's face list (uniform over the CTA)
-    if (tid == 0) atomicExch(err, 7);
-    return;
-  }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(bar)));
+    for (int i = 0; i < 6; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(bar_full + i)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *abort_flag = 0;
+    *s_issued = 0;
   }
-  if (tid < nf) sHF[tid] = hf[h0 + tid];
-  if (tid < NS) sRacc[tid] = 0.0;
-  for (int t = tid; t < NS * Dm::SD_LD; t += TF_THREADS) sD[t] = 0.0;
+  for (int t = tid; t < NS * SD_LD; t += TP_THREADS) sD[t] = 0.0;
+  if (tid < 64) sRacc[tid] = 0.0;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
-                 "r"(TF_TMEM_COLS));
+                 "r"(512));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -317,232 +379,263 @@ __global__ void __launch_bounds__(TF_THREADS, 2) dg_tc_faces_kernel(
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  // ---- the per-point geometry of all the element's faces ----
-  for (int t = tid; t < nf * TF_NQ * TF_GEO; t += TF_THREADS) {
-    const int f = t / (TF_NQ * TF_GEO), r = t % (TF_NQ * TF_GEO);
-    sface[f * FD + (r / TF_GEO) * TF_GEOS + r % TF_GEO] = geo[(size_t)sHF[f].face * TF_NQ * TF_GEO + r];
-  }
-  // (the per-face loop starts with a barrier)
-
-  // epilogue threads: warp w reads TMEM lane quarter w % 4 (rows = M rows =
-  // A rows: e's functions 0..NS-1, then the neighbour's) and column half
-  // w / 4 of the current chunk of e's functions
-  const int lq = warp & 3, half = warp >> 2;
-  const int r_ep = lq * 32 + (tid & 31);
-  bool failed = false, bad_input = false;
-  int fail_parity = 0, ncommit = 0;
-
-  for (int f = 0; f < nf; f++) {
-    const DgHalfFace &F = sHF[f];
-    const double *sGeo = sface + f * FD;
-    const bool interior = F.el2 >= 0;
-    const int own2 = F.owner_is_2;
-    const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
-    const int ti = F.nfv == 4 ? 1 : 0;
-    const int pr = (interior && tf_nqf[p2][ti] > tf_nqf[p1][ti]) ? p2 : p1;
-    const int nq = tf_nqf[pr][ti];
-    const int pnb = own2 ? p1 : p2;  // the other side's degree
-    const int ns_nb = interior ? tf_ns[pnb] : 0;
-    const int rows = NS + ns_nb;
-    const int own_side = own2 ? 2 : 1;
-    const int cfg_own = own2 ? F.cfg2 : F.cfg1, cfg_nb = own2 ? F.cfg1 : F.cfg2;
-    if (pr > 3 || rows > Dm::ROWS || nq > TF_NQ) {  // a degree-4 neighbour: not this kernel's (uniform)
-      bad_input = true;
-      break;
-    }
-    // basis tables of this face: own side, other side ([point][function][4])
-    const double *tab_own = ftab + ftab_off[(cfg_own * 3 + pr - 1) * 3 + P - 1];
-    const double *tab_nb = interior ? ftab + ftab_off[(cfg_nb * 3 + pr - 1) * 3 + pnb - 1] : tab_own;
-    // owner-row sign s_o: L = f a g + s_o c a phi, M = -s_o f a phi
-    const long long so_bit = own2 ? (long long)1 << 63 : 0;
-    // table values of a (row, point) pair, loaded one round ahead of their
-    // use so that the L2 latency of round k + 1 overlaps the work of round k
-    // (the first round's loads overlap the barrier below)
-    auto tab_load = [&](int t, double2 &x01, double2 &x23) {
-      const int r = t >> 4, q = t & 15;
-      if (r < rows && q < nq) {
-        const bool own = r < NS;
-        const double *tb = (own ? tab_own : tab_nb) + ((size_t)q * (own ? NS : ns_nb) + (own ? r : r - NS)) * 4;
-        x01 = __ldg(reinterpret_cast<const double2 *>(tb));
-        x23 = __ldg(reinterpret_cast<const double2 *>(tb) + 1);
-      } else {
-        x01 = make_double2(0.0, 0.0);
-        x23 = x01;
-      }
-    };
-    double2 n01, n23;
-    tab_load(tid, n01, n23);
-    __syncthreads();  // the previous face's operand slices are consumed; the geometry is in place
-    // operands in one pass, a 16-lane segment per row r and a lane per point
-    // q (k = 2q: Phi / L, 2q + 1: Gam / M; lanes q >= nq give the K
-    // padding): FP64 values (phi from the table, g = v . grad phi), the row
-    // exponent by a segment max of the exponent fields, then the seven BF16
-    // slices of the pair as one 32-bit word each.  A rows: e's functions
-    // then the neighbour's; B rows: e's functions.
-    for (int base = 0; base < rows * 16; base += TF_THREADS) {
-      const int t = base + tid, r = t >> 4, q = t & 15;
-      const bool live = r < rows, own = r < NS;  // uniform over the segment
-      const double2 t01 = n01, t23 = n23;
-      if (base + TF_THREADS < rows * 16) tab_load(t + TF_THREADS, n01, n23);
-      double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
-      if (live && q < nq) {
-        const int side = own ? own_side : 3 - own_side;
-        const double *G = sGeo + q * TF_GEOS;
-        const double *v = G + (side == 1 ? 2 : 5);
-        const double phi = t01.x;
-        const double g = fma(v[0], t01.y, fma(v[1], t23.x, v[2] * t23.y));
-        // Phi = s_t phi: the sign flip on the integer side
-        a0 = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
-        a1 = g;
-        if (own) {
-          const double sphi = __longlong_as_double(__double_as_longlong(phi) ^ so_bit);  // s_o phi
-          b0 = fma(G[0], g, G[1] * sphi);
-          b1 = -(G[0] * sphi);
-        }
-      }
-      int xa = max(tf_biased_exp(a0), tf_biased_exp(a1)), xb = max(tf_biased_exp(b0), tf_biased_exp(b1));
-#pragma unroll
-      for (int o = 8; o >= 1; o >>= 1) {
-        xa = max(xa, __shfl_xor_sync(0xffffffffu, xa, o));
-        xb = max(xb, __shfl_xor_sync(0xffffffffu, xb, o));
-      }
-      if (!interior) {  // boundary face: the rhs of row r gets g sum_q L (uniform over the CTA)
-        double sl = b0;
-#pragma unroll
-        for (int o = 8; o >= 1; o >>= 1) sl += __shfl_xor_sync(0xffffffffu, sl, o);
-        if (live && own && q == 0) sRacc[r] = fma(gval, sl, sRacc[r]);
-      }
-      if (live) {
-        const int EA = tf_row_exp(xa), EB = tf_row_exp(xb);
-        if (q == 0) {
-          ea[r] = EA;
-          if (own) eb[r] = EB;
-        }
-        const int off = tc_off(r, 2 * q, TF_KP, 2);
-        {
-          const unsigned long long f0 = tf_fixed(a0, EA), f1 = tf_fixed(a1, EA);
-          const uint32_t h0 = (uint32_t)(f0 >> 24), l0 = (uint32_t)f0 & 0xFFFFFFu;
-          const uint32_t h1 = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
-          const bool n0 = __double_as_longlong(a0) < 0, n1 = __double_as_longlong(a1) < 0;
-#pragma unroll
-          for (int i = 0; i < TF_SL; i++) {
-            const uint32_t c0 = i < 4 ? (h0 >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
-            const uint32_t c1 = i < 4 ? (h1 >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
-            *(uint32_t *)(asl + i * Dm::A_STRIDE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
-          }
-        }
-        if (own) {
-          const unsigned long long f0 = tf_fixed(b0, EB), f1 = tf_fixed(b1, EB);
-          const uint32_t h0 = (uint32_t)(f0 >> 24), l0 = (uint32_t)f0 & 0xFFFFFFu;
-          const uint32_t h1 = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
-          const bool n0 = __double_as_longlong(b0) < 0, n1 = __double_as_longlong(b1) < 0;
-#pragma unroll
-          for (int i = 0; i < TF_SL; i++) {
-            const uint32_t c0 = i < 4 ? (h0 >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
-            const uint32_t c1 = i < 4 ? (h1 >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
-            *(uint32_t *)(bsl + i * Dm::B_SLICE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
-          }
-        }
-      }
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    // per chunk of e's functions (N = TF_NCH columns at most): MMAs, commit,
-    // wait, epilogue; the accumulators are reused chunk after chunk
-    for (int ch = 0; ch < Dm::NCHUNK; ch++) {
-      const int clo = ch * TF_NCH, cn = NPAD - clo < TF_NCH ? NPAD - clo : TF_NCH;
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(cn >> 3) << 17) |
-                               ((uint32_t)(TF_M >> 4) << 24);
-        // the descriptors of one chunk differ only in their start-address
-        // field (address / 16, 14 bits: every shared address fits without a
-        // carry), so each MMA's are constant offsets from two base
-        // descriptors and the 56 issues unroll into straight-line code
-        const uint64_t ad0 = tc_desc(tc_smem(asl), 128, (TF_KP / 8) * 128);
-        const uint64_t bd0 = tc_desc(tc_smem(bsl) + (clo / 8) * (TF_KP / 8) * 128, 128, (TF_KP / 8) * 128);
-#pragma unroll
-        for (int i = 0; i < TF_SL; i++)
-#pragma unroll
-          for (int j = 0; j < TF_SL - i; j++)
-#pragma unroll
-            for (int ks = 0; ks < TF_KP / 16; ks++)
-              tc_mma<0>(tmem + (i + j) * cn, ad0 + (uint64_t)((i * Dm::A_STRIDE + ks * 256) >> 4),
-                        bd0 + (uint64_t)((j * Dm::B_SLICE + ks * 256) >> 4), idesc, (i == 0 && ks == 0) ? 0u : 1u);
-        tc_commit(tc_smem(bar));
-      }
-      __syncthreads();
-      const bool waited = tc_wait(tc_smem(bar), ncommit & 1);
-      if (__syncthreads_or(!waited)) {
-        failed = true;
-        fail_parity = ncommit & 1;
+  if (warp < 8) {
+    // ------------------------------ producers ------------------------------
+    const int ptid = tid;
+    int fi = 0;
+    bool stop = false;
+    for (int o = blockIdx.x; o < count && !stop; o += gridDim.x) {
+      const int e = ent_el[o];
+      const int h0 = hf_ptr[e], nf = hf_ptr[e + 1] - h0;
+      if (nf <= 0) continue;
+      if (nf > TF_NF) {  // not a prism's face list (uniform over every role)
+        if (ptid == 0) atomicCAS(err, 0, 7);
         break;
       }
-      ncommit++;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // epilogue: D[r][i] = K[i][function r] (warps whose lane quarter holds
-      // no row skip it as a whole)
-      if (lq * 32 < rows) {
-        const bool rok = r_ep < rows;
-        const int sa = rok ? ea[r_ep] : 0;
-        double *oblk = interior ? val + F.blk : nullptr;
-        for (int grp = 0; grp < cn / 16; grp++) {
-          const int cl = half * (cn / 2) + grp * 8;  // column within the chunk
-          if (clo + cl >= NS) continue;              // padding columns only (uniform over the warp)
-          float C[TF_SL][8];
+      if (ptid < nf) sHF[ptid] = hf[h0 + ptid];
+      tp_bar(1);
+      for (int t = ptid; t < nf * TF_NQ * TF_GEO; t += 256) {
+        const int f = t / (TF_NQ * TF_GEO), r = t % (TF_NQ * TF_GEO);
+        sface[f * FD + (r / TF_GEO) * TF_GEOS + r % TF_GEO] = geo[(size_t)sHF[f].face * TF_NQ * TF_GEO + r];
+      }
+      tp_bar(1);
+      for (int f = 0; f < nf; f++, fi++) {
+        const int b = fi & 1;
+        // buffer b is free once the epilogue finished face fi - 2
+        if (fi >= 2 && !tp_group_wait(bar_free + b, ((fi >> 1) - 1) & 1, ptid == 0, 1, abort_flag, slots + (fi & 1))) {
+          stop = true;
+          break;
+        }
+        const DgHalfFace &F = sHF[f];
+        const double *sGeo = sface + f * FD;
+        const bool interior = F.el2 >= 0;
+        const int own2 = F.owner_is_2;
+        const int p1 = el_p[F.el1], p2 = interior ? el_p[F.el2] : 1;
+        const int ti = F.nfv == 4 ? 1 : 0;
+        const int pr = (interior && tf_nqf[p2][ti] > tf_nqf[p1][ti]) ? p2 : p1;
+        const int nq = tf_nqf[pr][ti];
+        const int pnb = own2 ? p1 : p2;
+        const int ns_nb = interior ? tf_ns[pnb] : 0;
+        const int rows = NS + ns_nb;
+        const int own_side = own2 ? 2 : 1;
+        const int cfg_own = own2 ? F.cfg2 : F.cfg1, cfg_nb = own2 ? F.cfg1 : F.cfg2;
+        if (pr > 3 || rows > Dm::ROWS || nq > TF_NQ) {  // a degree-4 neighbour (uniform)
+          if (ptid == 0) {
+            atomicCAS(err, 0, 7);
+            *abort_flag = 1;
+          }
+          stop = true;
+          break;
+        }
+        uint8_t *asl = smem + b * Tp::BUF, *bsl = asl + Dm::A_BYTES;
+        int *ea = sexp + 192 * b, *eb = ea + 128;
+        const double *tab_own = ftab + ftab_off[(cfg_own * 3 + pr - 1) * 3 + P - 1];
+        const double *tab_nb = interior ? ftab + ftab_off[(cfg_nb * 3 + pr - 1) * 3 + pnb - 1] : tab_own;
+        const long long so_bit = own2 ? (long long)1 << 63 : 0;
+        auto tab_load = [&](int t, double2 &x01, double2 &x23) {
+          const int r = t >> 4, q = t & 15;
+          if (r < rows && q < nq) {
+            const bool own = r < NS;
+            const double *tb = (own ? tab_own : tab_nb) + ((size_t)q * (own ? NS : ns_nb) + (own ? r : r - NS)) * 4;
+            x01 = __ldg(reinterpret_cast<const double2 *>(tb));
+            x23 = __ldg(reinterpret_cast<const double2 *>(tb) + 1);
+          } else {
+            x01 = make_double2(0.0, 0.0);
+            x23 = x01;
+          }
+        };
+        double2 n01, n23;
+        tab_load(ptid, n01, n23);
+        for (int base = 0; base < rows * 16; base += 256) {
+          const int t = base + ptid, r = t >> 4, q = t & 15;
+          const bool live = r < rows, own = r < NS;  // uniform over the segment
+          const double2 t01 = n01, t23 = n23;
+          if (base + 256 < rows * 16) tab_load(t + 256, n01, n23);
+          double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
+          if (live && q < nq) {
+            const int side = own ? own_side : 3 - own_side;
+            const double *G = sGeo + q * TF_GEOS;
+            const double *v = G + (side == 1 ? 2 : 5);
+            const double phi = t01.x;
+            const double g = fma(v[0], t01.y, fma(v[1], t23.x, v[2] * t23.y));
+            a0 = __longlong_as_double(__double_as_longlong(phi) ^ (side == 2 ? (long long)1 << 63 : 0));
+            a1 = g;
+            if (own) {
+              const double sphi = __longlong_as_double(__double_as_longlong(phi) ^ so_bit);
+              b0 = fma(G[0], g, G[1] * sphi);
+              b1 = -(G[0] * sphi);
+            }
+          }
+          int xa = max(tf_biased_exp(a0), tf_biased_exp(a1)), xb = max(tf_biased_exp(b0), tf_biased_exp(b1));
 #pragma unroll
-          for (int d = 0; d < TF_SL; d++) tc_ld8(tmem + ((uint32_t)(lq * 32) << 16) + d * cn + cl, C[d]);
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          for (int o2 = 8; o2 >= 1; o2 >>= 1) {
+            xa = max(xa, __shfl_xor_sync(0xffffffffu, xa, o2));
+            xb = max(xb, __shfl_xor_sync(0xffffffffu, xb, o2));
+          }
+          if (!interior) {
+            double sl = b0;
 #pragma unroll
-          for (int c = 0; c < 8; c++) {
-            const int i = clo + cl + c;
-            if (!rok || i >= NS) continue;
-            // sum_d C_d 2^(-8(d+2)) = (hi 2^24 + lo) 2^-64 with hi = C_0..C_3
-            // and lo = C_4..C_6 in base 256 (|hi| < 2^48.01, |lo| <
-            // 2^40.01); T = hi 2^14 + lo / 2^10 (< 2^63), so the sum is
-            // T 2^-54, with 9 bits beyond the 53 the double rounds to
-            // |C_d| <= 32 * 255^2 < 2^21: pairs of them combine in int32
-            static_assert(TF_SL == 7 && TF_KP == 32, "seven accumulators of K = 32 products");
-            const int u01 = tf_exact_int(C[0][c]) * 256 + tf_exact_int(C[1][c]);
-            const int u23 = tf_exact_int(C[2][c]) * 256 + tf_exact_int(C[3][c]);
-            const int u45 = tf_exact_int(C[4][c]) * 256 + tf_exact_int(C[5][c]);
-            const long long hi = (long long)u01 * 65536 + u23, lo = (long long)u45 * 256 + tf_exact_int(C[6][c]);
-            const double v = tf_i64_scaled(hi * 16384LL + (lo >> 10), sa + eb[i] - 54);
-            if (r_ep < NS)
-              sD[r_ep * Dm::SD_LD + i] += v;
-            else
-              oblk[i + (size_t)NS * (r_ep - NS)] = v;
+            for (int o2 = 8; o2 >= 1; o2 >>= 1) sl += __shfl_xor_sync(0xffffffffu, sl, o2);
+            if (live && own && q == 0) sRacc[r] = fma(gval, sl, sRacc[r]);
+          }
+          if (live) {
+            const int EA = tf_row_exp(xa), EB = tf_row_exp(xb);
+            if (q == 0) {
+              ea[r] = EA;
+              if (own) eb[r] = EB;
+            }
+            const int off = tc_off(r, 2 * q, TF_KP, 2);
+            {
+              const unsigned long long f0 = tf_fixed(a0, EA), f1 = tf_fixed(a1, EA);
+              const uint32_t h0w = (uint32_t)(f0 >> 24), l0 = (uint32_t)f0 & 0xFFFFFFu;
+              const uint32_t h1w = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
+              const bool n0 = __double_as_longlong(a0) < 0, n1 = __double_as_longlong(a1) < 0;
+#pragma unroll
+              for (int i = 0; i < TF_SL; i++) {
+                const uint32_t c0 = i < 4 ? (h0w >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
+                const uint32_t c1 = i < 4 ? (h1w >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
+                *(uint32_t *)(asl + i * Dm::A_STRIDE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
+              }
+            }
+            if (own) {
+              const unsigned long long f0 = tf_fixed(b0, EB), f1 = tf_fixed(b1, EB);
+              const uint32_t h0w = (uint32_t)(f0 >> 24), l0 = (uint32_t)f0 & 0xFFFFFFu;
+              const uint32_t h1w = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
+              const bool n0 = __double_as_longlong(b0) < 0, n1 = __double_as_longlong(b1) < 0;
+#pragma unroll
+              for (int i = 0; i < TF_SL; i++) {
+                const uint32_t c0 = i < 4 ? (h0w >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
+                const uint32_t c1 = i < 4 ? (h1w >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
+                *(uint32_t *)(bsl + i * Dm::B_SLICE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
+              }
+            }
           }
         }
+        if (ptid == 0) {
+          meta[b].blk = interior ? F.blk : -1;
+          meta[b].rows = rows;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tp_bar(1);
+        if (ptid == 0) tp_arrive(bar_full + b);
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();  // TMEM read before the next chunk's MMAs overwrite it
+      if (stop) break;
+      // the owner's boundary rhs share (complete after the last barrier);
+      // the next owner's first writes to sRacc follow its first barrier
+      if (ptid < NS) {
+        const double v = sRacc[ptid];
+        sRacc[ptid] = 0.0;
+        if (share)
+          share[(size_t)o * (NS * NS + NS) + NS * NS + ptid] = v;
+        else
+          rhs[roff[e] + ptid] += v;
+      }
     }
-    if (failed) break;
+  } else {
+    // ----------------------------- MMA + epilogue -----------------------------
+    const int etid = tid - 256, ew = warp - 8, lq = ew & 3, half = ew >> 2;
+    const int r_ep = lq * 32 + (tid & 31);
+    int fi = 0;
+    bool stop = false;
+    for (int o = blockIdx.x; o < count && !stop; o += gridDim.x) {
+      const int e = ent_el[o];
+      const int nf = hf_ptr[e + 1] - hf_ptr[e];
+      if (nf <= 0) continue;
+      if (nf > TF_NF) break;
+      for (int f = 0; f < nf; f++, fi++) {
+        const int b = fi & 1;
+        if (etid == 0 && tp_wait1(bar_full + b, (fi >> 1) & 1, abort_flag)) {
+          // operands of face fi written; the accumulators are free (this
+          // group finished face fi - 1 before getting here)
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NPAD >> 3) << 17) |
+                                 ((uint32_t)(TF_M >> 4) << 24);
+          const uint64_t ad0 = tc_desc(tc_smem(smem + b * Tp::BUF), 128, (TF_KP / 8) * 128);
+          const uint64_t bd0 = tc_desc(tc_smem(smem + b * Tp::BUF + Dm::A_BYTES), 128, (TF_KP / 8) * 128);
+#pragma unroll
+          for (int i = 0; i < TF_SL; i++)
+#pragma unroll
+            for (int j = 0; j < TF_SL - i; j++)
+#pragma unroll
+              for (int ks = 0; ks < TF_KP / 16; ks++)
+                tc_mma<0>(tmem + (i + j) * NPAD, ad0 + (uint64_t)((i * Dm::A_STRIDE + ks * 256) >> 4),
+                          bd0 + (uint64_t)((j * Dm::B_SLICE + ks * 256) >> 4), idesc, (i == 0 && ks == 0) ? 0u : 1u);
+          tc_commit(tc_smem(bar_mma + b));
+          *s_issued = fi + 1;
+        }
+        __syncwarp();  // warp 8 reconverged before its aligned TMEM loads
+        if (!tp_group_wait(bar_mma + b, (fi >> 1) & 1, etid == 0, 2, abort_flag, slots + 2 + (fi & 1))) {
+          stop = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int rows = meta[b].rows;
+        const long long blk = meta[b].blk;
+        const int *ea = sexp + 192 * b, *eb = ea + 128;
+        if (lq * 32 < rows) {
+          const bool rok = r_ep < rows;
+          const int sa = rok ? ea[r_ep] : 0;
+          double *oblk = blk >= 0 ? val + blk : nullptr;
+#pragma unroll
+          for (int grp = 0; grp < NPAD / 16; grp++) {
+            const int cl = half * (NPAD / 2) + grp * 8;
+            if (cl >= NS) continue;  // padding columns only (uniform over the warp)
+            float C[TF_SL][8];
+#pragma unroll
+            for (int d = 0; d < TF_SL; d++) tc_ld8(tmem + ((uint32_t)(lq * 32) << 16) + d * NPAD + cl, C[d]);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+              const int i = cl + c;
+              if (!rok || i >= NS) continue;
+              const int u01 = tf_exact_int(C[0][c]) * 256 + tf_exact_int(C[1][c]);
+              const int u23 = tf_exact_int(C[2][c]) * 256 + tf_exact_int(C[3][c]);
+              const int u45 = tf_exact_int(C[4][c]) * 256 + tf_exact_int(C[5][c]);
+              const long long hi = (long long)u01 * 65536 + u23, lo = (long long)u45 * 256 + tf_exact_int(C[6][c]);
+              const double v = tf_i64_scaled(hi * 16384LL + (lo >> 10), sa + eb[i] - 54);
+              if (r_ep < NS)
+                sD[r_ep * SD_LD + i] += v;
+              else
+                oblk[i + (size_t)NS * (r_ep - NS)] = v;
+            }
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        tp_bar(2);  // TMEM, meta and exponents of buffer b read
+        if (etid == 0) tp_arrive(bar_free + b);
+      }
+      if (stop) break;
+      // the owner's diagonal-block share (complete after the last barrier),
+      // then cleared for the next owner
+      if (share) {
+        double *sd = share + (size_t)o * (NS * NS + NS);
+        for (int t = etid; t < NS * NS; t += 256) {
+          double &s = sD[(t / NS) * SD_LD + t % NS];
+          sd[t] = s;
+          s = 0.0;
+        }
+      } else {
+        double *dblk = val + boff_diag[e];
+        for (int t = etid; t < NS * NS; t += 256) {
+          double &s = sD[(t / NS) * SD_LD + t % NS];
+          dblk[t] += s;
+          s = 0.0;
+        }
+      }
+      tp_bar(2);
+    }
   }
-  if (failed) tc_wait(tc_smem(bar), fail_parity);  // let the issued MMAs drain (bounded) before freeing TMEM
+  __syncwarp();
   __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TF_TMEM_COLS));
-  if (failed || bad_input) {
-    if (tid == 0) atomicExch(err, failed ? 6 : 7);
-    return;
+  if (tid == 256 && *s_issued > 0) {
+    // MMAs issued but not waited for (a role gave up): let them finish
+    // (bounded) before the TMEM is freed
+    const int last = *s_issued - 1;
+    tc_wait(tc_smem(bar_mma + (last & 1)), (last >> 1) & 1);
   }
-  if (share) {
-    // the diagonal-block and rhs shares to this owner's scratch slot: the
-    // volume kernel may still be writing the block (it runs alongside)
-    double *sd = share + (size_t)bi * (NS * NS + NS);
-    for (int t = tid; t < NS * NS; t += TF_THREADS) sd[t] = sD[(t / NS) * Dm::SD_LD + t % NS];
-    if (tid < NS) sd[NS * NS + tid] = sRacc[tid];
-    return;
-  }
-  {
-    // the diagonal block is column-major (entry (i, r) at i + NS r): sD's row r
-    double *dblk = val + boff_diag[e];
-    for (int t = tid; t < NS * NS; t += TF_THREADS) dblk[t] += sD[(t / NS) * Dm::SD_LD + t % NS];
-  }
-  if (tid < NS) rhs[roff[e] + tid] += sRacc[tid];
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  if (tid == 0 && *abort_flag) atomicCAS(err, 0, 6);
 }
 
 bool dg_tc_faces_supported(int p) { return p >= 1 && p <= 3; }
@@ -584,12 +677,17 @@ int launch_dg_tc_faces(cudaStream_t st, int p, int count, const int *ent_el, con
   if (count <= 0) return 0;
   GB_CHECK(dg_tc_faces_supported(p), "tensor-core DG face kernel covers p = 1..3");
   GB_CHECK(geo && ftab && ftab_off, "tensor-core DG faces need the face geometry and basis tables");
-#define GB_TF_LAUNCH(PP)                                                                                      \
-  {                                                                                                           \
-    const int smem = TfDims<PP>::SMEM;                                                                        \
-    GB_CUDA(cudaFuncSetAttribute(dg_tc_faces_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
-    dg_tc_faces_kernel<PP><<<count, TF_THREADS, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, geo, ftab,       \
-                                                            ftab_off, g, boff_diag, roff, val, rhs, err, share); \
+  // persistent: one CTA per SM (each takes the whole TMEM), owners strided
+  int dev = 0, nsm = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  GB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = count < nsm ? count : nsm;
+#define GB_TF_LAUNCH(PP)                                                                                          \
+  {                                                                                                               \
+    const int smem = TpDims<PP>::SMEM;                                                                            \
+    GB_CUDA(cudaFuncSetAttribute(dg_tc_faces_pipe_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
+    dg_tc_faces_pipe_kernel<PP><<<grid, TP_THREADS, smem, st>>>(count, ent_el, hf_ptr, hf, el_p, geo, ftab,       \
+                                                                ftab_off, g, boff_diag, roff, val, rhs, err, share); \
   }
   switch (p) {
     case 1: GB_TF_LAUNCH(1); break;
