@@ -50,6 +50,8 @@
 // Every wait has an iteration limit: on expiry the CTA records an error, lets
 // its MMAs drain (again with a limit), frees its TMEM and returns.
 
+#include <type_traits>
+
 #include "dg_face.cuh"
 #include "gbfem_internal.h"
 #include "tc_ptx.cuh"
@@ -163,11 +165,16 @@ __device__ __forceinline__ v3 tf_face_v(v3 j1, v3 j2, v3 j3, const double *A, v3
 // subtract instead of a conversion instruction
 __device__ __forceinline__ int tf_exact_int(float c) { return __float_as_int(c + 12582912.0f) - 0x4B400000; }
 
-// BF16 bit pattern of the integer c (|c| <= 255): through an FP32 add on the
-// FMA pipe (exact), the sign set separately
-__device__ __forceinline__ uint32_t tf_bf16_bits(uint32_t mag, bool neg) {
-  const float fv = __uint_as_float(0x4B000000u | mag) - 8388608.0f;
-  return (__float_as_uint(fv) >> 16) | (neg ? 0x8000u : 0u);
+// Two signed 8-bit slice values as a packed BF16 pair (first in the low
+// half): each as the exact FP32 s c (s = +-1) through one FMA on 2^23 + c,
+// then one conversion packs both (exact: |c| <= 255).  A zero slice packs as
+// +0 whatever its sign; the products it enters are zero either way.
+__device__ __forceinline__ uint32_t tf_bf16x2(uint32_t c0, float s0, uint32_t c1, float s1) {
+  const float f0 = fmaf(__uint_as_float(0x4B000000u | c0), s0, -8388608.0f * s0);
+  const float f1 = fmaf(__uint_as_float(0x4B000000u | c1), s1, -8388608.0f * s1);
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(f1), "f"(f0));
+  return r;
 }
 
 // The reference basis at the face points of every configuration: one block
@@ -279,6 +286,13 @@ __global__ void __launch_bounds__(128) dg_face_geometry_kernel(
 // the outcome, so every decision is uniform over the group.  The
 // arithmetic is that of dg_tc_faces_kernel: bit-identical results.
 constexpr int TP_THREADS = 512;
+// MMA issuers: lane 0 of warps 8 .. 8 + TP_ISSUERS - 1, each owning whole
+// accumulators (d = 6 | 5, 0 | 4, 1 | 3, 2: seven slice pairs, 14 MMAs
+// each), so that their issue runs side by side; all commit to mma[b]
+constexpr int TP_ISSUERS = 4;
+__host__ __device__ constexpr int tp_acc(int k, int m) {  // issuer k's m-th accumulator (-1: none)
+  return k == 0 ? (m == 0 ? 6 : -1) : m == 0 ? 6 - k : k - 1;
+}
 
 struct TpMeta {
   long long blk;  // block (owner, neighbour); -1 on the boundary
@@ -297,8 +311,8 @@ struct TpDims {
   static constexpr int OFF_HF = OFF_RACC + 64 * 8;                          // [TF_NF]
   static constexpr int OFF_META = (OFF_HF + TF_NF * (int)sizeof(DgHalfFace) + 15) / 16 * 16;  // [2]
   static constexpr int OFF_EXP = OFF_META + 2 * (int)sizeof(TpMeta);       // [2][128 + 64]
-  static constexpr int OFF_BAR = OFF_EXP + 2 * 192 * 4;                     // full[2], mma[2], free[2]
-  static constexpr int SMEM_USED = OFF_BAR + 6 * 8 + 32;
+  static constexpr int OFF_BAR = OFF_EXP + 2 * 192 * 4;  // full[2], mma[2], free[2], drain[TP_ISSUERS]
+  static constexpr int SMEM_USED = OFF_BAR + 10 * 8 + 32;
   // requested at least 116 KB so that no two CTAs share an SM (each
   // allocates all 512 TMEM columns)
   static constexpr int SMEM = SMEM_USED > 116 * 1024 ? SMEM_USED : 116 * 1024;
@@ -356,16 +370,17 @@ __global__ void __launch_bounds__(TP_THREADS, 1) dg_tc_faces_pipe_kernel(
   TpMeta *meta = (TpMeta *)(smem + Tp::OFF_META);
   int *sexp = (int *)(smem + Tp::OFF_EXP);        // buffer b: ea at 192 b, eb at 192 b + 128
   uint64_t *bar_full = (uint64_t *)(smem + Tp::OFF_BAR), *bar_mma = bar_full + 2, *bar_free = bar_full + 4;
-  uint32_t *tmem_slot = (uint32_t *)(bar_full + 6);
+  uint64_t *bar_drain = bar_full + 6;
+  uint32_t *tmem_slot = (uint32_t *)(bar_full + 6 + TP_ISSUERS);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   volatile int *slots = (volatile int *)(tmem_slot + 2);  // [2] producers, [2] epilogue
-  int *s_issued = (int *)(tmem_slot + 6);                 // faces whose MMAs were issued
   const int tid = threadIdx.x, warp = tid >> 5;
   if (tid == 0) {
-    for (int i = 0; i < 6; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(bar_full + i)));
+    for (int i = 0; i < 6 + TP_ISSUERS; i++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(bar_full + i)),
+                   "r"(i == 2 || i == 3 ? TP_ISSUERS : 1));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     *abort_flag = 0;
-    *s_issued = 0;
   }
   for (int t = tid; t < NS * SD_LD; t += TP_THREADS) sD[t] = 0.0;
   if (tid < 64) sRacc[tid] = 0.0;
@@ -378,6 +393,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) dg_tc_faces_pipe_kernel(
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
+  bool issued_any = false;  // this thread issued MMAs (an issuer)
 
   if (warp < 8) {
     // ------------------------------ producers ------------------------------
@@ -489,24 +505,24 @@ __global__ void __launch_bounds__(TP_THREADS, 1) dg_tc_faces_pipe_kernel(
               const unsigned long long f0 = tf_fixed(a0, EA), f1 = tf_fixed(a1, EA);
               const uint32_t h0w = (uint32_t)(f0 >> 24), l0 = (uint32_t)f0 & 0xFFFFFFu;
               const uint32_t h1w = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
-              const bool n0 = __double_as_longlong(a0) < 0, n1 = __double_as_longlong(a1) < 0;
+              const float s0 = __double_as_longlong(a0) < 0 ? -1.0f : 1.0f, s1 = __double_as_longlong(a1) < 0 ? -1.0f : 1.0f;
 #pragma unroll
               for (int i = 0; i < TF_SL; i++) {
                 const uint32_t c0 = i < 4 ? (h0w >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
                 const uint32_t c1 = i < 4 ? (h1w >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
-                *(uint32_t *)(asl + i * Dm::A_STRIDE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
+                *(uint32_t *)(asl + i * Dm::A_STRIDE + off) = tf_bf16x2(c0, s0, c1, s1);
               }
             }
             if (own) {
               const unsigned long long f0 = tf_fixed(b0, EB), f1 = tf_fixed(b1, EB);
               const uint32_t h0w = (uint32_t)(f0 >> 24), l0 = (uint32_t)f0 & 0xFFFFFFu;
               const uint32_t h1w = (uint32_t)(f1 >> 24), l1 = (uint32_t)f1 & 0xFFFFFFu;
-              const bool n0 = __double_as_longlong(b0) < 0, n1 = __double_as_longlong(b1) < 0;
+              const float s0 = __double_as_longlong(b0) < 0 ? -1.0f : 1.0f, s1 = __double_as_longlong(b1) < 0 ? -1.0f : 1.0f;
 #pragma unroll
               for (int i = 0; i < TF_SL; i++) {
                 const uint32_t c0 = i < 4 ? (h0w >> (24 - 8 * i)) & 255u : (l0 >> (16 - 8 * (i - 4))) & 255u;
                 const uint32_t c1 = i < 4 ? (h1w >> (24 - 8 * i)) & 255u : (l1 >> (16 - 8 * (i - 4))) & 255u;
-                *(uint32_t *)(bsl + i * Dm::B_SLICE + off) = tf_bf16_bits(c0, n0) | (tf_bf16_bits(c1, n1) << 16);
+                *(uint32_t *)(bsl + i * Dm::B_SLICE + off) = tf_bf16x2(c0, s0, c1, s1);
               }
             }
           }
@@ -535,6 +551,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) dg_tc_faces_pipe_kernel(
     // ----------------------------- MMA + epilogue -----------------------------
     const int etid = tid - 256, ew = warp - 8, lq = ew & 3, half = ew >> 2;
     const int r_ep = lq * 32 + (tid & 31);
+    const int issuer = (tid & 31) == 0 && ew < TP_ISSUERS ? ew : -1;
     int fi = 0;
     bool stop = false;
     for (int o = blockIdx.x; o < count && !stop; o += gridDim.x) {
@@ -544,7 +561,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) dg_tc_faces_pipe_kernel(
       if (nf > TF_NF) break;
       for (int f = 0; f < nf; f++, fi++) {
         const int b = fi & 1;
-        if (etid == 0 && tp_wait1(bar_full + b, (fi >> 1) & 1, abort_flag)) {
+        if (issuer >= 0 && tp_wait1(bar_full + b, (fi >> 1) & 1, abort_flag)) {
           // operands of face fi written; the accumulators are free (this
           // group finished face fi - 1 before getting here)
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -552,18 +569,31 @@ __global__ void __launch_bounds__(TP_THREADS, 1) dg_tc_faces_pipe_kernel(
                                  ((uint32_t)(TF_M >> 4) << 24);
           const uint64_t ad0 = tc_desc(tc_smem(smem + b * Tp::BUF), 128, (TF_KP / 8) * 128);
           const uint64_t bd0 = tc_desc(tc_smem(smem + b * Tp::BUF + Dm::A_BYTES), 128, (TF_KP / 8) * 128);
+          auto issue = [&](auto KK) {
+            constexpr int K = decltype(KK)::value;
 #pragma unroll
-          for (int i = 0; i < TF_SL; i++)
+            for (int m = 0; m < 2; m++) {
+              const int d = tp_acc(K, m);
+              if (d < 0) continue;
 #pragma unroll
-            for (int j = 0; j < TF_SL - i; j++)
+              for (int i = 0; i <= d; i++)
 #pragma unroll
-              for (int ks = 0; ks < TF_KP / 16; ks++)
-                tc_mma<0>(tmem + (i + j) * NPAD, ad0 + (uint64_t)((i * Dm::A_STRIDE + ks * 256) >> 4),
-                          bd0 + (uint64_t)((j * Dm::B_SLICE + ks * 256) >> 4), idesc, (i == 0 && ks == 0) ? 0u : 1u);
+                for (int ks = 0; ks < TF_KP / 16; ks++)
+                  tc_mma<0>(tmem + d * NPAD, ad0 + (uint64_t)((i * Dm::A_STRIDE + ks * 256) >> 4),
+                            bd0 + (uint64_t)(((d - i) * Dm::B_SLICE + ks * 256) >> 4), idesc,
+                            (i == 0 && ks == 0) ? 0u : 1u);
+            }
+          };
+          switch (issuer) {
+            case 0: issue(std::integral_constant<int, 0>{}); break;
+            case 1: issue(std::integral_constant<int, 1>{}); break;
+            case 2: issue(std::integral_constant<int, 2>{}); break;
+            default: issue(std::integral_constant<int, 3>{}); break;
+          }
           tc_commit(tc_smem(bar_mma + b));
-          *s_issued = fi + 1;
+          issued_any = true;
         }
-        __syncwarp();  // warp 8 reconverged before its aligned TMEM loads
+        __syncwarp();  // the issuing warps reconverged before their aligned TMEM loads
         if (!tp_group_wait(bar_mma + b, (fi >> 1) & 1, etid == 0, 2, abort_flag, slots + 2 + (fi & 1))) {
           stop = true;
           break;
@@ -588,11 +618,21 @@ __global__ void __launch_bounds__(TP_THREADS, 1) dg_tc_faces_pipe_kernel(
             for (int c = 0; c < 8; c++) {
               const int i = cl + c;
               if (!rok || i >= NS) continue;
-              const int u01 = tf_exact_int(C[0][c]) * 256 + tf_exact_int(C[1][c]);
-              const int u23 = tf_exact_int(C[2][c]) * 256 + tf_exact_int(C[3][c]);
-              const int u45 = tf_exact_int(C[4][c]) * 256 + tf_exact_int(C[5][c]);
-              const long long hi = (long long)u01 * 65536 + u23, lo = (long long)u45 * 256 + tf_exact_int(C[6][c]);
-              const double v = tf_i64_scaled(hi * 16384LL + (lo >> 10), sa + eb[i] - 54);
+              // u_ab = C_a 256 + C_b from the float bits (exact-integer
+              // trick, its offset folded into one constant; modulo 2^32,
+              // the true values fit int32); then
+              // T = u01 2^30 + u23 2^14 + floor((u45 256 + C_6) / 2^10)
+              // with the floor in int32 (u45 = 4 q + r, 0 <= r < 4)
+              const uint32_t K2 = 257u * 0x4B400000u;
+              const int u01 = (int)((uint32_t)__float_as_int(C[0][c] + 12582912.0f) * 256u +
+                                    (uint32_t)__float_as_int(C[1][c] + 12582912.0f) - K2);
+              const int u23 = (int)((uint32_t)__float_as_int(C[2][c] + 12582912.0f) * 256u +
+                                    (uint32_t)__float_as_int(C[3][c] + 12582912.0f) - K2);
+              const int u45 = (int)((uint32_t)__float_as_int(C[4][c] + 12582912.0f) * 256u +
+                                    (uint32_t)__float_as_int(C[5][c] + 12582912.0f) - K2);
+              const int lo10 = (u45 >> 2) + ((((u45 & 3) << 8) + tf_exact_int(C[6][c])) >> 10);
+              const long long T = (long long)u01 * (1LL << 30) + (long long)u23 * (1LL << 14) + lo10;
+              const double v = tf_i64_scaled(T, sa + eb[i] - 54);
               if (r_ep < NS)
                 sD[r_ep * SD_LD + i] += v;
               else
@@ -625,14 +665,13 @@ __global__ void __launch_bounds__(TP_THREADS, 1) dg_tc_faces_pipe_kernel(
       tp_bar(2);
     }
   }
-  __syncwarp();
-  __syncthreads();
-  if (tid == 256 && *s_issued > 0) {
-    // MMAs issued but not waited for (a role gave up): let them finish
-    // (bounded) before the TMEM is freed
-    const int last = *s_issued - 1;
-    tc_wait(tc_smem(bar_mma + (last & 1)), (last >> 1) & 1);
+  // an issuer whose MMAs may still run (a role gave up after they were
+  // issued) lets them finish (bounded) before the TMEM is freed
+  if (warp >= 8 && (tid & 31) == 0 && warp - 8 < TP_ISSUERS && issued_any) {
+    tc_commit(tc_smem(bar_drain + (warp - 8)));
+    tc_wait(tc_smem(bar_drain + (warp - 8)), 0);
   }
+  __syncwarp();
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
   if (tid == 0 && *abort_flag) atomicCAS(err, 0, 6);
