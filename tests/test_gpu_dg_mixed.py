@@ -171,3 +171,36 @@ def test_mixed_mesh_refuses_std_path_and_bad_faces(gb):
     from modfem_gb300.mesh import MixedMesh
     with pytest.raises(GbFemError, match="vertex count"):
         c.set_mesh_mixed(MixedMesh(2, m.coords, m.el_nodes, bad, 1))
+
+
+def test_mixed_solves_double_word_operator_and_refinement(gb):
+    """On a mixed mesh: GMRES with the double-word Arnoldi operator (block
+    SpMV classes of both element types) and compensated-residual refinement,
+    both against a dense solve of the oracle's system."""
+    m, F, p, A, k = _problem(3, 1, 13, pmax=2, aniso=True)
+    dense, R, _ = _oracle_dense(m, F, p, A, k)
+    xr = np.linalg.solve(dense, R)
+    c = _context(gb, m, F, p, A, k)
+    c.set_option(gb.OPT_DG_SPMV_ARITH, gb.STD_DWORD)
+    x, it, res, rel = c.dg_solve(krylov=50, max_iter=20000, tol_rel=1e-12)
+    assert rel < 1e-12
+    assert vec_rel_err(x, xr) < 1e-7
+    c.set_option(gb.OPT_DG_RESIDUAL, gb.RESIDUAL_COMPENSATED)
+    x2, it2, outer, rel2 = c.dg_solve_ir(krylov=50, max_iter=20000, tol_rel=1e-300)
+    assert vec_rel_err(x2, xr) < 1e-9
+
+
+def test_mixed_autotuned_shapes_are_bit_identical(gb):
+    """The launch-shape autotuner on a mixed mesh (it times the prism
+    kernels); every variant gives the same matrix bit for bit."""
+    m, F, p, A, k = _problem(4, 2, 17)
+    c = _context(gb, m, F, p, A, k)
+    v0, r0 = c.dg_get_matrix()
+    vol, face, ms = c.dg_autotune(sample=256)
+    c.dg_assemble()
+    v1, r1 = c.dg_get_matrix()
+    assert np.array_equal(v0, v1) and np.array_equal(r0, r1)
+    c.dg_set_variants(vol=[0, 1, 1, 1, 1], face=[0, 1, 1, 1, 1])
+    c.dg_assemble()
+    v2, r2 = c.dg_get_matrix()
+    assert np.array_equal(v0, v2) and np.array_equal(r0, r2)
