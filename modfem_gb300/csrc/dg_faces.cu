@@ -41,6 +41,13 @@ __host__ __device__ constexpr int dg_face_threads(int p, int v) {
   return p == 1 ? (v == 0 ? 64 : 128) : p == 2 ? (v == 0 ? 192 : 128) : p == 3 ? (v == 0 ? 320 : 160)
                                                                               : (v == 0 ? 256 : 384);
 }
+// The double-word form at p = 4 keeps 22 float-triple accumulators a thread
+// at 256 threads (255 registers, one CTA of 8 warps per SM); 512 threads
+// halve them (128 registers, 16 warps): 87 ms instead of 103 (92 at 384) for
+// a 128k-prism mixed-degree mesh.  Other degrees as the FP64 form.
+__host__ __device__ constexpr int dg_face_threads_dw(int p, int v) {
+  return p == 4 ? (v == 0 ? 512 : 384) : dg_face_threads(p, v);
+}
 
 // LOW: the owner and all its neighbours have degree <= 3, so a face has at
 // most 16 points and a neighbour at most 40 functions: the point tables
@@ -315,7 +322,7 @@ int launch_dg_prism_faces(cudaStream_t st, int p, int count, const int *ent_el, 
   GB_CHECK(variant >= 0 && variant < DG_FACE_VARIANTS, "face kernel variant out of range");
 #define GB_DGF_LAUNCH(PP, VV, WW, LL)                                                                          \
   {                                                                                                             \
-    constexpr int T_ = dg_face_threads(PP, VV);                                                                 \
+    constexpr int T_ = WW ? dg_face_threads_dw(PP, VV) : dg_face_threads(PP, VV);                               \
     const size_t smem = sizeof(double) * DgFaceDims<PP, T_, LL>::SMEM_DOUBLES;                                  \
     GB_CUDA(cudaFuncSetAttribute(dg_prism_faces_kernel<PP, T_, WW, LL>,                                        \
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));                      \
