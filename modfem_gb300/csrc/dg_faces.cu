@@ -112,6 +112,19 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
 #pragma unroll
   for (int m = 0; m < (DW ? Dm::PER : 1); m++) dacc[m] = DwAcc{0.0f, 0.0f, 0.0f};
   double racc = 0.0;
+  // p = 4 double word: register tiles of block entries (dwacc_face_tile):
+  // the diagonal share in 3 x 5 tiles (375 of them, one a thread), kept over
+  // the faces; the off-diagonal blocks in 3 x 3 tiles
+  constexpr bool TILED = DW && P == 4;
+  constexpr int DTI = 3, DTJ = 5, NDI = NS / DTI, NDJ = NS / DTJ, OTI = 3, OTJ = 3, NOI = NS / OTI;
+  static_assert(!TILED || (NS % DTI == 0 && NS % DTJ == 0 && NS % OTI == 0 && NDI * NDJ <= DGF_THREADS),
+                "tiles of the p = 4 diagonal block");
+  DwAcc dtile[TILED ? DTI : 1][TILED ? DTJ : 1];
+#pragma unroll
+  for (int x = 0; x < (TILED ? DTI : 1); x++)
+#pragma unroll
+    for (int y = 0; y < (TILED ? DTJ : 1); y++) dtile[x][y] = DwAcc{0.0f, 0.0f, 0.0f};
+  const int dti = tid % NDI, dtj = tid / NDI;  // this thread's diagonal tile (tid < NDI NDJ)
   float2 *fL = reinterpret_cast<float2 *>(sL), *fM = reinterpret_cast<float2 *>(sM);
   float2 *fPhi = reinterpret_cast<float2 *>(sPhi), *fGam = reinterpret_cast<float2 *>(sGam);
   const int h0 = hf_ptr[e], h1 = hf_ptr[e + 1];
@@ -251,7 +264,11 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
     __syncthreads();
     // the face's share of the diagonal block: entry k = i + NS j
     const int own_lo = own2 ? ns1 : 0;
-    if (DW) {
+    if (TILED) {
+      if (tid < NDI * NDJ)
+        dwacc_face_tile<NS, (TILED ? DTI : 1), (TILED ? DTJ : 1)>(dtile, fL, fM, fPhi, fGam, nq, NCOL, dti * DTI,
+                                                                 dtj * DTJ, NS, own_lo);
+    } else if (DW) {
       dwacc_face_block<NS, THR, (DW ? Dm::PER : 1)>(dacc, fL, fM, fPhi, fGam, nq, NCOL, tid, NS * NS, own_lo);
     } else {
 #pragma unroll
@@ -270,7 +287,26 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
       // block (e, neighbour): NS x ns_nb, column-major, leading dimension NS
       const int nb_lo = own2 ? 0 : ns1, ns_nb = own2 ? ns1 : ns2;
       double *blk = val + F.blk;
-      if (DW) {
+      if (TILED) {
+        const int noj = (ns_nb + OTJ - 1) / OTJ;
+        for (int t = tid; t < NOI * noj; t += DGF_THREADS) {
+          const int oi = t % NOI, oj = t / NOI;
+          DwAcc o[TILED ? OTI : 1][TILED ? OTJ : 1];
+#pragma unroll
+          for (int x = 0; x < (TILED ? OTI : 1); x++)
+#pragma unroll
+            for (int y = 0; y < (TILED ? OTJ : 1); y++) o[x][y] = DwAcc{0.0f, 0.0f, 0.0f};
+          dwacc_face_tile<NS, (TILED ? OTI : 1), (TILED ? OTJ : 1)>(o, fL, fM, fPhi, fGam, nq, NCOL, oi * OTI,
+                                                                   oj * OTJ, ns_nb, nb_lo);
+#pragma unroll
+          for (int x = 0; x < (TILED ? OTI : 1); x++)
+#pragma unroll
+            for (int y = 0; y < (TILED ? OTJ : 1); y++) {
+              const int j = oj * OTJ + y;
+              if (j < ns_nb) blk[oi * OTI + x + (size_t)NS * j] = dwacc_value(o[x][y]);
+            }
+        }
+      } else if (DW) {
         constexpr int PB = DW ? Dm::PER : 1;
         for (int k0 = tid; k0 < NS * ns_nb; k0 += PB * DGF_THREADS) {
           DwAcc a[PB];
@@ -305,10 +341,20 @@ __global__ void __launch_bounds__(THR) dg_prism_faces_kernel(
   }
   if (h1 == h0) return;
   double *dblk = val + boff_diag[e];
+  if (TILED) {
+    if (tid < NDI * NDJ) {
 #pragma unroll
-  for (int m = 0; m < Dm::PER; m++) {
-    const int k = tid + m * DGF_THREADS;
-    if (k < NS * NS) dblk[k] += DW ? dwacc_value(dacc[DW ? m : 0]) : acc[m];
+      for (int x = 0; x < (TILED ? DTI : 1); x++)
+#pragma unroll
+        for (int y = 0; y < (TILED ? DTJ : 1); y++)
+          dblk[dti * DTI + x + (size_t)NS * (dtj * DTJ + y)] += dwacc_value(dtile[x][y]);
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < Dm::PER; m++) {
+      const int k = tid + m * DGF_THREADS;
+      if (k < NS * NS) dblk[k] += DW ? dwacc_value(dacc[DW ? m : 0]) : acc[m];
+    }
   }
   if (tid < NS) rhs[roff[e] + tid] += racc;
 }

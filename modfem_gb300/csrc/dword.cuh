@@ -301,6 +301,52 @@ __device__ __forceinline__ void dwacc_face_block(DwAcc (&a)[PER], const float2 *
 #pragma unroll
   for (int m = 0; m < PER; m++) dwacc_fold(a[m]);
 }
+
+// A TI x TJ tile of an NS-row block per thread: rows i0 .. i0 + TI - 1 (all
+// below NS), table columns col_lo + j0 + y for j0 + y < jend (columns past
+// jend repeat column j0 and are not to be stored).  A point's L, M values
+// are loaded once per tile row and its Phi, Gam values once per tile column
+// (TI + TJ pairs of loads for TI TJ entries instead of four loads an entry);
+// each entry gets the products and folds of dwacc_face_block in the same
+// order, so the sums are bit-identical.
+template <int NS, int TI, int TJ>
+__device__ __forceinline__ void dwacc_face_tile(DwAcc (&a)[TI][TJ], const float2 *sL, const float2 *sM,
+                                                const float2 *sPhi, const float2 *sGam, int nq, int ncol, int i0,
+                                                int j0, int jend, int col_lo) {
+  for (int q = 0; q < nq; q++) {
+    const float2 *Lq = sL + q * NS + i0, *Mq = sM + q * NS + i0;
+    const float2 *Pq = sPhi + q * ncol + col_lo, *Gq = sGam + q * ncol + col_lo;
+    float2 L[TI], M[TI], P[TJ], G[TJ];
+#pragma unroll
+    for (int x = 0; x < TI; x++) {
+      L[x] = Lq[x];
+      M[x] = Mq[x];
+    }
+#pragma unroll
+    for (int y = 0; y < TJ; y++) {
+      const int j = j0 + y < jend ? j0 + y : j0;
+      P[y] = Pq[j];
+      G[y] = Gq[j];
+    }
+#pragma unroll
+    for (int x = 0; x < TI; x++)
+#pragma unroll
+      for (int y = 0; y < TJ; y++) {
+        dwacc_prod(a[x][y], L[x], P[y]);
+        dwacc_prod(a[x][y], M[x], G[y]);
+      }
+    if ((q & 3) == 3) {
+#pragma unroll
+      for (int x = 0; x < TI; x++)
+#pragma unroll
+        for (int y = 0; y < TJ; y++) dwacc_fold(a[x][y]);
+    }
+  }
+#pragma unroll
+  for (int x = 0; x < TI; x++)
+#pragma unroll
+    for (int y = 0; y < TJ; y++) dwacc_fold(a[x][y]);
+}
 #endif
 
 }  // namespace gbfem
