@@ -10,7 +10,12 @@
 // the rotations, the convergence test and the small triangular solve run in
 // one-block "logic" kernels on the device, and every kernel of a restart
 // cycle (restart residual, m Arnoldi steps, update of x) reads a state word
-// and returns at once when the cycle has already ended.  One cycle is
+// and returns at once when the cycle has already ended.  An Arnoldi step is
+// four kernels: the SpMV, the Gram-Schmidt dot partials, the
+// orthogonalisation (each block sums the dot partials itself; beyond 128
+// blocks a kernel of one warp per column sums them once) and the logic;
+// Krylov vectors after the first are stored unnormalised with a scale each
+// (V_k = sc_k W_k), applied by their readers, so no normalisation pass runs.  One cycle is
 // captured as a CUDA graph (per context, matrix size and Krylov dimension)
 // and replayed; the host reads the state once per cycle.
 //
@@ -39,6 +44,8 @@
 namespace gbfem {
 
 constexpr int GM_T = 256;
+constexpr int GM_MMAX = 256;  // largest Krylov dimension (gbfem_solve's check)
+constexpr int GM_SUM_HERE = 128;  // reduction blocks up to which gm_orthogonalize sums the dot partials
 constexpr int SELL_C = 32;
 
 // ---------------------------------------------------------------- SELL-32
@@ -203,6 +210,7 @@ struct GmArgs {
   const float2 *sell_valdw;
   const double *dinv, *b;
   double *x, *V, *tmp, *H, *cs, *sn, *s, *y, *hcol, *partial;
+  double *sc;  // scale of each Krylov vector: V_k = sc_k W_k, W_k stored
   float2 *xdw;  // double-word copy of the current Arnoldi vector (double-word SpMV only)
   GmState *st;
 };
@@ -295,6 +303,7 @@ __global__ void __launch_bounds__(GM_T) gm_logic_restart(GmArgs a) {
   }
   a.s[0] = rn;
   for (int i = 1; i <= S.m; i++) a.s[i] = 0.0;
+  a.sc[0] = 1.0;  // V_0 is stored normalised
   S.beta = rn;
   S.j = 0;
   S.phase = GM_ARNOLDI;
@@ -326,7 +335,8 @@ __global__ void __launch_bounds__(GM_T) gm_arnoldi_spmv(GmArgs a, const VT *__re
     acc = sell_row_dw(sv + o + l, scol + o + l, w, sell_base(r, a.n), a.xdw);
   else
     acc = sell_row(sv + o + l, scol + o + l, w, sell_base(r, a.n), a.V + (size_t)j * a.n);
-  if (r < a.n) a.V[(size_t)(j + 1) * a.n + r] = acc;  // the copy holds D^-1 A
+  // the copy holds D^-1 A; W_j is stored unnormalised: V_j = sc_j W_j
+  if (r < a.n) a.V[(size_t)(j + 1) * a.n + r] = a.sc[j] * acc;
 }
 
 // Gram-Schmidt dot products <V[k], V[j+1]>, k = blockIdx.y <= j
@@ -342,24 +352,54 @@ __global__ void __launch_bounds__(GM_T) gm_dot_partial(GmArgs a, int j) {
   if (threadIdx.x == 0) a.partial[(size_t)k * a.nb + blockIdx.x] = s;
 }
 
-__global__ void __launch_bounds__(GM_T) gm_dot_sum(GmArgs a, int j) {
-  const GmState &S = *a.st;
-  if (S.phase != GM_ARNOLDI || S.j != j) return;
-  const double t = gm_block_total(a.partial + (size_t)blockIdx.x * a.nb, a.nb);
-  if (threadIdx.x == 0) a.hcol[blockIdx.x] = t;
+// h_k = <V_k, w> = sc_k sum_b partial[k][b] by one warp: lane-strided
+// sums, then a shuffle tree (the same order wherever it runs)
+__device__ __forceinline__ double gm_hk(const GmArgs &a, int k) {
+  const int lane = threadIdx.x & 31;
+  double t = 0.0;
+  for (int b = lane; b < a.nb; b += 32) t += a.partial[(size_t)k * a.nb + b];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  return a.sc[k] * t;
 }
 
-// V[j+1] -= V[:, :j+1] hcol, and the block partials of its squared norm
+// the Gram-Schmidt column, one warp per k, for many reduction blocks (summed
+// once instead of in every block of gm_orthogonalize)
+__global__ void __launch_bounds__(32) gm_dot_sum(GmArgs a, int j) {
+  const GmState &S = *a.st;
+  if (S.phase != GM_ARNOLDI || S.j != j) return;
+  const double h = gm_hk(a, blockIdx.x);
+  if (threadIdx.x == 0) a.hcol[blockIdx.x] = h;
+}
+
+// w = W_{j+1} -= sum_k h_k sc_k W_k, the block partials of its squared norm
+// and its double-word copy for the next SpMV.  With at most GM_SUM_HERE
+// reduction blocks every block sums the dot partials itself (block 0 stores
+// the column for the logic kernel), which saves the launch of gm_dot_sum.
 __global__ void __launch_bounds__(GM_T) gm_orthogonalize(GmArgs a, int j) {
   const GmState &S = *a.st;
   if (S.phase != GM_ARNOLDI || S.j != j) return;
+  __shared__ double coef[GM_MMAX + 1];
+  if (a.nb <= GM_SUM_HERE) {
+    for (int k = threadIdx.x >> 5; k <= j; k += GM_T / 32) {
+      const double h = gm_hk(a, k);
+      if ((threadIdx.x & 31) == 0) {
+        coef[k] = h * a.sc[k];
+        if (blockIdx.x == 0) a.hcol[k] = h;
+      }
+    }
+  } else {
+    for (int k = threadIdx.x; k <= j; k += GM_T) coef[k] = a.hcol[k] * a.sc[k];
+  }
+  __syncthreads();
   double *w = a.V + (size_t)(j + 1) * a.n;
   double s = 0.0;
   for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T) {
     double acc = 0.0;
-    for (int k = 0; k <= j; k++) acc = fma(a.hcol[k], __ldg(a.V + (size_t)k * a.n + i), acc);
+    for (int k = 0; k <= j; k++) acc = fma(coef[k], __ldg(a.V + (size_t)k * a.n + i), acc);
     const double wi = w[i] - acc;
     w[i] = wi;
+    if (a.xdw) a.xdw[i] = dw_f2(wi);
     s = fma(wi, wi, s);
   }
   s = gm_block_sum(s);
@@ -397,6 +437,7 @@ __global__ void __launch_bounds__(GM_T) gm_logic_arnoldi(GmArgs a, int j) {
   S.it++;
   S.resid = fabs(a.s[j + 1]);
   S.hn = hn;
+  a.sc[j + 1] = 1.0 / hn;
   const bool conv = S.resid < S.tol_abs || S.resid / S.beta0 < S.tol_rel;
   if (j == m - 1 || S.it >= S.max_iter || conv) {
     const int done = j + 1;
@@ -413,18 +454,6 @@ __global__ void __launch_bounds__(GM_T) gm_logic_arnoldi(GmArgs a, int j) {
   }
 }
 
-__global__ void __launch_bounds__(GM_T) gm_normalize(GmArgs a, int j) {
-  const GmState &S = *a.st;
-  if (S.phase != GM_ARNOLDI || S.j != j + 1) return;
-  double *w = a.V + (size_t)(j + 1) * a.n;
-  const double inv = 1.0 / S.hn;
-  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T) {
-    const double v = w[i] * inv;
-    w[i] = v;
-    if (a.xdw) a.xdw[i] = dw_f2(v);
-  }
-}
-
 // x += V[:, :done] y at the end of a cycle
 __global__ void __launch_bounds__(GM_T) gm_update_x(GmArgs a) {
   const GmState &S = *a.st;
@@ -432,7 +461,7 @@ __global__ void __launch_bounds__(GM_T) gm_update_x(GmArgs a) {
   const int done = S.done_cols;
   for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T) {
     double acc = 0.0;
-    for (int k = 0; k < done; k++) acc = fma(a.y[k], __ldg(a.V + (size_t)k * a.n + i), acc);
+    for (int k = 0; k < done; k++) acc = fma(a.y[k] * a.sc[k], __ldg(a.V + (size_t)k * a.n + i), acc);
     a.x[i] += acc;
   }
 }
@@ -540,11 +569,13 @@ int capture_cycle(gbfem_ctx c, const GmArgs &a, int m, bool dword, int *kernels)
     }
     if (j == 0) cudaEventRecordWithFlags(c->ev3, st, cudaEventRecordExternal);
     gbfem::gm_dot_partial<<<dim3(gv, j + 1), gbfem::GM_T, 0, st>>>(a, j);
-    gbfem::gm_dot_sum<<<j + 1, gbfem::GM_T, 0, st>>>(a, j);
+    if (a.nb > gbfem::GM_SUM_HERE) {
+      gbfem::gm_dot_sum<<<j + 1, 32, 0, st>>>(a, j);
+      k++;
+    }
     gbfem::gm_orthogonalize<<<gv, gbfem::GM_T, 0, st>>>(a, j);
     gbfem::gm_logic_arnoldi<<<1, gbfem::GM_T, 0, st>>>(a, j);
-    gbfem::gm_normalize<<<gv, gbfem::GM_T, 0, st>>>(a, j);
-    k += 6;
+    k += 4;
   }
   gbfem::gm_update_x<<<gv, gbfem::GM_T, 0, st>>>(a);
   k += 1;
@@ -579,12 +610,12 @@ int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int 
   GB_TRY(c->x.alloc(n));
   GB_TRY(c->tmp.alloc(n));
   GB_TRY(c->partial.alloc((size_t)nb * (m + 2)));
-  // H (m+1)^2, cs, sn, s (m+1 each), y (m), hcol (m+1), state
-  const size_t nsmall = (size_t)(m + 1) * (m + 1) + 3 * (size_t)(m + 1) + m + (m + 1) + 16;
+  // H (m+1)^2, cs, sn, s (m+1 each), y (m), hcol (m+1), sc (m+1), state
+  const size_t nsmall = (size_t)(m + 1) * (m + 1) + 3 * (size_t)(m + 1) + m + 2 * (size_t)(m + 1) + 16;
   GB_TRY(c->gm_small.alloc(nsmall));
   double *H = c->gm_small.p, *cs = H + (size_t)(m + 1) * (m + 1), *sn = cs + (m + 1), *s = sn + (m + 1),
-         *y = s + (m + 1), *hcol = y + m;
-  GmState *state = reinterpret_cast<GmState *>(hcol + (m + 1));
+         *y = s + (m + 1), *hcol = y + m, *scv = hcol + (m + 1);
+  GmState *state = reinterpret_cast<GmState *>(scv + (m + 1));
   GmArgs a;
   memset(&a, 0, sizeof(a));  // padding too: the struct is compared bytewise below
   a.n = n;
@@ -609,6 +640,7 @@ int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int 
   a.s = s;
   a.y = y;
   a.hcol = hcol;
+  a.sc = scv;
   a.partial = c->partial.p;
   if (c->std_spmv_dword) {
     GB_TRY(c->gm_xdw.alloc(n));
