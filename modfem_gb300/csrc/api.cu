@@ -40,6 +40,28 @@ static inline int dg_cls(gbfem_ctx c, int e) { return c->dg_p[e] + (el_is_tet(c,
 // the tetrahedron kernels' vertex array (4 per element)
 static inline const int *tet_nodes(gbfem_ctx c) { return c->mixed ? c->el_nodes4.p : c->el_nodes.p; }
 
+// The host copies of a device-built structure (dof of each node, CRS rows
+// and columns, element tables), downloaded once on first use after a build.
+static int fetch_host_structure(gbfem_ctx c) {
+  if (!c->hs_stale) return 0;
+  const int nd = c->ndof;
+  c->hs.dof_of_node.resize(c->nno);
+  c->hs.row_ptr.resize((size_t)nd + 1);
+  c->hs.col_ind.resize((size_t)c->nnz);
+  c->hs.el_table.resize(c->el_table.n);
+  GB_CUDA(cudaMemcpyAsync(c->hs.dof_of_node.data(), c->dof_of_node.p, (size_t)c->nno * sizeof(int),
+                          cudaMemcpyDeviceToHost, c->stream));
+  GB_CUDA(cudaMemcpyAsync(c->hs.row_ptr.data(), c->row_ptr.p, ((size_t)nd + 1) * sizeof(int), cudaMemcpyDeviceToHost,
+                          c->stream));
+  GB_CUDA(cudaMemcpyAsync(c->hs.col_ind.data(), c->col_ind.p, (size_t)c->nnz * sizeof(int), cudaMemcpyDeviceToHost,
+                          c->stream));
+  GB_CUDA(cudaMemcpyAsync(c->hs.el_table.data(), c->el_table.p, c->el_table.n * sizeof(int), cudaMemcpyDeviceToHost,
+                          c->stream));
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  c->hs_stale = false;
+  return 0;
+}
+
 // Block SpMV over all DG block rows, one launch per element class (1..4:
 // prisms of degree 1..4, 5..8: tetrahedra of degree 1..4).
 static int dg_spmv(gbfem_ctx c, int mode, const double *x, const double *b, double *out) {
@@ -384,6 +406,7 @@ int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long 
   GB_CHECK(row_ptr[0] == 0 && row_ptr[ndof] == nnz, "row_ptr inconsistent with nnz");
   c->ndof = ndof;
   c->nnz = nnz;
+  c->hs_stale = false;
   c->hs.ndof = ndof;
   c->hs.row_ptr.assign(row_ptr, row_ptr + ndof + 1);
   c->hs.col_ind.assign(col_ind, col_ind + nnz);
@@ -417,6 +440,7 @@ int gbfem_build_structure(gbfem_ctx c, int *ndof, long long *nnz, int *nr_colors
   GB_CHECK(!c->mixed, "meshes of prisms and tetrahedra together are for the DG path (gbfem_dg_*)");
   GB_TRY(gbfem::build_host_structure(c->nno, c->nel, c->nv, c->h_el_nodes.data(), c->nfa, c->h_fa_el.data(),
                                      c->h_fa_side.data(), c->hs));
+  c->hs_stale = false;
   c->ndof = c->hs.ndof;
   c->nnz = (long long)c->hs.col_ind.size();
   GB_TRY(upload(c, c->row_ptr, c->hs.row_ptr.data(), c->hs.row_ptr.size()));
@@ -450,25 +474,20 @@ int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
                                        &c->h_el_color_ptr));
   c->ndof = nd;
   c->nnz = nz;
-  // host copies for the getters; no colouring (atomic scatter only)
+  // the host copies (for the getters and the drop-in's chunked download) are
+  // fetched when first needed: at 2M prisms the columns and element tables
+  // are 420 MB, most of the build's time if copied every build
   c->hs.ndof = nd;
-  c->hs.dof_of_node.resize(c->nno);
-  c->hs.row_ptr.resize((size_t)nd + 1);
-  c->hs.col_ind.resize((size_t)nz);
-  c->hs.el_table.resize(c->el_table.n);
-  GB_CUDA(cudaMemcpyAsync(c->hs.dof_of_node.data(), c->dof_of_node.p, (size_t)c->nno * sizeof(int),
-                          cudaMemcpyDeviceToHost, c->stream));
-  GB_CUDA(cudaMemcpyAsync(c->hs.row_ptr.data(), c->row_ptr.p, ((size_t)nd + 1) * sizeof(int), cudaMemcpyDeviceToHost,
-                          c->stream));
-  GB_CUDA(cudaMemcpyAsync(c->hs.col_ind.data(), c->col_ind.p, (size_t)nz * sizeof(int), cudaMemcpyDeviceToHost,
-                          c->stream));
-  GB_CUDA(cudaMemcpyAsync(c->hs.el_table.data(), c->el_table.p, c->el_table.n * sizeof(int), cudaMemcpyDeviceToHost,
-                          c->stream));
-  GB_CUDA(cudaStreamSynchronize(c->stream));
+  c->hs.dof_of_node.clear();
+  c->hs.row_ptr.clear();
+  c->hs.col_ind.clear();
+  c->hs.el_table.clear();
+  c->hs_stale = true;
   // boundary faces (few): first-fit colouring on the host over the dofs of
   // their elements, as the host build does
   c->h_fa_color_ptr.clear();
   if (c->nfa > 0) {
+    GB_TRY(fetch_host_structure(c));
     std::vector<int> fa_dofs((size_t)c->nfa * c->nv), perm;
     for (int f = 0; f < c->nfa; f++)
       for (int j = 0; j < c->nv; j++)
@@ -488,6 +507,7 @@ int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
 
 int gbfem_get_crs_structure(gbfem_ctx c, int *dof_of_node, int *row_ptr, int *col_ind) {
   GB_CHECK(c && c->have_structure, "structure not set");
+  GB_TRY(fetch_host_structure(c));
   if (dof_of_node && !c->hs.dof_of_node.empty())
     memcpy(dof_of_node, c->hs.dof_of_node.data(), c->hs.dof_of_node.size() * sizeof(int));
   if (row_ptr) memcpy(row_ptr, c->hs.row_ptr.data(), c->hs.row_ptr.size() * sizeof(int));
@@ -498,6 +518,7 @@ int gbfem_get_crs_structure(gbfem_ctx c, int *dof_of_node, int *row_ptr, int *co
 int gbfem_get_element_tables(gbfem_ctx c, int *tables) {
   GB_CHECK(c && c->have_tables, "structure not built (gbfem_build_structure)");
   GB_CHECK(tables, "null output");
+  GB_TRY(fetch_host_structure(c));
   memcpy(tables, c->hs.el_table.data(), c->hs.el_table.size() * sizeof(int));
   return 0;
 }
@@ -728,6 +749,7 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     if (!same) GB_TRY(build_pipe_plan(c, e0, e1));
   }
   if (pipe) {
+    GB_TRY(fetch_host_structure(c));
     const int K = (int)c->pipe_el.size() - 1;
     const int *rp = c->hs.row_ptr.data();
     // all chunks first: a copy into pageable memory returns only when done

@@ -263,6 +263,9 @@ struct gbfem_ctx_s {
   gbfem::DevBuf<int> el_table, el_perm, fa_perm, fa_map;
   std::vector<int> h_el_color_ptr, h_fa_color_ptr;
   gbfem::HostStructure hs;
+  // the device build leaves the host copies in hs to be fetched on first use
+  // (getters, the drop-in's chunked download), not downloaded every build
+  bool hs_stale = false;
   bool have_structure = false, have_tables = false;
   // matrix
   gbfem::DevBuf<double> val, rhs, dinv;
