@@ -337,17 +337,22 @@ int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int 
   GB_CUDA(cudaGetLastError());
   // 5. colouring (optional)
   if (el_perm && el_color_ptr) {
+    // rounds in batches of SG_JP_BATCH between host reads of the last
+    // round's count of elements left (a round after the last one colours
+    // nothing and returns at once), each round with its own counter
+    constexpr int SG_JP_BATCH = 8;
     DevBuf<int> state, cnt;
-    if (state.alloc(nel) < 0 || cnt.alloc(64 + 1) < 0 || el_perm->alloc(nel) < 0) return fail(-1);
+    if (state.alloc(nel) < 0 || cnt.alloc(64 + SG_JP_BATCH) < 0 || el_perm->alloc(nel) < 0) return fail(-1);
     sg_fill<<<(nel + 255) / 256, 256, 0, st>>>(nel, -1, state.p);
     int remaining = nel, rnd = 0;
     while (remaining > 0) {
-      GB_CUDA(cudaMemsetAsync(cnt.p + 64, 0, sizeof(int), st));
-      sg_jp_round<<<(nel + 255) / 256, 256, 0, st>>>(nel, nv, rnd, el_dofs.p, inc_ptr.p, inc.p, state.p, cnt.p + 64,
-                                                    err);
-      GB_CUDA(cudaMemcpyAsync(&remaining, cnt.p + 64, sizeof(int), cudaMemcpyDeviceToHost, st));
+      GB_CUDA(cudaMemsetAsync(cnt.p + 64, 0, SG_JP_BATCH * sizeof(int), st));
+      for (int b = 0; b < SG_JP_BATCH; b++, rnd++)
+        sg_jp_round<<<(nel + 255) / 256, 256, 0, st>>>(nel, nv, rnd, el_dofs.p, inc_ptr.p, inc.p, state.p,
+                                                      cnt.p + 64 + b, err);
+      GB_CUDA(cudaMemcpyAsync(&remaining, cnt.p + 64 + SG_JP_BATCH - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
       GB_CUDA(cudaStreamSynchronize(st));
-      if (++rnd > (1 << 22)) break;  // cannot happen: every round colours the top-priority element left
+      if (rnd > (1 << 22)) break;  // cannot happen: every round colours the top-priority element left
     }
     GB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaMemsetAsync(cnt.p, 0, 64 * sizeof(int), st));
