@@ -111,6 +111,16 @@ int gbfem_create(gbfem_ctx *ctx, int device) {
     return -1;
   }
   cudaMemset(c->err.p, 0, sizeof(int));
+  {
+    // scratch taken with cudaMallocAsync (the device structure build) stays
+    // in the device's default pool between builds, up to 1 GB, instead of
+    // going back at every synchronisation (a setting of this process only)
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t thr = 1ULL << 30;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  }
   *ctx = c;
   return 0;
 }

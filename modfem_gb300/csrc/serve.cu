@@ -419,6 +419,13 @@ struct gbfem_server_s {
   bool stop = false;
   std::vector<std::thread> workers;
   std::thread engine;
+  // contexts and Krylov spaces of finished requests, freed by the reaper
+  // thread: a cudaFree synchronises the device, which on the engine thread
+  // would hold every lane until all GPU work drained
+  std::deque<std::pair<gbfem_ctx, double *>> reapq;
+  std::condition_variable cv_reap;
+  bool reap_stop = false;
+  std::thread reaper;
   // engine-owned
   SrvLane lanes[2];  // 0: std requests, 1: DG requests
   ReqPtr slots[gbfem::SRV_MAXSLOTS];
@@ -435,6 +442,37 @@ struct gbfem_server_s {
 };
 
 namespace {
+
+// Hands a finished request's context and Krylov space to the reaper (no
+// device work of it may be in flight).
+void reap(gbfem_server s, SrvRequest &r) {
+  double *kry = r.kry.p;
+  r.kry.p = nullptr;  // ownership passes to the reaper
+  r.kry.n = 0;
+  gbfem_ctx c = r.ctx;
+  r.ctx = nullptr;
+  if (!c && !kry) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->reapq.emplace_back(c, kry);
+  }
+  s->cv_reap.notify_one();
+}
+
+void reaper_loop(gbfem_server s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    s->cv_reap.wait(lk, [&] { return s->reap_stop || !s->reapq.empty(); });
+    if (s->reapq.empty()) return;  // stop, and nothing left
+    const auto item = s->reapq.front();
+    s->reapq.pop_front();
+    lk.unlock();
+    if (item.first) gbfem_destroy(item.first);
+    if (item.second) cudaFree(item.second);
+    lk.lock();
+  }
+}
 
 // A lane may hold half of max_active requests, or more while the other lane
 // has nobody waiting; the HBM budget is shared.
@@ -569,9 +607,9 @@ void prep_worker(gbfem_server s) {
     if (rc < 0 || r->cancel) {
       r->status = rc < 0 ? -1 : -2;
       r->err = rc < 0 ? gbfem_last_error() : "cancelled";
-      if (r->ctx) gbfem_destroy(r->ctx);
-      r->ctx = nullptr;
-      r->kry.release();
+      lk.unlock();
+      reap(s, *r);
+      lk.lock();
       s->in_use -= r->charged;
       r->charged = 0;
       r->t_done = now_s();
@@ -592,9 +630,8 @@ void prep_worker(gbfem_server s) {
       double res = 0.0, rel = 0.0;
       const int it = gbfem::gmres_device_std(r->ctx, r->krylov, r->max_iter, r->tol, 1, r->x.data(), &res, &rel);
       const std::string err = it < 0 ? std::string(gbfem_last_error()) : std::string();
-      gbfem_destroy(r->ctx);
+      reap(s, *r);
       lk.lock();
-      r->ctx = nullptr;
       r->iters = it < 0 ? 0 : it;
       r->rel = rel;
       s->in_use -= r->charged;
@@ -790,9 +827,7 @@ void retire(gbfem_server s, SrvLane &ln, int i, bool cancelled = false) {
     r->iters = S.it;
     r->rel = S.beta0 > 0 ? S.resid / S.beta0 : 0.0;
   }
-  gbfem_destroy(r->ctx);
-  r->ctx = nullptr;
-  r->kry.release();
+  reap(s, *r);
   s->slots[i].reset();
   std::lock_guard<std::mutex> lk(s->mu);
   s->in_use -= r->charged;
@@ -958,6 +993,7 @@ int gbfem_server_create(gbfem_server *out, int device, long long hbm_budget, int
   cudaMemset(s->d_state.p, 0, sizeof(SrvState) * gbfem::SRV_MAXSLOTS);
   for (int i = 0; i < prep_threads; i++) s->workers.emplace_back(prep_worker, s);
   s->engine = std::thread(engine_loop, s);
+  s->reaper = std::thread(reaper_loop, s);
   *out = s;
   return 0;
 }
@@ -974,6 +1010,12 @@ int gbfem_server_destroy(gbfem_server s) {
   for (auto &t : s->workers) t.join();
   // the engine finishes the requests it holds, then returns
   if (s->engine.joinable()) s->engine.join();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->reap_stop = true;
+  }
+  s->cv_reap.notify_all();
+  if (s->reaper.joinable()) s->reaper.join();  // after freeing what was queued
   cudaSetDevice(s->device);
   for (auto &kv : s->reqs) {
     if (kv.second->ctx) gbfem_destroy(kv.second->ctx);

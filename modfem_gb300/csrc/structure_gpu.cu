@@ -104,8 +104,40 @@ __global__ void sg_chunk_scan(long long n, const int *__restrict__ in, const int
   }
 }
 
+// Scratch of one build, allocated and freed in the build stream's order
+// (cudaMallocAsync / cudaFreeAsync, used on that stream only): unlike
+// cudaFree, nothing here synchronises the device, so a build running beside
+// other streams (the serving engine's) does not wait for their work.
+template <typename T>
+struct SgTemp {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaStream_t st = nullptr;
+  explicit SgTemp(cudaStream_t s) : st(s) {}
+  SgTemp(const SgTemp &) = delete;
+  SgTemp &operator=(const SgTemp &) = delete;
+  ~SgTemp() { release(); }
+  int alloc(size_t count) {
+    if (count <= n && p) return 0;
+    release();
+    if (count == 0) return 0;
+    if (cudaMallocAsync(reinterpret_cast<void **>(&p), count * sizeof(T), st) != cudaSuccess) {
+      p = nullptr;
+      set_error("cudaMallocAsync failed for " + std::to_string(count * sizeof(T)) + " bytes");
+      return -1;
+    }
+    n = count;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, st);
+    p = nullptr;
+    n = 0;
+  }
+};
+
 // out[i] = sum_{k < i} in[k] for i <= n (out has n + 1 entries); total in out[n]
-static int sg_scan(cudaStream_t st, long long n, const int *in, int *out, DevBuf<int> &tmp) {
+static int sg_scan(cudaStream_t st, long long n, const int *in, int *out, SgTemp<int> &tmp) {
   const int nb = (int)((n + SG_CHUNK - 1) / SG_CHUNK);
   GB_CHECK(nb <= SG_T * 4096, "scan too long");
   if (tmp.alloc((size_t)nb + 1) < 0) return -1;
@@ -290,7 +322,7 @@ int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int 
                            int *ndof_out, long long *nnz_out, DevBuf<int> *el_perm,
                            std::vector<int> *el_color_ptr) {
   const long long m = (long long)nel * nv;
-  DevBuf<int> first, mark, rank, el_dofs, inc_cnt, inc_ptr, inc, len, tmp;
+  SgTemp<int> first(st), mark(st), rank(st), el_dofs(st), inc_cnt(st), inc_ptr(st), inc(st), len(st), tmp(st);
   auto cleanup = [&]() {
     first.release(); mark.release(); rank.release(); el_dofs.release(); inc_cnt.release();
     inc_ptr.release(); inc.release(); len.release(); tmp.release();
@@ -341,7 +373,7 @@ int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int 
     // round's count of elements left (a round after the last one colours
     // nothing and returns at once), each round with its own counter
     constexpr int SG_JP_BATCH = 8;
-    DevBuf<int> state, cnt;
+    SgTemp<int> state(st), cnt(st);
     if (state.alloc(nel) < 0 || cnt.alloc(64 + SG_JP_BATCH) < 0 || el_perm->alloc(nel) < 0) return fail(-1);
     sg_fill<<<(nel + 255) / 256, 256, 0, st>>>(nel, -1, state.p);
     int remaining = nel, rnd = 0;
