@@ -144,6 +144,8 @@ int gbfem_destroy(gbfem_ctx c) {
   c->sell_valdw.release();
   c->gm_xdw.release();
   c->gm_small.release();
+  c->gm_npart.release();
+  c->gm_cnt.release();
   if (c->side_stream) {
     cudaStreamSynchronize(c->side_stream);
     cudaStreamDestroy(c->side_stream);

@@ -298,7 +298,8 @@ struct gbfem_ctx_s {
   // device-resident std GMRES (gmres_dev.cu): sliced-ELL copy of the CRS
   // matrix, small arrays and state, the captured restart cycle
   gbfem::DevBuf<int> sell_off, sell_col;
-  gbfem::DevBuf<double> sell_val, gm_small;
+  gbfem::DevBuf<double> sell_val, gm_small, gm_npart;
+  gbfem::DevBuf<unsigned> gm_cnt;
   gbfem::DevBuf<float2> sell_valdw, gm_xdw;
   gbfem::DevBuf<short> sell_col16;  // columns relative to the row, where they fit in 16 bits
   bool sell_ready = false, std_spmv_dword = false, sell_cols16 = false;

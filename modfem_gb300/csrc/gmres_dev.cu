@@ -11,11 +11,13 @@
 // one-block "logic" kernels on the device, and every kernel of a restart
 // cycle (restart residual, m Arnoldi steps, update of x) reads a state word
 // and returns at once when the cycle has already ended.  An Arnoldi step is
-// four kernels: the SpMV, the Gram-Schmidt dot partials, the
-// orthogonalisation (each block sums the dot partials itself; beyond 128
-// blocks a kernel of one warp per column sums them once) and the logic;
-// Krylov vectors after the first are stored unnormalised with a scale each
-// (V_k = sc_k W_k), applied by their readers, so no normalisation pass runs.  One cycle is
+// three kernels: the SpMV, the Gram-Schmidt dot products (the last block of
+// each column entry to finish sums its block partials) and the
+// orthogonalisation, one row a thread (its last block to finish runs the
+// step's logic); Krylov vectors after the first are stored unnormalised with
+// a scale each (V_k = sc_k W_k), applied by their readers, so no
+// normalisation pass runs; the cycle's triangular solve runs in the update of
+// x.  "Last block" is an atomic count after a memory fence: nothing waits.  One cycle is
 // captured as a CUDA graph (per context, matrix size and Krylov dimension)
 // and replayed; the host reads the state once per cycle.
 //
@@ -34,6 +36,7 @@
 // Row sums run in column order in one thread, as the reference's loop does.  Reductions are two-stage over a fixed block
 // partition and fixed tree order: the solve is bit-reproducible.
 
+#include <algorithm>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -45,7 +48,7 @@ namespace gbfem {
 
 constexpr int GM_T = 256;
 constexpr int GM_MMAX = 256;  // largest Krylov dimension (gbfem_solve's check)
-constexpr int GM_SUM_HERE = 128;  // reduction blocks up to which gm_orthogonalize sums the dot partials
+constexpr int GM_RSTAGE = 64;  // Krylov dimensions up to which the triangular solve runs on a shared copy of R
 constexpr int SELL_C = 32;
 
 // ---------------------------------------------------------------- SELL-32
@@ -213,6 +216,9 @@ struct GmArgs {
   double *sc;  // scale of each Krylov vector: V_k = sc_k W_k, W_k stored
   float2 *xdw;  // double-word copy of the current Arnoldi vector (double-word SpMV only)
   GmState *st;
+  int ng;          // blocks of the row-parallel kernels
+  double *npart;   // [ng] their norm partials
+  unsigned *cnt;   // [m + 2] finished-block counts (dot products 0..m-1, orthogonalisation m + 1)
 };
 
 // sum of nb partials in a fixed order (one block of GM_T threads); valid in thread 0
@@ -339,58 +345,108 @@ __global__ void __launch_bounds__(GM_T) gm_arnoldi_spmv(GmArgs a, const VT *__re
   if (r < a.n) a.V[(size_t)(j + 1) * a.n + r] = a.sc[j] * acc;
 }
 
-// Gram-Schmidt dot products <V[k], V[j+1]>, k = blockIdx.y <= j
+// Gram-Schmidt dot products <W_k, w>, k = blockIdx.y <= j (w = W_{j+1}),
+// block partials; the last block of each
+// k to finish (an atomic count after a fence, no waiting) sums the partials
+// in block order (one warp, lane-strided then a shuffle tree) and stores the
+// column entry h_k = <V_k, w> = sc_k total.  Partials of other blocks are
+// read through L2 (__ldcg).
 __global__ void __launch_bounds__(GM_T) gm_dot_partial(GmArgs a, int j) {
   const GmState &S = *a.st;
   if (S.phase != GM_ARNOLDI || S.j != j) return;
+  __shared__ bool last;
   const int k = blockIdx.y;
   const double *v = a.V + (size_t)k * a.n, *w = a.V + (size_t)(j + 1) * a.n;
-  double s = 0.0;
+  double s0 = 0.0;
   for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T)
-    s = fma(__ldg(v + i), __ldg(w + i), s);
-  s = gm_block_sum(s);
-  if (threadIdx.x == 0) a.partial[(size_t)k * a.nb + blockIdx.x] = s;
-}
-
-// h_k = <V_k, w> = sc_k sum_b partial[k][b] by one warp: lane-strided
-// sums, then a shuffle tree (the same order wherever it runs)
-__device__ __forceinline__ double gm_hk(const GmArgs &a, int k) {
-  const int lane = threadIdx.x & 31;
+    s0 = fma(__ldg(v + i), __ldg(w + i), s0);
+  const double s = gm_block_sum(s0);
+  if (threadIdx.x == 0) {
+    a.partial[(size_t)k * a.nb + blockIdx.x] = s;
+    __threadfence();
+    last = atomicAdd(a.cnt + k, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x >= 32) return;
+  __threadfence();
   double t = 0.0;
-  for (int b = lane; b < a.nb; b += 32) t += a.partial[(size_t)k * a.nb + b];
+  for (int b = threadIdx.x; b < a.nb; b += 32) t += __ldcg(a.partial + (size_t)k * a.nb + b);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-  return a.sc[k] * t;
+  if (threadIdx.x == 0) {
+    a.hcol[k] = a.sc[k] * t;
+    a.cnt[k] = 0;  // for the next step
+  }
 }
 
-// the Gram-Schmidt column, one warp per k, for many reduction blocks (summed
-// once instead of in every block of gm_orthogonalize)
-__global__ void __launch_bounds__(32) gm_dot_sum(GmArgs a, int j) {
-  const GmState &S = *a.st;
-  if (S.phase != GM_ARNOLDI || S.j != j) return;
-  const double h = gm_hk(a, blockIdx.x);
-  if (threadIdx.x == 0) a.hcol[blockIdx.x] = h;
+// The step's logic, by the last block of gm_orthogonalize: |w| from the
+// norm partials, the Hessenberg column j with the earlier rotations applied
+// (column and rotations staged in shared memory: thread 0's chain of
+// dependent operations then waits on no global memory), the new rotation,
+// the residual estimate and the decision (next step, or end of the cycle).
+__device__ void gm_step_logic(const GmArgs &a, int j, GmState &S) {
+  __shared__ double col[GM_MMAX + 2], rc[GM_MMAX + 1], rs[GM_MMAX + 1];
+  const int tid = threadIdx.x;
+  double v = 0.0;
+  for (int b = tid; b < a.ng; b += GM_T) v += __ldcg(a.npart + b);
+  __shared__ double sh[GM_T];
+  sh[tid] = v;
+  for (int k = tid; k <= j; k += GM_T) col[k] = __ldcg(a.hcol + k);
+  for (int k = tid; k < j; k += GM_T) {
+    rc[k] = a.cs[k];
+    rs[k] = a.sn[k];
+  }
+  __syncthreads();
+  for (int o = GM_T / 2; o > 0; o >>= 1) {
+    if (tid < o) sh[tid] += sh[tid + o];
+    __syncthreads();
+  }
+  if (tid != 0) return;
+  const int m = S.m, ld = m + 1;
+  const double hn = sqrt(sh[0]);
+  col[j + 1] = hn;
+  for (int k = 0; k < j; k++) {
+    const double x0 = col[k], x1 = col[k + 1];
+    col[k] = rc[k] * x0 + rs[k] * x1;
+    col[k + 1] = rc[k] * x1 - rs[k] * x0;
+  }
+  const double x0 = col[j], x1 = col[j + 1];
+  const double rr = hypot(x0, x1), cj = x0 / rr, sj = x1 / rr;
+  col[j] = rr;
+  col[j + 1] = 0.0;
+  double *H = a.H + (size_t)j * ld;
+  for (int k = 0; k <= j + 1; k++) H[k] = col[k];
+  a.cs[j] = cj;
+  a.sn[j] = sj;
+  const double s0 = a.s[j];
+  a.s[j] = cj * s0;
+  const double s1 = -sj * s0;
+  a.s[j + 1] = s1;
+  const int it = S.it + 1;
+  const double resid = fabs(s1);
+  S.it = it;
+  S.resid = resid;
+  S.hn = hn;
+  a.sc[j + 1] = 1.0 / hn;
+  const bool conv = resid < S.tol_abs || resid / S.beta0 < S.tol_rel;
+  if (j == m - 1 || it >= S.max_iter || conv) {
+    S.done_cols = j + 1;  // the triangular solve runs in gm_update_x
+    S.final_flag = (conv || it >= S.max_iter) ? 1 : 0;
+    S.phase = GM_RESTART;
+  } else {
+    S.j = j + 1;
+  }
 }
 
-// w = W_{j+1} -= sum_k h_k sc_k W_k, the block partials of its squared norm
-// and its double-word copy for the next SpMV.  With at most GM_SUM_HERE
-// reduction blocks every block sums the dot partials itself (block 0 stores
-// the column for the logic kernel), which saves the launch of gm_dot_sum.
+// w = W_{j+1} -= sum_k h_k sc_k W_k (one row a thread), the block partials
+// of its squared norm and its double-word copy for the next SpMV; the last
+// block to finish then runs the step's logic.
 __global__ void __launch_bounds__(GM_T) gm_orthogonalize(GmArgs a, int j) {
-  const GmState &S = *a.st;
+  GmState &S = *a.st;
   if (S.phase != GM_ARNOLDI || S.j != j) return;
   __shared__ double coef[GM_MMAX + 1];
-  if (a.nb <= GM_SUM_HERE) {
-    for (int k = threadIdx.x >> 5; k <= j; k += GM_T / 32) {
-      const double h = gm_hk(a, k);
-      if ((threadIdx.x & 31) == 0) {
-        coef[k] = h * a.sc[k];
-        if (blockIdx.x == 0) a.hcol[k] = h;
-      }
-    }
-  } else {
-    for (int k = threadIdx.x; k <= j; k += GM_T) coef[k] = a.hcol[k] * a.sc[k];
-  }
+  __shared__ bool last;
+  for (int k = threadIdx.x; k <= j; k += GM_T) coef[k] = a.hcol[k] * a.sc[k];
   __syncthreads();
   double *w = a.V + (size_t)(j + 1) * a.n;
   double s = 0.0;
@@ -403,65 +459,46 @@ __global__ void __launch_bounds__(GM_T) gm_orthogonalize(GmArgs a, int j) {
     s = fma(wi, wi, s);
   }
   s = gm_block_sum(s);
-  if (threadIdx.x == 0) a.partial[(size_t)(j + 1) * a.nb + blockIdx.x] = s;
+  if (threadIdx.x == 0) {
+    a.npart[blockIdx.x] = s;
+    __threadfence();
+    last = atomicAdd(a.cnt + S.m + 1, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x == 0) a.cnt[S.m + 1] = 0;  // for the next step
+  gm_step_logic(a, j, S);
 }
 
-// Hessenberg column j, Givens rotations, residual estimate; at the end of a
-// cycle the triangular solve for y
-__global__ void __launch_bounds__(GM_T) gm_logic_arnoldi(GmArgs a, int j) {
-  GmState &S = *a.st;
-  if (S.phase != GM_ARNOLDI || S.j != j) return;
-  const double tot = gm_block_total(a.partial + (size_t)(j + 1) * a.nb, a.nb);
-  if (threadIdx.x != 0) return;
-  const int m = S.m, ld = m + 1;
-  const double hn = sqrt(tot);
-  double *H = a.H;
-  for (int k = 0; k <= j; k++) H[k + (size_t)j * ld] = a.hcol[k];
-  H[j + 1 + (size_t)j * ld] = hn;
-  for (int k = 0; k < j; k++) {
-    const double x0 = H[k + (size_t)j * ld], x1 = H[k + 1 + (size_t)j * ld];
-    H[k + (size_t)j * ld] = a.cs[k] * x0 + a.sn[k] * x1;
-    H[k + 1 + (size_t)j * ld] = a.cs[k] * x1 - a.sn[k] * x0;
-  }
-  {
-    const double x0 = H[j + (size_t)j * ld], x1 = H[j + 1 + (size_t)j * ld];
-    const double rr = hypot(x0, x1);
-    a.cs[j] = x0 / rr;
-    a.sn[j] = x1 / rr;
-    H[j + (size_t)j * ld] = rr;
-    H[j + 1 + (size_t)j * ld] = 0.0;
-    const double s0 = a.s[j];
-    a.s[j] = a.cs[j] * s0;
-    a.s[j + 1] = -a.sn[j] * s0;
-  }
-  S.it++;
-  S.resid = fabs(a.s[j + 1]);
-  S.hn = hn;
-  a.sc[j + 1] = 1.0 / hn;
-  const bool conv = S.resid < S.tol_abs || S.resid / S.beta0 < S.tol_rel;
-  if (j == m - 1 || S.it >= S.max_iter || conv) {
-    const int done = j + 1;
-    for (int k = done - 1; k >= 0; k--) {
-      double v = a.s[k];
-      for (int i = k + 1; i < done; i++) v -= H[k + (size_t)i * ld] * a.y[i];
-      a.y[k] = v / H[k + (size_t)k * ld];
-    }
-    S.done_cols = done;
-    S.final_flag = (conv || S.it >= S.max_iter) ? 1 : 0;
-    S.phase = GM_RESTART;
-  } else {
-    S.j = j + 1;
-  }
-}
-
-// x += V[:, :done] y at the end of a cycle
+// At the end of a cycle: y from the triangular system R y = s (every block
+// solves it, the same arithmetic in each: thread 0 on a shared-memory copy
+// of R when the Krylov dimension is at most GM_RSTAGE, else on R in global
+// memory), then x += sum_k y_k V_k, one row a thread.
 __global__ void __launch_bounds__(GM_T) gm_update_x(GmArgs a) {
   const GmState &S = *a.st;
   if (S.phase != GM_RESTART || S.done_cols == 0) return;
-  const int done = S.done_cols;
-  for (long long i = (long long)blockIdx.x * GM_T + threadIdx.x; i < a.n; i += (long long)gridDim.x * GM_T) {
+  __shared__ double R[GM_RSTAGE * GM_RSTAGE], yc[GM_MMAX + 1];
+  const int done = S.done_cols, ld = S.m + 1, tid = threadIdx.x;
+  const bool staged = done <= GM_RSTAGE;
+  if (staged)
+    for (int t = tid; t < done * done; t += GM_T) R[t] = a.H[(size_t)(t / done) * ld + t % done];  // column t / done
+  __syncthreads();
+  if (tid == 0) {
+    for (int k = done - 1; k >= 0; k--) {
+      double v = a.s[k];
+      if (staged)
+        for (int i = k + 1; i < done; i++) v -= R[i * done + k] * yc[i];
+      else
+        for (int i = k + 1; i < done; i++) v -= a.H[k + (size_t)i * ld] * yc[i];
+      yc[k] = v / (staged ? R[k * done + k] : a.H[k + (size_t)k * ld]);
+    }
+    for (int k = 0; k < done; k++) yc[k] *= a.sc[k];  // to the stored W_k
+  }
+  __syncthreads();
+  for (long long i = (long long)blockIdx.x * GM_T + tid; i < a.n; i += (long long)gridDim.x * GM_T) {
     double acc = 0.0;
-    for (int k = 0; k < done; k++) acc = fma(a.y[k] * a.sc[k], __ldg(a.V + (size_t)k * a.n + i), acc);
+    for (int k = 0; k < done; k++) acc = fma(yc[k], __ldg(a.V + (size_t)k * a.n + i), acc);
     a.x[i] += acc;
   }
 }
@@ -569,15 +606,10 @@ int capture_cycle(gbfem_ctx c, const GmArgs &a, int m, bool dword, int *kernels)
     }
     if (j == 0) cudaEventRecordWithFlags(c->ev3, st, cudaEventRecordExternal);
     gbfem::gm_dot_partial<<<dim3(gv, j + 1), gbfem::GM_T, 0, st>>>(a, j);
-    if (a.nb > gbfem::GM_SUM_HERE) {
-      gbfem::gm_dot_sum<<<j + 1, 32, 0, st>>>(a, j);
-      k++;
-    }
-    gbfem::gm_orthogonalize<<<gv, gbfem::GM_T, 0, st>>>(a, j);
-    gbfem::gm_logic_arnoldi<<<1, gbfem::GM_T, 0, st>>>(a, j);
-    k += 4;
+    gbfem::gm_orthogonalize<<<(unsigned)a.ng, gbfem::GM_T, 0, st>>>(a, j);
+    k += 3;
   }
-  gbfem::gm_update_x<<<gv, gbfem::GM_T, 0, st>>>(a);
+  gbfem::gm_update_x<<<(unsigned)a.ng, gbfem::GM_T, 0, st>>>(a);
   k += 1;
   const cudaError_t e1 = cudaGetLastError();
   const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
@@ -610,6 +642,13 @@ int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int 
   GB_TRY(c->x.alloc(n));
   GB_TRY(c->tmp.alloc(n));
   GB_TRY(c->partial.alloc((size_t)nb * (m + 2)));
+  // row-parallel grid: one row a thread up to 8 blocks per SM (1,216 on
+  // GB300), beyond that a grid-stride loop (every block counts itself into
+  // one atomic word at the end of the step)
+  const int ng = (int)std::min<unsigned>(nblk(n, GM_T), 1216u);
+  GB_TRY(c->gm_npart.alloc((size_t)ng));
+  GB_TRY(c->gm_cnt.alloc((size_t)m + 2));
+  GB_CUDA(cudaMemsetAsync(c->gm_cnt.p, 0, ((size_t)m + 2) * sizeof(unsigned), st));
   // H (m+1)^2, cs, sn, s (m+1 each), y (m), hcol (m+1), sc (m+1), state
   const size_t nsmall = (size_t)(m + 1) * (m + 1) + 3 * (size_t)(m + 1) + m + 2 * (size_t)(m + 1) + 16;
   GB_TRY(c->gm_small.alloc(nsmall));
@@ -642,6 +681,9 @@ int gmres_device_std(gbfem_ctx c, int krylov, int max_iter, double tol_rel, int 
   a.hcol = hcol;
   a.sc = scv;
   a.partial = c->partial.p;
+  a.ng = ng;
+  a.npart = c->gm_npart.p;
+  a.cnt = c->gm_cnt.p;
   if (c->std_spmv_dword) {
     GB_TRY(c->gm_xdw.alloc(n));
     a.xdw = c->gm_xdw.p;
