@@ -48,14 +48,16 @@ static int fetch_host_structure(gbfem_ctx c) {
   c->hs.dof_of_node.resize(c->nno);
   c->hs.row_ptr.resize((size_t)nd + 1);
   c->hs.col_ind.resize((size_t)c->nnz);
-  c->hs.el_table.resize(c->el_table.n);
+  // sized by the current structure, never by a buffer's grown capacity
+  const size_t ntab = (size_t)c->nel * (c->nv * c->nv + c->nv);
+  c->hs.el_table.resize(ntab);
   GB_CUDA(cudaMemcpyAsync(c->hs.dof_of_node.data(), c->dof_of_node.p, (size_t)c->nno * sizeof(int),
                           cudaMemcpyDeviceToHost, c->stream));
   GB_CUDA(cudaMemcpyAsync(c->hs.row_ptr.data(), c->row_ptr.p, ((size_t)nd + 1) * sizeof(int), cudaMemcpyDeviceToHost,
                           c->stream));
   GB_CUDA(cudaMemcpyAsync(c->hs.col_ind.data(), c->col_ind.p, (size_t)c->nnz * sizeof(int), cudaMemcpyDeviceToHost,
                           c->stream));
-  GB_CUDA(cudaMemcpyAsync(c->hs.el_table.data(), c->el_table.p, c->el_table.n * sizeof(int), cudaMemcpyDeviceToHost,
+  GB_CUDA(cudaMemcpyAsync(c->hs.el_table.data(), c->el_table.p, ntab * sizeof(int), cudaMemcpyDeviceToHost,
                           c->stream));
   GB_CUDA(cudaStreamSynchronize(c->stream));
   c->hs_stale = false;

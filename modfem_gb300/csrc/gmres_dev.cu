@@ -7,19 +7,19 @@
 // both tolerances floored at 1e-12 (lss_mkb_core.c:2377-2378).
 //
 // Nothing of an Arnoldi step goes through the host: the Hessenberg column,
-// the rotations, the convergence test and the small triangular solve run in
-// one-block "logic" kernels on the device, and every kernel of a restart
-// cycle (restart residual, m Arnoldi steps, update of x) reads a state word
-// and returns at once when the cycle has already ended.  An Arnoldi step is
-// three kernels: the SpMV, the Gram-Schmidt dot products (the last block of
-// each column entry to finish sums its block partials) and the
-// orthogonalisation, one row a thread (its last block to finish runs the
-// step's logic); Krylov vectors after the first are stored unnormalised with
-// a scale each (V_k = sc_k W_k), applied by their readers, so no
-// normalisation pass runs; the cycle's triangular solve runs in the update of
-// x.  "Last block" is an atomic count after a memory fence: nothing waits.  One cycle is
-// captured as a CUDA graph (per context, matrix size and Krylov dimension)
-// and replayed; the host reads the state once per cycle.
+// the rotations, the convergence test and the small triangular solve run on
+// the device, and every kernel of a restart cycle (restart residual, m
+// Arnoldi steps, update of x) reads a state word and returns at once when the
+// cycle has already ended.  An Arnoldi step is three kernels: the SpMV, the
+// Gram-Schmidt dot products (the last block of each column entry to finish
+// sums its block partials) and the orthogonalisation, one row a thread (its
+// last block to finish runs the step's logic: norm, Givens rotations, test).
+// Krylov vectors after the first are stored unnormalised with a scale each
+// (V_k = sc_k W_k), applied by their readers, so no normalisation pass runs;
+// the cycle's triangular solve runs in the update of x.  "Last block" is an
+// atomic count after a memory fence: nothing waits.  One cycle is captured
+// as a CUDA graph (per context, matrix size and Krylov dimension) and
+// replayed; the host reads the state once per cycle.
 //
 // The SpMV runs on a sliced-ELL copy of the CRS matrix (SELL-32 in natural
 // row order: slice s = rows 32 s .. 32 s + 31, padded to the slice's longest
@@ -33,8 +33,9 @@
 // (GB300's FP64 pipe, ~0.6 T FMA/s, is itself near the HBM rate for one FMA
 // per 12 bytes).  The copy holds the rows of D^-1 A (the point-Jacobi
 // scaling folded in once per solve), so the product reads no preconditioner.
-// Row sums run in column order in one thread, as the reference's loop does.  Reductions are two-stage over a fixed block
-// partition and fixed tree order: the solve is bit-reproducible.
+// Row sums run in column order in one thread, as the reference's loop does.
+// Reductions are two-stage over a fixed block partition and fixed tree
+// order: the solve is bit-reproducible.
 
 #include <algorithm>
 #include <cstring>

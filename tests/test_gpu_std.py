@@ -5,6 +5,8 @@ golden fixtures made by the reference ModFEM compiled in-tree
 (tests/golden/make_golden.py) and, for sizes without fixtures, the C oracle
 pinned by tests/test_oracle.py.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -790,3 +792,29 @@ def test_device_structure_vs_host_larger(gb, kind):
     rp, ci = d[1], d[2]
     assert crs_rel_err(rp, v1, vh, energy_scale(rp, ci, vh)) < REL_TOL
     assert vec_rel_err(r1, rh) < REL_TOL
+
+
+def test_device_structure_smaller_in_a_live_context(gb):
+    """Device builds of a large mesh, then of a smaller one, in the same
+    context: the host copies of the structure are sized by the current
+    structure, not by the device buffers' grown capacity (the element tables
+    land in an exactly-sized view of a guarded buffer, guards untouched), and
+    equal a fresh context's."""
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    big, small = structured_prism_mesh(10, jitter=0.2, seed=5), structured_prism_mesh(4, jitter=0.2, seed=6)
+    c = gb.Context(0)
+    for m in (big, small):
+        c.set_mesh(m)
+        c.set_coefficients(k=lognormal_k(m.nel, seed=7), f=1.0, g=0.0, penalty=1e7)
+        c.build_structure_device()
+    ref = make_ctx(gb, small, lognormal_k(small.nel, seed=7))
+    ref.build_structure_device()
+    n = small.nel * (6 * 6 + 6)
+    buf = np.full(n + 64, -7, np.int32)
+    c._check(c.L.gbfem_get_element_tables(c._h, ctypes.c_void_p(buf[:n].ctypes.data)))
+    assert np.all(buf[n:] == -7)
+    assert np.array_equal(buf[:n], ref.get_element_tables())
+    for a, b in zip(c.get_crs_structure(), ref.get_crs_structure()):
+        assert np.array_equal(a, b)
+    c.close()
+    ref.close()
