@@ -142,6 +142,24 @@ int gbfem_set_node_coords(gbfem_ctx ctx, const double *node_xyz);
 int gbfem_set_coefficients(gbfem_ctx ctx, const double *k_el, const double *D_el, double f,
                            double g, double penalty);
 
+/* Constrained (hanging) vertices of a refined std prism mesh, replacing
+ * apr_get_constr_data (apd_std_lin/aps_std_util.c:358-395) for the
+ * assembly: vertex[k] (0-based) carries no dof and stands for its
+ * nr_constr[k] = 2 (mid-edge) or 4 (mid-face) constraining vertices
+ * constr_id[4k..4k+nr_constr[k]-1] (the order of apr_get_constr_data),
+ * each with coefficient 1/2 or 1/4.  An element with such a vertex has the
+ * expanded dof list of apr_get_stiff_mat_data (aps_std_lin_intf.c:2978-
+ * 3035; a constrained vertex replaced in place by its constraining vertices)
+ * and gbfem_create_assemble_stiff_mat rewrites its element and boundary-face
+ * matrices as that function does (:3077-3160) before the table-driven
+ * scatter; its table block then holds n x n + n entries, n the expanded
+ * length.  Constraining vertices are themselves unconstrained (1-irregular
+ * meshes).  Call after gbfem_set_mesh (which clears them) and before
+ * gbfem_set_crs_structure; n = 0 clears.  The library's own structure
+ * builds and gbfem_assemble refuse a mesh with constraints: ModFEM's
+ * sir_create supplies the structure and tables. */
+int gbfem_set_constraints(gbfem_ctx ctx, int n, const int *vertex, const int *nr_constr, const int *constr_id);
+
 /* CRS structure as sir_create leaves it (sid_mkb/sis_mkb_intf.c:396-1690,
  * lad_crs/las_crs_intf.c:72-300): dof index of each node (-1 if none), row
  * pointers and ascending column indices with the diagonal included. */

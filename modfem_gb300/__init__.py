@@ -43,6 +43,7 @@ SIGNATURES = [
     ("gbfem_set_mesh_mixed", _ci, [_vp, _ci, _vp, _ci, _vp, _vp]),
     ("gbfem_set_node_coords", _ci, [_vp, _vp]),
     ("gbfem_set_coefficients", _ci, [_vp, _vp, _vp, _cd, _cd, _cd]),
+    ("gbfem_set_constraints", _ci, [_vp, _ci, _vp, _vp, _vp]),
     ("gbfem_set_crs_structure", _ci, [_vp, _ci, _vp, _cll, _vp, _vp]),
     ("gbfem_build_structure", _ci, [_vp, _pi, _pll, _pi]),
     ("gbfem_build_structure_device", _ci, [_vp, _pi, _pll]),
@@ -211,6 +212,13 @@ class Context:
         D = _f64(D)
         self._keep["k"], self._keep["D"] = k, D
         self._check(self.L.gbfem_set_coefficients(self._h, _p(k), _p(D), f, g, penalty))
+
+    def set_constraints(self, vertex, nr_constr, constr_id):
+        """gbfem_set_constraints: constrained (hanging) vertices with their 2
+        or 4 constraining vertices (constr_id: 4 per vertex, -1 padded)."""
+        v, n = _i32(vertex), _i32(nr_constr)
+        p = _i32(np.asarray(constr_id).reshape(-1, 4)) if len(v) else np.zeros((0, 4), np.int32)
+        self._check(self.L.gbfem_set_constraints(self._h, v.size, _p(v), _p(n), _p(p)))
 
     def set_crs_structure(self, dof_of_node, row_ptr, col_ind):
         dn, rp, ci = _i32(dof_of_node), _i32(row_ptr), _i32(col_ind)

@@ -259,6 +259,15 @@ int gbfem_set_option(gbfem_ctx c, int option, long long value) {
   return -2;
 }
 
+static void clear_constraints(gbfem_ctx c) {
+  c->ncon = 0;
+  c->con_gen++;
+  c->h_con_node.clear();
+  c->h_con_par.clear();
+  c->h_el_con.clear();
+  c->con_split_key[0] = c->con_split_key[1] = nullptr;
+}
+
 int gbfem_set_mesh(gbfem_ctx c, int nno, const double *node_xyz, int nel, int nv, const int *el_nodes,
                    int nfa, const int *fa_id, const int *fa_el, const int *fa_side, const int *fa_bc) {
   GB_CHECK(c, "null context");
@@ -280,6 +289,7 @@ int gbfem_set_mesh(gbfem_ctx c, int nno, const double *node_xyz, int nel, int nv
   c->nv = nv;
   c->nfa = nfa;
   c->mixed = false;
+  clear_constraints(c);
   c->h_el_tet.clear();
   c->el_nodes4.release();
   c->h_el_nodes.assign(el_nodes, el_nodes + (size_t)nel * nv);
@@ -328,6 +338,7 @@ int gbfem_set_mesh_mixed(gbfem_ctx c, int nno, const double *node_xyz, int nel, 
   c->nv = GBFEM_PRISM;  // element slots
   c->nfa = 0;
   c->mixed = true;
+  clear_constraints(c);
   c->h_el_tet.swap(tet);
   c->h_el_nodes.swap(en);
   c->h_fa_el.clear();
@@ -412,6 +423,55 @@ int gbfem_table_cache_stats(gbfem_ctx c, long long *generation, long long *uploa
   return 0;
 }
 
+int gbfem_set_constraints(gbfem_ctx c, int n, const int *vertex, const int *nr_constr, const int *constr_id) {
+  GB_CHECK(c && c->nno > 0, "mesh not set");
+  GB_CHECK(!c->mixed && c->nv == GBFEM_PRISM, "constrained vertices are supported on std prism meshes");
+  GB_CHECK(n >= 0 && n <= c->nno, "constrained vertex count out of range");
+  GB_CHECK(n == 0 || (vertex && nr_constr && constr_id), "missing constraint arrays");
+  GB_CUDA(cudaSetDevice(c->device));
+  std::vector<int> node(c->nno, -1), par((size_t)4 * std::max(n, 1), -1);
+  for (int k = 0; k < n; k++) {
+    const int v = vertex[k], cnt = nr_constr[k];
+    GB_CHECK(v >= 0 && v < c->nno, "constrained vertex index out of range");
+    GB_CHECK(node[v] < 0, "vertex " + std::to_string(v) + " listed twice");
+    GB_CHECK(cnt == 2 || cnt == 4, "a constrained vertex has 2 (mid-edge) or 4 (mid-face) constraining vertices");
+    for (int j = 0; j < cnt; j++) {
+      const int p = constr_id[4 * (size_t)k + j];
+      GB_CHECK(p >= 0 && p < c->nno && p != v, "constraining vertex index out of range");
+      par[4 * (size_t)k + j] = p;
+    }
+    node[v] = k;
+  }
+  // one level of constraints, as on the reference's 1-irregular meshes
+  // (apr_get_stiff_mat_data expands a constrained vertex once)
+  for (int k = 0; k < 4 * n; k++)
+    GB_CHECK(par[k] < 0 || node[par[k]] < 0, "a constraining vertex is itself constrained");
+  clear_constraints(c);
+  std::vector<unsigned char> el_con(c->nel, 0);
+  if (n > 0)
+    for (long long i = 0; i < (long long)c->nel * c->nv; i++)
+      if (node[c->h_el_nodes[i]] >= 0) el_con[i / c->nv] = 1;
+  GB_TRY(upload(c, c->con_node, node.data(), node.size()));
+  GB_TRY(upload(c, c->con_par, par.data(), par.size()));
+  c->h_con_node.swap(node);
+  c->h_con_par.swap(par);
+  c->h_el_con.swap(el_con);
+  c->ncon = n;
+  GB_CUDA(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+// length of the expanded vertex list of an element (its table block holds
+// n x n + n entries)
+static int constrained_list_length(gbfem_ctx c, int el) {
+  int n = 0;
+  for (int j = 0; j < c->nv; j++) {
+    const int k = c->ncon ? c->h_con_node[c->h_el_nodes[(size_t)el * c->nv + j]] : -1;
+    n += k < 0 ? 1 : (c->h_con_par[4 * (size_t)k + 2] >= 0 ? 4 : 2);
+  }
+  return n;
+}
+
 int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long long nnz, const int *row_ptr,
                             const int *col_ind) {
   GB_CHECK(c && c->nno > 0, "mesh not set");
@@ -427,13 +487,16 @@ int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long 
   if (dof_of_node) {
     // a vertex of an element without a dof is a constrained (hanging) vertex
     // (apr_get_ent_pdeg(...) == 0, apd_std_lin/aps_std_lin_intf.c:2998): its
-    // element's contributions would need the constraint rewrite of
-    // apr_get_stiff_mat_data (:2995-3170), which this library does not do
+    // element's contributions take the constraint rewrite of
+    // apr_get_stiff_mat_data (:2995-3170), which needs its constraining
+    // vertices (gbfem_set_constraints, called before this)
     for (long long i = 0; i < (long long)c->nel * c->nv; i++) {
-      const int d = dof_of_node[c->h_el_nodes[i]];
-      GB_CHECK(d >= 0 && d < ndof,
+      const int v = c->h_el_nodes[i], d = dof_of_node[v];
+      const bool constrained = c->ncon && c->h_con_node[v] >= 0;
+      GB_CHECK(constrained || (d >= 0 && d < ndof),
                "element " + std::to_string(i / c->nv) + " has a vertex without a dof (a constrained / hanging "
-               "vertex): the constraint rewrite of apr_get_stiff_mat_data is not supported");
+               "vertex) that gbfem_set_constraints did not name");
+      GB_CHECK(!constrained || d < 0, "a constrained vertex carries a dof");
     }
     c->hs.dof_of_node.assign(dof_of_node, dof_of_node + c->nno);
   }
@@ -451,6 +514,8 @@ int gbfem_set_crs_structure(gbfem_ctx c, int ndof, const int *dof_of_node, long 
 
 int gbfem_build_structure(gbfem_ctx c, int *ndof, long long *nnz, int *nr_colors) {
   GB_CHECK(c && c->nno > 0, "mesh not set");
+  GB_CHECK(c->ncon == 0, "constrained vertices: the structure and tables come from the caller "
+                         "(gbfem_set_crs_structure, gbfem_create_assemble_stiff_mat)");
   GB_CHECK(!c->mixed, "meshes of prisms and tetrahedra together are for the DG path (gbfem_dg_*)");
   GB_TRY(gbfem::build_host_structure(c->nno, c->nel, c->nv, c->h_el_nodes.data(), c->nfa, c->h_fa_el.data(),
                                      c->h_fa_side.data(), c->hs));
@@ -479,6 +544,8 @@ int gbfem_build_structure(gbfem_ctx c, int *ndof, long long *nnz, int *nr_colors
 int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
   GB_CHECK(c && c->nno > 0, "mesh not set");
   GB_CHECK(!c->mixed, "meshes of prisms and tetrahedra together are for the DG path (gbfem_dg_*)");
+  GB_CHECK(c->ncon == 0, "constrained vertices: the structure and tables come from the caller "
+                         "(gbfem_set_crs_structure, gbfem_create_assemble_stiff_mat)");
   GB_CUDA(cudaSetDevice(c->device));
   GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
   int nd = 0;
@@ -677,6 +744,65 @@ static int build_pipe_plan(gbfem_ctx c, int e0, int e1) {
   return 0;
 }
 
+// Splits the drop-in's element range [e0, e1) and face range [f0, f1) into
+// entities without and with constrained vertices and uploads the lists
+// (element ids and table positions, face ids and positions) to con_lists:
+// plain elements (ids, positions: e1 - e0 slots each), plain faces (f1 - f0
+// slots each), then the constrained elements' ids and positions and the
+// constrained faces' (con_split_n: the four counts).  Kept while the tables
+// are cached and nothing it depends on changed.
+static int split_constrained(gbfem_ctx c, const int *ent_id, const int *ent_pos, int n_ent, int e0, int e1, int f0,
+                             int f1) {
+  const long long sig[7] = {n_ent, e0, e1, f0, f1, c->con_gen, c->table_generation};
+  bool same = c->cache_tables && c->con_split_key[0] == ent_id && c->con_split_key[1] == ent_pos;
+  for (int i = 0; i < 7; i++) same = same && c->con_split_sig[i] == sig[i];
+  if (same) return 0;
+  const int ne = e1 - e0, nf = f1 - f0;
+  std::vector<int> lists(2 * (size_t)(ne + nf) + 2 * (size_t)(ne + nf));
+  std::vector<int> ce, cf;
+  int nfe = 0, nff = 0;
+  for (int i = e0; i < e1; i++) {
+    const int el = ent_id[i] - 1;
+    if (el >= 0 && el < c->nel && c->h_el_con[el]) {
+      ce.push_back(i);
+    } else {  // (ids outside the mesh reach the plain kernel, which reports them)
+      lists[nfe] = ent_id[i];
+      lists[ne + nfe] = ent_pos[i];
+      nfe++;
+    }
+  }
+  for (int i = f0; i < f1; i++) {
+    const int id = ent_id[i];
+    const int fa = (id >= 0 && id < (int)c->fa_index_of_id.size()) ? c->fa_index_of_id[id] : -1;
+    if (fa >= 0 && c->h_el_con[c->h_fa_el[fa]]) {
+      cf.push_back(i);
+    } else {
+      lists[2 * (size_t)ne + nff] = id;
+      lists[2 * (size_t)ne + nf + nff] = ent_pos[i];
+      nff++;
+    }
+  }
+  const size_t b = 2 * (size_t)(ne + nf);
+  const int nce = (int)ce.size(), ncf = (int)cf.size();
+  for (int k = 0; k < nce; k++) {
+    lists[b + k] = ent_id[ce[k]];
+    lists[b + nce + k] = ent_pos[ce[k]];
+  }
+  for (int k = 0; k < ncf; k++) {
+    lists[b + 2 * nce + k] = ent_id[cf[k]];
+    lists[b + 2 * nce + ncf + k] = ent_pos[cf[k]];
+  }
+  GB_TRY(upload(c, c->con_lists, lists.data(), std::max<size_t>(b + 2 * (size_t)(nce + ncf), 1)));
+  c->con_split_n[0] = nfe;
+  c->con_split_n[1] = nce;
+  c->con_split_n[2] = nff;
+  c->con_split_n[3] = ncf;
+  c->con_split_key[0] = ent_id;
+  c->con_split_key[1] = ent_pos;
+  for (int i = 0; i < 7; i++) c->con_split_sig[i] = sig[i];
+  return 0;
+}
+
 int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, const int *Pdeg_coarse_p,
                                     int Nr_int_ent, const int *L_int_ent_type, const int *L_int_ent_id,
                                     int Nr_colors_elems, const int *L_color_index_elems, int Nr_colors_faces,
@@ -689,11 +815,16 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   GB_CHECK(Comp_type >= GBFEM_COMP_SM && Comp_type <= GBFEM_COMP_BOTH, "Comp_type must be SM, RHS or BOTH");
   GB_CHECK(Nr_int_ent >= 0 && L_int_ent_id && Asse_pos_first_dof_int_ent && Assembly_table,
            "missing entity lists or assembly table");
-  GB_CHECK(Max_dofs_int_ent <= c->nv,
-           "Max_dofs_int_ent exceeds the element vertex count: an entity's dof list holds the constraining "
-           "vertices of a constrained (hanging) vertex; the constraint rewrite of apr_get_stiff_mat_data "
-           "(apd_std_lin/aps_std_lin_intf.c:2995-3170) is not supported, refine conformingly");
-  GB_CHECK(Max_dofs_int_ent == c->nv, "Max_dofs_int_ent must equal the element vertex count");
+  if (c->ncon == 0) {
+    GB_CHECK(Max_dofs_int_ent <= c->nv,
+             "Max_dofs_int_ent exceeds the element vertex count: an entity's dof list holds the constraining "
+             "vertices of a constrained (hanging) vertex; name them with gbfem_set_constraints");
+    GB_CHECK(Max_dofs_int_ent == c->nv, "Max_dofs_int_ent must equal the element vertex count");
+  } else {
+    // an expanded list holds up to 4 constraining vertices per vertex
+    GB_CHECK(Max_dofs_int_ent >= c->nv && Max_dofs_int_ent <= 4 * c->nv,
+             "Max_dofs_int_ent out of range for a mesh with constrained vertices");
+  }
   GB_CUDA(cudaSetDevice(c->device));
   // element and face ranges in the entity lists
   int e0, e1, f0, f1;
@@ -723,11 +854,24 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   }
   long long tlen = 0;
   {
-    // table length: last entity's position + n*n + n
-    int last = 0;
-    for (int i : {e1 - 1, f1 - 1})
-      if (i >= 0 && Asse_pos_first_dof_int_ent[i] > last) last = Asse_pos_first_dof_int_ent[i];
-    tlen = (long long)last + c->nv * c->nv + c->nv;
+    // table length: last entity's position + n*n + n (n: its dof count,
+    // longer than nv where its element has constrained vertices)
+    for (int i : {e1 - 1, f1 - 1}) {
+      if (i < 0) continue;
+      int n = c->nv;
+      if (c->ncon) {
+        int el = -1;
+        if (i < e1 && i >= e0) {
+          el = L_int_ent_id[i] - 1;
+        } else {
+          const int id = L_int_ent_id[i];
+          const int fa = (id >= 0 && id < (int)c->fa_index_of_id.size()) ? c->fa_index_of_id[id] : -1;
+          el = fa >= 0 ? c->h_fa_el[fa] : -1;
+        }
+        if (el >= 0 && el < c->nel) n = constrained_list_length(c, el);
+      }
+      tlen = std::max(tlen, (long long)Asse_pos_first_dof_int_ent[i] + (long long)n * n + n);
+    }
   }
   cudaEventRecord(c->ev0, c->stream);
   GB_TRY(stage_input(c, 0, c->in_id, L_int_ent_id, Nr_int_ent));
@@ -737,26 +881,64 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   if (do_sm) GB_CUDA(cudaMemsetAsync(c->val.p, 0, (size_t)c->nnz * sizeof(double), c->stream));
   if (do_rhs) GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, (size_t)c->ndof * sizeof(double), c->stream));
   int launches = 0, r;
-  const bool side = f1 > f0;  // the faces run beside the element chunks
+  // with constrained vertices: the entities whose element has one are split
+  // off (their tables are n x n + n with the expanded lists) to the rewrite
+  // kernels; the others keep the plain kernels
+  const int *fe_id = c->in_id.p + e0, *fe_pos = c->in_pos.p + e0;
+  const int *ff_id = c->in_id.p + f0, *ff_pos = c->in_pos.p + f0;
+  int nfe = e1 - e0, nff = f1 - f0, nce = 0, ncf = 0;
+  if (c->ncon) {
+    GB_TRY(split_constrained(c, L_int_ent_id, Asse_pos_first_dof_int_ent, Nr_int_ent, e0, e1, f0, f1));
+    const int *L = c->con_lists.p;
+    nfe = c->con_split_n[0];
+    nce = c->con_split_n[1];
+    nff = c->con_split_n[2];
+    ncf = c->con_split_n[3];
+    const int ne = e1 - e0;
+    fe_id = L;
+    fe_pos = L + ne;
+    ff_id = L + 2 * ne;
+    ff_pos = L + 2 * ne + (f1 - f0);
+  }
+  const bool side = nff > 0;  // the faces run beside the element chunks
   if (side)
-    GB_TRY(launch_faces_beside(c, f1 - f0, c->in_id.p + f0, c->fa_map.p, (int)c->fa_map.n, c->in_pos.p + f0,
-                               c->in_table.p, do_sm, do_rhs, &launches));
+    GB_TRY(launch_faces_beside(c, nff, ff_id, c->fa_map.p, (int)c->fa_map.n, ff_pos, c->in_table.p, do_sm, do_rhs,
+                               &launches));
   cudaEventRecord(c->ev2, c->stream);
   GB_CHECK(c->nv == GBFEM_PRISM || !c->aniso, "std tetrahedra take an isotropic k_el (tensors: prisms and DG)");
+  // elements a..b of the (plain) element list
   auto elements = [&](int a, int b) -> int {
     if (b <= a) return 0;
     if (c->nv == GBFEM_PRISM)
-      return gbfem::launch_prism_elements(c->stream, true, c->aniso, b - a, c->in_id.p + a, 1, c->in_pos.p + a,
-                                          c->nel, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f,
-                                          c->in_table.p, c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p,
-                                          c->std_dword);
-    return gbfem::launch_tet_elements(c->stream, true, b - a, c->in_id.p + a, 1, c->in_pos.p + a, c->nel,
-                                      c->el_nodes.p, c->xyz.p, c->k_el.p, c->f, c->in_table.p, c->val.p, c->rhs.p,
-                                      do_sm, do_rhs, c->err.p);
+      return gbfem::launch_prism_elements(c->stream, true, c->aniso, b - a, fe_id + a, 1, fe_pos + a, c->nel,
+                                          c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->in_table.p,
+                                          c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p, c->std_dword);
+    return gbfem::launch_tet_elements(c->stream, true, b - a, fe_id + a, 1, fe_pos + a, c->nel, c->el_nodes.p,
+                                      c->xyz.p, c->k_el.p, c->f, c->in_table.p, c->val.p, c->rhs.p, do_sm, do_rhs,
+                                      c->err.p);
+  };
+  // the entities with constrained vertices, after the plain elements
+  auto constrained = [&]() -> int {
+    int n = 0;
+    if (!c->ncon) return 0;
+    const int ne = e1 - e0, nf = f1 - f0;
+    const int *L = c->con_lists.p;
+    for (int fc = 0; fc < 2; fc++) {
+      const int cnt = fc ? ncf : nce;
+      if (cnt == 0) continue;
+      const int *ids = fc ? L + 2 * ne + 2 * nf + 2 * nce : L + 2 * ne + 2 * nf;
+      const int r2 = gbfem::launch_prism_constrained(
+          c->stream, fc == 1, c->aniso, cnt, ids, ids + cnt, c->nel, c->fa_map.p, (int)c->fa_map.n, c->nfa,
+          c->fa_el.p, c->fa_side.p, c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->penalty, c->g,
+          c->con_node.p, c->con_par.p, c->in_table.p, c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p);
+      if (r2 < 0) return r2;
+      n += r2;
+    }
+    return n;
   };
   // with cached tables and host outputs: element chunks, each chunk's
-  // finished rows downloaded while the next chunk runs
-  bool pipe = c->cache_tables && (crs_val || rhs) && e1 > e0;
+  // finished rows downloaded while the next chunk runs (plain meshes)
+  bool pipe = c->cache_tables && (crs_val || rhs) && e1 > e0 && c->ncon == 0;
   if (pipe) {
     bool same = c->pipe_e0 == e0 && c->pipe_e1 == e1 && c->pipe_dword == c->std_dword;
     for (int i = 0; i < 3; i++) same = same && c->pipe_key[i] == c->cache_key[i] && c->pipe_len[i] == c->cache_len[i];
@@ -768,7 +950,7 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     const int *rp = c->hs.row_ptr.data();
     // all chunks first: a copy into pageable memory returns only when done
     for (int k = 0; k < K; k++) {
-      GB_TRY(r = elements(e0 + c->pipe_el[k], e0 + c->pipe_el[k + 1]));
+      GB_TRY(r = elements(c->pipe_el[k], c->pipe_el[k + 1]));
       launches += r;
       GB_CUDA(cudaEventRecord(c->pipe_ev[k], c->stream));
     }
@@ -791,7 +973,9 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     GB_CUDA(cudaEventRecord(c->pipe_ev[K], c->copy_stream));
     GB_CUDA(cudaStreamWaitEvent(c->stream, c->pipe_ev[K], 0));
   } else {
-    GB_TRY(r = elements(e0, e1));
+    GB_TRY(r = elements(0, nfe));
+    launches += r;
+    GB_TRY(r = constrained());
     launches += r;
     cudaEventRecord(c->ev3, c->stream);
     if (side) GB_TRY(join_side(c, c->stream));
@@ -808,6 +992,8 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
 
 int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
   GB_CHECK(c && c->have_tables, "structure not built (gbfem_build_structure)");
+  GB_CHECK(c->ncon == 0, "constrained vertices: assemble through gbfem_create_assemble_stiff_mat with the "
+                         "caller's tables");
   GB_CHECK(c->nv == GBFEM_PRISM || !c->aniso, "std tetrahedra take an isotropic k_el (tensors: prisms and DG)");
   GB_CHECK(scatter_mode == GBFEM_SCATTER_ATOMIC || scatter_mode == GBFEM_SCATTER_COLOR, "bad scatter mode");
   GB_CUDA(cudaSetDevice(c->device));

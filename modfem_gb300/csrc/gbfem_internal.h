@@ -109,6 +109,15 @@ int launch_prism_faces(cudaStream_t st, bool atomic, int count, const int *ent_f
                        const int *fa_el, const int *fa_side, const int *el_nodes,
                        const double *xyz, double penalty, double g, const int *tab, double *val,
                        double *rhs, int do_sm, int do_rhs, int *err);
+// Elements (faces = false, 1-based element ids) or boundary faces (mesh face
+// ids through fa_map) whose element has constrained vertices: local matrices
+// rewritten for the constraints and scattered through n x n + n tables.
+int launch_prism_constrained(cudaStream_t st, bool faces, bool aniso, int count, const int *ent_id,
+                             const int *ent_pos, int nel, const int *fa_map, int fa_map_len, int nfa,
+                             const int *fa_el, const int *fa_side, const int *el_nodes, const double *xyz,
+                             const double *k_el, const double *D_el, double f, double penalty, double g,
+                             const int *con_node, const int *con_par, const int *tab, double *val, double *rhs,
+                             int do_sm, int do_rhs, int *err);
 int launch_tet_elements(cudaStream_t st, bool atomic, int count, const int *ent_el, int el_base,
                         const int *ent_pos, int nel, const int *el_nodes, const double *xyz,
                         const double *k_el, double f, const int *tab, double *val, double *rhs,
@@ -252,6 +261,20 @@ struct gbfem_ctx_s {
   gbfem::DevBuf<int> fa_el, fa_side;
   std::vector<int> h_fa_id, h_fa_el, h_fa_side, h_el_nodes;
   std::vector<int> fa_index_of_id;  // reference face id -> bc face index (-1 none)
+  // constrained (hanging) vertices (gbfem_set_constraints): per vertex -1 or
+  // the index k of its constraining vertices con_par[4k..4k+3] (-1 padded);
+  // h_el_con marks the elements with a constrained vertex
+  int ncon = 0;
+  long long con_gen = 0;
+  std::vector<int> h_con_node, h_con_par;
+  std::vector<unsigned char> h_el_con;
+  gbfem::DevBuf<int> con_node, con_par;
+  // the drop-in's entity lists split into entities with and without
+  // constrained vertices (element ids, positions; face ids, positions)
+  gbfem::DevBuf<int> con_lists;
+  int con_split_n[4] = {0, 0, 0, 0};
+  const void *con_split_key[2] = {nullptr, nullptr};
+  long long con_split_sig[7] = {-1, -1, -1, -1, -1, -1, -1};
   // coefficients
   gbfem::DevBuf<double> k_el, D_el;
   int aniso = 0;

@@ -267,56 +267,22 @@ __global__ void __launch_bounds__(kDwThreads, 3) prism_elements_dw_kernel(
   }
 }
 
-// Boundary penalty faces of the std weak form (pdd_conv_diff/weak_formulation/
-// approx_std/pds_conv_diff_weakform_std.c:253-630):
-// K_ij += penalty phi_i phi_j |dS| w, R_i += penalty g phi_i |dS| w, with the
-// face rule of apr_set_quadr_2D (aps_std_util.c:1445-1500) and |dS| of the
-// side cases of apr_elem_calc_3D_prism (aps_std_util.c:770-805).  Only the
-// face's own vertices get non-zero entries.
-template <bool ATOMIC>
-__global__ void __launch_bounds__(128) prism_faces_kernel(
-    int count, const int *__restrict__ ent_fa, int fa_base, const int *__restrict__ fa_map,
-    int fa_map_len, const int *__restrict__ ent_pos, int nfa, const int *__restrict__ fa_el,
-    const int *__restrict__ fa_side, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
-    double penalty, double g, const int *__restrict__ tab, double *__restrict__ val,
-    double *__restrict__ rhs, int do_sm, int do_rhs, int *__restrict__ err) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  // face index: i, or ent_fa[i] (a face index when fa_map is null, else a
-  // mesh face id translated through fa_map)
-  int fa = i;
-  if (ent_fa) {
-    int id = __ldg(ent_fa + i) - fa_base;
-    if (fa_map)
-      fa = (id >= 0 && id < fa_map_len) ? __ldg(fa_map + id) : -1;
-    else
-      fa = id;
-  }
-  if (fa < 0 || fa >= nfa) {
-    atomicExch(err, 2);
-    return;
-  }
-  const int e = __ldg(fa_el + fa), side = __ldg(fa_side + fa);
-  const int *tb = tab + (ent_pos ? (size_t)__ldg(ent_pos + i) : (size_t)42 * e);
-  const int *nd = el_nodes + 6 * (size_t)e;
-  d3 X[6];
-#pragma unroll
-  for (int j = 0; j < 6; j++) X[j] = load_node(xyz, __ldg(nd + j));
+// The penalty face integrals of one boundary face (side 0..4 of its prism,
+// vertices X): K over the face's own vertices loc[0..nloc) (upper triangle
+// of a 4x4 block packed row by row), R their load entries.
+__device__ __forceinline__ void prism_face_local(const d3 (&X)[6], int side, double penalty, double g,
+                                                 int (&loc)[4], int &nloc, double (&K)[10], double (&Rl)[4]) {
   const d3 a0 = X[0], a1 = X[1], a2 = X[2], b0 = X[3], b1 = X[4], b2 = X[5];
   const d3 ea = a1 - a0, eb = b1 - b0, fa_ = a2 - a0, fb = b2 - b0;
   const d3 m1 = 0.5 * (ea + eb), d1 = 0.5 * (eb - ea);
   const d3 m2 = 0.5 * (fa_ + fb), d2 = 0.5 * (fb - fa_);
   const d3 c0 = 0.5 * (b0 - a0);
-  // local vertex ids of the face
-  int loc[4];
-  int nloc;
   if (side == 0) { loc[0] = 0; loc[1] = 1; loc[2] = 2; nloc = 3; }
   else if (side == 1) { loc[0] = 3; loc[1] = 4; loc[2] = 5; nloc = 3; }
   else {
     int a = side - 2, b = (side - 1) % 3;
     loc[0] = a; loc[1] = b; loc[2] = a + 3; loc[3] = b + 3; nloc = 4;
   }
-  double K[10], Rl[4];
 #pragma unroll
   for (int j = 0; j < 10; j++) K[j] = 0.0;
 #pragma unroll
@@ -357,6 +323,46 @@ __global__ void __launch_bounds__(128) prism_faces_kernel(
         if (a < nloc && b < nloc) K[k] = fma(pa * ph[a], ph[b], K[k]);
     for (int a = 0; a < nloc; a++) Rl[a] = fma(pa * g, ph[a], Rl[a]);
   }
+}
+
+// Boundary penalty faces of the std weak form (pdd_conv_diff/weak_formulation/
+// approx_std/pds_conv_diff_weakform_std.c:253-630):
+// K_ij += penalty phi_i phi_j |dS| w, R_i += penalty g phi_i |dS| w, with the
+// face rule of apr_set_quadr_2D (aps_std_util.c:1445-1500) and |dS| of the
+// side cases of apr_elem_calc_3D_prism (aps_std_util.c:770-805).  Only the
+// face's own vertices get non-zero entries.
+template <bool ATOMIC>
+__global__ void __launch_bounds__(128) prism_faces_kernel(
+    int count, const int *__restrict__ ent_fa, int fa_base, const int *__restrict__ fa_map,
+    int fa_map_len, const int *__restrict__ ent_pos, int nfa, const int *__restrict__ fa_el,
+    const int *__restrict__ fa_side, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
+    double penalty, double g, const int *__restrict__ tab, double *__restrict__ val,
+    double *__restrict__ rhs, int do_sm, int do_rhs, int *__restrict__ err) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  // face index: i, or ent_fa[i] (a face index when fa_map is null, else a
+  // mesh face id translated through fa_map)
+  int fa = i;
+  if (ent_fa) {
+    int id = __ldg(ent_fa + i) - fa_base;
+    if (fa_map)
+      fa = (id >= 0 && id < fa_map_len) ? __ldg(fa_map + id) : -1;
+    else
+      fa = id;
+  }
+  if (fa < 0 || fa >= nfa) {
+    atomicExch(err, 2);
+    return;
+  }
+  const int e = __ldg(fa_el + fa), side = __ldg(fa_side + fa);
+  const int *tb = tab + (ent_pos ? (size_t)__ldg(ent_pos + i) : (size_t)42 * e);
+  const int *nd = el_nodes + 6 * (size_t)e;
+  d3 X[6];
+#pragma unroll
+  for (int j = 0; j < 6; j++) X[j] = load_node(xyz, __ldg(nd + j));
+  int loc[4], nloc;
+  double K[10], Rl[4];
+  prism_face_local(X, side, penalty, g, loc, nloc, K, Rl);
   if (do_sm) {
     int k = 0;
     for (int a = 0; a < 4; a++)
@@ -430,6 +436,126 @@ __global__ void __launch_bounds__(128) tet_elements_kernel(
   }
 }
 
+// Elements and boundary faces whose element has constrained (hanging)
+// vertices: the local 6x6 matrix and load vector are rewritten as
+// apr_get_stiff_mat_data does (apd_std_lin/aps_std_lin_intf.c:2978-3160)
+// and scattered through the entity's assembly table of n x n + n entries,
+// n the length of the expanded vertex list: in vertex order a real vertex
+// stands for itself with coefficient 1, a constrained vertex for its 2
+// (mid-edge) or 4 (mid-face) constraining vertices with coefficient 1/2 or
+// 1/4; entry (a, b) = c_a c_b K[i(a)][i(b)], rhs entry a = c_a R[i(a)].
+// con_node[v] is -1 for a vertex with a dof, else the index k of its
+// constraining vertices con_par[4k..4k+3] (-1 padded).  These entities lie
+// along refinement interfaces only: one thread an entity, FP64 arithmetic.
+__device__ __forceinline__ int con_expand(const int (&nodes)[6], const int *__restrict__ con_node,
+                                          const int *__restrict__ con_par, unsigned char (&src)[24],
+                                          double (&cf)[24]) {
+  int n = 0;
+#pragma unroll
+  for (int v = 0; v < 6; v++) {
+    const int k = __ldg(con_node + nodes[v]);
+    if (k < 0) {
+      src[n] = (unsigned char)v;
+      cf[n++] = 1.0;
+    } else {
+      const int cnt = __ldg(con_par + 4 * (size_t)k + 2) >= 0 ? 4 : 2;
+      const double c = cnt == 2 ? 0.5 : 0.25;
+      for (int j = 0; j < cnt; j++) {
+        src[n] = (unsigned char)v;
+        cf[n++] = c;
+      }
+    }
+  }
+  return n;
+}
+
+template <bool ANISO, bool FACE>
+__global__ void __launch_bounds__(128) prism_constrained_kernel(
+    int count, const int *__restrict__ ent_id, const int *__restrict__ ent_pos, int nel,
+    const int *__restrict__ fa_map, int fa_map_len, int nfa, const int *__restrict__ fa_el,
+    const int *__restrict__ fa_side, const int *__restrict__ el_nodes, const double *__restrict__ xyz,
+    const double *__restrict__ k_el, const double *__restrict__ D_el, double f, double penalty, double g,
+    const int *__restrict__ con_node, const int *__restrict__ con_par, const int *__restrict__ tab,
+    double *__restrict__ val, double *__restrict__ rhs, int do_sm, int do_rhs, int *__restrict__ err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  int e, side = 0;
+  if (FACE) {
+    const int id = __ldg(ent_id + i);
+    const int fa = (id >= 0 && id < fa_map_len) ? __ldg(fa_map + id) : -1;
+    if (fa < 0 || fa >= nfa) {
+      atomicExch(err, 2);
+      return;
+    }
+    e = __ldg(fa_el + fa);
+    side = __ldg(fa_side + fa);
+  } else {
+    e = __ldg(ent_id + i) - 1;
+    if (e < 0 || e >= nel) {
+      atomicExch(err, 1);
+      return;
+    }
+  }
+  int nodes[6];
+  d3 X[6];
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    nodes[j] = __ldg(el_nodes + 6 * (size_t)e + j);
+    X[j] = load_node(xyz, nodes[j]);
+  }
+  // the local matrix, K[u * 6 + w] = (row w, column u), and load vector
+  double K[36], R[6];
+  if (FACE) {
+    int loc[4], nloc;
+    double Kf[10], Rl[4];
+    prism_face_local(X, side, penalty, g, loc, nloc, Kf, Rl);
+#pragma unroll
+    for (int j = 0; j < 36; j++) K[j] = 0.0;
+#pragma unroll
+    for (int j = 0; j < 6; j++) R[j] = 0.0;
+    int k = 0;
+    for (int a = 0; a < 4; a++)
+      for (int b = a; b < 4; b++, k++) {
+        if (a >= nloc || b >= nloc) continue;
+        K[loc[a] * 6 + loc[b]] = Kf[k];
+        K[loc[b] * 6 + loc[a]] = Kf[k];
+      }
+    for (int a = 0; a < nloc; a++) R[loc[a]] = Rl[a];
+  } else if (ANISO) {
+    prism_element_aniso(X, D_el + 9 * (size_t)e, f, K, R);
+  } else {
+    double Ks[21];
+    const v3 Xv[6] = {{X[0].x, X[0].y, X[0].z}, {X[1].x, X[1].y, X[1].z}, {X[2].x, X[2].y, X[2].z},
+                      {X[3].x, X[3].y, X[3].z}, {X[4].x, X[4].y, X[4].z}, {X[5].x, X[5].y, X[5].z}};
+    prism_std_element(Xv, k_el ? __ldg(k_el + e) : 1.0, f, Ks, R);
+    int k = 0;
+#pragma unroll
+    for (int u = 0; u < 6; u++)
+#pragma unroll
+      for (int w = u; w < 6; w++, k++) {
+        K[u * 6 + w] = Ks[k];
+        K[w * 6 + u] = Ks[k];
+      }
+  }
+  unsigned char src[24];
+  double cf[24];
+  const int n = con_expand(nodes, con_node, con_par, src, cf);
+  const int *tb = tab + __ldg(ent_pos + i);
+  if (do_sm) {
+    for (int b = 0; b < n; b++)
+      for (int a = 0; a < n; a++) {
+        const double kv = K[src[b] * 6 + src[a]];
+        if (kv != 0.0) atomicAdd(val + __ldg(tb + a + n * b), cf[b] * cf[a] * kv);
+      }
+  }
+  if (do_rhs) {
+    for (int a = 0; a < n; a++) {
+      const double rv = R[src[a]];
+      if (rv != 0.0) atomicAdd(rhs + __ldg(tb + n * n + a), cf[a] * rv);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
@@ -481,6 +607,27 @@ int launch_prism_faces(cudaStream_t st, bool atomic, int count, const int *ent_f
     prism_faces_kernel<false><<<nblk(count, T), T, 0, st>>>(count, ent_fa, fa_base, fa_map, fa_map_len,
                                                             ent_pos, nfa, fa_el, fa_side, el_nodes, xyz,
                                                             penalty, g, tab, val, rhs, do_sm, do_rhs, err);
+  GB_CUDA(cudaGetLastError());
+  return 1;
+}
+
+int launch_prism_constrained(cudaStream_t st, bool faces, bool aniso, int count, const int *ent_id,
+                             const int *ent_pos, int nel, const int *fa_map, int fa_map_len, int nfa,
+                             const int *fa_el, const int *fa_side, const int *el_nodes, const double *xyz,
+                             const double *k_el, const double *D_el, double f, double penalty, double g,
+                             const int *con_node, const int *con_par, const int *tab, double *val, double *rhs,
+                             int do_sm, int do_rhs, int *err) {
+  if (count <= 0) return 0;
+  const int T = 128;
+#define GB_LAUNCH(A, F)                                                                                         \
+  prism_constrained_kernel<A, F><<<nblk(count, T), T, 0, st>>>(count, ent_id, ent_pos, nel, fa_map, fa_map_len, \
+                                                              nfa, fa_el, fa_side, el_nodes, xyz, k_el, D_el, f, \
+                                                              penalty, g, con_node, con_par, tab, val, rhs,      \
+                                                              do_sm, do_rhs, err)
+  if (faces) GB_LAUNCH(false, true);
+  else if (aniso) GB_LAUNCH(true, false);
+  else GB_LAUNCH(false, false);
+#undef GB_LAUNCH
   GB_CUDA(cudaGetLastError());
   return 1;
 }

@@ -84,12 +84,14 @@ def _tri_grid(n):
     return xy, tri, nb
 
 
-def write_jk(path, n, bc=1):
-    """Writes the jk file of the n^3-hexahedra unit cube split into prisms."""
+def write_jk(path, n, bc=1, capacity=(0, 0, 0, 0)):
+    """Writes the jk file of the n^3-hexahedra unit cube split into prisms.
+    ``capacity``: the first line's node, edge, face and element array sizes
+    (0: exactly the mesh read; refinement needs room for the new entities)."""
     xy, tri, nb = _tri_grid(n)
     nbj = np.where(nb < 0, -bc, nb)
     with open(path, "w") as f:
-        f.write("0 0 0 0\n")
+        f.write("%d %d %d %d\n" % tuple(capacity))
         f.write(f"{xy.shape[0]} 0.0 1.0 {n} {bc} {bc}\n")
         for x, y in xy:
             f.write(f"{x:.17g} {y:.17g}\n")

@@ -241,6 +241,72 @@ def std_prism_assemble_abs(mesh, k_el, dof_of_node, row_ptr, col_ind, **kw):
         lib().orc_set_accumulate_abs(0)
 
 
+def std_constraint_expand(nodes, con_cnt, con_par):
+    """The dof entity list of a std element whose vertices may be hanging,
+    with the coefficients of its rewrite (apr_get_stiff_mat_data,
+    apd_std_lin/aps_std_lin_intf.c:2978-3035): in vertex order, a real vertex
+    stands for itself with coefficient 1, a constrained vertex for its
+    constraining vertices (apr_get_constr_data order) with coefficient 1/2
+    (2 of them: mid-edge) or 1/4 (4: mid-face).  Returns (local vertex of
+    each entry, coefficient, vertex id)."""
+    src, coef, ids = [], [], []
+    for ino, v in enumerate(nodes):
+        c = int(con_cnt[v])
+        if c == 0:
+            src.append(ino)
+            coef.append(1.0)
+            ids.append(int(v))
+        else:
+            cv = 0.5 if c == 2 else 0.25
+            for j in range(c):
+                src.append(ino)
+                coef.append(cv)
+                ids.append(int(con_par[v][j]))
+    return np.array(src), np.array(coef), np.array(ids, np.int32)
+
+
+def std_constraint_rewrite(K, R, nodes, con_cnt, con_par):
+    """The rewrite of a local matrix (row w, column u) and load vector for
+    hanging vertices (aps_std_lin_intf.c:3077-3160): entry (a, b) of the
+    rewritten matrix is c_b c_a K[i(a), i(b)], entry a of the load vector
+    c_a R[i(a)], over the expanded list of std_constraint_expand."""
+    src, coef, ids = std_constraint_expand(nodes, con_cnt, con_par)
+    Kc = (coef[None, :] * coef[:, None]) * K[np.ix_(src, src)]
+    return Kc, coef * R[src], ids
+
+
+def std_dropin_assemble(coords, el_nodes, k_el, int_ent_type, int_ent_id, asse_pos, table, ndof, nnz,
+                        fa_of_id, f=1.0, penalty=1e7, g=0.0, con_cnt=None, con_par=None, D_el=None,
+                        absolute=False):
+    """The table-driven assembly of utr_create_assemble_stiff_mat
+    (utd_util/uts_ls_intf.c:3629-3858) over the reference's entity lists:
+    each element (type 4, 1-based id) and boundary face (type 3, id mapped by
+    ``fa_of_id`` to (element, side)) computes its local matrix
+    (std_prism_element / std_prism_face), rewritten through
+    std_constraint_rewrite when constraint data is given, and adds entry
+    (a, b) at table[pos + a + n b], rhs row a at table[pos + n n + a].
+    ``absolute``: sums of |contribution| instead (the comparison scale)."""
+    val = np.zeros(nnz)
+    rhs = np.zeros(ndof)
+    for t, i, pos in zip(int_ent_type, int_ent_id, asse_pos):
+        if t == 4:
+            e = int(i) - 1
+            A = D_el[e] if D_el is not None else k_el[e] * np.eye(3)
+            K, R = std_prism_element(coords[el_nodes[e]], A, f)
+        else:
+            e, side = fa_of_id[int(i)]
+            K, R = std_prism_face(coords[el_nodes[e]], side, penalty, g)
+        if con_cnt is not None:
+            K, R, _ = std_constraint_rewrite(K, R, el_nodes[e], con_cnt, con_par)
+        n = K.shape[0]
+        tb = table[pos:pos + n * n + n]
+        KK = np.abs(K) if absolute else K
+        RR = np.abs(R) if absolute else R
+        np.add.at(val, tb[:n * n], KK.T.ravel())
+        np.add.at(rhs, tb[n * n:], RR)
+    return val, rhs
+
+
 def crs_residual(row_ptr, col_ind, val, x, b=None):
     n = row_ptr.size - 1
     v = np.zeros(n)

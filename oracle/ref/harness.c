@@ -741,6 +741,74 @@ int refh_solver_free(void)
 }
 
 #ifdef HARNESS_STD
+/* One adaptation step as utr_adapt runs it for refinement only
+   (utd_util/uts_adapt.c:1458-1539): mmr_init_ref, apr_refine of each listed
+   active element (which also refines neighbours to keep the mesh 1-irregular,
+   aps_std_lin_intf.c:4007-4190), apr_proj_dof_ref (which creates the
+   constraint data of the hanging vertices, aps_std_lin_intf.c:3440-3615) and
+   mmr_final_ref.  The mesh's adaptation limits are set first: max_gen
+   generations, generation difference 1 (1-irregular meshes).  Returns the
+   number of active elements. */
+int refh_refine(int n, const int *el_ids, int max_gen)
+{
+  int nmno = mmr_get_max_node_id(h_mesh_id), nmed = mmr_get_max_edge_id(h_mesh_id);
+  int nmfa = mmr_get_max_face_id(h_mesh_id), nmel = mmr_get_max_elem_id(h_mesh_id), i;
+  if (n <= 0) return mmr_get_nr_elem(h_mesh_id);
+  mmr_set_max_gen(h_mesh_id, max_gen);
+  mmr_set_max_gen_diff(h_mesh_id, 1);
+  mmr_init_ref(h_mesh_id);
+  for (i = 0; i < n; i++)
+    if (mmr_el_status(h_mesh_id, el_ids[i]) == MMC_ACTIVE) apr_refine(h_field_id, el_ids[i]);
+  apr_proj_dof_ref(h_field_id, n > 1 ? -3 : el_ids[0], nmel, nmfa, nmed, nmno);
+  mmr_final_ref(h_mesh_id);
+  return mmr_get_nr_elem(h_mesh_id);
+}
+
+/* status of elements 1..max_el_id (1 active, -1 refined, 0 free) */
+int refh_el_status(int *st)
+{
+  int nmax = mmr_get_max_elem_id(h_mesh_id), el;
+  for (el = 1; el <= nmax; el++) st[el - 1] = mmr_el_status(h_mesh_id, el);
+  return nmax;
+}
+
+/* per node 1..max_node_id: cnt[id-1] = 0 for a node with dofs (or free
+   space), else the number of constraining vertices (2 mid-edge, 4 mid-face)
+   with their ids in par[4*(id-1) ...] (apr_get_constr_data) */
+int refh_constr(int *cnt, int *par)
+{
+  int nmax = mmr_get_max_node_id(h_mesh_id), v, j, ncon = 0;
+  for (v = 1; v <= nmax; v++) {
+    int c[5] = {0, 0, 0, 0, 0};
+    cnt[v - 1] = 0;
+    for (j = 0; j < 4; j++) par[4 * (v - 1) + j] = 0;
+    if (mmr_node_status(h_mesh_id, v) != MMC_ACTIVE) continue;
+    if (apr_get_ent_pdeg(h_field_id, APC_VERTEX, v) != 0) continue;
+    apr_get_constr_data(h_field_id, v, APC_VERTEX, c, NULL);
+    cnt[v - 1] = c[0];
+    for (j = 0; j < c[0] && j < 4; j++) par[4 * (v - 1) + j] = c[j + 1];
+    ncon++;
+  }
+  return ncon;
+}
+
+/* side (0..4, position in mmr_el_faces) of each boundary face of
+   refh_bc_faces in its element */
+int refh_bc_face_sides(int n, const int *fa_id, const int *fa_el, int *side)
+{
+  int i, j;
+  for (i = 0; i < n; i++) {
+    int faces[MMC_MAXELFAC + 1];
+    mmr_el_faces(h_mesh_id, fa_el[i], faces, NULL);
+    side[i] = -1;
+    for (j = 1; j <= faces[0]; j++)
+      if (faces[j] == fa_id[i]) side[i] = j - 1;
+  }
+  return n;
+}
+#endif
+
+#ifdef HARNESS_STD
 /* Std linear tetrahedron through the reference's own element calculations:
    apr_set_quadr_3D (aps_std_util.c:1335) and apr_elem_calc_3D with the
    tetra base (aps_std_util.c:869), accumulated with the 9-term diffusion and

@@ -40,6 +40,36 @@ class FixtureMesh:
         return self.el_nodes.shape[0]
 
 
+class RefinedMesh:
+    """A refined std prism mesh of a fixture made by the reference's own
+    refinement (tests/golden/make_golden.py run_hanging): every element id
+    the mesh module holds (refined parents included, only active ones are
+    in the entity lists), the active boundary faces with their sides, and
+    the constraint data of the hanging vertices."""
+
+    def __init__(self, g):
+        self.coords = g["coords"]
+        self.el_nodes = g["el_nodes"].astype(np.int32)
+        self.bc_face_id = g["bc_face_id"].astype(np.int32)
+        self.bc_face_el = g["bc_face_el"].astype(np.int32)
+        self.bc_face_bc = g["bc_face_bc"].astype(np.int32)
+        self.bc_face_side = g["bc_face_side"].astype(np.int32)
+        cnt = g["con_cnt"]
+        self.con_vertex = np.nonzero(cnt > 0)[0].astype(np.int32)
+        self.con_nr = cnt[self.con_vertex].astype(np.int32)
+        self.con_par = g["con_par"][self.con_vertex].astype(np.int32)
+        self.fa_of_id = {int(i): (int(e), int(s)) for i, e, s in
+                         zip(self.bc_face_id, self.bc_face_el, self.bc_face_side)}
+
+    @property
+    def nno(self):
+        return self.coords.shape[0]
+
+    @property
+    def nel(self):
+        return self.el_nodes.shape[0]
+
+
 def crs_rel_err(row_ptr, a, b, scale=None):
     """Assembled-value error.
 

@@ -89,6 +89,97 @@ def run_case(name):
           f"gmres {nit} it", file=sys.stderr)
 
 
+# name: (n, jitter, seed, passes of 1-based element ids to refine, max generation)
+HANG_CASES = {
+    "std_n9_hang": (9, 0.2, 8, [[1, 200, 731], [1459, 1000]], 2),
+}
+
+
+def run_hanging(name):
+    """A std prism mesh after the reference's own refinement (apr_refine with
+    the 1-irregular rule, apr_proj_dof_ref creating the constraint data): the
+    active elements' dof lists hold the constraining vertices of their
+    hanging vertices, and the reference's apr_get_stiff_mat_data rewrites
+    their element and face matrices.  Records the refined mesh, the
+    constraint data, the rewritten local matrices of the constrained
+    entities, the solver lists and tables and the assembled system."""
+    import ctypes
+    import refmod
+    from refmod import _p
+    from modfem_gb300.mesh import lognormal_k, structured_prism_mesh, write_jk
+
+    n, jitter, seed, passes, max_gen = HANG_CASES[name]
+    m = structured_prism_mesh(n, jitter=jitter, seed=seed)
+    tmp = tempfile.mkdtemp()
+    jk = os.path.join(tmp, "mesh.jk")
+    mkb = os.path.join(tmp, "mkb.dat")
+    write_jk(jk, n, capacity=(20000, 60000, 60000, 20000))
+    refmod.write_mkb(mkb, krylov=30, max_iter=5000, tol=1e-8)
+    R = refmod.RefModfem("std")
+    R.load_jk(jk)
+    R.set_node_coords(m.coords)
+    R.init_field("s", 1)
+    for ids in passes:
+        ids = np.array(ids, np.int32)
+        R.L.refh_refine(ids.size, _p(ids), max_gen)
+    s = [ctypes.c_int() for _ in range(6)]
+    R.L.refh_mesh_sizes(*[ctypes.byref(x) for x in s])
+    R.nno, R.max_node, R.nel, R.max_el = s[0].value, s[1].value, s[2].value, s[3].value
+    status = np.zeros(R.max_el, np.int32)
+    R.L.refh_el_status(_p(status))
+    cnt = np.zeros(R.max_node, np.int32)
+    par = np.zeros(4 * R.max_node, np.int32)
+    R.L.refh_constr(_p(cnt), _p(par))
+    k = lognormal_k(R.max_el, seed=seed)
+    R.set_coeffs(k=k, f=1.0, g=0.0)
+    fid, fbc, fel = R.bc_faces()
+    side = np.zeros(fid.size, np.int32)
+    R.L.refh_bc_face_sides(fid.size, _p(fid), _p(fel), _p(side))
+    out = dict(n=n, jitter=jitter, seed=seed, coords=R.node_coords(), el_nodes=R.el_nodes() - 1,
+               el_status=status, k=k, con_cnt=cnt, con_par=par.reshape(-1, 4) - 1,
+               bc_face_id=fid, bc_face_bc=fbc, bc_face_el=fel - 1, bc_face_side=side)
+    # rewritten local matrices of every active element and boundary face
+    # whose dof list holds constraining vertices, with that list
+    ents, sms, rhss, dofs = [], [], [], []
+    for e in np.nonzero(status == 1)[0]:
+        K, r, d = R.int_ent_stiff(refmod.APC_ELEMENT, int(e) + 1, maxn=30)
+        if K.shape[0] > 6:
+            ents.append((refmod.APC_ELEMENT, int(e) + 1))
+            sms.append(K)
+            rhss.append(r)
+            dofs.append(d)
+    for f in fid:
+        K, r, d = R.int_ent_stiff(refmod.APC_FACE, int(f), maxn=30)
+        if K.shape[0] > 6:
+            ents.append((refmod.APC_FACE, int(f)))
+            sms.append(K)
+            rhss.append(r)
+            dofs.append(d)
+    ns = np.array([K.shape[0] for K in sms], np.int32)
+    out.update(con_ent=np.array(ents, np.int32).reshape(-1, 2), con_ns=ns,
+               con_sm=np.concatenate([K.ravel() for K in sms]), con_rhs=np.concatenate(rhss),
+               con_dofs=np.concatenate(dofs) - 1)
+    R.solver_create(mkb)
+    ll = R.level_lists()
+    R.assemble()
+    rp, ci, val, rhs = R.crs()
+    dof_of_node = np.full(R.max_node, -1, np.int32)
+    dof_of_node[ll["dof_ent_id"] - 1] = ll["dof_posglob"]
+    out.update(row_ptr=rp, col_ind=ci, crs_val=val, crs_rhs=rhs, dof_of_node=dof_of_node,
+               int_ent_type=ll["int_ent_type"], int_ent_id=ll["int_ent_id"], color_elems=ll["color_elems"],
+               color_faces=ll["color_faces"], asse_pos=ll["asse_pos"], assembly_table=ll["assembly_table"],
+               max_dofs_int_ent=R.max_dofs_int_ent)
+    sol, nit, meas, _ = R.solve(-1, -1.0)
+    xs = np.zeros(R.ndof)
+    has = dof_of_node >= 0
+    xs[dof_of_node[has]] = sol[1:R.max_node + 1][has]
+    out.update(gmres_x=xs, gmres_iters=nit, gmres_meas=meas)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}: {R.nel} active of {R.max_el} elements, {int((cnt > 0).sum())} constrained vertices "
+          f"({int((cnt == 2).sum())} mid-edge, {int((cnt == 4).sum())} mid-face), {len(ents)} rewritten "
+          f"entities, ndof {R.ndof} nnz {R.nnz} max dofs {R.max_dofs_int_ent}, gmres {nit} it", file=sys.stderr)
+
+
 def run_tets(name="std_tet_n2"):
     """Std linear tetrahedra through the reference's apr_elem_calc_3D (tetra
     base) and quadrature; no tet mesh module is linked, so the elements come
@@ -262,7 +353,7 @@ def main(argv):
     ref = os.environ.get("MODFEM_REF_SRC") or os.path.normpath(
         os.path.join(ROOT, "..", "reference", "modfem2017", "src"))
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref}"])
-    names = argv or list(CASES) + ["std_tet_n2", "dg_el_n2", "dg_el_aniso_n2"] + list(DG_ASM_CASES) + ["fields"]
+    names = argv or list(CASES) + list(HANG_CASES) + ["std_tet_n2", "dg_el_n2", "dg_el_aniso_n2"] + list(DG_ASM_CASES) + ["fields"]
     if len(names) == 1 and os.environ.get("MAKE_GOLDEN_CHILD"):
         with open(os.devnull, "w") as dn:
             # the reference prints progress on stdout; keep only our stderr summary
@@ -275,6 +366,8 @@ def main(argv):
                 run_dg_assembly(names[0])
             elif names[0] == "fields":
                 run_fields()
+            elif names[0] in HANG_CASES:
+                run_hanging(names[0])
             else:
                 run_case(names[0])
         return

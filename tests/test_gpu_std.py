@@ -312,9 +312,9 @@ def test_constrained_vertices_are_refused(gb):
     """A once-refined ModFEM mesh has constrained (hanging) vertices: they
     carry no dof, and the dof lists of their elements name the constraining
     vertices instead (apr_get_stiff_mat_data, aps_std_lin_intf.c:2995-3170),
-    so sir_create reports more dofs per entity than vertices.  The library
-    does not do the constraint rewrite; both signs of it are refused with an
-    error instead of assembling a wrong matrix."""
+    so sir_create reports more dofs per entity than vertices.  Without the
+    constraint data (gbfem_set_constraints) both signs of it are refused
+    with an error instead of assembling a wrong matrix."""
     g = load("std_n10")
     m = FixtureMesh(g)
     c = make_ctx(gb, m, g["k"])
