@@ -15,9 +15,12 @@
  * On the first call it gathers, through the module interfaces the CPU
  * element loop uses:
  *   - node coordinates (mmr_node_coor) and element vertices in
- *     mmr_el_node_coor order, elements and nodes numbered 1..max id with no
- *     gaps (an unrefined mesh; a refined one has constrained vertices, which
- *     the library refuses);
+ *     mmr_el_node_coor order for every element and node id 1..max id
+ *     (refined parents included: only active elements are in the entity
+ *     lists; meshes refined without derefinement leave no free ids);
+ *   - the constrained (hanging) vertices of a refined mesh, the vertices
+ *     without a dof (apr_get_ent_pdeg == 0), with their constraining
+ *     vertices from apr_get_constr_data;
  *   - the boundary faces with a Dirichlet flag (pdr_get_bc_type), their first
  *     neighbour and its side (mmr_fa_eq_neig);
  *   - the CRS structure of MKB's matrix;
@@ -36,6 +39,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 
+#include "aph_intf.h"
 #include "lah_crs.h"
 #include "mmh_intf.h"
 #include "pdh_control_intf.h"
@@ -97,6 +101,26 @@ static int gbs_setup(int Problem_id)
   if (gbfem_create(&gbs_ctx, 0) < 0) return gbs_fail("gbfem_create");
   if (gbfem_set_mesh(gbs_ctx, nno, xyz, nel, GBFEM_PRISM, el, nbf, fid, fel, fside, fbc) < 0)
     return gbs_fail("gbfem_set_mesh");
+  {
+    const int field_id = pdr_ctrl_i_params(Problem_id, 3);
+    int *cv = malloc(sizeof(int) * (size_t)nno), *cn = malloc(sizeof(int) * (size_t)nno);
+    int *cp = malloc(4 * sizeof(int) * (size_t)nno), nc = 0, rc;
+    if (!cv || !cn || !cp) return -1;
+    for (i = 1; i <= nno; i++) {
+      int constr[5];
+      if (mmr_node_status(mesh_id, i) != MMC_ACTIVE || apr_get_ent_pdeg(field_id, APC_VERTEX, i) != 0) continue;
+      apr_get_constr_data(field_id, i, APC_VERTEX, constr, NULL);
+      cv[nc] = i - 1;
+      cn[nc] = constr[0];
+      for (j = 0; j < 4; j++) cp[4 * nc + j] = j < constr[0] ? constr[j + 1] - 1 : -1;
+      nc++;
+    }
+    rc = gbfem_set_constraints(gbs_ctx, nc, cv, cn, cp);
+    free(cv);
+    free(cn);
+    free(cp);
+    if (rc < 0) return gbs_fail("gbfem_set_constraints");
+  }
   {
     itt_crs_matrices *m = gbs_matrix();
     if (gbfem_set_crs_structure(gbs_ctx, m->Nrdofgl, NULL, m->Nnz, m->crs_row_ptr, m->crs_col_ind) < 0)
