@@ -93,7 +93,12 @@ int gbfem_version(void) { return 1; }
 
 const char *gbfem_last_error(void) { return gbfem::g_err.c_str(); }
 
-int gbfem_create(gbfem_ctx *ctx, int device) {
+int gbfem_create(gbfem_ctx *ctx, int device) { return gbfem::create_context(ctx, device, 0); }
+
+}  // extern "C"
+
+// A context whose stream has the given CUDA priority (0: the default).
+int gbfem::create_context(gbfem_ctx *ctx, int device, int priority) {
   GB_CHECK(ctx != nullptr, "null context pointer");
   int ndev = 0;
   GB_CUDA(cudaGetDeviceCount(&ndev));
@@ -101,7 +106,7 @@ int gbfem_create(gbfem_ctx *ctx, int device) {
   GB_CUDA(cudaSetDevice(device));
   gbfem_ctx c = new gbfem_ctx_s();
   c->device = device;
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, priority) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       cudaEventCreate(&c->ev2) != cudaSuccess || cudaEventCreate(&c->ev3) != cudaSuccess) {
     delete c;
@@ -126,6 +131,8 @@ int gbfem_create(gbfem_ctx *ctx, int device) {
   *ctx = c;
   return 0;
 }
+
+extern "C" {
 
 int gbfem_destroy(gbfem_ctx c) {
   if (!c) return 0;

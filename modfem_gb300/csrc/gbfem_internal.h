@@ -99,6 +99,8 @@ void color_entities(int nent, int nv, const std::vector<int> &ent_dofs, int nd, 
                     std::vector<int> &perm);
 
 // kernel launchers (return the number of kernels launched, < 0 on error)
+// gbfem_create with a CUDA stream priority for the context's stream
+int create_context(gbfem_ctx *ctx, int device, int priority);
 int launch_prism_elements(cudaStream_t st, bool atomic, bool aniso, int count, const int *ent_el,
                           int el_base, const int *ent_pos, int nel, const int *el_nodes,
                           const double *xyz, const double *k_el, const double *D_el, double f,

@@ -360,6 +360,7 @@ struct SrvRequest {
   int status = 0;  // 0 queued, 1 preparing, 2 ready, 3 solving, 4 done, -1 failed, -2 cancelled
   bool cancel = false;  // cancellation asked while preparing or solving
   bool solo = false;    // large std request: solved alone by its preparation worker
+  bool solo_admit = false;  // admitted as a solo request, outside the lane's slots
   std::string err;
   gbfem_ctx ctx = nullptr;
   DevBuf<double> kry;
@@ -438,6 +439,7 @@ struct gbfem_server_s {
   int steps_per_poll = 4;
   int inject_prep_failures = 0;  // GBFEM_SERVE_OPT_FAIL_PREPARATIONS
   int solo_dofs = 40000;         // GBFEM_SERVE_OPT_SOLO_DOFS
+  int prio_std = 0;              // stream priority of std requests' contexts (the greatest)
   std::string fatal;
 };
 
@@ -478,6 +480,30 @@ void reaper_loop(gbfem_server s) {
 // has nobody waiting; the HBM budget is shared.
 void try_admit(gbfem_server s) {  // caller holds s->mu
   const int share = std::max(1, s->max_active / 2);
+  // std requests of at least solo_dofs dofs (one per vertex) are solved by
+  // their preparation worker on their own stream, not in the engine's
+  // lanes: they take no lane slot, only their share of the HBM budget
+  if (s->solo_dofs > 0) {
+    auto &q = s->lanes[0].waitq;
+    for (auto it = q.begin(); it != q.end();) {
+      ReqPtr r = *it;
+      if (r->nno < s->solo_dofs) {
+        ++it;
+        continue;
+      }
+      if (s->in_use + r->footprint > s->budget && s->in_use > 0) break;
+      it = q.erase(it);
+      r->solo_admit = true;
+      s->in_use += r->footprint;
+      r->charged = r->footprint;
+      s->peak_in_use = std::max(s->peak_in_use, s->in_use);
+      r->status = 1;
+      r->t_admit = now_s();
+      s->n_preparing++;
+      s->prepq.push_back(r);
+      s->cv_prep.notify_one();
+    }
+  }
   for (int L = 0; L < 2; L++) {
     SrvLane &ln = s->lanes[L], &other = s->lanes[1 - L];
     while (!ln.waitq.empty()) {
@@ -511,7 +537,9 @@ int prepare(gbfem_server s, SrvRequest &r) {
     }
   }
   gbfem_ctx c = nullptr;
-  int rc = gbfem_create(&c, s->device);
+  // std requests' preparation and solo solves at the std lane's priority:
+  // the DG lane's long block SpMVs (lowest priority) do not hold them up
+  int rc = gbfem::create_context(&c, s->device, r.kind == 0 ? s->prio_std : 0);
   if (rc < 0) return rc;
   r.ctx = c;
   std::vector<int> fid, fbc;
@@ -537,7 +565,7 @@ int prepare(gbfem_server s, SrvRequest &r) {
     r.n = nd;
     {
       std::lock_guard<std::mutex> lk(s->mu);
-      r.solo = s->solo_dofs > 0 && nd >= s->solo_dofs;
+      r.solo = r.solo_admit || (s->solo_dofs > 0 && nd >= s->solo_dofs);
     }
     if (r.solo) {
       // solved by the preparation worker with the device-resident GMRES
@@ -613,7 +641,7 @@ void prep_worker(gbfem_server s) {
       s->in_use -= r->charged;
       r->charged = 0;
       r->t_done = now_s();
-      s->lanes[r->kind].held--;
+      if (!r->solo_admit) s->lanes[r->kind].held--;
       try_admit(s);
       s->cv_done.notify_all();
       continue;
@@ -641,7 +669,7 @@ void prep_worker(gbfem_server s) {
       if (r->cancel && it >= 0) r->err = "cancelled";
       r->t_done = now_s();
       s->n_active--;
-      s->lanes[r->kind].held--;
+      if (!r->solo_admit) s->lanes[r->kind].held--;
       try_admit(s);
       s->cv_done.notify_all();
       continue;
@@ -968,6 +996,7 @@ int gbfem_server_create(gbfem_server *out, int device, long long hbm_budget, int
   // block scheduler starts std blocks first
   int prio_least = 0, prio_greatest = 0;
   cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  s->prio_std = prio_greatest;
   for (int L = 0; L < 2 && ok; L++) {
     SrvLane &ln = s->lanes[L];
     ok = cudaStreamCreateWithPriority(&ln.stream, cudaStreamNonBlocking, L == 0 ? prio_greatest : prio_least) ==
@@ -1157,7 +1186,7 @@ int gbfem_server_cancel(gbfem_server s, long long id) {
     r->kry.release();
     s->in_use -= r->charged;
     r->charged = 0;
-    s->lanes[r->kind].held--;
+    if (!r->solo_admit) s->lanes[r->kind].held--;
     try_admit(s);
   } else {  // preparing or solving: its worker or the engine retires it
     r->cancel = true;
