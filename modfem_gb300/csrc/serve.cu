@@ -13,13 +13,16 @@
 //  * admission: FIFO per lane; a request starts when its lane has a free slot
 //    (half of max_active, or more while the other lane has nobody waiting)
 //    and its estimated device footprint fits in the shared HBM budget
-//    (replaced by the measured footprint once it is built);
-//  * preparation (worker threads, one CUDA stream each; std requests taken
-//    before DG ones): upload, structure (built and coloured on the device for
-//    std requests), integrate + assemble, preconditioner; overlaps with the
-//    solves running.  Std requests of GBFEM_SERVE_OPT_SOLO_DOFS dofs or more
-//    are then solved by their worker, alone on their stream, with the
-//    device-resident GMRES of gbfem_solve;
+//    (replaced by the measured footprint once it is built).  Std requests of
+//    GBFEM_SERVE_OPT_SOLO_DOFS dofs or more never enter the engine's lanes:
+//    they are admitted on the budget alone;
+//  * preparation (worker threads, one CUDA stream each, std requests' at the
+//    highest priority; solo-sized std requests taken first, then the other
+//    std ones, then DG): upload, structure (built and coloured on the device
+//    for std requests), integrate + assemble, preconditioner; overlaps with
+//    the solves running.  Solo-sized requests are then solved by one of two
+//    solo threads, alone on their stream, with the device-resident GMRES of
+//    gbfem_solve;
 //  * solve (engine thread, one stream per lane): every step of a lane
 //    advances each of its active requests by one GMRES iteration with
 //    batched kernels over all of them - one CRS SpMV launch for all std
@@ -359,7 +362,7 @@ struct SrvRequest {
   double t_submit = 0, t_admit = 0, t_ready = 0, t_start = 0, t_done = 0;
   int status = 0;  // 0 queued, 1 preparing, 2 ready, 3 solving, 4 done, -1 failed, -2 cancelled
   bool cancel = false;  // cancellation asked while preparing or solving
-  bool solo = false;    // large std request: solved alone by its preparation worker
+  bool solo = false;    // large std request: solved alone by a solo thread
   bool solo_admit = false;  // admitted as a solo request, outside the lane's slots
   std::string err;
   gbfem_ctx ctx = nullptr;
@@ -412,8 +415,12 @@ struct gbfem_server_s {
   long long budget = 0, in_use = 0, peak_in_use = 0;
   int max_active = 0;
   std::mutex mu;
-  std::condition_variable cv_engine, cv_prep, cv_done;
+  std::condition_variable cv_engine, cv_prep, cv_done, cv_solo;
   std::deque<ReqPtr> prepq, readyq;
+  // prepared solo requests, solved by the solo threads (so that a long solve
+  // does not hold a preparation worker)
+  std::deque<ReqPtr> soloq;
+  std::vector<std::thread> solo_workers;
   std::map<long long, ReqPtr> reqs;
   long long next_id = 0;
   int n_preparing = 0, n_active = 0;
@@ -621,9 +628,13 @@ void prep_worker(gbfem_server s) {
       std::unique_lock<std::mutex> lk(s->mu);
       s->cv_prep.wait(lk, [&] { return s->stop || !s->prepq.empty(); });
       if (s->prepq.empty()) return;
-      // std requests first (their preparation is short and their solve
-      // is latency bound), in admission order; then DG in admission order
-      auto it = std::find_if(s->prepq.begin(), s->prepq.end(), [](const ReqPtr &q) { return q->kind == 0; });
+      // solo-sized std requests first (the longest latency-bound path:
+      // preparation, then a device GMRES of hundreds of iterations), then
+      // the other std requests (short preparation, latency-bound solve),
+      // then DG, each in admission order
+      auto it = std::find_if(s->prepq.begin(), s->prepq.end(), [](const ReqPtr &q) { return q->solo_admit; });
+      if (it == s->prepq.end())
+        it = std::find_if(s->prepq.begin(), s->prepq.end(), [](const ReqPtr &q) { return q->kind == 0; });
       if (it == s->prepq.end()) it = s->prepq.begin();
       r = *it;
       s->prepq.erase(it);
@@ -647,31 +658,10 @@ void prep_worker(gbfem_server s) {
       continue;
     }
     if (r->solo) {
-      // a large std request: its own stream and restart-cycle graph
-      // (gbfem_solve's device GMRES), beside the engine's batched lanes;
-      // the estimate (which includes the Krylov space) stays charged
-      s->n_active++;
+      // a large std request: solved by a solo thread on its own stream
       r->status = 3;
-      r->t_start = now_s();
-      lk.unlock();
-      r->x.assign(r->n, 0.0);
-      double res = 0.0, rel = 0.0;
-      const int it = gbfem::gmres_device_std(r->ctx, r->krylov, r->max_iter, r->tol, 1, r->x.data(), &res, &rel);
-      const std::string err = it < 0 ? std::string(gbfem_last_error()) : std::string();
-      reap(s, *r);
-      lk.lock();
-      r->iters = it < 0 ? 0 : it;
-      r->rel = rel;
-      s->in_use -= r->charged;
-      r->charged = 0;
-      r->status = it < 0 ? -1 : (r->cancel ? -2 : 4);
-      if (it < 0) r->err = err;
-      if (r->cancel && it >= 0) r->err = "cancelled";
-      r->t_done = now_s();
-      s->n_active--;
-      if (!r->solo_admit) s->lanes[r->kind].held--;
-      try_admit(s);
-      s->cv_done.notify_all();
+      s->soloq.push_back(r);
+      s->cv_solo.notify_one();
       continue;
     }
     // replace the estimate by what the request holds
@@ -683,6 +673,48 @@ void prep_worker(gbfem_server s) {
     s->readyq.push_back(r);
     s->cv_engine.notify_one();
     try_admit(s);
+  }
+}
+
+// Solo requests (large std): gbfem_solve's device GMRES on the request's own
+// stream and restart-cycle graph, beside the engine's batched lanes; the
+// estimate (which includes the Krylov space) stays charged until done.
+void solo_worker(gbfem_server s) {
+  cudaSetDevice(s->device);
+  for (;;) {
+    ReqPtr r;
+    bool skip = false;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv_solo.wait(lk, [&] { return s->stop || !s->soloq.empty(); });
+      if (s->soloq.empty()) return;
+      r = s->soloq.front();
+      s->soloq.pop_front();
+      s->n_active++;
+      r->t_start = now_s();
+      skip = r->cancel;
+    }
+    r->x.assign(r->n, 0.0);
+    double res = 0.0, rel = 0.0;
+    // (cancelled while queued here: not solved)
+    const int it = skip ? 0
+                        : gbfem::gmres_device_std(r->ctx, r->krylov, r->max_iter, r->tol, 1, r->x.data(), &res,
+                                                       &rel);
+    const std::string err = it < 0 ? std::string(gbfem_last_error()) : std::string();
+    reap(s, *r);
+    std::lock_guard<std::mutex> lk(s->mu);
+    r->iters = it < 0 ? 0 : it;
+    r->rel = rel;
+    s->in_use -= r->charged;
+    r->charged = 0;
+    r->status = it < 0 ? -1 : (r->cancel ? -2 : 4);
+    if (it < 0) r->err = err;
+    if (r->cancel && it >= 0) r->err = "cancelled";
+    r->t_done = now_s();
+    s->n_active--;
+    if (!r->solo_admit) s->lanes[r->kind].held--;
+    try_admit(s);
+    s->cv_done.notify_all();
   }
 }
 
@@ -1021,6 +1053,7 @@ int gbfem_server_create(gbfem_server *out, int device, long long hbm_budget, int
   memset(s->h_desc, 0, sizeof(SrvDesc) * gbfem::SRV_MAXSLOTS);
   cudaMemset(s->d_state.p, 0, sizeof(SrvState) * gbfem::SRV_MAXSLOTS);
   for (int i = 0; i < prep_threads; i++) s->workers.emplace_back(prep_worker, s);
+  for (int i = 0; i < 2; i++) s->solo_workers.emplace_back(solo_worker, s);
   s->engine = std::thread(engine_loop, s);
   s->reaper = std::thread(reaper_loop, s);
   *out = s;
@@ -1037,6 +1070,9 @@ int gbfem_server_destroy(gbfem_server s) {
   s->cv_prep.notify_all();
   s->cv_engine.notify_all();
   for (auto &t : s->workers) t.join();
+  // the solo threads solve what is queued for them, then return
+  s->cv_solo.notify_all();
+  for (auto &t : s->solo_workers) t.join();
   // the engine finishes the requests it holds, then returns
   if (s->engine.joinable()) s->engine.join();
   {
