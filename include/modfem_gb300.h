@@ -490,7 +490,8 @@ int gbfem_batch_get(gbfem_batch batch, double *vals, double *rhs);
  * own stream (std requests before DG ones) while the engine thread advances
  * each lane's requests in the solve phase together, one GMRES iteration per
  * step with batched kernels and the GMRES scalar logic on the device; large
- * std requests are solved by their worker instead (GBFEM_SERVE_OPT_SOLO_DOFS).  A request's
+ * std requests are solved alone on their own stream instead
+ * (GBFEM_SERVE_OPT_SOLO_DOFS, GBFEM_SERVE_OPT_STD_PRECEDENCE).  A request's
  * result does not depend on the other requests in the mix (bit-identical
  * alone and together).  The numerics per request are those of
  * gbfem_assemble + gbfem_solve (std) and gbfem_dg_assemble + gbfem_dg_solve
@@ -549,12 +550,19 @@ int gbfem_server_cancel(gbfem_server srv, long long id);
 #define GBFEM_SERVE_OPT_STEPS_PER_POLL 1
 #define GBFEM_SERVE_OPT_FAIL_PREPARATIONS 2
 /* GBFEM_SERVE_OPT_SOLO_DOFS: std requests with at least this many dofs
- * (default 40,000; 0: none) are not batched into the engine's steps: their
- * preparation worker solves them alone with gbfem_solve's device-resident
+ * (default 40,000; 0: none) are not batched into the engine's steps: they
+ * are admitted on the HBM budget alone (no lane slot), prepared first, and
+ * solved by one of two solo threads with gbfem_solve's device-resident
  * GMRES (sliced-ELL SpMV, restart cycles as a CUDA graph) on the request's
- * own stream, beside the batched lanes.  Same stopping rule; the result does
- * not depend on the other requests either way. */
+ * own highest-priority stream, beside the batched lanes.  Same stopping
+ * rule; the result does not depend on the other requests either way. */
 #define GBFEM_SERVE_OPT_SOLO_DOFS 3
+/* GBFEM_SERVE_OPT_STD_PRECEDENCE: 1 (default): while a solo-sized std
+ * request is being prepared or solved, the engine launches no new DG-lane
+ * steps (DG steps already in flight finish), so the large latency-bound std
+ * requests have the GPU to themselves and the DG requests, whose solves run
+ * for seconds, wait for those windows; 0: both lanes always step. */
+#define GBFEM_SERVE_OPT_STD_PRECEDENCE 4
 int gbfem_server_set_option(gbfem_server srv, int option, long long value);
 /* stats[8]: engine steps, kernel launches, peak active requests, peak
  * bytes charged, budget, bytes charged now, queued, active. */

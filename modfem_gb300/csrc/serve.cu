@@ -44,6 +44,7 @@
 // change of that set as a CUDA graph and replayed every step.
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -446,6 +447,8 @@ struct gbfem_server_s {
   int steps_per_poll = 4;
   int inject_prep_failures = 0;  // GBFEM_SERVE_OPT_FAIL_PREPARATIONS
   int solo_dofs = 40000;         // GBFEM_SERVE_OPT_SOLO_DOFS
+  int std_precedence = 1;        // GBFEM_SERVE_OPT_STD_PRECEDENCE
+  std::atomic<int> n_solo{0};    // solo requests admitted and not finished
   int prio_std = 0;              // stream priority of std requests' contexts (the greatest)
   std::string fatal;
 };
@@ -501,6 +504,7 @@ void try_admit(gbfem_server s) {  // caller holds s->mu
       if (s->in_use + r->footprint > s->budget && s->in_use > 0) break;
       it = q.erase(it);
       r->solo_admit = true;
+      s->n_solo++;
       s->in_use += r->footprint;
       r->charged = r->footprint;
       s->peak_in_use = std::max(s->peak_in_use, s->in_use);
@@ -653,6 +657,7 @@ void prep_worker(gbfem_server s) {
       r->charged = 0;
       r->t_done = now_s();
       if (!r->solo_admit) s->lanes[r->kind].held--;
+      if (r->solo_admit) s->n_solo--;
       try_admit(s);
       s->cv_done.notify_all();
       continue;
@@ -713,6 +718,7 @@ void solo_worker(gbfem_server s) {
     r->t_done = now_s();
     s->n_active--;
     if (!r->solo_admit) s->lanes[r->kind].held--;
+    if (r->solo_admit) s->n_solo--;
     try_admit(s);
     s->cv_done.notify_all();
   }
@@ -975,6 +981,8 @@ void engine_loop(gbfem_server s) {
         ln.changed = false;
       }
       if (ln.act.empty()) continue;
+      // std precedence: no new DG steps while a solo request is in flight
+      if (L == 1 && s->std_precedence && s->n_solo.load() > 0) continue;
       // several steps per poll: a finished request's kernels are no-ops until
       // it is retired, so the extra steps only cost their launch
       cudaError_t ge = cudaSuccess;
@@ -1257,6 +1265,12 @@ int gbfem_server_set_option(gbfem_server s, int option, long long value) {
     GB_CHECK(value >= 0 && value <= 2000000000LL, "solo threshold out of range");
     std::lock_guard<std::mutex> lk(s->mu);
     s->solo_dofs = (int)value;
+    return 0;
+  }
+  if (option == GBFEM_SERVE_OPT_STD_PRECEDENCE) {
+    GB_CHECK(value == 0 || value == 1, "std precedence is 0 or 1");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->std_precedence = (int)value;
     return 0;
   }
   if (option == GBFEM_SERVE_OPT_FAIL_PREPARATIONS) {

@@ -106,6 +106,16 @@ class Server:
         (GBFEM_SERVE_OPT_FAIL_PREPARATIONS; host-side fault injection)."""
         self._check(self.L.gbfem_server_set_option(self._h, 2, int(count)))
 
+    def set_std_precedence(self, on):
+        """GBFEM_SERVE_OPT_STD_PRECEDENCE: no new DG steps while a solo-sized
+        std request is prepared or solved (default on)."""
+        self._check(self.L.gbfem_server_set_option(self._h, 4, int(bool(on))))
+
+    def set_solo_dofs(self, n):
+        """GBFEM_SERVE_OPT_SOLO_DOFS: the size from which std requests are
+        solved alone on their own stream (0: never)."""
+        self._check(self.L.gbfem_server_set_option(self._h, 3, int(n)))
+
     def stats(self):
         st = np.zeros(8, np.int64)
         self._check(self.L.gbfem_server_stats(self._h, st.ctypes.data))

@@ -244,3 +244,24 @@ def test_large_std_request_solved_alone_on_its_stream(gb):
     c.close()
     assert abs(it - ia) <= 1
     assert np.max(np.abs(x - xa)) <= 1e-6 * np.max(np.abs(x))
+
+
+def test_std_precedence_and_solo_threshold_keep_results(gb):
+    """Scheduling policies change when work runs, not what it computes: a
+    mix with a solo-sized std request (threshold lowered so that the 11^3
+    mesh qualifies) gives every request the same bits with the DG lane held
+    back during the solo windows (default) and without."""
+    from modfem_gb300.serve import Server
+    probs = _problems()
+    out = []
+    for prec in (1, 0):
+        srv = Server(0, max_active=16, prep_threads=4)
+        try:
+            srv.set_solo_dofs(1500)  # the 11^3 x 2 request (1,728 dofs) is solved alone
+            srv.set_std_precedence(prec)
+            out.append(_serve(srv, probs, True))
+        finally:
+            srv.close()
+    for (xa, ia, ra, _), (xb, ib, rb, _) in zip(*out):
+        assert ia == ib and np.array_equal(xa, xb)
+        assert ra < 1e-8
