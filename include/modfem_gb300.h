@@ -40,6 +40,9 @@ typedef struct gbfem_ctx_s *gbfem_ctx;
 /* scatter modes of gbfem_assemble */
 #define GBFEM_SCATTER_ATOMIC 0 /* one launch, FP64 atomics (summation order varies) */
 #define GBFEM_SCATTER_COLOR 1  /* one launch per colour, plain adds (deterministic) */
+#define GBFEM_SCATTER_GATHER 2 /* local matrices stored, then one thread a row sums them over
+                                  the incident elements in element order (deterministic, no
+                                  colouring; std prisms, FP64 element arithmetic) */
 
 /* ---------------------------------------------------------------------- */
 /* context                                                                  */
@@ -172,10 +175,12 @@ int gbfem_build_structure(gbfem_ctx ctx, int *ndof, long long *nnz, int *nr_colo
 /* The same structure built on the device (first-appearance ranks by an
  * atomicMin and a scan, incidence lists, per-row sorted unique columns,
  * binary-searched tables): identical arrays, no host pass over the mesh.
- * Also colours the elements on the device (Jones-Plassmann with hashed
- * priorities: deterministic, more colours than the host's first-fit walk)
- * and the boundary faces on the host, so both scatter modes of
- * gbfem_assemble work; the colour-batched one sums in a fixed order. */
+ * The boundary faces are coloured on the host; the elements are coloured on
+ * the device by the first colour-batched gbfem_assemble (Jones-Plassmann
+ * with hashed priorities: deterministic, more colours than the host's
+ * first-fit walk), and the gather scatter builds its DOF -> element
+ * incidence on its first call, so all scatter modes work after either
+ * build; the colour and gather modes sum in a fixed order. */
 int gbfem_build_structure_device(gbfem_ctx ctx, int *ndof, long long *nnz);
 /* Copies the structure out (any pointer may be NULL). */
 int gbfem_get_crs_structure(gbfem_ctx ctx, int *dof_of_node, int *row_ptr, int *col_ind);
@@ -209,7 +214,8 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx ctx, int Level_id, int Comp_type,
                                     double *crs_val, double *rhs);
 
 /* Device-resident integrate + assemble with the tables gbfem_build_structure
- * made (no host transfers): clears and fills the device CRS values and rhs. */
+ * made (no host transfers): clears and fills the device CRS values and rhs.
+ * scatter_mode: GBFEM_SCATTER_ATOMIC, _COLOR or _GATHER (see above). */
 int gbfem_assemble(gbfem_ctx ctx, int scatter_mode);
 /* Copies the device CRS values / rhs to host arrays (either may be NULL). */
 int gbfem_get_matrix(gbfem_ctx ctx, double *crs_val, double *rhs);

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "libmodfem_gb300.so")
 
 ELEMENT, FACE = 4, 3
 COMP_SM, COMP_RHS, COMP_BOTH = 1, 2, 3
-SCATTER_ATOMIC, SCATTER_COLOR = 0, 1
+SCATTER_ATOMIC, SCATTER_COLOR, SCATTER_GATHER = 0, 1, 2
 OPT_CACHE_TABLES = 1
 OPT_STD_ARITH = 2
 OPT_DG_SPMV_ARITH = 3

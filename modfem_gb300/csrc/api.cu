@@ -537,6 +537,8 @@ int gbfem_build_structure(gbfem_ctx c, int *ndof, long long *nnz, int *nr_colors
   GB_TRY(upload(c, c->fa_perm, c->hs.fa_perm.data(), c->hs.fa_perm.size()));
   c->h_el_color_ptr = c->hs.el_color_ptr;
   c->h_fa_color_ptr = c->hs.fa_color_ptr;
+  c->el_colour_pending = false;
+  c->have_inc = false;
   GB_TRY(alloc_matrix(c));
   forget_dropin_tables(c);
   c->have_structure = c->have_tables = true;
@@ -558,8 +560,11 @@ int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
   int nd = 0;
   long long nz = 0;
   GB_TRY(gbfem::build_device_structure(c->stream, c->nno, c->nel, c->nv, c->el_nodes.p, c->dof_of_node, c->row_ptr,
-                                       c->col_ind, c->el_table, c->err.p, &nd, &nz, &c->el_perm,
-                                       &c->h_el_color_ptr));
+                                       c->col_ind, c->el_table, c->err.p, &nd, &nz));
+  // the element colouring is made by the first colour scatter that needs it
+  c->h_el_color_ptr.clear();
+  c->el_colour_pending = true;
+  c->have_inc = false;
   c->ndof = nd;
   c->nnz = nz;
   // the host copies (for the getters and the drop-in's chunked download) are
@@ -575,11 +580,16 @@ int gbfem_build_structure_device(gbfem_ctx c, int *ndof, long long *nnz) {
   // their elements, as the host build does
   c->h_fa_color_ptr.clear();
   if (c->nfa > 0) {
-    GB_TRY(fetch_host_structure(c));
+    // only the dof of each node is needed here (the other host copies stay
+    // on the device until something asks for them)
+    std::vector<int> dn(c->nno);
+    GB_CUDA(cudaMemcpyAsync(dn.data(), c->dof_of_node.p, (size_t)c->nno * sizeof(int), cudaMemcpyDeviceToHost,
+                            c->stream));
+    GB_CUDA(cudaStreamSynchronize(c->stream));
     std::vector<int> fa_dofs((size_t)c->nfa * c->nv), perm;
     for (int f = 0; f < c->nfa; f++)
       for (int j = 0; j < c->nv; j++)
-        fa_dofs[(size_t)f * c->nv + j] = c->hs.dof_of_node[c->h_el_nodes[(size_t)c->h_fa_el[f] * c->nv + j]];
+        fa_dofs[(size_t)f * c->nv + j] = dn[c->h_el_nodes[(size_t)c->h_fa_el[f] * c->nv + j]];
     gbfem::color_entities(c->nfa, c->nv, fa_dofs, nd, c->h_fa_color_ptr, perm);
     GB_TRY(upload(c, c->fa_perm, perm.data(), perm.size()));
   }
@@ -617,8 +627,9 @@ static int check_err_flag(gbfem_ctx c) {
   GB_CUDA(cudaStreamSynchronize(c->stream));
   if (h) {
     cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream);
-    set_error(h == 1 ? "integration entity list names an element outside the mesh"
-                     : "integration entity list names a face that is not a boundary face of the mesh");
+    set_error(h == 1   ? "integration entity list names an element outside the mesh"
+              : h == 9 ? "the element incidence does not match the element tables"
+                       : "integration entity list names a face that is not a boundary face of the mesh");
     return -3;
   }
   return 0;
@@ -1002,9 +1013,25 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
   GB_CHECK(c->ncon == 0, "constrained vertices: assemble through gbfem_create_assemble_stiff_mat with the "
                          "caller's tables");
   GB_CHECK(c->nv == GBFEM_PRISM || !c->aniso, "std tetrahedra take an isotropic k_el (tensors: prisms and DG)");
-  GB_CHECK(scatter_mode == GBFEM_SCATTER_ATOMIC || scatter_mode == GBFEM_SCATTER_COLOR, "bad scatter mode");
+  GB_CHECK(scatter_mode == GBFEM_SCATTER_ATOMIC || scatter_mode == GBFEM_SCATTER_COLOR ||
+               scatter_mode == GBFEM_SCATTER_GATHER,
+           "bad scatter mode");
+  GB_CHECK(scatter_mode != GBFEM_SCATTER_GATHER || (c->nv == GBFEM_PRISM && !c->std_dword),
+           "the gather scatter takes std prisms in FP64 element arithmetic");
   GB_CUDA(cudaSetDevice(c->device));
   const bool atomic = scatter_mode == GBFEM_SCATTER_ATOMIC;
+  const bool gather = scatter_mode == GBFEM_SCATTER_GATHER;
+  if (!atomic && !c->have_inc && (gather || c->el_colour_pending)) {
+    GB_TRY(gbfem::build_device_incidence(c->stream, c->nel, c->nv, c->el_table.p, c->ndof, c->inc_ptr, c->inc));
+    c->have_inc = true;
+  }
+  if (scatter_mode == GBFEM_SCATTER_COLOR && c->el_colour_pending) {
+    GB_CUDA(cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+    GB_TRY(gbfem::build_device_colouring(c->stream, c->nel, c->nv, c->el_table.p, c->inc_ptr.p, c->inc.p,
+                                         c->el_perm, c->h_el_color_ptr, c->err.p));
+    c->el_colour_pending = false;
+  }
+  if (gather) GB_TRY(c->ek.alloc((size_t)c->nel * 42));
   cudaEventRecord(c->ev0, c->stream);
   GB_CUDA(cudaMemsetAsync(c->val.p, 0, (size_t)c->nnz * sizeof(double), c->stream));
   GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, (size_t)c->ndof * sizeof(double), c->stream));
@@ -1037,6 +1064,12 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
       r = gbfem::launch_tet_elements(c->stream, true, c->nel, nullptr, 0, nullptr, c->nel, c->el_nodes.p,
                                      c->xyz.p, c->k_el.p, c->f, c->el_table.p, c->val.p, c->rhs.p, 1, 1,
                                      c->err.p);
+    GB_TRY(r);
+    launches += r;
+  } else if (gather) {
+    r = gbfem::launch_std_gather(c->stream, c->aniso, c->nel, c->ndof, c->el_nodes.p, c->xyz.p, c->k_el.p,
+                                 c->D_el.p, c->f, c->inc_ptr.p, c->inc.p, c->el_table.p, c->ek.p, c->val.p,
+                                 c->rhs.p, c->err.p);
     GB_TRY(r);
     launches += r;
   } else {

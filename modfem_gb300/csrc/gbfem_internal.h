@@ -93,8 +93,13 @@ int build_host_structure(int nno, int nel, int nv, const int *el_nodes, int nfa,
 // for the colour-batched scatter
 int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int *el_nodes, DevBuf<int> &dof_of_node,
                            DevBuf<int> &row_ptr, DevBuf<int> &col_ind, DevBuf<int> &el_table, int *err,
-                           int *ndof_out, long long *nnz_out, DevBuf<int> *el_perm = nullptr,
-                           std::vector<int> *el_color_ptr = nullptr);
+                           int *ndof_out, long long *nnz_out);
+// DOF -> element incidence from the element tables, each list in element order
+int build_device_incidence(cudaStream_t st, int nel, int nv, const int *el_table, int nd, DevBuf<int> &inc_ptr,
+                           DevBuf<int> &inc);
+// elements-sharing-a-DOF colouring (Jones-Plassmann) from the tables and incidence
+int build_device_colouring(cudaStream_t st, int nel, int nv, const int *el_table, const int *inc_ptr,
+                           const int *inc, DevBuf<int> &el_perm, std::vector<int> &el_color_ptr, int *err);
 void color_entities(int nent, int nv, const std::vector<int> &ent_dofs, int nd, std::vector<int> &color_ptr,
                     std::vector<int> &perm);
 
@@ -111,6 +116,11 @@ int launch_prism_faces(cudaStream_t st, bool atomic, int count, const int *ent_f
                        const int *fa_el, const int *fa_side, const int *el_nodes,
                        const double *xyz, double penalty, double g, const int *tab, double *val,
                        double *rhs, int do_sm, int do_rhs, int *err);
+// Prism elements by the deterministic gather scatter: local matrices stored
+// to ek (42 doubles an element), then one thread a row over the incidence
+int launch_std_gather(cudaStream_t st, bool aniso, int nel, int nd, const int *el_nodes, const double *xyz,
+                      const double *k_el, const double *D_el, double f, const int *inc_ptr, const int *inc,
+                      const int *tab, double *ek, double *val, double *rhs, int *err);
 // Elements (faces = false, 1-based element ids) or boundary faces (mesh face
 // ids through fa_map) whose element has constrained vertices: local matrices
 // rewritten for the constraints and scattered through n x n + n tables.
@@ -286,6 +296,11 @@ struct gbfem_ctx_s {
   long long nnz = 0;
   gbfem::DevBuf<int> row_ptr, col_ind, dof_of_node;
   gbfem::DevBuf<int> el_table, el_perm, fa_perm, fa_map;
+  // the device build leaves the element colouring to the first colour
+  // scatter; the DOF -> element incidence (gather scatter) is built on demand
+  bool el_colour_pending = false, have_inc = false;
+  gbfem::DevBuf<int> inc_ptr, inc;
+  gbfem::DevBuf<double> ek;  // local matrices of the gather scatter
   std::vector<int> h_el_color_ptr, h_fa_color_ptr;
   gbfem::HostStructure hs;
   // the device build leaves the host copies in hs to be fetched on first use

@@ -18,8 +18,8 @@
 //    they are admitted on the budget alone;
 //  * preparation (worker threads, one CUDA stream each, std requests' at the
 //    highest priority; solo-sized std requests taken first, then the other
-//    std ones, then DG): upload, structure (built and coloured on the device
-//    for std requests), integrate + assemble, preconditioner; overlaps with
+//    std ones, then DG): upload, structure (built on the device for std
+//    requests), integrate + assemble, preconditioner; overlaps with
 //    the solves running.  Solo-sized requests are then solved by one of four
 //    solo threads, alone on their stream, with the device-resident GMRES of
 //    gbfem_solve;
@@ -33,7 +33,7 @@
 //    no host round trip per request; the host reads the requests' phases once
 //    per step to retire finished ones and admit new ones between steps.
 //
-// Assembly is deterministic (colour-ordered scatter for std requests, one
+// Assembly is deterministic (the gather scatter for std requests, one
 // owning thread per block entry for DG) and every request's reductions are
 // partitioned by its own size only and summed in a fixed order, so its result
 // does not depend on which other requests share the steps: a request gives
@@ -384,6 +384,7 @@ long long gbfem_serve_footprint_impl(int kind, int p, int nno, int nel, int nbf,
   if (kind == 0) {
     const long long n = nno, nnz = 27LL * nno;  // prism meshes hold about 21 entries per row
     b += 12LL * nnz + 4LL * (n + 1) + 4LL * nno + 168LL * nel + 8LL * nel + 16LL * nbf;  // CRS, tables, colours
+    b += 336LL * nel + 24LL * nel + 4LL * (n + 1);  // gather scatter: local matrices, incidence
     b += 8LL * n * (m1 + 4) + 8LL * m1 * m1;                                           // Krylov
   } else {
     const long long ns = kNs[p], n = ns * nel, blocks = nel + 2LL * nfa;
@@ -568,11 +569,12 @@ int prepare(gbfem_server s, SrvRequest &r) {
   if (r.kind == 0) {
     int nd = 0;
     long long nnz = 0;
-    // structure and element colouring on the device (deterministic)
+    // structure on the device
     if ((rc = gbfem_build_structure_device(c, &nd, &nnz)) < 0) return rc;
-    // colour-ordered scatter: the same summation order every time, so a
-    // request's matrix (and result) does not depend on when it runs
-    if ((rc = gbfem_assemble(c, GBFEM_SCATTER_COLOR)) < 0) return rc;
+    // the gather scatter: the same summation order every time (no element
+    // colouring needed), so a request's matrix (and result) does not depend
+    // on when it runs
+    if ((rc = gbfem_assemble(c, GBFEM_SCATTER_GATHER)) < 0) return rc;
     r.n = nd;
     {
       std::lock_guard<std::mutex> lk(s->mu);

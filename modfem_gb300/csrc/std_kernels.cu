@@ -436,6 +436,75 @@ __global__ void __launch_bounds__(128) tet_elements_kernel(
   }
 }
 
+// The deterministic gather scatter: each element's local matrix and load
+// vector are stored (ek[e*42 + a*6 + b] = row a, column b; ek[e*42 + 36 + a]
+// = load entry a), then one thread a row adds its row's entries over the
+// incident elements in element order, through the elements' tables.  Every
+// CRS entry and rhs row has one writer and a fixed summation order, without
+// the colouring the colour scatter needs.
+template <bool ANISO>
+__global__ void __launch_bounds__(128) prism_elements_store_kernel(
+    int nel, const int *__restrict__ el_nodes, const double *__restrict__ xyz, const double *__restrict__ k_el,
+    const double *__restrict__ D_el, double f, double *__restrict__ ek) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  const int2 *n2 = reinterpret_cast<const int2 *>(el_nodes + 6 * (size_t)e);
+  const int2 na = __ldg(n2), nb = __ldg(n2 + 1), nc = __ldg(n2 + 2);
+  d3 X[6] = {load_node(xyz, na.x), load_node(xyz, na.y), load_node(xyz, nb.x),
+             load_node(xyz, nb.y), load_node(xyz, nc.x), load_node(xyz, nc.y)};
+  double *o = ek + 42 * (size_t)e;
+  double R[6];
+  if (!ANISO) {
+    double K[21];
+    const v3 Xv[6] = {{X[0].x, X[0].y, X[0].z}, {X[1].x, X[1].y, X[1].z}, {X[2].x, X[2].y, X[2].z},
+                      {X[3].x, X[3].y, X[3].z}, {X[4].x, X[4].y, X[4].z}, {X[5].x, X[5].y, X[5].z}};
+    prism_std_element(Xv, k_el ? __ldg(k_el + e) : 1.0, f, K, R);
+    int k = 0;
+#pragma unroll
+    for (int u = 0; u < 6; u++)
+#pragma unroll
+      for (int w = u; w < 6; w++, k++) {
+        o[u * 6 + w] = K[k];
+        if (w != u) o[w * 6 + u] = K[k];
+      }
+  } else {
+    double K[36];
+    prism_element_aniso(X, D_el + 9 * (size_t)e, f, K, R);
+    // K[u * 6 + w] is (row w, column u)
+#pragma unroll
+    for (int a = 0; a < 6; a++)
+#pragma unroll
+      for (int b = 0; b < 6; b++) o[a * 6 + b] = K[b * 6 + a];
+  }
+#pragma unroll
+  for (int a = 0; a < 6; a++) o[36 + a] = R[a];
+}
+
+__global__ void __launch_bounds__(128) std_gather_kernel(int nd, int nv, const int *__restrict__ inc_ptr,
+                                                         const int *__restrict__ inc, const int *__restrict__ tab,
+                                                         const double *__restrict__ ek, double *__restrict__ val,
+                                                         double *__restrict__ rhs, int *__restrict__ err) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nd) return;
+  const int tl = nv * nv + nv;
+  double racc = 0.0;
+  for (int k = __ldg(inc_ptr + r); k < __ldg(inc_ptr + r + 1); k++) {
+    const int e = __ldg(inc + k);
+    const int *tb = tab + (size_t)e * tl;
+    int a = -1;
+    for (int j = 0; j < nv; j++)
+      if (__ldg(tb + nv * nv + j) == r) a = j;
+    if (a < 0) {  // the incidence does not match the tables
+      atomicExch(err, 9);
+      return;
+    }
+    const double *ke = ek + (size_t)e * tl + a * nv;
+    for (int b = 0; b < nv; b++) val[__ldg(tb + a + nv * b)] += __ldg(ke + b);
+    racc += __ldg(ek + (size_t)e * tl + nv * nv + a);
+  }
+  rhs[r] += racc;
+}
+
 // Elements and boundary faces whose element has constrained (hanging)
 // vertices: the local 6x6 matrix and load vector are rewritten as
 // apr_get_stiff_mat_data does (apd_std_lin/aps_std_lin_intf.c:2978-3160)
@@ -609,6 +678,20 @@ int launch_prism_faces(cudaStream_t st, bool atomic, int count, const int *ent_f
                                                             penalty, g, tab, val, rhs, do_sm, do_rhs, err);
   GB_CUDA(cudaGetLastError());
   return 1;
+}
+
+int launch_std_gather(cudaStream_t st, bool aniso, int nel, int nd, const int *el_nodes, const double *xyz,
+                      const double *k_el, const double *D_el, double f, const int *inc_ptr, const int *inc,
+                      const int *tab, double *ek, double *val, double *rhs, int *err) {
+  if (nel <= 0) return 0;
+  const int T = 128;
+  if (aniso)
+    prism_elements_store_kernel<true><<<nblk(nel, T), T, 0, st>>>(nel, el_nodes, xyz, k_el, D_el, f, ek);
+  else
+    prism_elements_store_kernel<false><<<nblk(nel, T), T, 0, st>>>(nel, el_nodes, xyz, k_el, D_el, f, ek);
+  std_gather_kernel<<<nblk(nd, T), T, 0, st>>>(nd, 6, inc_ptr, inc, tab, ek, val, rhs, err);
+  GB_CUDA(cudaGetLastError());
+  return 2;
 }
 
 int launch_prism_constrained(cudaStream_t st, bool faces, bool aniso, int count, const int *ent_id,

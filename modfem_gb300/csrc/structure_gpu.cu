@@ -15,9 +15,12 @@
 //     position found by binary search in row j, then the rhs rows
 //     (lar_fill_assembly_table_int_ent_crs, las_crs_intf.c:354-438).
 // Every output is independent of thread scheduling, so it equals the host
-// build bit for bit.  The elements-sharing-a-DOF colouring for the colour
-// scatter stays on the host (gbfem_build_structure).
+// build bit for bit.  Built on demand from the element tables (whichever
+// build made them): the DOF -> element incidence with each list in element
+// order (the deterministic gather scatter reads it), and the
+// elements-sharing-a-DOF colouring of the colour scatter.
 
+#include <algorithm>
 #include <climits>
 
 #include "gbfem_internal.h"
@@ -270,7 +273,7 @@ __device__ __forceinline__ unsigned sg_prio(int e) {
   return h;
 }
 
-__global__ void sg_jp_round(int nel, int nv, int rnd, const int *__restrict__ el_dofs,
+__global__ void sg_jp_round(int nel, int nv, int rnd, const int *__restrict__ el_dofs, int stride,
                             const int *__restrict__ inc_ptr, const int *__restrict__ inc, int *state,
                             int *remaining, int *err) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -279,7 +282,7 @@ __global__ void sg_jp_round(int nel, int nv, int rnd, const int *__restrict__ el
   unsigned long long used = 0;
   bool wins = true;
   for (int j = 0; j < nv && wins; j++) {
-    const int d = el_dofs[(size_t)e * nv + j];
+    const int d = el_dofs[(size_t)e * stride + j];
     for (int k = inc_ptr[d]; k < inc_ptr[d + 1]; k++) {
       const int f = inc[k];
       if (f == e) continue;
@@ -319,8 +322,7 @@ __global__ void sg_color_fill(int nel, const int *__restrict__ state, int *curso
 
 int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int *el_nodes, DevBuf<int> &dof_of_node,
                            DevBuf<int> &row_ptr, DevBuf<int> &col_ind, DevBuf<int> &el_table, int *err,
-                           int *ndof_out, long long *nnz_out, DevBuf<int> *el_perm,
-                           std::vector<int> *el_color_ptr) {
+                           int *ndof_out, long long *nnz_out) {
   const long long m = (long long)nel * nv;
   SgTemp<int> first(st), mark(st), rank(st), el_dofs(st), inc_cnt(st), inc_ptr(st), inc(st), len(st), tmp(st);
   auto cleanup = [&]() {
@@ -367,48 +369,100 @@ int build_device_structure(cudaStream_t st, int nno, int nel, int nv, const int 
   if (el_table.alloc((size_t)nel * (nv * nv + nv)) < 0) return fail(-1);
   sg_tables<<<(nel + 127) / 128, 128, 0, st>>>(nel, nv, el_dofs.p, row_ptr.p, col_ind.p, el_table.p);
   GB_CUDA(cudaGetLastError());
-  // 5. colouring (optional)
-  if (el_perm && el_color_ptr) {
-    // rounds in batches of SG_JP_BATCH between host reads of the last
-    // round's count of elements left (a round after the last one colours
-    // nothing and returns at once), each round with its own counter
-    constexpr int SG_JP_BATCH = 8;
-    SgTemp<int> state(st), cnt(st);
-    if (state.alloc(nel) < 0 || cnt.alloc(64 + SG_JP_BATCH) < 0 || el_perm->alloc(nel) < 0) return fail(-1);
-    sg_fill<<<(nel + 255) / 256, 256, 0, st>>>(nel, -1, state.p);
-    int remaining = nel, rnd = 0;
-    while (remaining > 0) {
-      GB_CUDA(cudaMemsetAsync(cnt.p + 64, 0, SG_JP_BATCH * sizeof(int), st));
-      for (int b = 0; b < SG_JP_BATCH; b++, rnd++)
-        sg_jp_round<<<(nel + 255) / 256, 256, 0, st>>>(nel, nv, rnd, el_dofs.p, inc_ptr.p, inc.p, state.p,
-                                                      cnt.p + 64 + b, err);
-      GB_CUDA(cudaMemcpyAsync(&remaining, cnt.p + 64 + SG_JP_BATCH - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-      GB_CUDA(cudaStreamSynchronize(st));
-      if (rnd > (1 << 22)) break;  // cannot happen: every round colours the top-priority element left
-    }
-    GB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    GB_CUDA(cudaMemsetAsync(cnt.p, 0, 64 * sizeof(int), st));
-    sg_color_count<<<(nel + 255) / 256, 256, 0, st>>>(nel, state.p, cnt.p);
-    std::vector<int> counts(64);
-    GB_CUDA(cudaMemcpyAsync(counts.data(), cnt.p, 64 * sizeof(int), cudaMemcpyDeviceToHost, st));
-    GB_CUDA(cudaStreamSynchronize(st));
-    if (herr || remaining > 0) {
-      cleanup();
-      GB_CHECK(false, "device colouring needs more than 64 colours");
-    }
-    int ncol = 64;
-    while (ncol > 0 && counts[ncol - 1] == 0) ncol--;
-    el_color_ptr->assign(ncol + 1, 0);
-    for (int c = 0; c < ncol; c++) (*el_color_ptr)[c + 1] = (*el_color_ptr)[c] + counts[c];
-    GB_CUDA(cudaMemcpyAsync(cnt.p, el_color_ptr->data(), ncol * sizeof(int), cudaMemcpyHostToDevice, st));
-    sg_color_fill<<<(nel + 255) / 256, 256, 0, st>>>(nel, state.p, cnt.p, el_perm->p);
-    GB_CUDA(cudaGetLastError());
-    GB_CUDA(cudaStreamSynchronize(st));
-  }
   GB_CUDA(cudaStreamSynchronize(st));
   cleanup();
   *ndof_out = nd;
   *nnz_out = nnz;
+  return 0;
+}
+
+
+// Incidence from the element tables (the rhs rows t[nv*nv + j] are the
+// element's dofs): count, scan, fill, then each list sorted by element.
+__global__ void sg_inc_count_tab(int nel, int nv, const int *__restrict__ table, int *cnt) {
+  const long long m = (long long)nel * nv, tl = nv * nv + nv;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x)
+    atomicAdd(cnt + table[(i / nv) * tl + nv * nv + i % nv], 1);
+}
+
+__global__ void sg_inc_fill_tab(int nel, int nv, const int *__restrict__ table, int *cursor, int *inc) {
+  const long long m = (long long)nel * nv, tl = nv * nv + nv;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x)
+    inc[atomicAdd(cursor + table[(i / nv) * tl + nv * nv + i % nv], 1)] = (int)(i / nv);
+}
+
+__global__ void sg_inc_sort(int nd, const int *__restrict__ inc_ptr, int *inc) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nd) return;
+  int *a = inc + inc_ptr[r];
+  const int n = inc_ptr[r + 1] - inc_ptr[r];
+  for (int i = 1; i < n; i++) {
+    const int v = a[i];
+    int j = i;
+    while (j > 0 && a[j - 1] > v) {
+      a[j] = a[j - 1];
+      j--;
+    }
+    a[j] = v;
+  }
+}
+
+int build_device_incidence(cudaStream_t st, int nel, int nv, const int *el_table, int nd, DevBuf<int> &inc_ptr,
+                           DevBuf<int> &inc) {
+  const long long m = (long long)nel * nv;
+  SgTemp<int> cnt(st), tmp(st);
+  if (cnt.alloc((size_t)nd + 1) < 0 || inc_ptr.alloc((size_t)nd + 1) < 0 || inc.alloc((size_t)std::max(m, 1LL)) < 0)
+    return -1;
+  const int g1 = 152 * 8;
+  GB_CUDA(cudaMemsetAsync(cnt.p, 0, ((size_t)nd + 1) * sizeof(int), st));
+  sg_inc_count_tab<<<g1, 256, 0, st>>>(nel, nv, el_table, cnt.p);
+  if (sg_scan(st, nd, cnt.p, inc_ptr.p, tmp) < 0) return -1;
+  GB_CUDA(cudaMemcpyAsync(cnt.p, inc_ptr.p, (size_t)nd * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  sg_inc_fill_tab<<<g1, 256, 0, st>>>(nel, nv, el_table, cnt.p, inc.p);
+  sg_inc_sort<<<(nd + 127) / 128, 128, 0, st>>>(nd, inc_ptr.p, inc.p);
+  GB_CUDA(cudaGetLastError());
+  // the scratch is released in stream order: nothing here waits for the device
+  return 0;
+}
+
+// The colouring of the colour scatter (Jones-Plassmann, sg_jp_round), from
+// the element tables and the incidence.
+int build_device_colouring(cudaStream_t st, int nel, int nv, const int *el_table, const int *inc_ptr,
+                           const int *inc, DevBuf<int> &el_perm, std::vector<int> &el_color_ptr, int *err) {
+  // rounds in batches of SG_JP_BATCH between host reads of the last round's
+  // count of elements left (a round after the last one colours nothing and
+  // returns at once), each round with its own counter
+  constexpr int SG_JP_BATCH = 8;
+  const int tl = nv * nv + nv;
+  const int *el_dofs = el_table + nv * nv;
+  SgTemp<int> state(st), cnt(st);
+  if (state.alloc(nel) < 0 || cnt.alloc(64 + SG_JP_BATCH) < 0 || el_perm.alloc(nel) < 0) return -1;
+  sg_fill<<<(nel + 255) / 256, 256, 0, st>>>(nel, -1, state.p);
+  int remaining = nel, rnd = 0, herr = 0;
+  while (remaining > 0) {
+    GB_CUDA(cudaMemsetAsync(cnt.p + 64, 0, SG_JP_BATCH * sizeof(int), st));
+    for (int b = 0; b < SG_JP_BATCH; b++, rnd++)
+      sg_jp_round<<<(nel + 255) / 256, 256, 0, st>>>(nel, nv, rnd, el_dofs, tl, inc_ptr, inc, state.p,
+                                                    cnt.p + 64 + b, err);
+    GB_CUDA(cudaMemcpyAsync(&remaining, cnt.p + 64 + SG_JP_BATCH - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if (rnd > (1 << 22)) break;  // cannot happen: every round colours the top-priority element left
+  }
+  GB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaMemsetAsync(cnt.p, 0, 64 * sizeof(int), st));
+  sg_color_count<<<(nel + 255) / 256, 256, 0, st>>>(nel, state.p, cnt.p);
+  std::vector<int> counts(64);
+  GB_CUDA(cudaMemcpyAsync(counts.data(), cnt.p, 64 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  GB_CHECK(!herr && remaining == 0, "device colouring needs more than 64 colours");
+  int ncol = 64;
+  while (ncol > 0 && counts[ncol - 1] == 0) ncol--;
+  el_color_ptr.assign(ncol + 1, 0);
+  for (int c = 0; c < ncol; c++) el_color_ptr[c + 1] = el_color_ptr[c] + counts[c];
+  GB_CUDA(cudaMemcpyAsync(cnt.p, el_color_ptr.data(), ncol * sizeof(int), cudaMemcpyHostToDevice, st));
+  sg_color_fill<<<(nel + 255) / 256, 256, 0, st>>>(nel, state.p, cnt.p, el_perm.p);
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
   return 0;
 }
 

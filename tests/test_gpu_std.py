@@ -465,24 +465,71 @@ def test_built_structure_and_assembly_vs_reference(gb, name):
     assert np.array_equal(rp, g["row_ptr"])
     assert np.array_equal(ci, g["col_ind"])
     sc = energy_scale(rp, ci, g["crs_val"])
-    for mode in (gb.SCATTER_ATOMIC, gb.SCATTER_COLOR):
+    for mode in (gb.SCATTER_ATOMIC, gb.SCATTER_COLOR, gb.SCATTER_GATHER):
         c.assemble(mode)
         val, rhs = c.get_matrix()
         assert crs_rel_err(rp, val, g["crs_val"], sc) < REL_TOL, mode
         assert vec_rel_err(rhs, g["crs_rhs"]) < REL_TOL, mode
 
 
-def test_color_mode_is_deterministic(gb):
+@pytest.mark.parametrize("mode", ["color", "gather"])
+def test_color_and_gather_modes_are_deterministic(gb, mode):
     from modfem_gb300.mesh import lognormal_k, structured_prism_mesh
+    md = gb.SCATTER_COLOR if mode == "color" else gb.SCATTER_GATHER
     m = structured_prism_mesh(16, jitter=0.2, seed=9)
     k = lognormal_k(m.nel, seed=9)
     c = make_ctx(gb, m, k)
     c.build_structure()
-    c.assemble(gb.SCATTER_COLOR)
+    c.assemble(md)
     v1, r1 = c.get_matrix()
-    c.assemble(gb.SCATTER_COLOR)
+    c.assemble(md)
     v2, r2 = c.get_matrix()
     assert np.array_equal(v1, v2) and np.array_equal(r1, r2)
+
+
+def test_gather_scatter_after_device_build(gb):
+    """The gather scatter (one thread a row over the incident elements in
+    element order) on a device-built structure, isotropic and anisotropic,
+    against the oracle; bit-identical on a second context (no dependence on
+    thread scheduling); the tetrahedron and double-word forms refused."""
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, structured_prism_mesh, structured_tet_mesh
+    m = structured_prism_mesh(14, jitter=0.2, seed=12)
+    k = lognormal_k(m.nel, seed=12)
+    D = anisotropic_tensors(m.nel, seed=13).reshape(-1, 9)
+    for coef in ("k", "D"):
+        outs = []
+        for _ in range(2):
+            c = gb.Context(0)
+            c.set_mesh(m)
+            if coef == "k":
+                c.set_coefficients(k=k, f=1.0, g=0.3, penalty=1e7)
+            else:
+                c.set_coefficients(D=D, f=1.0, g=0.3, penalty=1e7)
+            c.build_structure_device()
+            c.assemble(gb.SCATTER_GATHER)
+            outs.append(c.get_matrix())
+            dn, rp, ci = c.get_crs_structure()
+            c.close()
+        assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+        kw = dict(D_el=D) if coef == "D" else {}
+        vo, ro, _ = O.std_prism_assemble(m, k, dn, rp, ci, f=1.0, penalty=1e7, g=0.3, **kw)
+        so, sr, _ = O.std_prism_assemble_abs(m, k, dn, rp, ci, f=1.0, penalty=1e7, g=0.3, **kw)
+        assert crs_rel_err(rp, outs[0][0], vo, so) < REL_TOL, coef
+        assert np.max(np.abs(outs[0][1] - ro) / np.where(sr > 0, sr, 1.0)) < REL_TOL, coef
+    c = gb.Context(0)
+    c.set_mesh(m)
+    c.set_coefficients(k=k, f=1.0, g=0.0)
+    c.set_option(gb.OPT_STD_ARITH, gb.STD_DWORD)
+    c.build_structure_device()
+    with pytest.raises(gb.GbFemError, match="gather scatter"):
+        c.assemble(gb.SCATTER_GATHER)
+    c.close()
+    t = structured_tet_mesh(3, jitter=0.1, seed=2)
+    c = make_ctx(gb, t, lognormal_k(t.nel, seed=2))
+    c.build_structure()
+    with pytest.raises(gb.GbFemError, match="gather scatter"):
+        c.assemble(gb.SCATTER_GATHER)
+    c.close()
 
 
 # ------------------------------------------------------------ SpMV and GMRES
