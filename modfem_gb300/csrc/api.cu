@@ -26,6 +26,51 @@ static int upload(gbfem_ctx c, DevBuf<T> &d, const T *h, size_t n) {
   return 0;
 }
 
+// Pieces of a coordinate (b = 0) or coefficient (b = 1) upload: up_stream
+// first waits for the work queued on the context stream (which may still
+// read the old values), then copies nitems x width doubles in 8 pieces with
+// an event after each.
+static int piece_upload(gbfem_ctx c, int b, double *dst, const double *src, long long nitems, int width) {
+  if (!c->up_stream) {
+    GB_CUDA(cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking));
+    GB_CUDA(cudaEventCreateWithFlags(&c->up_now, cudaEventDisableTiming));
+    for (auto &row : c->up_ev)
+      for (auto &ev : row) GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  GB_CUDA(cudaEventRecord(c->up_now, c->stream));
+  GB_CUDA(cudaStreamWaitEvent(c->up_stream, c->up_now, 0));
+  const int P = 8;
+  const long long per = std::max(1LL, (nitems + P - 1) / P);
+  for (int p = 0; p < P; p++) {
+    const long long lo = std::min(nitems, p * per), hi = std::min(nitems, lo + per);
+    if (hi > lo)
+      GB_CUDA(cudaMemcpyAsync(dst + lo * width, src + lo * width, (size_t)(hi - lo) * width * sizeof(double),
+                              cudaMemcpyHostToDevice, c->up_stream));
+    GB_CUDA(cudaEventRecord(c->up_ev[b][p], c->up_stream));
+  }
+  c->up_np[b] = P;
+  c->up_per[b] = per;
+  c->up_pending = true;
+  return 0;
+}
+
+// The context stream waits for every piece still in flight.
+static int settle_uploads(gbfem_ctx c) {
+  if (!c->up_pending) return 0;
+  for (int b = 0; b < 2; b++)
+    if (c->up_np[b] > 0) GB_CUDA(cudaStreamWaitEvent(c->stream, c->up_ev[b][c->up_np[b] - 1], 0));
+  c->up_np[0] = c->up_np[1] = 0;
+  c->up_pending = false;
+  return 0;
+}
+
+// Before a buffer the pieces write is freed or reallocated: they are done.
+static int drain_uploads(gbfem_ctx c) {
+  GB_TRY(settle_uploads(c));
+  if (c->up_stream) GB_CUDA(cudaStreamSynchronize(c->up_stream));
+  return 0;
+}
+
 static const int kDgNs[5] = {0, 6, 18, 40, 75};
 static const int kDgTetNs[5] = {0, 4, 10, 20, 35};
 static inline bool el_is_tet(gbfem_ctx c, int e) { return c->mixed ? c->h_el_tet[e] != 0 : c->nv == GBFEM_TETRA; }
@@ -138,6 +183,19 @@ int gbfem_destroy(gbfem_ctx c) {
   if (!c) return 0;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->up_stream) {
+    cudaStreamSynchronize(c->up_stream);
+    cudaStreamDestroy(c->up_stream);
+    cudaEventDestroy(c->up_now);
+    for (auto &row : c->up_ev)
+      for (auto &ev : row)
+        if (ev) cudaEventDestroy(ev);
+  }
+  if (c->elem_stream) {
+    cudaStreamSynchronize(c->elem_stream);
+    cudaStreamDestroy(c->elem_stream);
+    cudaEventDestroy(c->elem_ev0);
+  }
   if (c->copy_stream) {
     cudaStreamSynchronize(c->copy_stream);
     cudaStreamDestroy(c->copy_stream);
@@ -284,6 +342,7 @@ int gbfem_set_mesh(gbfem_ctx c, int nno, const double *node_xyz, int nel, int nv
   GB_CHECK(nfa == 0 || (fa_el && fa_side), "face arrays missing");
   GB_CHECK(nv == GBFEM_PRISM || nfa == 0, "boundary faces are supported for prisms only");
   GB_CUDA(cudaSetDevice(c->device));
+  GB_TRY(drain_uploads(c));
   for (long long i = 0; i < (long long)nel * nv; i++)
     GB_CHECK(el_nodes[i] >= 0 && el_nodes[i] < nno, "element vertex index out of range");
   for (int f = 0; f < nfa; f++) {
@@ -296,6 +355,7 @@ int gbfem_set_mesh(gbfem_ctx c, int nno, const double *node_xyz, int nel, int nv
   c->nv = nv;
   c->nfa = nfa;
   c->mixed = false;
+  c->pipe_e0 = c->pipe_e1 = -1;  // the download plan reads the element vertices
   clear_constraints(c);
   c->h_el_tet.clear();
   c->el_nodes4.release();
@@ -324,6 +384,7 @@ int gbfem_set_mesh(gbfem_ctx c, int nno, const double *node_xyz, int nel, int nv
 int gbfem_set_mesh_mixed(gbfem_ctx c, int nno, const double *node_xyz, int nel, const int *el_nv,
                          const int *el_nodes) {
   GB_CHECK(c, "null context");
+  GB_TRY(drain_uploads(c));
   GB_CHECK(nno > 0 && nel > 0 && node_xyz && el_nodes && el_nv, "empty mesh");
   GB_CUDA(cudaSetDevice(c->device));
   std::vector<int> en((size_t)nel * 6), en4((size_t)nel * 4);
@@ -369,6 +430,9 @@ int gbfem_set_mesh_mixed(gbfem_ctx c, int nno, const double *node_xyz, int nel, 
 
 int gbfem_set_node_coords(gbfem_ctx c, const double *node_xyz) {
   GB_CHECK(c && c->nno > 0, "mesh not set");
+  GB_CHECK(node_xyz, "null coordinates");
+  if (c->cache_tables) return piece_upload(c, 0, c->xyz.p, node_xyz, c->nno, 3);
+  GB_TRY(settle_uploads(c));
   GB_CUDA(cudaMemcpyAsync(c->xyz.p, node_xyz, (size_t)c->nno * 3 * sizeof(double), cudaMemcpyHostToDevice,
                           c->stream));
   return 0;
@@ -378,16 +442,28 @@ int gbfem_set_coefficients(gbfem_ctx c, const double *k_el, const double *D_el, 
                            double penalty) {
   GB_CHECK(c && c->nel > 0, "mesh not set");
   GB_CHECK(!(k_el && D_el), "give either k_el or D_el");
+  // the buffers are kept while their sizes stay: pieces in flight into them
+  // need waiting for only when one is freed or reallocated
+  const bool keep = (k_el ? c->k_el.p && c->k_el.n >= (size_t)c->nel : !c->k_el.p) &&
+                    (D_el ? c->D_el.p && c->D_el.n >= (size_t)9 * c->nel : !c->D_el.p);
+  if (!keep) GB_TRY(drain_uploads(c));
+  if (!c->cache_tables) GB_TRY(settle_uploads(c));
   if (k_el) {
     GB_TRY(c->k_el.alloc(c->nel));
-    GB_CUDA(cudaMemcpyAsync(c->k_el.p, k_el, (size_t)c->nel * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (c->cache_tables)
+      GB_TRY(piece_upload(c, 1, c->k_el.p, k_el, c->nel, 1));
+    else
+      GB_CUDA(cudaMemcpyAsync(c->k_el.p, k_el, (size_t)c->nel * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   } else {
     c->k_el.release();
   }
   if (D_el) {
     GB_TRY(c->D_el.alloc((size_t)9 * c->nel));
-    GB_CUDA(cudaMemcpyAsync(c->D_el.p, D_el, (size_t)9 * c->nel * sizeof(double), cudaMemcpyHostToDevice,
-                            c->stream));
+    if (c->cache_tables)
+      GB_TRY(piece_upload(c, 1, c->D_el.p, D_el, c->nel, 9));
+    else
+      GB_CUDA(cudaMemcpyAsync(c->D_el.p, D_el, (size_t)9 * c->nel * sizeof(double), cudaMemcpyHostToDevice,
+                              c->stream));
     c->aniso = 1;
   } else {
     c->D_el.release();
@@ -678,10 +754,12 @@ static int ensure_side(gbfem_ctx c) {
   return 0;
 }
 static int launch_faces_beside(gbfem_ctx c, int count, const int *ent_fa, const int *fa_map, int fa_map_len,
-                               const int *ent_pos, const int *tab, int do_sm, int do_rhs, int *launches) {
+                               const int *ent_pos, const int *tab, int do_sm, int do_rhs, int *launches,
+                               cudaStream_t after = nullptr, cudaEvent_t coords_ready = nullptr) {
   GB_TRY(ensure_side(c));
-  GB_CUDA(cudaEventRecord(c->side_ev[0], c->stream));
+  GB_CUDA(cudaEventRecord(c->side_ev[0], after ? after : c->stream));
   GB_CUDA(cudaStreamWaitEvent(c->side_stream, c->side_ev[0], 0));
+  if (coords_ready) GB_CUDA(cudaStreamWaitEvent(c->side_stream, coords_ready, 0));
   const int r = gbfem::launch_prism_faces(c->side_stream, true, count, ent_fa, 0, fa_map, fa_map_len,
                                           ent_pos, c->nfa, c->fa_el.p, c->fa_side.p, c->el_nodes.p, c->xyz.p,
                                           c->penalty, c->g, tab, c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p);
@@ -724,7 +802,7 @@ __global__ void row_last_kernel(int count, const int *__restrict__ pos, const in
 // Chunks of the element range and, per chunk, the number of leading rows that
 // no later element touches (dof order by first appearance makes rows finish
 // roughly in element order); built once per cached set of tables.
-static int build_pipe_plan(gbfem_ctx c, int e0, int e1) {
+static int build_pipe_plan(gbfem_ctx c, int e0, int e1, const int *h_ent_id) {
   const int count = e1 - e0, nd = c->ndof;
   GB_TRY(c->row_last.alloc((size_t)nd));
   GB_CUDA(cudaMemsetAsync(c->row_last.p, 0xFF, (size_t)nd * sizeof(int), c->stream));
@@ -748,6 +826,22 @@ static int build_pipe_plan(gbfem_ctx c, int e0, int e1) {
   for (int k = 0; k <= K; k++) c->pipe_el[k] = (int)std::min<long long>(count, chunk * k);
   for (int k = 0; k + 1 < K; k++)
     c->pipe_rows[k] = (int)(std::upper_bound(last.begin(), last.end(), c->pipe_el[k + 1] - 1) - last.begin());
+  // the largest node and element index each chunk reads (which pieces of a
+  // coordinate / coefficient upload it waits for); ids outside the mesh are
+  // the kernel's to report
+  c->pipe_maxnode.assign(K, c->nno - 1);
+  c->pipe_maxel.assign(K, c->nel - 1);
+  for (int k = 0; k < K; k++) {
+    int mn = 0, me = 0;
+    for (int i = e0 + c->pipe_el[k]; i < e0 + c->pipe_el[k + 1]; i++) {
+      const int el = h_ent_id[i] - 1;
+      if (el < 0 || el >= c->nel) continue;
+      me = std::max(me, el);
+      for (int j = 0; j < c->nv; j++) mn = std::max(mn, c->h_el_nodes[(size_t)el * c->nv + j]);
+    }
+    c->pipe_maxnode[k] = mn;
+    c->pipe_maxel[k] = me;
+  }
   if (!c->copy_stream) {
     GB_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     for (auto &ev : c->pipe_ev) GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
@@ -892,12 +986,37 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     }
   }
   cudaEventRecord(c->ev0, c->stream);
+  const long long uploads0 = c->table_uploads;
   GB_TRY(stage_input(c, 0, c->in_id, L_int_ent_id, Nr_int_ent));
   GB_TRY(stage_input(c, 1, c->in_pos, Asse_pos_first_dof_int_ent, Nr_int_ent));
   GB_TRY(stage_input(c, 2, c->in_table, Assembly_table, tlen));
   const int do_sm = Comp_type != GBFEM_COMP_RHS, do_rhs = Comp_type != GBFEM_COMP_SM;
-  if (do_sm) GB_CUDA(cudaMemsetAsync(c->val.p, 0, (size_t)c->nnz * sizeof(double), c->stream));
-  if (do_rhs) GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, (size_t)c->ndof * sizeof(double), c->stream));
+  // with cached tables and host outputs: element chunks, each chunk's
+  // finished rows downloaded while the next chunk runs (plain meshes)
+  const bool pipe = c->cache_tables && (crs_val || rhs) && e1 > e0 && c->ncon == 0;
+  if (pipe) {
+    bool same = c->pipe_e0 == e0 && c->pipe_e1 == e1 && c->pipe_dword == c->std_dword;
+    for (int i = 0; i < 3; i++) same = same && c->pipe_key[i] == c->cache_key[i] && c->pipe_len[i] == c->cache_len[i];
+    if (!same) GB_TRY(build_pipe_plan(c, e0, e1, L_int_ent_id));
+  }
+  // coordinates / coefficients still going up in pieces (set while the
+  // tables are cached) overlap the element chunks, which run on their own
+  // stream after the work queued on the context stream and wait for the
+  // pieces they read; otherwise everything waits for the whole uploads
+  const bool overlap = pipe && c->up_pending && c->table_uploads == uploads0;
+  if (!overlap) GB_TRY(settle_uploads(c));
+  cudaStream_t est = c->stream;
+  if (overlap) {
+    if (!c->elem_stream) {
+      GB_CUDA(cudaStreamCreateWithFlags(&c->elem_stream, cudaStreamNonBlocking));
+      GB_CUDA(cudaEventCreateWithFlags(&c->elem_ev0, cudaEventDisableTiming));
+    }
+    GB_CUDA(cudaEventRecord(c->elem_ev0, c->stream));
+    GB_CUDA(cudaStreamWaitEvent(c->elem_stream, c->elem_ev0, 0));
+    est = c->elem_stream;
+  }
+  if (do_sm) GB_CUDA(cudaMemsetAsync(c->val.p, 0, (size_t)c->nnz * sizeof(double), est));
+  if (do_rhs) GB_CUDA(cudaMemsetAsync(c->rhs.p, 0, (size_t)c->ndof * sizeof(double), est));
   int launches = 0, r;
   // with constrained vertices: the entities whose element has one are split
   // off (their tables are n x n + n with the expanded lists) to the rewrite
@@ -921,17 +1040,17 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   const bool side = nff > 0;  // the faces run beside the element chunks
   if (side)
     GB_TRY(launch_faces_beside(c, nff, ff_id, c->fa_map.p, (int)c->fa_map.n, ff_pos, c->in_table.p, do_sm, do_rhs,
-                               &launches));
-  cudaEventRecord(c->ev2, c->stream);
+                               &launches, est, overlap && c->up_np[0] > 0 ? c->up_ev[0][c->up_np[0] - 1] : nullptr));
+  cudaEventRecord(c->ev2, est);
   GB_CHECK(c->nv == GBFEM_PRISM || !c->aniso, "std tetrahedra take an isotropic k_el (tensors: prisms and DG)");
   // elements a..b of the (plain) element list
   auto elements = [&](int a, int b) -> int {
     if (b <= a) return 0;
     if (c->nv == GBFEM_PRISM)
-      return gbfem::launch_prism_elements(c->stream, true, c->aniso, b - a, fe_id + a, 1, fe_pos + a, c->nel,
+      return gbfem::launch_prism_elements(est, true, c->aniso, b - a, fe_id + a, 1, fe_pos + a, c->nel,
                                           c->el_nodes.p, c->xyz.p, c->k_el.p, c->D_el.p, c->f, c->in_table.p,
                                           c->val.p, c->rhs.p, do_sm, do_rhs, c->err.p, c->std_dword);
-    return gbfem::launch_tet_elements(c->stream, true, b - a, fe_id + a, 1, fe_pos + a, c->nel, c->el_nodes.p,
+    return gbfem::launch_tet_elements(est, true, b - a, fe_id + a, 1, fe_pos + a, c->nel, c->el_nodes.p,
                                       c->xyz.p, c->k_el.p, c->f, c->in_table.p, c->val.p, c->rhs.p, do_sm, do_rhs,
                                       c->err.p);
   };
@@ -954,25 +1073,24 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     }
     return n;
   };
-  // with cached tables and host outputs: element chunks, each chunk's
-  // finished rows downloaded while the next chunk runs (plain meshes)
-  bool pipe = c->cache_tables && (crs_val || rhs) && e1 > e0 && c->ncon == 0;
-  if (pipe) {
-    bool same = c->pipe_e0 == e0 && c->pipe_e1 == e1 && c->pipe_dword == c->std_dword;
-    for (int i = 0; i < 3; i++) same = same && c->pipe_key[i] == c->cache_key[i] && c->pipe_len[i] == c->cache_len[i];
-    if (!same) GB_TRY(build_pipe_plan(c, e0, e1));
-  }
   if (pipe) {
     GB_TRY(fetch_host_structure(c));
     const int K = (int)c->pipe_el.size() - 1;
     const int *rp = c->hs.row_ptr.data();
     // all chunks first: a copy into pageable memory returns only when done
     for (int k = 0; k < K; k++) {
+      if (overlap)
+        for (int b = 0; b < 2; b++) {
+          if (c->up_np[b] == 0) continue;
+          const long long item = b == 0 ? c->pipe_maxnode[k] : c->pipe_maxel[k];
+          const int piece = (int)std::min<long long>(c->up_np[b] - 1, item / c->up_per[b]);
+          GB_CUDA(cudaStreamWaitEvent(est, c->up_ev[b][piece], 0));
+        }
       GB_TRY(r = elements(c->pipe_el[k], c->pipe_el[k + 1]));
       launches += r;
-      GB_CUDA(cudaEventRecord(c->pipe_ev[k], c->stream));
+      GB_CUDA(cudaEventRecord(c->pipe_ev[k], est));
     }
-    cudaEventRecord(c->ev3, c->stream);
+    cudaEventRecord(c->ev3, est);
     if (side) GB_TRY(join_side(c, c->copy_stream));  // face rows are final before any download
     int rprev = 0;
     for (int k = 0; k < K; k++) {
@@ -990,6 +1108,9 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
     }
     GB_CUDA(cudaEventRecord(c->pipe_ev[K], c->copy_stream));
     GB_CUDA(cudaStreamWaitEvent(c->stream, c->pipe_ev[K], 0));
+    // (the copy stream waited for every chunk and the faces; the context
+    // stream now also waits for every piece of the uploads)
+    if (overlap) GB_TRY(settle_uploads(c));
   } else {
     GB_TRY(r = elements(0, nfe));
     launches += r;
@@ -1019,6 +1140,7 @@ int gbfem_assemble(gbfem_ctx c, int scatter_mode) {
   GB_CHECK(scatter_mode != GBFEM_SCATTER_GATHER || (c->nv == GBFEM_PRISM && !c->std_dword),
            "the gather scatter takes std prisms in FP64 element arithmetic");
   GB_CUDA(cudaSetDevice(c->device));
+  GB_TRY(settle_uploads(c));
   const bool atomic = scatter_mode == GBFEM_SCATTER_ATOMIC;
   const bool gather = scatter_mode == GBFEM_SCATTER_GATHER;
   if (!atomic && !c->have_inc && (gather || c->el_colour_pending)) {
@@ -1419,6 +1541,7 @@ int gbfem_dg_get_structure(gbfem_ctx c, int *dof_off, int *bptr, int *bcol, long
 
 int gbfem_dg_assemble(gbfem_ctx c) {
   GB_CHECK(c && c->dg_ready, "DG structure not built (gbfem_dg_build_structure)");
+  GB_TRY(settle_uploads(c));
   GB_CUDA(cudaSetDevice(c->device));
   int launches = 0;
   // volume terms write every diagonal block and the rhs; the face kernel then
@@ -1621,6 +1744,7 @@ int gbfem_dg_set_variants(gbfem_ctx c, const int *vol, const int *face) {
 // matrix is overwritten: assemble afterwards) and keeps the fastest.
 int gbfem_dg_autotune(gbfem_ctx c, int sample, int *vol_out, int *face_out, double *ms_out) {
   GB_CHECK(c && c->dg_ready, "DG structure not built (gbfem_dg_build_structure)");
+  GB_TRY(settle_uploads(c));
   GB_CHECK(c->nv == GBFEM_PRISM, "the launch-shape autotuner covers the prism kernels");
   GB_CUDA(cudaSetDevice(c->device));
   if (sample <= 0) sample = 16384;

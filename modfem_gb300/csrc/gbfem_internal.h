@@ -333,6 +333,17 @@ struct gbfem_ctx_s {
   cudaStream_t side_stream = nullptr;
   cudaEvent_t side_ev[2] = {};
   std::vector<int> pipe_el, pipe_rows;
+  std::vector<int> pipe_maxnode, pipe_maxel;  // largest node / element index an element chunk reads
+  // node coordinates and coefficients set while the tables are cached go up
+  // in pieces on up_stream (events per piece), so that the drop-in's element
+  // chunks (on elem_stream) start as soon as the pieces they read are there;
+  // every other user of these arrays first makes the context stream wait
+  // for all pieces (settle_uploads)
+  cudaStream_t up_stream = nullptr, elem_stream = nullptr;
+  cudaEvent_t up_ev[2][8] = {}, up_now = nullptr, elem_ev0 = nullptr;
+  bool up_pending = false;
+  int up_np[2] = {0, 0};        // pieces in flight: [0] coordinates, [1] k_el or D_el
+  long long up_per[2] = {1, 1};  // nodes / elements a piece
   // Krylov workspace
   gbfem::DevBuf<double> V, w, tmp, x, b, partial, hcol;
   // device-resident std GMRES (gmres_dev.cu): sliced-ELL copy of the CRS

@@ -378,6 +378,60 @@ def test_dropin_pipelined_download(gb, shuffle):
     assert vec_rel_err(r2, ro) < REL_TOL
 
 
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_dropin_overlaps_coordinate_and_coefficient_uploads(gb, shuffle):
+    """With cached tables, new node coordinates and coefficients set before
+    each call go up in pieces while the element chunks that do not read the
+    rest already run: over three calls with different coordinates, k or a
+    full tensor, every result equals the oracle's (in element order and
+    shuffled, where a chunk reads nodes all over the mesh), and so do the
+    library's own assembly and a residual right after (the context stream
+    waits for every piece)."""
+    from modfem_gb300.mesh import anisotropic_tensors, lognormal_k, structured_prism_mesh
+    n = 50
+    c = None
+    order = np.random.default_rng(6).permutation(n ** 3 * 2) if shuffle else np.arange(n ** 3 * 2)
+    for it, seed in enumerate((3, 4, 5)):
+        m = structured_prism_mesh(n, jitter=0.2, seed=seed)
+        k = lognormal_k(m.nel, seed=seed)
+        D = anisotropic_tensors(m.nel, seed=seed).reshape(-1, 9) if it == 2 else None
+        if c is None:
+            c = make_ctx(gb, m, k)
+            nd, nnz, _ = c.build_structure()
+            tables = c.get_element_tables().reshape(m.nel, 42)
+            fa_tab = tables[m.bc_face_el].reshape(-1)
+            ids = np.concatenate([order + 1, m.bc_face_id]).astype(np.int32)
+            types = np.concatenate([np.full(m.nel, gb.ELEMENT), np.full(m.bc_face_id.size, gb.FACE)]).astype(np.int32)
+            table = np.concatenate([tables[order].reshape(-1), fa_tab]).astype(np.int32)
+            pos = (np.arange(ids.size) * 42).astype(np.int32)
+            args = (types, ids, np.array([0, m.nel], np.int32), np.array([m.nel, ids.size], np.int32), pos, table)
+            c.set_option(gb.OPT_CACHE_TABLES, 1)
+            dn, rp, ci = c.get_crs_structure()
+        c.set_node_coords(m.coords)
+        if D is None:
+            c.set_coefficients(k=k, f=1.0, g=0.0, penalty=1e7)
+        else:
+            c.set_coefficients(D=D, f=1.0, g=0.0, penalty=1e7)
+        v, r = np.full(nnz, np.nan), np.full(nd, np.nan)
+        c.create_assemble_stiff_mat(*args, crs_val=v, rhs=r)
+        kw = dict(D_el=D) if D is not None else {}
+        vo, ro, _ = O.std_prism_assemble(m, k, dn, rp, ci, nthreads=8, **kw)
+        so, sr, _ = O.std_prism_assemble_abs(m, k, dn, rp, ci, nthreads=8, **kw)
+        assert crs_rel_err(rp, v, vo, so) < REL_TOL, it
+        assert np.max(np.abs(r - ro) / np.where(sr > 0, sr, 1.0)) < REL_TOL, it
+    # the library's own assembly after piece uploads
+    m = structured_prism_mesh(n, jitter=0.2, seed=7)
+    k = lognormal_k(m.nel, seed=7)
+    c.set_node_coords(m.coords)
+    c.set_coefficients(k=k, f=1.0, g=0.0, penalty=1e7)
+    c.assemble(gb.SCATTER_ATOMIC)
+    v, r = c.get_matrix()
+    vo, ro, _ = O.std_prism_assemble(m, k, dn, rp, ci, nthreads=8)
+    so, sr, _ = O.std_prism_assemble_abs(m, k, dn, rp, ci, nthreads=8)
+    assert crs_rel_err(rp, v, vo, so) < REL_TOL
+    c.close()
+
+
 def test_double_word_assembly_vs_reference_and_oracle(gb):
     """Element matrices in double-word arithmetic (float pairs on the FP32
     pipe): the reference's own assembled matrix (golden, std_n10), and on a
