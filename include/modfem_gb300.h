@@ -558,7 +558,7 @@ int gbfem_server_cancel(gbfem_server srv, long long id);
 /* GBFEM_SERVE_OPT_SOLO_DOFS: std requests with at least this many dofs
  * (default 40,000; 0: none) are not batched into the engine's steps: they
  * are admitted on the HBM budget alone (no lane slot), prepared first, and
- * solved by one of four solo threads with gbfem_solve's device-resident
+ * solved by one of eight solo threads with gbfem_solve's device-resident
  * GMRES (sliced-ELL SpMV, restart cycles as a CUDA graph) on the request's
  * own highest-priority stream, beside the batched lanes.  Same stopping
  * rule; the result does not depend on the other requests either way. */

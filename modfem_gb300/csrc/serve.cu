@@ -20,7 +20,7 @@
 //    highest priority; solo-sized std requests taken first, then the other
 //    std ones, then DG): upload, structure (built on the device for std
 //    requests), integrate + assemble, preconditioner; overlaps with
-//    the solves running.  Solo-sized requests are then solved by one of four
+//    the solves running.  Solo-sized requests are then solved by one of eight
 //    solo threads, alone on their stream, with the device-resident GMRES of
 //    gbfem_solve;
 //  * solve (engine thread, one stream per lane): every step of a lane
@@ -1063,7 +1063,7 @@ int gbfem_server_create(gbfem_server *out, int device, long long hbm_budget, int
   memset(s->h_desc, 0, sizeof(SrvDesc) * gbfem::SRV_MAXSLOTS);
   cudaMemset(s->d_state.p, 0, sizeof(SrvState) * gbfem::SRV_MAXSLOTS);
   for (int i = 0; i < prep_threads; i++) s->workers.emplace_back(prep_worker, s);
-  for (int i = 0; i < 4; i++) s->solo_workers.emplace_back(solo_worker, s);
+  for (int i = 0; i < 8; i++) s->solo_workers.emplace_back(solo_worker, s);
   s->engine = std::thread(engine_loop, s);
   s->reaper = std::thread(reaper_loop, s);
   *out = s;
