@@ -58,14 +58,15 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help=argparse.SUPPRESS)
     p.add_argument("--profile", choices=["dg", "dg_tc", "dg_tcf", "dg_dwf", "dg_dw", "dg_best", "batch", "std", "std_dw",
-                                         "std_solve"], default=None,
+                                         "std_solve", "std_prep"], default=None,
                    help="small cases for ncu captures: DG p=3 anisotropic (n^3 x 2 prisms, --n), 3 assemblies "
                         "(FP64, tensor-core volume, tensor-core volume and faces, FP64 volume and double-word faces, or "
                         "double-word volume and faces) and one "
                         "block residual; or the mixed batch "
                         "(40,000 prisms + 30,000 tetrahedra, p 1..4), 3 runs; or the std prism assembly "
                         "(FP64 or double-word element arithmetic, n^3 x 2 prisms), 3 assemblies; or "
-                        "the std GMRES(30) (one restart cycle, device-resident, SELL SpMV)")
+                        "the std GMRES(30) (one restart cycle, device-resident, SELL SpMV); or a served std "
+                        "request's preparation (device structure build and gather scatter, 3 times)")
     return p.parse_args()
 
 
@@ -86,6 +87,24 @@ def run_profile_case(args):
             c.assemble(gb.SCATTER_ATOMIC)
             ms.append(c.last_timing()[:2])
         print(json.dumps({"profile_case": args.profile, "elements": m.nel, "timing_ms": ms}))
+        c.close()
+        return
+    if args.profile == "std_prep":
+        # a served request's std preparation: device structure build, then
+        # the gather scatter (incidence on its first call), 3 times
+        m, k = make_problem(args.n)
+        c = gb.Context(0)
+        c.set_mesh(m)
+        c.set_coefficients(k=k, f=1.0, g=0.0, penalty=1e7)
+        ms = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            c.build_structure_device()
+            t1 = time.perf_counter()
+            c.assemble(gb.SCATTER_GATHER)
+            t2 = time.perf_counter()
+            ms.append([round(1e3 * (t1 - t0), 3), round(1e3 * (t2 - t1), 3)])
+        print(json.dumps({"profile_case": args.profile, "elements": m.nel, "host_ms_build_assemble": ms}))
         c.close()
         return
     if args.profile == "std_solve":
