@@ -802,7 +802,7 @@ __global__ void row_last_kernel(int count, const int *__restrict__ pos, const in
 // Chunks of the element range and, per chunk, the number of leading rows that
 // no later element touches (dof order by first appearance makes rows finish
 // roughly in element order); built once per cached set of tables.
-static int build_pipe_plan(gbfem_ctx c, int e0, int e1, const int *h_ent_id) {
+static int build_pipe_plan(gbfem_ctx c, int e0, int e1) {
   const int count = e1 - e0, nd = c->ndof;
   GB_TRY(c->row_last.alloc((size_t)nd));
   GB_CUDA(cudaMemsetAsync(c->row_last.p, 0xFF, (size_t)nd * sizeof(int), c->stream));
@@ -826,9 +826,30 @@ static int build_pipe_plan(gbfem_ctx c, int e0, int e1, const int *h_ent_id) {
   for (int k = 0; k <= K; k++) c->pipe_el[k] = (int)std::min<long long>(count, chunk * k);
   for (int k = 0; k + 1 < K; k++)
     c->pipe_rows[k] = (int)(std::upper_bound(last.begin(), last.end(), c->pipe_el[k + 1] - 1) - last.begin());
-  // the largest node and element index each chunk reads (which pieces of a
-  // coordinate / coefficient upload it waits for); ids outside the mesh are
-  // the kernel's to report
+  // (the chunks' largest node and element indices are found when a call
+  // first overlaps uploads with them: pipe_chunk_reach)
+  c->pipe_maxnode.clear();
+  c->pipe_maxel.clear();
+  if (!c->copy_stream) {
+    GB_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (auto &ev : c->pipe_ev) GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  for (int i = 0; i < 3; i++) {
+    c->pipe_key[i] = c->cache_key[i];
+    c->pipe_len[i] = c->cache_len[i];
+  }
+  c->pipe_e0 = e0;
+  c->pipe_e1 = e1;
+  c->pipe_dword = c->std_dword;
+  return 0;
+}
+
+// The largest node and element index each chunk of the download plan reads
+// (which pieces of a coordinate / coefficient upload it waits for), from the
+// entity ids the plan's tables were cached with; ids outside the mesh are
+// the kernel's to report.
+static void pipe_chunk_reach(gbfem_ctx c, int e0, const int *h_ent_id) {
+  const int K = (int)c->pipe_el.size() - 1;
   c->pipe_maxnode.assign(K, c->nno - 1);
   c->pipe_maxel.assign(K, c->nel - 1);
   for (int k = 0; k < K; k++) {
@@ -842,18 +863,6 @@ static int build_pipe_plan(gbfem_ctx c, int e0, int e1, const int *h_ent_id) {
     c->pipe_maxnode[k] = mn;
     c->pipe_maxel[k] = me;
   }
-  if (!c->copy_stream) {
-    GB_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-    for (auto &ev : c->pipe_ev) GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-  }
-  for (int i = 0; i < 3; i++) {
-    c->pipe_key[i] = c->cache_key[i];
-    c->pipe_len[i] = c->cache_len[i];
-  }
-  c->pipe_e0 = e0;
-  c->pipe_e1 = e1;
-  c->pipe_dword = c->std_dword;
-  return 0;
 }
 
 // Splits the drop-in's element range [e0, e1) and face range [f0, f1) into
@@ -997,7 +1006,7 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   if (pipe) {
     bool same = c->pipe_e0 == e0 && c->pipe_e1 == e1 && c->pipe_dword == c->std_dword;
     for (int i = 0; i < 3; i++) same = same && c->pipe_key[i] == c->cache_key[i] && c->pipe_len[i] == c->cache_len[i];
-    if (!same) GB_TRY(build_pipe_plan(c, e0, e1, L_int_ent_id));
+    if (!same) GB_TRY(build_pipe_plan(c, e0, e1));
   }
   // coordinates / coefficients still going up in pieces (set while the
   // tables are cached) overlap the element chunks, which run on their own
@@ -1005,6 +1014,7 @@ int gbfem_create_assemble_stiff_mat(gbfem_ctx c, int Level_id, int Comp_type, co
   // pieces they read; otherwise everything waits for the whole uploads
   const bool overlap = pipe && c->up_pending && c->table_uploads == uploads0;
   if (!overlap) GB_TRY(settle_uploads(c));
+  if (overlap && c->pipe_maxnode.size() + 1 != c->pipe_el.size()) pipe_chunk_reach(c, e0, L_int_ent_id);
   cudaStream_t est = c->stream;
   if (overlap) {
     if (!c->elem_stream) {
