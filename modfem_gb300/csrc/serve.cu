@@ -16,8 +16,9 @@
 //    (replaced by the measured footprint once it is built).  Std requests of
 //    GBFEM_SERVE_OPT_SOLO_DOFS dofs or more never enter the engine's lanes:
 //    they are admitted on the budget alone;
-//  * preparation (worker threads, one CUDA stream each, std requests' at the
-//    highest priority; solo-sized std requests taken first, then the other
+//  * preparation (worker threads, one CUDA stream each, std requests' at a
+//    high priority, solo-sized ones' at the highest; solo-sized std
+//    requests taken first, then the other
 //    std ones, then DG): upload, structure (built on the device for std
 //    requests), integrate + assemble, preconditioner; overlaps with
 //    the solves running.  Solo-sized requests are then solved by one of eight
@@ -450,7 +451,8 @@ struct gbfem_server_s {
   int solo_dofs = 40000;         // GBFEM_SERVE_OPT_SOLO_DOFS
   int std_precedence = 1;        // GBFEM_SERVE_OPT_STD_PRECEDENCE
   std::atomic<int> n_solo{0};    // solo requests admitted and not finished
-  int prio_std = 0;              // stream priority of std requests' contexts (the greatest)
+  int prio_std = 0;              // stream priority of std requests' contexts
+  int prio_solo = 0;             // of solo-sized std requests' contexts (the greatest)
   std::string fatal;
 };
 
@@ -551,7 +553,7 @@ int prepare(gbfem_server s, SrvRequest &r) {
   gbfem_ctx c = nullptr;
   // std requests' preparation and solo solves at the std lane's priority:
   // the DG lane's long block SpMVs (lowest priority) do not hold them up
-  int rc = gbfem::create_context(&c, s->device, r.kind == 0 ? s->prio_std : 0);
+  int rc = gbfem::create_context(&c, s->device, r.kind == 0 ? (r.solo_admit ? s->prio_solo : s->prio_std) : 0);
   if (rc < 0) return rc;
   r.ctx = c;
   std::vector<int> fid, fbc;
@@ -1033,15 +1035,20 @@ int gbfem_server_create(gbfem_server *out, int device, long long hbm_budget, int
   bool ok = s->d_desc.alloc(gbfem::SRV_MAXSLOTS) >= 0 && s->d_state.alloc(gbfem::SRV_MAXSLOTS) >= 0 &&
             cudaHostAlloc(&s->h_init, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) == cudaSuccess &&
             cudaHostAlloc(&s->h_desc, sizeof(SrvDesc) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) == cudaSuccess;
-  // the std lane's short steps get the highest stream priority, the DG lane's
-  // long FP64-bound SpMVs the lowest: when both lanes have work queued the
-  // block scheduler starts std blocks first
+  // the std lane's short steps get a high stream priority (below only the
+  // solo-sized std requests' streams), the DG lane's long FP64-bound SpMVs
+  // the lowest: when both lanes have work queued the block scheduler starts
+  // std blocks first
   int prio_least = 0, prio_greatest = 0;
   cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
-  s->prio_std = prio_greatest;
+  // solo-sized std requests above every other stream, the other std work
+  // (preparations, the std lane) next, the DG lane last (greatest is the
+  // numerically smallest priority)
+  s->prio_solo = prio_greatest;
+  s->prio_std = prio_greatest < prio_least ? prio_greatest + 1 : prio_greatest;
   for (int L = 0; L < 2 && ok; L++) {
     SrvLane &ln = s->lanes[L];
-    ok = cudaStreamCreateWithPriority(&ln.stream, cudaStreamNonBlocking, L == 0 ? prio_greatest : prio_least) ==
+    ok = cudaStreamCreateWithPriority(&ln.stream, cudaStreamNonBlocking, L == 0 ? s->prio_std : prio_least) ==
              cudaSuccess &&
          cudaEventCreateWithFlags(&ln.done, cudaEventDisableTiming) == cudaSuccess &&
          cudaHostAlloc(&ln.h_state, sizeof(SrvState) * gbfem::SRV_MAXSLOTS, cudaHostAllocPortable) == cudaSuccess;
