@@ -30,6 +30,8 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# the whole measurement record (the printed line carries its summary)
+DETAIL_FILE = os.path.abspath(os.environ.get("BENCH_DETAIL", os.path.join(ROOT, "bench_detail.json")))
 sys.path.insert(0, ROOT)
 
 METRIC = "elem/s integrate+assemble vs plain FP64 GPU @1e-10 rel; served p50/p99 latency"
@@ -41,7 +43,7 @@ JITTER, SEED = 0.2, 1
 # quadrature-aggregated formulation executes 289 DFMA + 213 other FP64
 # instructions per element (ncu instruction mix, profiles/std_prism_elements_2M.md),
 # i.e. 791 flop and 502 FP64-pipe issue slots.
-SURVEY_FLOP_PER_ELEM = 6 * (151 + 18 * 6 + 2 * 6) + 2 * 3 * 6 * 36
+TEXTBOOK_FLOP_PER_ELEM = 6 * (151 + 18 * 6 + 2 * 6) + 2 * 3 * 6 * 36
 # Algorithmic DRAM bytes per element of the 100^3 x 2 workload: connectivity
 # 24 + k 8 + coordinates 24 nno/nel + CRS values written once 8 nnz/nel +
 # rhs 8 ndof/nel + the 42-entry int32 assembly table 168 (302 B in all)
@@ -606,7 +608,8 @@ def bench_batch(gb, local, steps, fp64_peak):
 
 
 def bench_tet_dg(gb, local, steps):
-    """The tetrahedral part of config 3 as a DG system: 37^3 x 6 = 303,918
+    """The tetrahedral part of the mixed prism + tetrahedron workload as a
+    DG system: 37^3 x 6 = 303,918
     jittered affine tetrahedra, p uniform in 1..4 (seeded), lognormal(0,1)
     k, interior-penalty faces (616,050 faces) into the variable-block
     storage; then a fixed 100 GMRES(50) iterations with block Jacobi."""
@@ -889,7 +892,8 @@ def compact_line(full):
     """The contract keys plus the summaries the headline rests on, a few KB:
     the plain FP64 path, precision, the std solver, the DG p = 3 and mixed
     assemblies, the mixed-precision solution error, the batch and serving
-    summaries.  The whole record goes to gpurun_out/bench_detail.json."""
+    summaries.  The whole record goes to the detail file (BENCH_DETAIL, by
+    default bench_detail.json beside this script)."""
     keep = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
             "vs_baseline", "dtype", "data", "config", "roofline", "cpu_baseline", "e2e", "clocks", "gpu_launches",
             "speedup_vs_plain_fp64")
@@ -933,7 +937,7 @@ def compact_line(full):
     out["batch_mixed"] = {"step_ms": _r(b["step_ms"]), "elem_per_s": _r(b["elem_per_s"]),
                           "fp64_frac": _r(b["fp64_frac"], 3),
                           "double_word_step_ms": _r(b["double_word_prisms"]["step_ms"])}
-    # BASELINE config 3 as a whole step: the mixed-degree prism DG system and
+    # the mixed prism + tetrahedron workload as a whole step: the mixed-degree prism DG system and
     # the tetrahedral DG system (volume and faces each, measured above in this
     # run; the two element types form separate systems, no prism-tetrahedron
     # faces)
@@ -943,7 +947,7 @@ def compact_line(full):
             "fp64": _r(mx["assemble_ms"] + tet["assemble_ms"]),
             "double_word": _r(mx["double_word_assembly"]["assemble_ms"] + tet["double_word_faces"]["assemble_ms"]),
             "elements": mx["elements"] + tet["elements"]}
-    # config 3 as one system on one connected prism + tetrahedron mesh
+    # the same workload as one system on one connected prism + tetrahedron mesh
     ms = b.get("mixed_dg_system")
     if ms:
         out["batch_mixed"]["config3_one_system"] = {
@@ -960,7 +964,7 @@ def compact_line(full):
                           "problems_per_s": {str(r["rate_req_s"]): _r(r["problems_per_s"]) for r in sv["rates"]},
                           "plain_p99_ms": {str(r["rate_req_s"]): _r(r["plain_one_at_a_time"]["p99_ms"])
                                            for r in sv["rates"]}}
-    out["detail_file"] = "gpurun_out/bench_detail.json"
+    out["detail_file"] = os.path.relpath(DETAIL_FILE, ROOT)
     return out
 
 
@@ -1214,7 +1218,7 @@ def main():
                          "frac": achieved64 / fp64_peak, "traffic": traffic,
                          "kernel": "prism_elements_kernel", "kernel_ms": el64,
                          "flop_per_elem": FLOP_PER_ELEM, "fp64_pipe_slot_frac": slot_frac,
-                         "survey_flop_per_elem": SURVEY_FLOP_PER_ELEM,
+                         "textbook_flop_per_elem": TEXTBOOK_FLOP_PER_ELEM,
                          "peak_source": "FP64 FMA-chain kernel measured in this run (no FP64 figure in the peaks "
                                         "file)"}},
         "cpu_baseline": cpu,
@@ -1237,8 +1241,10 @@ def main():
         # the whole record to a file; one compact line (the figures the
         # headline rests on) to stdout
         try:
-            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-            with open(os.path.join(ROOT, "gpurun_out", "bench_detail.json"), "w") as fh:
+            d = os.path.dirname(DETAIL_FILE)
+            if d:
+                os.makedirs(d, exist_ok=True)
+            with open(DETAIL_FILE, "w") as fh:
                 json.dump(line, fh, indent=1)
         except OSError:
             pass

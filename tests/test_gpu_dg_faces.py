@@ -465,8 +465,9 @@ def test_dg_iterative_refinement_vs_reference(gb, name):
     assert vec_rel_err(x, g["gmres_x"]) < 1e-6
 
 
-def _config4_form(n, seed=44):
-    """BASELINE config 4's problem at a small size: DG p = 3 prisms on a
+def _p3_aniso_form(n, seed=44):
+    """The p = 3 anisotropic DG problem (432k prisms at full size) at a
+    small size: DG p = 3 prisms on a
     jittered n^3 x 2 mesh, the anisotropic tensor R diag(1, 0.1, 0.01) R^T per
     element, Dirichlet value 0.3."""
     from modfem_gb300.mesh import anisotropic_tensors, prism_faces, structured_prism_mesh
@@ -522,7 +523,7 @@ def test_mixed_precision_solution_error_vs_oracle(gb, n):
     every entry moves the solution by ~1e-11), so the GPU FP64 matrix itself
     (within ~1.4e-15 of the oracle's on the entry scale) lands 3-5e-11 from
     the oracle's solution; the mixed forms land as close."""
-    m, F, D = _config4_form(n)
+    m, F, D = _p3_aniso_form(n)
     rp, ci, v, rhs, off = O.dg_assemble(m, F, np.full(m.nel, 3), D, pen=10.0, g=0.3, f=1.0)
     xo = _accurate_dense_solution(rp, ci, v, rhs)
     for name, (vol, face) in MIXED_FORMS.items():
@@ -537,8 +538,8 @@ def test_mixed_precision_solution_error_vs_fp64_larger(gb):
     mixed forms' refined solutions against the plain FP64 assembly's refined
     solution (measured 6.4e-11 for both).  The double-word faces (4e-14 of
     the largest entry) move the solution by ~1.5e-9 on this system, which is
-    why config 4's mixed form takes the tensor-core faces."""
-    m, F, D = _config4_form(10)
+    why the mixed p = 3 form takes the tensor-core faces."""
+    m, F, D = _p3_aniso_form(10)
     x64 = _refined_solution(gb, m, F, D, 0, 0)
     for name in ("tc_volume_tc_faces", "dword_volume_tc_faces"):
         x = _refined_solution(gb, m, F, D, *MIXED_FORMS[name])
@@ -553,7 +554,7 @@ def test_compensated_residual(gb):
     """The compensated DG residual against an exact rational evaluation of
     b - A x for a sample of rows, and against the FP64 residual."""
     from fractions import Fraction
-    m, F, D = _config4_form(3)
+    m, F, D = _p3_aniso_form(3)
     c = _context(gb, m, F, np.full(m.nel, 3), D=D, g=0.3)
     c.dg_assemble()
     rp, ci, v, rhs, off = _expand(c)
