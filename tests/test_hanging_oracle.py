@@ -84,3 +84,21 @@ def test_planted_coefficient_mistake_is_caught(monkeypatch):
             g["row_ptr"].size - 1, g["col_ind"].size, m.fa_of_id)
     val, rhs = O.std_dropin_assemble(*args, con_cnt=g["con_cnt"], con_par=g["con_par"])
     assert np.max(np.abs(val - g["crs_val"])) > 1e-3 * np.max(np.abs(g["crs_val"]))
+
+
+def test_table_blocks_follow_the_expanded_lists():
+    """The reference's assembly table gives every entity a block of n x n + n
+    positions, n its expanded dof count (an element's constrained vertices
+    replaced by their constraining vertices; a boundary face takes its
+    element's list): the sizes the drop-in derives from the constraint data
+    for the table length and for each entity's block."""
+    g, m = _case()
+    pos = g["asse_pos"]
+    sizes = np.diff(np.concatenate([pos, [g["assembly_table"].size]]))
+    for i, (t, ent) in enumerate(zip(g["int_ent_type"], g["int_ent_id"])):
+        e = int(ent) - 1 if t == 4 else m.fa_of_id[int(ent)][0]
+        _, _, ids = O.std_constraint_expand(m.el_nodes[e], g["con_cnt"], g["con_par"])
+        n = ids.size
+        assert sizes[i] == n * n + n, (i, t, ent)
+        # the rhs rows of the block are the dofs of the expanded list
+        assert np.array_equal(g["assembly_table"][pos[i] + n * n:pos[i] + n * n + n], g["dof_of_node"][ids])
